@@ -1,0 +1,652 @@
+// C ABI of libgDMR (GB300 build): the reference's gDMR.h / gDMRC.h entry
+// points, their complex128 twins, and the context API of gdmr_ext.h.
+#include <cuComplex.h>
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "gdmr_engine.h"
+
+#define GDMR_WITH_CUDA_TYPES 1
+extern "C" {
+#include "../../include/gDMR.h"
+#include "../../include/gDMRC.h"
+#include "../../include/gdmr_ext.h"
+}
+
+using namespace gdmr;
+
+namespace {
+
+std::mutex g_api_mu;     // the legacy entry points are process-global, as in the reference
+gdmr_stats g_last_stats{0, 0, 0, 0.0, -1.0, GDMR_OK, 0, 0.0};
+
+void record(const SolveStats &s) {
+    g_last_stats.cycles = s.cycles;
+    g_last_stats.its = s.its;
+    g_last_stats.matvecs = s.matvecs;
+    g_last_stats.rel_res = s.rel_res;
+    g_last_stats.true_rel_res = s.true_rel_res;
+    g_last_stats.status = s.status;
+    g_last_stats.breakdowns = s.breakdowns;
+}
+
+int fail(int status, const char *where, const char *what) {
+    char buf[512];
+    snprintf(buf, sizeof buf, "%s: %s", where, what);
+    set_last_error(status, buf);
+    fprintf(stderr, "%s\n", buf);
+    return status;
+}
+
+// ---------------------------------------------------------------- legacy solver state
+template <class R> struct LegacySolver {
+    Engine<R> eng;
+    void (*hook)(void) = nullptr;
+    int device = 0;
+};
+LegacySolver<float> g_s32;
+LegacySolver<double> g_s64;
+
+template <class R>
+void legacy_init(LegacySolver<R> &S, const char *name, int blocks, int tpb, int *devList, int numDevs, int elements,
+                 int basisDim, int deflatDim, void (*linComp)(void)) {
+    (void)blocks;
+    (void)tpb;
+    // the reference's validation (gDMR.cu:844-860): print and return with nothing allocated
+    if (numDevs < 1 || !devList) { fail(GDMR_EINVAL, name, "at least one device is required"); return; }
+    if ((basisDim + 1) % numDevs != 0) {
+        fail(GDMR_EINVAL, name, "The dimension basisDim + 1 must be divisible by the number of requested devices.");
+        return;
+    }
+    if (deflatDim % numDevs != 0) {
+        fail(GDMR_EINVAL, name, "The deflation space dimension must be divisible by the number of requested devices.");
+        return;
+    }
+    if (basisDim - deflatDim < 2) {
+        fail(GDMR_EINVAL, name,
+             "After removing the deflation space, the basis dimension is too small to perform Arnoldi iterations.");
+        return;
+    }
+    if (!linComp) { fail(GDMR_EINVAL, name, "a linear operator hook is required"); return; }
+    S.device = devList[0];
+    if (S.eng.init(elements, basisDim, deflatDim, 1, S.device) != GDMR_OK) {
+        fprintf(stderr, "%s: %s\n", name, last_error());
+        return;
+    }
+    S.hook = linComp;
+    S.eng.op.kind = Operator<R>::HOOK;
+    S.eng.op.hook = linComp;
+    set_last_error(GDMR_OK, "ok");
+}
+
+template <class R>
+double legacy_solve(LegacySolver<R> &S, const char *name, int mode, typename CT<R>::t *src, typename CT<R>::t *img,
+                    cudaStream_t st, int dev, double tol, int matRank, int *numIts) {
+    if (!S.eng.ready()) {
+        fail(GDMR_ENOTINIT, name, "solver not initialised");
+        if (numIts) *numIts = matRank * matRank;
+        return 1.0;
+    }
+    if (!src || !img) {
+        fail(GDMR_EINVAL, name, "null source or image vector");
+        return 1.0;
+    }
+    if (dev != S.device) fprintf(stderr, "%s: operator device %d differs from solver device %d; using %d\n", name, dev,
+                                 S.device, S.device);
+    cudaSetDevice(S.device);
+    S.eng.stream = st;
+    S.eng.op.ext = src;
+    SolveStats stats;
+    double r = S.eng.solve_reference(mode, img, src, tol, matRank, &stats);
+    if (numIts) *numIts = stats.its;
+    record(stats);
+    if (stats.status == GDMR_ENOCONV)
+        fprintf(stderr, "%s Inverse Solve Error: failed to converge to a solution after %d iterations.\n", name,
+                stats.cycles);
+    else if (stats.status == GDMR_ERUNAWAY)
+        fprintf(stderr, "%s Inverse Solve Error: Runaway!\n", name);
+    else if (stats.status == GDMR_OK && stats.cycles == 0)
+        fprintf(stdout, "Initial guess within solution tolerance.\n");
+    return r;
+}
+
+template <class R> void legacy_imp_z(LegacySolver<R> &S, const void *host, const char *name) {
+    std::lock_guard<std::mutex> lk(g_api_mu);
+    if (!S.eng.ready()) { fail(GDMR_ENOTINIT, name, "solver not initialised"); return; }
+    cudaSetDevice(S.device);
+    if (S.eng.import_deflation((const typename CT<R>::t *)host) != GDMR_OK) fprintf(stderr, "%s: %s\n", name, last_error());
+}
+template <class R> void legacy_exp_z(LegacySolver<R> &S, void *host, const char *name) {
+    std::lock_guard<std::mutex> lk(g_api_mu);
+    if (!S.eng.ready()) { fail(GDMR_ENOTINIT, name, "solver not initialised"); return; }
+    cudaSetDevice(S.device);
+    if (S.eng.export_deflation((typename CT<R>::t *)host) != GDMR_OK) fprintf(stderr, "%s: %s\n", name, last_error());
+}
+
+// ---------------------------------------------------------------- plugin (testLS.cu's role)
+template <class R> struct Plugin {
+    using C = typename CT<R>::t;
+    int n = 0, dev = 0;
+    C *src = nullptr, *img = nullptr, *tmp = nullptr, *opt = nullptr;
+    DeviceSell csr;
+    bool use_csr = false;
+    cudaStream_t st = nullptr;
+    bool ready = false;
+};
+Plugin<float> g_p32;
+Plugin<double> g_p64;
+
+template <class C> __global__ void k_identity(int n, C *A) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < (long)n * n; i += (long)gridDim.x * blockDim.x) {
+        C v;
+        v.x = (i / n == i % n) ? 1 : 0;
+        v.y = 0;
+        A[i] = v;
+    }
+}
+
+template <class R> void plugin_apply(Plugin<R> &P) {
+    if (!P.ready) { fail(GDMR_ENOTINIT, "linOptLS", "linear system not initialised"); return; }
+    cudaSetDevice(P.dev);
+    // y = A x into a separate buffer, then copy back: the reference's hook aliases input and output
+    if (P.use_csr) {
+        int zero = 0;
+        static thread_local int *d_zero = nullptr;
+        if (!d_zero) {
+            cudaMalloc(&d_zero, sizeof(int));
+            cudaMemcpy(d_zero, &zero, sizeof(int), cudaMemcpyHostToDevice);
+        }
+        SellMatrix A = sizeof(R) == 4 ? P.csr.view32() : P.csr.view64();
+        launch_spmm<R>(A, P.src, 0, P.tmp, 0, d_zero, 1, P.st);
+    } else {
+        launch_dense_gemv<R>(P.n, P.opt, P.src, P.tmp, P.st);
+    }
+    cudaMemcpyAsync(P.src, P.tmp, sizeof(typename Plugin<R>::C) * P.n, cudaMemcpyDeviceToDevice, P.st);
+}
+
+void linop32(void) { plugin_apply(g_p32); }
+void linop64(void) { plugin_apply(g_p64); }
+
+template <class R> void plugin_free(Plugin<R> &P) {
+    if (P.src) cudaFree(P.src);
+    if (P.img) cudaFree(P.img);
+    if (P.tmp) cudaFree(P.tmp);
+    if (P.opt) cudaFree(P.opt);
+    sell_free(P.csr);
+    if (P.st) cudaStreamDestroy(P.st);
+    P = Plugin<R>();
+}
+
+template <class R>
+bool plugin_init(Plugin<R> &P, const char *name, int devNumLO, int cells) {
+    using C = typename Plugin<R>::C;
+    plugin_free(P);
+    if (cells <= 0) { fail(GDMR_EINVAL, name, "cells must be positive"); return false; }
+    P.n = cells;
+    P.dev = devNumLO;
+    if (cudaSetDevice(devNumLO) != cudaSuccess) { fail(GDMR_ECUDA, name, "Failed to set device"); return false; }
+    const size_t vb = sizeof(C) * (size_t)cells;
+    if (cudaMalloc(&P.src, vb) != cudaSuccess || cudaMalloc(&P.img, vb) != cudaSuccess ||
+        cudaMalloc(&P.tmp, vb) != cudaSuccess || cudaMalloc(&P.opt, vb * (size_t)cells) != cudaSuccess) {
+        plugin_free(P);
+        fail(GDMR_ENOMEM, name, "Failed to allocate device memory");
+        return false;
+    }
+    cudaMemset(P.src, 0, vb);
+    cudaMemset(P.img, 0, vb);
+    if (cudaStreamCreate(&P.st) != cudaSuccess) { plugin_free(P); fail(GDMR_ECUDA, name, "stream"); return false; }
+    k_identity<C><<<1024, 256, 0, P.st>>>(cells, P.opt);
+    cudaStreamSynchronize(P.st);
+    P.ready = true;
+    return true;
+}
+
+template <class R> void copy_in(Plugin<R> &P, typename Plugin<R>::C *dst, const void *host, size_t count, const char *name) {
+    std::lock_guard<std::mutex> lk(g_api_mu);
+    if (!P.ready) { fail(GDMR_ENOTINIT, name, "linear system not initialised"); return; }
+    cudaSetDevice(P.dev);
+    cudaStreamSynchronize(P.st);
+    if (cudaMemcpy(dst, host, sizeof(typename Plugin<R>::C) * count, cudaMemcpyHostToDevice) != cudaSuccess)
+        fail(GDMR_ECUDA, name, "Failed to copy memory from host to device");
+}
+template <class R> void copy_out(Plugin<R> &P, void *host, const typename Plugin<R>::C *src, size_t count, const char *name) {
+    std::lock_guard<std::mutex> lk(g_api_mu);
+    if (!P.ready) { fail(GDMR_ENOTINIT, name, "linear system not initialised"); return; }
+    cudaSetDevice(P.dev);
+    cudaStreamSynchronize(P.st);
+    if (cudaMemcpy(host, src, sizeof(typename Plugin<R>::C) * count, cudaMemcpyDeviceToHost) != cudaSuccess)
+        fail(GDMR_ECUDA, name, "Failed to copy memory from device to host");
+}
+
+template <class R>
+int plugin_csr(Plugin<R> &P, int nnz, const int *rowPtr, const int *colIdx, const R *vals_ri, const char *name) {
+    std::lock_guard<std::mutex> lk(g_api_mu);
+    if (!P.ready) return fail(GDMR_ENOTINIT, name, "linear system not initialised");
+    if (!rowPtr || !colIdx || !vals_ri || nnz < 0 || rowPtr[P.n] - rowPtr[0] != nnz)
+        return fail(GDMR_EINVAL, name, "CSR arrays inconsistent with nnz");
+    cudaSetDevice(P.dev);
+    std::vector<double> v((size_t)2 * nnz);
+    for (size_t i = 0; i < v.size(); ++i) v[i] = (double)vals_ri[i];
+    int rc = sell_from_csr(P.csr, P.n, rowPtr, colIdx, v.data(), sizeof(R) == 4, sizeof(R) == 8, P.st);
+    if (rc != GDMR_OK) return rc;
+    P.use_csr = true;
+    return GDMR_OK;
+}
+
+}  // namespace
+
+// ================================================================ gDMR.h
+extern "C" void initDMR(int blocks, int threadsPerBlock, int *devList, int numDevs, int elements, int basisDim,
+                        int deflatDim, void (*linComp)(void)) {
+    std::lock_guard<std::mutex> lk(g_api_mu);
+    legacy_init(g_s32, "initDMR", blocks, threadsPerBlock, devList, numDevs, elements, basisDim, deflatDim, linComp);
+}
+
+extern "C" void freeDMR(void) {
+    std::lock_guard<std::mutex> lk(g_api_mu);
+    g_s32.eng.release();
+    g_s32.hook = nullptr;
+}
+
+extern "C" float solverDMR(int mode, cuComplex *extSrcVec, cuComplex *extImgVec, cudaStream_t extStream,
+                           int extDevNum, float solTol, int matRank, int *numIts) {
+    std::lock_guard<std::mutex> lk(g_api_mu);
+    return (float)legacy_solve(g_s32, "solverDMR", mode, (float2 *)extSrcVec, (float2 *)extImgVec, extStream,
+                               extDevNum, (double)solTol, matRank, numIts);
+}
+
+extern "C" void impSVDMR(float _Complex *cMem) { legacy_imp_z(g_s32, cMem, "impSVDMR"); }
+extern "C" void expSVDMR(float _Complex *cMem) { legacy_exp_z(g_s32, cMem, "expSVDMR"); }
+
+// ================================================================ complex128 drop-in
+extern "C" void initDMR_z(int blocks, int threadsPerBlock, int *devList, int numDevs, int elements, int basisDim,
+                          int deflatDim, void (*linComp)(void)) {
+    std::lock_guard<std::mutex> lk(g_api_mu);
+    legacy_init(g_s64, "initDMR_z", blocks, threadsPerBlock, devList, numDevs, elements, basisDim, deflatDim, linComp);
+}
+extern "C" void freeDMR_z(void) {
+    std::lock_guard<std::mutex> lk(g_api_mu);
+    g_s64.eng.release();
+    g_s64.hook = nullptr;
+}
+extern "C" double solverDMR_z(int mode, cuDoubleComplex *extSrcVec, cuDoubleComplex *extImgVec, cudaStream_t extStream,
+                              int extDevNum, double solTol, int matRank, int *numIts) {
+    std::lock_guard<std::mutex> lk(g_api_mu);
+    return legacy_solve(g_s64, "solverDMR_z", mode, (double2 *)extSrcVec, (double2 *)extImgVec, extStream, extDevNum,
+                        solTol, matRank, numIts);
+}
+extern "C" void impSVDMR_z(double _Complex *cMem) { legacy_imp_z(g_s64, cMem, "impSVDMR_z"); }
+extern "C" void expSVDMR_z(double _Complex *cMem) { legacy_exp_z(g_s64, cMem, "expSVDMR_z"); }
+
+// ================================================================ gDMRC.h plugin (complex64)
+extern "C" void initLS(int blocksMDR, int threadsPerBlockMDR, int devNumLO, int cells, int *devListMDR, int numDevsMDR,
+                       int basisSizeMDR, int deflatSizeMDR) {
+    {
+        std::lock_guard<std::mutex> lk(g_api_mu);
+        if (!plugin_init(g_p32, "initLS", devNumLO, cells)) return;
+    }
+    initDMR(blocksMDR, threadsPerBlockMDR, devListMDR, numDevsMDR, cells, basisSizeMDR, deflatSizeMDR, linop32);
+}
+extern "C" void freeLS(void) {
+    {
+        std::lock_guard<std::mutex> lk(g_api_mu);
+        plugin_free(g_p32);
+    }
+    freeDMR();
+}
+extern "C" void impImgLS(float _Complex *c) { copy_in(g_p32, g_p32.img, c, g_p32.n, "impImgLS"); }
+extern "C" void expImgLS(float _Complex *c) { copy_out(g_p32, c, g_p32.img, g_p32.n, "expImgLS"); }
+extern "C" void impSrcLS(float _Complex *c) { copy_in(g_p32, g_p32.src, c, g_p32.n, "impSrcLS"); }
+extern "C" void expSrcLS(float _Complex *c) { copy_out(g_p32, c, g_p32.src, g_p32.n, "expSrcLS"); }
+extern "C" void impOptLS(float _Complex *c) {
+    copy_in(g_p32, g_p32.opt, c, (size_t)g_p32.n * g_p32.n, "impOptLS");
+    g_p32.use_csr = false;
+}
+extern "C" void expOptLS(float _Complex *c) { copy_out(g_p32, c, g_p32.opt, (size_t)g_p32.n * g_p32.n, "expOptLS"); }
+extern "C" float solveLS(int mode, float solTol, int matRank, int *numIts) {
+    if (!g_p32.ready) {
+        fail(GDMR_ENOTINIT, "solveLS", "linear system not initialised");
+        return 1.0f;
+    }
+    return solverDMR(mode, (cuComplex *)g_p32.src, (cuComplex *)g_p32.img, g_p32.st, g_p32.dev, solTol, matRank,
+                     numIts);
+}
+extern "C" void linOptLS(void) {
+    std::lock_guard<std::mutex> lk(g_api_mu);
+    plugin_apply(g_p32);
+    cudaStreamSynchronize(g_p32.st);
+}
+extern "C" int impCsrLS(int nnz, const int *rowPtr, const int *colIdx, const float _Complex *vals) {
+    return plugin_csr(g_p32, nnz, rowPtr, colIdx, (const float *)vals, "impCsrLS");
+}
+
+// ================================================================ complex128 plugin
+extern "C" void initLS_z(int blocksMDR, int threadsPerBlockMDR, int devNumLO, int cells, int *devListMDR,
+                         int numDevsMDR, int basisSizeMDR, int deflatSizeMDR) {
+    {
+        std::lock_guard<std::mutex> lk(g_api_mu);
+        if (!plugin_init(g_p64, "initLS_z", devNumLO, cells)) return;
+    }
+    initDMR_z(blocksMDR, threadsPerBlockMDR, devListMDR, numDevsMDR, cells, basisSizeMDR, deflatSizeMDR, linop64);
+}
+extern "C" void freeLS_z(void) {
+    {
+        std::lock_guard<std::mutex> lk(g_api_mu);
+        plugin_free(g_p64);
+    }
+    freeDMR_z();
+}
+extern "C" void impImgLS_z(double _Complex *c) { copy_in(g_p64, g_p64.img, c, g_p64.n, "impImgLS_z"); }
+extern "C" void expImgLS_z(double _Complex *c) { copy_out(g_p64, c, g_p64.img, g_p64.n, "expImgLS_z"); }
+extern "C" void impSrcLS_z(double _Complex *c) { copy_in(g_p64, g_p64.src, c, g_p64.n, "impSrcLS_z"); }
+extern "C" void expSrcLS_z(double _Complex *c) { copy_out(g_p64, c, g_p64.src, g_p64.n, "expSrcLS_z"); }
+extern "C" void impOptLS_z(double _Complex *c) {
+    copy_in(g_p64, g_p64.opt, c, (size_t)g_p64.n * g_p64.n, "impOptLS_z");
+    g_p64.use_csr = false;
+}
+extern "C" int impCsrLS_z(int nnz, const int *rowPtr, const int *colIdx, const double _Complex *vals) {
+    return plugin_csr(g_p64, nnz, rowPtr, colIdx, (const double *)vals, "impCsrLS_z");
+}
+extern "C" double solveLS_z(int mode, double solTol, int matRank, int *numIts) {
+    if (!g_p64.ready) {
+        fail(GDMR_ENOTINIT, "solveLS_z", "linear system not initialised");
+        return 1.0;
+    }
+    return solverDMR_z(mode, (cuDoubleComplex *)g_p64.src, (cuDoubleComplex *)g_p64.img, g_p64.st, g_p64.dev, solTol,
+                       matRank, numIts);
+}
+extern "C" void linOptLS_z(void) {
+    std::lock_guard<std::mutex> lk(g_api_mu);
+    plugin_apply(g_p64);
+    cudaStreamSynchronize(g_p64.st);
+}
+
+// ================================================================ status
+extern "C" int gdmrLastStatus(void) { return last_status(); }
+extern "C" const char *gdmrLastError(void) { return last_error(); }
+extern "C" const char *gdmrVersion(void) { return "1.0.1-gb300"; }
+extern "C" void gdmrLastStats(gdmr_stats *out) {
+    std::lock_guard<std::mutex> lk(g_api_mu);
+    if (out) *out = g_last_stats;
+}
+
+// ================================================================ instrumentation
+extern "C" long long gdmrKernelLaunches(void) { return launch_count(); }
+extern "C" void gdmrProfile(int on) { profile_enable(on != 0); }
+extern "C" void gdmrProfileReset(void) { profile_reset(); }
+extern "C" int gdmrProfileRead(int kernelClass, double *bytes, double *ms, long long *launches) {
+    if (kernelClass < 0 || kernelClass >= KC_COUNT) return fail(GDMR_EINVAL, "gdmrProfileRead", "no such kernel class");
+    profile_flush();
+    profile_read(kernelClass, bytes, ms, launches);
+    return GDMR_OK;
+}
+
+// ================================================================ context API
+// complex128 <-> complex64 helpers used by the context API
+namespace {
+__global__ void k_demote(int n, const double2 *a, float2 *b) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+__global__ void k_promote(int n, const float2 *a, double2 *b) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        b[i] = make_double2(a[i].x, a[i].y);
+}
+}  // namespace
+static void gdmr_demote_vec(int n, const double2 *a, float2 *b, cudaStream_t st) {
+    k_demote<<<std::min((n + 255) / 256, 4096), 256, 0, st>>>(n, a, b);
+}
+static void gdmr_promote_vec(int n, const float2 *a, double2 *b, cudaStream_t st) {
+    k_promote<<<std::min((n + 255) / 256, 4096), 256, 0, st>>>(n, a, b);
+}
+
+struct gdmr_system {
+    int n = 0, m = 0, k = 0, cap = 0, precision = 0, device = 0;
+    DeviceSell A;
+    Engine<float> e32;
+    Engine<double> e64;
+    cudaStream_t st = nullptr;
+    double2 *db = nullptr, *dx = nullptr;   // staging for host-buffer calls (cap vectors each)
+    std::mutex mu;
+};
+
+namespace {
+template <class R> Engine<R> &eng_of(gdmr_system *s);
+template <> Engine<float> &eng_of<float>(gdmr_system *s) { return s->e32; }
+template <> Engine<double> &eng_of<double>(gdmr_system *s) { return s->e64; }
+
+void to_stats(const SolveStats &s, gdmr_stats *o) {
+    o->cycles = s.cycles;
+    o->its = s.its;
+    o->matvecs = s.matvecs;
+    o->rel_res = s.rel_res;
+    o->true_rel_res = s.true_rel_res;
+    o->status = s.status;
+    o->breakdowns = s.breakdowns;
+    o->latency_ms = s.latency_ms;
+}
+
+template <class R>
+int batch_impl(gdmr_system *S, int nrhs, const double *b, double *x, const double *tol, int maxCycles, int on_device,
+               gdmr_stats *stats) {
+    Engine<R> &E = eng_of<R>(S);
+    const size_t vb = sizeof(double2) * (size_t)S->n;
+    int rc = E.refine_setup(S->A.view64());
+    if (rc != GDMR_OK) return rc;
+    std::vector<int> slot_of(E.capacity(), -1);
+    int next = 0, finished = 0, worst = GDMR_OK;
+    const auto t0 = std::chrono::steady_clock::now();
+    while (finished < nrhs) {
+        for (int s = 0; s < E.capacity() && next < nrhs; ++s) {
+            if (slot_of[s] >= 0) continue;
+            const double2 *bsrc, *xsrc;
+            if (on_device) {
+                bsrc = (const double2 *)b + (size_t)next * S->n;
+                xsrc = (const double2 *)x + (size_t)next * S->n;
+            } else {
+                if (cudaMemcpyAsync(S->db + (size_t)s * S->n, b + (size_t)2 * next * S->n, vb, cudaMemcpyHostToDevice,
+                                    S->st) != cudaSuccess ||
+                    cudaMemcpyAsync(S->dx + (size_t)s * S->n, x + (size_t)2 * next * S->n, vb, cudaMemcpyHostToDevice,
+                                    S->st) != cudaSuccess)
+                    return fail(GDMR_ECUDA, "gdmr_solve_batch", "host to device copy failed");
+                bsrc = S->db + (size_t)s * S->n;
+                xsrc = S->dx + (size_t)s * S->n;
+            }
+            if ((rc = E.refine_admit(s, bsrc, xsrc, tol ? tol[next] : 1e-10, maxCycles)) != GDMR_OK) return rc;
+            slot_of[s] = next++;
+        }
+        std::vector<int> done;
+        if ((rc = E.refine_cycle(&done)) != GDMR_OK) return rc;
+        for (int s : done) {
+            const int r = slot_of[s];
+            if (on_device)
+                cudaMemcpyAsync((double2 *)x + (size_t)r * S->n, E.slot_x(s), vb, cudaMemcpyDeviceToDevice, S->st);
+            else
+                cudaMemcpyAsync(x + (size_t)2 * r * S->n, E.slot_x(s), vb, cudaMemcpyDeviceToHost, S->st);
+            if (stats) {
+                to_stats(E.slot_stats(s), &stats[r]);
+                stats[r].latency_ms =
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            }
+            worst = std::max(worst, E.slot_stats(s).status);
+            slot_of[s] = -1;
+            ++finished;
+        }
+    }
+    if (cudaStreamSynchronize(S->st) != cudaSuccess) return fail(GDMR_ECUDA, "gdmr_solve_batch", "synchronise");
+    if (worst != GDMR_OK) set_last_error(worst, "gdmr_solve_batch: some right-hand sides did not converge");
+    else set_last_error(GDMR_OK, "ok");
+    return worst;
+}
+
+template <class R>
+int single_impl(gdmr_system *S, int mode, const double *b, double *x, double tol, int matRank, int on_device,
+                gdmr_stats *stats) {
+    using C = typename CT<R>::t;
+    Engine<R> &E = eng_of<R>(S);
+    const int n = S->n;
+    const size_t vb = sizeof(double2) * (size_t)n;
+    double2 *db = S->db, *dx = S->dx;
+    if (on_device) {
+        cudaMemcpyAsync(db, b, vb, cudaMemcpyDeviceToDevice, S->st);
+        cudaMemcpyAsync(dx, x, vb, cudaMemcpyDeviceToDevice, S->st);
+    } else {
+        cudaMemcpyAsync(db, b, vb, cudaMemcpyHostToDevice, S->st);
+        cudaMemcpyAsync(dx, x, vb, cudaMemcpyHostToDevice, S->st);
+    }
+    C *bR, *xR;
+    if (sizeof(R) == 8) {
+        bR = (C *)db;
+        xR = (C *)dx;
+    } else {
+        // complex64 working copies live in the staging area's second half
+        bR = (C *)(db + (size_t)n);
+        xR = (C *)(dx + (size_t)n);
+        gdmr_demote_vec(n, db, (float2 *)bR, S->st);
+        gdmr_demote_vec(n, dx, (float2 *)xR, S->st);
+    }
+    SolveStats st;
+    E.solve_reference(mode, bR, xR, tol, matRank, &st);
+    if (sizeof(R) == 4) {
+        gdmr_promote_vec(n, (const float2 *)xR, dx, S->st);
+    }
+    // true FP64 residual
+    double rel = -1;
+    if (E.refine_setup(S->A.view64()) == GDMR_OK) E.true_residual(1, db, dx, &rel);
+    st.true_rel_res = rel;
+    if (on_device) cudaMemcpyAsync(x, dx, vb, cudaMemcpyDeviceToDevice, S->st);
+    else cudaMemcpyAsync(x, dx, vb, cudaMemcpyDeviceToHost, S->st);
+    cudaStreamSynchronize(S->st);
+    if (stats) to_stats(st, stats);
+    record(st);
+    return st.status;
+}
+
+}  // namespace
+
+extern "C" int gdmr_system_create(gdmr_system **out, int n, const int *rowPtr, const int *colIdx, const double *vals_ri,
+                                  int basisDim, int deflatDim, int capacity, int precision, int device) {
+    if (!out) return fail(GDMR_EINVAL, "gdmr_system_create", "null output pointer");
+    *out = nullptr;
+    if (precision != 0 && precision != 1) return fail(GDMR_EINVAL, "gdmr_system_create", "precision must be 0 or 1");
+    if (capacity < 1) return fail(GDMR_EINVAL, "gdmr_system_create", "capacity must be >= 1");
+    if (cudaSetDevice(device) != cudaSuccess) return fail(GDMR_ECUDA, "gdmr_system_create", "cudaSetDevice");
+    std::unique_ptr<gdmr_system> S(new gdmr_system());
+    S->n = n; S->m = basisDim; S->k = deflatDim; S->cap = capacity; S->precision = precision; S->device = device;
+    if (cudaStreamCreateWithFlags(&S->st, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(GDMR_ECUDA, "gdmr_system_create", "stream");
+    int rc = sell_from_csr(S->A, n, rowPtr, colIdx, vals_ri, precision == 1, true, S->st);
+    if (rc != GDMR_OK) return rc;
+    if (precision == 1) {
+        rc = S->e32.init(n, basisDim, deflatDim, capacity, device);
+        S->e32.op.kind = Operator<float>::SELL;
+        S->e32.op.sell = S->A.view32();
+        S->e32.stream = S->st;
+    } else {
+        rc = S->e64.init(n, basisDim, deflatDim, capacity, device);
+        S->e64.op.kind = Operator<double>::SELL;
+        S->e64.op.sell = S->A.view64();
+        S->e64.stream = S->st;
+    }
+    if (rc != GDMR_OK) return rc;
+    const size_t stage = sizeof(double2) * (size_t)n * std::max(capacity, 2);
+    if (cudaMalloc(&S->db, stage) != cudaSuccess || cudaMalloc(&S->dx, stage) != cudaSuccess)
+        return fail(GDMR_ENOMEM, "gdmr_system_create", "staging buffers");
+    *out = S.release();
+    set_last_error(GDMR_OK, "ok");
+    return GDMR_OK;
+}
+
+extern "C" int gdmr_system_destroy(gdmr_system *S) {
+    if (!S) return GDMR_OK;
+    cudaSetDevice(S->device);
+    if (S->st) cudaStreamSynchronize(S->st);
+    S->e32.release();
+    S->e64.release();
+    sell_free(S->A);
+    if (S->db) cudaFree(S->db);
+    if (S->dx) cudaFree(S->dx);
+    if (S->st) cudaStreamDestroy(S->st);
+    delete S;
+    return GDMR_OK;
+}
+
+extern "C" long long gdmr_system_bytes(const gdmr_system *S) {
+    if (!S) return 0;
+    return (long long)(S->A.bytes() + S->e32.device_bytes() + S->e64.device_bytes() +
+                       2 * sizeof(double2) * (size_t)S->n * std::max(S->cap, 2));
+}
+
+extern "C" int gdmr_solve(gdmr_system *S, int mode, const double *b, double *x, double tol, int matRank, int on_device,
+                          gdmr_stats *stats) {
+    if (!S || !b || !x) return fail(GDMR_EINVAL, "gdmr_solve", "null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    cudaSetDevice(S->device);
+    return S->precision == 1 ? single_impl<float>(S, mode, b, x, tol, matRank, on_device, stats)
+                             : single_impl<double>(S, mode, b, x, tol, matRank, on_device, stats);
+}
+
+extern "C" int gdmr_solve_batch(gdmr_system *S, int nrhs, const double *b, double *x, const double *tol,
+                                int maxCycles, int on_device, gdmr_stats *stats) {
+    if (!S || !b || !x || nrhs < 1) return fail(GDMR_EINVAL, "gdmr_solve_batch", "null argument or nrhs < 1");
+    std::lock_guard<std::mutex> lk(S->mu);
+    cudaSetDevice(S->device);
+    return S->precision == 1 ? batch_impl<float>(S, nrhs, b, x, tol, maxCycles, on_device, stats)
+                             : batch_impl<double>(S, nrhs, b, x, tol, maxCycles, on_device, stats);
+}
+
+extern "C" int gdmr_true_residual(gdmr_system *S, int nrhs, const double *b, const double *x, int on_device,
+                                  double *relres) {
+    if (!S || !b || !x || !relres || nrhs < 1) return fail(GDMR_EINVAL, "gdmr_true_residual", "bad argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    cudaSetDevice(S->device);
+    const size_t vb = sizeof(double2) * (size_t)S->n;
+    auto run = [&](auto &E) -> int {
+        int rc = E.refine_setup(S->A.view64());
+        if (rc != GDMR_OK) return rc;
+        if (on_device) return E.true_residual(nrhs, (const double2 *)b, (const double2 *)x, relres);
+        for (int r = 0; r < nrhs; r += S->cap) {
+            const int cnt = std::min(S->cap, nrhs - r);
+            cudaMemcpyAsync(S->db, b + (size_t)2 * r * S->n, vb * cnt, cudaMemcpyHostToDevice, S->st);
+            cudaMemcpyAsync(S->dx, x + (size_t)2 * r * S->n, vb * cnt, cudaMemcpyHostToDevice, S->st);
+            if ((rc = E.true_residual(cnt, S->db, S->dx, relres + r)) != GDMR_OK) return rc;
+        }
+        return GDMR_OK;
+    };
+    return S->precision == 1 ? run(S->e32) : run(S->e64);
+}
+
+extern "C" int gdmr_export_deflation(gdmr_system *S, double *z) {
+    if (!S || !z) return fail(GDMR_EINVAL, "gdmr_export_deflation", "null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    cudaSetDevice(S->device);
+    if (S->precision == 0) return S->e64.export_deflation((double2 *)z);
+    std::vector<float2> tmp((size_t)S->k * S->n);
+    int rc = S->e32.export_deflation(tmp.data());
+    for (size_t i = 0; i < tmp.size(); ++i) { z[2 * i] = tmp[i].x; z[2 * i + 1] = tmp[i].y; }
+    return rc;
+}
+
+extern "C" int gdmr_import_deflation(gdmr_system *S, const double *z) {
+    if (!S || !z) return fail(GDMR_EINVAL, "gdmr_import_deflation", "null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    cudaSetDevice(S->device);
+    if (S->precision == 0) return S->e64.import_deflation((const double2 *)z);
+    std::vector<float2> tmp((size_t)S->k * S->n);
+    for (size_t i = 0; i < tmp.size(); ++i) tmp[i] = make_float2((float)z[2 * i], (float)z[2 * i + 1]);
+    return S->e32.import_deflation(tmp.data());
+}
+
+extern "C" int gdmr_drop_deflation(gdmr_system *S) {
+    if (!S) return fail(GDMR_EINVAL, "gdmr_drop_deflation", "null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->e32.drop_deflation();
+    S->e64.drop_deflation();
+    return GDMR_OK;
+}

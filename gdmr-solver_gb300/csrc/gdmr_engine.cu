@@ -1,0 +1,653 @@
+// Host engine of the GB300 DMR solver.  See gdmr_engine.h.
+#include "gdmr_engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+namespace gdmr {
+
+// ----------------------------------------------------------------- errors
+namespace {
+std::mutex g_err_mu;
+int g_status = GDMR_OK;
+std::string g_msg = "ok";
+}  // namespace
+
+void set_last_error(int status, const std::string &msg) {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_status = status;
+    g_msg = msg;
+}
+int last_status() {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    return g_status;
+}
+const char *last_error() {
+    static thread_local std::string copy;
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    copy = g_msg;
+    return copy.c_str();
+}
+
+#define GDMR_CK(call)                                                                                                  \
+    do {                                                                                                               \
+        cudaError_t e_ = (call);                                                                                       \
+        if (e_ != cudaSuccess) {                                                                                       \
+            set_last_error(GDMR_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));                            \
+            return GDMR_ECUDA;                                                                                         \
+        }                                                                                                              \
+    } while (0)
+
+// ----------------------------------------------------------------- helper kernels
+namespace {
+
+template <class C> __global__ void k_sub(int n, const C *__restrict__ a, const C *__restrict__ b, C *__restrict__ out) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        C u = a[i], v = b[i];
+        u.x -= v.x;
+        u.y -= v.y;
+        out[i] = u;
+    }
+}
+
+__global__ void k_cycle_reset(const int *__restrict__ act, int nsys, SysState *state, int set_unit) {
+    for (int i = threadIdx.x; i < nsys; i += blockDim.x) {
+        SysState &st = state[act[i]];
+        st.broken = 0;
+        if (set_unit) st.rho_abs = 1.0;
+    }
+}
+
+__global__ void k_state_init(SysState *state, int count) {
+    for (int i = threadIdx.x; i < count; i += blockDim.x) {
+        SysState z{};
+        state[i] = z;
+    }
+}
+
+template <class C> void sub(int n, const C *a, const C *b, C *out, cudaStream_t st) {
+    int blocks = (n + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    k_sub<C><<<blocks, 256, 0, st>>>(n, a, b, out);
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------- SELL build
+size_t DeviceSell::bytes() const {
+    return sizeof(int) * ((size_t)nslices + 1 + padded) + (vals32 ? sizeof(float2) * padded : 0) +
+           (vals64 ? sizeof(double2) * padded : 0);
+}
+
+int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, const double *vals_ri, bool want32,
+                  bool want64, cudaStream_t st) {
+    if (n <= 0 || !rowptr || !colidx || !vals_ri) {
+        set_last_error(GDMR_EINVAL, "sell_from_csr: empty matrix or null arrays");
+        return GDMR_EINVAL;
+    }
+    const int ns = (n + 31) / 32;
+    std::vector<int> sp(ns + 1, 0);
+    for (int s = 0; s < ns; ++s) {
+        int w = 0;
+        for (int r = s * 32; r < std::min(n, s * 32 + 32); ++r) {
+            int len = rowptr[r + 1] - rowptr[r];
+            if (len < 0) {
+                set_last_error(GDMR_EINVAL, "sell_from_csr: row pointers are not non-decreasing");
+                return GDMR_EINVAL;
+            }
+            w = std::max(w, len);
+        }
+        long next = (long)sp[s] + 32L * w;
+        if (next > 0x7fffffffL) {
+            set_last_error(GDMR_EINVAL, "sell_from_csr: more than 2^31 stored entries");
+            return GDMR_EINVAL;
+        }
+        sp[s + 1] = (int)next;
+    }
+    const long padded = sp[ns];
+    std::vector<int> cols(padded);
+    std::vector<float2> v32(want32 ? padded : 0);
+    std::vector<double2> v64(want64 ? padded : 0);
+    for (int s = 0; s < ns; ++s) {
+        const int w = (sp[s + 1] - sp[s]) / 32;
+        for (int lane = 0; lane < 32; ++lane) {
+            const int r = s * 32 + lane;
+            const int beg = r < n ? rowptr[r] : 0, len = r < n ? rowptr[r + 1] - rowptr[r] : 0;
+            for (int c = 0; c < w; ++c) {
+                const long e = (long)sp[s] + (long)c * 32 + lane;
+                int col = r < n ? r : 0;
+                double re = 0, im = 0;
+                if (c < len) {
+                    col = colidx[beg + c];
+                    if (col < 0 || col >= n) {
+                        set_last_error(GDMR_EINVAL, "sell_from_csr: column index out of range");
+                        return GDMR_EINVAL;
+                    }
+                    re = vals_ri[2 * (size_t)(beg + c)];
+                    im = vals_ri[2 * (size_t)(beg + c) + 1];
+                }
+                cols[e] = col;
+                if (want32) v32[e] = make_float2((float)re, (float)im);
+                if (want64) v64[e] = make_double2(re, im);
+            }
+        }
+    }
+    DeviceSell d;
+    d.n = n;
+    d.nnz = rowptr[n] - rowptr[0];
+    d.padded = padded;
+    d.nslices = ns;
+    GDMR_CK(cudaGetDevice(&d.device));
+    GDMR_CK(cudaMalloc(&d.slice_ptr, sizeof(int) * (ns + 1)));
+    GDMR_CK(cudaMalloc(&d.cols, sizeof(int) * std::max<long>(padded, 1)));
+    GDMR_CK(cudaMemcpyAsync(d.slice_ptr, sp.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice, st));
+    GDMR_CK(cudaMemcpyAsync(d.cols, cols.data(), sizeof(int) * padded, cudaMemcpyHostToDevice, st));
+    if (want32) {
+        GDMR_CK(cudaMalloc(&d.vals32, sizeof(float2) * std::max<long>(padded, 1)));
+        GDMR_CK(cudaMemcpyAsync(d.vals32, v32.data(), sizeof(float2) * padded, cudaMemcpyHostToDevice, st));
+    }
+    if (want64) {
+        GDMR_CK(cudaMalloc(&d.vals64, sizeof(double2) * std::max<long>(padded, 1)));
+        GDMR_CK(cudaMemcpyAsync(d.vals64, v64.data(), sizeof(double2) * padded, cudaMemcpyHostToDevice, st));
+    }
+    GDMR_CK(cudaStreamSynchronize(st));
+    sell_free(out);
+    out = d;
+    return GDMR_OK;
+}
+
+void sell_free(DeviceSell &s) {
+    if (s.slice_ptr) cudaFree(s.slice_ptr);
+    if (s.cols) cudaFree(s.cols);
+    if (s.vals32) cudaFree(s.vals32);
+    if (s.vals64) cudaFree(s.vals64);
+    s = DeviceSell();
+}
+
+// ----------------------------------------------------------------- engine
+template <class R> Engine<R>::~Engine() { release(); }
+
+template <class R> int Engine<R>::alloc(void **p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes > 0 ? bytes : 16);
+    if (e != cudaSuccess) {
+        set_last_error(GDMR_ENOMEM, std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes: " +
+                                        cudaGetErrorString(e));
+        return GDMR_ENOMEM;
+    }
+    allocs_.push_back(*p);
+    bytes_ += bytes;
+    return GDMR_OK;
+}
+
+template <class R> void Engine<R>::release() {
+    for (void *p : allocs_) cudaFree(p);
+    allocs_.clear();
+    if (hstate_) cudaFreeHost(hstate_);
+    hstate_ = nullptr;
+    V_ = W_ = Z_ = Znew_ = R_ = X_ = Y_ = T_ = AZ_ = nullptr;
+    H_ = Hd_ = coef_ = coefD_ = g_ = y_ = t_ = vs_ = svdwork_ = partials_ = r64_ = b64_ = x64_ = nullptr;
+    slot_.clear();
+    act_h_.clear();
+    sigma_ = znorm2_ = nullptr;
+    sweeps_ = nullptr;
+    tickets_ = nullptr;
+    state_ = nullptr;
+    act_ = ident_ = nullptr;
+    n_ = m_ = k_ = cap_ = 0;
+    bytes_ = 0;
+    have_z_ = false;
+}
+
+template <class R> int Engine<R>::init(int n, int m, int k, int capacity, int device) {
+    release();
+    if (n <= 0 || m < 2 || k < 0 || m - k < 2 || capacity < 1) {
+        set_last_error(GDMR_EINVAL, "engine: need n > 0, basisDim - deflatDim >= 2, capacity >= 1");
+        return GDMR_EINVAL;
+    }
+    if (m > 160) {
+        set_last_error(GDMR_EINVAL, "engine: basisDim above 160 is not supported (device least squares)");
+        return GDMR_EINVAL;
+    }
+    GDMR_CK(cudaSetDevice(device));
+    n_ = n; m_ = m; k_ = k; cap_ = capacity; dev_ = device;
+    const size_t vn = (size_t)n * sizeof(C);
+    int rc = GDMR_OK;
+#define A_(ptr, bytes)                                                                                                 \
+    if ((rc = alloc((void **)&ptr, bytes)) != GDMR_OK) { release(); return rc; }
+    A_(V_, vn * (m + 1) * capacity);
+    A_(W_, vn * std::max(k, 1));
+    A_(Z_, vn * std::max(k, 1));
+    A_(Znew_, vn * std::max(k, 1));
+    A_(R_, vn * capacity);
+    A_(X_, vn * capacity);
+    A_(Y_, vn * capacity);
+    A_(T_, vn * capacity);
+    A_(AZ_, vn);
+    A_(H_, sizeof(double2) * strideH() * capacity);
+    A_(Hd_, sizeof(double2) * strideH());
+    A_(coef_, sizeof(double2) * strideC() * (capacity + 1));
+    A_(coefD_, sizeof(double2) * strideC());
+    A_(g_, sizeof(double2) * strideC() * capacity);
+    A_(y_, sizeof(double2) * strideC() * capacity);
+    A_(t_, sizeof(double2) * strideC() * capacity);
+    A_(vs_, sizeof(double2) * (size_t)m * std::max(k, 1));
+    A_(svdwork_, sizeof(double2) * 2 * (size_t)m * (m + 1));
+    A_(sigma_, sizeof(double) * m);
+    A_(znorm2_, sizeof(double) * std::max(k, 1));
+    A_(sweeps_, sizeof(int));
+    A_(partials_, sizeof(double) * scratch_doubles(qmax() + 16, capacity + 1));
+    A_(tickets_, sizeof(unsigned) * (capacity + 1));
+    A_(state_, sizeof(SysState) * (capacity + 1));
+    A_(act_, sizeof(int) * (capacity + 1));
+    A_(ident_, sizeof(int) * (capacity + 1));
+#undef A_
+    if (cudaMallocHost(&hstate_, sizeof(SysState) * (capacity + 1)) != cudaSuccess) {
+        release();
+        set_last_error(GDMR_ENOMEM, "engine: pinned host state");
+        return GDMR_ENOMEM;
+    }
+    std::vector<int> id(capacity + 1);
+    for (int i = 0; i <= capacity; ++i) id[i] = i;
+    GDMR_CK(cudaMemcpy(ident_, id.data(), sizeof(int) * (capacity + 1), cudaMemcpyHostToDevice));
+    GDMR_CK(cudaMemset(tickets_, 0, sizeof(unsigned) * (capacity + 1)));
+    GDMR_CK(cudaMemset(V_, 0, vn * (m + 1) * capacity));
+    GDMR_CK(cudaMemset(Z_, 0, vn * std::max(k, 1)));
+    GDMR_CK(cudaMemset(X_, 0, vn * capacity));
+    k_state_init<<<1, 256>>>(state_, capacity + 1);
+    GDMR_CK(cudaGetLastError());
+    GDMR_CK(cudaDeviceSynchronize());
+    flag_count_ = 0;
+    have_z_ = false;
+    return GDMR_OK;
+}
+
+template <class R> int Engine<R>::set_active(const std::vector<int> &act) {
+    act_h_ = act;
+    if (!act.empty()) GDMR_CK(cudaMemcpyAsync(act_, act.data(), sizeof(int) * act.size(), cudaMemcpyHostToDevice, stream));
+    return GDMR_OK;
+}
+
+template <class R> int Engine<R>::read_state(int count) {
+    GDMR_CK(cudaMemcpyAsync(hstate_, state_, sizeof(SysState) * count, cudaMemcpyDeviceToHost, stream));
+    GDMR_CK(cudaStreamSynchronize(stream));
+    if (profile_enabled()) profile_flush();
+    return GDMR_OK;
+}
+
+// y_s = A x_s for the active systems (nsys of them; the active list is act_).
+template <class R>
+void Engine<R>::apply(const C *x0, size_t strideX, C *y0, size_t strideY, int nsys, long *matvecs) {
+    *matvecs += nsys;
+    switch (op.kind) {
+    case Operator<R>::SELL:
+        launch_spmm<R>(op.sell, x0, strideX, y0, strideY, act_, nsys, stream);
+        break;
+    case Operator<R>::DENSE:
+        for (int i = 0; i < nsys; ++i) {
+            const int s = act_h_[i];
+            launch_dense_gemv<R>(n_, op.dense, x0 + s * strideX, y0 + s * strideY, stream);
+        }
+        break;
+    case Operator<R>::HOOK: {
+        // the hook reads and overwrites its own buffer in place, on this stream
+        if (x0 != op.ext) cudaMemcpyAsync(op.ext, x0, sizeof(C) * n_, cudaMemcpyDeviceToDevice, stream);
+        op.hook();
+        if (y0 != op.ext) cudaMemcpyAsync(y0, op.ext, sizeof(C) * n_, cudaMemcpyDeviceToDevice, stream);
+        break;
+    }
+    default:
+        break;
+    }
+}
+
+template <class R> int Engine<R>::run_cycle(int kk, int nsys, int lead, double tol, long *matvecs) {
+    const int n = n_, m = m_;
+    const size_t sV = strideV(), sC = strideC();
+    const bool hook = op.kind == Operator<R>::HOOK;
+    GDMR_CK(cudaMemsetAsync(H_, 0, sizeof(double2) * strideH() * cap_, stream));
+    k_cycle_reset<<<1, 256, 0, stream>>>(act_, nsys, state_, 0);
+    if (kk > 0) {
+        // Deflation loop (arnoldiDMR, gDMR.cu:1823-2030): W_i = orth(A z_i), H[:i+1, i].
+        // The shared pseudo-system has state index cap_ and active list ident_+cap_.
+        GDMR_CK(cudaMemsetAsync(Hd_, 0, sizeof(double2) * strideH(), stream));
+        int *pact = ident_ + cap_;
+        for (int i = 0; i < kk; ++i) {
+            C *az = hook ? op.ext : AZ_;
+            // the SELL path uses the pseudo-system slot so the batch list is not disturbed
+            if (op.kind == Operator<R>::SELL) {
+                *matvecs += 1;
+                launch_spmm<R>(op.sell, Z_ + (size_t)i * n, 0, az, 0, ident_, 1, stream);
+            } else {
+                std::vector<int> keep = act_h_;
+                act_h_ = {0};
+                apply(Z_ + (size_t)i * n, 0, az, 0, 1, matvecs);
+                act_h_ = keep;
+            }
+            if (i > 0)
+                launch_mdot<R>(n, W_, i, nullptr, 0, 0, az, 0, pact, 1, partials_, qmax(), tickets_ + cap_, coefD_, 0,
+                               state_, false, stream);
+            FinishArgs f{};
+            f.mode = FIN_DEFLATION; f.col = i; f.nco = i; f.ldH = m + 1; f.m = m; f.kk = kk;
+            f.H = Hd_; f.strideH = 0; f.coef = coefD_; f.strideC = 0;
+            launch_update<R>(n, W_, i, nullptr, 0, 0, az, 0, T_, 0, pact, 1, coefD_, 0, partials_, tickets_ + cap_,
+                             state_, f, false, stream);
+            launch_scale<R>(n, T_, 0, W_ + (size_t)i * n, 0, nullptr, 0, pact, 1, state_, false, stream);
+        }
+        launch_broadcast_hdef(m, kk, Hd_, H_, strideH(), act_, nsys, stream);
+        // v0 <- (I - W W^H) v0 / ||.||  (deflatorDMR(0,0), gDMR.cu:2033-2059)
+        launch_mdot<R>(n, W_, kk, nullptr, 0, 0, V_, sV, act_, nsys, partials_, qmax(), tickets_, coef_, sC, state_,
+                       false, stream);
+        FinishArgs f{};
+        f.mode = FIN_UNIT;
+        launch_update<R>(n, W_, kk, nullptr, 0, 0, V_, sV, T_, n, act_, nsys, coef_, sC, partials_, tickets_, state_, f,
+                         false, stream);
+        launch_scale<R>(n, T_, n, V_, sV, hook ? op.ext : nullptr, 0, act_, nsys, state_, false, stream);
+    } else if (hook) {
+        cudaMemcpyAsync(op.ext, V_, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
+    }
+    // Krylov loop (gDMR.cu:2069-2328): classical Gram-Schmidt against [W V] in one pass.
+    for (int j = 1; j <= m - kk; ++j) {
+        const int col = kk + j - 1;
+        if (hook) {
+            *matvecs += 1;
+            op.hook();      // v_{j-1} is already in the hook buffer
+        } else {
+            apply(V_ + (size_t)(j - 1) * n, sV, Y_, n, nsys, matvecs);
+        }
+        const C *w = op_out(0);
+        const size_t sW = op_out_stride();
+        launch_mdot<R>(n, W_, kk, V_, sV, j, w, sW, act_, nsys, partials_, qmax(), tickets_, coef_, sC, state_, true,
+                       stream);
+        FinishArgs f{};
+        f.mode = FIN_KRYLOV; f.col = col; f.nco = kk + j; f.ldH = m + 1; f.m = m; f.kk = kk;
+        f.compat_eye = compat_eye ? 1 : 0; f.tol = tol; f.H = H_; f.strideH = strideH(); f.coef = coef_; f.strideC = sC;
+        launch_update<R>(n, W_, kk, V_, sV, j, w, sW, T_, n, act_, nsys, coef_, sC, partials_, tickets_, state_, f, true,
+                         stream);
+        launch_scale<R>(n, T_, n, V_ + (size_t)j * n, sV, hook ? op.ext : nullptr, 0, act_, nsys, state_, true, stream);
+    }
+    // g = [W V]^H r (updateTrgCoeffsDMR, gDMR.cu:2334-2408)
+    launch_mdot<R>(n, W_, kk, V_, sV, m + 1 - kk, R_, n, act_, nsys, partials_, qmax(), tickets_, g_, sC, state_, false,
+                   stream);
+    // y = argmin ||H y - g||, t = H y (qrHessArrDMR/qrSolveDMR/hessenbergMultDMR)
+    launch_ls(m, H_, strideH(), g_, y_, t_, sC, act_, nsys, stream);
+    // r -= [W V] t ; x += rho_abs [Z V] y ; rho = ||r|| (updateAppResDMR, gDMR.cu:2411-2582)
+    launch_combine<R>(n, kk, m, W_, Z_, V_, sV, R_, n, X_, n, t_, y_, sC, act_, nsys, partials_, tickets_, state_,
+                      stream);
+    launch_scale<R>(n, R_, n, R_, n, nullptr, 0, act_, nsys, state_, false, stream);
+    // deflation-space update from the lead system (genDeflatDMR, gDMR.cu:1583-1704)
+    if (k_ > 0) {
+        launch_svd_smallest(m, k_, H_ + (size_t)lead * strideH(), vs_, sigma_, svdwork_, sweeps_, stream);
+        launch_zupdate<R>(n, kk, m, k_, Z_, Vs(lead), vs_, Znew_, partials_, tickets_ + cap_, znorm2_, stream);
+        launch_znormalise<R>(n, k_, Znew_, znorm2_, Znew_, stream);
+        std::swap(Z_, Znew_);
+        have_z_ = true;
+    }
+    GDMR_CK(cudaGetLastError());
+    return GDMR_OK;
+}
+
+template <class R>
+double Engine<R>::solve_reference(int mode, const C *b, C *x, double tol, int mat_rank, SolveStats *stats) {
+    SolveStats local;
+    SolveStats &S = stats ? *stats : local;
+    S = SolveStats();
+    const int n = n_, m = m_, k = k_;
+    auto fail = [&](double ret) {
+        S.status = last_status();
+        S.rel_res = ret;
+        return ret;
+    };
+    if (!ready()) {
+        set_last_error(GDMR_ENOTINIT, "solver used before initialisation");
+        S.status = GDMR_ENOTINIT;
+        return 1.0;
+    }
+    S.its = mat_rank * mat_rank;
+    const bool hook = op.kind == Operator<R>::HOOK;
+    if (set_active({0}) != GDMR_OK) return fail(1.0);
+    // ||b||
+    launch_norm<R>(n, b, 0, act_, 1, partials_, tickets_, state_, 1, stream);
+    // x~ = x0; r = b - A x0  (the hook overwrites x with A x0, as the reference's does)
+    cudaMemcpyAsync(X_, x, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
+    apply(X_, 0, hook ? op.ext : Y_, 0, 1, &S.matvecs);
+    sub<C>(n, b, hook ? op.ext : Y_, R_, stream);
+    launch_norm<R>(n, R_, 0, act_, 1, partials_, tickets_, state_, 2, stream);
+    if (read_state(1) != GDMR_OK) return fail(1.0);
+    const double bnorm = hstate_[0].bnorm;
+    double rho_abs = hstate_[0].rho_abs;
+    if (rho_abs < bnorm * tol) {     // gDMR.cu:2785-2796: absolute norm returned, x unchanged
+        cudaMemcpyAsync(x, X_, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
+        cudaStreamSynchronize(stream);
+        S.rel_res = rho_abs;
+        S.cycles = 0;
+        return rho_abs;
+    }
+    launch_scale<R>(n, R_, 0, R_, 0, nullptr, 0, act_, 1, state_, false, stream);
+    const int first_def = mode == 0 ? 0 : k;
+    int loop_flag = 0, cycle = 0, kk_prev = 0;
+    if (mode != 0 && !have_z_ && k > 0) {
+        // the reference would use whatever its deflation buffers hold (zeros after init)
+    }
+    while (rho_abs > tol * bnorm) {
+        if (cycle > mat_rank) {
+            set_last_error(GDMR_ENOCONV, "solver failed to converge within matRank restart cycles");
+            S.its = cycle;
+            S.cycles = cycle;
+            S.status = GDMR_ENOCONV;
+            S.rel_res = rho_abs / bnorm;
+            cudaMemcpyAsync(x, X_, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
+            cudaStreamSynchronize(stream);
+            return rho_abs / bnorm;
+        }
+        if (rho_abs / bnorm > 1.0) {
+            set_last_error(GDMR_ERUNAWAY, "solver runaway: residual above the right-hand side norm");
+            S.its = cycle;
+            S.cycles = cycle;
+            S.status = GDMR_ERUNAWAY;
+            S.rel_res = rho_abs / bnorm;
+            cudaMemcpyAsync(x, X_, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
+            cudaStreamSynchronize(stream);
+            return rho_abs / bnorm;
+        }
+        const int kk = (cycle == 0 && first_def == 0) ? 0 : k;
+        // restart vector (arnoldiSetupDMR, gDMR.cu:2600-2621); a zero period would divide by zero there
+        const int period = (2 * mat_rank) / (m - k);
+        if (loop_flag == 0 || (period != 0 && flag_count_ % period == 0)) {
+            cudaMemcpyAsync(V_, R_, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
+        } else {
+            const int idx = kk + (m - k) / 2 - kk_prev;   // the reference indexes its [W|V] storage
+            if (idx > 0 && idx <= m) cudaMemcpyAsync(V_, V_ + (size_t)idx * n, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
+        }
+        if (run_cycle(kk, 1, 0, tol, &S.matvecs) != GDMR_OK) return fail(1.0);
+        if (read_state(1) != GDMR_OK) return fail(1.0);
+        const SysState &st = hstate_[0];
+        if (st.broken) S.breakdowns++;
+        const double rho = st.rho;
+        if (rho > 0.995) {            // gDMR.cu:2506-2514
+            loop_flag = 1;
+            ++flag_count_;
+        } else {
+            loop_flag = 0;
+        }
+        rho_abs = st.rho_abs;
+        kk_prev = kk;
+        ++cycle;
+    }
+    S.its = cycle - 1;
+    S.cycles = cycle;
+    S.rel_res = rho_abs / bnorm;
+    cudaMemcpyAsync(x, X_, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
+    if (cudaStreamSynchronize(stream) != cudaSuccess) {
+        set_last_error(GDMR_ECUDA, "solver: final synchronisation failed");
+        return fail(rho_abs / bnorm);
+    }
+    return rho_abs / bnorm;
+}
+
+template <class R> int Engine<R>::refine_setup(const SellMatrix &A64) {
+    if (!ready()) {
+        set_last_error(GDMR_ENOTINIT, "solver used before initialisation");
+        return GDMR_ENOTINIT;
+    }
+    if (op.kind != Operator<R>::SELL || !A64.vals) {
+        set_last_error(GDMR_EINVAL, "refined solve: needs a SELL operator with FP64 values");
+        return GDMR_EINVAL;
+    }
+    A64_ = A64;
+    if (!r64_) {
+        int rc;
+        if ((rc = alloc((void **)&r64_, sizeof(double2) * (size_t)n_ * cap_)) != GDMR_OK) return rc;
+        if ((rc = alloc((void **)&b64_, sizeof(double2) * (size_t)n_ * cap_)) != GDMR_OK) return rc;
+        if ((rc = alloc((void **)&x64_, sizeof(double2) * (size_t)n_ * cap_)) != GDMR_OK) return rc;
+    }
+    slot_.assign(cap_, Slot());
+    act_h_.clear();
+    kk_prev_ = 0;
+    GDMR_CK(cudaMemsetAsync(X_, 0, sizeof(C) * (size_t)n_ * cap_, stream));
+    return GDMR_OK;
+}
+
+template <class R>
+int Engine<R>::refine_admit(int slot, const double2 *b, const double2 *x0, double tol, int max_cycles) {
+    if (slot < 0 || slot >= cap_ || slot_[slot].active) {
+        set_last_error(GDMR_EINVAL, "refine_admit: slot out of range or busy");
+        return GDMR_EINVAL;
+    }
+    const size_t vb = sizeof(double2) * (size_t)n_;
+    GDMR_CK(cudaMemcpyAsync(slot_b(slot), b, vb, cudaMemcpyDeviceToDevice, stream));
+    if (x0) GDMR_CK(cudaMemcpyAsync(slot_x(slot), x0, vb, cudaMemcpyDeviceToDevice, stream));
+    else GDMR_CK(cudaMemsetAsync(slot_x(slot), 0, vb, stream));
+    GDMR_CK(cudaMemsetAsync(X_ + (size_t)slot * n_, 0, sizeof(C) * (size_t)n_, stream));
+    Slot &S = slot_[slot];
+    S = Slot();
+    S.active = true;
+    S.tol = tol;
+    S.max_cycles = max_cycles;
+    S.bnorm = -1;   // measured with the first residual
+    act_h_.push_back(slot);
+    return GDMR_OK;
+}
+
+template <class R> int Engine<R>::refine_cycle(std::vector<int> *done) {
+    const int n = n_, m = m_, k = k_;
+    if (act_h_.empty()) return GDMR_OK;
+    std::vector<int> act = act_h_;
+    if (set_active(act) != GDMR_OK) return GDMR_ECUDA;
+    int na = (int)act.size();
+    // ||b|| for newcomers
+    std::vector<int> fresh;
+    for (int s : act)
+        if (slot_[s].bnorm < 0) fresh.push_back(s);
+    if (!fresh.empty()) {
+        if (set_active(fresh) != GDMR_OK) return GDMR_ECUDA;
+        launch_norm<double>(n, b64_, n, act_, (int)fresh.size(), partials_, tickets_, state_, 1, stream);
+        if (set_active(act) != GDMR_OK) return GDMR_ECUDA;
+    }
+    // true FP64 residual of every active system
+    launch_residual64(A64_, b64_, n, x64_, n, r64_, n, act_, na, partials_, tickets_, state_, stream);
+    if (read_state(cap_) != GDMR_OK) return GDMR_ECUDA;
+    std::vector<int> next;
+    int lead = -1;
+    double worst = -1;
+    for (int s : act) {
+        Slot &S = slot_[s];
+        const SysState &st = hstate_[s];
+        if (S.bnorm < 0) S.bnorm = st.bnorm;
+        const double rel = S.bnorm > 0 ? st.true_res / S.bnorm : 0.0;
+        S.stats.true_rel_res = rel;
+        S.stats.rel_res = rel;
+        S.stats.matvecs += 1;   // the FP64 residual product
+        int fin = -1;
+        if (st.bad || !std::isfinite(rel)) fin = GDMR_ERUNAWAY;
+        else if (rel <= S.tol) fin = GDMR_OK;
+        else if (S.stats.cycles >= S.max_cycles) fin = GDMR_ENOCONV;
+        if (fin >= 0) {
+            S.stats.status = fin;
+            S.stats.its = S.stats.cycles > 0 ? S.stats.cycles - 1 : 0;
+            S.active = false;
+            if (done) done->push_back(s);
+            continue;
+        }
+        next.push_back(s);
+        if (rel > worst) { worst = rel; lead = s; }
+    }
+    act_h_ = next;
+    if (next.empty()) return GDMR_OK;
+    if (set_active(next) != GDMR_OK) return GDMR_ECUDA;
+    na = (int)next.size();
+    // unit residual direction in precision R; the inner recursion starts at rho_abs = 1
+    launch_demote_unit<R>(n, r64_, n, R_, n, act_, na, state_, stream);
+    k_cycle_reset<<<1, 256, 0, stream>>>(act_, na, state_, 1);
+    const int kk = (k > 0 && have_z_) ? k : 0;
+    for (int s : next) {
+        Slot &S = slot_[s];
+        const int period = (2 * S.max_cycles) / (m - k);
+        if (S.loop_flag == 0 || (period != 0 && S.flag_count % period == 0)) {
+            cudaMemcpyAsync(Vs(s), R_ + (size_t)s * n, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
+        } else {
+            const int idx = kk + (m - k) / 2 - kk_prev_;
+            if (idx > 0 && idx <= m)
+                cudaMemcpyAsync(Vs(s), Vs(s) + (size_t)idx * n, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
+        }
+    }
+    long mv = 0;
+    // breakdown of unit vectors: an invariant subspace at working precision
+    const double inner_tol = sizeof(R) == 4 ? 1e-6 : 1e-14;
+    if (run_cycle(kk, na, lead, inner_tol, &mv) != GDMR_OK) return GDMR_ECUDA;
+    launch_refine_update<R>(n, x64_, n, X_, n, act_, na, state_, stream);
+    if (read_state(cap_) != GDMR_OK) return GDMR_ECUDA;
+    for (int s : next) {
+        Slot &S = slot_[s];
+        const SysState &st = hstate_[s];
+        if (st.rho > 0.995) { S.loop_flag = 1; ++S.flag_count; } else S.loop_flag = 0;
+        S.stats.cycles += 1;
+        S.stats.matvecs += m;
+        if (st.broken) S.stats.breakdowns++;
+    }
+    kk_prev_ = kk;
+    return GDMR_OK;
+}
+
+template <class R> int Engine<R>::true_residual(int count, const double2 *b, const double2 *x, double *relres) {
+    if (!A64_.vals || !r64_) {
+        set_last_error(GDMR_ENOTINIT, "true_residual: refined form not set up");
+        return GDMR_ENOTINIT;
+    }
+    for (int c0 = 0; c0 < count; c0 += cap_) {
+        const int cnt = std::min(cap_, count - c0);
+        std::vector<int> act(cnt);
+        for (int i = 0; i < cnt; ++i) act[i] = i;
+        std::vector<int> keep = act_h_;
+        if (set_active(act) != GDMR_OK) return GDMR_ECUDA;
+        act_h_ = keep;
+        launch_norm<double>(n_, b + (size_t)c0 * n_, n_, act_, cnt, partials_, tickets_, state_, 1, stream);
+        launch_residual64(A64_, b + (size_t)c0 * n_, n_, x + (size_t)c0 * n_, n_, r64_, n_, act_, cnt, partials_,
+                          tickets_, state_, stream);
+        if (read_state(cnt) != GDMR_OK) return GDMR_ECUDA;
+        for (int i = 0; i < cnt; ++i)
+            relres[c0 + i] = hstate_[i].bnorm > 0 ? hstate_[i].true_res / hstate_[i].bnorm : hstate_[i].true_res;
+    }
+    return GDMR_OK;
+}
+
+template <class R> int Engine<R>::import_deflation(const C *host) {
+    if (!ready() || k_ == 0) return GDMR_OK;
+    GDMR_CK(cudaMemcpy(Z_, host, sizeof(C) * (size_t)k_ * n_, cudaMemcpyHostToDevice));
+    have_z_ = true;
+    return GDMR_OK;
+}
+
+template <class R> int Engine<R>::export_deflation(C *host) {
+    if (!ready() || k_ == 0) return GDMR_OK;
+    GDMR_CK(cudaStreamSynchronize(stream));
+    GDMR_CK(cudaMemcpy(host, Z_, sizeof(C) * (size_t)k_ * n_, cudaMemcpyDeviceToHost));
+    return GDMR_OK;
+}
+
+template class Engine<float>;
+template class Engine<double>;
+
+}  // namespace gdmr

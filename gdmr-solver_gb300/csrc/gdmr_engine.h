@@ -1,0 +1,173 @@
+// Host engine of the GB300 DMR solver: the restart cycle over B systems that
+// share one operator and one recycled deflation space.
+//
+// One engine owns every device buffer of a solve (no globals, no managed
+// memory, no per-call allocation); all work is enqueued on one stream and the
+// host synchronises once per restart cycle, to read the per-system residuals
+// that decide convergence.  B = 1 with reference semantics is the drop-in for
+// the reference's solverDMR (gDMR.cu:2638-2900); B > 1 with FP64 refinement is
+// the batched mixed-precision form.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "gdmr_kernels.cuh"
+
+extern "C" {
+#include "../../include/gdmr_ext.h"   // status codes GDMR_*
+}
+
+namespace gdmr {
+
+void set_last_error(int status, const std::string &msg);
+int last_status();
+const char *last_error();
+
+// A sparse operator resident on the device in SELL-32 form, with values in
+// complex64 and (optionally) complex128 sharing one index structure.
+struct DeviceSell {
+    int n = 0;
+    long nnz = 0;        // non-zeros of the source CSR
+    long padded = 0;     // stored entries (slices padded to their widest row)
+    int nslices = 0;
+    int *slice_ptr = nullptr;
+    int *cols = nullptr;
+    float2 *vals32 = nullptr;
+    double2 *vals64 = nullptr;
+    int device = 0;
+    SellMatrix view32() const { return SellMatrix{n, nslices, slice_ptr, cols, vals32, nnz}; }
+    SellMatrix view64() const { return SellMatrix{n, nslices, slice_ptr, cols, vals64, nnz}; }
+    size_t bytes() const;
+};
+// Builds the SELL-32 form of a CSR matrix (values interleaved re,im doubles).
+int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, const double *vals_ri, bool want32,
+                  bool want64, cudaStream_t st);
+void sell_free(DeviceSell &s);
+
+// Operator seen by an engine of precision R.
+template <class R> struct Operator {
+    using C = typename CT<R>::t;
+    enum Kind { NONE, HOOK, SELL, DENSE } kind = NONE;
+    void (*hook)(void) = nullptr;   // reference hook: applies A in place to `ext`
+    C *ext = nullptr;
+    SellMatrix sell{};
+    const C *dense = nullptr;      // column-major n x n
+};
+
+struct SolveStats {
+    int cycles = 0;
+    int its = 0;             // reference convention: cycles - 1
+    long matvecs = 0;
+    double rel_res = 0;      // what solverDMR returns
+    double true_rel_res = -1; // FP64 ||b - A x|| / ||b|| when measured
+    int status = GDMR_OK;
+    int breakdowns = 0;
+    double latency_ms = 0;
+};
+
+template <class R> class Engine {
+  public:
+    using C = typename CT<R>::t;
+    Engine() = default;
+    ~Engine();
+    Engine(const Engine &) = delete;
+    Engine &operator=(const Engine &) = delete;
+
+    // Allocates every buffer for `capacity` systems of size n, basis m, deflation k.
+    int init(int n, int m, int k, int capacity, int device);
+    void release();
+    bool ready() const { return n_ > 0; }
+
+    Operator<R> op;
+    cudaStream_t stream = nullptr;
+    bool compat_eye = true;     // reproduce the reference's breakdown identity tail (gDMR.cu:2275)
+
+    // Reference semantics on system 0 (solverDMR): b, x are device vectors of precision R;
+    // x holds x0 on entry and the solution on exit.  With a hook operator x must be the hook's
+    // buffer (op.ext).  Returns the reference's return value.
+    double solve_reference(int mode, const C *b, C *x, double tol, int mat_rank, SolveStats *stats);
+
+    // FP64-refined batched form, driven one restart cycle at a time so that
+    // systems can join and leave between cycles (continuous batching).  Each
+    // slot holds b and x in complex128 on the device; every cycle starts from
+    // the true FP64 residual b - A64 x, runs one DMR cycle in precision R on
+    // the unit residual, and adds the correction to x in FP64.  The SELL
+    // operator in `op` is the inner operator; A64 the FP64 one.
+    int refine_setup(const SellMatrix &A64);
+    // Copies b (and x0, or zeros when null) from device memory into a free slot.
+    int refine_admit(int slot, const double2 *b, const double2 *x0, double tol, int max_cycles);
+    // Residual check for every active slot, then one cycle for those not done.
+    // Slots that finished (converged, cycle cap, non-finite) are appended to `done`.
+    int refine_cycle(std::vector<int> *done);
+    double2 *slot_x(int s) const { return x64_ + (size_t)s * n_; }
+    double2 *slot_b(int s) const { return b64_ + (size_t)s * n_; }
+    const SolveStats &slot_stats(int s) const { return slot_[s].stats; }
+    int active_count() const { return (int)act_h_.size(); }
+    int capacity() const { return cap_; }
+    // FP64 relative residual ||b_s - A64 x_s|| / ||b_s|| of arbitrary device pairs (s < capacity slots used as scratch).
+    int true_residual(int count, const double2 *b, const double2 *x, double *relres);
+
+    // Deflation basis (k x n, vector-contiguous) between host and device, precision R.
+    int import_deflation(const C *host);
+    int export_deflation(C *host);
+    bool has_deflation() const { return have_z_; }
+    void drop_deflation() { have_z_ = false; }
+    // The reference keeps its stagnation counter across solves (gDMR.cu:2646-2655); reset on init.
+    int flag_count() const { return flag_count_; }
+
+    int n() const { return n_; }
+    int m() const { return m_; }
+    int k() const { return k_; }
+    size_t device_bytes() const { return bytes_; }
+
+  private:
+    int n_ = 0, m_ = 0, k_ = 0, cap_ = 0, dev_ = 0;
+    size_t bytes_ = 0;
+    bool have_z_ = false;
+    int flag_count_ = 0;        // reference kryFlagCountDMR (system 0)
+    // device buffers
+    C *V_ = nullptr, *W_ = nullptr, *Z_ = nullptr, *Znew_ = nullptr;
+    C *R_ = nullptr, *X_ = nullptr, *Y_ = nullptr, *T_ = nullptr, *AZ_ = nullptr;
+    double2 *H_ = nullptr, *Hd_ = nullptr, *coef_ = nullptr, *coefD_ = nullptr, *g_ = nullptr, *y_ = nullptr,
+            *t_ = nullptr;
+    double2 *vs_ = nullptr, *svdwork_ = nullptr, *partials_ = nullptr, *r64_ = nullptr;
+    double *sigma_ = nullptr, *znorm2_ = nullptr;
+    int *sweeps_ = nullptr;
+    unsigned *tickets_ = nullptr;
+    SysState *state_ = nullptr, *hstate_ = nullptr;
+    int *act_ = nullptr;        // active list (device)
+    int *ident_ = nullptr;      // 0..cap (device), ident_[cap] is the deflation pseudo-system
+    std::vector<int> act_h_;
+    std::vector<void *> allocs_;
+    // refined form
+    struct Slot {
+        bool active = false;
+        int loop_flag = 0, flag_count = 0, max_cycles = 0;
+        double bnorm = 0, tol = 0;
+        SolveStats stats;
+    };
+    std::vector<Slot> slot_;
+    SellMatrix A64_{};
+    double2 *b64_ = nullptr, *x64_ = nullptr;
+    int kk_prev_ = 0;
+
+    size_t strideV() const { return (size_t)(m_ + 1) * n_; }
+    size_t strideH() const { return (size_t)(m_ + 1) * m_; }
+    size_t strideC() const { return (size_t)(m_ + 1); }
+    int qmax() const { return m_ + 1; }
+    C *Vs(int s) const { return V_ + (size_t)s * strideV(); }
+
+    int alloc(void **p, size_t bytes);
+    int set_active(const std::vector<int> &act);
+    int read_state(int count);
+    void apply(const C *x0, size_t strideX, C *y0, size_t strideY, int nsys, long *matvecs);
+    C *op_out(int s) const { return op.kind == Operator<R>::HOOK ? op.ext : Y_ + (size_t)s * n_; }
+    size_t op_out_stride() const { return op.kind == Operator<R>::HOOK ? 0 : (size_t)n_; }
+    // One restart cycle over the active systems with deflation dimension kk; lead
+    // selects the system whose Hessenberg updates the shared deflation space.
+    int run_cycle(int kk, int nsys, int lead, double tol, long *matvecs);
+};
+
+}  // namespace gdmr

@@ -1,0 +1,1161 @@
+// Device kernels of the GB300 DMR restart cycle.  See gdmr_kernels.cuh.
+#include "gdmr_kernels.cuh"
+
+#include <math.h>
+
+#include <atomic>
+#include <mutex>
+#include <vector>
+
+namespace gdmr {
+
+namespace {
+
+constexpr int NT = 256;            // threads per CTA of the streaming kernels
+constexpr int NW = NT / 32;
+constexpr int QMAX = 168;          // max coefficients per projection (basisDim <= 160 -> m+1 <= 161)
+
+template <class C> __device__ __forceinline__ C from_d(double2 a);
+template <> __device__ __forceinline__ float2 from_d<float2>(double2 a) { return make_float2((float)a.x, (float)a.y); }
+template <> __device__ __forceinline__ double2 from_d<double2>(double2 a) { return a; }
+
+template <class C> __device__ __forceinline__ C czero() { C z; z.x = 0; z.y = 0; return z; }
+
+// acc += a * b
+template <class C> __device__ __forceinline__ void cfma(C &acc, C a, C b) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(a.y, b.x, acc.y);
+}
+// acc -= a * b
+template <class C> __device__ __forceinline__ void cfms(C &acc, C a, C b) {
+    acc.x = fma(-a.x, b.x, acc.x);
+    acc.x = fma(a.y, b.y, acc.x);
+    acc.y = fma(-a.x, b.y, acc.y);
+    acc.y = fma(-a.y, b.x, acc.y);
+}
+// acc += conj(a) * b
+template <class C> __device__ __forceinline__ void cdotacc(C &acc, C a, C b) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(-a.y, b.x, acc.y);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum of NV doubles per thread; result valid in thread 0.
+template <int NV> __device__ __forceinline__ void block_sum(double (&v)[NV], double (*red)[NW]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] = warp_sum(v[j]);
+    if (lane == 0)
+#pragma unroll
+        for (int j = 0; j < NV; ++j) red[j][warp] = v[j];
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+            double s = 0;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) s += red[j][w];
+            v[j] = s;
+        }
+}
+
+// Last-CTA-done protocol: returns true in every thread of the CTA that arrived last.
+__device__ __forceinline__ bool arrive_last(unsigned *ticket) {
+    __shared__ unsigned s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(ticket, 1u) == gridDim.x - 1) ? 1u : 0u;
+    __syncthreads();
+    if (s_last) __threadfence();
+    return s_last != 0;
+}
+
+// Sums NV partial vectors of length G (layout part[j*G + g]) with the whole CTA;
+// result valid in thread 0.  Fixed order: deterministic for a given grid.
+template <int NV> __device__ __forceinline__ void sum_partials(const double *part, int G, double (&out)[NV], double (*red)[NW]) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+        double s = 0;
+        for (int g = threadIdx.x; g < G; g += NT) s += __ldcg(part + (size_t)j * G + g);
+        out[j] = s;
+    }
+    block_sum<NV>(out, red);
+}
+
+int g_num_sms = 0;
+
+int num_sms() {
+    if (g_num_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || g_num_sms <= 0)
+            g_num_sms = 152;
+    }
+    return g_num_sms;
+}
+
+template <class R> __host__ __device__ constexpr int ept() { return sizeof(R) == 4 ? 8 : 4; }
+
+template <class R> int red_grid(int n, int nsys) {
+    const int ch = NT * ept<R>();
+    int chunks = (n + ch - 1) / ch;
+    int target = (num_sms() * 2 + nsys - 1) / (nsys > 0 ? nsys : 1);
+    if (target < 1) target = 1;
+    return chunks < target ? (chunks > 0 ? chunks : 1) : target;
+}
+
+// ----------------------------------------------------------------- finishing
+__device__ void run_finish(const FinishArgs &f, int s, SysState &st, double n2, double cre, double cim) {
+    st.nrm2 = n2;
+    st.cross_re = cre;
+    st.cross_im = cim;
+    const double nrm = sqrt(n2);
+    if (!isfinite(nrm)) st.bad = 1;
+    switch (f.mode) {
+    case FIN_KRYLOV: {
+        double2 *H = f.H + (size_t)s * f.strideH;
+        const double2 *c = f.coef + (size_t)s * f.strideC;
+        for (int p = 0; p < f.nco; ++p) H[(size_t)f.col * f.ldH + p] = c[p];
+        const int j = f.col - f.kk + 1;
+        if (nrm < f.tol) {   // absolute breakdown threshold, gDMR.cu:2256
+            st.broken = j;
+            st.alpha = 0.0;
+            for (int cc = f.compat_eye ? j : f.kk + j; cc < f.m; ++cc) H[(size_t)cc * f.ldH + cc] = make_double2(1.0, 0.0);
+        } else {
+            st.alpha = 1.0 / nrm;
+            H[(size_t)f.col * f.ldH + f.col + 1] = make_double2(cre / nrm, cim / nrm);
+        }
+        break;
+    }
+    case FIN_DEFLATION: {
+        double2 *H = f.H;
+        const double2 *c = f.coef;
+        for (int p = 0; p < f.nco; ++p) H[(size_t)f.col * f.ldH + p] = c[p];
+        st.alpha = 1.0 / nrm;
+        H[(size_t)f.col * f.ldH + f.col] = make_double2(cre / nrm, cim / nrm);
+        break;
+    }
+    case FIN_UNIT:
+        st.alpha = 1.0 / nrm;
+        break;
+    case FIN_RESIDUAL:
+        st.rho = nrm;
+        st.alpha = 1.0 / nrm;
+        st.rho_abs = st.rho_abs * nrm;
+        break;
+    default:
+        break;
+    }
+}
+
+// ----------------------------------------------------------------- multi-dot
+// coef_s[p] = <B_p, w_s> for B = [segA (qa vectors) | segB_s (qb vectors)].
+template <class R, int PU>
+__global__ void __launch_bounds__(NT) k_mdot(int n, const typename CT<R>::t *__restrict__ segA, int qa,
+                                             const typename CT<R>::t *__restrict__ segB0, size_t strideB, int qb,
+                                             const typename CT<R>::t *__restrict__ w0, size_t strideW,
+                                             const int *__restrict__ act, double2 *__restrict__ partials, int qmax,
+                                             unsigned *tickets, double2 *__restrict__ coef0, size_t strideC,
+                                             SysState *state, int skip_broken) {
+    using C = typename CT<R>::t;
+    constexpr int EPT = ept<R>();
+    const int slot = blockIdx.y, s = act[slot];
+    if (skip_broken && state[s].broken) return;
+    const C *segB = segB0 + (size_t)s * strideB;
+    const C *w = w0 + (size_t)s * strideW;
+    const int q = qa + qb, G = gridDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __shared__ double2 wsum[NW][QMAX];
+    __shared__ double red[2][NW];
+    for (int i = tid; i < NW * QMAX; i += NT) wsum[i / QMAX][i % QMAX] = make_double2(0, 0);
+    __syncthreads();
+    const long CH = (long)NT * EPT;
+    for (long c0 = (long)blockIdx.x * CH; c0 < n; c0 += (long)G * CH) {
+        C wv[EPT];
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            long i = c0 + tid + (long)e * NT;
+            wv[e] = i < n ? w[i] : czero<C>();
+        }
+        for (int p0 = 0; p0 < q; p0 += PU) {
+            C vv[PU][EPT];
+#pragma unroll
+            for (int u = 0; u < PU; ++u) {
+                const int p = p0 + u;
+                const C *vp = p < qa ? segA + (size_t)p * n : segB + (size_t)(p - qa) * n;
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) {
+                    long i = c0 + tid + (long)e * NT;
+                    vv[u][e] = (p < q && i < n) ? vp[i] : czero<C>();
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < PU; ++u) {
+                C a = czero<C>();
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) cdotacc(a, vv[u][e], wv[e]);
+                double re = warp_sum((double)a.x), im = warp_sum((double)a.y);
+                if (lane == 0 && p0 + u < q) {
+                    wsum[warp][p0 + u].x += re;
+                    wsum[warp][p0 + u].y += im;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    double *part = (double *)partials + (size_t)slot * qmax * 2 * G;   // [p][re|im][G]
+    for (int p = tid; p < q; p += NT) {
+        double re = 0, im = 0;
+#pragma unroll
+        for (int ww = 0; ww < NW; ++ww) { re += wsum[ww][p].x; im += wsum[ww][p].y; }
+        double *pp = part + (size_t)p * 2 * G;
+        pp[blockIdx.x] = re;
+        pp[G + blockIdx.x] = im;
+    }
+    if (!arrive_last(&tickets[slot])) return;
+    // one warp per coefficient, lanes stride over the G partials
+    double2 *coef = coef0 + (size_t)s * strideC;
+    for (int p = warp; p < q; p += NW) {
+        const double *pp = part + (size_t)p * 2 * G;
+        double re = 0, im = 0;
+        for (int g = lane; g < G; g += 32) { re += __ldcg(pp + g); im += __ldcg(pp + G + g); }
+        re = warp_sum(re);
+        im = warp_sum(im);
+        if (lane == 0) coef[p] = make_double2(re, im);
+    }
+    if (tid == 0) tickets[slot] = 0;
+    (void)red;
+}
+
+// ----------------------------------------------------------------- update + norms
+template <class R, int PU>
+__global__ void __launch_bounds__(NT) k_update(int n, const typename CT<R>::t *__restrict__ segA, int qa,
+                                               const typename CT<R>::t *__restrict__ segB0, size_t strideB, int qb,
+                                               const typename CT<R>::t *__restrict__ w0, size_t strideW,
+                                               typename CT<R>::t *__restrict__ out0, size_t strideO,
+                                               const int *__restrict__ act, const double2 *__restrict__ coef0,
+                                               size_t strideC, double2 *__restrict__ partials, unsigned *tickets,
+                                               SysState *state, FinishArgs fin, int skip_broken) {
+    using C = typename CT<R>::t;
+    constexpr int EPT = ept<R>();
+    const int slot = blockIdx.y, s = act[slot];
+    if (skip_broken && state[s].broken) return;
+    const C *segB = segB0 + (size_t)s * strideB;
+    const C *w = w0 + (size_t)s * strideW;
+    C *out = out0 + (size_t)s * strideO;
+    const int q = qa + qb, G = gridDim.x, tid = threadIdx.x;
+    __shared__ C cs[QMAX];
+    __shared__ double red[3][NW];
+    const double2 *coef = coef0 + (size_t)s * strideC;
+    for (int p = tid; p < q; p += NT) cs[p] = from_d<C>(coef[p]);
+    __syncthreads();
+    double n2 = 0, cre = 0, cim = 0;
+    const long CH = (long)NT * EPT;
+    for (long c0 = (long)blockIdx.x * CH; c0 < n; c0 += (long)G * CH) {
+        C acc[EPT], org[EPT];
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            long i = c0 + tid + (long)e * NT;
+            org[e] = i < n ? w[i] : czero<C>();
+            acc[e] = org[e];
+        }
+        for (int p0 = 0; p0 < q; p0 += PU) {
+            C vv[PU][EPT];
+#pragma unroll
+            for (int u = 0; u < PU; ++u) {
+                const int p = p0 + u;
+                const C *vp = p < qa ? segA + (size_t)p * n : segB + (size_t)(p - qa) * n;
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) {
+                    long i = c0 + tid + (long)e * NT;
+                    vv[u][e] = (p < q && i < n) ? vp[i] : czero<C>();
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < PU; ++u) {
+                if (p0 + u < q) {
+                    const C c = cs[p0 + u];
+#pragma unroll
+                    for (int e = 0; e < EPT; ++e) cfms(acc[e], c, vv[u][e]);
+                }
+            }
+        }
+        C ln = czero<C>(), lc = czero<C>();
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            long i = c0 + tid + (long)e * NT;
+            if (i < n) out[i] = acc[e];
+            cdotacc(ln, acc[e], acc[e]);
+            cdotacc(lc, acc[e], org[e]);
+        }
+        n2 += ln.x;
+        cre += lc.x;
+        cim += lc.y;
+    }
+    double v[3] = {n2, cre, cim};
+    block_sum<3>(v, red);
+    double *part = (double *)partials + (size_t)slot * 3 * G;
+    if (tid == 0) {
+        part[blockIdx.x] = v[0];
+        part[G + blockIdx.x] = v[1];
+        part[2 * G + blockIdx.x] = v[2];
+    }
+    if (!arrive_last(&tickets[slot])) return;
+    double tot[3];
+    __syncthreads();
+    sum_partials<3>(part, G, tot, red);
+    if (tid == 0) {
+        run_finish(fin, s, state[s], tot[0], tot[1], tot[2]);
+        tickets[slot] = 0;
+    }
+}
+
+// ----------------------------------------------------------------- scale
+template <class R>
+__global__ void __launch_bounds__(NT) k_scale(int n, const typename CT<R>::t *__restrict__ in0, size_t strideI,
+                                              typename CT<R>::t *__restrict__ o10, size_t strideO1,
+                                              typename CT<R>::t *__restrict__ o20, size_t strideO2,
+                                              const int *__restrict__ act, const SysState *__restrict__ state,
+                                              int honour_broken) {
+    using C = typename CT<R>::t;
+    const int s = act[blockIdx.y];
+    const bool zero = honour_broken && state[s].broken;
+    const R a = (R)state[s].alpha;
+    const C *in = in0 + (size_t)s * strideI;
+    C *o1 = o10 + (size_t)s * strideO1;
+    C *o2 = o20 ? o20 + (size_t)s * strideO2 : nullptr;
+    for (long i = (long)blockIdx.x * NT + threadIdx.x; i < n; i += (long)gridDim.x * NT) {
+        C v = zero ? czero<C>() : in[i];
+        v.x *= a;
+        v.y *= a;
+        if (zero) v = czero<C>();
+        o1[i] = v;
+        if (o2) o2[i] = v;
+    }
+}
+
+// ----------------------------------------------------------------- cycle-end combination
+template <class R>
+__global__ void __launch_bounds__(NT) k_combine(int n, int kk, int m, const typename CT<R>::t *__restrict__ W,
+                                                const typename CT<R>::t *__restrict__ Z,
+                                                const typename CT<R>::t *__restrict__ V0, size_t strideV,
+                                                typename CT<R>::t *__restrict__ r0, size_t strideR,
+                                                typename CT<R>::t *__restrict__ x0, size_t strideX,
+                                                const double2 *__restrict__ t0, const double2 *__restrict__ y0,
+                                                size_t strideC, const int *__restrict__ act,
+                                                double2 *__restrict__ partials, unsigned *tickets, SysState *state) {
+    using C = typename CT<R>::t;
+    constexpr int EPT = ept<R>();
+    const int slot = blockIdx.y, s = act[slot];
+    const C *V = V0 + (size_t)s * strideV;
+    C *r = r0 + (size_t)s * strideR;
+    C *x = x0 + (size_t)s * strideX;
+    const int G = gridDim.x, tid = threadIdx.x;
+    __shared__ C ts[QMAX], ys[QMAX];
+    __shared__ double red[1][NW];
+    const R ra = (R)state[s].rho_abs;
+    for (int p = tid; p <= m; p += NT) {
+        ts[p] = from_d<C>(t0[(size_t)s * strideC + p]);
+        C yy = p < m ? from_d<C>(y0[(size_t)s * strideC + p]) : czero<C>();
+        yy.x *= ra;
+        yy.y *= ra;
+        ys[p] = yy;
+    }
+    __syncthreads();
+    double n2 = 0;
+    const long CH = (long)NT * EPT;
+    for (long c0 = (long)blockIdx.x * CH; c0 < n; c0 += (long)G * CH) {
+        C ra_[EPT], xa[EPT];
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            long i = c0 + tid + (long)e * NT;
+            ra_[e] = i < n ? r[i] : czero<C>();
+            xa[e] = i < n ? x[i] : czero<C>();
+        }
+        for (int p = 0; p < kk; ++p) {
+            const C tc = ts[p], yc = ys[p];
+            const C *wp = W + (size_t)p * n;
+            const C *zp = Z + (size_t)p * n;
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) {
+                long i = c0 + tid + (long)e * NT;
+                if (i < n) {
+                    cfms(ra_[e], tc, wp[i]);
+                    cfma(xa[e], yc, zp[i]);
+                }
+            }
+        }
+        for (int p = 0; p <= m - kk; ++p) {
+            const C tc = ts[kk + p], yc = ys[kk + p];   // ys[m] = 0: the last Krylov vector is target-side only
+            const C *vp = V + (size_t)p * n;
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) {
+                long i = c0 + tid + (long)e * NT;
+                if (i < n) {
+                    const C vv = vp[i];
+                    cfms(ra_[e], tc, vv);
+                    cfma(xa[e], yc, vv);
+                }
+            }
+        }
+        C ln = czero<C>();
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            long i = c0 + tid + (long)e * NT;
+            if (i < n) {
+                r[i] = ra_[e];
+                x[i] = xa[e];
+            }
+            cdotacc(ln, ra_[e], ra_[e]);
+        }
+        n2 += ln.x;
+    }
+    double v[1] = {n2};
+    block_sum<1>(v, red);
+    double *part = (double *)partials + (size_t)slot * G;
+    if (tid == 0) part[blockIdx.x] = v[0];
+    if (!arrive_last(&tickets[slot])) return;
+    double tot[1];
+    __syncthreads();
+    sum_partials<1>(part, G, tot, red);
+    if (tid == 0) {
+        FinishArgs f{};
+        f.mode = FIN_RESIDUAL;
+        run_finish(f, s, state[s], tot[0], 0, 0);
+        tickets[slot] = 0;
+    }
+}
+
+// ----------------------------------------------------------------- deflation-space update
+template <class R, int KB>
+__global__ void __launch_bounds__(NT) k_zupdate(int n, int kk, int m, int k, int t0, const typename CT<R>::t *__restrict__ Z,
+                                                const typename CT<R>::t *__restrict__ V,
+                                                const double2 *__restrict__ vs, typename CT<R>::t *__restrict__ Znew,
+                                                double2 *__restrict__ partials, unsigned *ticket, double *znorm2) {
+    using C = typename CT<R>::t;
+    extern __shared__ unsigned char smraw[];
+    C *cs = reinterpret_cast<C *>(smraw);            // m x KB coefficients
+    __shared__ double red[KB][NW];
+    const int nt = min(KB, k - t0), G = gridDim.x, tid = threadIdx.x;
+    for (int i = tid; i < m * KB; i += NT) {
+        int p = i / KB, t = i % KB;
+        cs[i] = t < nt ? from_d<C>(vs[(size_t)(t0 + t) * m + p]) : czero<C>();
+    }
+    __syncthreads();
+    double nrm[KB];
+#pragma unroll
+    for (int t = 0; t < KB; ++t) nrm[t] = 0;
+    for (long i = (long)blockIdx.x * NT + tid; i < n; i += (long)G * NT) {
+        C acc[KB];
+#pragma unroll
+        for (int t = 0; t < KB; ++t) acc[t] = czero<C>();
+        for (int p = 0; p < m; ++p) {
+            const C b = p < kk ? Z[(size_t)p * n + i] : V[(size_t)(p - kk) * n + i];
+#pragma unroll
+            for (int t = 0; t < KB; ++t) cfma(acc[t], cs[p * KB + t], b);
+        }
+#pragma unroll
+        for (int t = 0; t < KB; ++t) {
+            if (t < nt) Znew[(size_t)(t0 + t) * n + i] = acc[t];
+            nrm[t] += (double)acc[t].x * acc[t].x + (double)acc[t].y * acc[t].y;
+        }
+    }
+    block_sum<KB>(nrm, red);
+    double *part = (double *)partials;
+    if (tid == 0)
+        for (int t = 0; t < nt; ++t) part[(size_t)t * G + blockIdx.x] = nrm[t];
+    if (!arrive_last(ticket)) return;
+    __syncthreads();
+    double tot[KB];
+#pragma unroll
+    for (int t = 0; t < KB; ++t) {
+        double sacc = 0;
+        if (t < nt)
+            for (int g = tid; g < G; g += NT) sacc += __ldcg(part + (size_t)t * G + g);
+        tot[t] = sacc;
+    }
+    block_sum<KB>(tot, red);
+    if (tid == 0) {
+        for (int t = 0; t < nt; ++t) znorm2[t0 + t] = tot[t];
+        *ticket = 0;
+    }
+}
+
+template <class R>
+__global__ void __launch_bounds__(NT) k_znormalise(int n, const typename CT<R>::t *__restrict__ Znew,
+                                                   const double *__restrict__ znorm2, typename CT<R>::t *__restrict__ Z) {
+    using C = typename CT<R>::t;
+    const int t = blockIdx.y;
+    const R a = (R)(1.0 / sqrt(znorm2[t]));
+    for (long i = (long)blockIdx.x * NT + threadIdx.x; i < n; i += (long)gridDim.x * NT) {
+        C v = Znew[(size_t)t * n + i];
+        v.x *= a;
+        v.y *= a;
+        Z[(size_t)t * n + i] = v;
+    }
+}
+
+// ----------------------------------------------------------------- least squares (FP64 Givens)
+// H is upper Hessenberg, (m+1) x m, ld m+1.  Column c is stored packed in shared
+// memory at off(c) = c(c+3)/2, rows 0..c+1.
+__device__ __forceinline__ int hoff(int c) { return c * (c + 3) / 2; }
+
+__global__ void __launch_bounds__(128) k_ls(int m, const double2 *__restrict__ H0, size_t strideH,
+                                            const double2 *__restrict__ g0, double2 *__restrict__ y0,
+                                            double2 *__restrict__ t0, size_t strideC, const int *__restrict__ act) {
+    extern __shared__ double2 sm[];
+    const int s = act[blockIdx.x], tid = threadIdx.x, ld = m + 1;
+    const double2 *H = H0 + (size_t)s * strideH;
+    double2 *Hp = sm;                         // packed Hessenberg
+    double2 *gg = sm + hoff(m);               // m+1
+    double2 *yy = gg + (m + 1);               // m
+    double *cs = (double *)(yy + m);          // m cosines
+    double2 *sn = (double2 *)(cs + m + (m & 1));   // m sines (keep 16-byte alignment)
+    for (int c = 0; c < m; ++c)
+        for (int r = tid; r <= c + 1 && r <= m; r += blockDim.x) Hp[hoff(c) + r] = H[(size_t)c * ld + r];
+    for (int r = tid; r <= m; r += blockDim.x) gg[r] = g0[(size_t)s * strideC + r];
+    __syncthreads();
+    for (int i = 0; i < m; ++i) {
+        if (tid == 0) {
+            double2 a = Hp[hoff(i) + i], b = Hp[hoff(i) + i + 1];
+            double aa = hypot(a.x, a.y), bb = hypot(b.x, b.y);
+            double c, rr;
+            double2 sv, ph;
+            if (bb == 0.0) {
+                c = 1.0; sv = make_double2(0, 0); rr = aa; ph = aa > 0 ? make_double2(a.x / aa, a.y / aa) : make_double2(1, 0);
+            } else if (aa == 0.0) {
+                c = 0.0; sv = make_double2(b.x / bb, -b.y / bb); rr = bb; ph = make_double2(1, 0);
+            } else {
+                double rho = hypot(aa, bb);
+                ph = make_double2(a.x / aa, a.y / aa);
+                c = aa / rho;
+                // s = ph * conj(b) / rho
+                sv = make_double2((ph.x * b.x + ph.y * b.y) / rho, (ph.y * b.x - ph.x * b.y) / rho);
+                rr = rho;
+            }
+            cs[i] = c;
+            sn[i] = sv;
+            Hp[hoff(i) + i] = make_double2(ph.x * rr, ph.y * rr);
+            Hp[hoff(i) + i + 1] = make_double2(0, 0);
+            double2 g1 = gg[i], g2 = gg[i + 1];
+            // [c s; -conj(s) c] [g1; g2]
+            gg[i] = make_double2(c * g1.x + sv.x * g2.x - sv.y * g2.y, c * g1.y + sv.x * g2.y + sv.y * g2.x);
+            gg[i + 1] = make_double2(-(sv.x * g1.x + sv.y * g1.y) + c * g2.x, -(sv.x * g1.y - sv.y * g1.x) + c * g2.y);
+        }
+        __syncthreads();
+        const double c = cs[i];
+        const double2 sv = sn[i];
+        for (int col = i + 1 + tid; col < m; col += blockDim.x) {
+            double2 h1 = Hp[hoff(col) + i], h2 = Hp[hoff(col) + i + 1];
+            Hp[hoff(col) + i] = make_double2(c * h1.x + sv.x * h2.x - sv.y * h2.y, c * h1.y + sv.x * h2.y + sv.y * h2.x);
+            Hp[hoff(col) + i + 1] = make_double2(-(sv.x * h1.x + sv.y * h1.y) + c * h2.x, -(sv.x * h1.y - sv.y * h1.x) + c * h2.y);
+        }
+        __syncthreads();
+    }
+    // back substitution R y = g (R = upper m x m part); zero pivots give zero components
+    for (int c = m - 1; c >= 0; --c) {
+        if (tid == 0) {
+            double2 d = Hp[hoff(c) + c], g = gg[c];
+            double dd = d.x * d.x + d.y * d.y;
+            yy[c] = dd > 0 ? make_double2((g.x * d.x + g.y * d.y) / dd, (g.y * d.x - g.x * d.y) / dd) : make_double2(0, 0);
+        }
+        __syncthreads();
+        const double2 yc = yy[c];
+        for (int r = tid; r < c; r += blockDim.x) {
+            double2 h = Hp[hoff(c) + r];
+            gg[r].x -= h.x * yc.x - h.y * yc.y;
+            gg[r].y -= h.x * yc.y + h.y * yc.x;
+        }
+        __syncthreads();
+    }
+    for (int c = tid; c < m; c += blockDim.x) y0[(size_t)s * strideC + c] = yy[c];
+    // t = H y with the original H
+    for (int r = tid; r <= m; r += blockDim.x) {
+        double2 acc = make_double2(0, 0);
+        for (int c = (r > 0 ? r - 1 : 0); c < m; ++c) {
+            double2 h = H[(size_t)c * ld + r], yc = yy[c];
+            acc.x += h.x * yc.x - h.y * yc.y;
+            acc.y += h.x * yc.y + h.y * yc.x;
+        }
+        t0[(size_t)s * strideC + r] = acc;
+    }
+}
+
+// ----------------------------------------------------------------- SVD (FP64 one-sided Jacobi)
+// A: (m+1) x m working copy (ld m+1), V: m x m, both in shared memory when they
+// fit, else in global scratch.  Round-robin ("circle") ordering of disjoint pairs,
+// one warp per pair.  Column norms are kept incrementally.
+__global__ void __launch_bounds__(512) k_svd(int m, int k, const double2 *__restrict__ H, double2 *__restrict__ vs,
+                                             double *__restrict__ sigma, double2 *__restrict__ gwork, int use_smem,
+                                             int *sweeps_out) {
+    extern __shared__ double2 sm[];
+    const int rows = m + 1, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    double2 *A = use_smem ? sm : gwork;
+    double2 *V = A + (size_t)rows * m;
+    __shared__ double nrm[168];
+    __shared__ int perm[168];
+    __shared__ int s_rot;
+    for (int i = tid; i < rows * m; i += blockDim.x) A[i] = H[i];
+    for (int i = tid; i < m * m; i += blockDim.x) V[i] = make_double2((i % m) == (i / m) ? 1.0 : 0.0, 0.0);
+    __syncthreads();
+    for (int c = warp; c < m; c += nwarps) {
+        double a = 0;
+        for (int r = lane; r < rows; r += 32) { double2 v = A[(size_t)c * rows + r]; a += v.x * v.x + v.y * v.y; }
+        a = warp_sum(a);
+        if (lane == 0) nrm[c] = a;
+    }
+    const int mm = m + (m & 1);          // even number of slots (slot m is a dummy when m is odd)
+    for (int i = tid; i < mm; i += blockDim.x) perm[i] = i;
+    __syncthreads();
+    const double eps = 1e-15;
+    int sweep = 0;
+    for (; sweep < 60; ++sweep) {
+        if (tid == 0) s_rot = 0;
+        __syncthreads();
+        for (int round = 0; round < mm - 1; ++round) {
+            for (int pi = warp; pi < mm / 2; pi += nwarps) {
+                int p = perm[pi], q = perm[mm - 1 - pi];
+                if (p >= m || q >= m) continue;
+                if (p > q) { int t = p; p = q; q = t; }
+                double gr = 0, gi = 0;
+                for (int r = lane; r < rows; r += 32) {
+                    double2 ap = A[(size_t)p * rows + r], aq = A[(size_t)q * rows + r];
+                    gr += ap.x * aq.x + ap.y * aq.y;
+                    gi += ap.x * aq.y - ap.y * aq.x;
+                }
+                gr = warp_sum(gr);
+                gi = warp_sum(gi);
+                const double a = nrm[p], b = nrm[q];
+                const double ag = hypot(gr, gi);
+                if (ag == 0.0 || ag <= eps * sqrt(a * b)) continue;
+                if (lane == 0) s_rot = 1;
+                const double phr = gr / ag, phi = -gi / ag;    // e^{-i phi}
+                const double zeta = (b - a) / (2.0 * ag);
+                const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                const double c = 1.0 / sqrt(1.0 + t * t), sn = c * t;
+                for (int r = lane; r < rows; r += 32) {
+                    double2 ap = A[(size_t)p * rows + r], aq0 = A[(size_t)q * rows + r];
+                    double2 aq = make_double2(aq0.x * phr - aq0.y * phi, aq0.x * phi + aq0.y * phr);
+                    A[(size_t)p * rows + r] = make_double2(c * ap.x - sn * aq.x, c * ap.y - sn * aq.y);
+                    A[(size_t)q * rows + r] = make_double2(sn * ap.x + c * aq.x, sn * ap.y + c * aq.y);
+                }
+                for (int r = lane; r < m; r += 32) {
+                    double2 vp = V[(size_t)p * m + r], vq0 = V[(size_t)q * m + r];
+                    double2 vq = make_double2(vq0.x * phr - vq0.y * phi, vq0.x * phi + vq0.y * phr);
+                    V[(size_t)p * m + r] = make_double2(c * vp.x - sn * vq.x, c * vp.y - sn * vq.y);
+                    V[(size_t)q * m + r] = make_double2(sn * vp.x + c * vq.x, sn * vp.y + c * vq.y);
+                }
+                if (lane == 0) {
+                    nrm[p] = a - t * ag;
+                    nrm[q] = b + t * ag;
+                }
+            }
+            __syncthreads();
+            // rotate the circle: slot 0 fixed, others shift by one
+            if (tid == 0) {
+                int last = perm[mm - 1];
+                for (int i = mm - 1; i > 1; --i) perm[i] = perm[i - 1];
+                perm[1] = last;
+            }
+            __syncthreads();
+        }
+        // refresh norms from the columns (the incremental update drifts)
+        for (int c = warp; c < m; c += nwarps) {
+            double a = 0;
+            for (int r = lane; r < rows; r += 32) { double2 v = A[(size_t)c * rows + r]; a += v.x * v.x + v.y * v.y; }
+            a = warp_sum(a);
+            if (lane == 0) nrm[c] = a;
+        }
+        __syncthreads();
+        if (!s_rot) break;
+        __syncthreads();
+    }
+    // rank in descending order (ties broken by column index)
+    for (int c = tid; c < m; c += blockDim.x) {
+        const double sc = nrm[c];
+        int rank = 0;
+        for (int c2 = 0; c2 < m; ++c2) {
+            const double s2 = nrm[c2];
+            rank += (s2 > sc) || (s2 == sc && c2 < c);
+        }
+        sigma[rank] = sqrt(sc);
+        const int t = rank - (m - k);
+        if (t >= 0)
+            for (int r = 0; r < m; ++r) vs[(size_t)t * m + r] = V[(size_t)c * m + r];
+    }
+    if (tid == 0 && sweeps_out) *sweeps_out = sweep + 1;
+}
+
+// ----------------------------------------------------------------- SELL-32 SpMM
+template <class R, int SG>
+__global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slice_ptr, const int *__restrict__ cols,
+                                             const typename CT<R>::t *__restrict__ vals,
+                                             const typename CT<R>::t *__restrict__ x0, size_t strideX,
+                                             typename CT<R>::t *__restrict__ y0, size_t strideY,
+                                             const int *__restrict__ act, int nsys) {
+    using C = typename CT<R>::t;
+    const int row = blockIdx.x * NT + threadIdx.x;
+    if (row >= n) return;
+    const int slice = row >> 5, lane = row & 31;
+    const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
+    const int g0 = blockIdx.y * SG;
+    for (int g = 0; g < SG && g0 + g < nsys; ++g) {
+        const int s = act[g0 + g];
+        const C *x = x0 + (size_t)s * strideX;
+        C acc = czero<C>();
+        for (int c = 0; c < width; ++c) {
+            const int e = beg + c * 32 + lane;
+            cfma(acc, vals[e], x[cols[e]]);
+        }
+        y0[(size_t)s * strideY + row] = acc;
+    }
+}
+
+// r = b - A x in FP64 with ||r||^2 reduced; last CTA sets true_res and alpha.
+__global__ void __launch_bounds__(NT) k_residual64(int n, const int *__restrict__ slice_ptr, const int *__restrict__ cols,
+                                                   const double2 *__restrict__ vals, const double2 *__restrict__ b0,
+                                                   size_t strideB, const double2 *__restrict__ x0, size_t strideX,
+                                                   double2 *__restrict__ r0, size_t strideR, const int *__restrict__ act,
+                                                   double2 *__restrict__ partials, unsigned *tickets, SysState *state) {
+    const int slot = blockIdx.y, s = act[slot], G = gridDim.x, tid = threadIdx.x;
+    const double2 *b = b0 + (size_t)s * strideB;
+    const double2 *x = x0 + (size_t)s * strideX;
+    double2 *r = r0 + (size_t)s * strideR;
+    __shared__ double red[1][NW];
+    double n2 = 0;
+    for (int row = blockIdx.x * NT + tid; row < n; row += G * NT) {
+        const int slice = row >> 5, lane = row & 31;
+        const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
+        double2 acc = b[row];
+        for (int c = 0; c < width; ++c) {
+            const int e = beg + c * 32 + lane;
+            cfms(acc, vals[e], x[cols[e]]);
+        }
+        r[row] = acc;
+        n2 += acc.x * acc.x + acc.y * acc.y;
+    }
+    double v[1] = {n2};
+    block_sum<1>(v, red);
+    double *part = (double *)partials + (size_t)slot * G;
+    if (tid == 0) part[blockIdx.x] = v[0];
+    if (!arrive_last(&tickets[slot])) return;
+    double tot[1];
+    __syncthreads();
+    sum_partials<1>(part, G, tot, red);
+    if (tid == 0) {
+        SysState &st = state[s];
+        st.nrm2 = tot[0];
+        const double nr = sqrt(tot[0]);
+        st.true_res = nr;
+        st.alpha = nr > 0 ? 1.0 / nr : 0.0;
+        if (!isfinite(nr)) st.bad = 1;
+        tickets[slot] = 0;
+    }
+}
+
+template <class R>
+__global__ void __launch_bounds__(NT) k_dense_gemv(int n, const typename CT<R>::t *__restrict__ A,
+                                                   const typename CT<R>::t *__restrict__ x, typename CT<R>::t *__restrict__ y) {
+    using C = typename CT<R>::t;
+    __shared__ C xs[NT];
+    const int row = blockIdx.x * NT + threadIdx.x;
+    C acc = czero<C>();
+    for (int j0 = 0; j0 < n; j0 += NT) {
+        __syncthreads();
+        xs[threadIdx.x] = j0 + threadIdx.x < n ? x[j0 + threadIdx.x] : czero<C>();
+        __syncthreads();
+        if (row < n) {
+            const int lim = min(NT, n - j0);
+            for (int j = 0; j < lim; ++j) cfma(acc, A[(size_t)(j0 + j) * n + row], xs[j]);
+        }
+    }
+    if (row < n) y[row] = acc;
+}
+
+template <class R>
+__global__ void __launch_bounds__(NT) k_copy(int n, const typename CT<R>::t *__restrict__ src, size_t strideS,
+                                             typename CT<R>::t *__restrict__ dst, size_t strideD, const int *__restrict__ act) {
+    const int s = act[blockIdx.y];
+    for (long i = (long)blockIdx.x * NT + threadIdx.x; i < n; i += (long)gridDim.x * NT)
+        dst[(size_t)s * strideD + i] = src[(size_t)s * strideS + i];
+}
+
+template <class R>
+__global__ void __launch_bounds__(NT) k_refine_update(int n, double2 *__restrict__ x0, size_t strideX,
+                                                      typename CT<R>::t *__restrict__ d0, size_t strideD,
+                                                      const int *__restrict__ act, const SysState *__restrict__ state) {
+    using C = typename CT<R>::t;
+    const int s = act[blockIdx.y];
+    const double sc = state[s].true_res;
+    double2 *x = x0 + (size_t)s * strideX;
+    C *d = d0 + (size_t)s * strideD;
+    for (long i = (long)blockIdx.x * NT + threadIdx.x; i < n; i += (long)gridDim.x * NT) {
+        C dv = d[i];
+        double2 xv = x[i];
+        xv.x += sc * (double)dv.x;
+        xv.y += sc * (double)dv.y;
+        x[i] = xv;
+        d[i] = czero<C>();
+    }
+}
+
+template <class R>
+__global__ void __launch_bounds__(NT) k_demote_unit(int n, const double2 *__restrict__ r0, size_t strideR,
+                                                    typename CT<R>::t *__restrict__ h0, size_t strideH,
+                                                    const int *__restrict__ act, const SysState *__restrict__ state) {
+    using C = typename CT<R>::t;
+    const int s = act[blockIdx.y];
+    const double a = state[s].alpha;
+    for (long i = (long)blockIdx.x * NT + threadIdx.x; i < n; i += (long)gridDim.x * NT) {
+        double2 v = r0[(size_t)s * strideR + i];
+        h0[(size_t)s * strideH + i] = from_d<C>(make_double2(v.x * a, v.y * a));
+    }
+}
+
+template <class R>
+__global__ void __launch_bounds__(NT) k_norm(int n, const typename CT<R>::t *__restrict__ v0, size_t strideV,
+                                             const int *__restrict__ act, double2 *__restrict__ partials,
+                                             unsigned *tickets, SysState *state, int mode) {
+    using C = typename CT<R>::t;
+    const int slot = blockIdx.y, s = act[slot], G = gridDim.x, tid = threadIdx.x;
+    const C *v = v0 + (size_t)s * strideV;
+    __shared__ double red[1][NW];
+    double n2 = 0;
+    for (long i = (long)blockIdx.x * NT + tid; i < n; i += (long)G * NT) {
+        C a = v[i];
+        n2 += (double)a.x * a.x + (double)a.y * a.y;
+    }
+    double vv[1] = {n2};
+    block_sum<1>(vv, red);
+    double *part = (double *)partials + (size_t)slot * G;
+    if (tid == 0) part[blockIdx.x] = vv[0];
+    if (!arrive_last(&tickets[slot])) return;
+    double tot[1];
+    __syncthreads();
+    sum_partials<1>(part, G, tot, red);
+    if (tid == 0) {
+        SysState &st = state[s];
+        st.nrm2 = tot[0];
+        const double nr = sqrt(tot[0]);
+        if (mode == 1) st.bnorm = nr;
+        if (mode == 2) { st.rho_abs = nr; st.alpha = nr > 0 ? 1.0 / nr : 0.0; }
+        if (!isfinite(nr)) st.bad = 1;
+        tickets[slot] = 0;
+    }
+}
+
+__global__ void k_broadcast_hdef(int m, int kk, const double2 *__restrict__ Hd, double2 *__restrict__ H0, size_t strideH,
+                                 const int *__restrict__ act) {
+    const int s = act[blockIdx.x], ld = m + 1;
+    double2 *H = H0 + (size_t)s * strideH;
+    for (int i = threadIdx.x; i < kk * kk; i += blockDim.x) {
+        const int c = i / kk, r = i % kk;
+        if (r <= c) H[(size_t)c * ld + r] = Hd[(size_t)c * ld + r];
+    }
+}
+
+inline dim3 grid2(int gx, int gy) { return dim3((unsigned)gx, (unsigned)gy, 1); }
+
+template <class R> int stream_grid(int n, int nsys) {
+    int chunks = (n + NT - 1) / NT;
+    int target = (num_sms() * 8 + nsys - 1) / (nsys > 0 ? nsys : 1);
+    if (target < 1) target = 1;
+    return chunks < target ? (chunks > 0 ? chunks : 1) : target;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------- instrumentation
+namespace {
+std::atomic<long long> g_launches{0};
+bool g_prof = false;
+struct Pending {
+    int kc;
+    double bytes;
+    cudaEvent_t a, b;
+};
+std::vector<Pending> g_pending;
+std::vector<cudaEvent_t> g_event_pool;
+double g_bytes[KC_COUNT], g_ms[KC_COUNT];
+long long g_calls[KC_COUNT];
+std::mutex g_prof_mu;
+
+cudaEvent_t take_event() {
+    if (!g_event_pool.empty()) {
+        cudaEvent_t e = g_event_pool.back();
+        g_event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// RAII bracket around one kernel launch.
+struct Launch {
+    int kc;
+    double bytes;
+    cudaStream_t st;
+    cudaEvent_t a = nullptr;
+    Launch(int kc_, double bytes_, cudaStream_t st_, int nlaunch = 1) : kc(kc_), bytes(bytes_), st(st_) {
+        g_launches += nlaunch;
+        if (g_prof) {
+            std::lock_guard<std::mutex> lk(g_prof_mu);
+            a = take_event();
+            cudaEventRecord(a, st);
+        }
+    }
+    ~Launch() {
+        if (a) {
+            std::lock_guard<std::mutex> lk(g_prof_mu);
+            cudaEvent_t b = take_event();
+            cudaEventRecord(b, st);
+            g_pending.push_back(Pending{kc, bytes, a, b});
+        }
+    }
+};
+}  // namespace
+
+long long launch_count() { return g_launches.load(); }
+void profile_enable(bool on) { g_prof = on; }
+bool profile_enabled() { return g_prof; }
+void profile_flush() {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    for (auto &p : g_pending) {
+        float ms = 0;
+        cudaEventSynchronize(p.b);
+        cudaEventElapsedTime(&ms, p.a, p.b);
+        g_ms[p.kc] += ms;
+        g_bytes[p.kc] += p.bytes;
+        g_calls[p.kc] += 1;
+        g_event_pool.push_back(p.a);
+        g_event_pool.push_back(p.b);
+    }
+    g_pending.clear();
+}
+void profile_read(int kc, double *bytes, double *ms, long long *launches) {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (kc < 0 || kc >= KC_COUNT) return;
+    if (bytes) *bytes = g_bytes[kc];
+    if (ms) *ms = g_ms[kc];
+    if (launches) *launches = g_calls[kc];
+}
+void profile_reset() {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    for (int i = 0; i < KC_COUNT; ++i) g_bytes[i] = g_ms[i] = 0, g_calls[i] = 0;
+}
+
+namespace {
+// Algorithmic bytes of y_s = A x_s for nsys systems, CSR accounting: every non-zero
+// read once (value + 4-byte index), row pointers once, x_s read once, y_s written once.
+double spmm_bytes(const SellMatrix &A, size_t vs, int nsys) {
+    return (double)A.nnz * (vs + 4.0) + (A.n + 1.0) * 4.0 + (double)nsys * 2.0 * vs * A.n;
+}
+}  // namespace
+size_t scratch_doubles(int qmax, int nsys) { return (size_t)(2 * qmax + 32) * (size_t)(num_sms() * 8 + nsys); }
+
+namespace {
+template <class K> void allow_smem(K kernel, size_t bytes) {
+    if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+}  // namespace
+
+template <class R>
+void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
+                 const typename CT<R>::t *w, size_t strideW, const int *act, int nsys, double2 *partials, int qmax,
+                 unsigned *tickets, double2 *coef, size_t strideC, SysState *state, bool skip_broken, cudaStream_t st) {
+    if (nsys <= 0 || qa + qb <= 0) return;
+    Launch L_(KC_MDOT, (double)sizeof(typename CT<R>::t) * n * ((double)qa + (double)nsys * (qb + 1)), st, 1);
+    const int G = red_grid<R>(n, nsys);
+    k_mdot<R, 4><<<grid2(G, nsys), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW, act, partials, qmax,
+                                                 tickets, coef, strideC, state, skip_broken ? 1 : 0);
+}
+
+template <class R>
+void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
+                   const typename CT<R>::t *w, size_t strideW, typename CT<R>::t *out, size_t strideO, const int *act,
+                   int nsys, const double2 *coef, size_t strideC, double2 *partials, unsigned *tickets,
+                   SysState *state, FinishArgs fin, bool skip_broken, cudaStream_t st) {
+    if (nsys <= 0) return;
+    Launch L_(KC_UPDATE, (double)sizeof(typename CT<R>::t) * n * ((double)qa + (double)nsys * (qb + 2)), st, 1);
+    const int G = red_grid<R>(n, nsys);
+    k_update<R, 4><<<grid2(G, nsys), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, coef,
+                                                   strideC, partials, tickets, state, fin, skip_broken ? 1 : 0);
+}
+
+template <class R>
+void launch_scale(int n, const typename CT<R>::t *in, size_t strideI, typename CT<R>::t *out1, size_t strideO1,
+                  typename CT<R>::t *out2, size_t strideO2, const int *act, int nsys, const SysState *state,
+                  bool honour_broken, cudaStream_t st) {
+    if (nsys <= 0) return;
+    Launch L_(KC_OTHER, (double)sizeof(typename CT<R>::t) * n * nsys * (out2 ? 3.0 : 2.0), st, 1);
+    k_scale<R><<<grid2(stream_grid<R>(n, nsys), nsys), NT, 0, st>>>(n, in, strideI, out1, strideO1, out2, strideO2,
+                                                                      act, state, honour_broken ? 1 : 0);
+}
+
+template <class R>
+void launch_combine(int n, int kk, int m, const typename CT<R>::t *W, const typename CT<R>::t *Z,
+                    const typename CT<R>::t *V, size_t strideV, typename CT<R>::t *r, size_t strideR,
+                    typename CT<R>::t *x, size_t strideX, const double2 *t, const double2 *y, size_t strideC,
+                    const int *act, int nsys, double2 *partials, unsigned *tickets, SysState *state, cudaStream_t st) {
+    if (nsys <= 0) return;
+    Launch L_(KC_COMBINE, (double)sizeof(typename CT<R>::t) * n * (2.0 * kk + (double)nsys * (m + 1 - kk + 4)), st, 1);
+    const int G = red_grid<R>(n, nsys);
+    k_combine<R><<<grid2(G, nsys), NT, 0, st>>>(n, kk, m, W, Z, V, strideV, r, strideR, x, strideX, t, y, strideC, act,
+                                                 partials, tickets, state);
+}
+
+template <class R>
+void launch_zupdate(int n, int kk, int m, int k, const typename CT<R>::t *Z, const typename CT<R>::t *V,
+                    const double2 *vs, typename CT<R>::t *Znew, double2 *partials, unsigned *ticket, double *znorm2,
+                    cudaStream_t st) {
+    Launch L_(KC_ZUPDATE, (double)sizeof(typename CT<R>::t) * n * ((double)m + k), st, (k + (sizeof(R) == 4 ? 16 : 8) - 1) / (sizeof(R) == 4 ? 16 : 8));
+    using C = typename CT<R>::t;
+    constexpr int KB = sizeof(R) == 4 ? 16 : 8;
+    int chunks = (n + NT - 1) / NT;
+    int G = num_sms() * 4;
+    if (G > chunks) G = chunks;
+    for (int t0 = 0; t0 < k; t0 += KB) {
+        size_t smem = (size_t)m * KB * sizeof(C);
+        k_zupdate<R, KB><<<G, NT, smem, st>>>(n, kk, m, k, t0, Z, V, vs, Znew, partials, ticket, znorm2);
+    }
+}
+
+template <class R>
+void launch_znormalise(int n, int k, const typename CT<R>::t *Znew, const double *znorm2, typename CT<R>::t *Z,
+                       cudaStream_t st) {
+    if (k <= 0) return;
+    Launch L_(KC_ZUPDATE, (double)sizeof(typename CT<R>::t) * n * 2.0 * k, st, 1);
+    k_znormalise<R><<<grid2(stream_grid<R>(n, k), k), NT, 0, st>>>(n, Znew, znorm2, Z);
+}
+
+void launch_ls(int m, const double2 *H, size_t strideH, const double2 *g, double2 *y, double2 *t, size_t strideC,
+               const int *act, int nsys, cudaStream_t st) {
+    if (nsys <= 0) return;
+    Launch L_(KC_LS, (double)sizeof(double2) * nsys * (m + 1.0) * m, st, 1);
+    size_t smem = sizeof(double2) * ((size_t)m * (m + 3) / 2 + (m + 1) + m + m) + sizeof(double) * (m + 1);
+    allow_smem(k_ls, smem);
+    k_ls<<<nsys, 128, smem, st>>>(m, H, strideH, g, y, t, strideC, act);
+}
+
+size_t svd_smem_bytes(int m) { return sizeof(double2) * ((size_t)(m + 1) * m + (size_t)m * m); }
+
+void launch_svd_smallest(int m, int k, const double2 *H, double2 *vs, double *sigma, double2 *work, int *sweeps,
+                         cudaStream_t st) {
+    Launch L_(KC_SVD, (double)sizeof(double2) * (m + 1.0) * m, st, 1);
+    size_t smem = svd_smem_bytes(m);
+    int use_smem = smem <= 200 * 1024;
+    if (use_smem) allow_smem(k_svd, smem);
+    k_svd<<<1, 512, use_smem ? smem : 0, st>>>(m, k, H, vs, sigma, work, use_smem, sweeps);
+}
+
+template <class R>
+void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX, typename CT<R>::t *y, size_t strideY,
+                 const int *act, int nsys, cudaStream_t st) {
+    if (nsys <= 0) return;
+    Launch L_(KC_SPMM, spmm_bytes(A, sizeof(typename CT<R>::t), nsys), st, 1);
+    constexpr int SG = 8;
+    dim3 grid((A.n + NT - 1) / NT, (nsys + SG - 1) / SG);
+    k_spmm<R, SG><<<grid, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const typename CT<R>::t *)A.vals, x, strideX, y,
+                                       strideY, act, nsys);
+}
+
+void launch_residual64(const SellMatrix &A, const double2 *b, size_t strideB, const double2 *x, size_t strideX,
+                       double2 *r, size_t strideR, const int *act, int nsys, double2 *partials, unsigned *tickets,
+                       SysState *state, cudaStream_t st) {
+    if (nsys <= 0) return;
+    Launch L_(KC_RESID64, spmm_bytes(A, sizeof(double2), nsys) + (double)sizeof(double2) * A.n * nsys, st, 1);
+    int chunks = (A.n + NT - 1) / NT;
+    int G = (num_sms() * 4 + nsys - 1) / nsys;
+    if (G > chunks) G = chunks;
+    if (G < 1) G = 1;
+    k_residual64<<<grid2(G, nsys), NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const double2 *)A.vals, b, strideB, x,
+                                                strideX, r, strideR, act, partials, tickets, state);
+}
+
+template <class R>
+void launch_dense_gemv(int n, const typename CT<R>::t *A, const typename CT<R>::t *x, typename CT<R>::t *y,
+                       cudaStream_t st) {
+    Launch L_(KC_SPMM, (double)sizeof(typename CT<R>::t) * ((double)n * n + 2.0 * n), st, 1);
+    k_dense_gemv<R><<<(n + NT - 1) / NT, NT, 0, st>>>(n, A, x, y);
+}
+
+template <class R>
+void launch_copy_vec(int n, const typename CT<R>::t *src, size_t strideS, typename CT<R>::t *dst, size_t strideD,
+                     const int *act, int nsys, cudaStream_t st) {
+    if (nsys <= 0) return;
+    Launch L_(KC_OTHER, (double)sizeof(typename CT<R>::t) * n * nsys * 2.0, st, 1);
+    k_copy<R><<<grid2(stream_grid<R>(n, nsys), nsys), NT, 0, st>>>(n, src, strideS, dst, strideD, act);
+}
+
+template <class R>
+void launch_refine_update(int n, double2 *x, size_t strideX, typename CT<R>::t *d, size_t strideD, const int *act,
+                          int nsys, const SysState *state, cudaStream_t st) {
+    if (nsys <= 0) return;
+    Launch L_(KC_OTHER, (double)(sizeof(typename CT<R>::t) * 2 + sizeof(double2) * 2) * n * nsys, st, 1);
+    k_refine_update<R><<<grid2(stream_grid<R>(n, nsys), nsys), NT, 0, st>>>(n, x, strideX, d, strideD, act, state);
+}
+
+template <class R>
+void launch_demote_unit(int n, const double2 *r64, size_t strideR, typename CT<R>::t *rhat, size_t strideH,
+                        const int *act, int nsys, const SysState *state, cudaStream_t st) {
+    if (nsys <= 0) return;
+    Launch L_(KC_OTHER, (double)(sizeof(typename CT<R>::t) + sizeof(double2)) * n * nsys, st, 1);
+    k_demote_unit<R><<<grid2(stream_grid<R>(n, nsys), nsys), NT, 0, st>>>(n, r64, strideR, rhat, strideH, act, state);
+}
+
+template <class R>
+void launch_norm(int n, const typename CT<R>::t *v, size_t strideV, const int *act, int nsys, double2 *partials,
+                 unsigned *tickets, SysState *state, int mode, cudaStream_t st) {
+    if (nsys <= 0) return;
+    Launch L_(KC_OTHER, (double)sizeof(typename CT<R>::t) * n * nsys, st, 1);
+    const int G = red_grid<R>(n, nsys);
+    k_norm<R><<<grid2(G, nsys), NT, 0, st>>>(n, v, strideV, act, partials, tickets, state, mode);
+}
+
+void launch_broadcast_hdef(int m, int kk, const double2 *Hd, double2 *H, size_t strideH, const int *act, int nsys,
+                           cudaStream_t st) {
+    if (nsys <= 0 || kk <= 0) return;
+    Launch L_(KC_OTHER, 0.0, st, 1);
+    k_broadcast_hdef<<<nsys, 256, 0, st>>>(m, kk, Hd, H, strideH, act);
+}
+
+#define GDMR_INST(R)                                                                                                   \
+    template void launch_mdot<R>(int, const CT<R>::t *, int, const CT<R>::t *, size_t, int, const CT<R>::t *, size_t,  \
+                                 const int *, int, double2 *, int, unsigned *, double2 *, size_t, SysState *, bool,   \
+                                 cudaStream_t);                                                                        \
+    template void launch_update<R>(int, const CT<R>::t *, int, const CT<R>::t *, size_t, int, const CT<R>::t *,        \
+                                   size_t, CT<R>::t *, size_t, const int *, int, const double2 *, size_t, double2 *,   \
+                                   unsigned *, SysState *, FinishArgs, bool, cudaStream_t);                            \
+    template void launch_scale<R>(int, const CT<R>::t *, size_t, CT<R>::t *, size_t, CT<R>::t *, size_t, const int *, \
+                                  int, const SysState *, bool, cudaStream_t);                                          \
+    template void launch_combine<R>(int, int, int, const CT<R>::t *, const CT<R>::t *, const CT<R>::t *, size_t,       \
+                                    CT<R>::t *, size_t, CT<R>::t *, size_t, const double2 *, const double2 *, size_t, \
+                                    const int *, int, double2 *, unsigned *, SysState *, cudaStream_t);                \
+    template void launch_zupdate<R>(int, int, int, int, const CT<R>::t *, const CT<R>::t *, const double2 *,          \
+                                    CT<R>::t *, double2 *, unsigned *, double *, cudaStream_t);                        \
+    template void launch_znormalise<R>(int, int, const CT<R>::t *, const double *, CT<R>::t *, cudaStream_t);          \
+    template void launch_spmm<R>(const SellMatrix &, const CT<R>::t *, size_t, CT<R>::t *, size_t, const int *, int,  \
+                                 cudaStream_t);                                                                        \
+    template void launch_dense_gemv<R>(int, const CT<R>::t *, const CT<R>::t *, CT<R>::t *, cudaStream_t);             \
+    template void launch_copy_vec<R>(int, const CT<R>::t *, size_t, CT<R>::t *, size_t, const int *, int,              \
+                                     cudaStream_t);                                                                    \
+    template void launch_refine_update<R>(int, double2 *, size_t, CT<R>::t *, size_t, const int *, int,                \
+                                          const SysState *, cudaStream_t);                                             \
+    template void launch_demote_unit<R>(int, const double2 *, size_t, CT<R>::t *, size_t, const int *, int,            \
+                                        const SysState *, cudaStream_t);                                               \
+    template void launch_norm<R>(int, const CT<R>::t *, size_t, const int *, int, double2 *, unsigned *, SysState *,   \
+                                 int, cudaStream_t);
+
+GDMR_INST(float)
+GDMR_INST(double)
+
+}  // namespace gdmr

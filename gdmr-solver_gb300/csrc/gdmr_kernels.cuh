@@ -1,0 +1,184 @@
+// Device kernels of the GB300 DMR restart cycle (sm_103a).
+//
+// Every kernel here is HBM-bound streaming work over n-long complex vectors,
+// except the small dense FP64 problems on the Hessenberg matrix (least squares
+// by Givens rotations, one-sided Jacobi SVD), which are latency-bound and run
+// one CTA per system.  Vectors are complex64 (float2) or complex128 (double2);
+// cross-thread reductions accumulate in double and finish deterministically
+// (fixed grid, fixed order, last-CTA-done ticket), replacing the racy
+// innerProdKerDMR reduction of the reference (gDMR.cu:268-326).
+//
+// Batching: most kernels run over an "active list" of systems (blockIdx.y
+// indexes the list), each system s owning a Krylov basis V_s of (m+1)
+// vectors at V + s*sysStride, while the deflation vectors W and Z are shared.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gdmr {
+
+template <class R> struct CT;
+template <> struct CT<float> { using t = float2; };
+template <> struct CT<double> { using t = double2; };
+
+__host__ __device__ inline float2 mk(float a, float b) { return make_float2(a, b); }
+__host__ __device__ inline double2 mk(double a, double b) { return make_double2(a, b); }
+
+// Per-system state that the device kernels update and the host reads once per cycle.
+struct SysState {
+    double nrm2;        // last reduced squared norm
+    double cross_re;    // last reduced <w_new, w_orig>
+    double cross_im;
+    double alpha;       // scale for the pending normalisation (1/norm, 0 after breakdown)
+    double rho;         // ||r_new|| / ||r_old|| of the last cycle (unit residual direction)
+    double rho_abs;     // absolute residual norm carried by the recursion
+    double bnorm;       // ||b||
+    double true_res;    // last FP64 ||b - A x|| (refined form)
+    int broken;         // Krylov step at which breakdown happened this cycle (0 = none)
+    int bad;            // non-finite value met
+    int pad[2];
+};
+
+// Finishing actions run by the last CTA of a reduction kernel.
+enum FinishMode : int {
+    FIN_NONE = 0,       // store nrm2/cross only
+    FIN_KRYLOV = 1,     // Krylov step: H column, breakdown test, alpha
+    FIN_DEFLATION = 2,  // deflation step: H[i,i] = <w,Az>/||w||, alpha
+    FIN_UNIT = 3,       // alpha = 1/||w||
+    FIN_RESIDUAL = 4,   // cycle end: rho, alpha = 1/rho
+};
+
+struct FinishArgs {
+    int mode;
+    int col;            // Hessenberg column being completed
+    int nco;            // number of projection coefficients in that column (rows 0..nco-1)
+    int ldH;            // m + 1
+    int m;              // Hessenberg columns
+    int kk;             // deflation dimension in this cycle
+    int compat_eye;     // breakdown identity tail starts at column j (reference) instead of kk+j
+    double tol;         // absolute breakdown threshold (the reference's solTol)
+    double2 *H;         // H of system 0; system s at H + s*strideH
+    size_t strideH;
+    const double2 *coef;  // projection coefficients of system 0; s at coef + s*strideC
+    size_t strideC;
+};
+
+// ----------------------------------------------------------------- instrumentation
+// Every launcher counts its kernel launches.  With profiling on, it also brackets
+// each launch with CUDA events on its stream and books the launch's algorithmic
+// bytes (the minimum HBM traffic of the operation) to its kernel class;
+// profile_flush() (after the stream is synchronised) turns the events into times.
+enum KernelClass : int {
+    KC_MDOT = 0,      // projection coefficients  [W V]^H w
+    KC_UPDATE = 1,    // w - [W V] c with norms
+    KC_SPMM = 2,      // SELL operator products (inner precision)
+    KC_COMBINE = 3,   // cycle-end residual / solution combinations
+    KC_ZUPDATE = 4,   // deflation-space update
+    KC_RESID64 = 5,   // FP64 true residual
+    KC_LS = 6,        // Givens least squares
+    KC_SVD = 7,       // Jacobi SVD
+    KC_OTHER = 8,     // scales, copies, norms, refinement updates
+    KC_COUNT = 9
+};
+long long launch_count();
+void profile_enable(bool on);
+bool profile_enabled();
+void profile_flush();
+void profile_read(int kc, double *bytes, double *ms, long long *launches);
+void profile_reset();
+
+// ----------------------------------------------------------------- launchers
+// All launchers enqueue on `st` and never synchronise.
+
+// Reduction scratch: every reducing kernel below needs `partials` of at least
+// scratch_doubles(qmax, nsys) doubles and `tickets` of nsys zero-initialised
+// counters (each kernel resets the counters it used).  Kernels on one stream
+// may share both.
+size_t scratch_doubles(int qmax, int nsys);
+
+template <class R>
+void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
+                 const typename CT<R>::t *w, size_t strideW, const int *act, int nsys, double2 *partials, int qmax,
+                 unsigned *tickets, double2 *coef, size_t strideC, SysState *state, bool skip_broken, cudaStream_t st);
+
+// out = w - [segA segB] coef, reduces ||out||^2 and <out, w>, then runs `fin` in the last CTA.
+template <class R>
+void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
+                   const typename CT<R>::t *w, size_t strideW, typename CT<R>::t *out, size_t strideO, const int *act,
+                   int nsys, const double2 *coef, size_t strideC, double2 *partials, unsigned *tickets,
+                   SysState *state, FinishArgs fin, bool skip_broken, cudaStream_t st);
+
+// out1 (and out2 if non-null) = alpha_s * in; zeros when the system broke down.
+template <class R>
+void launch_scale(int n, const typename CT<R>::t *in, size_t strideI, typename CT<R>::t *out1, size_t strideO1,
+                  typename CT<R>::t *out2, size_t strideO2, const int *act, int nsys, const SysState *state,
+                  bool honour_broken, cudaStream_t st);
+
+// Cycle-end combinations: r -= [W V] t ; x += rho_abs [Z V] y ; reduce ||r||^2, finish FIN_RESIDUAL.
+template <class R>
+void launch_combine(int n, int kk, int m, const typename CT<R>::t *W, const typename CT<R>::t *Z,
+                    const typename CT<R>::t *V, size_t strideV, typename CT<R>::t *r, size_t strideR,
+                    typename CT<R>::t *x, size_t strideX, const double2 *t, const double2 *y, size_t strideC,
+                    const int *act, int nsys, double2 *partials, unsigned *tickets, SysState *state, cudaStream_t st);
+
+// Z_new[t] = [Z V] vs[:, t] for t < k, plus squared norms into znorm2 (k doubles).
+template <class R>
+void launch_zupdate(int n, int kk, int m, int k, const typename CT<R>::t *Z, const typename CT<R>::t *V,
+                    const double2 *vs, typename CT<R>::t *Znew, double2 *partials, unsigned *ticket, double *znorm2,
+                    cudaStream_t st);
+// Z[t] = Znew[t] / sqrt(znorm2[t]).
+template <class R>
+void launch_znormalise(int n, int k, const typename CT<R>::t *Znew, const double *znorm2, typename CT<R>::t *Z,
+                       cudaStream_t st);
+
+// Batched least squares min ||H_s y - g_s|| (FP64 Givens), t_s = H_s y_s.
+void launch_ls(int m, const double2 *H, size_t strideH, const double2 *g, double2 *y, double2 *t, size_t strideC,
+               const int *act, int nsys, cudaStream_t st);
+// Right singular vectors of the k smallest singular values of H ((m+1) x m), FP64 one-sided Jacobi.
+// vs: m x k column-major; sigma: m values (descending); work: global scratch of 2*m*(m+1) double2.
+void launch_svd_smallest(int m, int k, const double2 *H, double2 *vs, double *sigma, double2 *work, int *sweeps,
+                         cudaStream_t st);
+
+// SELL-32 sparse matrix times a batch of vectors: y_s = A x_s over the active systems.
+struct SellMatrix {
+    int n;              // rows
+    int nslices;        // ceil(n/32)
+    const int *slice_ptr;   // nslices+1 offsets (entries), int32
+    const int *cols;        // padded column indices
+    const void *vals;       // padded values (float2 or double2)
+    long nnz;               // non-zeros of the source matrix (for algorithmic byte counts)
+};
+template <class R>
+void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX, typename CT<R>::t *y,
+                 size_t strideY, const int *act, int nsys, cudaStream_t st);
+// y_s = b_s - A x_s in FP64 with ||y_s||^2 reduced into state[s].nrm2 (refined form).
+void launch_residual64(const SellMatrix &A, const double2 *b, size_t strideB, const double2 *x, size_t strideX,
+                       double2 *r, size_t strideR, const int *act, int nsys, double2 *partials, unsigned *tickets,
+                       SysState *state, cudaStream_t st);
+// Dense column-major n x n operator (the reference's impOptLS form): y = A x.
+template <class R>
+void launch_dense_gemv(int n, const typename CT<R>::t *A, const typename CT<R>::t *x, typename CT<R>::t *y,
+                       cudaStream_t st);
+
+// Small helpers.
+template <class R>
+void launch_copy_vec(int n, const typename CT<R>::t *src, size_t strideS, typename CT<R>::t *dst, size_t strideD,
+                     const int *act, int nsys, cudaStream_t st);
+// x64_s += scale_s * d_s (d complex64/128 inner correction), then d_s = 0.
+template <class R>
+void launch_refine_update(int n, double2 *x, size_t strideX, typename CT<R>::t *d, size_t strideD,
+                          const int *act, int nsys, const SysState *state, cudaStream_t st);
+// rhat_s = (R) (r64_s / sqrt(nrm2_s)).
+template <class R>
+void launch_demote_unit(int n, const double2 *r64, size_t strideR, typename CT<R>::t *rhat, size_t strideH,
+                        const int *act, int nsys, const SysState *state, cudaStream_t st);
+// Squared norm of each active vector into state[s].nrm2 (and bnorm if set_bnorm).
+// mode 0: nrm2 only; 1: also bnorm = ||v||; 2: also rho_abs = ||v|| and alpha = 1/||v||.
+template <class R>
+void launch_norm(int n, const typename CT<R>::t *v, size_t strideV, const int *act, int nsys, double2 *partials,
+                 unsigned *tickets, SysState *state, int mode, cudaStream_t st);
+// Deflation block broadcast: H_s[0:kk, 0:kk] = Hd[0:kk, 0:kk] (ld m+1) for each active system.
+void launch_broadcast_hdef(int m, int kk, const double2 *Hd, double2 *H, size_t strideH, const int *act, int nsys,
+                           cudaStream_t st);
+
+}  // namespace gdmr

@@ -1,0 +1,321 @@
+"""Python binding of libgDMR (GB300 build) over its C ABI (ctypes).
+
+Mirrors the reference's plugin interface (gDMRC.h: initLS / imp*LS / exp*LS /
+solveLS / linOptLS / impSVDMR / expSVDMR) with the same names and argument
+meaning, plus the complex128 twins and the context API of gdmr_ext.h.  There
+is no fallback: if the CUDA library is missing or no GPU is visible, calls
+raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libgDMR.so.1")
+
+# Every C entry point declared in include/*.h, with its ctypes signature.
+P, I, F, D, LL = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_double, ctypes.c_longlong
+SIGNATURES = {
+    # gDMR.h
+    "initDMR": (None, [I, I, P, I, I, I, I, P]),
+    "freeDMR": (None, []),
+    "solverDMR": (F, [I, P, P, P, I, F, I, P]),
+    "impSVDMR": (None, [P]),
+    "expSVDMR": (None, [P]),
+    # gDMRC.h
+    "initLS": (None, [I, I, I, I, P, I, I, I]),
+    "freeLS": (None, []),
+    "impImgLS": (None, [P]), "expImgLS": (None, [P]),
+    "impSrcLS": (None, [P]), "expSrcLS": (None, [P]),
+    "impOptLS": (None, [P]), "expOptLS": (None, [P]),
+    "solveLS": (F, [I, F, I, P]),
+    "linOptLS": (None, []),
+    # gdmr_ext.h
+    "gdmrLastStatus": (I, []),
+    "gdmrLastError": (ctypes.c_char_p, []),
+    "gdmrVersion": (ctypes.c_char_p, []),
+    "gdmrLastStats": (None, [P]),
+    "initDMR_z": (None, [I, I, P, I, I, I, I, P]),
+    "freeDMR_z": (None, []),
+    "solverDMR_z": (D, [I, P, P, P, I, D, I, P]),
+    "impSVDMR_z": (None, [P]), "expSVDMR_z": (None, [P]),
+    "impCsrLS": (I, [I, P, P, P]),
+    "initLS_z": (None, [I, I, I, I, P, I, I, I]),
+    "freeLS_z": (None, []),
+    "impImgLS_z": (None, [P]), "expImgLS_z": (None, [P]),
+    "impSrcLS_z": (None, [P]), "expSrcLS_z": (None, [P]),
+    "impOptLS_z": (None, [P]),
+    "impCsrLS_z": (I, [I, P, P, P]),
+    "solveLS_z": (D, [I, D, I, P]),
+    "linOptLS_z": (None, []),
+    "gdmrKernelLaunches": (LL, []),
+    "gdmrProfile": (None, [I]),
+    "gdmrProfileReset": (None, []),
+    "gdmrProfileRead": (I, [I, P, P, P]),
+    "gdmr_system_create": (I, [P, I, P, P, P, I, I, I, I, I]),
+    "gdmr_system_destroy": (I, [P]),
+    "gdmr_system_bytes": (LL, [P]),
+    "gdmr_solve": (I, [P, I, P, P, D, I, I, P]),
+    "gdmr_solve_batch": (I, [P, I, P, P, P, I, I, P]),
+    "gdmr_true_residual": (I, [P, I, P, P, I, P]),
+    "gdmr_export_deflation": (I, [P, P]),
+    "gdmr_import_deflation": (I, [P, P]),
+    "gdmr_drop_deflation": (I, [P]),
+}
+
+STATUS = {0: "GDMR_OK", 1: "GDMR_EINVAL", 2: "GDMR_ENOMEM", 3: "GDMR_ENOCONV", 4: "GDMR_ERUNAWAY",
+          5: "GDMR_ECUDA", 6: "GDMR_ENOTINIT", 7: "GDMR_EBREAKDOWN"}
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("cycles", I), ("its", I), ("matvecs", LL), ("rel_res", D), ("true_rel_res", D),
+                ("status", I), ("breakdowns", I), ("latency_ms", D)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+KERNEL_CLASSES = ["projection", "update", "operator", "combine", "deflation_update", "residual64",
+                  "least_squares", "svd", "other"]
+
+
+def kernel_launches() -> int:
+    return int(load().gdmrKernelLaunches())
+
+
+def profile(on: bool) -> None:
+    load().gdmrProfile(1 if on else 0)
+
+
+def profile_reset() -> None:
+    load().gdmrProfileReset()
+
+
+def profile_read() -> dict:
+    """Per kernel class: algorithmic bytes, CUDA-event milliseconds, launches."""
+    out = {}
+    for i, name in enumerate(KERNEL_CLASSES):
+        b, ms, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+        load().gdmrProfileRead(i, ctypes.byref(b), ctypes.byref(ms), ctypes.byref(n))
+        out[name] = {"bytes": b.value, "ms": ms.value, "launches": n.value}
+    return out
+
+
+class GDMRError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Loads the library (building it first if the sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("gdmr_build", os.path.join(HERE, "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    L = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return load().gdmrLastError().decode()
+
+
+def last_stats() -> dict:
+    s = Stats()
+    load().gdmrLastStats(ctypes.byref(s))
+    return s.as_dict()
+
+
+def _check(rc: int, what: str):
+    if rc != 0:
+        raise GDMRError(rc, f"{what}: {last_error()}")
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _csr_arrays(A):
+    indptr = np.ascontiguousarray(A.indptr, dtype=np.int32)
+    indices = np.ascontiguousarray(A.indices, dtype=np.int32)
+    return indptr, indices
+
+
+class LinearSystem:
+    """The reference's plugin (gDMRC.h) in complex64 ('c64', the reference's
+    precision) or complex128 ('c128', the *_z entry points).  One instance per
+    precision may be live at a time: the plugin, like the reference's, is
+    process-global."""
+
+    def __init__(self, n: int, basis: int, deflat: int, precision: str = "c64", device: int = 0,
+                 blocks: int = 32, threads: int = 512, devices=(0,)):
+        self.L = load()
+        self.n, self.m, self.k = n, basis, deflat
+        self.z = precision == "c128"
+        self.cdt = np.complex128 if self.z else np.complex64
+        devs = (ctypes.c_int * len(devices))(*devices)
+        init = self.L.initLS_z if self.z else self.L.initLS
+        init(blocks, threads, device, n, devs, len(devices), basis, deflat)
+        if self.L.gdmrLastStatus() != 0:
+            raise GDMRError(self.L.gdmrLastStatus(), last_error())
+        self._live = True
+
+    def _fn(self, name):
+        return getattr(self.L, name + ("_z" if self.z else ""))
+
+    def imp_img(self, b):
+        b = np.ascontiguousarray(b, dtype=self.cdt)
+        self._fn("impImgLS")(_ptr(b))
+
+    def exp_img(self):
+        out = np.zeros(self.n, self.cdt)
+        self._fn("expImgLS")(_ptr(out))
+        return out
+
+    def imp_src(self, x):
+        x = np.ascontiguousarray(x, dtype=self.cdt)
+        self._fn("impSrcLS")(_ptr(x))
+
+    def exp_src(self):
+        out = np.zeros(self.n, self.cdt)
+        self._fn("expSrcLS")(_ptr(out))
+        return out
+
+    def imp_opt(self, dense):
+        """Dense operator, (n, n) array; stored column-major as the reference does."""
+        a = np.asfortranarray(dense, dtype=self.cdt)
+        self._fn("impOptLS")(_ptr(a.reshape(-1, order="F")))
+
+    def imp_csr(self, A):
+        indptr, indices = _csr_arrays(A)
+        vals = np.ascontiguousarray(A.data, dtype=self.cdt)
+        _check(self._fn("impCsrLS")(int(A.nnz), _ptr(indptr), _ptr(indices), _ptr(vals)), "impCsrLS")
+
+    def lin_opt(self):
+        self._fn("linOptLS")()
+
+    def solve(self, mode: int, tol: float, mat_rank: int):
+        its = ctypes.c_int()
+        r = self._fn("solveLS")(int(mode), float(tol), int(mat_rank), ctypes.byref(its))
+        return float(r), its.value
+
+    def imp_sv(self, Z):
+        Z = np.ascontiguousarray(Z, dtype=self.cdt).reshape(-1)
+        (self.L.impSVDMR_z if self.z else self.L.impSVDMR)(_ptr(Z))
+
+    def exp_sv(self):
+        out = np.zeros(self.k * self.n, self.cdt)
+        (self.L.expSVDMR_z if self.z else self.L.expSVDMR)(_ptr(out))
+        return out.reshape(self.k, self.n)
+
+    def close(self):
+        if self._live:
+            self._fn("freeLS")()
+            self._live = False
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class System:
+    """Context API (gdmr_ext.h): a resident CSR operator plus a solver engine of
+    `capacity` systems sharing one recycled deflation space.
+    precision: 'fp64' (plain complex128 iteration) or 'mixed' (complex64 inner
+    iteration inside FP64 refinement)."""
+
+    def __init__(self, A, basis: int, deflat: int, capacity: int = 1, precision: str = "fp64", device: int = 0):
+        self.L = load()
+        self.n, self.m, self.k, self.capacity = A.n, basis, deflat, capacity
+        indptr, indices = _csr_arrays(A)
+        vals = np.ascontiguousarray(A.data, dtype=np.complex128)
+        h = ctypes.c_void_p()
+        prec = {"fp64": 0, "mixed": 1}[precision]
+        _check(self.L.gdmr_system_create(ctypes.byref(h), A.n, _ptr(indptr), _ptr(indices), _ptr(vals),
+                                         basis, deflat, capacity, prec, device), "gdmr_system_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.L.gdmr_system_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self.L.gdmr_system_bytes(self._h))
+
+    def solve(self, b, x0=None, mode: int = 0, tol: float = 1e-10, mat_rank: int = 2000):
+        """Reference-semantics solve of one right-hand side; returns (x, stats)."""
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.zeros(self.n, np.complex128) if x0 is None else np.array(x0, dtype=np.complex128)
+        st = Stats()
+        rc = self.L.gdmr_solve(self._h, int(mode), _ptr(b), _ptr(x), float(tol), int(mat_rank), 0, ctypes.byref(st))
+        if rc not in (0, 3, 4):
+            _check(rc, "gdmr_solve")
+        return x, st.as_dict()
+
+    def solve_batch(self, B, X0=None, tol=1e-10, max_cycles: int = 5000):
+        """FP64-refined batched solve; B is (nrhs, n).  Returns (X, [stats])."""
+        B = np.ascontiguousarray(B, dtype=np.complex128)
+        nrhs = B.shape[0]
+        X = np.zeros_like(B) if X0 is None else np.array(X0, dtype=np.complex128)
+        tols = np.ascontiguousarray(np.broadcast_to(np.asarray(tol, dtype=np.float64), (nrhs,)))
+        stats = (Stats * nrhs)()
+        rc = self.L.gdmr_solve_batch(self._h, nrhs, _ptr(B), _ptr(X), _ptr(tols), int(max_cycles), 0, stats)
+        if rc not in (0, 3, 4):
+            _check(rc, "gdmr_solve_batch")
+        return X, [s.as_dict() for s in stats]
+
+    def solve_batch_device(self, b_ptr: int, x_ptr: int, nrhs: int, tol, max_cycles: int = 5000):
+        """Same on device buffers (raw pointers to complex128 arrays of nrhs*n)."""
+        tols = np.ascontiguousarray(np.broadcast_to(np.asarray(tol, dtype=np.float64), (nrhs,)))
+        stats = (Stats * nrhs)()
+        rc = self.L.gdmr_solve_batch(self._h, nrhs, ctypes.c_void_p(b_ptr), ctypes.c_void_p(x_ptr), _ptr(tols),
+                                     int(max_cycles), 1, stats)
+        if rc not in (0, 3, 4):
+            _check(rc, "gdmr_solve_batch")
+        return [s.as_dict() for s in stats]
+
+    def true_residual(self, B, X):
+        B = np.ascontiguousarray(np.atleast_2d(B), dtype=np.complex128)
+        X = np.ascontiguousarray(np.atleast_2d(X), dtype=np.complex128)
+        out = np.zeros(B.shape[0])
+        _check(self.L.gdmr_true_residual(self._h, B.shape[0], _ptr(B), _ptr(X), 0, _ptr(out)), "gdmr_true_residual")
+        return out
+
+    def export_deflation(self):
+        Z = np.zeros((self.k, self.n), np.complex128)
+        _check(self.L.gdmr_export_deflation(self._h, _ptr(Z)), "gdmr_export_deflation")
+        return Z
+
+    def import_deflation(self, Z):
+        Z = np.ascontiguousarray(Z, dtype=np.complex128)
+        _check(self.L.gdmr_import_deflation(self._h, _ptr(Z)), "gdmr_import_deflation")
+
+    def drop_deflation(self):
+        _check(self.L.gdmr_drop_deflation(self._h), "gdmr_drop_deflation")

@@ -1,0 +1,132 @@
+/* Extensions of libgDMR (GB300 build): status reporting, the complex128
+ * drop-in (the reference is complex64 only), sparse plugins, and a
+ * context API for the batched FP64-refined mixed-precision solver.
+ *
+ * None of these symbols exists in the reference; each names the reference
+ * interface it extends.  Complex values cross the ABI as interleaved
+ * (re, im) doubles or floats, or as C99 _Complex, so plain C callers need no
+ * CUDA headers (only the *_z solver entry points take cudaStream_t).
+ */
+#ifndef GDMR_GB300_EXT_H
+#define GDMR_GB300_EXT_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes (the reference prints to stderr and resets the device instead,
+ * gDMR.cu:409-429; this library never resets a device). */
+enum {
+    GDMR_OK = 0,
+    GDMR_EINVAL = 1,     /* bad argument or size */
+    GDMR_ENOMEM = 2,     /* device allocation failed */
+    GDMR_ENOCONV = 3,    /* cycle cap reached (reference: "failed to converge", gDMR.cu:2816) */
+    GDMR_ERUNAWAY = 4,   /* residual above ||b|| (reference: "Runaway", gDMR.cu:2823) */
+    GDMR_ECUDA = 5,      /* CUDA runtime error */
+    GDMR_ENOTINIT = 6,   /* used before init */
+    GDMR_EBREAKDOWN = 7
+};
+
+/* Last status and message of any entry point (process-wide). */
+int gdmrLastStatus(void);
+const char *gdmrLastError(void);
+/* Library version string, e.g. "1.0.1-gb300". */
+const char *gdmrVersion(void);
+
+/* ---- complex128 drop-in: reference solver semantics in FP64 ----------------
+ * Same arguments and behaviour as initDMR/freeDMR/solverDMR/impSVDMR/expSVDMR
+ * (gDMR.h), with complex128 vectors and a double tolerance.  The hook must
+ * overwrite the complex128 source buffer passed to solverDMR_z. */
+#ifdef GDMR_WITH_CUDA_TYPES
+void initDMR_z(int blocks, int threadsPerBlock, int *devList, int numDevs, int elements, int basisDim, int deflatDim,
+               void (*linComp)(void));
+void freeDMR_z(void);
+double solverDMR_z(int mode, cuDoubleComplex *extSrcVec, cuDoubleComplex *extImgVec, cudaStream_t extStream,
+                   int extDevNum, double solTol, int matRank, int *numIts);
+#endif
+void impSVDMR_z(double _Complex *cMem);
+void expSVDMR_z(double _Complex *cMem);
+
+/* ---- plugin extensions (extend gDMRC.h) ------------------------------------
+ * impCsrLS: make the plugin's operator the CSR matrix (int32 row pointers of
+ * length cells+1, int32 column indices, complex64 values), stored on the
+ * device in SELL-32 form; replaces any dense operator. */
+int impCsrLS(int nnz, const int *rowPtr, const int *colIdx, const float _Complex *vals);
+/* The complex128 plugin: the same functions with a _z suffix, solving through
+ * solverDMR_z. */
+void initLS_z(int blocksMDR, int threadsPerBlockMDR, int devNumLO, int cells, int *devListMDR, int numDevsMDR,
+              int basisSizeMDR, int deflatSizeMDR);
+void freeLS_z(void);
+void impImgLS_z(double _Complex *cImg);
+void expImgLS_z(double _Complex *cImg);
+void impSrcLS_z(double _Complex *cSrc);
+void expSrcLS_z(double _Complex *cSrc);
+void impOptLS_z(double _Complex *cOpt);
+int impCsrLS_z(int nnz, const int *rowPtr, const int *colIdx, const double _Complex *vals);
+double solveLS_z(int mode, double solTol, int matRank, int *numIts);
+void linOptLS_z(void);
+/* Statistics of the last solveLS/solveLS_z/solverDMR/solverDMR_z call. */
+typedef struct {
+    int cycles;            /* restart cycles run */
+    int its;               /* reference convention: cycles - 1 */
+    long long matvecs;     /* operator applications */
+    double rel_res;        /* value returned by the solve */
+    double true_rel_res;   /* FP64 ||b - A x|| / ||b|| when measured, else -1 */
+    int status;            /* GDMR_* */
+    int breakdowns;        /* cycles that ended in a Krylov breakdown */
+    double latency_ms;     /* batched solves: time from the call's start to this solution's return */
+} gdmr_stats;
+void gdmrLastStats(gdmr_stats *out);
+
+/* ---- instrumentation --------------------------------------------------------
+ * Kernel launches issued by this library since load.  With profiling on, each
+ * launch is bracketed by CUDA events on its stream and booked, with its
+ * algorithmic bytes, to a kernel class: 0 projection [W V]^H w, 1 update
+ * w - [W V] c, 2 operator products, 3 cycle-end combinations, 4 deflation
+ * update, 5 FP64 true residual, 6 least squares, 7 SVD, 8 other. */
+long long gdmrKernelLaunches(void);
+void gdmrProfile(int on);
+void gdmrProfileReset(void);
+int gdmrProfileRead(int kernelClass, double *bytes, double *ms, long long *launches);
+
+/* ---- context API: one resident operator, many right-hand sides -------------
+ * A gdmr_system holds a CSR operator on the device (SELL-32, complex64 and
+ * complex128 values), a solver engine of `capacity` systems and one recycled
+ * deflation space shared by every right-hand side solved through it.
+ * precision 0: plain FP64 inner iteration; 1: complex64 inner iteration.
+ * Both forms check convergence on the true FP64 residual b - A x. */
+typedef struct gdmr_system gdmr_system;
+int gdmr_system_create(gdmr_system **out, int n, const int *rowPtr, const int *colIdx, const double *vals_ri,
+                       int basisDim, int deflatDim, int capacity, int precision, int device);
+int gdmr_system_destroy(gdmr_system *sys);
+/* Bytes of device memory the system holds. */
+long long gdmr_system_bytes(const gdmr_system *sys);
+
+/* Reference-semantics solve of one right-hand side (solverDMR's algorithm,
+ * complex128 or complex64 per the system's precision), then the true FP64
+ * residual.  b, x: interleaved complex128, on the host (on_device = 0) or the
+ * device (on_device = 1); x is the initial guess on entry. */
+int gdmr_solve(gdmr_system *sys, int mode, const double *b, double *x, double tol, int matRank, int on_device,
+               gdmr_stats *stats);
+
+/* Batched FP64-refined solve of nrhs right-hand sides (right-hand side s at
+ * offset s*n, interleaved complex128), all sharing the system's deflation
+ * space.  Each restart cycle starts from the true FP64 residual; a system
+ * leaves the batch when ||b - A x|| <= tol[s] ||b||.  nrhs may exceed the
+ * capacity: the batch is refilled as systems converge.  stats: nrhs entries
+ * or NULL. */
+int gdmr_solve_batch(gdmr_system *sys, int nrhs, const double *b, double *x, const double *tol, int maxCycles,
+                     int on_device, gdmr_stats *stats);
+
+/* FP64 ||b_s - A x_s|| / ||b_s|| for nrhs pairs. */
+int gdmr_true_residual(gdmr_system *sys, int nrhs, const double *b, const double *x, int on_device, double *relres);
+
+/* Deflation space in and out: deflatDim x n interleaved complex128 on the host.
+ * Import makes the next solve start from it; drop forgets it. */
+int gdmr_export_deflation(gdmr_system *sys, double *z);
+int gdmr_import_deflation(gdmr_system *sys, const double *z);
+int gdmr_drop_deflation(gdmr_system *sys);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

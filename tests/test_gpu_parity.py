@@ -1,0 +1,246 @@
+"""Parity of libgDMR's CUDA path with the oracle, through the C ABI.
+
+Every test here runs the sm_103a kernels (SELL SpMV, fused Gram-Schmidt,
+Givens least squares, Jacobi SVD, deflation update) via ctypes and compares
+with the host oracle (oracle/dmr_oracle.cpp), the golden fixtures, or a
+sparse direct solve.  Tolerances:
+  * complex128 forms: same restart-cycle count as the oracle on a first solve
+    (+-2 later in a recycled sequence, whose deflation space is sensitive to
+    rounding), x within 1e-8 relative of the oracle, true FP64 residual
+    <= 2x the requested tolerance;
+  * complex64 (reference precision) forms: cycles +-2, x within 1e-3.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import gdmr
+import problems
+from problems import CSR
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _golden(name):
+    d = np.load(os.path.join(GOLDEN, name))
+    return CSR(int(d["indptr"].size - 1), d["indptr"], d["indices"], d["data"]), d
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _true(A, b, x):
+    return float(np.linalg.norm(b - A.to_scipy() @ x) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module")
+def c1():
+    import scipy.sparse.linalg as spl
+    A, rhs, cfg = problems.config_2d64()
+    lu = spl.splu(A.to_scipy().tocsc())
+    return A, rhs, cfg, [lu.solve(b) for b in rhs]
+
+
+def test_fp64_first_solve_matches_oracle(c1, oracle_mod):
+    A, rhs, cfg, direct = c1
+    sys_ = gdmr.System(A, cfg["m"], cfg["k"], capacity=1, precision="fp64")
+    x, st = sys_.solve(rhs[0], mode=0, tol=1e-10, mat_rank=2000)
+    o = oracle_mod.Oracle(A, cfg["m"], cfg["k"], fuse_deflation=True)
+    r = o.solve(rhs[0], mode=0, tol=1e-10, mat_rank=2000)
+    assert st["status"] == 0
+    assert st["cycles"] == r["cycles"]
+    assert st["its"] == r["its"] == r["cycles"] - 1
+    assert abs(st["rel_res"] - r["ret"]) <= 1e-3 * r["ret"]
+    assert _rel(x, r["x"]) < 1e-8
+    assert st["true_rel_res"] <= 2e-10
+    assert _true(A, rhs[0], x) <= 2e-10
+    assert _rel(x, direct[0]) < 1e-8
+
+
+def test_fp64_recycled_sequence(c1, oracle_mod):
+    A, rhs, cfg, direct = c1
+    sys_ = gdmr.System(A, cfg["m"], cfg["k"], capacity=1, precision="fp64")
+    o = oracle_mod.Oracle(A, cfg["m"], cfg["k"], fuse_deflation=True)
+    total_gpu = total_orc = 0
+    for i, b in enumerate(rhs):
+        x, st = sys_.solve(b, mode=0 if i == 0 else 1, tol=1e-10, mat_rank=2000)
+        r = o.solve(b, mode=0 if i == 0 else 1, tol=1e-10, mat_rank=2000)
+        assert st["status"] == 0
+        assert abs(st["cycles"] - r["cycles"]) <= 2 + r["cycles"] // 10, (i, st["cycles"], r["cycles"])
+        assert _true(A, b, x) <= 2e-10
+        assert _rel(x, direct[i]) < 1e-8
+        total_gpu += st["cycles"]
+        total_orc += r["cycles"]
+    assert abs(total_gpu - total_orc) <= 2 * len(rhs)
+
+
+def test_fp64_golden_sequence():
+    A, d = _golden("helmholtz10.npz")
+    sys_ = gdmr.System(A, int(d["m"]), int(d["k"]), capacity=1, precision="fp64")
+    for i in range(int(d["nrhs"])):
+        x, st = sys_.solve(d[f"b{i}"], mode=0 if i == 0 else 1, tol=float(d["tol"]), mat_rank=int(d["mat_rank"]))
+        assert st["status"] == 0
+        assert abs(st["cycles"] - int(d[f"cycles{i}"])) <= 2
+        assert _rel(x, d[f"x{i}"]) < 1e-9
+        assert _rel(x, d[f"direct{i}"]) < 1e-8
+
+
+def test_fp64_breakdown_identity_tail():
+    A, d = _golden("breakdown30.npz")
+    sys_ = gdmr.System(A, int(d["m"]), int(d["k"]), capacity=1, precision="fp64")
+    x, st = sys_.solve(d["b0"], mode=0, tol=float(d["tol"]), mat_rank=int(d["mat_rank"]))
+    assert st["status"] == 0 and st["cycles"] == 1 and st["breakdowns"] == 1
+    assert _rel(x, d["direct0"]) < 1e-12
+
+
+def test_legacy_complex64_plugin_csr(c1, oracle_mod):
+    """gDMRC.h in the reference's precision with a CSR operator (impCsrLS)."""
+    A, rhs, cfg, direct = c1
+    ls = gdmr.LinearSystem(A.n, cfg["m"], cfg["k"], precision="c64")
+    try:
+        ls.imp_csr(A)
+        o = oracle_mod.Oracle(A, cfg["m"], cfg["k"], precision="c64", fuse_deflation=True)
+        for i, b in enumerate(rhs[:3]):
+            ls.imp_img(b)
+            ls.imp_src(np.zeros(A.n))
+            ret, its = ls.solve(0 if i == 0 else 1, 1e-5, 2000)
+            x = ls.exp_src()
+            r = o.solve(b, mode=0 if i == 0 else 1, tol=1e-5, mat_rank=2000)
+            assert ret < 1e-5
+            assert abs(its - r["its"]) <= 2 + r["its"] // 10
+            assert _rel(x, direct[i]) < 1e-3
+            assert _rel(x, r["x"]) < 1e-3
+        Z = ls.exp_sv()
+        assert Z.shape == (cfg["k"], A.n)
+        assert np.allclose(np.linalg.norm(Z, axis=1), 1.0, atol=1e-4)
+    finally:
+        ls.close()
+
+
+def _dense_tridiag(n):
+    main = np.full(n, 2.5 + 0.2j, np.complex64)
+    off = np.full(n - 1, -1.0 + 0.0j, np.complex64)
+    return np.diag(main) + np.diag(off, 1) + np.diag(off, -1)
+
+
+def test_legacy_complex64_plugin_dense_like_control_program(oracle_mod):
+    """The reference control program's set-up: dense 1024 x 1024 operator,
+    basis 127, no deflation, tolerance 1e-5, five right-hand sides."""
+    n = 1024
+    Ad = _dense_tridiag(n)
+    import scipy.sparse as sp
+    S = sp.csr_matrix(Ad.astype(np.complex128))
+    A = CSR(n, S.indptr.astype(np.int32), S.indices.astype(np.int32), S.data)
+    ls = gdmr.LinearSystem(n, 127, 0, precision="c64")
+    try:
+        ls.imp_opt(Ad)
+        o = oracle_mod.Oracle(A, 127, 0, precision="c64", fuse_deflation=True)
+        for i in range(5):
+            b = problems.unit_gaussian_rhs(n, 40 + i)
+            ls.imp_img(b)
+            ls.imp_src(np.zeros(n))
+            ret, its = ls.solve(i, 1e-5, n)
+            x = ls.exp_src()
+            r = o.solve(b, mode=i, tol=1e-5, mat_rank=n)
+            assert ret < 1e-5
+            assert abs(its - r["its"]) <= 2
+            assert _rel(x, r["x"]) < 1e-3
+        # linOptLS applies the dense operator in place
+        v = problems.unit_gaussian_rhs(n, 99).astype(np.complex64)
+        ls.imp_src(v)
+        ls.lin_opt()
+        assert _rel(ls.exp_src(), Ad @ v) < 1e-5
+    finally:
+        ls.close()
+
+
+def test_legacy_complex128_plugin(c1, oracle_mod):
+    A, rhs, cfg, direct = c1
+    ls = gdmr.LinearSystem(A.n, cfg["m"], cfg["k"], precision="c128")
+    try:
+        ls.imp_csr(A)
+        o = oracle_mod.Oracle(A, cfg["m"], cfg["k"], fuse_deflation=True)
+        ls.imp_img(rhs[0])
+        ls.imp_src(np.zeros(A.n))
+        ret, its = ls.solve(0, 1e-10, 2000)
+        x = ls.exp_src()
+        r = o.solve(rhs[0], mode=0, tol=1e-10, mat_rank=2000)
+        assert its == r["its"]
+        assert _rel(x, r["x"]) < 1e-8
+        assert _true(A, rhs[0], x) <= 2e-10
+        assert gdmr.last_stats()["cycles"] == r["cycles"]
+    finally:
+        ls.close()
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_refined_batch_reaches_fp64_tolerance(c1, precision):
+    A, rhs, cfg, direct = c1
+    sys_ = gdmr.System(A, cfg["m"], cfg["k"], capacity=8, precision=precision)
+    X, stats = sys_.solve_batch(np.array(rhs), tol=1e-10, max_cycles=2000)
+    for i, st in enumerate(stats):
+        assert st["status"] == 0, st
+        assert st["true_rel_res"] <= 1e-10
+        assert _true(A, rhs[i], X[i]) <= 1.5e-10
+        assert _rel(X[i], direct[i]) < 1e-8
+    rel = sys_.true_residual(np.array(rhs), X)
+    assert np.all(rel <= 1.5e-10)
+
+
+def test_batch_result_is_the_same_alone_and_in_the_mix(c1):
+    """Continuous batching does not change answers beyond the tolerance: each
+    right-hand side solved alone equals its solution inside a mixed batch."""
+    A, rhs, cfg, direct = c1
+    batch = gdmr.System(A, cfg["m"], cfg["k"], capacity=4, precision="mixed")
+    Xb, _ = batch.solve_batch(np.array(rhs[:6]), tol=1e-10, max_cycles=2000)   # 6 > capacity: refills
+    for i in (0, 3, 5):
+        alone = gdmr.System(A, cfg["m"], cfg["k"], capacity=1, precision="mixed")
+        Xa, st = alone.solve_batch(np.array(rhs[i:i + 1]), tol=1e-10, max_cycles=2000)
+        assert st[0]["status"] == 0
+        # both are within the tolerance of the exact solution, hence of each other
+        assert _rel(Xa[0], Xb[i]) < 2e-8
+        assert _rel(Xb[i], direct[i]) < 1e-8
+
+
+def test_repeat_solves_are_bitwise_identical(c1):
+    A, rhs, cfg, direct = c1
+    xs = []
+    for _ in range(2):
+        s = gdmr.System(A, cfg["m"], cfg["k"], capacity=1, precision="fp64")
+        x, st = s.solve(rhs[1], mode=0, tol=1e-10, mat_rank=2000)
+        xs.append(x)
+    assert np.array_equal(xs[0], xs[1])
+
+
+def test_deflation_export_import_roundtrip(c1):
+    A, rhs, cfg, direct = c1
+    s1 = gdmr.System(A, cfg["m"], cfg["k"], capacity=1, precision="fp64")
+    s1.solve(rhs[0], mode=0, tol=1e-10, mat_rank=2000)
+    Z = s1.export_deflation()
+    assert np.allclose(np.linalg.norm(Z, axis=1), 1.0)
+    s2 = gdmr.System(A, cfg["m"], cfg["k"], capacity=1, precision="fp64")
+    s2.import_deflation(Z)
+    x1, st1 = s1.solve(rhs[1], mode=1, tol=1e-10, mat_rank=2000)
+    x2, st2 = s2.solve(rhs[1], mode=1, tol=1e-10, mat_rank=2000)
+    assert st1["cycles"] == st2["cycles"]
+    assert _rel(x1, x2) < 1e-12
+
+
+def test_initial_guess_within_tolerance_returns_absolute_norm(c1):
+    A, rhs, cfg, direct = c1
+    s = gdmr.System(A, cfg["m"], cfg["k"], capacity=1, precision="fp64")
+    x, st = s.solve(rhs[0], x0=direct[0], mode=0, tol=1e-6, mat_rank=10)
+    assert st["cycles"] == 0
+    assert st["rel_res"] < 1e-6 * np.linalg.norm(rhs[0])
+    assert np.array_equal(x, direct[0])
+
+
+def test_cycle_cap_reports_no_convergence(c1):
+    A, rhs, cfg, direct = c1
+    s = gdmr.System(A, cfg["m"], cfg["k"], capacity=1, precision="fp64")
+    x, st = s.solve(rhs[0], mode=0, tol=1e-10, mat_rank=3)
+    assert st["status"] == 3 and st["cycles"] == 4
+    assert "converge" in gdmr.last_error()
