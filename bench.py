@@ -210,6 +210,8 @@ def main():
     ap.add_argument("--cpu-cycles", type=int, default=3)
     ap.add_argument("--ref-cycles", type=int, default=2)
     ap.add_argument("--max-cycles", type=int, default=3000)
+    ap.add_argument("--solve-only", action="store_true",
+                    help="only the timed batched solves (for profiler captures); prints a short line")
     args = ap.parse_args()
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
@@ -260,6 +262,12 @@ def main():
     elapsed_ms = max_over_ranks(ev0.elapsed_time(ev1), world)
     value = world * nrhs * args.steps / (elapsed_ms / 1e3)
     clocks = clk.summary()
+    if args.solve_only:
+        if rank == 0:
+            print(json.dumps({"mode": "solve-only", "value": value, "unit": "solves/s", "nrhs": nrhs,
+                              "ms_per_step": elapsed_ms / args.steps, "verified": bool(verified),
+                              "gpu_launches": int(launches), "svd_sweeps": sysm.svd_sweeps()}), flush=True)
+        return
 
     # roofline: one more step with library-side CUDA events per kernel class
     gdmr.profile_reset()

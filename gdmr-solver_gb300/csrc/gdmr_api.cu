@@ -583,6 +583,11 @@ extern "C" long long gdmr_system_bytes(const gdmr_system *S) {
                        2 * sizeof(double2) * (size_t)S->n * std::max(S->cap, 2));
 }
 
+extern "C" int gdmr_system_svd_sweeps(const gdmr_system *S) {
+    if (!S) return 0;
+    return S->precision == 1 ? S->e32.last_svd_sweeps() : S->e64.last_svd_sweeps();
+}
+
 extern "C" int gdmr_solve(gdmr_system *S, int mode, const double *b, double *x, double tol, int matRank, int on_device,
                           gdmr_stats *stats) {
     if (!S || !b || !x) return fail(GDMR_EINVAL, "gdmr_solve", "null argument");

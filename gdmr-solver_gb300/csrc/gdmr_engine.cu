@@ -234,11 +234,11 @@ template <class R> int Engine<R>::init(int n, int m, int k, int capacity, int de
     A_(y_, sizeof(double2) * strideC() * capacity);
     A_(t_, sizeof(double2) * strideC() * capacity);
     A_(vs_, sizeof(double2) * (size_t)m * std::max(k, 1));
-    A_(svdwork_, sizeof(double2) * 2 * (size_t)m * (m + 1));
+    A_(svdwork_, sizeof(double2) * 3 * (size_t)m * (m + 1));
     A_(sigma_, sizeof(double) * m);
     A_(znorm2_, sizeof(double) * std::max(k, 1));
     A_(sweeps_, sizeof(int));
-    A_(partials_, sizeof(double) * scratch_doubles(qmax() + 16, capacity + 1));
+    A_(partials_, sizeof(double) * scratch_doubles(qmax() + 16, capacity + 1, n));
     A_(tickets_, sizeof(unsigned) * (capacity + 1));
     A_(state_, sizeof(SysState) * (capacity + 1));
     A_(act_, sizeof(int) * (capacity + 1));
@@ -272,7 +272,9 @@ template <class R> int Engine<R>::set_active(const std::vector<int> &act) {
 
 template <class R> int Engine<R>::read_state(int count) {
     GDMR_CK(cudaMemcpyAsync(hstate_, state_, sizeof(SysState) * count, cudaMemcpyDeviceToHost, stream));
+    if (k_ > 0) GDMR_CK(cudaMemcpyAsync(&hsweeps_, sweeps_, sizeof(int), cudaMemcpyDeviceToHost, stream));
     GDMR_CK(cudaStreamSynchronize(stream));
+    svd_sweeps_ = hsweeps_;
     if (profile_enabled()) profile_flush();
     return GDMR_OK;
 }

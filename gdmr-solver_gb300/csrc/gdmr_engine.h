@@ -117,6 +117,8 @@ template <class R> class Engine {
     // The reference keeps its stagnation counter across solves (gDMR.cu:2646-2655); reset on init.
     int flag_count() const { return flag_count_; }
 
+    // FP32 and FP64 Jacobi sweeps of the last deflation update (read after a cycle).
+    int last_svd_sweeps() const { return svd_sweeps_; }
     int n() const { return n_; }
     int m() const { return m_; }
     int k() const { return k_; }
@@ -152,6 +154,8 @@ template <class R> class Engine {
     SellMatrix A64_{};
     double2 *b64_ = nullptr, *x64_ = nullptr;
     int kk_prev_ = 0;
+    int svd_sweeps_ = 0;
+    int hsweeps_ = 0;
 
     size_t strideV() const { return (size_t)(m_ + 1) * n_; }
     size_t strideH() const { return (size_t)(m_ + 1) * m_; }

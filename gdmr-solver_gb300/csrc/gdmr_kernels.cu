@@ -48,6 +48,11 @@ __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
 
 // Block-wide sum of NV doubles per thread; result valid in thread 0.
 template <int NV> __device__ __forceinline__ void block_sum(double (&v)[NV], double (*red)[NW]) {
@@ -69,11 +74,11 @@ template <int NV> __device__ __forceinline__ void block_sum(double (&v)[NV], dou
 }
 
 // Last-CTA-done protocol: returns true in every thread of the CTA that arrived last.
-__device__ __forceinline__ bool arrive_last(unsigned *ticket) {
+__device__ __forceinline__ bool arrive_last(unsigned *ticket, unsigned count) {
     __shared__ unsigned s_last;
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) s_last = (atomicAdd(ticket, 1u) == gridDim.x - 1) ? 1u : 0u;
+    if (threadIdx.x == 0) s_last = (atomicAdd(ticket, 1u) == count - 1) ? 1u : 0u;
     __syncthreads();
     if (s_last) __threadfence();
     return s_last != 0;
@@ -105,10 +110,19 @@ int num_sms() {
 
 template <class R> __host__ __device__ constexpr int ept() { return sizeof(R) == 4 ? 8 : 4; }
 
-template <class R> int red_grid(int n, int nsys) {
+// Chunks of NT*EPT elements: the per-system grid dimension of the projection, update and
+// combination kernels (one chunk per CTA).  The system index is the fastest grid index, so
+// the CTAs that read the same chunk of the shared vectors (W, Z) run together and the
+// shared data comes from HBM once and from L2 for the other systems.
+template <class R> int nchunks(int n) {
     const int ch = NT * ept<R>();
-    int chunks = (n + ch - 1) / ch;
-    int target = (num_sms() * 2 + nsys - 1) / (nsys > 0 ? nsys : 1);
+    int c = (n + ch - 1) / ch;
+    return c > 0 ? c : 1;
+}
+// Capped per-system grid for the grid-stride kernels (norms, FP64 residual).
+int capped_grid(int n, int nsys, int per_sm) {
+    int chunks = (n + NT - 1) / NT;
+    int target = (num_sms() * per_sm + nsys - 1) / (nsys > 0 ? nsys : 1);
     if (target < 1) target = 1;
     return chunks < target ? (chunks > 0 ? chunks : 1) : target;
 }
@@ -159,6 +173,8 @@ __device__ void run_finish(const FinishArgs &f, int s, SysState &st, double n2, 
 
 // ----------------------------------------------------------------- multi-dot
 // coef_s[p] = <B_p, w_s> for B = [segA (qa vectors) | segB_s (qb vectors)].
+// Grid (systems, chunks); one chunk of NT*EPT elements per CTA, w in registers,
+// PU basis vectors in flight per thread, warp reductions in the working precision.
 template <class R, int PU>
 __global__ void __launch_bounds__(NT) k_mdot(int n, const typename CT<R>::t *__restrict__ segA, int qa,
                                              const typename CT<R>::t *__restrict__ segB0, size_t strideB, int qb,
@@ -168,46 +184,39 @@ __global__ void __launch_bounds__(NT) k_mdot(int n, const typename CT<R>::t *__r
                                              SysState *state, int skip_broken) {
     using C = typename CT<R>::t;
     constexpr int EPT = ept<R>();
-    const int slot = blockIdx.y, s = act[slot];
+    const int slot = blockIdx.x, s = act[slot], chunk = blockIdx.y, G = gridDim.y;
     if (skip_broken && state[s].broken) return;
     const C *segB = segB0 + (size_t)s * strideB;
     const C *w = w0 + (size_t)s * strideW;
-    const int q = qa + qb, G = gridDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    __shared__ double2 wsum[NW][QMAX];
-    __shared__ double red[2][NW];
-    for (int i = tid; i < NW * QMAX; i += NT) wsum[i / QMAX][i % QMAX] = make_double2(0, 0);
-    __syncthreads();
-    const long CH = (long)NT * EPT;
-    for (long c0 = (long)blockIdx.x * CH; c0 < n; c0 += (long)G * CH) {
-        C wv[EPT];
+    const int q = qa + qb, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __shared__ C wsum[NW][QMAX];
+    const long c0 = (long)chunk * NT * EPT;
+    C wv[EPT];
 #pragma unroll
-        for (int e = 0; e < EPT; ++e) {
-            long i = c0 + tid + (long)e * NT;
-            wv[e] = i < n ? w[i] : czero<C>();
+    for (int e = 0; e < EPT; ++e) {
+        long i = c0 + tid + (long)e * NT;
+        wv[e] = i < n ? w[i] : czero<C>();
+    }
+    for (int p0 = 0; p0 < q; p0 += PU) {
+        C vv[PU][EPT];
+#pragma unroll
+        for (int u = 0; u < PU; ++u) {
+            const int p = p0 + u;
+            const C *vp = p < qa ? segA + (size_t)p * n : segB + (size_t)(p - qa) * n;
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) {
+                long i = c0 + tid + (long)e * NT;
+                vv[u][e] = (p < q && i < n) ? vp[i] : czero<C>();
+            }
         }
-        for (int p0 = 0; p0 < q; p0 += PU) {
-            C vv[PU][EPT];
 #pragma unroll
-            for (int u = 0; u < PU; ++u) {
-                const int p = p0 + u;
-                const C *vp = p < qa ? segA + (size_t)p * n : segB + (size_t)(p - qa) * n;
+        for (int u = 0; u < PU; ++u) {
+            C a = czero<C>();
 #pragma unroll
-                for (int e = 0; e < EPT; ++e) {
-                    long i = c0 + tid + (long)e * NT;
-                    vv[u][e] = (p < q && i < n) ? vp[i] : czero<C>();
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < PU; ++u) {
-                C a = czero<C>();
-#pragma unroll
-                for (int e = 0; e < EPT; ++e) cdotacc(a, vv[u][e], wv[e]);
-                double re = warp_sum((double)a.x), im = warp_sum((double)a.y);
-                if (lane == 0 && p0 + u < q) {
-                    wsum[warp][p0 + u].x += re;
-                    wsum[warp][p0 + u].y += im;
-                }
-            }
+            for (int e = 0; e < EPT; ++e) cdotacc(a, vv[u][e], wv[e]);
+            a.x = warp_sum(a.x);
+            a.y = warp_sum(a.y);
+            if (lane == 0 && p0 + u < q) wsum[warp][p0 + u] = a;
         }
     }
     __syncthreads();
@@ -215,13 +224,13 @@ __global__ void __launch_bounds__(NT) k_mdot(int n, const typename CT<R>::t *__r
     for (int p = tid; p < q; p += NT) {
         double re = 0, im = 0;
 #pragma unroll
-        for (int ww = 0; ww < NW; ++ww) { re += wsum[ww][p].x; im += wsum[ww][p].y; }
+        for (int ww = 0; ww < NW; ++ww) { re += (double)wsum[ww][p].x; im += (double)wsum[ww][p].y; }
         double *pp = part + (size_t)p * 2 * G;
-        pp[blockIdx.x] = re;
-        pp[G + blockIdx.x] = im;
+        pp[chunk] = re;
+        pp[G + chunk] = im;
     }
-    if (!arrive_last(&tickets[slot])) return;
-    // one warp per coefficient, lanes stride over the G partials
+    if (!arrive_last(&tickets[slot], G)) return;
+    // one warp per coefficient, lanes stride over the G partials (fixed order)
     double2 *coef = coef0 + (size_t)s * strideC;
     for (int p = warp; p < q; p += NW) {
         const double *pp = part + (size_t)p * 2 * G;
@@ -232,7 +241,6 @@ __global__ void __launch_bounds__(NT) k_mdot(int n, const typename CT<R>::t *__r
         if (lane == 0) coef[p] = make_double2(re, im);
     }
     if (tid == 0) tickets[slot] = 0;
-    (void)red;
 }
 
 // ----------------------------------------------------------------- update + norms
@@ -246,69 +254,63 @@ __global__ void __launch_bounds__(NT) k_update(int n, const typename CT<R>::t *_
                                                SysState *state, FinishArgs fin, int skip_broken) {
     using C = typename CT<R>::t;
     constexpr int EPT = ept<R>();
-    const int slot = blockIdx.y, s = act[slot];
+    const int slot = blockIdx.x, s = act[slot], chunk = blockIdx.y, G = gridDim.y;
     if (skip_broken && state[s].broken) return;
     const C *segB = segB0 + (size_t)s * strideB;
     const C *w = w0 + (size_t)s * strideW;
     C *out = out0 + (size_t)s * strideO;
-    const int q = qa + qb, G = gridDim.x, tid = threadIdx.x;
+    const int q = qa + qb, tid = threadIdx.x;
     __shared__ C cs[QMAX];
     __shared__ double red[3][NW];
     const double2 *coef = coef0 + (size_t)s * strideC;
     for (int p = tid; p < q; p += NT) cs[p] = from_d<C>(coef[p]);
     __syncthreads();
-    double n2 = 0, cre = 0, cim = 0;
-    const long CH = (long)NT * EPT;
-    for (long c0 = (long)blockIdx.x * CH; c0 < n; c0 += (long)G * CH) {
-        C acc[EPT], org[EPT];
+    const long c0 = (long)chunk * NT * EPT;
+    C acc[EPT], org[EPT];
 #pragma unroll
-        for (int e = 0; e < EPT; ++e) {
-            long i = c0 + tid + (long)e * NT;
-            org[e] = i < n ? w[i] : czero<C>();
-            acc[e] = org[e];
-        }
-        for (int p0 = 0; p0 < q; p0 += PU) {
-            C vv[PU][EPT];
-#pragma unroll
-            for (int u = 0; u < PU; ++u) {
-                const int p = p0 + u;
-                const C *vp = p < qa ? segA + (size_t)p * n : segB + (size_t)(p - qa) * n;
-#pragma unroll
-                for (int e = 0; e < EPT; ++e) {
-                    long i = c0 + tid + (long)e * NT;
-                    vv[u][e] = (p < q && i < n) ? vp[i] : czero<C>();
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < PU; ++u) {
-                if (p0 + u < q) {
-                    const C c = cs[p0 + u];
-#pragma unroll
-                    for (int e = 0; e < EPT; ++e) cfms(acc[e], c, vv[u][e]);
-                }
-            }
-        }
-        C ln = czero<C>(), lc = czero<C>();
-#pragma unroll
-        for (int e = 0; e < EPT; ++e) {
-            long i = c0 + tid + (long)e * NT;
-            if (i < n) out[i] = acc[e];
-            cdotacc(ln, acc[e], acc[e]);
-            cdotacc(lc, acc[e], org[e]);
-        }
-        n2 += ln.x;
-        cre += lc.x;
-        cim += lc.y;
+    for (int e = 0; e < EPT; ++e) {
+        long i = c0 + tid + (long)e * NT;
+        org[e] = i < n ? w[i] : czero<C>();
+        acc[e] = org[e];
     }
-    double v[3] = {n2, cre, cim};
+    for (int p0 = 0; p0 < q; p0 += PU) {
+        C vv[PU][EPT];
+#pragma unroll
+        for (int u = 0; u < PU; ++u) {
+            const int p = p0 + u;
+            const C *vp = p < qa ? segA + (size_t)p * n : segB + (size_t)(p - qa) * n;
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) {
+                long i = c0 + tid + (long)e * NT;
+                vv[u][e] = (p < q && i < n) ? vp[i] : czero<C>();
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < PU; ++u) {
+            if (p0 + u < q) {
+                const C c = cs[p0 + u];
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) cfms(acc[e], c, vv[u][e]);
+            }
+        }
+    }
+    C ln = czero<C>(), lc = czero<C>();
+#pragma unroll
+    for (int e = 0; e < EPT; ++e) {
+        long i = c0 + tid + (long)e * NT;
+        if (i < n) out[i] = acc[e];
+        cdotacc(ln, acc[e], acc[e]);
+        cdotacc(lc, acc[e], org[e]);
+    }
+    double v[3] = {(double)ln.x, (double)lc.x, (double)lc.y};
     block_sum<3>(v, red);
     double *part = (double *)partials + (size_t)slot * 3 * G;
     if (tid == 0) {
-        part[blockIdx.x] = v[0];
-        part[G + blockIdx.x] = v[1];
-        part[2 * G + blockIdx.x] = v[2];
+        part[chunk] = v[0];
+        part[G + chunk] = v[1];
+        part[2 * G + chunk] = v[2];
     }
-    if (!arrive_last(&tickets[slot])) return;
+    if (!arrive_last(&tickets[slot], G)) return;
     double tot[3];
     __syncthreads();
     sum_partials<3>(part, G, tot, red);
@@ -354,11 +356,11 @@ __global__ void __launch_bounds__(NT) k_combine(int n, int kk, int m, const type
                                                 double2 *__restrict__ partials, unsigned *tickets, SysState *state) {
     using C = typename CT<R>::t;
     constexpr int EPT = ept<R>();
-    const int slot = blockIdx.y, s = act[slot];
+    const int slot = blockIdx.x, s = act[slot], chunk = blockIdx.y, G = gridDim.y;
     const C *V = V0 + (size_t)s * strideV;
     C *r = r0 + (size_t)s * strideR;
     C *x = x0 + (size_t)s * strideX;
-    const int G = gridDim.x, tid = threadIdx.x;
+    const int tid = threadIdx.x;
     __shared__ C ts[QMAX], ys[QMAX];
     __shared__ double red[1][NW];
     const R ra = (R)state[s].rho_abs;
@@ -370,59 +372,55 @@ __global__ void __launch_bounds__(NT) k_combine(int n, int kk, int m, const type
         ys[p] = yy;
     }
     __syncthreads();
-    double n2 = 0;
-    const long CH = (long)NT * EPT;
-    for (long c0 = (long)blockIdx.x * CH; c0 < n; c0 += (long)G * CH) {
-        C ra_[EPT], xa[EPT];
+    const long c0 = (long)chunk * NT * EPT;
+    C ra_[EPT], xa[EPT];
 #pragma unroll
-        for (int e = 0; e < EPT; ++e) {
-            long i = c0 + tid + (long)e * NT;
-            ra_[e] = i < n ? r[i] : czero<C>();
-            xa[e] = i < n ? x[i] : czero<C>();
-        }
-        for (int p = 0; p < kk; ++p) {
-            const C tc = ts[p], yc = ys[p];
-            const C *wp = W + (size_t)p * n;
-            const C *zp = Z + (size_t)p * n;
-#pragma unroll
-            for (int e = 0; e < EPT; ++e) {
-                long i = c0 + tid + (long)e * NT;
-                if (i < n) {
-                    cfms(ra_[e], tc, wp[i]);
-                    cfma(xa[e], yc, zp[i]);
-                }
-            }
-        }
-        for (int p = 0; p <= m - kk; ++p) {
-            const C tc = ts[kk + p], yc = ys[kk + p];   // ys[m] = 0: the last Krylov vector is target-side only
-            const C *vp = V + (size_t)p * n;
-#pragma unroll
-            for (int e = 0; e < EPT; ++e) {
-                long i = c0 + tid + (long)e * NT;
-                if (i < n) {
-                    const C vv = vp[i];
-                    cfms(ra_[e], tc, vv);
-                    cfma(xa[e], yc, vv);
-                }
-            }
-        }
-        C ln = czero<C>();
+    for (int e = 0; e < EPT; ++e) {
+        long i = c0 + tid + (long)e * NT;
+        ra_[e] = i < n ? r[i] : czero<C>();
+        xa[e] = i < n ? x[i] : czero<C>();
+    }
+    for (int p = 0; p < kk; ++p) {
+        const C tc = ts[p], yc = ys[p];
+        const C *wp = W + (size_t)p * n;
+        const C *zp = Z + (size_t)p * n;
 #pragma unroll
         for (int e = 0; e < EPT; ++e) {
             long i = c0 + tid + (long)e * NT;
             if (i < n) {
-                r[i] = ra_[e];
-                x[i] = xa[e];
+                cfms(ra_[e], tc, wp[i]);
+                cfma(xa[e], yc, zp[i]);
             }
-            cdotacc(ln, ra_[e], ra_[e]);
         }
-        n2 += ln.x;
     }
-    double v[1] = {n2};
+    for (int p = 0; p <= m - kk; ++p) {
+        const C tc = ts[kk + p], yc = ys[kk + p];   // ys[m] = 0: the last Krylov vector is target-side only
+        const C *vp = V + (size_t)p * n;
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            long i = c0 + tid + (long)e * NT;
+            if (i < n) {
+                const C vv = vp[i];
+                cfms(ra_[e], tc, vv);
+                cfma(xa[e], yc, vv);
+            }
+        }
+    }
+    C ln = czero<C>();
+#pragma unroll
+    for (int e = 0; e < EPT; ++e) {
+        long i = c0 + tid + (long)e * NT;
+        if (i < n) {
+            r[i] = ra_[e];
+            x[i] = xa[e];
+        }
+        cdotacc(ln, ra_[e], ra_[e]);
+    }
+    double v[1] = {(double)ln.x};
     block_sum<1>(v, red);
     double *part = (double *)partials + (size_t)slot * G;
-    if (tid == 0) part[blockIdx.x] = v[0];
-    if (!arrive_last(&tickets[slot])) return;
+    if (tid == 0) part[chunk] = v[0];
+    if (!arrive_last(&tickets[slot], G)) return;
     double tot[1];
     __syncthreads();
     sum_partials<1>(part, G, tot, red);
@@ -472,7 +470,7 @@ __global__ void __launch_bounds__(NT) k_zupdate(int n, int kk, int m, int k, int
     double *part = (double *)partials;
     if (tid == 0)
         for (int t = 0; t < nt; ++t) part[(size_t)t * G + blockIdx.x] = nrm[t];
-    if (!arrive_last(ticket)) return;
+    if (!arrive_last(ticket, gridDim.x)) return;
     __syncthreads();
     double tot[KB];
 #pragma unroll
@@ -589,112 +587,238 @@ __global__ void __launch_bounds__(128) k_ls(int m, const double2 *__restrict__ H
     }
 }
 
-// ----------------------------------------------------------------- SVD (FP64 one-sided Jacobi)
-// A: (m+1) x m working copy (ld m+1), V: m x m, both in shared memory when they
-// fit, else in global scratch.  Round-robin ("circle") ordering of disjoint pairs,
-// one warp per pair.  Column norms are kept incrementally.
-__global__ void __launch_bounds__(512) k_svd(int m, int k, const double2 *__restrict__ H, double2 *__restrict__ vs,
-                                             double *__restrict__ sigma, double2 *__restrict__ gwork, int use_smem,
-                                             int *sweeps_out) {
-    extern __shared__ double2 sm[];
+// ----------------------------------------------------------------- SVD (one-sided Jacobi, FP32 then FP64)
+// Right singular vectors of H ((m+1) x m) by one-sided Jacobi (Hestenes 1958) with the
+// round-robin ("circle") ordering of disjoint column pairs:
+//   1. FP32 sweeps to FP32 convergence (cheap: GB300 issues FP32 at ~64x its FP64 rate);
+//   2. FP64: V re-orthonormalised by two passes of Gram-Schmidt, A = H V;
+//   3. FP64 sweeps to FP64 convergence (typically one or two).
+// In FP64 the scalar rotation parameters of a round are computed one pair per lane of
+// warp 0, so a round pays for them once instead of once per pair in every lane.
+template <class T> struct CX;
+template <> struct CX<float> { using t = float2; };
+template <> struct CX<double> { using t = double2; };
+
+// Pair of slot pi in round r of the circle method over mm (even) slots.
+__device__ __forceinline__ void circle_pair(int r, int pi, int mm, int &p, int &q) {
+    auto pos = [&](int i) { return i == 0 ? 0 : 1 + ((i - 1 + r) % (mm - 1)); };
+    p = pos(pi);
+    q = pos(mm - 1 - pi);
+}
+
+template <class T>
+__device__ int jacobi_sweeps(int m, typename CX<T>::t *A, typename CX<T>::t *V, T *nrm, double2 *rot, T tol,
+                             int max_sweeps, int *s_flag) {
+    using C = typename CX<T>::t;
     const int rows = m + 1, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
-    double2 *A = use_smem ? sm : gwork;
-    double2 *V = A + (size_t)rows * m;
-    __shared__ double nrm[168];
-    __shared__ int perm[168];
-    __shared__ int s_rot;
-    for (int i = tid; i < rows * m; i += blockDim.x) A[i] = H[i];
-    for (int i = tid; i < m * m; i += blockDim.x) V[i] = make_double2((i % m) == (i / m) ? 1.0 : 0.0, 0.0);
-    __syncthreads();
-    for (int c = warp; c < m; c += nwarps) {
-        double a = 0;
-        for (int r = lane; r < rows; r += 32) { double2 v = A[(size_t)c * rows + r]; a += v.x * v.x + v.y * v.y; }
-        a = warp_sum(a);
-        if (lane == 0) nrm[c] = a;
-    }
-    const int mm = m + (m & 1);          // even number of slots (slot m is a dummy when m is odd)
-    for (int i = tid; i < mm; i += blockDim.x) perm[i] = i;
-    __syncthreads();
-    const double eps = 1e-15;
+    const int mm = m + (m & 1), npairs = mm / 2;
     int sweep = 0;
-    for (; sweep < 60; ++sweep) {
-        if (tid == 0) s_rot = 0;
+    for (; sweep < max_sweeps; ++sweep) {
+        for (int c = warp; c < m; c += nwarps) {   // column norms, refreshed every sweep
+            T a = 0;
+            for (int r = lane; r < rows; r += 32) { C v = A[(size_t)c * rows + r]; a += v.x * v.x + v.y * v.y; }
+            a = warp_sum(a);
+            if (lane == 0) nrm[c] = a;
+        }
+        if (tid == 0) *s_flag = 0;
         __syncthreads();
         for (int round = 0; round < mm - 1; ++round) {
-            for (int pi = warp; pi < mm / 2; pi += nwarps) {
-                int p = perm[pi], q = perm[mm - 1 - pi];
-                if (p >= m || q >= m) continue;
-                if (p > q) { int t = p; p = q; q = t; }
-                double gr = 0, gi = 0;
+            // (1) gamma of every pair, one warp per pair
+            for (int pi = warp; pi < npairs; pi += nwarps) {
+                int p, q;
+                circle_pair(round, pi, mm, p, q);
+                if (p >= m || q >= m) { if (lane == 0) rot[pi] = make_double2(0, 0); continue; }
+                T gr = 0, gi = 0;
                 for (int r = lane; r < rows; r += 32) {
-                    double2 ap = A[(size_t)p * rows + r], aq = A[(size_t)q * rows + r];
+                    C ap = A[(size_t)p * rows + r], aq = A[(size_t)q * rows + r];
                     gr += ap.x * aq.x + ap.y * aq.y;
                     gi += ap.x * aq.y - ap.y * aq.x;
                 }
                 gr = warp_sum(gr);
                 gi = warp_sum(gi);
-                const double a = nrm[p], b = nrm[q];
-                const double ag = hypot(gr, gi);
-                if (ag == 0.0 || ag <= eps * sqrt(a * b)) continue;
-                if (lane == 0) s_rot = 1;
-                const double phr = gr / ag, phi = -gi / ag;    // e^{-i phi}
-                const double zeta = (b - a) / (2.0 * ag);
-                const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                const double c = 1.0 / sqrt(1.0 + t * t), sn = c * t;
+                if (lane == 0) rot[pi] = make_double2((double)gr, (double)gi);
+            }
+            __syncthreads();
+            // (2) rotation parameters, one pair per lane: rot[pi] <- (c, t) and phase in rot[npairs+pi]
+            for (int pi = tid; pi < npairs; pi += blockDim.x) {
+                int p, q;
+                circle_pair(round, pi, mm, p, q);
+                const double2 gd = rot[pi];
+                T gx = (T)gd.x, gy = (T)gd.y;
+                T cc = 1, tt = 0, phr = 1, phi = 0;
+                if (p < m && q < m) {
+                    const T a = nrm[p < q ? p : q], b = nrm[p < q ? q : p];
+                    if (p > q) gy = -gy;                    // gamma for the ordered pair (min, max)
+                    const T ag = sqrt(gx * gx + gy * gy);
+                    if (ag > (T)0 && ag > tol * sqrt(a * b)) {
+                        *s_flag = 1;
+                        phr = gx / ag;
+                        phi = -gy / ag;
+                        const T zeta = (b - a) / ((T)2 * ag);
+                        tt = ((zeta >= (T)0) ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
+                        cc = (T)1 / sqrt((T)1 + tt * tt);
+                    }
+                }
+                rot[pi] = make_double2((double)cc, (double)tt);
+                rot[npairs + pi] = make_double2((double)phr, (double)phi);
+            }
+            __syncthreads();
+            // (3) apply: one warp per pair, columns (min, max) of A and V
+            for (int pi = warp; pi < npairs; pi += nwarps) {
+                int p, q;
+                circle_pair(round, pi, mm, p, q);
+                if (p >= m || q >= m) continue;
+                if (p > q) { int t = p; p = q; q = t; }
+                const double2 ct = rot[pi];
+                if (ct.y == 0.0) continue;
+                const double2 ph = rot[npairs + pi];
+                const T c = (T)ct.x, sn = (T)(ct.x * ct.y), pr = (T)ph.x, pim = (T)ph.y;
                 for (int r = lane; r < rows; r += 32) {
-                    double2 ap = A[(size_t)p * rows + r], aq0 = A[(size_t)q * rows + r];
-                    double2 aq = make_double2(aq0.x * phr - aq0.y * phi, aq0.x * phi + aq0.y * phr);
-                    A[(size_t)p * rows + r] = make_double2(c * ap.x - sn * aq.x, c * ap.y - sn * aq.y);
-                    A[(size_t)q * rows + r] = make_double2(sn * ap.x + c * aq.x, sn * ap.y + c * aq.y);
+                    C ap = A[(size_t)p * rows + r], aq0 = A[(size_t)q * rows + r];
+                    C aq;
+                    aq.x = aq0.x * pr - aq0.y * pim;
+                    aq.y = aq0.x * pim + aq0.y * pr;
+                    C np_, nq_;
+                    np_.x = c * ap.x - sn * aq.x; np_.y = c * ap.y - sn * aq.y;
+                    nq_.x = sn * ap.x + c * aq.x; nq_.y = sn * ap.y + c * aq.y;
+                    A[(size_t)p * rows + r] = np_;
+                    A[(size_t)q * rows + r] = nq_;
                 }
                 for (int r = lane; r < m; r += 32) {
-                    double2 vp = V[(size_t)p * m + r], vq0 = V[(size_t)q * m + r];
-                    double2 vq = make_double2(vq0.x * phr - vq0.y * phi, vq0.x * phi + vq0.y * phr);
-                    V[(size_t)p * m + r] = make_double2(c * vp.x - sn * vq.x, c * vp.y - sn * vq.y);
-                    V[(size_t)q * m + r] = make_double2(sn * vp.x + c * vq.x, sn * vp.y + c * vq.y);
-                }
-                if (lane == 0) {
-                    nrm[p] = a - t * ag;
-                    nrm[q] = b + t * ag;
+                    C vp = V[(size_t)p * m + r], vq0 = V[(size_t)q * m + r];
+                    C vq;
+                    vq.x = vq0.x * pr - vq0.y * pim;
+                    vq.y = vq0.x * pim + vq0.y * pr;
+                    C np_, nq_;
+                    np_.x = c * vp.x - sn * vq.x; np_.y = c * vp.y - sn * vq.y;
+                    nq_.x = sn * vp.x + c * vq.x; nq_.y = sn * vp.y + c * vq.y;
+                    V[(size_t)p * m + r] = np_;
+                    V[(size_t)q * m + r] = nq_;
                 }
             }
             __syncthreads();
-            // rotate the circle: slot 0 fixed, others shift by one
-            if (tid == 0) {
-                int last = perm[mm - 1];
-                for (int i = mm - 1; i > 1; --i) perm[i] = perm[i - 1];
-                perm[1] = last;
+            // norms of the rotated columns (exact recomputation keeps the next round consistent)
+            for (int pi = warp; pi < npairs; pi += nwarps) {
+                int p, q;
+                circle_pair(round, pi, mm, p, q);
+                if (p >= m || q >= m || rot[pi].y == 0.0) continue;
+                T a = 0, b = 0;
+                for (int r = lane; r < rows; r += 32) {
+                    C ap = A[(size_t)p * rows + r], aq = A[(size_t)q * rows + r];
+                    a += ap.x * ap.x + ap.y * ap.y;
+                    b += aq.x * aq.x + aq.y * aq.y;
+                }
+                a = warp_sum(a);
+                b = warp_sum(b);
+                if (lane == 0) { nrm[p] = a; nrm[q] = b; }
             }
             __syncthreads();
         }
-        // refresh norms from the columns (the incremental update drifts)
-        for (int c = warp; c < m; c += nwarps) {
-            double a = 0;
-            for (int r = lane; r < rows; r += 32) { double2 v = A[(size_t)c * rows + r]; a += v.x * v.x + v.y * v.y; }
-            a = warp_sum(a);
-            if (lane == 0) nrm[c] = a;
-        }
-        __syncthreads();
-        if (!s_rot) break;
+        if (!*s_flag) break;
         __syncthreads();
     }
+    return sweep + 1;
+}
+
+__global__ void __launch_bounds__(1024) k_svd(int m, int k, const double2 *__restrict__ H, double2 *__restrict__ vs,
+                                              double *__restrict__ sigma, double2 *__restrict__ gwork, int use_smem,
+                                              int *sweeps_out) {
+    extern __shared__ __align__(16) unsigned char svd_sm[];
+    const int rows = m + 1, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    unsigned char *base = use_smem ? svd_sm : (unsigned char *)gwork;
+    double2 *A64 = (double2 *)base;
+    double2 *V64 = A64 + (size_t)rows * m;
+    float2 *A32 = (float2 *)(V64 + (size_t)m * m);
+    float2 *V32 = A32 + (size_t)rows * m;
+    __shared__ double nrm64[168];
+    __shared__ float nrm32[168];
+    __shared__ double2 rot[2 * 84];
+    __shared__ int s_flag;
+    for (int i = tid; i < rows * m; i += blockDim.x) A32[i] = make_float2((float)H[i].x, (float)H[i].y);
+    for (int i = tid; i < m * m; i += blockDim.x) V32[i] = make_float2((i % m) == (i / m) ? 1.f : 0.f, 0.f);
+    __syncthreads();
+    const int s32 = jacobi_sweeps<float>(m, A32, V32, nrm32, rot, 4.0f * 1.1920929e-7f * m, 40, &s_flag);
+    // V64 = orthonormalised V32 (two passes of classical Gram-Schmidt, one warp per column dot)
+    for (int i = tid; i < m * m; i += blockDim.x) V64[i] = make_double2(V32[i].x, V32[i].y);
+    __syncthreads();
+    for (int c = 0; c < m; ++c) {
+        for (int pass = 0; pass < 2; ++pass) {
+            // coefficients against columns < c, one warp per earlier column
+            for (int j = warp; j < c; j += nwarps) {
+                double gr = 0, gi = 0;
+                for (int r = lane; r < m; r += 32) {
+                    double2 a = V64[(size_t)j * m + r], b = V64[(size_t)c * m + r];
+                    gr += a.x * b.x + a.y * b.y;
+                    gi += a.x * b.y - a.y * b.x;
+                }
+                gr = warp_sum(gr);
+                gi = warp_sum(gi);
+                if (lane == 0) rot[j] = make_double2(gr, gi);
+            }
+            __syncthreads();
+            for (int r = tid; r < m; r += blockDim.x) {
+                double2 v = V64[(size_t)c * m + r];
+                for (int j = 0; j < c; ++j) {
+                    const double2 g = rot[j], a = V64[(size_t)j * m + r];
+                    v.x -= g.x * a.x - g.y * a.y;
+                    v.y -= g.x * a.y + g.y * a.x;
+                }
+                V64[(size_t)c * m + r] = v;
+            }
+            __syncthreads();
+        }
+        if (warp == 0) {
+            double nn = 0;
+            for (int r = lane; r < m; r += 32) { double2 v = V64[(size_t)c * m + r]; nn += v.x * v.x + v.y * v.y; }
+            nn = warp_sum(nn);
+            if (lane == 0) nrm64[0] = 1.0 / sqrt(nn);
+        }
+        __syncthreads();
+        for (int r = tid; r < m; r += blockDim.x) {
+            double2 v = V64[(size_t)c * m + r];
+            V64[(size_t)c * m + r] = make_double2(v.x * nrm64[0], v.y * nrm64[0]);
+        }
+        __syncthreads();
+    }
+    // A64 = H V64
+    for (int i = tid; i < rows * m; i += blockDim.x) {
+        const int r = i % rows, c = i / rows;
+        double2 acc = make_double2(0, 0);
+        for (int p = 0; p < m; ++p) {
+            const double2 h = H[(size_t)p * rows + r], v = V64[(size_t)c * m + p];
+            acc.x += h.x * v.x - h.y * v.y;
+            acc.y += h.x * v.y + h.y * v.x;
+        }
+        A64[i] = acc;
+    }
+    __syncthreads();
+    const int s64 = jacobi_sweeps<double>(m, A64, V64, nrm64, rot, 4.0 * 2.220446049250313e-16 * m, 20, &s_flag);
+    for (int c = warp; c < m; c += nwarps) {
+        double a = 0;
+        for (int r = lane; r < rows; r += 32) { double2 v = A64[(size_t)c * rows + r]; a += v.x * v.x + v.y * v.y; }
+        a = warp_sum(a);
+        if (lane == 0) nrm64[c] = a;
+    }
+    __syncthreads();
     // rank in descending order (ties broken by column index)
     for (int c = tid; c < m; c += blockDim.x) {
-        const double sc = nrm[c];
+        const double sc = nrm64[c];
         int rank = 0;
         for (int c2 = 0; c2 < m; ++c2) {
-            const double s2 = nrm[c2];
+            const double s2 = nrm64[c2];
             rank += (s2 > sc) || (s2 == sc && c2 < c);
         }
         sigma[rank] = sqrt(sc);
         const int t = rank - (m - k);
         if (t >= 0)
-            for (int r = 0; r < m; ++r) vs[(size_t)t * m + r] = V[(size_t)c * m + r];
+            for (int r = 0; r < m; ++r) vs[(size_t)t * m + r] = V64[(size_t)c * m + r];
     }
-    if (tid == 0 && sweeps_out) *sweeps_out = sweep + 1;
+    if (tid == 0 && sweeps_out) *sweeps_out = s32 * 1000 + s64;
 }
 
 // ----------------------------------------------------------------- SELL-32 SpMM
+// Grid (system groups, row chunks): the groups of one row chunk run together, so the
+// matrix slice is read from HBM once and from L2 for the other groups.
 template <class R, int SG>
 __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slice_ptr, const int *__restrict__ cols,
                                              const typename CT<R>::t *__restrict__ vals,
@@ -702,20 +826,20 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
                                              typename CT<R>::t *__restrict__ y0, size_t strideY,
                                              const int *__restrict__ act, int nsys) {
     using C = typename CT<R>::t;
-    const int row = blockIdx.x * NT + threadIdx.x;
-    if (row >= n) return;
-    const int slice = row >> 5, lane = row & 31;
-    const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
-    const int g0 = blockIdx.y * SG;
-    for (int g = 0; g < SG && g0 + g < nsys; ++g) {
-        const int s = act[g0 + g];
-        const C *x = x0 + (size_t)s * strideX;
-        C acc = czero<C>();
-        for (int c = 0; c < width; ++c) {
-            const int e = beg + c * 32 + lane;
-            cfma(acc, vals[e], x[cols[e]]);
+    const int g0 = blockIdx.x * SG;
+    for (long row = (long)blockIdx.y * NT + threadIdx.x; row < n; row += (long)gridDim.y * NT) {
+        const int slice = (int)(row >> 5), lane = (int)(row & 31);
+        const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
+        for (int g = 0; g < SG && g0 + g < nsys; ++g) {
+            const int s = act[g0 + g];
+            const C *x = x0 + (size_t)s * strideX;
+            C acc = czero<C>();
+            for (int c = 0; c < width; ++c) {
+                const int e = beg + c * 32 + lane;
+                cfma(acc, vals[e], x[cols[e]]);
+            }
+            y0[(size_t)s * strideY + row] = acc;
         }
-        y0[(size_t)s * strideY + row] = acc;
     }
 }
 
@@ -725,13 +849,13 @@ __global__ void __launch_bounds__(NT) k_residual64(int n, const int *__restrict_
                                                    size_t strideB, const double2 *__restrict__ x0, size_t strideX,
                                                    double2 *__restrict__ r0, size_t strideR, const int *__restrict__ act,
                                                    double2 *__restrict__ partials, unsigned *tickets, SysState *state) {
-    const int slot = blockIdx.y, s = act[slot], G = gridDim.x, tid = threadIdx.x;
+    const int slot = blockIdx.x, s = act[slot], G = gridDim.y, tid = threadIdx.x;
     const double2 *b = b0 + (size_t)s * strideB;
     const double2 *x = x0 + (size_t)s * strideX;
     double2 *r = r0 + (size_t)s * strideR;
     __shared__ double red[1][NW];
     double n2 = 0;
-    for (int row = blockIdx.x * NT + tid; row < n; row += G * NT) {
+    for (int row = blockIdx.y * NT + tid; row < n; row += G * NT) {
         const int slice = row >> 5, lane = row & 31;
         const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
         double2 acc = b[row];
@@ -745,8 +869,8 @@ __global__ void __launch_bounds__(NT) k_residual64(int n, const int *__restrict_
     double v[1] = {n2};
     block_sum<1>(v, red);
     double *part = (double *)partials + (size_t)slot * G;
-    if (tid == 0) part[blockIdx.x] = v[0];
-    if (!arrive_last(&tickets[slot])) return;
+    if (tid == 0) part[blockIdx.y] = v[0];
+    if (!arrive_last(&tickets[slot], G)) return;
     double tot[1];
     __syncthreads();
     sum_partials<1>(part, G, tot, red);
@@ -825,19 +949,19 @@ __global__ void __launch_bounds__(NT) k_norm(int n, const typename CT<R>::t *__r
                                              const int *__restrict__ act, double2 *__restrict__ partials,
                                              unsigned *tickets, SysState *state, int mode) {
     using C = typename CT<R>::t;
-    const int slot = blockIdx.y, s = act[slot], G = gridDim.x, tid = threadIdx.x;
+    const int slot = blockIdx.x, s = act[slot], G = gridDim.y, tid = threadIdx.x;
     const C *v = v0 + (size_t)s * strideV;
     __shared__ double red[1][NW];
     double n2 = 0;
-    for (long i = (long)blockIdx.x * NT + tid; i < n; i += (long)G * NT) {
+    for (long i = (long)blockIdx.y * NT + tid; i < n; i += (long)G * NT) {
         C a = v[i];
         n2 += (double)a.x * a.x + (double)a.y * a.y;
     }
     double vv[1] = {n2};
     block_sum<1>(vv, red);
     double *part = (double *)partials + (size_t)slot * G;
-    if (tid == 0) part[blockIdx.x] = vv[0];
-    if (!arrive_last(&tickets[slot])) return;
+    if (tid == 0) part[blockIdx.y] = vv[0];
+    if (!arrive_last(&tickets[slot], G)) return;
     double tot[1];
     __syncthreads();
     sum_partials<1>(part, G, tot, red);
@@ -960,7 +1084,11 @@ double spmm_bytes(const SellMatrix &A, size_t vs, int nsys) {
     return (double)A.nnz * (vs + 4.0) + (A.n + 1.0) * 4.0 + (double)nsys * 2.0 * vs * A.n;
 }
 }  // namespace
-size_t scratch_doubles(int qmax, int nsys) { return (size_t)(2 * qmax + 32) * (size_t)(num_sms() * 8 + nsys); }
+size_t scratch_doubles(int qmax, int nsys, int n) {
+    const size_t per_chunk = (size_t)(2 * qmax + 4) * nsys * nchunks<double>(n);   // projection partials dominate
+    const size_t grid_stride = (size_t)32 * (num_sms() * 8 + nsys);                // norms, residuals, Z update
+    return per_chunk + grid_stride;
+}
 
 namespace {
 template <class K> void allow_smem(K kernel, size_t bytes) {
@@ -974,8 +1102,7 @@ void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT
                  unsigned *tickets, double2 *coef, size_t strideC, SysState *state, bool skip_broken, cudaStream_t st) {
     if (nsys <= 0 || qa + qb <= 0) return;
     Launch L_(KC_MDOT, (double)sizeof(typename CT<R>::t) * n * ((double)qa + (double)nsys * (qb + 1)), st, 1);
-    const int G = red_grid<R>(n, nsys);
-    k_mdot<R, 4><<<grid2(G, nsys), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW, act, partials, qmax,
+    k_mdot<R, 4><<<grid2(nsys, nchunks<R>(n)), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW, act, partials, qmax,
                                                  tickets, coef, strideC, state, skip_broken ? 1 : 0);
 }
 
@@ -986,8 +1113,7 @@ void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename 
                    SysState *state, FinishArgs fin, bool skip_broken, cudaStream_t st) {
     if (nsys <= 0) return;
     Launch L_(KC_UPDATE, (double)sizeof(typename CT<R>::t) * n * ((double)qa + (double)nsys * (qb + 2)), st, 1);
-    const int G = red_grid<R>(n, nsys);
-    k_update<R, 4><<<grid2(G, nsys), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, coef,
+    k_update<R, 4><<<grid2(nsys, nchunks<R>(n)), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, coef,
                                                    strideC, partials, tickets, state, fin, skip_broken ? 1 : 0);
 }
 
@@ -1008,8 +1134,7 @@ void launch_combine(int n, int kk, int m, const typename CT<R>::t *W, const type
                     const int *act, int nsys, double2 *partials, unsigned *tickets, SysState *state, cudaStream_t st) {
     if (nsys <= 0) return;
     Launch L_(KC_COMBINE, (double)sizeof(typename CT<R>::t) * n * (2.0 * kk + (double)nsys * (m + 1 - kk + 4)), st, 1);
-    const int G = red_grid<R>(n, nsys);
-    k_combine<R><<<grid2(G, nsys), NT, 0, st>>>(n, kk, m, W, Z, V, strideV, r, strideR, x, strideX, t, y, strideC, act,
+    k_combine<R><<<grid2(nsys, nchunks<R>(n)), NT, 0, st>>>(n, kk, m, W, Z, V, strideV, r, strideR, x, strideX, t, y, strideC, act,
                                                  partials, tickets, state);
 }
 
@@ -1046,7 +1171,9 @@ void launch_ls(int m, const double2 *H, size_t strideH, const double2 *g, double
     k_ls<<<nsys, 128, smem, st>>>(m, H, strideH, g, y, t, strideC, act);
 }
 
-size_t svd_smem_bytes(int m) { return sizeof(double2) * ((size_t)(m + 1) * m + (size_t)m * m); }
+size_t svd_smem_bytes(int m) {
+    return (sizeof(double2) + sizeof(float2)) * ((size_t)(m + 1) * m + (size_t)m * m);
+}
 
 void launch_svd_smallest(int m, int k, const double2 *H, double2 *vs, double *sigma, double2 *work, int *sweeps,
                          cudaStream_t st) {
@@ -1054,7 +1181,9 @@ void launch_svd_smallest(int m, int k, const double2 *H, double2 *vs, double *si
     size_t smem = svd_smem_bytes(m);
     int use_smem = smem <= 200 * 1024;
     if (use_smem) allow_smem(k_svd, smem);
-    k_svd<<<1, 512, use_smem ? smem : 0, st>>>(m, k, H, vs, sigma, work, use_smem, sweeps);
+    const int pairs = (m + 1) / 2;
+    int threads = 32 * (pairs < 32 ? (pairs > 4 ? pairs : 4) : 32);
+    k_svd<<<1, threads, use_smem ? smem : 0, st>>>(m, k, H, vs, sigma, work, use_smem, sweeps);
 }
 
 template <class R>
@@ -1063,7 +1192,8 @@ void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX
     if (nsys <= 0) return;
     Launch L_(KC_SPMM, spmm_bytes(A, sizeof(typename CT<R>::t), nsys), st, 1);
     constexpr int SG = 8;
-    dim3 grid((A.n + NT - 1) / NT, (nsys + SG - 1) / SG);
+    int rows = (A.n + NT - 1) / NT;
+    dim3 grid((nsys + SG - 1) / SG, rows < 65535 ? rows : 65535);
     k_spmm<R, SG><<<grid, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const typename CT<R>::t *)A.vals, x, strideX, y,
                                        strideY, act, nsys);
 }
@@ -1073,11 +1203,7 @@ void launch_residual64(const SellMatrix &A, const double2 *b, size_t strideB, co
                        SysState *state, cudaStream_t st) {
     if (nsys <= 0) return;
     Launch L_(KC_RESID64, spmm_bytes(A, sizeof(double2), nsys) + (double)sizeof(double2) * A.n * nsys, st, 1);
-    int chunks = (A.n + NT - 1) / NT;
-    int G = (num_sms() * 4 + nsys - 1) / nsys;
-    if (G > chunks) G = chunks;
-    if (G < 1) G = 1;
-    k_residual64<<<grid2(G, nsys), NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const double2 *)A.vals, b, strideB, x,
+    k_residual64<<<grid2(nsys, capped_grid(A.n, nsys, 8)), NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const double2 *)A.vals, b, strideB, x,
                                                 strideX, r, strideR, act, partials, tickets, state);
 }
 
@@ -1117,8 +1243,7 @@ void launch_norm(int n, const typename CT<R>::t *v, size_t strideV, const int *a
                  unsigned *tickets, SysState *state, int mode, cudaStream_t st) {
     if (nsys <= 0) return;
     Launch L_(KC_OTHER, (double)sizeof(typename CT<R>::t) * n * nsys, st, 1);
-    const int G = red_grid<R>(n, nsys);
-    k_norm<R><<<grid2(G, nsys), NT, 0, st>>>(n, v, strideV, act, partials, tickets, state, mode);
+    k_norm<R><<<grid2(nsys, capped_grid(n, nsys, 8)), NT, 0, st>>>(n, v, strideV, act, partials, tickets, state, mode);
 }
 
 void launch_broadcast_hdef(int m, int kk, const double2 *Hd, double2 *H, size_t strideH, const int *act, int nsys,

@@ -94,7 +94,7 @@ void profile_reset();
 // scratch_doubles(qmax, nsys) doubles and `tickets` of nsys zero-initialised
 // counters (each kernel resets the counters it used).  Kernels on one stream
 // may share both.
-size_t scratch_doubles(int qmax, int nsys);
+size_t scratch_doubles(int qmax, int nsys, int n);
 
 template <class R>
 void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
@@ -135,7 +135,7 @@ void launch_znormalise(int n, int k, const typename CT<R>::t *Znew, const double
 void launch_ls(int m, const double2 *H, size_t strideH, const double2 *g, double2 *y, double2 *t, size_t strideC,
                const int *act, int nsys, cudaStream_t st);
 // Right singular vectors of the k smallest singular values of H ((m+1) x m), FP64 one-sided Jacobi.
-// vs: m x k column-major; sigma: m values (descending); work: global scratch of 2*m*(m+1) double2.
+// vs: m x k column-major; sigma: m values (descending); work: global scratch of 3*m*(m+1) double2.
 void launch_svd_smallest(int m, int k, const double2 *H, double2 *vs, double *sigma, double2 *work, int *sweeps,
                          cudaStream_t st);
 

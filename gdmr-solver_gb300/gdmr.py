@@ -58,6 +58,7 @@ SIGNATURES = {
     "gdmr_system_create": (I, [P, I, P, P, P, I, I, I, I, I]),
     "gdmr_system_destroy": (I, [P]),
     "gdmr_system_bytes": (LL, [P]),
+    "gdmr_system_svd_sweeps": (I, [P]),
     "gdmr_solve": (I, [P, I, P, P, D, I, I, P]),
     "gdmr_solve_batch": (I, [P, I, P, P, P, I, I, P]),
     "gdmr_true_residual": (I, [P, I, P, P, I, P]),
@@ -264,6 +265,10 @@ class System:
             self.close()
         except Exception:
             pass
+
+    def svd_sweeps(self) -> dict:
+        v = int(self.L.gdmr_system_svd_sweeps(self._h))
+        return {"fp32": v // 1000, "fp64": v % 1000}
 
     @property
     def device_bytes(self) -> int:

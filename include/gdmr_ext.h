@@ -100,6 +100,8 @@ int gdmr_system_create(gdmr_system **out, int n, const int *rowPtr, const int *c
 int gdmr_system_destroy(gdmr_system *sys);
 /* Bytes of device memory the system holds. */
 long long gdmr_system_bytes(const gdmr_system *sys);
+/* Jacobi sweeps of the last deflation-space SVD: 1000 * (FP32 sweeps) + (FP64 sweeps). */
+int gdmr_system_svd_sweeps(const gdmr_system *sys);
 
 /* Reference-semantics solve of one right-hand side (solverDMR's algorithm,
  * complex128 or complex64 per the system's precision), then the true FP64

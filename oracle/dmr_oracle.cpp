@@ -102,7 +102,7 @@ static void ls_householder(int rows, int cols, const Z64 *Hin, const Z64 *gin, Z
 static void svd_jacobi(int rows, int cols, const Z64 *Ain, double *sigma, Z64 *Vout) {
     std::vector<Z64> A(Ain, Ain + (size_t)rows * cols), V((size_t)cols * cols, Z64{0, 0});
     for (int i = 0; i < cols; ++i) V[i * cols + i] = {1, 0};
-    const double eps = 1e-15;
+    const double eps = 4.0 * 2.220446049250313e-16 * cols;   // pairwise orthogonality target
     for (int sweep = 0; sweep < 100; ++sweep) {
         double off = 0;
         for (int p = 0; p < cols - 1; ++p)
@@ -174,14 +174,25 @@ template <typename R> struct Oracle {
             y[i] = s;
         }
     }
-    T dot(const T *a, const T *b) {   // sum conj(a_i) b_i, accumulated in R like the reference
-        R re = 0, im = 0;
-#pragma omp parallel for reduction(+ : re, im) schedule(static)
-        for (int i = 0; i < n; ++i) {
-            T p = cconjmul(a[i], b[i]);
-            re += p.re;
-            im += p.im;
+    // sum conj(a_i) b_i, accumulated in R like the reference; fixed chunks summed in order,
+    // so the result does not depend on the thread count or on scheduling
+    T dot(const T *a, const T *b) {
+        const int CH = 4096;
+        const int nch = (n + CH - 1) / CH;
+        std::vector<T> part(nch);
+#pragma omp parallel for schedule(static)
+        for (int c = 0; c < nch; ++c) {
+            R re = 0, im = 0;
+            const int hi = std::min(n, (c + 1) * CH);
+            for (int i = c * CH; i < hi; ++i) {
+                T p = cconjmul(a[i], b[i]);
+                re += p.re;
+                im += p.im;
+            }
+            part[c] = {re, im};
         }
+        R re = 0, im = 0;
+        for (int c = 0; c < nch; ++c) { re += part[c].re; im += part[c].im; }
         return {re, im};
     }
     R norm(const T *a) { return std::sqrt(dot(a, a).re); }
