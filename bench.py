@@ -314,6 +314,15 @@ def main():
     plain = {"value": args.plain_sample / plain_s, "unit": "solves/s", "cycles": plain_cycles,
              "latency_ms_each": plain_s / args.plain_sample * 1e3, "verified": bool(plain_ok),
              "sample": f"{args.plain_sample} right-hand sides solved in sequence (recycled deflation space)"}
+    # kernel-class shares of the plain form: 10 more cycles with library-side CUDA events
+    gdmr.profile_reset()
+    gdmr.profile(True)
+    sysp.solve(B[0], mode=1, tol=TOL, mat_rank=9)
+    gdmr.profile(False)
+    pp = gdmr.profile_read()
+    pt = sum(v["ms"] for v in pp.values())
+    plain["classes"] = {k: {"GB/s": (v["bytes"] / (v["ms"] / 1e3) / 1e9) if v["ms"] > 0 else None,
+                            "share": v["ms"] / pt} for k, v in pp.items() if v["launches"]}
     sysp.close()
 
     line = {

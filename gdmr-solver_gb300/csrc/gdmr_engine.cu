@@ -183,6 +183,17 @@ template <class R> int Engine<R>::alloc(void **p, size_t bytes) {
 }
 
 template <class R> void Engine<R>::release() {
+    if (side_) {
+        cudaStreamSynchronize(side_);
+        cudaStreamDestroy(side_);
+        side_ = nullptr;
+    }
+    if (ev_krylov_) cudaEventDestroy(ev_krylov_);
+    if (ev_zdone_) cudaEventDestroy(ev_zdone_);
+    ev_krylov_ = ev_zdone_ = nullptr;
+    z_pending_ = false;
+    partials_side_ = nullptr;
+    ticket_side_ = nullptr;
     for (void *p : allocs_) cudaFree(p);
     allocs_.clear();
     if (hstate_) cudaFreeHost(hstate_);
@@ -243,7 +254,16 @@ template <class R> int Engine<R>::init(int n, int m, int k, int capacity, int de
     A_(state_, sizeof(SysState) * (capacity + 1));
     A_(act_, sizeof(int) * (capacity + 1));
     A_(ident_, sizeof(int) * (capacity + 1));
+    A_(partials_side_, sizeof(double) * scratch_doubles(16, 1, 1));
+    A_(ticket_side_, sizeof(unsigned));
 #undef A_
+    if (cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev_krylov_, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev_zdone_, cudaEventDisableTiming) != cudaSuccess) {
+        release();
+        set_last_error(GDMR_ECUDA, "engine: side stream or events");
+        return GDMR_ECUDA;
+    }
     if (cudaMallocHost(&hstate_, sizeof(SysState) * (capacity + 1)) != cudaSuccess) {
         release();
         set_last_error(GDMR_ENOMEM, "engine: pinned host state");
@@ -253,6 +273,7 @@ template <class R> int Engine<R>::init(int n, int m, int k, int capacity, int de
     for (int i = 0; i <= capacity; ++i) id[i] = i;
     GDMR_CK(cudaMemcpy(ident_, id.data(), sizeof(int) * (capacity + 1), cudaMemcpyHostToDevice));
     GDMR_CK(cudaMemset(tickets_, 0, sizeof(unsigned) * (capacity + 1)));
+    GDMR_CK(cudaMemset(ticket_side_, 0, sizeof(unsigned)));
     GDMR_CK(cudaMemset(V_, 0, vn * (m + 1) * capacity));
     GDMR_CK(cudaMemset(Z_, 0, vn * std::max(k, 1)));
     GDMR_CK(cudaMemset(X_, 0, vn * capacity));
@@ -305,7 +326,17 @@ void Engine<R>::apply(const C *x0, size_t strideX, C *y0, size_t strideY, int ns
     }
 }
 
+template <class R> int Engine<R>::sync_deflation() {
+    if (!z_pending_) return GDMR_OK;
+    GDMR_CK(cudaStreamWaitEvent(stream, ev_zdone_, 0));
+    std::swap(Z_, Znew_);
+    have_z_ = true;
+    z_pending_ = false;
+    return GDMR_OK;
+}
+
 template <class R> int Engine<R>::run_cycle(int kk, int nsys, int lead, double tol, long *matvecs) {
+    if (sync_deflation() != GDMR_OK) return GDMR_ECUDA;
     const int n = n_, m = m_;
     const size_t sV = strideV(), sC = strideC();
     const bool hook = op.kind == Operator<R>::HOOK;
@@ -370,6 +401,17 @@ template <class R> int Engine<R>::run_cycle(int kk, int nsys, int lead, double t
                          stream);
         launch_scale<R>(n, T_, n, V_ + (size_t)j * n, sV, hook ? op.ext : nullptr, 0, act_, nsys, state_, true, stream);
     }
+    // deflation-space update from the lead system (genDeflatDMR, gDMR.cu:1583-1704), on the
+    // side stream: it needs only H_lead and the basis, which nothing below modifies
+    if (k_ > 0) {
+        GDMR_CK(cudaEventRecord(ev_krylov_, stream));
+        GDMR_CK(cudaStreamWaitEvent(side_, ev_krylov_, 0));
+        launch_svd_smallest(m, k_, H_ + (size_t)lead * strideH(), vs_, sigma_, svdwork_, sweeps_, side_);
+        launch_zupdate<R>(n, kk, m, k_, Z_, Vs(lead), vs_, Znew_, partials_side_, ticket_side_, znorm2_, side_);
+        launch_znormalise<R>(n, k_, Znew_, znorm2_, Znew_, side_);
+        GDMR_CK(cudaEventRecord(ev_zdone_, side_));
+        z_pending_ = true;
+    }
     // g = [W V]^H r (updateTrgCoeffsDMR, gDMR.cu:2334-2408)
     launch_mdot<R>(n, W_, kk, V_, sV, m + 1 - kk, R_, n, act_, nsys, partials_, qmax(), tickets_, g_, sC, state_, false,
                    stream);
@@ -379,14 +421,6 @@ template <class R> int Engine<R>::run_cycle(int kk, int nsys, int lead, double t
     launch_combine<R>(n, kk, m, W_, Z_, V_, sV, R_, n, X_, n, t_, y_, sC, act_, nsys, partials_, tickets_, state_,
                       stream);
     launch_scale<R>(n, R_, n, R_, n, nullptr, 0, act_, nsys, state_, false, stream);
-    // deflation-space update from the lead system (genDeflatDMR, gDMR.cu:1583-1704)
-    if (k_ > 0) {
-        launch_svd_smallest(m, k_, H_ + (size_t)lead * strideH(), vs_, sigma_, svdwork_, sweeps_, stream);
-        launch_zupdate<R>(n, kk, m, k_, Z_, Vs(lead), vs_, Znew_, partials_, tickets_ + cap_, znorm2_, stream);
-        launch_znormalise<R>(n, k_, Znew_, znorm2_, Znew_, stream);
-        std::swap(Z_, Znew_);
-        have_z_ = true;
-    }
     GDMR_CK(cudaGetLastError());
     return GDMR_OK;
 }
@@ -435,6 +469,7 @@ double Engine<R>::solve_reference(int mode, const C *b, C *x, double tol, int ma
     }
     while (rho_abs > tol * bnorm) {
         if (cycle > mat_rank) {
+            sync_deflation();
             set_last_error(GDMR_ENOCONV, "solver failed to converge within matRank restart cycles");
             S.its = cycle;
             S.cycles = cycle;
@@ -445,6 +480,7 @@ double Engine<R>::solve_reference(int mode, const C *b, C *x, double tol, int ma
             return rho_abs / bnorm;
         }
         if (rho_abs / bnorm > 1.0) {
+            sync_deflation();
             set_last_error(GDMR_ERUNAWAY, "solver runaway: residual above the right-hand side norm");
             S.its = cycle;
             S.cycles = cycle;
@@ -455,6 +491,7 @@ double Engine<R>::solve_reference(int mode, const C *b, C *x, double tol, int ma
             return rho_abs / bnorm;
         }
         const int kk = (cycle == 0 && first_def == 0) ? 0 : k;
+        if (sync_deflation() != GDMR_OK) return fail(1.0);
         // restart vector (arnoldiSetupDMR, gDMR.cu:2600-2621); a zero period would divide by zero there
         const int period = (2 * mat_rank) / (m - k);
         if (loop_flag == 0 || (period != 0 && flag_count_ % period == 0)) {
@@ -481,6 +518,7 @@ double Engine<R>::solve_reference(int mode, const C *b, C *x, double tol, int ma
     S.its = cycle - 1;
     S.cycles = cycle;
     S.rel_res = rho_abs / bnorm;
+    if (sync_deflation() != GDMR_OK) return fail(rho_abs / bnorm);
     cudaMemcpyAsync(x, X_, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
     if (cudaStreamSynchronize(stream) != cudaSuccess) {
         set_last_error(GDMR_ECUDA, "solver: final synchronisation failed");
@@ -577,12 +615,13 @@ template <class R> int Engine<R>::refine_cycle(std::vector<int> *done) {
         if (rel > worst) { worst = rel; lead = s; }
     }
     act_h_ = next;
-    if (next.empty()) return GDMR_OK;
+    if (next.empty()) return sync_deflation();
     if (set_active(next) != GDMR_OK) return GDMR_ECUDA;
     na = (int)next.size();
     // unit residual direction in precision R; the inner recursion starts at rho_abs = 1
     launch_demote_unit<R>(n, r64_, n, R_, n, act_, na, state_, stream);
     k_cycle_reset<<<1, 256, 0, stream>>>(act_, na, state_, 1);
+    if (sync_deflation() != GDMR_OK) return GDMR_ECUDA;
     const int kk = (k > 0 && have_z_) ? k : 0;
     for (int s : next) {
         Slot &S = slot_[s];
@@ -637,6 +676,8 @@ template <class R> int Engine<R>::true_residual(int count, const double2 *b, con
 
 template <class R> int Engine<R>::import_deflation(const C *host) {
     if (!ready() || k_ == 0) return GDMR_OK;
+    if (sync_deflation() != GDMR_OK) return GDMR_ECUDA;
+    GDMR_CK(cudaStreamSynchronize(stream));
     GDMR_CK(cudaMemcpy(Z_, host, sizeof(C) * (size_t)k_ * n_, cudaMemcpyHostToDevice));
     have_z_ = true;
     return GDMR_OK;
@@ -644,6 +685,7 @@ template <class R> int Engine<R>::import_deflation(const C *host) {
 
 template <class R> int Engine<R>::export_deflation(C *host) {
     if (!ready() || k_ == 0) return GDMR_OK;
+    if (sync_deflation() != GDMR_OK) return GDMR_ECUDA;
     GDMR_CK(cudaStreamSynchronize(stream));
     GDMR_CK(cudaMemcpy(host, Z_, sizeof(C) * (size_t)k_ * n_, cudaMemcpyDeviceToHost));
     return GDMR_OK;

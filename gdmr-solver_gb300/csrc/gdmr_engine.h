@@ -113,7 +113,10 @@ template <class R> class Engine {
     int import_deflation(const C *host);
     int export_deflation(C *host);
     bool has_deflation() const { return have_z_; }
-    void drop_deflation() { have_z_ = false; }
+    void drop_deflation() {
+        sync_deflation();
+        have_z_ = false;
+    }
     // The reference keeps its stagnation counter across solves (gDMR.cu:2646-2655); reset on init.
     int flag_count() const { return flag_count_; }
 
@@ -156,6 +159,15 @@ template <class R> class Engine {
     int kk_prev_ = 0;
     int svd_sweeps_ = 0;
     int hsweeps_ = 0;
+    // The deflation-space update (SVD of the lead Hessenberg, Z <- [Z V] Vs) runs on a side
+    // stream, overlapped with the rest of the cycle and the next cycle's residual; the main
+    // stream joins it before anything writes the basis or reads the new Z.
+    cudaStream_t side_ = nullptr;
+    cudaEvent_t ev_krylov_ = nullptr, ev_zdone_ = nullptr;
+    bool z_pending_ = false;
+    double2 *partials_side_ = nullptr;
+    unsigned *ticket_side_ = nullptr;
+    int sync_deflation();
 
     size_t strideV() const { return (size_t)(m_ + 1) * n_; }
     size_t strideH() const { return (size_t)(m_ + 1) * m_; }

@@ -176,7 +176,7 @@ __device__ void run_finish(const FinishArgs &f, int s, SysState &st, double n2, 
 // Grid (systems, chunks); one chunk of NT*EPT elements per CTA, w in registers,
 // PU basis vectors in flight per thread, warp reductions in the working precision.
 template <class R, int PU>
-__global__ void __launch_bounds__(NT) k_mdot(int n, const typename CT<R>::t *__restrict__ segA, int qa,
+__global__ void __launch_bounds__(NT, 3) k_mdot(int n, const typename CT<R>::t *__restrict__ segA, int qa,
                                              const typename CT<R>::t *__restrict__ segB0, size_t strideB, int qb,
                                              const typename CT<R>::t *__restrict__ w0, size_t strideW,
                                              const int *__restrict__ act, double2 *__restrict__ partials, int qmax,
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(NT) k_mdot(int n, const typename CT<R>::t *__r
 
 // ----------------------------------------------------------------- update + norms
 template <class R, int PU>
-__global__ void __launch_bounds__(NT) k_update(int n, const typename CT<R>::t *__restrict__ segA, int qa,
+__global__ void __launch_bounds__(NT, 3) k_update(int n, const typename CT<R>::t *__restrict__ segA, int qa,
                                                const typename CT<R>::t *__restrict__ segB0, size_t strideB, int qb,
                                                const typename CT<R>::t *__restrict__ w0, size_t strideW,
                                                typename CT<R>::t *__restrict__ out0, size_t strideO,
@@ -380,6 +380,7 @@ __global__ void __launch_bounds__(NT) k_combine(int n, int kk, int m, const type
         ra_[e] = i < n ? r[i] : czero<C>();
         xa[e] = i < n ? x[i] : czero<C>();
     }
+#pragma unroll 2
     for (int p = 0; p < kk; ++p) {
         const C tc = ts[p], yc = ys[p];
         const C *wp = W + (size_t)p * n;
@@ -393,6 +394,7 @@ __global__ void __launch_bounds__(NT) k_combine(int n, int kk, int m, const type
             }
         }
     }
+#pragma unroll 4
     for (int p = 0; p <= m - kk; ++p) {
         const C tc = ts[kk + p], yc = ys[kk + p];   // ys[m] = 0: the last Krylov vector is target-side only
         const C *vp = V + (size_t)p * n;
@@ -608,7 +610,7 @@ __device__ __forceinline__ void circle_pair(int r, int pi, int mm, int &p, int &
 
 template <class T>
 __device__ int jacobi_sweeps(int m, typename CX<T>::t *A, typename CX<T>::t *V, T *nrm, double2 *rot, T tol,
-                             int max_sweeps, int *s_flag) {
+                             int max_sweeps, int *s_flag, float *s_off) {
     using C = typename CX<T>::t;
     const int rows = m + 1, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
     const int mm = m + (m & 1), npairs = mm / 2;
@@ -620,7 +622,7 @@ __device__ int jacobi_sweeps(int m, typename CX<T>::t *A, typename CX<T>::t *V, 
             a = warp_sum(a);
             if (lane == 0) nrm[c] = a;
         }
-        if (tid == 0) *s_flag = 0;
+        if (tid == 0) { *s_flag = 0; *s_off = 0.f; }
         __syncthreads();
         for (int round = 0; round < mm - 1; ++round) {
             // (1) gamma of every pair, one warp per pair
@@ -639,19 +641,21 @@ __device__ int jacobi_sweeps(int m, typename CX<T>::t *A, typename CX<T>::t *V, 
                 if (lane == 0) rot[pi] = make_double2((double)gr, (double)gi);
             }
             __syncthreads();
-            // (2) rotation parameters, one pair per lane: rot[pi] <- (c, t) and phase in rot[npairs+pi]
+            // (2) rotation parameters, one pair per lane: (c, t), phase e^{-i phi}, |gamma|
             for (int pi = tid; pi < npairs; pi += blockDim.x) {
                 int p, q;
                 circle_pair(round, pi, mm, p, q);
                 const double2 gd = rot[pi];
                 T gx = (T)gd.x, gy = (T)gd.y;
-                T cc = 1, tt = 0, phr = 1, phi = 0;
+                T cc = 1, tt = 0, phr = 1, phi = 0, ag = 0;
                 if (p < m && q < m) {
                     const T a = nrm[p < q ? p : q], b = nrm[p < q ? q : p];
                     if (p > q) gy = -gy;                    // gamma for the ordered pair (min, max)
-                    const T ag = sqrt(gx * gx + gy * gy);
-                    if (ag > (T)0 && ag > tol * sqrt(a * b)) {
+                    ag = sqrt(gx * gx + gy * gy);
+                    const T rel = ag / sqrt(a * b);
+                    if (ag > (T)0 && rel > tol) {
                         *s_flag = 1;
+                        atomicMax((int *)s_off, __float_as_int((float)rel));   // non-negative floats order as ints
                         phr = gx / ag;
                         phi = -gy / ag;
                         const T zeta = (b - a) / ((T)2 * ag);
@@ -661,9 +665,11 @@ __device__ int jacobi_sweeps(int m, typename CX<T>::t *A, typename CX<T>::t *V, 
                 }
                 rot[pi] = make_double2((double)cc, (double)tt);
                 rot[npairs + pi] = make_double2((double)phr, (double)phi);
+                rot[2 * npairs + pi] = make_double2((double)ag, 0.0);
             }
             __syncthreads();
-            // (3) apply: one warp per pair, columns (min, max) of A and V
+            // (3) apply: one warp per pair, columns (min, max) of A and V; norms updated
+            //     incrementally (||a_p'||^2 = a - t|gamma|, ||a_q'||^2 = b + t|gamma|)
             for (int pi = warp; pi < npairs; pi += nwarps) {
                 int p, q;
                 circle_pair(round, pi, mm, p, q);
@@ -695,27 +701,20 @@ __device__ int jacobi_sweeps(int m, typename CX<T>::t *A, typename CX<T>::t *V, 
                     V[(size_t)p * m + r] = np_;
                     V[(size_t)q * m + r] = nq_;
                 }
-            }
-            __syncthreads();
-            // norms of the rotated columns (exact recomputation keeps the next round consistent)
-            for (int pi = warp; pi < npairs; pi += nwarps) {
-                int p, q;
-                circle_pair(round, pi, mm, p, q);
-                if (p >= m || q >= m || rot[pi].y == 0.0) continue;
-                T a = 0, b = 0;
-                for (int r = lane; r < rows; r += 32) {
-                    C ap = A[(size_t)p * rows + r], aq = A[(size_t)q * rows + r];
-                    a += ap.x * ap.x + ap.y * ap.y;
-                    b += aq.x * aq.x + aq.y * aq.y;
+                if (lane == 0) {
+                    const T tg = (T)(ct.y * rot[2 * npairs + pi].x);
+                    nrm[p] = nrm[p] - tg;
+                    nrm[q] = nrm[q] + tg;
                 }
-                a = warp_sum(a);
-                b = warp_sum(b);
-                if (lane == 0) { nrm[p] = a; nrm[q] = b; }
             }
             __syncthreads();
         }
         if (!*s_flag) break;
+        // quadratic convergence: after a sweep whose largest relative off-diagonal was d,
+        // the next is of order d^2; stop once that is below the tolerance
+        const float d = *s_off;
         __syncthreads();
+        if ((double)d * (double)d < (double)tol * 1e-2) { ++sweep; break; }
     }
     return sweep + 1;
 }
@@ -732,51 +731,66 @@ __global__ void __launch_bounds__(1024) k_svd(int m, int k, const double2 *__res
     float2 *V32 = A32 + (size_t)rows * m;
     __shared__ double nrm64[168];
     __shared__ float nrm32[168];
-    __shared__ double2 rot[2 * 84];
+    __shared__ double2 rot[3 * 84];
     __shared__ int s_flag;
+    __shared__ float s_off;
     for (int i = tid; i < rows * m; i += blockDim.x) A32[i] = make_float2((float)H[i].x, (float)H[i].y);
     for (int i = tid; i < m * m; i += blockDim.x) V32[i] = make_float2((i % m) == (i / m) ? 1.f : 0.f, 0.f);
     __syncthreads();
-    const int s32 = jacobi_sweeps<float>(m, A32, V32, nrm32, rot, 4.0f * 1.1920929e-7f * m, 40, &s_flag);
-    // V64 = orthonormalised V32 (two passes of classical Gram-Schmidt, one warp per column dot)
+    const int s32 = jacobi_sweeps<float>(m, A32, V32, nrm32, rot, 4.0f * 1.1920929e-7f * m, 40, &s_flag, &s_off);
+    // V64 = V32 re-orthonormalised in FP64 by Cholesky QR: S = V^H V = L L^H, V <- V L^{-H}.
+    // V32 is orthonormal to FP32 accuracy, so S is within ~1e-6 of I and the factorisation
+    // is well conditioned.  S lives in the FP32 scratch region, free after phase 1.
     for (int i = tid; i < m * m; i += blockDim.x) V64[i] = make_double2(V32[i].x, V32[i].y);
     __syncthreads();
-    for (int c = 0; c < m; ++c) {
-        for (int pass = 0; pass < 2; ++pass) {
-            // coefficients against columns < c, one warp per earlier column
-            for (int j = warp; j < c; j += nwarps) {
-                double gr = 0, gi = 0;
-                for (int r = lane; r < m; r += 32) {
-                    double2 a = V64[(size_t)j * m + r], b = V64[(size_t)c * m + r];
-                    gr += a.x * b.x + a.y * b.y;
-                    gi += a.x * b.y - a.y * b.x;
-                }
-                gr = warp_sum(gr);
-                gi = warp_sum(gi);
-                if (lane == 0) rot[j] = make_double2(gr, gi);
-            }
-            __syncthreads();
-            for (int r = tid; r < m; r += blockDim.x) {
-                double2 v = V64[(size_t)c * m + r];
-                for (int j = 0; j < c; ++j) {
-                    const double2 g = rot[j], a = V64[(size_t)j * m + r];
-                    v.x -= g.x * a.x - g.y * a.y;
-                    v.y -= g.x * a.y + g.y * a.x;
-                }
-                V64[(size_t)c * m + r] = v;
-            }
-            __syncthreads();
+    double2 *S = (double2 *)A32;            // m x m, column-major
+    for (int e = tid; e < m * m; e += blockDim.x) {
+        const int i = e % m, j = e / m;
+        if (i < j) continue;                // lower triangle S[i][j], i >= j
+        double gr = 0, gi = 0;
+        for (int r = 0; r < m; ++r) {       // S_ij = sum_r conj(V_ri) V_rj
+            const double2 a = V64[(size_t)i * m + r], b = V64[(size_t)j * m + r];
+            gr += a.x * b.x + a.y * b.y;
+            gi += a.x * b.y - a.y * b.x;
         }
-        if (warp == 0) {
-            double nn = 0;
-            for (int r = lane; r < m; r += 32) { double2 v = V64[(size_t)c * m + r]; nn += v.x * v.x + v.y * v.y; }
-            nn = warp_sum(nn);
-            if (lane == 0) nrm64[0] = 1.0 / sqrt(nn);
+        S[(size_t)j * m + i] = make_double2(gr, gi);
+    }
+    __syncthreads();
+    for (int j = 0; j < m; ++j) {           // right-looking Cholesky, lower triangle in place
+        if (tid == 0) {
+            const double d = sqrt(S[(size_t)j * m + j].x);
+            S[(size_t)j * m + j] = make_double2(d, 0.0);
+            nrm64[0] = 1.0 / d;
         }
         __syncthreads();
+        const double inv = nrm64[0];
+        for (int i = j + 1 + tid; i < m; i += blockDim.x) {
+            double2 v = S[(size_t)j * m + i];
+            S[(size_t)j * m + i] = make_double2(v.x * inv, v.y * inv);
+        }
+        __syncthreads();
+        const int tail = m - j - 1;
+        for (int e = tid; e < tail * tail; e += blockDim.x) {
+            const int i = j + 1 + e % tail, kcol = j + 1 + e / tail;
+            if (i < kcol) continue;
+            const double2 lij = S[(size_t)j * m + i], lkj = S[(size_t)j * m + kcol];
+            double2 v = S[(size_t)kcol * m + i];   // S_ik -= L_ij conj(L_kj)
+            v.x -= lij.x * lkj.x + lij.y * lkj.y;
+            v.y -= lij.y * lkj.x - lij.x * lkj.y;
+            S[(size_t)kcol * m + i] = v;
+        }
+        __syncthreads();
+    }
+    for (int j = 0; j < m; ++j) {           // V[:, j] <- (V[:, j] - sum_{k<j} V[:, k] conj(L_jk)) / L_jj
+        const double inv = 1.0 / S[(size_t)j * m + j].x;
         for (int r = tid; r < m; r += blockDim.x) {
-            double2 v = V64[(size_t)c * m + r];
-            V64[(size_t)c * m + r] = make_double2(v.x * nrm64[0], v.y * nrm64[0]);
+            double2 v = V64[(size_t)j * m + r];
+            for (int kc = 0; kc < j; ++kc) {
+                const double2 l = S[(size_t)kc * m + j], a = V64[(size_t)kc * m + r];
+                v.x -= a.x * l.x + a.y * l.y;
+                v.y -= a.y * l.x - a.x * l.y;
+            }
+            V64[(size_t)j * m + r] = make_double2(v.x * inv, v.y * inv);
         }
         __syncthreads();
     }
@@ -792,7 +806,7 @@ __global__ void __launch_bounds__(1024) k_svd(int m, int k, const double2 *__res
         A64[i] = acc;
     }
     __syncthreads();
-    const int s64 = jacobi_sweeps<double>(m, A64, V64, nrm64, rot, 4.0 * 2.220446049250313e-16 * m, 20, &s_flag);
+    const int s64 = jacobi_sweeps<double>(m, A64, V64, nrm64, rot, 4.0 * 2.220446049250313e-16 * m, 20, &s_flag, &s_off);
     for (int c = warp; c < m; c += nwarps) {
         double a = 0;
         for (int r = lane; r < rows; r += 32) { double2 v = A64[(size_t)c * rows + r]; a += v.x * v.x + v.y * v.y; }
@@ -826,19 +840,60 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
                                              typename CT<R>::t *__restrict__ y0, size_t strideY,
                                              const int *__restrict__ act, int nsys) {
     using C = typename CT<R>::t;
+    constexpr int WMAX = 8;   // stencil rows (7-point) fit; wider slices take the loop below
     const int g0 = blockIdx.x * SG;
+    const int ng = min(SG, nsys - g0);
     for (long row = (long)blockIdx.y * NT + threadIdx.x; row < n; row += (long)gridDim.y * NT) {
         const int slice = (int)(row >> 5), lane = (int)(row & 31);
         const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
-        for (int g = 0; g < SG && g0 + g < nsys; ++g) {
-            const int s = act[g0 + g];
-            const C *x = x0 + (size_t)s * strideX;
-            C acc = czero<C>();
-            for (int c = 0; c < width; ++c) {
-                const int e = beg + c * 32 + lane;
-                cfma(acc, vals[e], x[cols[e]]);
+        if (width <= WMAX) {
+            C v[WMAX];
+            int c[WMAX];
+#pragma unroll
+            for (int e = 0; e < WMAX; ++e) {
+                if (e < width) {
+                    v[e] = vals[beg + e * 32 + lane];
+                    c[e] = cols[beg + e * 32 + lane];
+                } else {
+                    v[e] = czero<C>();
+                    c[e] = (int)row;
+                }
             }
-            y0[(size_t)s * strideY + row] = acc;
+            int g = 0;
+            for (; g + 1 < ng; g += 2) {       // two systems: 2*width independent gathers in flight
+                const int s0 = act[g0 + g], s1 = act[g0 + g + 1];
+                const C *xa = x0 + (size_t)s0 * strideX, *xb = x0 + (size_t)s1 * strideX;
+                C a0 = czero<C>(), a1 = czero<C>();
+#pragma unroll
+                for (int e = 0; e < WMAX; ++e) {
+                    if (e < width) {
+                        cfma(a0, v[e], xa[c[e]]);
+                        cfma(a1, v[e], xb[c[e]]);
+                    }
+                }
+                y0[(size_t)s0 * strideY + row] = a0;
+                y0[(size_t)s1 * strideY + row] = a1;
+            }
+            if (g < ng) {
+                const int s0 = act[g0 + g];
+                const C *xa = x0 + (size_t)s0 * strideX;
+                C a0 = czero<C>();
+#pragma unroll
+                for (int e = 0; e < WMAX; ++e)
+                    if (e < width) cfma(a0, v[e], xa[c[e]]);
+                y0[(size_t)s0 * strideY + row] = a0;
+            }
+        } else {
+            for (int g = 0; g < ng; ++g) {
+                const int s = act[g0 + g];
+                const C *x = x0 + (size_t)s * strideX;
+                C acc = czero<C>();
+                for (int e = 0; e < width; ++e) {
+                    const int idx = beg + e * 32 + lane;
+                    cfma(acc, vals[idx], x[cols[idx]]);
+                }
+                y0[(size_t)s * strideY + row] = acc;
+            }
         }
     }
 }
@@ -1102,7 +1157,7 @@ void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT
                  unsigned *tickets, double2 *coef, size_t strideC, SysState *state, bool skip_broken, cudaStream_t st) {
     if (nsys <= 0 || qa + qb <= 0) return;
     Launch L_(KC_MDOT, (double)sizeof(typename CT<R>::t) * n * ((double)qa + (double)nsys * (qb + 1)), st, 1);
-    k_mdot<R, 4><<<grid2(nsys, nchunks<R>(n)), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW, act, partials, qmax,
+    k_mdot<R, 2><<<grid2(nsys, nchunks<R>(n)), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW, act, partials, qmax,
                                                  tickets, coef, strideC, state, skip_broken ? 1 : 0);
 }
 
@@ -1113,7 +1168,7 @@ void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename 
                    SysState *state, FinishArgs fin, bool skip_broken, cudaStream_t st) {
     if (nsys <= 0) return;
     Launch L_(KC_UPDATE, (double)sizeof(typename CT<R>::t) * n * ((double)qa + (double)nsys * (qb + 2)), st, 1);
-    k_update<R, 4><<<grid2(nsys, nchunks<R>(n)), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, coef,
+    k_update<R, 2><<<grid2(nsys, nchunks<R>(n)), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, coef,
                                                    strideC, partials, tickets, state, fin, skip_broken ? 1 : 0);
 }
 
