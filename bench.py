@@ -138,7 +138,7 @@ class ClockSampler:
 
 def build_workload(nrhs: int, rank: int):
     A = problems.helmholtz(SHAPE, KAPPA, DAMPING)
-    B = np.stack([problems.gaussian_source_rhs(SHAPE, 100 + r + 1000 * rank) for r in range(nrhs)])
+    B = np.stack([problems.gaussian_source_rhs(SHAPE, seed) for seed in problems.shard_seeds(nrhs, rank)])
     return A, B
 
 
@@ -198,6 +198,61 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_serve(args, rank):
+    """Serving workload (BASELINE configs[4]): six resident operators (7-point Helmholtz 64^3 /
+    96^3 / 128^3 with kappa 16 / 24 / 32, each at damping 0.05 and 0.2), Poisson arrivals,
+    each request picks an operator uniformly and brings one Gaussian-source right-hand side
+    with a tolerance drawn from {1e-6, 1e-8, 1e-10}; m = 48, k = 24 per operator; device
+    memory bounded by a 150 GB budget split evenly across the operators."""
+    import gdmr
+    gdmr.load()
+    rng = np.random.default_rng(4)
+    specs = [((64,) * 3, 16.0), ((96,) * 3, 24.0), ((128,) * 3, 32.0)]
+    budget = int(args.budget_gb * (1 << 30))
+    srv = gdmr.Server(budget_bytes=budget, device=0)
+    ops, pools = [], []
+    share = budget // 6
+    for shape, kappa in specs:
+        for damping in (0.05, 0.2):
+            A = problems.helmholtz(shape, kappa, damping)
+            per = gdmr.load().gdmr_server_slot_bytes(A.n, M, 1 if args.serve_precision == "mixed" else 0)
+            fixed = A.nnz * 40 + A.n * 16 * (3 * K + 1) + (64 << 20)
+            cap = int(max(1, min(args.serve_slots, (share - fixed) // per)))
+            ops.append(srv.add_operator(A, M, K, capacity=cap, precision=args.serve_precision))
+            pools.append([problems.gaussian_source_rhs(shape, 7000 + 97 * len(ops) + j)
+                          for j in range(args.serve_pool)])
+    srv.start()
+    nreq = int(args.rate * args.duration)
+    gaps = rng.exponential(1.0 / args.rate, nreq)
+    choice = rng.integers(0, 6, nreq)
+    tols = rng.choice([1e-6, 1e-8, 1e-10], nreq)
+    tickets = []
+    t0 = time.perf_counter()
+    t_next = t0
+    for i in range(nreq):
+        t_next += gaps[i]
+        delay = t_next - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        j = int(choice[i])
+        tickets.append((j, float(tols[i]), srv.submit(ops[j], pools[j][i % args.serve_pool], tol=float(tols[i]))))
+    lat, ok = [], True
+    for j, tol, t in tickets:
+        x, st = srv.wait(t, timeout=3600)
+        lat.append(st["latency_ms"])
+        ok &= st["status"] == 0 and st["true_rel_res"] <= tol
+    wall = time.perf_counter() - t0
+    line = {"mode": "serve", "metric": METRIC, "value": nreq / wall, "unit": "solves/s",
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+            "requests": nreq, "rate_req_s": args.rate, "arrival_window_s": args.duration, "wall_s": wall,
+            "verified": bool(ok), "precision": args.serve_precision,
+            "capacity": [srv.capacity(o) for o in ops], "device_bytes": srv.device_bytes,
+            "config": {"workload": "serve6_helmholtz", "budget_gb": args.budget_gb, "m": M, "k": K}}
+    srv.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -210,12 +265,22 @@ def main():
     ap.add_argument("--cpu-cycles", type=int, default=3)
     ap.add_argument("--ref-cycles", type=int, default=2)
     ap.add_argument("--max-cycles", type=int, default=3000)
+    ap.add_argument("--serve", action="store_true", help="serving workload instead of the batched bench")
+    ap.add_argument("--serve-precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--duration", type=float, default=2.0, help="arrival window in seconds")
+    ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--serve-slots", type=int, default=64)
+    ap.add_argument("--serve-pool", type=int, default=4)
     ap.add_argument("--solve-only", action="store_true",
                     help="only the timed batched solves (for profiler captures); prints a short line")
     args = ap.parse_args()
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.serve:
+        run_serve(args, rank)
         return
 
     import torch
@@ -266,7 +331,8 @@ def main():
         if rank == 0:
             print(json.dumps({"mode": "solve-only", "value": value, "unit": "solves/s", "nrhs": nrhs,
                               "ms_per_step": elapsed_ms / args.steps, "verified": bool(verified),
-                              "gpu_launches": int(launches), "svd_sweeps": sysm.svd_sweeps()}), flush=True)
+                              "gpu_launches": int(launches), "svd_sweeps": sysm.svd_sweeps(),
+                              "tuning": gdmr.tune_report().strip().splitlines()}), flush=True)
         return
 
     # roofline: one more step with library-side CUDA events per kernel class
@@ -339,6 +405,7 @@ def main():
         "plain_fp64": plain, "mixed_over_plain": value / world / plain["value"],
         "e2e": e2e, "e2e_verified": bool(e2e_ok),
         "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline,
+        "tuning": gdmr.tune_report().strip().splitlines(),
     }
     if rank == 0 and args.cpu_cycles > 0:
         line["cpu_baseline"] = cpu_baseline(A, B[0], args.cpu_cycles, float(np.mean(plain_cycles)))

@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["gdmr_kernels.cu", "gdmr_engine.cu", "gdmr_api.cu"]
+SOURCES = ["gdmr_kernels.cu", "gdmr_engine.cu", "gdmr_api.cu", "gdmr_server.cu"]
 HEADERS = ["gdmr_kernels.cuh", "gdmr_engine.h"]
 PUBLIC = [os.path.join(HERE, "..", "include", h) for h in ("gDMR.h", "gDMRC.h", "gdmr_ext.h")]
 MAJOR, MINOR = "1", "0.1"
@@ -46,7 +46,7 @@ def _stale(target: str, deps: list) -> bool:
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
-def build(force: bool = False, jobs: int = 3, verbose: bool = False) -> str:
+def build(force: bool = False, jobs: int = 4, verbose: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
     os.makedirs(BUILD, exist_ok=True)
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + PUBLIC

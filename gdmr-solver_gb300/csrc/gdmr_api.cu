@@ -380,6 +380,12 @@ extern "C" void gdmrLastStats(gdmr_stats *out) {
 extern "C" long long gdmrKernelLaunches(void) { return launch_count(); }
 extern "C" void gdmrProfile(int on) { profile_enable(on != 0); }
 extern "C" void gdmrProfileReset(void) { profile_reset(); }
+extern "C" void gdmrTune(int on) { tune_enable(on != 0); }
+extern "C" const char *gdmrTuneReport(void) {
+    static thread_local std::string rep;
+    rep = tune_report();
+    return rep.c_str();
+}
 extern "C" int gdmrProfileRead(int kernelClass, double *bytes, double *ms, long long *launches) {
     if (kernelClass < 0 || kernelClass >= KC_COUNT) return fail(GDMR_EINVAL, "gdmrProfileRead", "no such kernel class");
     profile_flush();

@@ -3,8 +3,11 @@
 
 #include <math.h>
 
+#include <algorithm>
 #include <atomic>
+#include <cstdio>
 #include <mutex>
+#include <string>
 #include <vector>
 
 namespace gdmr {
@@ -172,18 +175,49 @@ __device__ void run_finish(const FinishArgs &f, int s, SysState &st, double n2, 
 }
 
 // ----------------------------------------------------------------- multi-dot
+// A CTA owns one chunk of NT*EPT elements of one system.  Thread tid holds EPT/VEC
+// packets of VEC consecutive elements, packet e at element c0 + (e*NT + tid)*VEC, so
+// every load instruction of a warp covers one contiguous 32*VEC*sizeof(C)-byte span
+// (VEC = 2 with complex64: 16-byte loads).
+template <class C, int VEC> struct Pack {
+    C v[VEC];
+};
+template <class C, int VEC> __device__ __forceinline__ Pack<C, VEC> load_pack(const C *p, long i0, int n) {
+    Pack<C, VEC> r;
+    if (VEC == 2 && sizeof(C) == 8 && i0 + 1 < n) {
+        const float4 f = *reinterpret_cast<const float4 *>(p + i0);
+        r.v[0].x = f.x; r.v[0].y = f.y;
+        r.v[VEC - 1].x = f.z; r.v[VEC - 1].y = f.w;
+    } else {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) r.v[j] = (i0 + j < n) ? p[i0 + j] : czero<C>();
+    }
+    return r;
+}
+template <class C, int VEC> __device__ __forceinline__ void store_pack(C *p, long i0, int n, const Pack<C, VEC> &r) {
+    if (VEC == 2 && sizeof(C) == 8 && i0 + 1 < n) {
+        *reinterpret_cast<float4 *>(p + i0) = make_float4(r.v[0].x, r.v[0].y, r.v[VEC - 1].x, r.v[VEC - 1].y);
+    } else {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j)
+            if (i0 + j < n) p[i0 + j] = r.v[j];
+    }
+}
+template <class C> __host__ __device__ constexpr int min_blocks(int ept, int pu) {
+    return ept * pu * (int)sizeof(C) > 128 ? 2 : 3;
+}
+
 // coef_s[p] = <B_p, w_s> for B = [segA (qa vectors) | segB_s (qb vectors)].
-// Grid (systems, chunks); one chunk of NT*EPT elements per CTA, w in registers,
-// PU basis vectors in flight per thread, warp reductions in the working precision.
-template <class R, int PU>
-__global__ void __launch_bounds__(NT, 3) k_mdot(int n, const typename CT<R>::t *__restrict__ segA, int qa,
-                                             const typename CT<R>::t *__restrict__ segB0, size_t strideB, int qb,
-                                             const typename CT<R>::t *__restrict__ w0, size_t strideW,
-                                             const int *__restrict__ act, double2 *__restrict__ partials, int qmax,
-                                             unsigned *tickets, double2 *__restrict__ coef0, size_t strideC,
-                                             SysState *state, int skip_broken) {
+// Grid (systems, chunks), w in registers, PU basis vectors in flight per thread, warp
+// reductions in the working precision, last CTA of each system sums the chunk partials.
+template <class R, int EPT, int PU, int VEC>
+__global__ void __launch_bounds__(NT, min_blocks<typename CT<R>::t>(EPT, PU))
+    k_mdot(int n, const typename CT<R>::t *__restrict__ segA, int qa, const typename CT<R>::t *__restrict__ segB0,
+           size_t strideB, int qb, const typename CT<R>::t *__restrict__ w0, size_t strideW,
+           const int *__restrict__ act, double2 *__restrict__ partials, int qmax, unsigned *tickets,
+           double2 *__restrict__ coef0, size_t strideC, SysState *state, int skip_broken) {
     using C = typename CT<R>::t;
-    constexpr int EPT = ept<R>();
+    constexpr int NP = EPT / VEC;
     const int slot = blockIdx.x, s = act[slot], chunk = blockIdx.y, G = gridDim.y;
     if (skip_broken && state[s].broken) return;
     const C *segB = segB0 + (size_t)s * strideB;
@@ -191,29 +225,25 @@ __global__ void __launch_bounds__(NT, 3) k_mdot(int n, const typename CT<R>::t *
     const int q = qa + qb, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     __shared__ C wsum[NW][QMAX];
     const long c0 = (long)chunk * NT * EPT;
-    C wv[EPT];
+    Pack<C, VEC> wv[NP];
 #pragma unroll
-    for (int e = 0; e < EPT; ++e) {
-        long i = c0 + tid + (long)e * NT;
-        wv[e] = i < n ? w[i] : czero<C>();
-    }
+    for (int e = 0; e < NP; ++e) wv[e] = load_pack<C, VEC>(w, c0 + ((long)e * NT + tid) * VEC, n);
     for (int p0 = 0; p0 < q; p0 += PU) {
-        C vv[PU][EPT];
+        Pack<C, VEC> vv[PU][NP];
 #pragma unroll
         for (int u = 0; u < PU; ++u) {
-            const int p = p0 + u;
+            const int p = p0 + u < q ? p0 + u : q - 1;   // duplicate the last vector; its result is dropped
             const C *vp = p < qa ? segA + (size_t)p * n : segB + (size_t)(p - qa) * n;
 #pragma unroll
-            for (int e = 0; e < EPT; ++e) {
-                long i = c0 + tid + (long)e * NT;
-                vv[u][e] = (p < q && i < n) ? vp[i] : czero<C>();
-            }
+            for (int e = 0; e < NP; ++e) vv[u][e] = load_pack<C, VEC>(vp, c0 + ((long)e * NT + tid) * VEC, n);
         }
 #pragma unroll
         for (int u = 0; u < PU; ++u) {
             C a = czero<C>();
 #pragma unroll
-            for (int e = 0; e < EPT; ++e) cdotacc(a, vv[u][e], wv[e]);
+            for (int e = 0; e < NP; ++e)
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) cdotacc(a, vv[u][e].v[j], wv[e].v[j]);
             a.x = warp_sum(a.x);
             a.y = warp_sum(a.y);
             if (lane == 0 && p0 + u < q) wsum[warp][p0 + u] = a;
@@ -244,16 +274,15 @@ __global__ void __launch_bounds__(NT, 3) k_mdot(int n, const typename CT<R>::t *
 }
 
 // ----------------------------------------------------------------- update + norms
-template <class R, int PU>
-__global__ void __launch_bounds__(NT, 3) k_update(int n, const typename CT<R>::t *__restrict__ segA, int qa,
-                                               const typename CT<R>::t *__restrict__ segB0, size_t strideB, int qb,
-                                               const typename CT<R>::t *__restrict__ w0, size_t strideW,
-                                               typename CT<R>::t *__restrict__ out0, size_t strideO,
-                                               const int *__restrict__ act, const double2 *__restrict__ coef0,
-                                               size_t strideC, double2 *__restrict__ partials, unsigned *tickets,
-                                               SysState *state, FinishArgs fin, int skip_broken) {
+template <class R, int EPT, int PU, int VEC>
+__global__ void __launch_bounds__(NT, min_blocks<typename CT<R>::t>(EPT, PU))
+    k_update(int n, const typename CT<R>::t *__restrict__ segA, int qa, const typename CT<R>::t *__restrict__ segB0,
+             size_t strideB, int qb, const typename CT<R>::t *__restrict__ w0, size_t strideW,
+             typename CT<R>::t *__restrict__ out0, size_t strideO, const int *__restrict__ act,
+             const double2 *__restrict__ coef0, size_t strideC, double2 *__restrict__ partials, unsigned *tickets,
+             SysState *state, FinishArgs fin, int skip_broken) {
     using C = typename CT<R>::t;
-    constexpr int EPT = ept<R>();
+    constexpr int NP = EPT / VEC;
     const int slot = blockIdx.x, s = act[slot], chunk = blockIdx.y, G = gridDim.y;
     if (skip_broken && state[s].broken) return;
     const C *segB = segB0 + (size_t)s * strideB;
@@ -266,41 +295,41 @@ __global__ void __launch_bounds__(NT, 3) k_update(int n, const typename CT<R>::t
     for (int p = tid; p < q; p += NT) cs[p] = from_d<C>(coef[p]);
     __syncthreads();
     const long c0 = (long)chunk * NT * EPT;
-    C acc[EPT], org[EPT];
+    Pack<C, VEC> acc[NP], org[NP];
 #pragma unroll
-    for (int e = 0; e < EPT; ++e) {
-        long i = c0 + tid + (long)e * NT;
-        org[e] = i < n ? w[i] : czero<C>();
+    for (int e = 0; e < NP; ++e) {
+        org[e] = load_pack<C, VEC>(w, c0 + ((long)e * NT + tid) * VEC, n);
         acc[e] = org[e];
     }
     for (int p0 = 0; p0 < q; p0 += PU) {
-        C vv[PU][EPT];
+        Pack<C, VEC> vv[PU][NP];
 #pragma unroll
         for (int u = 0; u < PU; ++u) {
-            const int p = p0 + u;
+            const int p = p0 + u < q ? p0 + u : q - 1;
             const C *vp = p < qa ? segA + (size_t)p * n : segB + (size_t)(p - qa) * n;
 #pragma unroll
-            for (int e = 0; e < EPT; ++e) {
-                long i = c0 + tid + (long)e * NT;
-                vv[u][e] = (p < q && i < n) ? vp[i] : czero<C>();
-            }
+            for (int e = 0; e < NP; ++e) vv[u][e] = load_pack<C, VEC>(vp, c0 + ((long)e * NT + tid) * VEC, n);
         }
 #pragma unroll
         for (int u = 0; u < PU; ++u) {
             if (p0 + u < q) {
                 const C c = cs[p0 + u];
 #pragma unroll
-                for (int e = 0; e < EPT; ++e) cfms(acc[e], c, vv[u][e]);
+                for (int e = 0; e < NP; ++e)
+#pragma unroll
+                    for (int j = 0; j < VEC; ++j) cfms(acc[e].v[j], c, vv[u][e].v[j]);
             }
         }
     }
     C ln = czero<C>(), lc = czero<C>();
 #pragma unroll
-    for (int e = 0; e < EPT; ++e) {
-        long i = c0 + tid + (long)e * NT;
-        if (i < n) out[i] = acc[e];
-        cdotacc(ln, acc[e], acc[e]);
-        cdotacc(lc, acc[e], org[e]);
+    for (int e = 0; e < NP; ++e) {
+        store_pack<C, VEC>(out, c0 + ((long)e * NT + tid) * VEC, n, acc[e]);
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            cdotacc(ln, acc[e].v[j], acc[e].v[j]);
+            cdotacc(lc, acc[e].v[j], org[e].v[j]);
+        }
     }
     double v[3] = {(double)ln.x, (double)lc.x, (double)lc.y};
     block_sum<3>(v, red);
@@ -1151,14 +1180,150 @@ template <class K> void allow_smem(K kernel, size_t bytes) {
 }
 }  // namespace
 
+// ----------------------------------------------------------------- Gram-Schmidt autotuner
+// The projection and update kernels come in (EPT, PU, VEC) variants.  The first launch for a
+// (precision, kernel, n, system-count bucket) times every variant on the caller's own
+// buffers (three runs each, CUDA events on the caller's stream), keeps the fastest, and
+// caches the choice for the process, so later launches (and repeat solves) are bitwise
+// reproducible.  Re-running a variant is harmless: both kernels are idempotent on their
+// inputs (outputs and finishing writes do not alias inputs).
+namespace {
+struct TuneKey {
+    int prec, kernel, n, bucket;
+    bool operator==(const TuneKey &o) const {
+        return prec == o.prec && kernel == o.kernel && n == o.n && bucket == o.bucket;
+    }
+};
+struct TuneEntry {
+    TuneKey key;
+    int variant;
+    float ms[8];
+    int nvar;
+};
+std::vector<TuneEntry> g_tuned;
+std::mutex g_tune_mu;
+bool g_tune_enabled = true;
+
+int bucket_of(int nsys) {
+    int b = 0;
+    while ((1 << b) < nsys) ++b;
+    return b;
+}
+
+template <class F>
+int tuned_variant(int prec, int kernel, int n, int nsys, int nvar, cudaStream_t st, F &&run) {
+    const TuneKey key{prec, kernel, n, bucket_of(nsys)};
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        for (auto &e : g_tuned)
+            if (e.key == key) return e.variant;
+        if (!g_tune_enabled) return 0;
+    }
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    TuneEntry ent{key, 0, {0}, nvar};
+    float best = 1e30f;
+    for (int v = 0; v < nvar; ++v) {
+        run(v);   // warm
+        float t[3];
+        for (int r = 0; r < 3; ++r) {
+            cudaEventRecord(a, st);
+            run(v);
+            cudaEventRecord(b, st);
+            cudaEventSynchronize(b);
+            cudaEventElapsedTime(&t[r], a, b);
+        }
+        std::sort(t, t + 3);
+        ent.ms[v] = t[1];
+        if (t[1] < best) { best = t[1]; ent.variant = v; }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (auto &e : g_tuned)
+        if (e.key == key) return e.variant;
+    g_tuned.push_back(ent);
+    return ent.variant;
+}
+}  // namespace
+
+void tune_enable(bool on) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_enabled = on;
+}
+
+std::string tune_report() {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    std::string out;
+    for (auto &e : g_tuned) {
+        char buf[256];
+        int len = snprintf(buf, sizeof buf, "%s %s n=%d nsys<=%d: variant %d [", e.key.prec == 4 ? "c64" : "c128",
+                           e.key.kernel == 0 ? "projection" : "update", e.key.n, 1 << e.key.bucket, e.variant);
+        out.append(buf, len);
+        for (int v = 0; v < e.nvar; ++v) {
+            len = snprintf(buf, sizeof buf, "%s%.4f", v ? " " : "", e.ms[v]);
+            out.append(buf, len);
+        }
+        out += " ms]\n";
+    }
+    return out;
+}
+
+// Variant tables: (EPT, PU, VEC).
+//   complex64:  0 (8,2,1)  1 (8,2,2)  2 (16,2,2)  3 (8,4,2)
+//   complex128: 0 (4,2,1)  1 (8,2,1)  2 (4,4,1)
+template <class R, int EPT, int PU, int VEC>
+void mdot_v(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
+            const typename CT<R>::t *w, size_t strideW, const int *act, int nsys, double2 *partials, int qmax,
+            unsigned *tickets, double2 *coef, size_t strideC, SysState *state, bool skip_broken, cudaStream_t st) {
+    const int G = (n + NT * EPT - 1) / (NT * EPT);
+    k_mdot<R, EPT, PU, VEC><<<grid2(nsys, G > 0 ? G : 1), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW, act,
+                                                                     partials, qmax, tickets, coef, strideC, state,
+                                                                     skip_broken ? 1 : 0);
+}
+template <class R, int EPT, int PU, int VEC>
+void update_v(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
+              const typename CT<R>::t *w, size_t strideW, typename CT<R>::t *out, size_t strideO, const int *act,
+              int nsys, const double2 *coef, size_t strideC, double2 *partials, unsigned *tickets, SysState *state,
+              FinishArgs fin, bool skip_broken, cudaStream_t st) {
+    const int G = (n + NT * EPT - 1) / (NT * EPT);
+    k_update<R, EPT, PU, VEC><<<grid2(nsys, G > 0 ? G : 1), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW,
+                                                                       out, strideO, act, coef, strideC, partials,
+                                                                       tickets, state, fin, skip_broken ? 1 : 0);
+}
+
+// 16-byte packets need every vector base 16-byte aligned: n even (complex64).
+inline bool vec2_ok(int n, size_t strideB, size_t strideW) { return (n % 2 == 0) && strideB % 2 == 0 && strideW % 2 == 0; }
+
 template <class R>
 void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
                  const typename CT<R>::t *w, size_t strideW, const int *act, int nsys, double2 *partials, int qmax,
                  unsigned *tickets, double2 *coef, size_t strideC, SysState *state, bool skip_broken, cudaStream_t st) {
     if (nsys <= 0 || qa + qb <= 0) return;
     Launch L_(KC_MDOT, (double)sizeof(typename CT<R>::t) * n * ((double)qa + (double)nsys * (qb + 1)), st, 1);
-    k_mdot<R, 2><<<grid2(nsys, nchunks<R>(n)), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW, act, partials, qmax,
-                                                 tickets, coef, strideC, state, skip_broken ? 1 : 0);
+    auto run = [&](int v) {
+        if constexpr (sizeof(R) == 4) {
+            const bool v2 = vec2_ok(n, strideB, strideW);
+            if (v == 1 && v2) mdot_v<R, 8, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+            else if (v == 2 && v2) mdot_v<R, 16, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+            else if (v == 3 && v2) mdot_v<R, 8, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+            else mdot_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+        } else {
+            if (v == 1) mdot_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+            else if (v == 2) mdot_v<R, 4, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+            else mdot_v<R, 4, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+        }
+    };
+    // tune on a representative width only (a full projection of at least 8 vectors)
+    int v = 0;
+    if (qa + qb >= 8 && !profile_enabled()) v = tuned_variant(sizeof(R), 0, n, nsys, sizeof(R) == 4 ? 4 : 3, st, run);
+    else {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        for (auto &e : g_tuned)
+            if (e.key == TuneKey{(int)sizeof(R), 0, n, bucket_of(nsys)}) v = e.variant;
+    }
+    run(v);
 }
 
 template <class R>
@@ -1168,8 +1333,27 @@ void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename 
                    SysState *state, FinishArgs fin, bool skip_broken, cudaStream_t st) {
     if (nsys <= 0) return;
     Launch L_(KC_UPDATE, (double)sizeof(typename CT<R>::t) * n * ((double)qa + (double)nsys * (qb + 2)), st, 1);
-    k_update<R, 2><<<grid2(nsys, nchunks<R>(n)), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, coef,
-                                                   strideC, partials, tickets, state, fin, skip_broken ? 1 : 0);
+    auto run = [&](int v) {
+        if constexpr (sizeof(R) == 4) {
+            const bool v2 = vec2_ok(n, strideB, strideW) && strideO % 2 == 0;
+            if (v == 1 && v2) update_v<R, 8, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+            else if (v == 2 && v2) update_v<R, 16, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+            else if (v == 3 && v2) update_v<R, 8, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+            else update_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+        } else {
+            if (v == 1) update_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+            else if (v == 2) update_v<R, 4, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+            else update_v<R, 4, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+        }
+    };
+    int v = 0;
+    if (qa + qb >= 8 && !profile_enabled()) v = tuned_variant(sizeof(R), 1, n, nsys, sizeof(R) == 4 ? 4 : 3, st, run);
+    else {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        for (auto &e : g_tuned)
+            if (e.key == TuneKey{(int)sizeof(R), 1, n, bucket_of(nsys)}) v = e.variant;
+    }
+    run(v);
 }
 
 template <class R>

@@ -15,6 +15,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 namespace gdmr {
 
 template <class R> struct CT;
@@ -86,6 +88,9 @@ bool profile_enabled();
 void profile_flush();
 void profile_read(int kc, double *bytes, double *ms, long long *launches);
 void profile_reset();
+// Gram-Schmidt variant autotuning (on by default) and its report, one line per tuned shape.
+void tune_enable(bool on);
+std::string tune_report();
 
 // ----------------------------------------------------------------- launchers
 // All launchers enqueue on `st` and never synchronise.

@@ -55,6 +55,8 @@ SIGNATURES = {
     "gdmrProfile": (None, [I]),
     "gdmrProfileReset": (None, []),
     "gdmrProfileRead": (I, [I, P, P, P]),
+    "gdmrTune": (None, [I]),
+    "gdmrTuneReport": (ctypes.c_char_p, []),
     "gdmr_system_create": (I, [P, I, P, P, P, I, I, I, I, I]),
     "gdmr_system_destroy": (I, [P]),
     "gdmr_system_bytes": (LL, [P]),
@@ -65,6 +67,16 @@ SIGNATURES = {
     "gdmr_export_deflation": (I, [P, P]),
     "gdmr_import_deflation": (I, [P, P]),
     "gdmr_drop_deflation": (I, [P]),
+    "gdmr_server_create": (I, [P, LL, I]),
+    "gdmr_server_add_operator": (I, [P, I, P, P, P, I, I, I, I, P]),
+    "gdmr_server_slot_bytes": (LL, [I, I, I]),
+    "gdmr_server_operator_capacity": (I, [P, I]),
+    "gdmr_server_bytes": (LL, [P]),
+    "gdmr_server_start": (I, [P]),
+    "gdmr_server_submit": (I, [P, I, P, P, D, I, P]),
+    "gdmr_server_wait": (I, [P, LL, D, P]),
+    "gdmr_server_poll": (I, [P, P, P, I]),
+    "gdmr_server_destroy": (I, [P]),
 }
 
 STATUS = {0: "GDMR_OK", 1: "GDMR_EINVAL", 2: "GDMR_ENOMEM", 3: "GDMR_ENOCONV", 4: "GDMR_ERUNAWAY",
@@ -93,6 +105,14 @@ def profile(on: bool) -> None:
 
 def profile_reset() -> None:
     load().gdmrProfileReset()
+
+
+def tune_report() -> str:
+    return load().gdmrTuneReport().decode()
+
+
+def tune(on: bool) -> None:
+    load().gdmrTune(1 if on else 0)
 
 
 def profile_read() -> dict:
@@ -324,3 +344,62 @@ class System:
 
     def drop_deflation(self):
         _check(self.L.gdmr_drop_deflation(self._h), "gdmr_drop_deflation")
+
+
+class Server:
+    """Serving layer (gdmr_server_*): resident operators with their deflation spaces,
+    continuous batching of requests, admission bounded by a device-memory budget."""
+
+    def __init__(self, budget_bytes: int, device: int = 0):
+        self.L = load()
+        h = ctypes.c_void_p()
+        _check(self.L.gdmr_server_create(ctypes.byref(h), int(budget_bytes), device), "gdmr_server_create")
+        self._h = h
+        self._keep = {}          # ticket -> (b, x) buffers that must outlive the request
+        self.n = {}
+
+    def add_operator(self, A, basis: int, deflat: int, capacity: int = 0, precision: str = "mixed") -> int:
+        indptr, indices = _csr_arrays(A)
+        vals = np.ascontiguousarray(A.data, dtype=np.complex128)
+        op = ctypes.c_int()
+        _check(self.L.gdmr_server_add_operator(self._h, A.n, _ptr(indptr), _ptr(indices), _ptr(vals), basis, deflat,
+                                               capacity, {"fp64": 0, "mixed": 1}[precision], ctypes.byref(op)),
+               "gdmr_server_add_operator")
+        self.n[op.value] = A.n
+        return op.value
+
+    def capacity(self, op: int) -> int:
+        return int(self.L.gdmr_server_operator_capacity(self._h, op))
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self.L.gdmr_server_bytes(self._h))
+
+    def start(self):
+        _check(self.L.gdmr_server_start(self._h), "gdmr_server_start")
+
+    def submit(self, op: int, b, tol: float = 1e-10, max_cycles: int = 5000) -> int:
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.zeros_like(b)
+        t = ctypes.c_longlong()
+        _check(self.L.gdmr_server_submit(self._h, op, _ptr(b), _ptr(x), float(tol), int(max_cycles),
+                                         ctypes.byref(t)), "gdmr_server_submit")
+        self._keep[t.value] = (b, x)
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = 0.0):
+        st = Stats()
+        _check(self.L.gdmr_server_wait(self._h, int(ticket), float(timeout), ctypes.byref(st)), "gdmr_server_wait")
+        b, x = self._keep.pop(ticket)
+        return x, st.as_dict()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.L.gdmr_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -215,6 +215,12 @@ def config_3d128():
     return A, (lambda count=32: drifting_sequence(A.n, count, seed=11)), dict(m=60, k=20, tol=1e-10)
 
 
+def shard_seeds(nrhs: int, rank: int) -> list:
+    """Seeds of the right-hand sides a rank solves when independent systems shard across
+    ranks (weak scaling): rank r gets 100 + 1000 r + [0, nrhs)."""
+    return [100 + 1000 * rank + r for r in range(nrhs)]
+
+
 def config_3d96_batch(count: int = 64):
     """3D 7-point Helmholtz 96^3, kappa=24, damping 0.1; `count` Gaussian-source RHS; m=48, k=24."""
     shape = (96, 96, 96)

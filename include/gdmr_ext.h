@@ -87,6 +87,11 @@ long long gdmrKernelLaunches(void);
 void gdmrProfile(int on);
 void gdmrProfileReset(void);
 int gdmrProfileRead(int kernelClass, double *bytes, double *ms, long long *launches);
+/* Gram-Schmidt kernel autotuning: the first launch of a shape times the kernel variants
+ * and keeps the fastest for the process (on by default; off selects the first variant).
+ * The report lists one line per tuned shape with the time of every variant. */
+void gdmrTune(int on);
+const char *gdmrTuneReport(void);
 
 /* ---- context API: one resident operator, many right-hand sides -------------
  * A gdmr_system holds a CSR operator on the device (SELL-32, complex64 and
@@ -127,6 +132,33 @@ int gdmr_true_residual(gdmr_system *sys, int nrhs, const double *b, const double
 int gdmr_export_deflation(gdmr_system *sys, double *z);
 int gdmr_import_deflation(gdmr_system *sys, const double *z);
 int gdmr_drop_deflation(gdmr_system *sys);
+
+/* ---- serving: resident operators, HBM-budget admission, continuous batching ----
+ * A server holds several resident operators.  Each has its matrix, its recycled
+ * deflation space and an engine of `capacity` slots: device memory fixed at
+ * registration and bounded by the server's budget (capacity 0: as many slots as
+ * the remaining budget allows, at most 256).  After gdmr_server_start, one worker
+ * per operator admits queued requests into free slots between restart cycles and
+ * runs FP64-refined cycles for all requests in flight; operators run on separate
+ * streams.  b and x are caller-owned host buffers (n interleaved complex128) that
+ * must stay valid until the request completes. */
+typedef struct gdmr_server gdmr_server;
+int gdmr_server_create(gdmr_server **out, long long budgetBytes, int device);
+int gdmr_server_add_operator(gdmr_server *srv, int n, const int *rowPtr, const int *colIdx, const double *vals_ri,
+                             int basisDim, int deflatDim, int capacity, int precision, int *opId);
+/* Device bytes one slot costs (basis, work vectors, FP64 slot vectors). */
+long long gdmr_server_slot_bytes(int n, int basisDim, int precision);
+int gdmr_server_operator_capacity(gdmr_server *srv, int opId);
+long long gdmr_server_bytes(gdmr_server *srv);
+int gdmr_server_start(gdmr_server *srv);
+int gdmr_server_submit(gdmr_server *srv, int opId, const double *b, double *x, double tol, int maxCycles,
+                       long long *ticket);
+/* Blocks until the request is done (or timeout_s passes; <= 0 waits without limit). */
+int gdmr_server_wait(gdmr_server *srv, long long ticket, double timeout_s, gdmr_stats *stats);
+/* Up to max completed requests since the last poll; returns how many. */
+int gdmr_server_poll(gdmr_server *srv, long long *tickets, gdmr_stats *stats, int max);
+/* Drains the queues, stops the workers and frees everything. */
+int gdmr_server_destroy(gdmr_server *srv);
 
 #ifdef __cplusplus
 }
