@@ -661,3 +661,134 @@ extern "C" int gdmr_drop_deflation(gdmr_system *S) {
     S->e64.drop_deflation();
     return GDMR_OK;
 }
+
+// ================================================================ allocation-free residual check
+// gdmr_true_residual_noalloc: the FP64 relative residual ||b_s - A x_s|| / ||b_s|| of up to
+// GDMR_NOALLOC_MAX_RHS pairs on the caller's device buffers, for callers that must not allocate
+// device memory: code running while a stream is being captured into a CUDA graph (cudaMalloc
+// is not a capturable operation), hosts that own the whole device-memory pool, and
+// latency-critical loops where an allocation could stall.  It allocates nothing: the
+// cross-CTA reduction scratch is the file-scope array below (256 KB of partial sums plus the
+// arrival counters), which every GPU that loads this library holds until the process exits.
+//
+// Set-up: the first call on a device (with that device current) looks the arrays up with
+// cudaGetSymbolAddress and zeroes the counters; make that first call before any stream
+// capture.  All calls share the arrays, which keep the last call's contents: the counters
+// return to zero at the end of every call, and calls that overlap on the GPU race on them.
+namespace {
+
+constexpr int NOALLOC_MAX_RHS = 64;
+constexpr int NOALLOC_CTAS = 256;                  // CTAs per right-hand side (grid-stride)
+__device__ __align__(256) double g_noalloc_partials[NOALLOC_MAX_RHS * 2 * NOALLOC_CTAS];
+__device__ __align__(256) unsigned g_noalloc_tickets[NOALLOC_MAX_RHS];
+
+struct NoallocScratch {
+    double *partials = nullptr;
+    unsigned *tickets = nullptr;
+};
+constexpr int NOALLOC_MAX_DEVICES = 64;
+NoallocScratch g_noalloc[NOALLOC_MAX_DEVICES];
+std::mutex g_noalloc_mu;
+
+int noalloc_scratch(int device, NoallocScratch *out) {
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES)
+        return fail(GDMR_EINVAL, "gdmr_true_residual_noalloc", "device ordinal out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    NoallocScratch &s = g_noalloc[device];
+    if (!s.partials) {
+        void *p = nullptr, *t = nullptr;
+        cudaError_t e1 = cudaGetSymbolAddress(&p, g_noalloc_partials);
+        cudaError_t e2 = cudaGetSymbolAddress(&t, g_noalloc_tickets);
+        if (e1 != cudaSuccess || e2 != cudaSuccess)
+            return fail(GDMR_ECUDA, "gdmr_true_residual_noalloc", "cudaGetSymbolAddress failed");
+        if (cudaMemset(t, 0, sizeof(g_noalloc_tickets)) != cudaSuccess)
+            return fail(GDMR_ECUDA, "gdmr_true_residual_noalloc", "clearing the arrival counters failed");
+        s.partials = (double *)p;
+        s.tickets = (unsigned *)t;
+    }
+    *out = s;
+    return GDMR_OK;
+}
+
+// One kernel: ||b - A x||^2 and ||b||^2 per right-hand side over a grid-stride row loop, CTA
+// partials into the static scratch, the last CTA of each right-hand side sums them in order.
+__global__ void __launch_bounds__(256) k_relres_noalloc(int n, const int *__restrict__ slice_ptr,
+                                                        const int *__restrict__ cols,
+                                                        const double2 *__restrict__ vals,
+                                                        const double2 *__restrict__ b0,
+                                                        const double2 *__restrict__ x0, double *partials,
+                                                        unsigned *tickets, double *relres) {
+    const int s = blockIdx.x, G = gridDim.y, tid = threadIdx.x;
+    const double2 *b = b0 + (size_t)s * n;
+    const double2 *x = x0 + (size_t)s * n;
+    double r2 = 0, b2 = 0;
+    for (long row = (long)blockIdx.y * 256 + tid; row < n; row += (long)G * 256) {
+        const int slice = (int)(row >> 5), lane = (int)(row & 31);
+        const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
+        const double2 bv = b[row];
+        double2 acc = bv;
+        for (int c = 0; c < width; ++c) {
+            const int e = beg + c * 32 + lane;
+            const double2 a = vals[e], xv = x[cols[e]];
+            // the same fused sequence as the allocating residual kernel: near convergence the
+            // residual cancels ~10 digits, so the per-entry rounding must match exactly
+            acc.x = fma(-a.x, xv.x, acc.x);
+            acc.x = fma(a.y, xv.y, acc.x);
+            acc.y = fma(-a.x, xv.y, acc.y);
+            acc.y = fma(-a.y, xv.x, acc.y);
+        }
+        r2 += acc.x * acc.x + acc.y * acc.y;
+        b2 += bv.x * bv.x + bv.y * bv.y;
+    }
+    __shared__ double red[2][8];
+    __shared__ unsigned last;
+    for (int o = 16; o > 0; o >>= 1) {
+        r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+        b2 += __shfl_xor_sync(0xffffffffu, b2, o);
+    }
+    if ((tid & 31) == 0) { red[0][tid >> 5] = r2; red[1][tid >> 5] = b2; }
+    __syncthreads();
+    double *part = partials + (size_t)s * 2 * NOALLOC_CTAS;
+    if (tid == 0) {
+        double a = 0, c = 0;
+        for (int w = 0; w < 8; ++w) { a += red[0][w]; c += red[1][w]; }
+        part[blockIdx.y] = a;
+        part[NOALLOC_CTAS + blockIdx.y] = c;
+        __threadfence();
+        last = atomicAdd(&tickets[s], 1u) == (unsigned)G - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (tid == 0) {
+        double a = 0, c = 0;
+        for (int g = 0; g < G; ++g) { a += __ldcg(part + g); c += __ldcg(part + NOALLOC_CTAS + g); }
+        relres[s] = c > 0 ? sqrt(a) / sqrt(c) : sqrt(a);
+        tickets[s] = 0;   // ready for the next call
+    }
+}
+
+}  // namespace
+
+extern "C" int gdmr_true_residual_noalloc(gdmr_system *S, int nrhs, const double *b, const double *x,
+                                          double *relres, void *stream) {
+    if (!S || !b || !x || !relres) return fail(GDMR_EINVAL, "gdmr_true_residual_noalloc", "null argument");
+    if (nrhs < 1 || nrhs > NOALLOC_MAX_RHS)
+        return fail(GDMR_EINVAL, "gdmr_true_residual_noalloc",
+                    "nrhs must be between 1 and 64 (the size of the static reduction scratch)");
+    if (!S->A.vals64) return fail(GDMR_ENOTINIT, "gdmr_true_residual_noalloc", "system has no FP64 operator");
+    if (cudaSetDevice(S->device) != cudaSuccess)
+        return fail(GDMR_ECUDA, "gdmr_true_residual_noalloc", "cudaSetDevice failed");
+    NoallocScratch sc;
+    int rc = noalloc_scratch(S->device, &sc);
+    if (rc != GDMR_OK) return rc;
+    int G = (S->n + 255) / 256;
+    if (G > NOALLOC_CTAS) G = NOALLOC_CTAS;
+    if (G < 1) G = 1;
+    k_relres_noalloc<<<dim3((unsigned)nrhs, (unsigned)G), 256, 0, (cudaStream_t)stream>>>(
+        S->n, S->A.slice_ptr, S->A.cols, S->A.vals64, (const double2 *)b, (const double2 *)x, sc.partials,
+        sc.tickets, relres);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(GDMR_ECUDA, "gdmr_true_residual_noalloc", cudaGetErrorString(e));
+    return GDMR_OK;
+}

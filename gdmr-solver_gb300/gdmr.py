@@ -64,6 +64,7 @@ SIGNATURES = {
     "gdmr_solve": (I, [P, I, P, P, D, I, I, P]),
     "gdmr_solve_batch": (I, [P, I, P, P, P, I, I, P]),
     "gdmr_true_residual": (I, [P, I, P, P, I, P]),
+    "gdmr_true_residual_noalloc": (I, [P, I, P, P, P, P]),
     "gdmr_export_deflation": (I, [P, P]),
     "gdmr_import_deflation": (I, [P, P]),
     "gdmr_drop_deflation": (I, [P]),
@@ -332,6 +333,13 @@ class System:
         out = np.zeros(B.shape[0])
         _check(self.L.gdmr_true_residual(self._h, B.shape[0], _ptr(B), _ptr(X), 0, _ptr(out)), "gdmr_true_residual")
         return out
+
+    def true_residual_noalloc(self, b_ptr: int, x_ptr: int, out_ptr: int, nrhs: int, stream: int = 0):
+        """gdmr_true_residual_noalloc on caller-owned device buffers (raw pointers); enqueued on
+        `stream` without synchronising; allocates nothing."""
+        _check(self.L.gdmr_true_residual_noalloc(self._h, int(nrhs), ctypes.c_void_p(b_ptr), ctypes.c_void_p(x_ptr),
+                                                 ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream)),
+               "gdmr_true_residual_noalloc")
 
     def export_deflation(self):
         Z = np.zeros((self.k, self.n), np.complex128)

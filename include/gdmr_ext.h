@@ -127,6 +127,18 @@ int gdmr_solve_batch(gdmr_system *sys, int nrhs, const double *b, double *x, con
 /* FP64 ||b_s - A x_s|| / ||b_s|| for nrhs pairs. */
 int gdmr_true_residual(gdmr_system *sys, int nrhs, const double *b, const double *x, int on_device, double *relres);
 
+/* Allocation-free residual check (no counterpart in the reference): the FP64
+ * ||b_s - A x_s|| / ||b_s|| of nrhs <= 64 pairs, b, x and relres all caller-owned device
+ * buffers (complex128 interleaved; relres nrhs doubles), enqueued on `stream` (a
+ * cudaStream_t, NULL for the default stream) without synchronising.  For callers that
+ * cannot call cudaMalloc: code inside a CUDA-graph stream capture, hosts that own the
+ * device-memory pool, latency-critical loops.  It uses a 256 KB static device array as
+ * reduction scratch instead of allocating; the first call on a device sets that up
+ * (cudaGetSymbolAddress), so make it before any stream capture.  Calls share the array:
+ * calls that overlap on the GPU race.  nrhs above 64 is rejected with GDMR_EINVAL. */
+int gdmr_true_residual_noalloc(gdmr_system *sys, int nrhs, const double *b, const double *x, double *relres,
+                               void *stream);
+
 /* Deflation space in and out: deflatDim x n interleaved complex128 on the host.
  * Import makes the next solve start from it; drop forgets it. */
 int gdmr_export_deflation(gdmr_system *sys, double *z);
