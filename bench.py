@@ -253,6 +253,93 @@ def run_serve(args, rank):
         print(json.dumps(line), flush=True)
 
 
+def run_multi_operator(args, rank):
+    """BASELINE configs[3]: 48 independent operators, 3D 7-point -div(a grad u) - kappa^2 (1+0.1i) u
+    with per-axis edge lengths log-uniform in [32, 128] (seeded), a piecewise constant on 8^3
+    blocks (Re U[1,4], Im U[0,0.2]), kappa 16; 4 complex Gaussian right-hand sides each;
+    m = 40, k = 16, tolerance 1e-9.  All 48 operators are resident at once, each with its own
+    engine and stream (the serving layer), so their restart cycles overlap on the device.
+    The metric is solves/s over the whole set (192 solves) and p50/p99 latency."""
+    import gdmr
+    gdmr.load()
+    u = problems.uniform01(31, 3 * args.operators)
+    shapes = [tuple(int(round(math.exp(math.log(32) + (math.log(128) - math.log(32)) * u[3 * i + a])))
+                    for a in range(3)) for i in range(args.operators)]
+    mats = [problems.variable_helmholtz(sh, 16.0, 0.1, seed=500 + i) for i, sh in enumerate(shapes)]
+    per_op = args.rhs_per_operator
+    srv = gdmr.Server(budget_bytes=int(args.budget_gb * (1 << 30)), device=0)
+    ops = [srv.add_operator(A, 40, 16, capacity=per_op, precision=args.serve_precision) for A in mats]
+    rhs = [[problems.unit_gaussian_rhs(A.n, 9000 + 10 * i + j) for j in range(per_op)] for i, A in enumerate(mats)]
+    srv.start()
+    t0 = time.perf_counter()
+    tickets = [(i, srv.submit(ops[i], rhs[i][j], tol=1e-9)) for i in range(len(mats)) for j in range(per_op)]
+    lat, ok, cyc = [], True, []
+    for i, t in tickets:
+        x, st = srv.wait(t, timeout=3600)
+        lat.append(st["latency_ms"])
+        cyc.append(st["cycles"])
+        ok &= st["status"] == 0 and st["true_rel_res"] <= 1e-9
+    wall = time.perf_counter() - t0
+    line = {"mode": "multi-operator", "metric": METRIC, "value": len(tickets) / wall, "unit": "solves/s",
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+            "solves": len(tickets), "wall_s": wall, "verified": bool(ok), "precision": args.serve_precision,
+            "cycles": {"mean": float(np.mean(cyc)), "max": int(np.max(cyc))},
+            "n_range": [min(A.n for A in mats), max(A.n for A in mats)],
+            "config": {"workload": "variable_helmholtz_48ops", "operators": len(mats), "rhs_per_operator": per_op,
+                       "m": 40, "k": 16, "tol": 1e-9}}
+    srv.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_small(args, rank):
+    """BASELINE configs[0] (the reference-parity case): 2D 5-point Helmholtz 64x64, kappa 20,
+    damping 0.05; 8 unit Gaussian right-hand sides solved in sequence with the recycled
+    deflation space (mode 0 then 1); m = 40, k = 10, tol 1e-10; the plain FP64 drop-in
+    (reference algorithm in complex128) through gdmr_solve, with and without CUDA graphs,
+    beside the host oracle on all host cores."""
+    import gdmr
+    gdmr.load()
+    A, rhs, cfg = problems.config_2d64()
+    out = {}
+    for graphs in (False, True):
+        s = gdmr.System(A, cfg["m"], cfg["k"], capacity=1, precision="fp64")
+        s.set_graphs(graphs)
+        s.solve(rhs[0], mode=0, tol=cfg["tol"], mat_rank=2000)      # warm-up (tuning, first capture)
+        s.drop_deflation()
+        t = time.perf_counter()
+        cyc, ok = [], True
+        for i, b in enumerate(rhs):
+            x, st = s.solve(b, mode=0 if i == 0 else 1, tol=cfg["tol"], mat_rank=2000)
+            cyc.append(st["cycles"])
+            ok &= st["status"] == 0 and st["true_rel_res"] <= 2 * cfg["tol"]
+        el = time.perf_counter() - t
+        out["graphs" if graphs else "eager"] = {"solves_s": len(rhs) / el, "ms_per_solve": el / len(rhs) * 1e3,
+                                                "cycles": cyc, "verified": bool(ok)}
+        if not graphs:
+            gdmr.profile_reset()
+            gdmr.profile(True)
+            s.solve(rhs[0], mode=1, tol=cfg["tol"], mat_rank=2000)
+            gdmr.profile(False)
+            pp = gdmr.profile_read()
+            pt = sum(v["ms"] for v in pp.values())
+            out["eager"]["classes_ms_share"] = {k: round(v["ms"] / pt, 4) for k, v in pp.items() if v["launches"]}
+            out["eager"]["kernel_ms_per_cycle"] = pt / max(1, st["cycles"])
+        s.close()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    o = oracle.Oracle(A, cfg["m"], cfg["k"], threads=os.cpu_count() or 1, fuse_deflation=True)
+    t = time.perf_counter()
+    ocyc = [o.solve(b, mode=0 if i == 0 else 1, tol=cfg["tol"], mat_rank=2000)["cycles"] for i, b in enumerate(rhs)]
+    el = time.perf_counter() - t
+    line = {"mode": "small", "metric": METRIC, "value": out["graphs"]["solves_s"], "unit": "solves/s",
+            "plain_fp64": out, "cpu_oracle": {"solves_s": len(rhs) / el, "cycles": ocyc, "cores": os.cpu_count()},
+            "config": {"workload": "helmholtz2d64_8rhs", "n": A.n, "nnz": A.nnz, "m": cfg["m"], "k": cfg["k"],
+                       "tol": cfg["tol"]}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -266,6 +353,10 @@ def main():
     ap.add_argument("--ref-cycles", type=int, default=2)
     ap.add_argument("--max-cycles", type=int, default=3000)
     ap.add_argument("--serve", action="store_true", help="serving workload instead of the batched bench")
+    ap.add_argument("--multi-operator", action="store_true", help="48-operator workload instead of the batched bench")
+    ap.add_argument("--small", action="store_true", help="64x64 reference-parity case (plain FP64 drop-in)")
+    ap.add_argument("--operators", type=int, default=48)
+    ap.add_argument("--rhs-per-operator", type=int, default=4)
     ap.add_argument("--serve-precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--rate", type=float, default=200.0)
     ap.add_argument("--duration", type=float, default=2.0, help="arrival window in seconds")
@@ -281,6 +372,12 @@ def main():
         return
     if args.serve:
         run_serve(args, rank)
+        return
+    if args.multi_operator:
+        run_multi_operator(args, rank)
+        return
+    if args.small:
+        run_small(args, rank)
         return
 
     import torch

@@ -589,6 +589,14 @@ extern "C" long long gdmr_system_bytes(const gdmr_system *S) {
                        2 * sizeof(double2) * (size_t)S->n * std::max(S->cap, 2));
 }
 
+extern "C" int gdmr_system_set_graphs(gdmr_system *S, int on) {
+    if (!S) return fail(GDMR_EINVAL, "gdmr_system_set_graphs", "null system");
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->e32.use_graphs = on != 0;
+    S->e64.use_graphs = on != 0;
+    return GDMR_OK;
+}
+
 extern "C" int gdmr_system_svd_sweeps(const gdmr_system *S) {
     if (!S) return 0;
     return S->precision == 1 ? S->e32.last_svd_sweeps() : S->e64.last_svd_sweeps();
@@ -652,6 +660,22 @@ extern "C" int gdmr_import_deflation(gdmr_system *S, const double *z) {
     std::vector<float2> tmp((size_t)S->k * S->n);
     for (size_t i = 0; i < tmp.size(); ++i) tmp[i] = make_float2((float)z[2 * i], (float)z[2 * i + 1]);
     return S->e32.import_deflation(tmp.data());
+}
+
+extern "C" int gdmr_save_deflation(gdmr_system *S, const char *path) {
+    if (!S || !path) return fail(GDMR_EINVAL, "gdmr_save_deflation", "null argument");
+    std::vector<double> z((size_t)2 * S->k * S->n);
+    int rc = gdmr_export_deflation(S, z.data());
+    if (rc != GDMR_OK) return rc;
+    return gdmr_deflation_write(path, S->n, S->k, z.data());
+}
+
+extern "C" int gdmr_load_deflation(gdmr_system *S, const char *path) {
+    if (!S || !path) return fail(GDMR_EINVAL, "gdmr_load_deflation", "null argument");
+    std::vector<double> z((size_t)2 * S->k * S->n);
+    int rc = gdmr_deflation_read(path, S->n, S->k, z.data());
+    if (rc != GDMR_OK) return rc;
+    return gdmr_import_deflation(S, z.data());
 }
 
 extern "C" int gdmr_drop_deflation(gdmr_system *S) {

@@ -183,6 +183,11 @@ template <class R> int Engine<R>::alloc(void **p, size_t bytes) {
 }
 
 template <class R> void Engine<R>::release() {
+    for (auto &g : graphs_) cudaGraphExecDestroy(g.exec);
+    graphs_.clear();
+    cycles_run_ = 0;
+    zpar_ = 0;
+    lead_dev_ = nullptr;
     if (side_) {
         cudaStreamSynchronize(side_);
         cudaStreamDestroy(side_);
@@ -255,6 +260,7 @@ template <class R> int Engine<R>::init(int n, int m, int k, int capacity, int de
     A_(act_, sizeof(int) * (capacity + 1));
     A_(ident_, sizeof(int) * (capacity + 1));
     A_(partials_side_, sizeof(double) * scratch_doubles(16, 1, 1));
+    A_(lead_dev_, sizeof(int));
     A_(ticket_side_, sizeof(unsigned));
 #undef A_
     if (cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking) != cudaSuccess ||
@@ -330,6 +336,7 @@ template <class R> int Engine<R>::sync_deflation() {
     if (!z_pending_) return GDMR_OK;
     GDMR_CK(cudaStreamWaitEvent(stream, ev_zdone_, 0));
     std::swap(Z_, Znew_);
+    zpar_ ^= 1;
     have_z_ = true;
     z_pending_ = false;
     return GDMR_OK;
@@ -337,6 +344,59 @@ template <class R> int Engine<R>::sync_deflation() {
 
 template <class R> int Engine<R>::run_cycle(int kk, int nsys, int lead, double tol, long *matvecs) {
     if (sync_deflation() != GDMR_OK) return GDMR_ECUDA;
+    lead_host_ = lead;
+    GDMR_CK(cudaMemcpyAsync(lead_dev_, &lead_host_, sizeof(int), cudaMemcpyHostToDevice, stream));
+    // CUDA graphs pay off where launch overhead is comparable to the work: small n x batch.
+    // The first cycle of an engine always runs eagerly (it also tunes the kernels).
+    const bool graphable = use_graphs && op.kind != Operator<R>::HOOK && !profile_enabled() && cycles_run_ > 0 &&
+                           (long)n_ * nsys <= (1L << 20);
+    ++cycles_run_;
+    if (!graphable) return enqueue_cycle(kk, nsys, tol, matvecs, false);
+    const int zpar = zpar_;
+    cudaGraphExec_t exec = nullptr;
+    for (auto &g : graphs_)
+        if (g.kk == kk && g.nsys == nsys && g.zpar == zpar && g.tol == tol) exec = g.exec;
+    if (!exec) {
+        if (graphs_.size() >= 32) {
+            for (auto &g : graphs_) cudaGraphExecDestroy(g.exec);
+            graphs_.clear();
+        }
+        GDMR_CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        set_capturing(true);
+        long mv = 0;
+        const bool hz = have_z_, zp = z_pending_;
+        int rc = enqueue_cycle(kk, nsys, tol, &mv, true);
+        set_capturing(false);
+        have_z_ = hz;
+        z_pending_ = zp;
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(stream, &graph);
+        if (rc != GDMR_OK) { if (graph) cudaGraphDestroy(graph); return rc; }
+        if (e != cudaSuccess) {
+            set_last_error(GDMR_ECUDA, std::string("restart-cycle capture: ") + cudaGetErrorString(e));
+            return GDMR_ECUDA;
+        }
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            set_last_error(GDMR_ECUDA, std::string("restart-cycle graph: ") + cudaGetErrorString(e));
+            return GDMR_ECUDA;
+        }
+        graphs_.push_back(GraphEntry{kk, nsys, zpar, tol, exec});
+    }
+    GDMR_CK(cudaGraphLaunch(exec, stream));
+    // the graph joins the deflation update into the main stream: the new Z is ready in order
+    *matvecs += kk + (long)nsys * (m_ - kk);
+    if (k_ > 0) {
+        std::swap(Z_, Znew_);
+        zpar_ ^= 1;
+        have_z_ = true;
+        z_pending_ = false;
+    }
+    return GDMR_OK;
+}
+
+template <class R> int Engine<R>::enqueue_cycle(int kk, int nsys, double tol, long *matvecs, bool join) {
     const int n = n_, m = m_;
     const size_t sV = strideV(), sC = strideC();
     const bool hook = op.kind == Operator<R>::HOOK;
@@ -406,8 +466,9 @@ template <class R> int Engine<R>::run_cycle(int kk, int nsys, int lead, double t
     if (k_ > 0) {
         GDMR_CK(cudaEventRecord(ev_krylov_, stream));
         GDMR_CK(cudaStreamWaitEvent(side_, ev_krylov_, 0));
-        launch_svd_smallest(m, k_, H_ + (size_t)lead * strideH(), vs_, sigma_, svdwork_, sweeps_, side_);
-        launch_zupdate<R>(n, kk, m, k_, Z_, Vs(lead), vs_, Znew_, partials_side_, ticket_side_, znorm2_, side_);
+        launch_svd_smallest(m, k_, H_, strideH(), lead_dev_, vs_, sigma_, svdwork_, sweeps_, side_);
+        launch_zupdate<R>(n, kk, m, k_, Z_, V_, sV, lead_dev_, vs_, Znew_, partials_side_, ticket_side_, znorm2_,
+                          side_);
         launch_znormalise<R>(n, k_, Znew_, znorm2_, Znew_, side_);
         GDMR_CK(cudaEventRecord(ev_zdone_, side_));
         z_pending_ = true;
@@ -421,6 +482,8 @@ template <class R> int Engine<R>::run_cycle(int kk, int nsys, int lead, double t
     launch_combine<R>(n, kk, m, W_, Z_, V_, sV, R_, n, X_, n, t_, y_, sC, act_, nsys, partials_, tickets_, state_,
                       stream);
     launch_scale<R>(n, R_, n, R_, n, nullptr, 0, act_, nsys, state_, false, stream);
+    // a captured cycle must join the side stream before the capture ends
+    if (join && k_ > 0) GDMR_CK(cudaStreamWaitEvent(stream, ev_zdone_, 0));
     GDMR_CK(cudaGetLastError());
     return GDMR_OK;
 }

@@ -82,6 +82,7 @@ template <class R> class Engine {
 
     Operator<R> op;
     cudaStream_t stream = nullptr;
+    bool use_graphs = true;     // capture restart cycles of small systems as CUDA graphs
     bool compat_eye = true;     // reproduce the reference's breakdown identity tail (gDMR.cu:2275)
 
     // Reference semantics on system 0 (solverDMR): b, x are device vectors of precision R;
@@ -168,6 +169,16 @@ template <class R> class Engine {
     double2 *partials_side_ = nullptr;
     unsigned *ticket_side_ = nullptr;
     int sync_deflation();
+    // restart-cycle graphs (key: deflation dimension, batch size, Z buffer parity, tolerance)
+    struct GraphEntry {
+        int kk, nsys, zpar;
+        double tol;
+        cudaGraphExec_t exec;
+    };
+    std::vector<GraphEntry> graphs_;
+    int cycles_run_ = 0, zpar_ = 0, lead_host_ = 0;
+    int *lead_dev_ = nullptr;
+    int enqueue_cycle(int kk, int nsys, double tol, long *matvecs, bool join);
 
     size_t strideV() const { return (size_t)(m_ + 1) * n_; }
     size_t strideH() const { return (size_t)(m_ + 1) * m_; }

@@ -466,10 +466,12 @@ __global__ void __launch_bounds__(NT) k_combine(int n, int kk, int m, const type
 // ----------------------------------------------------------------- deflation-space update
 template <class R, int KB>
 __global__ void __launch_bounds__(NT) k_zupdate(int n, int kk, int m, int k, int t0, const typename CT<R>::t *__restrict__ Z,
-                                                const typename CT<R>::t *__restrict__ V,
-                                                const double2 *__restrict__ vs, typename CT<R>::t *__restrict__ Znew,
-                                                double2 *__restrict__ partials, unsigned *ticket, double *znorm2) {
+                                                const typename CT<R>::t *__restrict__ V0, size_t strideV,
+                                                const int *__restrict__ lead, const double2 *__restrict__ vs,
+                                                typename CT<R>::t *__restrict__ Znew, double2 *__restrict__ partials,
+                                                unsigned *ticket, double *znorm2) {
     using C = typename CT<R>::t;
+    const typename CT<R>::t *__restrict__ V = V0 + (size_t)(*lead) * strideV;
     extern __shared__ unsigned char smraw[];
     C *cs = reinterpret_cast<C *>(smraw);            // m x KB coefficients
     __shared__ double red[KB][NW];
@@ -748,9 +750,11 @@ __device__ int jacobi_sweeps(int m, typename CX<T>::t *A, typename CX<T>::t *V, 
     return sweep + 1;
 }
 
-__global__ void __launch_bounds__(1024) k_svd(int m, int k, const double2 *__restrict__ H, double2 *__restrict__ vs,
+__global__ void __launch_bounds__(1024) k_svd(int m, int k, const double2 *__restrict__ H0, size_t strideH,
+                                              const int *__restrict__ lead, double2 *__restrict__ vs,
                                               double *__restrict__ sigma, double2 *__restrict__ gwork, int use_smem,
                                               int *sweeps_out) {
+    const double2 *__restrict__ H = H0 + (size_t)(*lead) * strideH;
     extern __shared__ __align__(16) unsigned char svd_sm[];
     const int rows = m + 1, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
     unsigned char *base = use_smem ? svd_sm : (unsigned char *)gwork;
@@ -1175,14 +1179,33 @@ size_t scratch_doubles(int qmax, int nsys, int n) {
 }
 
 namespace {
+// Raises a kernel's dynamic shared-memory limit once per (kernel, device) to the most the
+// device allows next to the kernel's static shared memory, so no attribute call happens
+// inside a stream capture (the first, eager cycle of an engine makes every call).
+std::mutex g_smem_mu;
+std::vector<std::pair<const void *, int>> g_smem_done;
 template <class K> void allow_smem(K kernel, size_t bytes) {
-    if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (bytes <= 48 * 1024) return;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const void *key = (const void *)kernel;
+    std::lock_guard<std::mutex> lk(g_smem_mu);
+    for (auto &e : g_smem_done)
+        if (e.first == key && e.second == dev) return;
+    // the opt-in per-block maximum minus the kernel's static shared memory
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa{};
+    cudaFuncGetAttributes(&fa, kernel);
+    const int dyn = optin - (int)fa.sharedSizeBytes;
+    if (dyn > 0 && cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) == cudaSuccess)
+        g_smem_done.emplace_back(key, dev);
 }
 }  // namespace
 
 // ----------------------------------------------------------------- Gram-Schmidt autotuner
 // The projection and update kernels come in (EPT, PU, VEC) variants.  The first launch for a
-// (precision, kernel, n, system-count bucket) times every variant on the caller's own
+// (precision, kernel, n) of at least 8 vectors times every variant on the caller's own
 // buffers (three runs each, CUDA events on the caller's stream), keeps the fastest, and
 // caches the choice for the process, so later launches (and repeat solves) are bitwise
 // reproducible.  Re-running a variant is harmless: both kernels are idempotent on their
@@ -1203,11 +1226,14 @@ struct TuneEntry {
 std::vector<TuneEntry> g_tuned;
 std::mutex g_tune_mu;
 bool g_tune_enabled = true;
+thread_local bool t_capturing = false;   // a stream capture is open on this thread: no timing
 
+// One choice per (precision, kernel, n): the measured winners do not depend on the batch
+// size, and a key without it is settled by the first (always eager) cycle of an engine, so a
+// cycle replayed from a CUDA graph uses exactly the kernels the eager cycle would.
 int bucket_of(int nsys) {
-    int b = 0;
-    while ((1 << b) < nsys) ++b;
-    return b;
+    (void)nsys;
+    return 0;
 }
 
 template <class F>
@@ -1217,7 +1243,7 @@ int tuned_variant(int prec, int kernel, int n, int nsys, int nvar, cudaStream_t 
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)
             if (e.key == key) return e.variant;
-        if (!g_tune_enabled) return 0;
+        if (!g_tune_enabled || t_capturing) return 0;
     }
     cudaEvent_t a, b;
     cudaEventCreate(&a);
@@ -1248,6 +1274,8 @@ int tuned_variant(int prec, int kernel, int n, int nsys, int nvar, cudaStream_t 
 }
 }  // namespace
 
+void set_capturing(bool on) { t_capturing = on; }
+
 void tune_enable(bool on) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_tune_enabled = on;
@@ -1258,8 +1286,8 @@ std::string tune_report() {
     std::string out;
     for (auto &e : g_tuned) {
         char buf[256];
-        int len = snprintf(buf, sizeof buf, "%s %s n=%d nsys<=%d: variant %d [", e.key.prec == 4 ? "c64" : "c128",
-                           e.key.kernel == 0 ? "projection" : "update", e.key.n, 1 << e.key.bucket, e.variant);
+        int len = snprintf(buf, sizeof buf, "%s %s n=%d: variant %d [", e.key.prec == 4 ? "c64" : "c128",
+                           e.key.kernel == 0 ? "projection" : "update", e.key.n, e.variant);
         out.append(buf, len);
         for (int v = 0; v < e.nvar; ++v) {
             len = snprintf(buf, sizeof buf, "%s%.4f", v ? " " : "", e.ms[v]);
@@ -1379,8 +1407,8 @@ void launch_combine(int n, int kk, int m, const typename CT<R>::t *W, const type
 
 template <class R>
 void launch_zupdate(int n, int kk, int m, int k, const typename CT<R>::t *Z, const typename CT<R>::t *V,
-                    const double2 *vs, typename CT<R>::t *Znew, double2 *partials, unsigned *ticket, double *znorm2,
-                    cudaStream_t st) {
+                    size_t strideV, const int *lead, const double2 *vs, typename CT<R>::t *Znew, double2 *partials,
+                    unsigned *ticket, double *znorm2, cudaStream_t st) {
     Launch L_(KC_ZUPDATE, (double)sizeof(typename CT<R>::t) * n * ((double)m + k), st, (k + (sizeof(R) == 4 ? 16 : 8) - 1) / (sizeof(R) == 4 ? 16 : 8));
     using C = typename CT<R>::t;
     constexpr int KB = sizeof(R) == 4 ? 16 : 8;
@@ -1389,7 +1417,8 @@ void launch_zupdate(int n, int kk, int m, int k, const typename CT<R>::t *Z, con
     if (G > chunks) G = chunks;
     for (int t0 = 0; t0 < k; t0 += KB) {
         size_t smem = (size_t)m * KB * sizeof(C);
-        k_zupdate<R, KB><<<G, NT, smem, st>>>(n, kk, m, k, t0, Z, V, vs, Znew, partials, ticket, znorm2);
+        k_zupdate<R, KB><<<G, NT, smem, st>>>(n, kk, m, k, t0, Z, V, strideV, lead, vs, Znew, partials, ticket,
+                                              znorm2);
     }
 }
 
@@ -1414,7 +1443,8 @@ size_t svd_smem_bytes(int m) {
     return (sizeof(double2) + sizeof(float2)) * ((size_t)(m + 1) * m + (size_t)m * m);
 }
 
-void launch_svd_smallest(int m, int k, const double2 *H, double2 *vs, double *sigma, double2 *work, int *sweeps,
+void launch_svd_smallest(int m, int k, const double2 *H, size_t strideH, const int *lead, double2 *vs, double *sigma,
+                         double2 *work, int *sweeps,
                          cudaStream_t st) {
     Launch L_(KC_SVD, (double)sizeof(double2) * (m + 1.0) * m, st, 1);
     size_t smem = svd_smem_bytes(m);
@@ -1422,7 +1452,7 @@ void launch_svd_smallest(int m, int k, const double2 *H, double2 *vs, double *si
     if (use_smem) allow_smem(k_svd, smem);
     const int pairs = (m + 1) / 2;
     int threads = 32 * (pairs < 32 ? (pairs > 4 ? pairs : 4) : 32);
-    k_svd<<<1, threads, use_smem ? smem : 0, st>>>(m, k, H, vs, sigma, work, use_smem, sweeps);
+    k_svd<<<1, threads, use_smem ? smem : 0, st>>>(m, k, H, strideH, lead, vs, sigma, work, use_smem, sweeps);
 }
 
 template <class R>
@@ -1504,8 +1534,8 @@ void launch_broadcast_hdef(int m, int kk, const double2 *Hd, double2 *H, size_t 
     template void launch_combine<R>(int, int, int, const CT<R>::t *, const CT<R>::t *, const CT<R>::t *, size_t,       \
                                     CT<R>::t *, size_t, CT<R>::t *, size_t, const double2 *, const double2 *, size_t, \
                                     const int *, int, double2 *, unsigned *, SysState *, cudaStream_t);                \
-    template void launch_zupdate<R>(int, int, int, int, const CT<R>::t *, const CT<R>::t *, const double2 *,          \
-                                    CT<R>::t *, double2 *, unsigned *, double *, cudaStream_t);                        \
+    template void launch_zupdate<R>(int, int, int, int, const CT<R>::t *, const CT<R>::t *, size_t, const int *,       \
+                                    const double2 *, CT<R>::t *, double2 *, unsigned *, double *, cudaStream_t);       \
     template void launch_znormalise<R>(int, int, const CT<R>::t *, const double *, CT<R>::t *, cudaStream_t);          \
     template void launch_spmm<R>(const SellMatrix &, const CT<R>::t *, size_t, CT<R>::t *, size_t, const int *, int,  \
                                  cudaStream_t);                                                                        \

@@ -90,6 +90,8 @@ void profile_read(int kc, double *bytes, double *ms, long long *launches);
 void profile_reset();
 // Gram-Schmidt variant autotuning (on by default) and its report, one line per tuned shape.
 void tune_enable(bool on);
+// Marks the calling thread as capturing a CUDA graph: launchers then use cached choices only.
+void set_capturing(bool on);
 std::string tune_report();
 
 // ----------------------------------------------------------------- launchers
@@ -127,10 +129,11 @@ void launch_combine(int n, int kk, int m, const typename CT<R>::t *W, const type
                     const int *act, int nsys, double2 *partials, unsigned *tickets, SysState *state, cudaStream_t st);
 
 // Z_new[t] = [Z V] vs[:, t] for t < k, plus squared norms into znorm2 (k doubles).
+// V: basis of system 0 (system s at V + s*strideV); the lead system is read from device memory.
 template <class R>
 void launch_zupdate(int n, int kk, int m, int k, const typename CT<R>::t *Z, const typename CT<R>::t *V,
-                    const double2 *vs, typename CT<R>::t *Znew, double2 *partials, unsigned *ticket, double *znorm2,
-                    cudaStream_t st);
+                    size_t strideV, const int *lead, const double2 *vs, typename CT<R>::t *Znew, double2 *partials,
+                    unsigned *ticket, double *znorm2, cudaStream_t st);
 // Z[t] = Znew[t] / sqrt(znorm2[t]).
 template <class R>
 void launch_znormalise(int n, int k, const typename CT<R>::t *Znew, const double *znorm2, typename CT<R>::t *Z,
@@ -141,8 +144,9 @@ void launch_ls(int m, const double2 *H, size_t strideH, const double2 *g, double
                const int *act, int nsys, cudaStream_t st);
 // Right singular vectors of the k smallest singular values of H ((m+1) x m), FP64 one-sided Jacobi.
 // vs: m x k column-major; sigma: m values (descending); work: global scratch of 3*m*(m+1) double2.
-void launch_svd_smallest(int m, int k, const double2 *H, double2 *vs, double *sigma, double2 *work, int *sweeps,
-                         cudaStream_t st);
+// H: Hessenberg of system 0 (system s at H + s*strideH); the lead system is read from device memory.
+void launch_svd_smallest(int m, int k, const double2 *H, size_t strideH, const int *lead, double2 *vs, double *sigma,
+                         double2 *work, int *sweeps, cudaStream_t st);
 
 // SELL-32 sparse matrix times a batch of vectors: y_s = A x_s over the active systems.
 struct SellMatrix {

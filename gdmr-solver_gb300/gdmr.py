@@ -61,6 +61,7 @@ SIGNATURES = {
     "gdmr_system_destroy": (I, [P]),
     "gdmr_system_bytes": (LL, [P]),
     "gdmr_system_svd_sweeps": (I, [P]),
+    "gdmr_system_set_graphs": (I, [P, I]),
     "gdmr_solve": (I, [P, I, P, P, D, I, I, P]),
     "gdmr_solve_batch": (I, [P, I, P, P, P, I, I, P]),
     "gdmr_true_residual": (I, [P, I, P, P, I, P]),
@@ -68,6 +69,10 @@ SIGNATURES = {
     "gdmr_export_deflation": (I, [P, P]),
     "gdmr_import_deflation": (I, [P, P]),
     "gdmr_drop_deflation": (I, [P]),
+    "gdmr_deflation_write": (I, [ctypes.c_char_p, I, I, P]),
+    "gdmr_deflation_read": (I, [ctypes.c_char_p, I, I, P]),
+    "gdmr_save_deflation": (I, [P, ctypes.c_char_p]),
+    "gdmr_load_deflation": (I, [P, ctypes.c_char_p]),
     "gdmr_server_create": (I, [P, LL, I]),
     "gdmr_server_add_operator": (I, [P, I, P, P, P, I, I, I, I, P]),
     "gdmr_server_slot_bytes": (LL, [I, I, I]),
@@ -153,6 +158,18 @@ def load(path: str = LIB_PATH):
         fn.argtypes = args
     _lib = L
     return L
+
+
+def write_deflation(path: str, Z) -> None:
+    """Host-only: write a k x n complex128 deflation space in the versioned on-disk format."""
+    Z = np.ascontiguousarray(Z, dtype=np.complex128)
+    _check(load().gdmr_deflation_write(os.fsencode(path), Z.shape[1], Z.shape[0], _ptr(Z)), "gdmr_deflation_write")
+
+
+def read_deflation(path: str, k: int, n: int) -> np.ndarray:
+    Z = np.zeros((k, n), np.complex128)
+    _check(load().gdmr_deflation_read(os.fsencode(path), n, k, _ptr(Z)), "gdmr_deflation_read")
+    return Z
 
 
 def last_error() -> str:
@@ -287,6 +304,9 @@ class System:
         except Exception:
             pass
 
+    def set_graphs(self, on: bool) -> None:
+        _check(self.L.gdmr_system_set_graphs(self._h, 1 if on else 0), "gdmr_system_set_graphs")
+
     def svd_sweeps(self) -> dict:
         v = int(self.L.gdmr_system_svd_sweeps(self._h))
         return {"fp32": v // 1000, "fp64": v % 1000}
@@ -349,6 +369,12 @@ class System:
     def import_deflation(self, Z):
         Z = np.ascontiguousarray(Z, dtype=np.complex128)
         _check(self.L.gdmr_import_deflation(self._h, _ptr(Z)), "gdmr_import_deflation")
+
+    def save_deflation(self, path: str) -> None:
+        _check(self.L.gdmr_save_deflation(self._h, os.fsencode(path)), "gdmr_save_deflation")
+
+    def load_deflation(self, path: str) -> None:
+        _check(self.L.gdmr_load_deflation(self._h, os.fsencode(path)), "gdmr_load_deflation")
 
     def drop_deflation(self):
         _check(self.L.gdmr_drop_deflation(self._h), "gdmr_drop_deflation")

@@ -107,6 +107,9 @@ int gdmr_system_destroy(gdmr_system *sys);
 long long gdmr_system_bytes(const gdmr_system *sys);
 /* Jacobi sweeps of the last deflation-space SVD: 1000 * (FP32 sweeps) + (FP64 sweeps). */
 int gdmr_system_svd_sweeps(const gdmr_system *sys);
+/* Restart cycles of small systems (n x batch <= 2^20) replay as CUDA graphs after the first
+ * cycle (on by default); 0 launches every kernel eagerly. */
+int gdmr_system_set_graphs(gdmr_system *sys, int on);
 
 /* Reference-semantics solve of one right-hand side (solverDMR's algorithm,
  * complex128 or complex64 per the system's precision), then the true FP64
@@ -144,6 +147,15 @@ int gdmr_true_residual_noalloc(gdmr_system *sys, int nrhs, const double *b, cons
 int gdmr_export_deflation(gdmr_system *sys, double *z);
 int gdmr_import_deflation(gdmr_system *sys, const double *z);
 int gdmr_drop_deflation(gdmr_system *sys);
+
+/* Deflation spaces on disk, versioned (magic "GDMRDEFL", format 1, k, n, FNV-1a hash, then
+ * k x n complex128 little endian): the reference's impSVDMR/expSVDMR only move them between
+ * host and device.  write/read are host-only; read checks magic, version, sizes and hash.
+ * save/load go through a system (export + write, read + import). */
+int gdmr_deflation_write(const char *path, int n, int k, const double *z);
+int gdmr_deflation_read(const char *path, int n, int k, double *z);
+int gdmr_save_deflation(gdmr_system *sys, const char *path);
+int gdmr_load_deflation(gdmr_system *sys, const char *path);
 
 /* ---- serving: resident operators, HBM-budget admission, continuous batching ----
  * A server holds several resident operators.  Each has its matrix, its recycled

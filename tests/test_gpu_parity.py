@@ -249,3 +249,39 @@ def test_cycle_cap_reports_no_convergence(c1):
     x, st = s.solve(rhs[0], mode=0, tol=1e-10, mat_rank=3)
     assert st["status"] == 3 and st["cycles"] == 4
     assert "converge" in gdmr.last_error()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_graph_replay_matches_eager_launches(c1, precision):
+    """Restart cycles replayed as CUDA graphs give the same iterates as eager launches."""
+    A, rhs, cfg, direct = c1
+    res = []
+    for graphs in (False, True):
+        s = gdmr.System(A, cfg["m"], cfg["k"], capacity=2, precision=precision)
+        s.set_graphs(graphs)
+        if precision == "fp64":
+            x0, st0 = s.solve(rhs[0], mode=0, tol=1e-10, mat_rank=2000)
+            x1, st1 = s.solve(rhs[1], mode=1, tol=1e-10, mat_rank=2000)
+            res.append((np.stack([x0, x1]), [st0["cycles"], st1["cycles"]]))
+        else:
+            X, st = s.solve_batch(np.array(rhs[:2]), tol=1e-10, max_cycles=2000)
+            res.append((X, [t["cycles"] for t in st]))
+    (xe, ce), (xg, cg) = res
+    assert ce == cg
+    assert np.array_equal(xe, xg)
+
+
+def test_deflation_space_survives_the_process_through_a_file(c1, tmp_path):
+    """save -> load through the versioned file gives the same next solve as keeping the
+    space resident (the reference can only move Z between host and device)."""
+    A, rhs, cfg, direct = c1
+    s1 = gdmr.System(A, cfg["m"], cfg["k"], capacity=1, precision="fp64")
+    s1.solve(rhs[0], mode=0, tol=1e-10, mat_rank=2000)
+    path = str(tmp_path / "z.gdmr")
+    s1.save_deflation(path)
+    s2 = gdmr.System(A, cfg["m"], cfg["k"], capacity=1, precision="fp64")
+    s2.load_deflation(path)
+    x1, st1 = s1.solve(rhs[1], mode=1, tol=1e-10, mat_rank=2000)
+    x2, st2 = s2.solve(rhs[1], mode=1, tol=1e-10, mat_rank=2000)
+    assert st1["cycles"] == st2["cycles"]
+    assert _rel(x1, x2) < 1e-12
