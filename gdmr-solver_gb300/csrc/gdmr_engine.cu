@@ -197,6 +197,7 @@ template <class R> void Engine<R>::release() {
     if (ev_zdone_) cudaEventDestroy(ev_zdone_);
     ev_krylov_ = ev_zdone_ = nullptr;
     z_pending_ = false;
+    if (partials_) unregister_scratch(partials_);
     partials_side_ = nullptr;
     ticket_side_ = nullptr;
     for (void *p : allocs_) cudaFree(p);
@@ -255,6 +256,7 @@ template <class R> int Engine<R>::init(int n, int m, int k, int capacity, int de
     A_(znorm2_, sizeof(double) * std::max(k, 1));
     A_(sweeps_, sizeof(int));
     A_(partials_, sizeof(double) * scratch_doubles(qmax() + 16, capacity + 1, n));
+    register_scratch(partials_, scratch_doubles(qmax() + 16, capacity + 1, n));
     A_(tickets_, sizeof(unsigned) * (capacity + 1));
     A_(state_, sizeof(SysState) * (capacity + 1));
     A_(act_, sizeof(int) * (capacity + 1));
@@ -347,8 +349,9 @@ template <class R> int Engine<R>::run_cycle(int kk, int nsys, int lead, double t
     lead_host_ = lead;
     GDMR_CK(cudaMemcpyAsync(lead_dev_, &lead_host_, sizeof(int), cudaMemcpyHostToDevice, stream));
     // CUDA graphs pay off where launch overhead is comparable to the work: small n x batch.
-    // The first cycle of an engine always runs eagerly (it also tunes the kernels).
-    const bool graphable = use_graphs && op.kind != Operator<R>::HOOK && !profile_enabled() && cycles_run_ > 0 &&
+    // The first two cycles of an engine run eagerly: they tune the kernels of both cycle
+    // shapes (without and with the deflation space) before anything is captured.
+    const bool graphable = use_graphs && op.kind != Operator<R>::HOOK && !profile_enabled() && cycles_run_ > 1 &&
                            (long)n_ * nsys <= (1L << 20);
     ++cycles_run_;
     if (!graphable) return enqueue_cycle(kk, nsys, tol, matvecs, false);

@@ -349,6 +349,251 @@ __global__ void __launch_bounds__(NT, min_blocks<typename CT<R>::t>(EPT, PU))
     }
 }
 
+// ----------------------------------------------------------------- system-grouped variants
+// One CTA serves SB systems of one chunk: every tile of the shared vectors (segment A, the
+// deflation basis W) is loaded once and used for all SB systems, instead of once per system
+// (from L2), which matters when a batch of systems shares W.  Per-system results, the
+// partial layout and the last-CTA finishing are those of k_mdot / k_update.
+template <class R, int EPT, int SB>
+__global__ void __launch_bounds__(NT, 2)
+    k_mdot_grp(int n, const typename CT<R>::t *__restrict__ segA, int qa, const typename CT<R>::t *__restrict__ segB0,
+               size_t strideB, int qb, const typename CT<R>::t *__restrict__ w0, size_t strideW,
+               const int *__restrict__ act, int nsys, double2 *__restrict__ partials, int qmax, unsigned *tickets,
+               double2 *__restrict__ coef0, size_t strideC) {
+    using C = typename CT<R>::t;
+    extern __shared__ unsigned char grp_sm[];
+    C *wsum = reinterpret_cast<C *>(grp_sm);           // [NW][SB][qmax]
+    const int slot0 = blockIdx.x * SB, ns = min(SB, nsys - slot0), chunk = blockIdx.y, G = gridDim.y;
+    const int q = qa + qb, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long c0 = (long)chunk * NT * EPT;
+    int sys[SB];
+    C wv[SB][EPT];
+#pragma unroll
+    for (int g = 0; g < SB; ++g) {
+        sys[g] = act[slot0 + (g < ns ? g : 0)];
+        const C *w = w0 + (size_t)sys[g] * strideW;
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            const long i = c0 + tid + (long)e * NT;
+            wv[g][e] = (g < ns && i < n) ? w[i] : czero<C>();
+        }
+    }
+    // shared segment: one load per tile, SB dot products
+    for (int p = 0; p < qa; ++p) {
+        C a[EPT];
+        const C *vp = segA + (size_t)p * n;
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            const long i = c0 + tid + (long)e * NT;
+            a[e] = i < n ? vp[i] : czero<C>();
+        }
+#pragma unroll
+        for (int g = 0; g < SB; ++g) {
+            C d = czero<C>();
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) cdotacc(d, a[e], wv[g][e]);
+            d.x = warp_sum(d.x);
+            d.y = warp_sum(d.y);
+            if (lane == 0) wsum[((size_t)warp * SB + g) * qmax + p] = d;
+        }
+    }
+    // per-system segments
+#pragma unroll
+    for (int g = 0; g < SB; ++g) {
+        if (g >= ns) break;
+        const C *segB = segB0 + (size_t)sys[g] * strideB;
+        for (int p = 0; p < qb; p += 2) {
+            C a0[EPT], a1[EPT];
+            const C *v0 = segB + (size_t)p * n;
+            const C *v1 = segB + (size_t)(p + 1 < qb ? p + 1 : p) * n;
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) {
+                const long i = c0 + tid + (long)e * NT;
+                a0[e] = i < n ? v0[i] : czero<C>();
+                a1[e] = i < n ? v1[i] : czero<C>();
+            }
+            C d0 = czero<C>(), d1 = czero<C>();
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) {
+                cdotacc(d0, a0[e], wv[g][e]);
+                cdotacc(d1, a1[e], wv[g][e]);
+            }
+            d0.x = warp_sum(d0.x);
+            d0.y = warp_sum(d0.y);
+            d1.x = warp_sum(d1.x);
+            d1.y = warp_sum(d1.y);
+            if (lane == 0) {
+                wsum[((size_t)warp * SB + g) * qmax + qa + p] = d0;
+                if (p + 1 < qb) wsum[((size_t)warp * SB + g) * qmax + qa + p + 1] = d1;
+            }
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < ns * q; e += NT) {
+        const int g = e / q, p = e % q;
+        double re = 0, im = 0;
+#pragma unroll
+        for (int ww = 0; ww < NW; ++ww) {
+            const C v = wsum[((size_t)ww * SB + g) * qmax + p];
+            re += (double)v.x;
+            im += (double)v.y;
+        }
+        double *pp = (double *)partials + ((size_t)(slot0 + g) * qmax + p) * 2 * G;
+        pp[chunk] = re;
+        pp[G + chunk] = im;
+    }
+    __shared__ unsigned lastmask;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+        unsigned mk = 0;
+        for (int g = 0; g < ns; ++g)
+            if (atomicAdd(&tickets[slot0 + g], 1u) == (unsigned)G - 1) mk |= 1u << g;
+        lastmask = mk;
+    }
+    __syncthreads();
+    if (!lastmask) return;
+    __threadfence();
+    for (int g = 0; g < ns; ++g) {
+        if (!(lastmask >> g & 1u)) continue;
+        double2 *coef = coef0 + (size_t)sys[g] * strideC;
+        const double *part = (const double *)partials + (size_t)(slot0 + g) * qmax * 2 * G;
+        for (int p = warp; p < q; p += NW) {
+            const double *pp = part + (size_t)p * 2 * G;
+            double re = 0, im = 0;
+            for (int gg = lane; gg < G; gg += 32) { re += __ldcg(pp + gg); im += __ldcg(pp + G + gg); }
+            re = warp_sum(re);
+            im = warp_sum(im);
+            if (lane == 0) coef[p] = make_double2(re, im);
+        }
+        if (tid == 0) tickets[slot0 + g] = 0;
+    }
+}
+
+template <class R, int EPT, int SB>
+__global__ void __launch_bounds__(NT, 2)
+    k_update_grp(int n, const typename CT<R>::t *__restrict__ segA, int qa, const typename CT<R>::t *__restrict__ segB0,
+                 size_t strideB, int qb, const typename CT<R>::t *__restrict__ w0, size_t strideW,
+                 typename CT<R>::t *__restrict__ out0, size_t strideO, const int *__restrict__ act, int nsys,
+                 const double2 *__restrict__ coef0, size_t strideC, double2 *__restrict__ partials,
+                 unsigned *tickets, SysState *state, FinishArgs fin, int skip_broken) {
+    using C = typename CT<R>::t;
+    extern __shared__ unsigned char grp_sm[];
+    C *cs = reinterpret_cast<C *>(grp_sm);              // [SB][qmax] coefficients
+    __shared__ double red[3][NW];
+    const int slot0 = blockIdx.x * SB, ns = min(SB, nsys - slot0), chunk = blockIdx.y, G = gridDim.y;
+    const int q = qa + qb, tid = threadIdx.x;
+    const int qmax = (int)strideC;
+    int sys[SB];
+    bool live[SB];
+#pragma unroll
+    for (int g = 0; g < SB; ++g) {
+        sys[g] = act[slot0 + (g < ns ? g : 0)];
+        live[g] = g < ns && !(skip_broken && state[sys[g]].broken);
+    }
+    for (int e = tid; e < ns * q; e += NT) {
+        const int g = e / q, p = e % q;
+        cs[(size_t)g * qmax + p] = from_d<C>(coef0[(size_t)sys[g] * strideC + p]);
+    }
+    __syncthreads();
+    const long c0 = (long)chunk * NT * EPT;
+    C acc[SB][EPT], org[SB][EPT];
+#pragma unroll
+    for (int g = 0; g < SB; ++g) {
+        const C *w = w0 + (size_t)sys[g] * strideW;
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            const long i = c0 + tid + (long)e * NT;
+            org[g][e] = (live[g] && i < n) ? w[i] : czero<C>();
+            acc[g][e] = org[g][e];
+        }
+    }
+    for (int p = 0; p < qa; ++p) {
+        C a[EPT];
+        const C *vp = segA + (size_t)p * n;
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            const long i = c0 + tid + (long)e * NT;
+            a[e] = i < n ? vp[i] : czero<C>();
+        }
+#pragma unroll
+        for (int g = 0; g < SB; ++g) {
+            const C c = g < ns ? cs[(size_t)g * qmax + p] : czero<C>();
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) cfms(acc[g][e], c, a[e]);
+        }
+    }
+#pragma unroll
+    for (int g = 0; g < SB; ++g) {
+        if (!live[g]) continue;
+        const C *segB = segB0 + (size_t)sys[g] * strideB;
+        for (int p = 0; p < qb; p += 2) {
+            C a0[EPT], a1[EPT];
+            const C *v0 = segB + (size_t)p * n;
+            const C *v1 = segB + (size_t)(p + 1 < qb ? p + 1 : p) * n;
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) {
+                const long i = c0 + tid + (long)e * NT;
+                a0[e] = i < n ? v0[i] : czero<C>();
+                a1[e] = i < n ? v1[i] : czero<C>();
+            }
+            const C c0v = cs[(size_t)g * qmax + qa + p];
+            const C c1v = p + 1 < qb ? cs[(size_t)g * qmax + qa + p + 1] : czero<C>();
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) {
+                cfms(acc[g][e], c0v, a0[e]);
+                cfms(acc[g][e], c1v, a1[e]);
+            }
+        }
+    }
+    // per-system outputs and norms
+#pragma unroll
+    for (int g = 0; g < SB; ++g) {
+        C ln = czero<C>(), lc = czero<C>();
+        if (live[g]) {
+            C *out = out0 + (size_t)sys[g] * strideO;
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) {
+                const long i = c0 + tid + (long)e * NT;
+                if (i < n) out[i] = acc[g][e];
+                cdotacc(ln, acc[g][e], acc[g][e]);
+                cdotacc(lc, acc[g][e], org[g][e]);
+            }
+        }
+        double v[3] = {(double)ln.x, (double)lc.x, (double)lc.y};
+        block_sum<3>(v, red);
+        if (tid == 0 && g < ns) {
+            double *part = (double *)partials + (size_t)(slot0 + g) * 3 * G;
+            part[chunk] = v[0];
+            part[G + chunk] = v[1];
+            part[2 * G + chunk] = v[2];
+        }
+        __syncthreads();
+    }
+    __shared__ unsigned lastmask;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+        unsigned mk = 0;
+        for (int g = 0; g < ns; ++g)
+            if (atomicAdd(&tickets[slot0 + g], 1u) == (unsigned)G - 1) mk |= 1u << g;
+        lastmask = mk;
+    }
+    __syncthreads();
+    if (!lastmask) return;
+    __threadfence();
+    for (int g = 0; g < ns; ++g) {
+        if (!(lastmask >> g & 1u)) continue;
+        double tot[3];
+        sum_partials<3>((double *)partials + (size_t)(slot0 + g) * 3 * G, G, tot, red);
+        if (tid == 0) {
+            if (live[g]) run_finish(fin, sys[g], state[sys[g]], tot[0], tot[1], tot[2]);
+            tickets[slot0 + g] = 0;
+        }
+        __syncthreads();
+    }
+}
+
 // ----------------------------------------------------------------- scale
 template <class R>
 __global__ void __launch_bounds__(NT) k_scale(int n, const typename CT<R>::t *__restrict__ in0, size_t strideI,
@@ -639,9 +884,16 @@ __device__ __forceinline__ void circle_pair(int r, int pi, int mm, int &p, int &
     q = pos(mm - 1 - pi);
 }
 
-template <class T>
+// Sweeps of one-sided Jacobi on A ((m+1) x m) accumulating V (m x m).  `only` (optional, m
+// flags) restricts the rotations to pairs with at least one flagged column: the columns of
+// the k smallest singular values, the only ones the deflation update uses.  Rotating a
+// flagged column against every other one makes it orthogonal to all columns of A, which
+// decouples the flagged block exactly; rotations among unflagged columns cannot change it.
+// SPLIT: compute each round's rotation parameters one pair per lane of one warp (FP64, where
+// scalar arithmetic is expensive) instead of in every lane of each pair's warp (FP32).
+template <class T, bool SPLIT>
 __device__ int jacobi_sweeps(int m, typename CX<T>::t *A, typename CX<T>::t *V, T *nrm, double2 *rot, T tol,
-                             int max_sweeps, int *s_flag, float *s_off) {
+                             int max_sweeps, int *s_flag, float *s_off, const unsigned char *only) {
     using C = typename CX<T>::t;
     const int rows = m + 1, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
     const int mm = m + (m & 1), npairs = mm / 2;
@@ -656,11 +908,13 @@ __device__ int jacobi_sweeps(int m, typename CX<T>::t *A, typename CX<T>::t *V, 
         if (tid == 0) { *s_flag = 0; *s_off = 0.f; }
         __syncthreads();
         for (int round = 0; round < mm - 1; ++round) {
-            // (1) gamma of every pair, one warp per pair
+            // (1) gamma of every pair, one warp per pair; in the fused form also (2) and (3)
             for (int pi = warp; pi < npairs; pi += nwarps) {
                 int p, q;
                 circle_pair(round, pi, mm, p, q);
-                if (p >= m || q >= m) { if (lane == 0) rot[pi] = make_double2(0, 0); continue; }
+                const bool skip = p >= m || q >= m || (only && !only[p] && !only[q]);
+                if (skip) { if (SPLIT && lane == 0) rot[pi] = make_double2(0, 0); continue; }
+                if (p > q) { int t = p; p = q; q = t; }
                 T gr = 0, gi = 0;
                 for (int r = lane; r < rows; r += 32) {
                     C ap = A[(size_t)p * rows + r], aq = A[(size_t)q * rows + r];
@@ -669,47 +923,23 @@ __device__ int jacobi_sweeps(int m, typename CX<T>::t *A, typename CX<T>::t *V, 
                 }
                 gr = warp_sum(gr);
                 gi = warp_sum(gi);
-                if (lane == 0) rot[pi] = make_double2((double)gr, (double)gi);
-            }
-            __syncthreads();
-            // (2) rotation parameters, one pair per lane: (c, t), phase e^{-i phi}, |gamma|
-            for (int pi = tid; pi < npairs; pi += blockDim.x) {
-                int p, q;
-                circle_pair(round, pi, mm, p, q);
-                const double2 gd = rot[pi];
-                T gx = (T)gd.x, gy = (T)gd.y;
-                T cc = 1, tt = 0, phr = 1, phi = 0, ag = 0;
-                if (p < m && q < m) {
-                    const T a = nrm[p < q ? p : q], b = nrm[p < q ? q : p];
-                    if (p > q) gy = -gy;                    // gamma for the ordered pair (min, max)
-                    ag = sqrt(gx * gx + gy * gy);
-                    const T rel = ag / sqrt(a * b);
-                    if (ag > (T)0 && rel > tol) {
-                        *s_flag = 1;
-                        atomicMax((int *)s_off, __float_as_int((float)rel));   // non-negative floats order as ints
-                        phr = gx / ag;
-                        phi = -gy / ag;
-                        const T zeta = (b - a) / ((T)2 * ag);
-                        tt = ((zeta >= (T)0) ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
-                        cc = (T)1 / sqrt((T)1 + tt * tt);
-                    }
+                if (SPLIT) {
+                    if (lane == 0) rot[pi] = make_double2((double)gr, (double)gi);
+                    continue;
                 }
-                rot[pi] = make_double2((double)cc, (double)tt);
-                rot[npairs + pi] = make_double2((double)phr, (double)phi);
-                rot[2 * npairs + pi] = make_double2((double)ag, 0.0);
-            }
-            __syncthreads();
-            // (3) apply: one warp per pair, columns (min, max) of A and V; norms updated
-            //     incrementally (||a_p'||^2 = a - t|gamma|, ||a_q'||^2 = b + t|gamma|)
-            for (int pi = warp; pi < npairs; pi += nwarps) {
-                int p, q;
-                circle_pair(round, pi, mm, p, q);
-                if (p >= m || q >= m) continue;
-                if (p > q) { int t = p; p = q; q = t; }
-                const double2 ct = rot[pi];
-                if (ct.y == 0.0) continue;
-                const double2 ph = rot[npairs + pi];
-                const T c = (T)ct.x, sn = (T)(ct.x * ct.y), pr = (T)ph.x, pim = (T)ph.y;
+                // fused: every lane computes the (cheap) FP32 parameters and applies them
+                const T a = nrm[p], b = nrm[q];
+                const T ag = sqrt(gr * gr + gi * gi);
+                const T rel = ag / sqrt(a * b);
+                if (!(ag > (T)0 && rel > tol)) continue;
+                if (lane == 0) {
+                    *s_flag = 1;
+                    atomicMax((int *)s_off, __float_as_int((float)rel));
+                }
+                const T pr = gr / ag, pim = -gi / ag;
+                const T zeta = (b - a) / ((T)2 * ag);
+                const T tt = ((zeta >= (T)0) ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
+                const T c = (T)1 / sqrt((T)1 + tt * tt), sn = c * tt;
                 for (int r = lane; r < rows; r += 32) {
                     C ap = A[(size_t)p * rows + r], aq0 = A[(size_t)q * rows + r];
                     C aq;
@@ -733,9 +963,75 @@ __device__ int jacobi_sweeps(int m, typename CX<T>::t *A, typename CX<T>::t *V, 
                     V[(size_t)q * m + r] = nq_;
                 }
                 if (lane == 0) {
-                    const T tg = (T)(ct.y * rot[2 * npairs + pi].x);
-                    nrm[p] = nrm[p] - tg;
-                    nrm[q] = nrm[q] + tg;
+                    nrm[p] = a - tt * ag;
+                    nrm[q] = b + tt * ag;
+                }
+            }
+            if (SPLIT) {
+                __syncthreads();
+                // (2) rotation parameters, one pair per lane: (c, t), phase e^{-i phi}, |gamma|
+                for (int pi = tid; pi < npairs; pi += blockDim.x) {
+                    int p, q;
+                    circle_pair(round, pi, mm, p, q);
+                    const double2 gd = rot[pi];
+                    T gx = (T)gd.x, gy = (T)gd.y;
+                    T cc = 1, tt = 0, phr = 1, phi = 0, ag = 0;
+                    if (p < m && q < m && !(only && !only[p] && !only[q])) {
+                        const T a = nrm[p < q ? p : q], b = nrm[p < q ? q : p];
+                        ag = sqrt(gx * gx + gy * gy);
+                        const T rel = ag / sqrt(a * b);
+                        if (ag > (T)0 && rel > tol) {
+                            *s_flag = 1;
+                            atomicMax((int *)s_off, __float_as_int((float)rel));
+                            phr = gx / ag;
+                            phi = -gy / ag;
+                            const T zeta = (b - a) / ((T)2 * ag);
+                            tt = ((zeta >= (T)0) ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
+                            cc = (T)1 / sqrt((T)1 + tt * tt);
+                        }
+                    }
+                    rot[pi] = make_double2((double)cc, (double)tt);
+                    rot[npairs + pi] = make_double2((double)phr, (double)phi);
+                    rot[2 * npairs + pi] = make_double2((double)ag, 0.0);
+                }
+                __syncthreads();
+                // (3) apply: one warp per pair, columns (min, max); incremental norms
+                for (int pi = warp; pi < npairs; pi += nwarps) {
+                    int p, q;
+                    circle_pair(round, pi, mm, p, q);
+                    if (p >= m || q >= m) continue;
+                    if (p > q) { int t = p; p = q; q = t; }
+                    const double2 ct = rot[pi];
+                    if (ct.y == 0.0) continue;
+                    const double2 ph = rot[npairs + pi];
+                    const T c = (T)ct.x, sn = (T)(ct.x * ct.y), pr = (T)ph.x, pim = (T)ph.y;
+                    for (int r = lane; r < rows; r += 32) {
+                        C ap = A[(size_t)p * rows + r], aq0 = A[(size_t)q * rows + r];
+                        C aq;
+                        aq.x = aq0.x * pr - aq0.y * pim;
+                        aq.y = aq0.x * pim + aq0.y * pr;
+                        C np_, nq_;
+                        np_.x = c * ap.x - sn * aq.x; np_.y = c * ap.y - sn * aq.y;
+                        nq_.x = sn * ap.x + c * aq.x; nq_.y = sn * ap.y + c * aq.y;
+                        A[(size_t)p * rows + r] = np_;
+                        A[(size_t)q * rows + r] = nq_;
+                    }
+                    for (int r = lane; r < m; r += 32) {
+                        C vp = V[(size_t)p * m + r], vq0 = V[(size_t)q * m + r];
+                        C vq;
+                        vq.x = vq0.x * pr - vq0.y * pim;
+                        vq.y = vq0.x * pim + vq0.y * pr;
+                        C np_, nq_;
+                        np_.x = c * vp.x - sn * vq.x; np_.y = c * vp.y - sn * vq.y;
+                        nq_.x = sn * vp.x + c * vq.x; nq_.y = sn * vp.y + c * vq.y;
+                        V[(size_t)p * m + r] = np_;
+                        V[(size_t)q * m + r] = nq_;
+                    }
+                    if (lane == 0) {
+                        const T tg = (T)(ct.y * rot[2 * npairs + pi].x);
+                        nrm[p] = nrm[p] - tg;
+                        nrm[q] = nrm[q] + tg;
+                    }
                 }
             }
             __syncthreads();
@@ -770,7 +1066,19 @@ __global__ void __launch_bounds__(1024) k_svd(int m, int k, const double2 *__res
     for (int i = tid; i < rows * m; i += blockDim.x) A32[i] = make_float2((float)H[i].x, (float)H[i].y);
     for (int i = tid; i < m * m; i += blockDim.x) V32[i] = make_float2((i % m) == (i / m) ? 1.f : 0.f, 0.f);
     __syncthreads();
-    const int s32 = jacobi_sweeps<float>(m, A32, V32, nrm32, rot, 4.0f * 1.1920929e-7f * m, 40, &s_flag, &s_off);
+    const int s32 = jacobi_sweeps<float, false>(m, A32, V32, nrm32, rot, 4.0f * 1.1920929e-7f * m, 40, &s_flag, &s_off,
+                                                nullptr);
+    // the k columns of smallest norm (smallest singular values) after the FP32 phase
+    __shared__ unsigned char small_col[168];
+    for (int c = tid; c < m; c += blockDim.x) {
+        const float sc = nrm32[c];
+        int below = 0;
+        for (int c2 = 0; c2 < m; ++c2) {
+            const float s2 = nrm32[c2];
+            below += (s2 < sc) || (s2 == sc && c2 < c);
+        }
+        small_col[c] = below < k ? 1 : 0;
+    }
     // V64 = V32 re-orthonormalised in FP64 by Cholesky QR: S = V^H V = L L^H, V <- V L^{-H}.
     // V32 is orthonormal to FP32 accuracy, so S is within ~1e-6 of I and the factorisation
     // is well conditioned.  S lives in the FP32 scratch region, free after phase 1.
@@ -839,7 +1147,8 @@ __global__ void __launch_bounds__(1024) k_svd(int m, int k, const double2 *__res
         A64[i] = acc;
     }
     __syncthreads();
-    const int s64 = jacobi_sweeps<double>(m, A64, V64, nrm64, rot, 4.0 * 2.220446049250313e-16 * m, 20, &s_flag, &s_off);
+    const int s64 = jacobi_sweeps<double, true>(m, A64, V64, nrm64, rot, 4.0 * 2.220446049250313e-16 * m, 3, &s_flag,
+                                                &s_off, small_col);
     for (int c = warp; c < m; c += nwarps) {
         double a = 0;
         for (int r = lane; r < rows; r += 32) { double2 v = A64[(size_t)c * rows + r]; a += v.x * v.x + v.y * v.y; }
@@ -1173,7 +1482,10 @@ double spmm_bytes(const SellMatrix &A, size_t vs, int nsys) {
 }
 }  // namespace
 size_t scratch_doubles(int qmax, int nsys, int n) {
-    const size_t per_chunk = (size_t)(2 * qmax + 4) * nsys * nchunks<double>(n);   // projection partials dominate
+    // projection partials dominate: qmax coefficients x (re, im) per chunk and system, for the
+    // smallest chunk any kernel variant uses (NT elements, one per thread)
+    const size_t min_chunks = ((size_t)n + NT - 1) / NT;
+    const size_t per_chunk = (size_t)(2 * qmax + 4) * nsys * (min_chunks > 0 ? min_chunks : 1);
     const size_t grid_stride = (size_t)32 * (num_sms() * 8 + nsys);                // norms, residuals, Z update
     return per_chunk + grid_stride;
 }
@@ -1203,6 +1515,32 @@ template <class K> void allow_smem(K kernel, size_t bytes) {
 }
 }  // namespace
 
+// ----------------------------------------------------------------- scratch registry
+// Engines register their reduction scratch (pointer, doubles); the Gram-Schmidt launchers
+// skip any kernel variant whose partial sums would not fit, so no variant can overrun it.
+namespace {
+std::mutex g_scratch_mu;
+std::vector<std::pair<const void *, size_t>> g_scratch;
+size_t scratch_capacity(const void *p) {
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    for (auto &e : g_scratch)
+        if (e.first == p) return e.second;
+    return 0;
+}
+}  // namespace
+
+void register_scratch(const void *p, size_t doubles) {
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    for (auto &e : g_scratch)
+        if (e.first == p) { e.second = doubles; return; }
+    g_scratch.emplace_back(p, doubles);
+}
+void unregister_scratch(const void *p) {
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    for (size_t i = 0; i < g_scratch.size(); ++i)
+        if (g_scratch[i].first == p) { g_scratch.erase(g_scratch.begin() + i); return; }
+}
+
 // ----------------------------------------------------------------- Gram-Schmidt autotuner
 // The projection and update kernels come in (EPT, PU, VEC) variants.  The first launch for a
 // (precision, kernel, n) of at least 8 vectors times every variant on the caller's own
@@ -1220,7 +1558,7 @@ struct TuneKey {
 struct TuneEntry {
     TuneKey key;
     int variant;
-    float ms[8];
+    float ms[12];
     int nvar;
 };
 std::vector<TuneEntry> g_tuned;
@@ -1228,17 +1566,16 @@ std::mutex g_tune_mu;
 bool g_tune_enabled = true;
 thread_local bool t_capturing = false;   // a stream capture is open on this thread: no timing
 
-// One choice per (precision, kernel, n): the measured winners do not depend on the batch
-// size, and a key without it is settled by the first (always eager) cycle of an engine, so a
-// cycle replayed from a CUDA graph uses exactly the kernels the eager cycle would.
-int bucket_of(int nsys) {
-    (void)nsys;
-    return 0;
-}
+// One choice per (precision, kernel, n, shape class).  The shape class separates launches
+// with and without a shared segment (the deflation vectors W) and single- from multi-system
+// launches, because a batch sharing W is limited by re-reading W and favours other tiles.
+// Engines run their first two cycles eagerly, so every class they use is settled before a
+// cycle is captured into a CUDA graph.
+int bucket_of(int nsys, int qa) { return (nsys > 1 ? 1 : 0) + (qa > 0 ? 2 : 0); }
 
 template <class F>
-int tuned_variant(int prec, int kernel, int n, int nsys, int nvar, cudaStream_t st, F &&run) {
-    const TuneKey key{prec, kernel, n, bucket_of(nsys)};
+int tuned_variant(int prec, int kernel, int n, int nsys, int qa, int nvar, cudaStream_t st, F &&run) {
+    const TuneKey key{prec, kernel, n, bucket_of(nsys, qa)};
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)
@@ -1286,8 +1623,9 @@ std::string tune_report() {
     std::string out;
     for (auto &e : g_tuned) {
         char buf[256];
-        int len = snprintf(buf, sizeof buf, "%s %s n=%d: variant %d [", e.key.prec == 4 ? "c64" : "c128",
-                           e.key.kernel == 0 ? "projection" : "update", e.key.n, e.variant);
+        int len = snprintf(buf, sizeof buf, "%s %s n=%d %s %s: variant %d [", e.key.prec == 4 ? "c64" : "c128",
+                           e.key.kernel == 0 ? "projection" : "update", e.key.n,
+                           (e.key.bucket & 1) ? "batch" : "single", (e.key.bucket & 2) ? "shared" : "own", e.variant);
         out.append(buf, len);
         for (int v = 0; v < e.nvar; ++v) {
             len = snprintf(buf, sizeof buf, "%s%.4f", v ? " " : "", e.ms[v]);
@@ -1298,9 +1636,9 @@ std::string tune_report() {
     return out;
 }
 
-// Variant tables: (EPT, PU, VEC).
-//   complex64:  0 (8,2,1)  1 (8,2,2)  2 (16,2,2)  3 (8,4,2)
-//   complex128: 0 (4,2,1)  1 (8,2,1)  2 (4,4,1)
+// Variant tables: (EPT, PU, VEC), or grp(EPT, SB) for the system-grouped kernels.
+//   complex64:  0 (8,2,1)  1 (8,2,2)  2 (16,2,2)  3 (8,4,2)  4 (2,2,1)  5 (1,4,1)  6 grp(4,4)  7 grp(4,2)
+//   complex128: 0 (4,2,1)  1 (8,2,1)  2 (4,4,1)  3 (1,4,1)  4 (2,2,1)  5 grp(4,2)
 template <class R, int EPT, int PU, int VEC>
 void mdot_v(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
             const typename CT<R>::t *w, size_t strideW, const int *act, int nsys, double2 *partials, int qmax,
@@ -1321,6 +1659,29 @@ void update_v(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>
                                                                        tickets, state, fin, skip_broken ? 1 : 0);
 }
 
+template <class R, int EPT, int SB>
+void mdot_g(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
+            const typename CT<R>::t *w, size_t strideW, const int *act, int nsys, double2 *partials, int qmax,
+            unsigned *tickets, double2 *coef, size_t strideC, cudaStream_t st) {
+    const int G = (n + NT * EPT - 1) / (NT * EPT);
+    const size_t smem = sizeof(typename CT<R>::t) * NW * SB * (size_t)qmax;
+    allow_smem(k_mdot_grp<R, EPT, SB>, smem);
+    k_mdot_grp<R, EPT, SB><<<grid2((nsys + SB - 1) / SB, G > 0 ? G : 1), NT, smem, st>>>(
+        n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC);
+}
+template <class R, int EPT, int SB>
+void update_g(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
+              const typename CT<R>::t *w, size_t strideW, typename CT<R>::t *out, size_t strideO, const int *act,
+              int nsys, const double2 *coef, size_t strideC, double2 *partials, unsigned *tickets, SysState *state,
+              FinishArgs fin, bool skip_broken, cudaStream_t st) {
+    const int G = (n + NT * EPT - 1) / (NT * EPT);
+    const size_t smem = sizeof(typename CT<R>::t) * SB * strideC;
+    allow_smem(k_update_grp<R, EPT, SB>, smem);
+    k_update_grp<R, EPT, SB><<<grid2((nsys + SB - 1) / SB, G > 0 ? G : 1), NT, smem, st>>>(
+        n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state,
+        fin, skip_broken ? 1 : 0);
+}
+
 // 16-byte packets need every vector base 16-byte aligned: n even (complex64).
 inline bool vec2_ok(int n, size_t strideB, size_t strideW) { return (n % 2 == 0) && strideB % 2 == 0 && strideW % 2 == 0; }
 
@@ -1330,26 +1691,42 @@ void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT
                  unsigned *tickets, double2 *coef, size_t strideC, SysState *state, bool skip_broken, cudaStream_t st) {
     if (nsys <= 0 || qa + qb <= 0) return;
     Launch L_(KC_MDOT, (double)sizeof(typename CT<R>::t) * n * ((double)qa + (double)nsys * (qb + 1)), st, 1);
+    const size_t cap = scratch_capacity(partials);
+    auto fits = [&](int ept) { return (size_t)nsys * qmax * 2 * (((size_t)n + NT * ept - 1) / (NT * ept)) <= cap; };
     auto run = [&](int v) {
+        if constexpr (sizeof(R) == 4) {
+            static const int ept_of[8] = {8, 8, 16, 8, 2, 1, 4, 4};
+            if (v < 0 || v > 7 || !fits(ept_of[v])) v = 0;
+        } else {
+            static const int ept_of[6] = {4, 8, 4, 1, 2, 4};
+            if (v < 0 || v > 5 || !fits(ept_of[v])) v = 0;
+        }
         if constexpr (sizeof(R) == 4) {
             const bool v2 = vec2_ok(n, strideB, strideW);
             if (v == 1 && v2) mdot_v<R, 8, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
             else if (v == 2 && v2) mdot_v<R, 16, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
             else if (v == 3 && v2) mdot_v<R, 8, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+            else if (v == 4) mdot_v<R, 2, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+            else if (v == 5) mdot_v<R, 1, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+            else if (v == 6) mdot_g<R, 4, 4>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, st);
+            else if (v == 7) mdot_g<R, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, st);
             else mdot_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
         } else {
             if (v == 1) mdot_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
             else if (v == 2) mdot_v<R, 4, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+            else if (v == 3) mdot_v<R, 1, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+            else if (v == 4) mdot_v<R, 2, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+            else if (v == 5) mdot_g<R, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, st);
             else mdot_v<R, 4, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
         }
     };
     // tune on a representative width only (a full projection of at least 8 vectors)
     int v = 0;
-    if (qa + qb >= 8 && !profile_enabled()) v = tuned_variant(sizeof(R), 0, n, nsys, sizeof(R) == 4 ? 4 : 3, st, run);
+    if (qa + qb >= 8 && !profile_enabled()) v = tuned_variant(sizeof(R), 0, n, nsys, qa, sizeof(R) == 4 ? 8 : 6, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)
-            if (e.key == TuneKey{(int)sizeof(R), 0, n, bucket_of(nsys)}) v = e.variant;
+            if (e.key == TuneKey{(int)sizeof(R), 0, n, bucket_of(nsys, qa)}) v = e.variant;
     }
     run(v);
 }
@@ -1361,25 +1738,41 @@ void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename 
                    SysState *state, FinishArgs fin, bool skip_broken, cudaStream_t st) {
     if (nsys <= 0) return;
     Launch L_(KC_UPDATE, (double)sizeof(typename CT<R>::t) * n * ((double)qa + (double)nsys * (qb + 2)), st, 1);
+    const size_t cap = scratch_capacity(partials);
+    auto fits = [&](int ept) { return (size_t)nsys * 3 * (((size_t)n + NT * ept - 1) / (NT * ept)) <= cap; };
     auto run = [&](int v) {
+        if constexpr (sizeof(R) == 4) {
+            static const int ept_of[8] = {8, 8, 16, 8, 2, 1, 4, 4};
+            if (v < 0 || v > 7 || !fits(ept_of[v])) v = 0;
+        } else {
+            static const int ept_of[6] = {4, 8, 4, 1, 2, 4};
+            if (v < 0 || v > 5 || !fits(ept_of[v])) v = 0;
+        }
         if constexpr (sizeof(R) == 4) {
             const bool v2 = vec2_ok(n, strideB, strideW) && strideO % 2 == 0;
             if (v == 1 && v2) update_v<R, 8, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
             else if (v == 2 && v2) update_v<R, 16, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
             else if (v == 3 && v2) update_v<R, 8, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+            else if (v == 4) update_v<R, 2, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+            else if (v == 5) update_v<R, 1, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+            else if (v == 6) update_g<R, 4, 4>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+            else if (v == 7) update_g<R, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
             else update_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
         } else {
             if (v == 1) update_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
             else if (v == 2) update_v<R, 4, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+            else if (v == 3) update_v<R, 1, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+            else if (v == 4) update_v<R, 2, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+            else if (v == 5) update_g<R, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
             else update_v<R, 4, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
         }
     };
     int v = 0;
-    if (qa + qb >= 8 && !profile_enabled()) v = tuned_variant(sizeof(R), 1, n, nsys, sizeof(R) == 4 ? 4 : 3, st, run);
+    if (qa + qb >= 8 && !profile_enabled()) v = tuned_variant(sizeof(R), 1, n, nsys, qa, sizeof(R) == 4 ? 8 : 6, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)
-            if (e.key == TuneKey{(int)sizeof(R), 1, n, bucket_of(nsys)}) v = e.variant;
+            if (e.key == TuneKey{(int)sizeof(R), 1, n, bucket_of(nsys, qa)}) v = e.variant;
     }
     run(v);
 }

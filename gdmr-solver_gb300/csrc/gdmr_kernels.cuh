@@ -102,6 +102,9 @@ std::string tune_report();
 // counters (each kernel resets the counters it used).  Kernels on one stream
 // may share both.
 size_t scratch_doubles(int qmax, int nsys, int n);
+// Reduction scratch handed to the Gram-Schmidt launchers must be registered with its size.
+void register_scratch(const void *p, size_t doubles);
+void unregister_scratch(const void *p);
 
 template <class R>
 void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
