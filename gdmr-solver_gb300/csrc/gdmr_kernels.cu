@@ -349,6 +349,66 @@ __global__ void __launch_bounds__(NT, min_blocks<typename CT<R>::t>(EPT, PU))
     }
 }
 
+// ----------------------------------------------------------------- split-vector projection
+// For short vectors the chunk count is small, so a CTA per chunk walks all q vectors in
+// series.  Here blockIdx.z also splits the vectors into groups of VPG: each (coefficient,
+// chunk) partial is still written by exactly one CTA, and the last of the G x groups CTAs of
+// a system sums them in the fixed order of k_mdot.
+template <class R, int VPG>
+__global__ void __launch_bounds__(NT) k_mdot_vs(int n, const typename CT<R>::t *__restrict__ segA, int qa,
+                                                const typename CT<R>::t *__restrict__ segB0, size_t strideB, int qb,
+                                                const typename CT<R>::t *__restrict__ w0, size_t strideW,
+                                                const int *__restrict__ act, double2 *__restrict__ partials,
+                                                int qmax, unsigned *tickets, double2 *__restrict__ coef0,
+                                                size_t strideC, SysState *state, int skip_broken) {
+    using C = typename CT<R>::t;
+    const int slot = blockIdx.x, s = act[slot], chunk = blockIdx.y, G = gridDim.y;
+    if (skip_broken && state[s].broken) return;
+    const C *segB = segB0 + (size_t)s * strideB;
+    const C *w = w0 + (size_t)s * strideW;
+    const int q = qa + qb, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int p0 = blockIdx.z * VPG, p1 = min(q, p0 + VPG);
+    __shared__ C wsum[NW][VPG];
+    const long i = (long)chunk * NT + tid;
+    const C wv = i < n ? w[i] : czero<C>();
+    C vv[VPG];
+#pragma unroll
+    for (int u = 0; u < VPG; ++u) {
+        const int p = p0 + u < p1 ? p0 + u : p0;
+        const C *vp = p < qa ? segA + (size_t)p * n : segB + (size_t)(p - qa) * n;
+        vv[u] = i < n ? vp[i] : czero<C>();
+    }
+#pragma unroll
+    for (int u = 0; u < VPG; ++u) {
+        C a = czero<C>();
+        cdotacc(a, vv[u], wv);
+        a.x = warp_sum(a.x);
+        a.y = warp_sum(a.y);
+        if (lane == 0) wsum[warp][u] = a;
+    }
+    __syncthreads();
+    double *part = (double *)partials + (size_t)slot * qmax * 2 * G;
+    for (int u = tid; u < p1 - p0; u += NT) {
+        double re = 0, im = 0;
+#pragma unroll
+        for (int ww = 0; ww < NW; ++ww) { re += (double)wsum[ww][u].x; im += (double)wsum[ww][u].y; }
+        double *pp = part + (size_t)(p0 + u) * 2 * G;
+        pp[chunk] = re;
+        pp[G + chunk] = im;
+    }
+    if (!arrive_last(&tickets[slot], (unsigned)G * gridDim.z)) return;
+    double2 *coef = coef0 + (size_t)s * strideC;
+    for (int p = warp; p < q; p += NW) {
+        const double *pp = part + (size_t)p * 2 * G;
+        double re = 0, im = 0;
+        for (int g = lane; g < G; g += 32) { re += __ldcg(pp + g); im += __ldcg(pp + G + g); }
+        re = warp_sum(re);
+        im = warp_sum(im);
+        if (lane == 0) coef[p] = make_double2(re, im);
+    }
+    if (tid == 0) tickets[slot] = 0;
+}
+
 // ----------------------------------------------------------------- system-grouped variants
 // One CTA serves SB systems of one chunk: every tile of the shared vectors (segment A, the
 // deflation basis W) is loaded once and used for all SB systems, instead of once per system
@@ -483,7 +543,7 @@ __global__ void __launch_bounds__(NT, 2)
     __shared__ double red[3][NW];
     const int slot0 = blockIdx.x * SB, ns = min(SB, nsys - slot0), chunk = blockIdx.y, G = gridDim.y;
     const int q = qa + qb, tid = threadIdx.x;
-    const int qmax = (int)strideC;
+    const int qmax = q;   // coefficient table row length (strideC may be 0: one shared coefficient vector)
     int sys[SB];
     bool live[SB];
 #pragma unroll
@@ -1638,7 +1698,9 @@ std::string tune_report() {
 
 // Variant tables: (EPT, PU, VEC), or grp(EPT, SB) for the system-grouped kernels.
 //   complex64:  0 (8,2,1)  1 (8,2,2)  2 (16,2,2)  3 (8,4,2)  4 (2,2,1)  5 (1,4,1)  6 grp(4,4)  7 grp(4,2)
+//               projection only: 8 split-vector(4)
 //   complex128: 0 (4,2,1)  1 (8,2,1)  2 (4,4,1)  3 (1,4,1)  4 (2,2,1)  5 grp(4,2)
+//               projection only: 6 split-vector(4)
 template <class R, int EPT, int PU, int VEC>
 void mdot_v(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
             const typename CT<R>::t *w, size_t strideW, const int *act, int nsys, double2 *partials, int qmax,
@@ -1659,6 +1721,16 @@ void update_v(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>
                                                                        tickets, state, fin, skip_broken ? 1 : 0);
 }
 
+template <class R, int VPG>
+void mdot_s(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
+            const typename CT<R>::t *w, size_t strideW, const int *act, int nsys, double2 *partials, int qmax,
+            unsigned *tickets, double2 *coef, size_t strideC, SysState *state, bool skip_broken, cudaStream_t st) {
+    const int G = (n + NT - 1) / NT, groups = (qa + qb + VPG - 1) / VPG;
+    k_mdot_vs<R, VPG><<<dim3((unsigned)nsys, (unsigned)(G > 0 ? G : 1), (unsigned)groups), NT, 0, st>>>(
+        n, segA, qa, segB, strideB, qb, w, strideW, act, partials, qmax, tickets, coef, strideC, state,
+        skip_broken ? 1 : 0);
+}
+
 template <class R, int EPT, int SB>
 void mdot_g(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
             const typename CT<R>::t *w, size_t strideW, const int *act, int nsys, double2 *partials, int qmax,
@@ -1675,7 +1747,7 @@ void update_g(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>
               int nsys, const double2 *coef, size_t strideC, double2 *partials, unsigned *tickets, SysState *state,
               FinishArgs fin, bool skip_broken, cudaStream_t st) {
     const int G = (n + NT * EPT - 1) / (NT * EPT);
-    const size_t smem = sizeof(typename CT<R>::t) * SB * strideC;
+    const size_t smem = sizeof(typename CT<R>::t) * SB * (size_t)(qa + qb > 0 ? qa + qb : 1);
     allow_smem(k_update_grp<R, EPT, SB>, smem);
     k_update_grp<R, EPT, SB><<<grid2((nsys + SB - 1) / SB, G > 0 ? G : 1), NT, smem, st>>>(
         n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state,
@@ -1695,14 +1767,15 @@ void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT
     auto fits = [&](int ept) { return (size_t)nsys * qmax * 2 * (((size_t)n + NT * ept - 1) / (NT * ept)) <= cap; };
     auto run = [&](int v) {
         if constexpr (sizeof(R) == 4) {
-            static const int ept_of[8] = {8, 8, 16, 8, 2, 1, 4, 4};
-            if (v < 0 || v > 7 || !fits(ept_of[v])) v = 0;
+            static const int ept_of[9] = {8, 8, 16, 8, 2, 1, 4, 4, 1};
+            if (v < 0 || v > 8 || !fits(ept_of[v])) v = 0;
         } else {
-            static const int ept_of[6] = {4, 8, 4, 1, 2, 4};
-            if (v < 0 || v > 5 || !fits(ept_of[v])) v = 0;
+            static const int ept_of[7] = {4, 8, 4, 1, 2, 4, 1};
+            if (v < 0 || v > 6 || !fits(ept_of[v])) v = 0;
         }
         if constexpr (sizeof(R) == 4) {
             const bool v2 = vec2_ok(n, strideB, strideW);
+            if (v == 8) { mdot_s<R, 4>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st); return; }
             if (v == 1 && v2) mdot_v<R, 8, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
             else if (v == 2 && v2) mdot_v<R, 16, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
             else if (v == 3 && v2) mdot_v<R, 8, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
@@ -1712,6 +1785,7 @@ void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT
             else if (v == 7) mdot_g<R, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, st);
             else mdot_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
         } else {
+            if (v == 6) { mdot_s<R, 4>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st); return; }
             if (v == 1) mdot_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
             else if (v == 2) mdot_v<R, 4, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
             else if (v == 3) mdot_v<R, 1, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
@@ -1722,7 +1796,7 @@ void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT
     };
     // tune on a representative width only (a full projection of at least 8 vectors)
     int v = 0;
-    if (qa + qb >= 8 && !profile_enabled()) v = tuned_variant(sizeof(R), 0, n, nsys, qa, sizeof(R) == 4 ? 8 : 6, st, run);
+    if (qa + qb >= 8 && !profile_enabled()) v = tuned_variant(sizeof(R), 0, n, nsys, qa, sizeof(R) == 4 ? 9 : 7, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)
