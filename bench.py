@@ -46,6 +46,14 @@ SHAPE = (96, 96, 96)
 KAPPA, DAMPING, M, K, TOL = 24.0, 0.1, 48, 24, 1e-10
 
 
+# DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic byte, per kernel
+# class, from one capture of every launch of three batched cycles on the same operator
+# (profiles/dram_traffic_mixed96_8rhs.md).  The ratio does not depend on the batch size: every
+# system's vectors are separate streams and the shared deflation vectors are counted once.
+TRAFFIC_PER_ALGORITHMIC_BYTE = {"projection": 1.003, "update": 0.991, "operator": 0.847, "combine": 0.994,
+                                "deflation_update": 1.329, "residual64": 1.312, "other": 0.595}
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -365,6 +373,11 @@ def main():
     ap.add_argument("--serve-pool", type=int, default=4)
     ap.add_argument("--solve-only", action="store_true",
                     help="only the timed batched solves (for profiler captures); prints a short line")
+    ap.add_argument("--force-variants", default=None, metavar="P,U",
+                    help="pin the Gram-Schmidt projection and update variants (gdmrTuneForce)")
+    ap.add_argument("--profile-classes", action="store_true",
+                    help="with --solve-only: record the library's per-class algorithmic bytes and CUDA-event "
+                         "times over the timed steps (tuning off) and print them")
     args = ap.parse_args()
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
@@ -386,6 +399,8 @@ def main():
     gdmr.load()
     hbm_peak, peak_kind = peaks()
 
+    if args.force_variants:
+        gdmr.tune_force(*(int(v) for v in args.force_variants.split(",")))
     A, B = build_workload(args.nrhs, rank)
     nrhs, n = B.shape
     sysm = gdmr.System(A, M, K, capacity=nrhs, precision="mixed", device=local)
@@ -401,6 +416,9 @@ def main():
 
     for _ in range(args.warmup):
         step()
+    if args.profile_classes:
+        gdmr.profile_reset()
+        gdmr.profile(True)
     # timed region: device-resident inputs
     lat, cycles, verified, worst_res = [], [], True, 0.0
     barrier(world)
@@ -425,11 +443,15 @@ def main():
     value = world * nrhs * args.steps / (elapsed_ms / 1e3)
     clocks = clk.summary()
     if args.solve_only:
+        out = {"mode": "solve-only", "value": value, "unit": "solves/s", "nrhs": nrhs,
+               "ms_per_step": elapsed_ms / args.steps, "verified": bool(verified),
+               "gpu_launches": int(launches), "svd_sweeps": sysm.svd_sweeps(),
+               "tuning": gdmr.tune_report().strip().splitlines()}
+        if args.profile_classes:
+            gdmr.profile(False)
+            out["classes"] = {k: v for k, v in gdmr.profile_read().items() if v["launches"]}
         if rank == 0:
-            print(json.dumps({"mode": "solve-only", "value": value, "unit": "solves/s", "nrhs": nrhs,
-                              "ms_per_step": elapsed_ms / args.steps, "verified": bool(verified),
-                              "gpu_launches": int(launches), "svd_sweeps": sysm.svd_sweeps(),
-                              "tuning": gdmr.tune_report().strip().splitlines()}), flush=True)
+            print(json.dumps(out), flush=True)
         return
 
     # roofline: one more step with library-side CUDA events per kernel class
@@ -442,9 +464,16 @@ def main():
     tot_ms = sum(v["ms"] for v in prof.values())
     d = prof[dom]
     achieved = d["bytes"] / (d["ms"] / 1e3) / 1e9
+    ratio = TRAFFIC_PER_ALGORITHMIC_BYTE.get(dom)
+    per_launch = d["bytes"] / max(1, d["launches"])
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "peak_kind": peak_kind,
-                "traffic": None, "share": d["ms"] / tot_ms,
+                "algorithmic_bytes_per_launch": per_launch,
+                "traffic": ratio * per_launch if ratio is not None else None,
+                "traffic_basis": (f"ncu DRAM bytes = {ratio} x algorithmic bytes for this class "
+                                  "(every launch of 3 cycles, 96^3, 8 RHS), times this run's mean "
+                                  "algorithmic bytes per launch") if ratio is not None else None,
+                "share": d["ms"] / tot_ms,
                 "classes": {k: {"GB/s": (v["bytes"] / (v["ms"] / 1e3) / 1e9) if v["ms"] > 0 else None,
                                 "share": v["ms"] / tot_ms, "launches": v["launches"]} for k, v in prof.items()}}
 

@@ -381,6 +381,9 @@ extern "C" long long gdmrKernelLaunches(void) { return launch_count(); }
 extern "C" void gdmrProfile(int on) { profile_enable(on != 0); }
 extern "C" void gdmrProfileReset(void) { profile_reset(); }
 extern "C" void gdmrTune(int on) { tune_enable(on != 0); }
+extern "C" void gdmrTuneForce(int projectionVariant, int updateVariant) {
+    tune_force(projectionVariant, updateVariant);
+}
 extern "C" const char *gdmrTuneReport(void) {
     static thread_local std::string rep;
     rep = tune_report();

@@ -349,6 +349,294 @@ __global__ void __launch_bounds__(NT, min_blocks<typename CT<R>::t>(EPT, PU))
     }
 }
 
+// ----------------------------------------------------------------- batched W projection
+// coef_s[p] = <W_p, y_s> for every active system s and deflation vector p: the shared part
+// of a batched projection as one split-K product, so W is read once for the whole batch
+// instead of once per system.  Persistent CTAs walk row tiles; a tile of W (kk x RT) and of
+// the batch (nsys x RT) is copied into shared memory with cp.async, double-buffered, in its
+// natural vector-major layout (leading dimension RT+2, so the strided thread tiling below
+// reads distinct banks).  Thread (ip, js) of row group grp accumulates the 4 x 4 outputs
+// p = ip + tilesP*a, s = js + tilesS*b over the rows grp, grp+KS, ... of each tile, and
+// flushes them to double after every tile.  The KS row groups are summed in shared memory
+// in a fixed order, and k_wproj_reduce sums the CTAs' partials in a fixed order.
+constexpr int WP_KMAX = 32, WP_SMAX = 64;
+template <class R> __host__ __device__ constexpr int wp_rt() { return sizeof(R) == 4 ? 64 : 32; }
+
+__device__ __forceinline__ void cp_async_el(void *dst, const void *src, int bytes, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    const int sz = valid ? bytes : 0;   // 0: zero-fill, nothing read
+    if (bytes == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(sz) : "memory");
+    else
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(sz) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+struct WprojShape {
+    int tilesP, tilesS, KP, SP, nout, KS;
+};
+__host__ __device__ inline WprojShape wproj_shape(int kk, int nsys) {
+    WprojShape w;
+    w.tilesP = (kk + 3) / 4;
+    w.tilesS = (nsys + 3) / 4;
+    w.KP = 4 * w.tilesP;
+    w.SP = 4 * w.tilesS;
+    w.nout = w.tilesP * w.tilesS;
+    w.KS = NT / w.nout;
+    if (w.KS > 8) w.KS = 8;
+    return w;
+}
+template <class R> size_t wproj_smem(int kk, int nsys) {
+    const WprojShape w = wproj_shape(kk, nsys);
+    const size_t tiles = 2 * (size_t)(w.KP + w.SP) * (wp_rt<R>() + 2) * sizeof(typename CT<R>::t);
+    const size_t red = (size_t)NT * 16 * sizeof(double2);
+    return tiles > red ? tiles : red;
+}
+
+template <class R>
+__global__ void __launch_bounds__(NT, 2) k_wproj(int n, int kk, const typename CT<R>::t *__restrict__ W,
+                                                 const typename CT<R>::t *__restrict__ Y0, size_t strideY,
+                                                 const int *__restrict__ act, int nsys, double *__restrict__ part) {
+    using C = typename CT<R>::t;
+    constexpr int RT = wp_rt<R>(), LD = RT + 2;
+    extern __shared__ __align__(16) unsigned char wp_sm[];
+    __shared__ int s_act[WP_SMAX];
+    const WprojShape sh = wproj_shape(kk, nsys);
+    const int stage = (sh.KP + sh.SP) * LD;
+    C *buf = reinterpret_cast<C *>(wp_sm);
+    const int tid = threadIdx.x, G = gridDim.x;
+    const int grp = tid / sh.nout, o = tid % sh.nout, ip = o % sh.tilesP, js = o / sh.tilesP;
+    const bool mine = grp < sh.KS;
+    // zero both buffers once: the padding vectors (p >= kk, s >= nsys) are never copied
+    for (int e = tid; e < 2 * stage; e += NT) buf[e] = czero<C>();
+    if (tid < nsys) s_act[tid] = act[tid];
+    __syncthreads();
+    const long nrt = (n + RT - 1) / RT;
+    auto issue = [&](long rt, int b) {
+        C *Wt = buf + (size_t)b * stage;
+        C *Yt = Wt + (size_t)sh.KP * LD;
+        const long r0 = rt * RT;
+        for (int e = tid; e < kk * RT; e += NT) {
+            const int p = e / RT, r = e % RT;
+            const bool v = r0 + r < n;
+            cp_async_el(Wt + p * LD + r, W + (size_t)p * n + (v ? r0 + r : 0), sizeof(C), v);
+        }
+        for (int e = tid; e < nsys * RT; e += NT) {
+            const int sl = e / RT, r = e % RT;
+            const bool v = r0 + r < n;
+            cp_async_el(Yt + sl * LD + r, Y0 + (size_t)s_act[sl] * strideY + (v ? r0 + r : 0), sizeof(C), v);
+        }
+        cp_async_commit();
+    };
+    double2 accd[4][4];
+    C acc[4][4];   // complex64: one tile's sums; complex128: the running sums
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            accd[a][c] = make_double2(0.0, 0.0);
+            acc[a][c] = czero<C>();
+        }
+    int b = 0;
+    if ((long)blockIdx.x < nrt) issue(blockIdx.x, 0);
+    for (long rt = blockIdx.x; rt < nrt; rt += G, b ^= 1) {
+        if (rt + G < nrt) issue(rt + G, b ^ 1);
+        else cp_async_commit();   // empty group keeps wait_group 1 meaning "tile rt landed"
+        cp_async_wait1();
+        __syncthreads();
+        if (mine) {
+            const C *Wt = buf + (size_t)b * stage;
+            const C *Yt = Wt + (size_t)sh.KP * LD;
+            if constexpr (sizeof(R) == 4) {
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) acc[a][c] = czero<C>();
+            }
+#pragma unroll 2
+            for (int r = grp; r < RT; r += sh.KS) {
+                C wv[4], yv[4];
+#pragma unroll
+                for (int a = 0; a < 4; ++a) wv[a] = Wt[(ip + sh.tilesP * a) * LD + r];
+#pragma unroll
+                for (int c = 0; c < 4; ++c) yv[c] = Yt[(js + sh.tilesS * c) * LD + r];
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) cdotacc(acc[a][c], wv[a], yv[c]);
+            }
+            if constexpr (sizeof(R) == 4) {   // complex64: flush the tile's sums to double
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        accd[a][c].x += (double)acc[a][c].x;
+                        accd[a][c].y += (double)acc[a][c].y;
+                    }
+            }
+        }
+        __syncthreads();
+    }
+    if constexpr (sizeof(R) == 8) {
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) accd[a][c] = make_double2(acc[a][c].x, acc[a][c].y);
+    }
+    // sum the row groups (fixed order) through shared memory, then write this CTA's partials
+    double2 *red = reinterpret_cast<double2 *>(wp_sm);   // [thread][16]
+    if (mine && grp > 0)
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) red[(size_t)tid * 16 + a * 4 + c] = accd[a][c];
+    __syncthreads();
+    if (mine && grp == 0) {
+        for (int g = 1; g < sh.KS; ++g) {
+            const double2 *rg = red + (size_t)(g * sh.nout + o) * 16;
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    accd[a][c].x += rg[a * 4 + c].x;
+                    accd[a][c].y += rg[a * 4 + c].y;
+                }
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int p = ip + sh.tilesP * a, sl = js + sh.tilesS * c;
+                if (p < kk && sl < nsys) {
+                    double *pp = part + ((size_t)p * nsys + sl) * 2 * G;
+                    pp[blockIdx.x] = accd[a][c].x;
+                    pp[G + blockIdx.x] = accd[a][c].y;
+                }
+            }
+    }
+}
+
+// coef_s[p] = sum over the G partials of output (p, s), one warp per output, fixed order.
+__global__ void __launch_bounds__(NT) k_wproj_reduce(int kk, int nsys, int G, const double *__restrict__ part,
+                                                     const int *__restrict__ act, double2 *__restrict__ coef0,
+                                                     size_t strideC) {
+    const int lane = threadIdx.x & 31;
+    const int o = blockIdx.x * NW + (threadIdx.x >> 5);
+    if (o >= kk * nsys) return;
+    const int p = o / nsys, sl = o % nsys;
+    const double *pp = part + (size_t)o * 2 * G;
+    double re = 0, im = 0;
+    for (int g = lane; g < G; g += 32) { re += pp[g]; im += pp[G + g]; }
+    re = warp_sum(re);
+    im = warp_sum(im);
+    if (lane == 0) coef0[(size_t)act[sl] * strideC + p] = make_double2(re, im);
+}
+
+// ----------------------------------------------------------------- batched update, W in registers
+// out_s = w_s - W c_s[0:kk] - V_s c_s[kk:kk+qb] for a group of SGU systems and NT rows per CTA:
+// each thread keeps its row of W (kk <= KW values) in registers and applies it to every system
+// of the group, so W is read from memory once per group instead of once per system.  Norm
+// partials reduce per warp into shared memory and once per CTA; the finish is k_update's.
+// Grid (groups, chunks): the groups of one chunk run side by side and share W through L2.
+template <class R, int KW, int SGU>
+__global__ void __launch_bounds__(NT, 2) k_update_wreg(int n, int kk, const typename CT<R>::t *__restrict__ W,
+                                                       const typename CT<R>::t *__restrict__ V0, size_t strideV, int qb,
+                                                       const typename CT<R>::t *__restrict__ w0, size_t strideW,
+                                                       typename CT<R>::t *__restrict__ out0, size_t strideO,
+                                                       const int *__restrict__ act, int nsys,
+                                                       const double2 *__restrict__ coef0, size_t strideC,
+                                                       double2 *__restrict__ partials, unsigned *tickets,
+                                                       SysState *state, FinishArgs fin, int skip_broken) {
+    using C = typename CT<R>::t;
+    extern __shared__ __align__(16) unsigned char uw_sm[];
+    const int q = kk + qb;
+    C *cs = reinterpret_cast<C *>(uw_sm);   // [SGU][q]
+    __shared__ double red[3][SGU][NW];
+    __shared__ int s_act[SGU], s_live[SGU];
+    __shared__ unsigned lastmask;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int g0 = blockIdx.x * SGU, ng = min(SGU, nsys - g0);
+    const int chunk = blockIdx.y, G = gridDim.y;
+    const long i = (long)chunk * NT + tid;
+    const bool in = i < n;
+    C wr[KW];
+#pragma unroll
+    for (int p = 0; p < KW; ++p) wr[p] = (p < kk && in) ? W[(size_t)p * n + i] : czero<C>();
+    for (int e = tid; e < ng * q; e += NT) {
+        const int g = e / q, p = e % q;
+        cs[(size_t)g * q + p] = from_d<C>(coef0[(size_t)act[g0 + g] * strideC + p]);
+    }
+    if (tid < ng) {
+        const int s = act[g0 + tid];
+        s_act[tid] = s;
+        s_live[tid] = !(skip_broken && state[s].broken);
+    }
+    __syncthreads();
+    for (int g = 0; g < ng; ++g) {
+        const int s = s_act[g];
+        C org = czero<C>(), acc = czero<C>();
+        if (s_live[g] && in) {
+            org = w0[(size_t)s * strideW + i];
+            acc = org;
+            const C *c = cs + (size_t)g * q;
+#pragma unroll
+            for (int p = 0; p < KW; ++p)
+                if (p < kk) cfms(acc, c[p], wr[p]);
+            const C *V = V0 + (size_t)s * strideV + i;
+#pragma unroll 4
+            for (int p = 0; p < qb; ++p) cfms(acc, c[kk + p], V[(size_t)p * n]);
+            out0[(size_t)s * strideO + i] = acc;
+        }
+        C ln = czero<C>(), lc = czero<C>();
+        cdotacc(ln, acc, acc);
+        cdotacc(lc, acc, org);
+        const double v0 = warp_sum((double)ln.x), v1 = warp_sum((double)lc.x), v2 = warp_sum((double)lc.y);
+        if (lane == 0) {
+            red[0][g][warp] = v0;
+            red[1][g][warp] = v1;
+            red[2][g][warp] = v2;
+        }
+    }
+    __syncthreads();
+    if (tid < ng) {
+        double t0 = 0, t1 = 0, t2 = 0;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            t0 += red[0][tid][w];
+            t1 += red[1][tid][w];
+            t2 += red[2][tid][w];
+        }
+        double *part = (double *)partials + (size_t)(g0 + tid) * 3 * G;
+        part[chunk] = t0;
+        part[G + chunk] = t1;
+        part[2 * G + chunk] = t2;
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) {
+        unsigned mk = 0;
+        for (int g = 0; g < ng; ++g)
+            if (atomicAdd(&tickets[g0 + g], 1u) == (unsigned)G - 1) mk |= 1u << g;
+        lastmask = mk;
+    }
+    __syncthreads();
+    if (!lastmask) return;
+    __threadfence();
+    __shared__ double red2[3][NW];
+    for (int g = 0; g < ng; ++g) {
+        if (!(lastmask >> g & 1u)) continue;
+        const int s = s_act[g];
+        double tot[3];
+        sum_partials<3>((double *)partials + (size_t)(g0 + g) * 3 * G, G, tot, red2);
+        if (tid == 0) {
+            if (s_live[g]) run_finish(fin, s, state[s], tot[0], tot[1], tot[2]);
+            tickets[g0 + g] = 0;
+        }
+        __syncthreads();
+    }
+}
+
 // ----------------------------------------------------------------- split-vector projection
 // For short vectors the chunk count is small, so a CTA per chunk walks all q vectors in
 // series.  Here blockIdx.z also splits the vectors into groups of VPG: each (coefficient,
@@ -1494,6 +1782,7 @@ struct Launch {
             cudaEventRecord(a, st);
         }
     }
+    void add(int k) { g_launches += k; }
     ~Launch() {
         if (a) {
             std::lock_guard<std::mutex> lk(g_prof_mu);
@@ -1624,6 +1913,11 @@ struct TuneEntry {
 std::vector<TuneEntry> g_tuned;
 std::mutex g_tune_mu;
 bool g_tune_enabled = true;
+int g_forced[2] = {-1, -1};
+int forced_variant(int kernel) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    return g_forced[kernel];
+}
 thread_local bool t_capturing = false;   // a stream capture is open on this thread: no timing
 
 // One choice per (precision, kernel, n, shape class).  The shape class separates launches
@@ -1632,6 +1926,11 @@ thread_local bool t_capturing = false;   // a stream capture is open on this thr
 // Engines run their first two cycles eagerly, so every class they use is settled before a
 // cycle is captured into a CUDA graph.
 int bucket_of(int nsys, int qa) { return (nsys > 1 ? 1 : 0) + (qa > 0 ? 2 : 0); }
+
+// A class is tuned on its first launch with at least 8 own-basis vectors (mid-cycle Krylov
+// steps, where the own part weighs as it does on average), or, for a single system, at least
+// 8 shared vectors (the deflation loop, which has no own part).
+bool representative(int nsys, int qa, int qb) { return qb >= 8 || (nsys == 1 && qa >= 8); }
 
 template <class F>
 int tuned_variant(int prec, int kernel, int n, int nsys, int qa, int nvar, cudaStream_t st, F &&run) {
@@ -1672,6 +1971,12 @@ int tuned_variant(int prec, int kernel, int n, int nsys, int qa, int nvar, cudaS
 }  // namespace
 
 void set_capturing(bool on) { t_capturing = on; }
+
+void tune_force(int projection, int update) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_forced[0] = projection;
+    g_forced[1] = update;
+}
 
 void tune_enable(bool on) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -1757,52 +2062,131 @@ void update_g(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>
 // 16-byte packets need every vector base 16-byte aligned: n even (complex64).
 inline bool vec2_ok(int n, size_t strideB, size_t strideW) { return (n % 2 == 0) && strideB % 2 == 0 && strideW % 2 == 0; }
 
+bool batched_w_ok(int kk, int nsys) { return kk > 0 && kk <= WP_KMAX && nsys >= 8 && nsys <= WP_SMAX; }
+
+int wproj_grid(int n, int rt) {
+    const long nrt = (n + rt - 1) / rt;
+    long G = (long)num_sms() * 2;
+    if (G > nrt) G = nrt;
+    return G < 1 ? 1 : (int)G;
+}
+
+// Shared-W projection for a batch: two launches, no profiling bracket of its own (the
+// caller's covers it).
+template <class R>
+void wproj_run(int n, int kk, const typename CT<R>::t *W, const typename CT<R>::t *Y, size_t strideY, const int *act,
+               int nsys, double2 *partials, double2 *coef, size_t strideC, cudaStream_t st) {
+    const int G = wproj_grid(n, wp_rt<R>());
+    const size_t smem = wproj_smem<R>(kk, nsys);
+    allow_smem(k_wproj<R>, smem);
+    k_wproj<R><<<G, NT, smem, st>>>(n, kk, W, Y, strideY, act, nsys, (double *)partials);
+    const int outs = kk * nsys;
+    k_wproj_reduce<<<(outs + NW - 1) / NW, NT, 0, st>>>(kk, nsys, G, (const double *)partials, act, coef, strideC);
+}
+
+// W rows held in registers: complex64 up to 32 vectors, complex128 up to 16.
+template <class R> constexpr int wreg_max() { return sizeof(R) == 4 ? 32 : 16; }
+
+template <class R>
+void update_wreg_run(int n, int kk, const typename CT<R>::t *W, const typename CT<R>::t *V, size_t strideV, int qb,
+                     const typename CT<R>::t *w, size_t strideW, typename CT<R>::t *out, size_t strideO,
+                     const int *act, int nsys, const double2 *coef, size_t strideC, double2 *partials,
+                     unsigned *tickets, SysState *state, FinishArgs fin, bool skip_broken, cudaStream_t st) {
+    constexpr int SGU = 16;
+    const int G = (n + NT - 1) / NT;
+    const size_t smem = sizeof(typename CT<R>::t) * (size_t)SGU * (kk + qb);
+    const dim3 grid((nsys + SGU - 1) / SGU, G);
+    if (kk <= 16) {
+        allow_smem(k_update_wreg<R, 16, SGU>, smem);
+        k_update_wreg<R, 16, SGU><<<grid, NT, smem, st>>>(n, kk, W, V, strideV, qb, w, strideW, out, strideO, act,
+                                                          nsys, coef, strideC, partials, tickets, state, fin,
+                                                          skip_broken ? 1 : 0);
+    } else {
+        constexpr int KW = wreg_max<R>() > 16 ? wreg_max<R>() : 16;
+        allow_smem(k_update_wreg<R, KW, SGU>, smem);
+        k_update_wreg<R, KW, SGU><<<grid, NT, smem, st>>>(n, kk, W, V, strideV, qb, w, strideW, out, strideO, act,
+                                                          nsys, coef, strideC, partials, tickets, state, fin,
+                                                          skip_broken ? 1 : 0);
+    }
+}
+
+// The projection variants; returns the number of kernels launched.
+template <class R>
+int mdot_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB,
+                  int qb, const typename CT<R>::t *w, size_t strideW, const int *act, int nsys, double2 *partials,
+                  int qmax, unsigned *tickets, double2 *coef, size_t strideC, SysState *state, bool skip_broken,
+                  cudaStream_t st) {
+    const size_t cap = scratch_capacity(partials);
+    auto fits = [&](int ept) { return (size_t)nsys * qmax * 2 * (((size_t)n + NT * ept - 1) / (NT * ept)) <= cap; };
+    constexpr int VW = sizeof(R) == 4 ? 9 : 7;   // batched shared-W variant
+    if (v == VW) {
+        if (qa > 0 && batched_w_ok(qa, nsys) && (size_t)qa * nsys * 2 * wproj_grid(n, wp_rt<R>()) <= cap) {
+            wproj_run<R>(n, qa, segA, w, strideW, act, nsys, partials, coef, strideC, st);
+            if (qb == 0) return 2;
+            // own-basis part: the tuned choice for a batch without a shared segment
+            int vown = 0;
+            {
+                std::lock_guard<std::mutex> lk(g_tune_mu);
+                for (auto &e : g_tuned)
+                    if (e.key == TuneKey{(int)sizeof(R), 0, n, bucket_of(nsys, 0)}) vown = e.variant;
+            }
+            if (vown == VW) vown = 0;
+            return 2 + mdot_dispatch<R>(vown, n, nullptr, 0, segB, strideB, qb, w, strideW, act, nsys, partials, qmax,
+                                        tickets, coef + qa, strideC, state, skip_broken, st);
+        }
+        v = 0;
+    }
+    if constexpr (sizeof(R) == 4) {
+        static const int ept_of[9] = {8, 8, 16, 8, 2, 1, 4, 4, 1};
+        if (v < 0 || v > 8 || !fits(ept_of[v])) v = 0;
+    } else {
+        static const int ept_of[7] = {4, 8, 4, 1, 2, 4, 1};
+        if (v < 0 || v > 6 || !fits(ept_of[v])) v = 0;
+    }
+    if constexpr (sizeof(R) == 4) {
+        const bool v2 = vec2_ok(n, strideB, strideW);
+        if (v == 8) { mdot_s<R, 4>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st); return 1; }
+        if (v == 1 && v2) mdot_v<R, 8, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+        else if (v == 2 && v2) mdot_v<R, 16, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+        else if (v == 3 && v2) mdot_v<R, 8, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+        else if (v == 4) mdot_v<R, 2, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+        else if (v == 5) mdot_v<R, 1, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+        else if (v == 6) mdot_g<R, 4, 4>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, st);
+        else if (v == 7) mdot_g<R, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, st);
+        else mdot_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+    } else {
+        if (v == 6) { mdot_s<R, 4>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st); return 1; }
+        if (v == 1) mdot_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+        else if (v == 2) mdot_v<R, 4, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+        else if (v == 3) mdot_v<R, 1, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+        else if (v == 4) mdot_v<R, 2, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+        else if (v == 5) mdot_g<R, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, st);
+        else mdot_v<R, 4, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
+    }
+    return 1;
+}
+
 template <class R>
 void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
                  const typename CT<R>::t *w, size_t strideW, const int *act, int nsys, double2 *partials, int qmax,
                  unsigned *tickets, double2 *coef, size_t strideC, SysState *state, bool skip_broken, cudaStream_t st) {
     if (nsys <= 0 || qa + qb <= 0) return;
-    Launch L_(KC_MDOT, (double)sizeof(typename CT<R>::t) * n * ((double)qa + (double)nsys * (qb + 1)), st, 1);
-    const size_t cap = scratch_capacity(partials);
-    auto fits = [&](int ept) { return (size_t)nsys * qmax * 2 * (((size_t)n + NT * ept - 1) / (NT * ept)) <= cap; };
+    Launch L_(KC_MDOT, (double)sizeof(typename CT<R>::t) * n * ((double)qa + (double)nsys * (qb + 1)), st, 0);
+    int launched = 0;
     auto run = [&](int v) {
-        if constexpr (sizeof(R) == 4) {
-            static const int ept_of[9] = {8, 8, 16, 8, 2, 1, 4, 4, 1};
-            if (v < 0 || v > 8 || !fits(ept_of[v])) v = 0;
-        } else {
-            static const int ept_of[7] = {4, 8, 4, 1, 2, 4, 1};
-            if (v < 0 || v > 6 || !fits(ept_of[v])) v = 0;
-        }
-        if constexpr (sizeof(R) == 4) {
-            const bool v2 = vec2_ok(n, strideB, strideW);
-            if (v == 8) { mdot_s<R, 4>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st); return; }
-            if (v == 1 && v2) mdot_v<R, 8, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
-            else if (v == 2 && v2) mdot_v<R, 16, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
-            else if (v == 3 && v2) mdot_v<R, 8, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
-            else if (v == 4) mdot_v<R, 2, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
-            else if (v == 5) mdot_v<R, 1, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
-            else if (v == 6) mdot_g<R, 4, 4>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, st);
-            else if (v == 7) mdot_g<R, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, st);
-            else mdot_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
-        } else {
-            if (v == 6) { mdot_s<R, 4>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st); return; }
-            if (v == 1) mdot_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
-            else if (v == 2) mdot_v<R, 4, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
-            else if (v == 3) mdot_v<R, 1, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
-            else if (v == 4) mdot_v<R, 2, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
-            else if (v == 5) mdot_g<R, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, st);
-            else mdot_v<R, 4, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets, coef, strideC, state, skip_broken, st);
-        }
+        launched = mdot_dispatch<R>(v, n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets,
+                                    coef, strideC, state, skip_broken, st);
     };
-    // tune on a representative width only (a full projection of at least 8 vectors)
     int v = 0;
-    if (qa + qb >= 8 && !profile_enabled()) v = tuned_variant(sizeof(R), 0, n, nsys, qa, sizeof(R) == 4 ? 9 : 7, st, run);
+    if (forced_variant(0) >= 0) v = forced_variant(0);
+    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(sizeof(R), 0, n, nsys, qa, sizeof(R) == 4 ? 10 : 8, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)
             if (e.key == TuneKey{(int)sizeof(R), 0, n, bucket_of(nsys, qa)}) v = e.variant;
     }
     run(v);
+    L_.add(launched);
 }
 
 template <class R>
@@ -1814,7 +2198,16 @@ void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename 
     Launch L_(KC_UPDATE, (double)sizeof(typename CT<R>::t) * n * ((double)qa + (double)nsys * (qb + 2)), st, 1);
     const size_t cap = scratch_capacity(partials);
     auto fits = [&](int ept) { return (size_t)nsys * 3 * (((size_t)n + NT * ept - 1) / (NT * ept)) <= cap; };
+    constexpr int VW = sizeof(R) == 4 ? 8 : 6;   // batched shared-W variant
     auto run = [&](int v) {
+        if (v == VW) {
+            if (qa > 0 && batched_w_ok(qa, nsys) && qa <= wreg_max<R>() && fits(1) && (n + NT - 1) / NT <= 65535) {
+                update_wreg_run<R>(n, qa, segA, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC,
+                                  partials, tickets, state, fin, skip_broken, st);
+                return;
+            }
+            v = 0;
+        }
         if constexpr (sizeof(R) == 4) {
             static const int ept_of[8] = {8, 8, 16, 8, 2, 1, 4, 4};
             if (v < 0 || v > 7 || !fits(ept_of[v])) v = 0;
@@ -1842,7 +2235,8 @@ void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename 
         }
     };
     int v = 0;
-    if (qa + qb >= 8 && !profile_enabled()) v = tuned_variant(sizeof(R), 1, n, nsys, qa, sizeof(R) == 4 ? 8 : 6, st, run);
+    if (forced_variant(1) >= 0) v = forced_variant(1);
+    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(sizeof(R), 1, n, nsys, qa, VW + 1, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)

@@ -90,6 +90,8 @@ void profile_read(int kc, double *bytes, double *ms, long long *launches);
 void profile_reset();
 // Gram-Schmidt variant autotuning (on by default) and its report, one line per tuned shape.
 void tune_enable(bool on);
+// Pins the projection and update variants (-1 returns each to the tuner).
+void tune_force(int projection, int update);
 // Marks the calling thread as capturing a CUDA graph: launchers then use cached choices only.
 void set_capturing(bool on);
 std::string tune_report();

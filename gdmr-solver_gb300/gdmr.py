@@ -57,6 +57,7 @@ SIGNATURES = {
     "gdmrProfileRead": (I, [I, P, P, P]),
     "gdmrTune": (None, [I]),
     "gdmrTuneReport": (ctypes.c_char_p, []),
+    "gdmrTuneForce": (None, [I, I]),
     "gdmr_system_create": (I, [P, I, P, P, P, I, I, I, I, I]),
     "gdmr_system_destroy": (I, [P]),
     "gdmr_system_bytes": (LL, [P]),
@@ -119,6 +120,11 @@ def tune_report() -> str:
 
 def tune(on: bool) -> None:
     load().gdmrTune(1 if on else 0)
+
+
+def tune_force(projection: int = -1, update: int = -1) -> None:
+    """Pins the Gram-Schmidt variants (index as in tune_report; -1 hands back to the tuner)."""
+    load().gdmrTuneForce(int(projection), int(update))
 
 
 def profile_read() -> dict:

@@ -92,6 +92,11 @@ int gdmrProfileRead(int kernelClass, double *bytes, double *ms, long long *launc
  * The report lists one line per tuned shape with the time of every variant. */
 void gdmrTune(int on);
 const char *gdmrTuneReport(void);
+/* Pins the Gram-Schmidt variants by their index in the tuner report (-1: tuner).  Used to
+ * check every variant against the others; an index a launch cannot use falls back to 0.
+ * complex64 projection 0-9, update 0-8; complex128 projection 0-7, update 0-6.  The last
+ * index of each is the batched shared-deflation-basis variant (8 to 64 systems, k <= 32). */
+void gdmrTuneForce(int projectionVariant, int updateVariant);
 
 /* ---- context API: one resident operator, many right-hand sides -------------
  * A gdmr_system holds a CSR operator on the device (SELL-32, complex64 and
