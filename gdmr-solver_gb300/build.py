@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["gdmr_kernels.cu", "gdmr_engine.cu", "gdmr_api.cu", "gdmr_server.cu", "gdmr_io.cu"]
+SOURCES = ["gdmr_kernels.cu", "gdmr_tc.cu", "gdmr_engine.cu", "gdmr_api.cu", "gdmr_server.cu", "gdmr_io.cu"]
 HEADERS = ["gdmr_kernels.cuh", "gdmr_engine.h"]
 PUBLIC = [os.path.join(HERE, "..", "include", h) for h in ("gDMR.h", "gDMRC.h", "gdmr_ext.h")]
 MAJOR, MINOR = "1", "0.1"

@@ -2003,7 +2003,8 @@ std::string tune_report() {
 
 // Variant tables: (EPT, PU, VEC), or grp(EPT, SB) for the system-grouped kernels.
 //   complex64:  0 (8,2,1)  1 (8,2,2)  2 (16,2,2)  3 (8,4,2)  4 (2,2,1)  5 (1,4,1)  6 grp(4,4)  7 grp(4,2)
-//               projection only: 8 split-vector(4)
+//               projection only: 8 split-vector(4); 9 batched shared-W (CUDA cores);
+//               10 batched shared-W on the tensor cores (tcgen05, 3xTF32); update: 8 batched shared-W
 //   complex128: 0 (4,2,1)  1 (8,2,1)  2 (4,4,1)  3 (1,4,1)  4 (2,2,1)  5 grp(4,2)
 //               projection only: 6 split-vector(4)
 template <class R, int EPT, int PU, int VEC>
@@ -2119,6 +2120,25 @@ int mdot_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const typ
     const size_t cap = scratch_capacity(partials);
     auto fits = [&](int ept) { return (size_t)nsys * qmax * 2 * (((size_t)n + NT * ept - 1) / (NT * ept)) <= cap; };
     constexpr int VW = sizeof(R) == 4 ? 9 : 7;   // batched shared-W variant
+    if constexpr (sizeof(R) == 4) {
+        if (v == 10) {   // batched shared-W projection on the tensor cores
+            if (qa > 0 && wproj_tc_ok(n, qa, nsys, segA, w, strideW) &&
+                (size_t)qa * nsys * 2 * wproj_tc_grid(n) <= cap) {
+                launch_wproj_tc(n, qa, segA, w, strideW, act, nsys, (double *)partials, coef, strideC, st);
+                if (qb == 0) return 2;
+                int vown = 0;
+                {
+                    std::lock_guard<std::mutex> lk(g_tune_mu);
+                    for (auto &e : g_tuned)
+                        if (e.key == TuneKey{(int)sizeof(R), 0, n, bucket_of(nsys, 0)}) vown = e.variant;
+                }
+                if (vown >= VW) vown = 0;
+                return 2 + mdot_dispatch<R>(vown, n, nullptr, 0, segB, strideB, qb, w, strideW, act, nsys, partials,
+                                            qmax, tickets, coef + qa, strideC, state, skip_broken, st);
+            }
+            v = 0;
+        }
+    }
     if (v == VW) {
         if (qa > 0 && batched_w_ok(qa, nsys) && (size_t)qa * nsys * 2 * wproj_grid(n, wp_rt<R>()) <= cap) {
             wproj_run<R>(n, qa, segA, w, strideW, act, nsys, partials, coef, strideC, st);
@@ -2130,7 +2150,7 @@ int mdot_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const typ
                 for (auto &e : g_tuned)
                     if (e.key == TuneKey{(int)sizeof(R), 0, n, bucket_of(nsys, 0)}) vown = e.variant;
             }
-            if (vown == VW) vown = 0;
+            if (vown >= VW) vown = 0;
             return 2 + mdot_dispatch<R>(vown, n, nullptr, 0, segB, strideB, qb, w, strideW, act, nsys, partials, qmax,
                                         tickets, coef + qa, strideC, state, skip_broken, st);
         }
@@ -2179,7 +2199,7 @@ void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT
     };
     int v = 0;
     if (forced_variant(0) >= 0) v = forced_variant(0);
-    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(sizeof(R), 0, n, nsys, qa, sizeof(R) == 4 ? 10 : 8, st, run);
+    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(sizeof(R), 0, n, nsys, qa, sizeof(R) == 4 ? 11 : 8, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)

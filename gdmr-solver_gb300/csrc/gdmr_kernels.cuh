@@ -120,6 +120,18 @@ void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename 
                    int nsys, const double2 *coef, size_t strideC, double2 *partials, unsigned *tickets,
                    SysState *state, FinishArgs fin, bool skip_broken, cudaStream_t st);
 
+// Tensor-core split-K projection of a batch onto the shared deflation vectors (complex64;
+// gdmr_tc.cu): coef[act[s]*strideC + p] = <W_p, y_s> for p < kk, s < nsys, through per-CTA
+// partials in `part` (wproj_tc_grid(n) x kk x nsys x 2 doubles); returns the number of
+// kernels launched.  wproj_tc_ok says when it applies (kk <= 32, 8 <= nsys <= 64, even n and
+// stride, 16-byte aligned vectors).
+bool wproj_tc_ok(int n, int kk, int nsys, const void *W, const void *Y, size_t strideY);
+int wproj_tc_grid(int n);
+int launch_wproj_tc(int n, int kk, const float2 *W, const float2 *Y, size_t strideY, const int *act, int nsys,
+                    double *part, double2 *coef, size_t strideC, cudaStream_t st);
+// mbarrier waits of the tensor-core kernel that ran out of time (0 in a healthy process).
+unsigned wproj_tc_timeouts();
+
 // out1 (and out2 if non-null) = alpha_s * in; zeros when the system broke down.
 template <class R>
 void launch_scale(int n, const typename CT<R>::t *in, size_t strideI, typename CT<R>::t *out1, size_t strideO1,

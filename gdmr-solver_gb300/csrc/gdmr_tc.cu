@@ -1,0 +1,455 @@
+// Tensor-core (tcgen05) projection of a batch onto the shared deflation basis.
+//
+// In a batched restart cycle every system orthogonalises its Krylov vector y_s against the
+// same kk deflation vectors W (the deflator of the reference, gDMR.cu:1710-1787, applied to
+// many right-hand sides at once).  The kk x nsys coefficients W^H Y are a GEMM with a huge
+// K (= n) and tiny M, N, so this kernel runs it split-K on the 5th-generation tensor cores:
+//
+//   * complex -> real: with y, w viewed as interleaved real vectors of length 2n,
+//       Re <w, y> = (wr, wi) . (yr, yi)      Im <w, y> = (-wi, wr) . (yr, yi)
+//     so A has 2kk rows: w_p and its twin w'_p = (-wi, wr), and B has the nsys rows y_s;
+//   * FP32 accuracy from TF32 inputs (3xTF32 with the fourth product for free): every
+//     operand x is split into big = tf32(x) and small = x - big.  A is M = 128 rows:
+//     rows 0-31 big(w), 32-63 big(w'), 64-95 small(w), 96-127 small(w'), and B has 2 np
+//     rows: big(y) then small(y).  One MMA per K step (N = 2 np) forms all four products
+//     big/small x big/small; coef is the sum of the four blocks of D;
+//   * persistent CTAs (one per SM) walk K tiles of 32 complex elements in a warp-specialised
+//     pipeline synchronised by mbarriers only: warps 0-15 load the raw tiles three tiles ahead
+//     into registers (about 66 KB in flight per SM at 64 systems), split them into big/small
+//     TF32 parts and store them in the 128-byte-swizzled K-major layout (coalesced 256-byte
+//     row loads, conflict-free 16-byte stores) in one of three operand buffers, then arrive on
+//     its "full" mbarrier;
+//     warp 16 issues the MMAs and commits them to the buffer's "empty" mbarrier.  (Staging the
+//     raw tiles with 256-byte bulk copies instead measured slower: 88 copies per tile.)
+//   * tile i accumulates into TMEM region i mod 4 (4 x 128 columns), so no FP32 accumulation
+//     chain is longer than a quarter of the CTA's tiles; at the end the regions are read
+//     back (tcgen05.ld) and summed in double-float, the CTA's partials are written as doubles
+//     and k_wproj_tc_reduce sums them over CTAs in a fixed order (deterministic).
+//
+// Every wait on an mbarrier is bounded (about two seconds of clock); a timeout is counted
+// in g_tc_timeouts, the kernel skips its remaining work and still frees its TMEM.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <type_traits>
+#include <vector>
+
+#include "gdmr_kernels.cuh"
+
+namespace gdmr {
+namespace {
+
+constexpr int TC_PRODUCERS = 512;              // warps 0-15 load, split and store operand tiles
+constexpr int TC_MMA_WARP = TC_PRODUCERS / 32; // warp 16 issues the MMAs
+constexpr int TC_THREADS = TC_PRODUCERS + 32;
+constexpr int TC_KT = 32;                      // complex elements per K tile
+constexpr int TC_KCH = 2 * TC_KT / 4;          // 16-byte chunks per operand row per tile (2 swizzle atoms)
+constexpr int TC_ROW = 128;                    // bytes per operand row inside a 128-byte swizzle atom
+constexpr int TC_SBO = 1024;                   // 8-row swizzle atoms
+constexpr int TC_M = 128;
+constexpr int TC_NMAX = 64;
+constexpr int TC_KMAX = 32;
+constexpr int TC_NB = 3;                       // operand buffers
+constexpr int TC_AHEAD = 3;                    // tiles whose loads are in flight ahead of the one stored
+constexpr int TC_REGIONS = 4;                  // TMEM accumulators, 128 columns each, tiles round-robin
+constexpr int TC_REGION_COLS = 128;            // [A big(y) | A small(y)], 2 x np <= 128 columns
+constexpr int TC_TMEM_COLS = 512;
+constexpr int TC_ITEMS = (TC_KMAX + TC_NMAX) * TC_KCH / TC_PRODUCERS;   // chunks per producer per tile
+constexpr int TC_A_FLOATS = TC_M * 2 * TC_KT;
+constexpr long long TC_WAIT_CYCLES = 4000000000LL;                       // ~2 s at 2 GHz
+
+__device__ unsigned g_tc_timeouts = 0;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor, K-major with 128-byte swizzle: rows of 128 bytes (32 tf32),
+// 8-row atoms of 1024 bytes, the 16-byte chunk index of a row XOR-ed with (row & 7).
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;                          // leading byte offset: unused for swizzled K-major
+    d |= (uint64_t)((TC_SBO >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;                          // descriptor version of the sm_100 family
+    d |= (uint64_t)2 << 61;                          // SWIZZLE_128B
+    return d;
+}
+
+// kind::tf32 instruction descriptor: D f32, A and B tf32, both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_tf32(int m, int n) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+// Float offset of (row r, 16-byte chunk c of the tile's 256-byte row) in a 128-byte-swizzled
+// K-major operand of `rows` rows: atom column c / 8, chunk (c % 8) XOR (r & 7).
+__device__ __forceinline__ int sw_ofs(int r, int c, int rows) {
+    return ((c >> 3) * rows * TC_ROW + r * TC_ROW + (((c & 7) ^ (r & 7)) << 4)) >> 2;
+}
+
+__device__ __forceinline__ float tf32_big(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity, volatile int *abort) {
+    const long long t0 = clock64();
+    while (true) {
+        uint32_t ok;
+        // the thread may sleep in the instruction up to the hint (ns) until the phase completes
+        asm volatile("{\n.reg .pred P;\nmbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2, %3;\nselp.b32 %0, 1, 0, P;\n}\n"
+                     : "=r"(ok) : "r"(addr), "r"(parity), "r"(20000) : "memory");
+        if (ok) return true;
+        if ((abort && *abort) || clock64() - t0 > TC_WAIT_CYCLES) return false;
+    }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t addr) {
+    asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(addr) : "memory");
+}
+
+__device__ __forceinline__ void st4(float *p, float a, float b, float c, float d) {
+    *reinterpret_cast<float4 *>(p) = make_float4(a, b, c, d);
+}
+
+// Double-float accumulate: (hi, lo) += v with the rounding error of the add kept in lo.
+__device__ __forceinline__ void df_add(float &hi, float &lo, float v) {
+    const float s = hi + v;
+    const float bb = s - hi;
+    const float err = (hi - (s - bb)) + (v - bb);
+    hi = s;
+    lo += err;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t addr, uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(addr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+
+// Lane 0 waits on an mbarrier phase and the warp follows its verdict (warp-uniform).
+__device__ __forceinline__ bool warp_wait(uint32_t addr, uint32_t parity, volatile int *abort, int lane) {
+    int ok = 1;
+    if (lane == 0) {
+        ok = mbar_wait(addr, parity, abort);
+        if (!ok && !*abort) {
+            atomicAdd(&g_tc_timeouts, 1u);
+            *abort = 1;
+        }
+    }
+    return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_wproj_tc(int n, int kk, const float2 *__restrict__ W, const float2 *__restrict__ Y0, size_t strideY,
+               const int *__restrict__ act, int nsys, int np, double *__restrict__ part) {
+    extern __shared__ __align__(1024) unsigned char tc_sm[];
+    // operand buffer b: A (128 rows), then B = [big(y) rows; small(y) rows] (2 np rows); the
+    // swizzle atoms need 1024-byte alignment, so the buffers start at the next 1 KB boundary
+    float *ops = reinterpret_cast<float *>(tc_sm + ((1024u - (smem_u32(tc_sm) & 1023u)) & 1023u));
+    const int b_floats = np * 2 * TC_KT, buf_floats = TC_A_FLOATS + 2 * b_floats;
+    __shared__ __align__(8) uint64_t full[TC_NB], empty[TC_NB], done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_act[TC_NMAX];
+    __shared__ volatile int s_abort;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, G = gridDim.x;
+    const long ntiles = ((long)n + TC_KT - 1) / TC_KT;
+    const int my_tiles = (int)((ntiles - blockIdx.x + G - 1) / G);
+
+    // zero the operand rows that are never written: A rows of p >= kk (all four row sets),
+    // B rows of s >= nsys (big and small); 16 float4 per row (both swizzle atom columns)
+    {
+        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        const int arows = 32 - kk, brows = np - nsys;
+        const int per_buf = (4 * arows + 2 * brows) * TC_KCH;
+        for (int e = tid; e < TC_NB * per_buf; e += TC_THREADS) {
+            const int b = e / per_buf, le = e % per_buf, c = le % TC_KCH, rr = le / TC_KCH;
+            float *base = ops + (size_t)b * buf_floats;
+            int r, rows;
+            if (rr < 4 * arows) {
+                r = (rr / arows) * 32 + kk + rr % arows;
+                rows = TC_M;
+            } else {
+                const int q = rr - 4 * arows;
+                base += TC_A_FLOATS;
+                r = (q / brows) * np + nsys + q % brows;
+                rows = 2 * np;
+            }
+            *reinterpret_cast<float4 *>(base + sw_ofs(r, c, rows)) = z;
+        }
+    }
+    if (tid < nsys) s_act[tid] = act[tid];
+    if (tid == 0) {
+        s_abort = 0;
+        for (int b = 0; b < TC_NB; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&full[b])), "r"(TC_PRODUCERS / 32));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&empty[b])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&done)));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
+                     "n"(TC_TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t taddr = tmem_base;
+
+    if (warp < TC_MMA_WARP) {
+        // ---- producers.  Chunk items of a tile: the kk W rows, then the nsys Y rows, 16 chunks
+        // of 16 bytes each, chunk fastest: a warp loads two rows' 256-byte segments (coalesced)
+        // and the eight lanes of a 16-byte store phase fill one swizzled 128-byte row (distinct banks).
+        const int witems = kk * TC_KCH, items = witems + nsys * TC_KCH;
+        const float2 *gp[TC_ITEMS];
+        int so[TC_ITEMS], c2[TC_ITEMS], kind[TC_ITEMS];   // kind: 0 none, 1 W row, 2 Y row
+#pragma unroll
+        for (int u = 0; u < TC_ITEMS; ++u) {
+            const int e = tid + u * TC_PRODUCERS;
+            kind[u] = 0;
+            gp[u] = W;
+            so[u] = c2[u] = 0;
+            if (e < items) {
+                const bool isw = e < witems;
+                const int le = isw ? e : e - witems;
+                const int r = le / TC_KCH, c = le % TC_KCH;
+                c2[u] = 2 * c;
+                if (isw) {
+                    kind[u] = 1;
+                    so[u] = sw_ofs(r, c, TC_M);
+                    gp[u] = W + (size_t)r * n + 2 * c;
+                } else {
+                    kind[u] = 2;
+                    so[u] = TC_A_FLOATS + sw_ofs(r, c, 2 * np);
+                    gp[u] = Y0 + (size_t)s_act[r] * strideY + 2 * c;
+                }
+            }
+        }
+        auto load_tile = [&](long t, float4(&dst)[TC_ITEMS]) {
+#pragma unroll
+            for (int u = 0; u < TC_ITEMS; ++u) {
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (kind[u] && t * TC_KT + c2[u] < n) v = *reinterpret_cast<const float4 *>(gp[u] + t * TC_KT);
+                dst[u] = v;
+            }
+        };
+        auto store_tile = [&](float *buf0, const float4(&src)[TC_ITEMS]) {
+#pragma unroll
+            for (int u = 0; u < TC_ITEMS; ++u) {
+                if (!kind[u]) continue;
+                const float4 v = src[u];
+                const float b0 = tf32_big(v.x), b1 = tf32_big(v.y), b2 = tf32_big(v.z), b3 = tf32_big(v.w);
+                const float s0 = v.x - b0, s1 = v.y - b1, s2 = v.z - b2, s3 = v.w - b3;
+                float *a = buf0 + so[u];
+                if (kind[u] == 1) {   // rows r, 32+r, 64+r, 96+r: same swizzle, 32 rows apart
+                    st4(a, b0, b1, b2, b3);
+                    st4(a + 32 * TC_ROW / 4, -b1, b0, -b3, b2);
+                    st4(a + 64 * TC_ROW / 4, s0, s1, s2, s3);
+                    st4(a + 96 * TC_ROW / 4, -s1, s0, -s3, s2);
+                } else {              // big(y) row s and small(y) row np + s (np a multiple of 8)
+                    st4(a, b0, b1, b2, b3);
+                    st4(a + np * TC_ROW / 4, s0, s1, s2, s3);
+                }
+            }
+        };
+        // register ring of TC_AHEAD + 1 tiles; the loop is unrolled by four so every slot is a
+        // fixed set of registers (slot i % 4 is stored while slot (i + 3) % 4 is being loaded)
+        float4 R0[TC_ITEMS], R1[TC_ITEMS], R2[TC_ITEMS], R3[TC_ITEMS];
+        static_assert(TC_AHEAD == 3, "the ring below has four slots");
+        const long t0 = blockIdx.x;
+        if (my_tiles > 0) load_tile(t0, R0);
+        if (my_tiles > 1) load_tile(t0 + G, R1);
+        if (my_tiles > 2) load_tile(t0 + 2 * G, R2);
+        auto step = [&](auto S, int i) -> bool {
+            constexpr int sl = decltype(S)::value;
+            float4(&cur)[TC_ITEMS] = sl == 0 ? R0 : sl == 1 ? R1 : sl == 2 ? R2 : R3;
+            float4(&fut)[TC_ITEMS] = sl == 0 ? R3 : sl == 1 ? R0 : sl == 2 ? R1 : R2;
+            const int buf = i % TC_NB;
+            if (i + TC_AHEAD < my_tiles) load_tile(t0 + (long)(i + TC_AHEAD) * G, fut);
+            if (i >= TC_NB && !warp_wait(smem_u32(&empty[buf]), ((i / TC_NB) - 1) & 1, &s_abort, lane)) return false;
+            store_tile(ops + (size_t)buf * buf_floats, cur);
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&full[buf]));
+            return true;
+        };
+        for (int i = 0; i < my_tiles; i += 4) {
+            if (!step(std::integral_constant<int, 0>{}, i)) break;
+            if (i + 1 >= my_tiles || !step(std::integral_constant<int, 1>{}, i + 1)) break;
+            if (i + 2 >= my_tiles || !step(std::integral_constant<int, 2>{}, i + 2)) break;
+            if (i + 3 >= my_tiles || !step(std::integral_constant<int, 3>{}, i + 3)) break;
+        }
+    } else if (warp == TC_MMA_WARP) {
+        if (lane == 0) {
+            // ---- MMA issuer: one MMA per K step with N = 2 np, B = [big(y) rows; small(y) rows];
+            // tile i accumulates into TMEM region i % TC_REGIONS.  K step ks reads swizzle atom
+            // column ks / 4 at byte offset (ks % 4) * 32 inside the 128-byte rows; only the
+            // start-address field of the descriptors changes (no carry below 256 KB).
+            const uint32_t idesc = idesc_tf32(TC_M, 2 * np);
+            const uint64_t adesc0 = sdesc(smem_u32(ops)), bdesc0 = sdesc(smem_u32(ops) + TC_A_FLOATS * 4);
+            const uint64_t buf_step = (uint64_t)(buf_floats * 4) >> 4;   // start-address units per buffer
+            const uint64_t acol = (uint64_t)(TC_M * TC_ROW) >> 4, bcol = (uint64_t)(2 * np * TC_ROW) >> 4;
+            for (int i = 0; i < my_tiles; ++i) {
+                const int buf = i % TC_NB;
+                if (!mbar_wait(smem_u32(&full[buf]), (i / TC_NB) & 1, &s_abort)) {
+                    if (!s_abort) { atomicAdd(&g_tc_timeouts, 1u); s_abort = 1; }
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint64_t ad0 = adesc0 + buf * buf_step, bd0 = bdesc0 + buf * buf_step;
+                const uint32_t d = taddr + (uint32_t)((i % TC_REGIONS) * TC_REGION_COLS);
+                asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                             "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+                             "l"(ad0), "l"(bd0), "r"(idesc), "r"(i >= TC_REGIONS ? 1u : 0u));
+#pragma unroll
+                for (int ks = 1; ks < 2 * TC_KT / 8; ++ks) {
+                    const uint64_t koff = (uint64_t)((ks & 3) * 32) >> 4;
+                    const uint64_t ad = ad0 + (ks >> 2) * acol + koff, bd = bd0 + (ks >> 2) * bcol + koff;
+                    asm volatile("tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, 1;\n" ::"r"(d), "l"(ad),
+                                 "l"(bd), "r"(idesc));
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                 smem_u32(&empty[buf]))
+                             : "memory");
+            }
+            // completes when every MMA issued above has finished (also after an abort)
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             smem_u32(&done))
+                         : "memory");
+        }
+    }
+    __syncthreads();
+    if (!mbar_wait(smem_u32(&done), 0, nullptr) && tid == 0) {
+        atomicAdd(&g_tc_timeouts, 1u);
+        s_abort = 1;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    // ---- sum the regions (double-float), then big + small rows, through shared memory
+    float *acc_hi = ops, *acc_lo = ops + nsys * 2 * 32;   // [s][re|im][32]; operand buffers are free now
+    const int used = my_tiles < TC_REGIONS ? my_tiles : TC_REGIONS;
+    for (int phase = 0; phase < 2; ++phase) {
+        if (warp < 4 && (warp >> 1) == phase && !s_abort) {
+            const int m = warp * 32 + lane, p = m & 31, ri = (m >> 5) & 1;
+            for (int c0 = 0; c0 < np; c0 += 16) {
+                float hi[16], lo[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) hi[j] = lo[j] = 0.f;
+                for (int rg = 0; rg < used; ++rg)
+                    for (int half = 0; half < 2; ++half) {   // columns of big(y), then of small(y)
+                        uint32_t v[16];
+                        tmem_ld16(taddr + ((uint32_t)(warp * 32) << 16) +
+                                      (uint32_t)(rg * TC_REGION_COLS + half * np + c0),
+                                  v);
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) df_add(hi[j], lo[j], __uint_as_float(v[j]));
+                    }
+                if (p < kk) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int s = c0 + j;
+                        if (s >= nsys) break;
+                        const int o = (s * 2 + ri) * 32 + p;
+                        if (phase == 0) {
+                            acc_hi[o] = hi[j];
+                            acc_lo[o] = lo[j];
+                        } else {
+                            df_add(acc_hi[o], acc_lo[o], hi[j]);
+                            acc_lo[o] += lo[j];
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "n"(TC_TMEM_COLS));
+    // this CTA's partials, contiguous: part[blockIdx.x][p*nsys + s][re|im]
+    double *pc = part + (size_t)blockIdx.x * kk * nsys * 2;
+    for (int e = tid; e < kk * nsys * 2; e += TC_THREADS) {
+        const int o = e >> 1, p = o / nsys, s = o % nsys, ri = e & 1;
+        const int idx = (s * 2 + ri) * 32 + p;
+        pc[e] = s_abort ? 0.0 : (double)acc_hi[idx] + (double)acc_lo[idx];
+    }
+}
+
+// coef_s[p] = sum over the G CTAs of part[g][p*nsys + s], one thread per (p, s), fixed order.
+__global__ void __launch_bounds__(256) k_wproj_tc_reduce(int kk, int nsys, int G, const double *__restrict__ part,
+                                                         const int *__restrict__ act, double2 *__restrict__ coef0,
+                                                         size_t strideC) {
+    const int o = blockIdx.x * blockDim.x + threadIdx.x, O = kk * nsys;
+    if (o >= O) return;
+    double re = 0, im = 0;
+#pragma unroll 8
+    for (int g = 0; g < G; ++g) {
+        const double2 v = *reinterpret_cast<const double2 *>(part + ((size_t)g * O + o) * 2);
+        re += v.x;
+        im += v.y;
+    }
+    coef0[(size_t)act[o % nsys] * strideC + o / nsys] = make_double2(re, im);
+}
+
+std::mutex g_tc_mu;
+std::vector<int> g_tc_sms;       // per device
+std::vector<char> g_tc_smem_set;
+
+int device_sms(int dev) {
+    std::lock_guard<std::mutex> lk(g_tc_mu);
+    if ((int)g_tc_sms.size() <= dev) g_tc_sms.resize(dev + 1, 0), g_tc_smem_set.resize(dev + 1, 0);
+    if (!g_tc_sms[dev]) cudaDeviceGetAttribute(&g_tc_sms[dev], cudaDevAttrMultiProcessorCount, dev);
+    return g_tc_sms[dev];
+}
+
+size_t tc_smem_bytes(int np) { return sizeof(float) * (size_t)TC_NB * (TC_A_FLOATS + 2 * np * 2 * TC_KT) + 1024; }
+
+}  // namespace
+
+bool wproj_tc_ok(int n, int kk, int nsys, const void *W, const void *Y, size_t strideY) {
+    return kk > 0 && kk <= TC_KMAX && nsys >= 8 && nsys <= TC_NMAX && n % 2 == 0 && strideY % 2 == 0 &&
+           ((uintptr_t)W & 15) == 0 && ((uintptr_t)Y & 15) == 0;
+}
+
+int wproj_tc_grid(int n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const long ntiles = ((long)n + TC_KT - 1) / TC_KT;
+    const int sms = device_sms(dev);
+    return (int)(ntiles < sms ? ntiles : sms);
+}
+
+int launch_wproj_tc(int n, int kk, const float2 *W, const float2 *Y, size_t strideY, const int *act, int nsys,
+                    double *part, double2 *coef, size_t strideC, cudaStream_t st) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int G = wproj_tc_grid(n);
+    const int np = ((nsys + 15) / 16) * 16;
+    const size_t smem = tc_smem_bytes(np);
+    {
+        std::lock_guard<std::mutex> lk(g_tc_mu);
+        if (!g_tc_smem_set[dev]) {
+            cudaFuncSetAttribute(k_wproj_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tc_smem_bytes(TC_NMAX));
+            g_tc_smem_set[dev] = 1;
+        }
+    }
+    k_wproj_tc<<<G, TC_THREADS, smem, st>>>(n, kk, W, Y, strideY, act, nsys, np, part);
+    const int O = kk * nsys;
+    k_wproj_tc_reduce<<<(O + 255) / 256, 256, 0, st>>>(kk, nsys, G, part, act, coef, strideC);
+    return 2;
+}
+
+unsigned wproj_tc_timeouts() {
+    unsigned v = 0;
+    cudaMemcpyFromSymbol(&v, g_tc_timeouts, sizeof v);
+    return v;
+}
+
+}  // namespace gdmr

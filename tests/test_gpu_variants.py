@@ -7,8 +7,9 @@ problem (m=40, k=10, tol 1e-10) that shares one deflation basis, and the
 answers are checked against a sparse direct solve (relative 1e-8) and the
 true FP64 residual (<= 1.5e-10).  The last index of each list is the batched
 shared-basis pair (split-K projection of W for the whole batch, update with
-the W chunk in shared memory for 16 systems at a time), which only runs while
-8 or more systems are active.
+W in registers for 16 systems at a time), which only runs while 8 or more
+systems are active; complex64 projection variant 10 is the same shared-W
+projection on the tensor cores (tcgen05, TF32 operands split big + small).
 """
 import numpy as np
 import pytest
@@ -20,7 +21,7 @@ pytestmark = pytest.mark.gpu
 
 NRHS = 20
 PAIRS = {
-    "mixed": [(i, i) for i in range(9)] + [(9, 8)],
+    "mixed": [(i, i) for i in range(9)] + [(9, 8), (10, 0), (10, 8)],
     "fp64": [(i, i) for i in range(7)] + [(7, 6)],
 }
 
