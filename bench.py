@@ -12,9 +12,11 @@ residual and solution.  The working set (~27 GB) is far larger than L2, so no
 flush is needed between steps.
 
 Also reported: `e2e` (the same step with the right-hand sides and solutions
-in pinned host memory, copies inside the timed region), a timed sample of
-the plain-FP64 drop-in (reference algorithm in complex128, one right-hand
-side at a time with recycling), the roofline of the dominant kernel class
+in pinned host memory, copies inside the timed region), timed samples of
+the plain forms (reference algorithm, one right-hand side at a time with
+recycling) in native complex128 (the drop-in) and in fp64e (the same
+iteration in double-float arithmetic on the FP32 pipes) with the HBM
+fraction of their kernel classes, the roofline of the dominant kernel class
 from CUDA events recorded by the library on its own stream, the SM clocks
 during the timed region, and the host oracle as CPU baseline.
 
@@ -144,10 +146,23 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def build_workload(nrhs: int, rank: int):
-    A = problems.helmholtz(SHAPE, KAPPA, DAMPING)
-    B = np.stack([problems.gaussian_source_rhs(SHAPE, seed) for seed in problems.shard_seeds(nrhs, rank)])
+def build_workload(nrhs: int, rank: int, shape=SHAPE):
+    A = problems.helmholtz(shape, KAPPA, DAMPING)
+    B = np.stack([problems.gaussian_source_rhs(shape, seed) for seed in problems.shard_seeds(nrhs, rank)])
     return A, B
+
+
+def class_table(prof: dict, hbm_peak: float) -> dict:
+    """Per kernel class: algorithmic GB/s, fraction of the HBM peak, share of kernel time."""
+    tot = sum(v["ms"] for v in prof.values()) or 1.0
+    out = {}
+    for k, v in prof.items():
+        if not v["launches"]:
+            continue
+        gbs = v["bytes"] / (v["ms"] / 1e3) / 1e9 if v["ms"] > 0 else None
+        out[k] = {"GB/s": gbs, "frac": (gbs / hbm_peak) if gbs else None, "share": v["ms"] / tot,
+                  "launches": v["launches"]}
+    return out
 
 
 def cpu_baseline(A, b, cycles: int, plain_cycles_per_solve: float):
@@ -373,8 +388,13 @@ def main():
     ap.add_argument("--serve-pool", type=int, default=4)
     ap.add_argument("--solve-only", action="store_true",
                     help="only the timed batched solves (for profiler captures); prints a short line")
+    ap.add_argument("--grid", type=int, default=SHAPE[0],
+                    help="edge of the cubic grid (profiling captures of the batched kernels use a smaller one)")
+    ap.add_argument("--m", type=int, default=M, help="basis size m (profiling captures)")
     ap.add_argument("--force-variants", default=None, metavar="P,U",
                     help="pin the Gram-Schmidt projection and update variants (gdmrTuneForce)")
+    ap.add_argument("--plain", default=None, choices=["fp64", "fp64e"],
+                    help="only the plain-form sample in this precision (for profiler captures); short line")
     ap.add_argument("--profile-classes", action="store_true",
                     help="with --solve-only: record the library's per-class algorithmic bytes and CUDA-event "
                          "times over the timed steps (tuning off) and print them")
@@ -401,9 +421,17 @@ def main():
 
     if args.force_variants:
         gdmr.tune_force(*(int(v) for v in args.force_variants.split(",")))
-    A, B = build_workload(args.nrhs, rank)
+    shape = (args.grid,) * 3
+    A, B = build_workload(args.nrhs, rank, shape)
     nrhs, n = B.shape
-    sysm = gdmr.System(A, M, K, capacity=nrhs, precision="mixed", device=local)
+    m_basis = args.m
+    if args.plain:
+        # plain-form sample only: one right-hand side at a time, no batched engine
+        res = plain_form_only(args, A, B, m_basis, local, hbm_peak)
+        if rank == 0:
+            print(json.dumps(res), flush=True)
+        return
+    sysm = gdmr.System(A, m_basis, K, capacity=nrhs, precision="mixed", device=local)
     Bd = torch.from_numpy(B).to(f"cuda:{local}")
     Xd = torch.zeros_like(Bd)
     tols = [TOL] * nrhs
@@ -473,9 +501,7 @@ def main():
                 "traffic_basis": (f"ncu DRAM bytes = {ratio} x algorithmic bytes for this class "
                                   "(every launch of 3 cycles, 96^3, 8 RHS), times this run's mean "
                                   "algorithmic bytes per launch") if ratio is not None else None,
-                "share": d["ms"] / tot_ms,
-                "classes": {k: {"GB/s": (v["bytes"] / (v["ms"] / 1e3) / 1e9) if v["ms"] > 0 else None,
-                                "share": v["ms"] / tot_ms, "launches": v["launches"]} for k, v in prof.items()}}
+                "share": d["ms"] / tot_ms, "classes": class_table(prof, hbm_peak)}
 
     # e2e: host buffers (pinned), copies inside the timed region, through the C ABI
     Bh = torch.from_numpy(B).pin_memory()
@@ -492,51 +518,69 @@ def main():
            "h2d_bytes_per_step": int(2 * B.nbytes), "d2h_bytes_per_step": int(B.nbytes)}
     e2e_ok = all(s["status"] == 0 and s["true_rel_res"] <= TOL for s in st_e2e)
 
-    # plain FP64 drop-in: reference algorithm in complex128, one right-hand side at a time
-    sysp = gdmr.System(A, M, K, capacity=1, precision="fp64", device=local)
-    plain_cycles = []
-    plain_ok = True
-    torch.cuda.synchronize()
-    t = time.perf_counter()
-    for i in range(args.plain_sample):
-        x, st = sysp.solve(B[i], mode=0 if i == 0 else 1, tol=TOL, mat_rank=args.max_cycles)
-        plain_cycles.append(st["cycles"])
-        plain_ok &= st["status"] == 0 and st["true_rel_res"] <= 2 * TOL
-    plain_s = time.perf_counter() - t
-    plain = {"value": args.plain_sample / plain_s, "unit": "solves/s", "cycles": plain_cycles,
-             "latency_ms_each": plain_s / args.plain_sample * 1e3, "verified": bool(plain_ok),
-             "sample": f"{args.plain_sample} right-hand sides solved in sequence (recycled deflation space)"}
-    # kernel-class shares of the plain form: 10 more cycles with library-side CUDA events
-    gdmr.profile_reset()
-    gdmr.profile(True)
-    sysp.solve(B[0], mode=1, tol=TOL, mat_rank=9)
-    gdmr.profile(False)
-    pp = gdmr.profile_read()
-    pt = sum(v["ms"] for v in pp.values())
-    plain["classes"] = {k: {"GB/s": (v["bytes"] / (v["ms"] / 1e3) / 1e9) if v["ms"] > 0 else None,
-                            "share": v["ms"] / pt} for k, v in pp.items() if v["launches"]}
-    sysp.close()
+    # plain forms, one right-hand side at a time (reference algorithm): native complex128
+    # (the drop-in) and fp64e (the same iteration in double-float arithmetic on the FP32 pipes)
+    def plain_form(precision, max_cycles):
+        sysp = gdmr.System(A, m_basis, K, capacity=1, precision=precision, device=local)
+        cyc, ok = [], True
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for i in range(args.plain_sample):
+            x, st = sysp.solve(B[i], mode=0 if i == 0 else 1, tol=TOL, mat_rank=max_cycles)
+            cyc.append(st["cycles"])
+            ok &= st["status"] == 0 and st["true_rel_res"] <= 2 * TOL
+        el = time.perf_counter() - t
+        out = {"value": args.plain_sample / el, "unit": "solves/s", "cycles": cyc,
+               "latency_ms_each": el / args.plain_sample * 1e3, "verified": bool(ok),
+               "sample": f"{args.plain_sample} right-hand sides solved in sequence (recycled deflation space)"}
+        # kernel classes of the plain form: 10 more cycles with library-side CUDA events
+        gdmr.profile_reset()
+        gdmr.profile(True)
+        sysp.solve(B[0], mode=1, tol=TOL, mat_rank=9)
+        gdmr.profile(False)
+        out["classes"] = class_table(gdmr.profile_read(), hbm_peak)
+        sysp.close()
+        return out
+
+    plain = plain_form("fp64", args.max_cycles)
+    plain_e = plain_form("fp64e", args.max_cycles)
 
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64-inner/f64-refine", "data": "synthetic",
-        "config": {"workload": "helmholtz96_64rhs", "grid": list(SHAPE), "n": n, "nnz": A.nnz, "kappa": KAPPA,
-                   "damping": DAMPING, "nrhs_per_gpu": nrhs, "m": M, "k": K, "tol": TOL,
+        "config": {"workload": f"helmholtz{shape[0]}_{nrhs}rhs", "grid": list(shape), "n": n, "nnz": A.nnz,
+                   "kappa": KAPPA, "damping": DAMPING, "nrhs_per_gpu": nrhs, "m": m_basis, "k": K, "tol": TOL,
                    "form": "mixed batched (complex64 inner DMR, FP64 true residual each cycle)",
                    "l2": "working set ~27 GB >> 129 MB L2; no flush"},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
         "cycles": {"mean": float(np.mean(cycles)), "max": int(np.max(cycles))},
         "verified": bool(verified), "worst_true_rel_res": worst_res,
         "plain_fp64": plain, "mixed_over_plain": value / world / plain["value"],
+        "plain_fp64e": plain_e, "mixed_over_plain_fp64e": value / world / plain_e["value"],
         "e2e": e2e, "e2e_verified": bool(e2e_ok),
         "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline,
         "tuning": gdmr.tune_report().strip().splitlines(),
     }
     if rank == 0 and args.cpu_cycles > 0:
-        line["cpu_baseline"] = cpu_baseline(A, B[0], args.cpu_cycles, float(np.mean(plain_cycles)))
+        line["cpu_baseline"] = cpu_baseline(A, B[0], args.cpu_cycles, float(np.mean(plain["cycles"])))
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def plain_form_only(args, A, B, m_basis, device, hbm_peak):
+    """--plain: the plain-form sample of bench's main line, alone (profiling captures)."""
+    import gdmr
+    s = gdmr.System(A, m_basis, K, capacity=1, precision=args.plain, device=device)
+    cyc = []
+    t = time.perf_counter()
+    for i in range(args.plain_sample):
+        x, st = s.solve(B[i], mode=0 if i == 0 else 1, tol=TOL, mat_rank=args.max_cycles)
+        cyc.append(st["cycles"])
+    el = time.perf_counter() - t
+    s.close()
+    return {"mode": "plain", "precision": args.plain, "value": args.plain_sample / el, "unit": "solves/s",
+            "cycles": cyc, "tuning": gdmr.tune_report().strip().splitlines()}
 
 
 def _solve_host(sysm, Bh_np, Xh_np, max_cycles):

@@ -8,6 +8,7 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "gdmr_engine.h"
@@ -407,6 +408,18 @@ __global__ void k_promote(int n, const float2 *a, double2 *b) {
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
         b[i] = make_double2(a[i].x, a[i].y);
 }
+__global__ void k_to_dfc(int n, const double2 *a, dfc *b) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        dfc c;
+        c.x = dfr(a[i].x);
+        c.y = dfr(a[i].y);
+        b[i] = c;
+    }
+}
+__global__ void k_from_dfc(int n, const dfc *a, double2 *b) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        b[i] = make_double2((double)a[i].x, (double)a[i].y);
+}
 }  // namespace
 static void gdmr_demote_vec(int n, const double2 *a, float2 *b, cudaStream_t st) {
     k_demote<<<std::min((n + 255) / 256, 4096), 256, 0, st>>>(n, a, b);
@@ -414,12 +427,19 @@ static void gdmr_demote_vec(int n, const double2 *a, float2 *b, cudaStream_t st)
 static void gdmr_promote_vec(int n, const float2 *a, double2 *b, cudaStream_t st) {
     k_promote<<<std::min((n + 255) / 256, 4096), 256, 0, st>>>(n, a, b);
 }
+static void gdmr_to_dfc_vec(int n, const double2 *a, dfc *b, cudaStream_t st) {
+    k_to_dfc<<<std::min((n + 255) / 256, 4096), 256, 0, st>>>(n, a, b);
+}
+static void gdmr_from_dfc_vec(int n, const dfc *a, double2 *b, cudaStream_t st) {
+    k_from_dfc<<<std::min((n + 255) / 256, 4096), 256, 0, st>>>(n, a, b);
+}
 
 struct gdmr_system {
     int n = 0, m = 0, k = 0, cap = 0, precision = 0, device = 0;
     DeviceSell A;
     Engine<float> e32;
     Engine<double> e64;
+    Engine<dfr> edf;   // precision 2: FP64-class double-float on the FP32 pipes
     cudaStream_t st = nullptr;
     double2 *db = nullptr, *dx = nullptr;   // staging for host-buffer calls (cap vectors each)
     std::mutex mu;
@@ -429,6 +449,7 @@ namespace {
 template <class R> Engine<R> &eng_of(gdmr_system *s);
 template <> Engine<float> &eng_of<float>(gdmr_system *s) { return s->e32; }
 template <> Engine<double> &eng_of<double>(gdmr_system *s) { return s->e64; }
+template <> Engine<dfr> &eng_of<dfr>(gdmr_system *s) { return s->edf; }
 
 void to_stats(const SolveStats &s, gdmr_stats *o) {
     o->cycles = s.cycles;
@@ -510,21 +531,25 @@ int single_impl(gdmr_system *S, int mode, const double *b, double *x, double tol
         cudaMemcpyAsync(dx, x, vb, cudaMemcpyHostToDevice, S->st);
     }
     C *bR, *xR;
-    if (sizeof(R) == 8) {
+    if constexpr (std::is_same<R, double>::value) {
         bR = (C *)db;
         xR = (C *)dx;
     } else {
-        // complex64 working copies live in the staging area's second half
+        // complex64 / double-float working copies live in the staging area's second half
         bR = (C *)(db + (size_t)n);
         xR = (C *)(dx + (size_t)n);
-        gdmr_demote_vec(n, db, (float2 *)bR, S->st);
-        gdmr_demote_vec(n, dx, (float2 *)xR, S->st);
+        if constexpr (std::is_same<R, float>::value) {
+            gdmr_demote_vec(n, db, (float2 *)bR, S->st);
+            gdmr_demote_vec(n, dx, (float2 *)xR, S->st);
+        } else {
+            gdmr_to_dfc_vec(n, db, (dfc *)bR, S->st);
+            gdmr_to_dfc_vec(n, dx, (dfc *)xR, S->st);
+        }
     }
     SolveStats st;
     E.solve_reference(mode, bR, xR, tol, matRank, &st);
-    if (sizeof(R) == 4) {
-        gdmr_promote_vec(n, (const float2 *)xR, dx, S->st);
-    }
+    if constexpr (std::is_same<R, float>::value) gdmr_promote_vec(n, (const float2 *)xR, dx, S->st);
+    if constexpr (std::is_same<R, dfr>::value) gdmr_from_dfc_vec(n, (const dfc *)xR, dx, S->st);
     // true FP64 residual
     double rel = -1;
     if (E.refine_setup(S->A.view64()) == GDMR_OK) E.true_residual(1, db, dx, &rel);
@@ -543,20 +568,25 @@ extern "C" int gdmr_system_create(gdmr_system **out, int n, const int *rowPtr, c
                                   int basisDim, int deflatDim, int capacity, int precision, int device) {
     if (!out) return fail(GDMR_EINVAL, "gdmr_system_create", "null output pointer");
     *out = nullptr;
-    if (precision != 0 && precision != 1) return fail(GDMR_EINVAL, "gdmr_system_create", "precision must be 0 or 1");
+    if (precision < 0 || precision > 2) return fail(GDMR_EINVAL, "gdmr_system_create", "precision must be 0, 1 or 2");
     if (capacity < 1) return fail(GDMR_EINVAL, "gdmr_system_create", "capacity must be >= 1");
     if (cudaSetDevice(device) != cudaSuccess) return fail(GDMR_ECUDA, "gdmr_system_create", "cudaSetDevice");
     std::unique_ptr<gdmr_system> S(new gdmr_system());
     S->n = n; S->m = basisDim; S->k = deflatDim; S->cap = capacity; S->precision = precision; S->device = device;
     if (cudaStreamCreateWithFlags(&S->st, cudaStreamNonBlocking) != cudaSuccess)
         return fail(GDMR_ECUDA, "gdmr_system_create", "stream");
-    int rc = sell_from_csr(S->A, n, rowPtr, colIdx, vals_ri, precision == 1, true, S->st);
+    int rc = sell_from_csr(S->A, n, rowPtr, colIdx, vals_ri, precision == 1, true, S->st, precision == 2);
     if (rc != GDMR_OK) return rc;
     if (precision == 1) {
         rc = S->e32.init(n, basisDim, deflatDim, capacity, device);
         S->e32.op.kind = Operator<float>::SELL;
         S->e32.op.sell = S->A.view32();
         S->e32.stream = S->st;
+    } else if (precision == 2) {
+        rc = S->edf.init(n, basisDim, deflatDim, capacity, device);
+        S->edf.op.kind = Operator<dfr>::SELL;
+        S->edf.op.sell = S->A.viewdf();
+        S->edf.stream = S->st;
     } else {
         rc = S->e64.init(n, basisDim, deflatDim, capacity, device);
         S->e64.op.kind = Operator<double>::SELL;
@@ -578,6 +608,7 @@ extern "C" int gdmr_system_destroy(gdmr_system *S) {
     if (S->st) cudaStreamSynchronize(S->st);
     S->e32.release();
     S->e64.release();
+    S->edf.release();
     sell_free(S->A);
     if (S->db) cudaFree(S->db);
     if (S->dx) cudaFree(S->dx);
@@ -588,7 +619,7 @@ extern "C" int gdmr_system_destroy(gdmr_system *S) {
 
 extern "C" long long gdmr_system_bytes(const gdmr_system *S) {
     if (!S) return 0;
-    return (long long)(S->A.bytes() + S->e32.device_bytes() + S->e64.device_bytes() +
+    return (long long)(S->A.bytes() + S->e32.device_bytes() + S->e64.device_bytes() + S->edf.device_bytes() +
                        2 * sizeof(double2) * (size_t)S->n * std::max(S->cap, 2));
 }
 
@@ -597,12 +628,14 @@ extern "C" int gdmr_system_set_graphs(gdmr_system *S, int on) {
     std::lock_guard<std::mutex> lk(S->mu);
     S->e32.use_graphs = on != 0;
     S->e64.use_graphs = on != 0;
+    S->edf.use_graphs = on != 0;
     return GDMR_OK;
 }
 
 extern "C" int gdmr_system_svd_sweeps(const gdmr_system *S) {
     if (!S) return 0;
-    return S->precision == 1 ? S->e32.last_svd_sweeps() : S->e64.last_svd_sweeps();
+    return S->precision == 1 ? S->e32.last_svd_sweeps()
+                             : S->precision == 2 ? S->edf.last_svd_sweeps() : S->e64.last_svd_sweeps();
 }
 
 extern "C" int gdmr_solve(gdmr_system *S, int mode, const double *b, double *x, double tol, int matRank, int on_device,
@@ -610,8 +643,9 @@ extern "C" int gdmr_solve(gdmr_system *S, int mode, const double *b, double *x, 
     if (!S || !b || !x) return fail(GDMR_EINVAL, "gdmr_solve", "null argument");
     std::lock_guard<std::mutex> lk(S->mu);
     cudaSetDevice(S->device);
-    return S->precision == 1 ? single_impl<float>(S, mode, b, x, tol, matRank, on_device, stats)
-                             : single_impl<double>(S, mode, b, x, tol, matRank, on_device, stats);
+    if (S->precision == 1) return single_impl<float>(S, mode, b, x, tol, matRank, on_device, stats);
+    if (S->precision == 2) return single_impl<dfr>(S, mode, b, x, tol, matRank, on_device, stats);
+    return single_impl<double>(S, mode, b, x, tol, matRank, on_device, stats);
 }
 
 extern "C" int gdmr_solve_batch(gdmr_system *S, int nrhs, const double *b, double *x, const double *tol,
@@ -619,8 +653,9 @@ extern "C" int gdmr_solve_batch(gdmr_system *S, int nrhs, const double *b, doubl
     if (!S || !b || !x || nrhs < 1) return fail(GDMR_EINVAL, "gdmr_solve_batch", "null argument or nrhs < 1");
     std::lock_guard<std::mutex> lk(S->mu);
     cudaSetDevice(S->device);
-    return S->precision == 1 ? batch_impl<float>(S, nrhs, b, x, tol, maxCycles, on_device, stats)
-                             : batch_impl<double>(S, nrhs, b, x, tol, maxCycles, on_device, stats);
+    if (S->precision == 1) return batch_impl<float>(S, nrhs, b, x, tol, maxCycles, on_device, stats);
+    if (S->precision == 2) return batch_impl<dfr>(S, nrhs, b, x, tol, maxCycles, on_device, stats);
+    return batch_impl<double>(S, nrhs, b, x, tol, maxCycles, on_device, stats);
 }
 
 extern "C" int gdmr_true_residual(gdmr_system *S, int nrhs, const double *b, const double *x, int on_device,
@@ -641,7 +676,7 @@ extern "C" int gdmr_true_residual(gdmr_system *S, int nrhs, const double *b, con
         }
         return GDMR_OK;
     };
-    return S->precision == 1 ? run(S->e32) : run(S->e64);
+    return S->precision == 1 ? run(S->e32) : S->precision == 2 ? run(S->edf) : run(S->e64);
 }
 
 extern "C" int gdmr_export_deflation(gdmr_system *S, double *z) {
@@ -649,6 +684,15 @@ extern "C" int gdmr_export_deflation(gdmr_system *S, double *z) {
     std::lock_guard<std::mutex> lk(S->mu);
     cudaSetDevice(S->device);
     if (S->precision == 0) return S->e64.export_deflation((double2 *)z);
+    if (S->precision == 2) {
+        std::vector<dfc> tmp((size_t)S->k * S->n);
+        int rc = S->edf.export_deflation(tmp.data());
+        for (size_t i = 0; i < tmp.size(); ++i) {
+            z[2 * i] = (double)tmp[i].x;
+            z[2 * i + 1] = (double)tmp[i].y;
+        }
+        return rc;
+    }
     std::vector<float2> tmp((size_t)S->k * S->n);
     int rc = S->e32.export_deflation(tmp.data());
     for (size_t i = 0; i < tmp.size(); ++i) { z[2 * i] = tmp[i].x; z[2 * i + 1] = tmp[i].y; }
@@ -660,6 +704,14 @@ extern "C" int gdmr_import_deflation(gdmr_system *S, const double *z) {
     std::lock_guard<std::mutex> lk(S->mu);
     cudaSetDevice(S->device);
     if (S->precision == 0) return S->e64.import_deflation((const double2 *)z);
+    if (S->precision == 2) {
+        std::vector<dfc> tmp((size_t)S->k * S->n);
+        for (size_t i = 0; i < tmp.size(); ++i) {
+            tmp[i].x = dfr(z[2 * i]);
+            tmp[i].y = dfr(z[2 * i + 1]);
+        }
+        return S->edf.import_deflation(tmp.data());
+    }
     std::vector<float2> tmp((size_t)S->k * S->n);
     for (size_t i = 0; i < tmp.size(); ++i) tmp[i] = make_float2((float)z[2 * i], (float)z[2 * i + 1]);
     return S->e32.import_deflation(tmp.data());
@@ -686,6 +738,7 @@ extern "C" int gdmr_drop_deflation(gdmr_system *S) {
     std::lock_guard<std::mutex> lk(S->mu);
     S->e32.drop_deflation();
     S->e64.drop_deflation();
+    S->edf.drop_deflation();
     return GDMR_OK;
 }
 

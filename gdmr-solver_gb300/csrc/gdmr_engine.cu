@@ -79,11 +79,11 @@ template <class C> void sub(int n, const C *a, const C *b, C *out, cudaStream_t 
 // ----------------------------------------------------------------- SELL build
 size_t DeviceSell::bytes() const {
     return sizeof(int) * ((size_t)nslices + 1 + padded) + (vals32 ? sizeof(float2) * padded : 0) +
-           (vals64 ? sizeof(double2) * padded : 0);
+           (vals64 ? sizeof(double2) * padded : 0) + (valsdf ? sizeof(dfc) * padded : 0);
 }
 
 int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, const double *vals_ri, bool want32,
-                  bool want64, cudaStream_t st) {
+                  bool want64, cudaStream_t st, bool wantdf) {
     if (n <= 0 || !rowptr || !colidx || !vals_ri) {
         set_last_error(GDMR_EINVAL, "sell_from_csr: empty matrix or null arrays");
         return GDMR_EINVAL;
@@ -111,6 +111,7 @@ int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, 
     std::vector<int> cols(padded);
     std::vector<float2> v32(want32 ? padded : 0);
     std::vector<double2> v64(want64 ? padded : 0);
+    std::vector<dfc> vdf(wantdf ? padded : 0);
     for (int s = 0; s < ns; ++s) {
         const int w = (sp[s + 1] - sp[s]) / 32;
         for (int lane = 0; lane < 32; ++lane) {
@@ -132,6 +133,10 @@ int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, 
                 cols[e] = col;
                 if (want32) v32[e] = make_float2((float)re, (float)im);
                 if (want64) v64[e] = make_double2(re, im);
+                if (wantdf) {
+                    vdf[e].x = dfr(re);
+                    vdf[e].y = dfr(im);
+                }
             }
         }
     }
@@ -153,6 +158,10 @@ int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, 
         GDMR_CK(cudaMalloc(&d.vals64, sizeof(double2) * std::max<long>(padded, 1)));
         GDMR_CK(cudaMemcpyAsync(d.vals64, v64.data(), sizeof(double2) * padded, cudaMemcpyHostToDevice, st));
     }
+    if (wantdf) {
+        GDMR_CK(cudaMalloc(&d.valsdf, sizeof(dfc) * std::max<long>(padded, 1)));
+        GDMR_CK(cudaMemcpyAsync(d.valsdf, vdf.data(), sizeof(dfc) * padded, cudaMemcpyHostToDevice, st));
+    }
     GDMR_CK(cudaStreamSynchronize(st));
     sell_free(out);
     out = d;
@@ -164,6 +173,7 @@ void sell_free(DeviceSell &s) {
     if (s.cols) cudaFree(s.cols);
     if (s.vals32) cudaFree(s.vals32);
     if (s.vals64) cudaFree(s.vals64);
+    if (s.valsdf) cudaFree(s.valsdf);
     s = DeviceSell();
 }
 
@@ -759,5 +769,6 @@ template <class R> int Engine<R>::export_deflation(C *host) {
 
 template class Engine<float>;
 template class Engine<double>;
+template class Engine<dfr>;
 
 }  // namespace gdmr

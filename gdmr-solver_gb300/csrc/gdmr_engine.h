@@ -36,14 +36,16 @@ struct DeviceSell {
     int *cols = nullptr;
     float2 *vals32 = nullptr;
     double2 *vals64 = nullptr;
+    dfc *valsdf = nullptr;   // double-float values of the fp64e form
     int device = 0;
     SellMatrix view32() const { return SellMatrix{n, nslices, slice_ptr, cols, vals32, nnz}; }
     SellMatrix view64() const { return SellMatrix{n, nslices, slice_ptr, cols, vals64, nnz}; }
+    SellMatrix viewdf() const { return SellMatrix{n, nslices, slice_ptr, cols, valsdf, nnz}; }
     size_t bytes() const;
 };
 // Builds the SELL-32 form of a CSR matrix (values interleaved re,im doubles).
 int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, const double *vals_ri, bool want32,
-                  bool want64, cudaStream_t st);
+                  bool want64, cudaStream_t st, bool wantdf = false);
 void sell_free(DeviceSell &s);
 
 // Operator seen by an engine of precision R.

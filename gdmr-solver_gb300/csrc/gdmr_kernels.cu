@@ -1,6 +1,8 @@
 // Device kernels of the GB300 DMR restart cycle.  See gdmr_kernels.cuh.
 #include "gdmr_kernels.cuh"
 
+#include <type_traits>
+
 #include <math.h>
 
 #include <algorithm>
@@ -21,29 +23,66 @@ constexpr int QMAX = 168;          // max coefficients per projection (basisDim 
 template <class C> __device__ __forceinline__ C from_d(double2 a);
 template <> __device__ __forceinline__ float2 from_d<float2>(double2 a) { return make_float2((float)a.x, (float)a.y); }
 template <> __device__ __forceinline__ double2 from_d<double2>(double2 a) { return a; }
+template <> __device__ __forceinline__ dfc from_d<dfc>(double2 a) {
+    dfc c;
+    c.x = dfr(a.x);
+    c.y = dfr(a.y);
+    return c;
+}
+__device__ __forceinline__ double2 to_d(float2 a) { return make_double2(a.x, a.y); }
+__device__ __forceinline__ double2 to_d(double2 a) { return a; }
+__device__ __forceinline__ double2 to_d(dfc a) { return make_double2((double)a.x, (double)a.y); }
 
 template <class C> __device__ __forceinline__ C czero() { C z; z.x = 0; z.y = 0; return z; }
 
+// a * b + c in the working real type
+__device__ __forceinline__ float rfma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double rfma(double a, double b, double c) { return ::fma(a, b, c); }
+// Double-float a * b + c for accumulation chains: the exact two-product and two-sum, with no
+// renormalisation; hi + lo stays exact and lo grows by about an ulp of hi per step, so a
+// chain ends with canon() before its value is stored or squared.
+__device__ __forceinline__ dfr rfma(dfr a, dfr b, dfr c) {
+    const float p = a.hi * b.hi;
+    const float pe = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p)));
+    const float s = p + c.hi, bb = s - p;
+    return dfr(s, ((p - (s - bb)) + (c.hi - bb)) + (pe + c.lo));
+}
+// canonical form of an accumulated value (identity for the native types)
+__device__ __forceinline__ float2 canon(float2 a) { return a; }
+__device__ __forceinline__ double2 canon(double2 a) { return a; }
+__device__ __forceinline__ dfc canon(dfc a) {
+    a.x = df_renorm(a.x.hi, a.x.lo);
+    a.y = df_renorm(a.y.hi, a.y.lo);
+    return a;
+}
+// |a|^2 in double
+__device__ __forceinline__ double abs2_d(float2 a) { return (double)a.x * a.x + (double)a.y * a.y; }
+__device__ __forceinline__ double abs2_d(double2 a) { return a.x * a.x + a.y * a.y; }
+__device__ __forceinline__ double abs2_d(dfc a) {
+    const double x = (double)a.x, y = (double)a.y;
+    return x * x + y * y;
+}
+
 // acc += a * b
 template <class C> __device__ __forceinline__ void cfma(C &acc, C a, C b) {
-    acc.x = fma(a.x, b.x, acc.x);
-    acc.x = fma(-a.y, b.y, acc.x);
-    acc.y = fma(a.x, b.y, acc.y);
-    acc.y = fma(a.y, b.x, acc.y);
+    acc.x = rfma(a.x, b.x, acc.x);
+    acc.x = rfma(-a.y, b.y, acc.x);
+    acc.y = rfma(a.x, b.y, acc.y);
+    acc.y = rfma(a.y, b.x, acc.y);
 }
 // acc -= a * b
 template <class C> __device__ __forceinline__ void cfms(C &acc, C a, C b) {
-    acc.x = fma(-a.x, b.x, acc.x);
-    acc.x = fma(a.y, b.y, acc.x);
-    acc.y = fma(-a.x, b.y, acc.y);
-    acc.y = fma(-a.y, b.x, acc.y);
+    acc.x = rfma(-a.x, b.x, acc.x);
+    acc.x = rfma(a.y, b.y, acc.x);
+    acc.y = rfma(-a.x, b.y, acc.y);
+    acc.y = rfma(-a.y, b.x, acc.y);
 }
 // acc += conj(a) * b
 template <class C> __device__ __forceinline__ void cdotacc(C &acc, C a, C b) {
-    acc.x = fma(a.x, b.x, acc.x);
-    acc.x = fma(a.y, b.y, acc.x);
-    acc.y = fma(a.x, b.y, acc.y);
-    acc.y = fma(-a.y, b.x, acc.y);
+    acc.x = rfma(a.x, b.x, acc.x);
+    acc.x = rfma(a.y, b.y, acc.x);
+    acc.y = rfma(a.x, b.y, acc.y);
+    acc.y = rfma(-a.y, b.x, acc.y);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -54,6 +93,12 @@ __device__ __forceinline__ double warp_sum(double v) {
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ dfr warp_sum(dfr v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v = v + dfr(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o));
     return v;
 }
 
@@ -184,27 +229,32 @@ template <class C, int VEC> struct Pack {
 };
 template <class C, int VEC> __device__ __forceinline__ Pack<C, VEC> load_pack(const C *p, long i0, int n) {
     Pack<C, VEC> r;
-    if (VEC == 2 && sizeof(C) == 8 && i0 + 1 < n) {
+    if constexpr (VEC == 2 && std::is_same<C, float2>::value) {
+      if (i0 + 1 < n) {
         const float4 f = *reinterpret_cast<const float4 *>(p + i0);
         r.v[0].x = f.x; r.v[0].y = f.y;
         r.v[VEC - 1].x = f.z; r.v[VEC - 1].y = f.w;
-    } else {
-#pragma unroll
-        for (int j = 0; j < VEC; ++j) r.v[j] = (i0 + j < n) ? p[i0 + j] : czero<C>();
+        return r;
+      }
     }
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) r.v[j] = (i0 + j < n) ? p[i0 + j] : czero<C>();
     return r;
 }
 template <class C, int VEC> __device__ __forceinline__ void store_pack(C *p, long i0, int n, const Pack<C, VEC> &r) {
-    if (VEC == 2 && sizeof(C) == 8 && i0 + 1 < n) {
-        *reinterpret_cast<float4 *>(p + i0) = make_float4(r.v[0].x, r.v[0].y, r.v[VEC - 1].x, r.v[VEC - 1].y);
-    } else {
-#pragma unroll
-        for (int j = 0; j < VEC; ++j)
-            if (i0 + j < n) p[i0 + j] = r.v[j];
+    if constexpr (VEC == 2 && std::is_same<C, float2>::value) {
+        if (i0 + 1 < n) {
+            *reinterpret_cast<float4 *>(p + i0) = make_float4(r.v[0].x, r.v[0].y, r.v[VEC - 1].x, r.v[VEC - 1].y);
+            return;
+        }
     }
+#pragma unroll
+    for (int j = 0; j < VEC; ++j)
+        if (i0 + j < n) p[i0 + j] = r.v[j];
 }
 template <class C> __host__ __device__ constexpr int min_blocks(int ept, int pu) {
-    return ept * pu * (int)sizeof(C) > 128 ? 2 : 3;
+    // double-float values carry two FP32 words per component plus two-sum temporaries
+    return std::is_same<C, dfc>::value || ept * pu * (int)sizeof(C) > 128 ? 2 : 3;
 }
 
 // coef_s[p] = <B_p, w_s> for B = [segA (qa vectors) | segB_s (qb vectors)].
@@ -320,10 +370,18 @@ __global__ void __launch_bounds__(NT, min_blocks<typename CT<R>::t>(EPT, PU))
                     for (int j = 0; j < VEC; ++j) cfms(acc[e].v[j], c, vv[u][e].v[j]);
             }
         }
+        if constexpr (std::is_same<C, dfc>::value) {   // keep double-float chains short
+#pragma unroll
+            for (int e = 0; e < NP; ++e)
+#pragma unroll
+                for (int j = 0; j < VEC; ++j) acc[e].v[j] = canon(acc[e].v[j]);
+        }
     }
     C ln = czero<C>(), lc = czero<C>();
 #pragma unroll
     for (int e = 0; e < NP; ++e) {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) acc[e].v[j] = canon(acc[e].v[j]);
         store_pack<C, VEC>(out, c0 + ((long)e * NT + tid) * VEC, n, acc[e]);
 #pragma unroll
         for (int j = 0; j < VEC; ++j) {
@@ -903,6 +961,7 @@ __global__ void __launch_bounds__(NT, 2)
 #pragma unroll
             for (int e = 0; e < EPT; ++e) {
                 const long i = c0 + tid + (long)e * NT;
+                acc[g][e] = canon(acc[g][e]);
                 if (i < n) out[i] = acc[g][e];
                 cdotacc(ln, acc[g][e], acc[g][e]);
                 cdotacc(lc, acc[g][e], org[g][e]);
@@ -1014,6 +1073,8 @@ __global__ void __launch_bounds__(NT) k_combine(int n, int kk, int m, const type
                 cfms(ra_[e], tc, wp[i]);
                 cfma(xa[e], yc, zp[i]);
             }
+            ra_[e] = canon(ra_[e]);
+            xa[e] = canon(xa[e]);
         }
     }
 #pragma unroll 4
@@ -1028,12 +1089,16 @@ __global__ void __launch_bounds__(NT) k_combine(int n, int kk, int m, const type
                 cfms(ra_[e], tc, vv);
                 cfma(xa[e], yc, vv);
             }
+            ra_[e] = canon(ra_[e]);
+            xa[e] = canon(xa[e]);
         }
     }
     C ln = czero<C>();
 #pragma unroll
     for (int e = 0; e < EPT; ++e) {
         long i = c0 + tid + (long)e * NT;
+        ra_[e] = canon(ra_[e]);
+        xa[e] = canon(xa[e]);
         if (i < n) {
             r[i] = ra_[e];
             x[i] = xa[e];
@@ -1084,12 +1149,17 @@ __global__ void __launch_bounds__(NT) k_zupdate(int n, int kk, int m, int k, int
         for (int p = 0; p < m; ++p) {
             const C b = p < kk ? Z[(size_t)p * n + i] : V[(size_t)(p - kk) * n + i];
 #pragma unroll
-            for (int t = 0; t < KB; ++t) cfma(acc[t], cs[p * KB + t], b);
+            for (int t = 0; t < KB; ++t) {
+                cfma(acc[t], cs[p * KB + t], b);
+                if constexpr (std::is_same<C, dfc>::value)
+                    if ((p & 3) == 3) acc[t] = canon(acc[t]);
+            }
         }
 #pragma unroll
         for (int t = 0; t < KB; ++t) {
+            acc[t] = canon(acc[t]);
             if (t < nt) Znew[(size_t)(t0 + t) * n + i] = acc[t];
-            nrm[t] += (double)acc[t].x * acc[t].x + (double)acc[t].y * acc[t].y;
+            nrm[t] += abs2_d(acc[t]);
         }
     }
     block_sum<KB>(nrm, red);
@@ -1561,8 +1631,8 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
                         cfma(a1, v[e], xb[c[e]]);
                     }
                 }
-                y0[(size_t)s0 * strideY + row] = a0;
-                y0[(size_t)s1 * strideY + row] = a1;
+                y0[(size_t)s0 * strideY + row] = canon(a0);
+                y0[(size_t)s1 * strideY + row] = canon(a1);
             }
             if (g < ng) {
                 const int s0 = act[g0 + g];
@@ -1571,7 +1641,7 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
 #pragma unroll
                 for (int e = 0; e < WMAX; ++e)
                     if (e < width) cfma(a0, v[e], xa[c[e]]);
-                y0[(size_t)s0 * strideY + row] = a0;
+                y0[(size_t)s0 * strideY + row] = canon(a0);
             }
         } else {
             for (int g = 0; g < ng; ++g) {
@@ -1582,7 +1652,7 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
                     const int idx = beg + e * 32 + lane;
                     cfma(acc, vals[idx], x[cols[idx]]);
                 }
-                y0[(size_t)s * strideY + row] = acc;
+                y0[(size_t)s * strideY + row] = canon(acc);
             }
         }
     }
@@ -1643,10 +1713,13 @@ __global__ void __launch_bounds__(NT) k_dense_gemv(int n, const typename CT<R>::
         __syncthreads();
         if (row < n) {
             const int lim = min(NT, n - j0);
-            for (int j = 0; j < lim; ++j) cfma(acc, A[(size_t)(j0 + j) * n + row], xs[j]);
+            for (int j = 0; j < lim; ++j) {
+                cfma(acc, A[(size_t)(j0 + j) * n + row], xs[j]);
+                acc = canon(acc);
+            }
         }
     }
-    if (row < n) y[row] = acc;
+    if (row < n) y[row] = canon(acc);
 }
 
 template <class R>
@@ -1700,7 +1773,7 @@ __global__ void __launch_bounds__(NT) k_norm(int n, const typename CT<R>::t *__r
     double n2 = 0;
     for (long i = (long)blockIdx.y * NT + tid; i < n; i += (long)G * NT) {
         C a = v[i];
-        n2 += (double)a.x * a.x + (double)a.y * a.y;
+        n2 += abs2_d(a);
     }
     double vv[1] = {n2};
     block_sum<1>(vv, red);
@@ -1988,7 +2061,8 @@ std::string tune_report() {
     std::string out;
     for (auto &e : g_tuned) {
         char buf[256];
-        int len = snprintf(buf, sizeof buf, "%s %s n=%d %s %s: variant %d [", e.key.prec == 4 ? "c64" : "c128",
+        int len = snprintf(buf, sizeof buf, "%s %s n=%d %s %s: variant %d [",
+                           e.key.prec == 4 ? "c64" : e.key.prec == 9 ? "df64" : "c128",
                            e.key.kernel == 0 ? "projection" : "update", e.key.n,
                            (e.key.bucket & 1) ? "batch" : "single", (e.key.bucket & 2) ? "shared" : "own", e.variant);
         out.append(buf, len);
@@ -2130,7 +2204,7 @@ int mdot_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const typ
                 {
                     std::lock_guard<std::mutex> lk(g_tune_mu);
                     for (auto &e : g_tuned)
-                        if (e.key == TuneKey{(int)sizeof(R), 0, n, bucket_of(nsys, 0)}) vown = e.variant;
+                        if (e.key == TuneKey{prec_key<R>(), 0, n, bucket_of(nsys, 0)}) vown = e.variant;
                 }
                 if (vown >= VW) vown = 0;
                 return 2 + mdot_dispatch<R>(vown, n, nullptr, 0, segB, strideB, qb, w, strideW, act, nsys, partials,
@@ -2139,8 +2213,9 @@ int mdot_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const typ
             v = 0;
         }
     }
-    if (v == VW) {
-        if (qa > 0 && batched_w_ok(qa, nsys) && (size_t)qa * nsys * 2 * wproj_grid(n, wp_rt<R>()) <= cap) {
+    if (v == VW && !std::is_same<R, dfr>::value) {
+        if constexpr (!std::is_same<R, dfr>::value) {
+          if (qa > 0 && batched_w_ok(qa, nsys) && (size_t)qa * nsys * 2 * wproj_grid(n, wp_rt<R>()) <= cap) {
             wproj_run<R>(n, qa, segA, w, strideW, act, nsys, partials, coef, strideC, st);
             if (qb == 0) return 2;
             // own-basis part: the tuned choice for a batch without a shared segment
@@ -2148,11 +2223,12 @@ int mdot_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const typ
             {
                 std::lock_guard<std::mutex> lk(g_tune_mu);
                 for (auto &e : g_tuned)
-                    if (e.key == TuneKey{(int)sizeof(R), 0, n, bucket_of(nsys, 0)}) vown = e.variant;
+                    if (e.key == TuneKey{prec_key<R>(), 0, n, bucket_of(nsys, 0)}) vown = e.variant;
             }
             if (vown >= VW) vown = 0;
             return 2 + mdot_dispatch<R>(vown, n, nullptr, 0, segB, strideB, qb, w, strideW, act, nsys, partials, qmax,
                                         tickets, coef + qa, strideC, state, skip_broken, st);
+          }
         }
         v = 0;
     }
@@ -2199,11 +2275,11 @@ void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT
     };
     int v = 0;
     if (forced_variant(0) >= 0) v = forced_variant(0);
-    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(sizeof(R), 0, n, nsys, qa, sizeof(R) == 4 ? 11 : 8, st, run);
+    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(prec_key<R>(), 0, n, nsys, qa, sizeof(R) == 4 ? 11 : 8, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)
-            if (e.key == TuneKey{(int)sizeof(R), 0, n, bucket_of(nsys, qa)}) v = e.variant;
+            if (e.key == TuneKey{prec_key<R>(), 0, n, bucket_of(nsys, qa)}) v = e.variant;
     }
     run(v);
     L_.add(launched);
@@ -2220,13 +2296,16 @@ void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename 
     auto fits = [&](int ept) { return (size_t)nsys * 3 * (((size_t)n + NT * ept - 1) / (NT * ept)) <= cap; };
     constexpr int VW = sizeof(R) == 4 ? 8 : 6;   // batched shared-W variant
     auto run = [&](int v) {
-        if (v == VW) {
+        if (v == VW && std::is_same<R, dfr>::value) v = 0;   // no double-float form of the batched pair
+        if constexpr (!std::is_same<R, dfr>::value) {
+          if (v == VW) {
             if (qa > 0 && batched_w_ok(qa, nsys) && qa <= wreg_max<R>() && fits(1) && (n + NT - 1) / NT <= 65535) {
                 update_wreg_run<R>(n, qa, segA, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC,
                                   partials, tickets, state, fin, skip_broken, st);
                 return;
             }
             v = 0;
+          }
         }
         if constexpr (sizeof(R) == 4) {
             static const int ept_of[8] = {8, 8, 16, 8, 2, 1, 4, 4};
@@ -2256,11 +2335,11 @@ void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename 
     };
     int v = 0;
     if (forced_variant(1) >= 0) v = forced_variant(1);
-    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(sizeof(R), 1, n, nsys, qa, VW + 1, st, run);
+    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(prec_key<R>(), 1, n, nsys, qa, VW + 1, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)
-            if (e.key == TuneKey{(int)sizeof(R), 1, n, bucket_of(nsys, qa)}) v = e.variant;
+            if (e.key == TuneKey{prec_key<R>(), 1, n, bucket_of(nsys, qa)}) v = e.variant;
     }
     run(v);
 }
@@ -2432,5 +2511,6 @@ void launch_broadcast_hdef(int m, int kk, const double2 *Hd, double2 *H, size_t 
 
 GDMR_INST(float)
 GDMR_INST(double)
+GDMR_INST(dfr)
 
 }  // namespace gdmr

@@ -19,12 +19,65 @@
 
 namespace gdmr {
 
+// Double-float real: value = hi + lo with |lo| <= ulp(hi)/2, about 48 significant bits.  It
+// carries the FP64-class "fp64e" precision form through the streaming kernels on the FP32
+// pipes (GB300 retires FP32 at 69 TFLOP/s but FP64 at 1 TFLOP/s, too slow for HBM-rate
+// complex dot products).  Products use the exact FMA two-product, sums the two-sum of Knuth
+// (Dekker 1971; Knuth, TAOCP vol. 2, 4.2.2), each result renormalised by fast-two-sum.
+struct dfr {
+    float hi, lo;
+    dfr() = default;
+    __host__ __device__ constexpr dfr(float h, float l) : hi(h), lo(l) {}
+    __host__ __device__ dfr(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
+    __host__ __device__ dfr(int v) : hi((float)v), lo(0.f) {}
+    __host__ __device__ explicit operator double() const { return (double)hi + (double)lo; }
+};
+// complex double-float: (re.hi, re.lo, im.hi, im.lo), one 16-byte load
+struct __align__(16) dfc {
+    dfr x, y;
+};
+
 template <class R> struct CT;
 template <> struct CT<float> { using t = float2; };
 template <> struct CT<double> { using t = double2; };
+template <> struct CT<dfr> { using t = dfc; };
+
+// Tuner / report key of a precision: 4 complex64, 8 complex128, 9 double-float complex.
+template <class R> constexpr int prec_key() { return sizeof(R) == 4 ? 4 : 8; }
+template <> constexpr int prec_key<dfr>() { return 9; }
 
 __host__ __device__ inline float2 mk(float a, float b) { return make_float2(a, b); }
 __host__ __device__ inline double2 mk(double a, double b) { return make_double2(a, b); }
+
+#ifdef __CUDACC__
+__device__ __forceinline__ dfr df_renorm(float s, float e) {   // fast-two-sum, |s| >= |e|
+    const float h = s + e;
+    return dfr(h, e - (h - s));
+}
+__device__ __forceinline__ dfr operator+(dfr a, dfr b) {
+    const float s = a.hi + b.hi, bb = s - a.hi;
+    const float e = ((a.hi - (s - bb)) + (b.hi - bb)) + (a.lo + b.lo);
+    return df_renorm(s, e);
+}
+__device__ __forceinline__ dfr operator-(dfr a) { return dfr(-a.hi, -a.lo); }
+__device__ __forceinline__ dfr operator-(dfr a, dfr b) { return a + (-b); }
+__device__ __forceinline__ dfr operator*(dfr a, dfr b) {
+    const float p = a.hi * b.hi;
+    const float e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p)));
+    return df_renorm(p, e);
+}
+// a * b + c
+__device__ __forceinline__ dfr fma(dfr a, dfr b, dfr c) {
+    const float p = a.hi * b.hi;
+    const float pe = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p)));
+    const float s = p + c.hi, bb = s - p;
+    const float e = ((p - (s - bb)) + (c.hi - bb)) + (pe + c.lo);
+    return df_renorm(s, e);
+}
+__device__ __forceinline__ dfr &operator+=(dfr &a, dfr b) { return a = a + b; }
+__device__ __forceinline__ dfr &operator-=(dfr &a, dfr b) { return a = a - b; }
+__device__ __forceinline__ dfr &operator*=(dfr &a, dfr b) { return a = a * b; }
+#endif
 
 // Per-system state that the device kernels update and the host reads once per cycle.
 struct SysState {

@@ -285,8 +285,9 @@ class LinearSystem:
 class System:
     """Context API (gdmr_ext.h): a resident CSR operator plus a solver engine of
     `capacity` systems sharing one recycled deflation space.
-    precision: 'fp64' (plain complex128 iteration) or 'mixed' (complex64 inner
-    iteration inside FP64 refinement)."""
+    precision: 'fp64' (plain complex128 iteration), 'fp64e' (the same iteration in
+    double-float arithmetic on the FP32 pipes, about 48 significant bits) or 'mixed'
+    (complex64 inner iteration inside FP64 refinement)."""
 
     def __init__(self, A, basis: int, deflat: int, capacity: int = 1, precision: str = "fp64", device: int = 0):
         self.L = load()
@@ -294,7 +295,7 @@ class System:
         indptr, indices = _csr_arrays(A)
         vals = np.ascontiguousarray(A.data, dtype=np.complex128)
         h = ctypes.c_void_p()
-        prec = {"fp64": 0, "mixed": 1}[precision]
+        prec = {"fp64": 0, "mixed": 1, "fp64e": 2}[precision]
         _check(self.L.gdmr_system_create(ctypes.byref(h), A.n, _ptr(indptr), _ptr(indices), _ptr(vals),
                                          basis, deflat, capacity, prec, device), "gdmr_system_create")
         self._h = h

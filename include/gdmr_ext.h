@@ -102,8 +102,12 @@ void gdmrTuneForce(int projectionVariant, int updateVariant);
  * A gdmr_system holds a CSR operator on the device (SELL-32, complex64 and
  * complex128 values), a solver engine of `capacity` systems and one recycled
  * deflation space shared by every right-hand side solved through it.
- * precision 0: plain FP64 inner iteration; 1: complex64 inner iteration.
- * Both forms check convergence on the true FP64 residual b - A x. */
+ * precision 0: plain FP64 inner iteration; 1: complex64 inner iteration;
+ * 2: "fp64e", the FP64 iteration carried in double-float arithmetic (pairs of
+ * FP32 values, about 48 significant bits) on the FP32 pipes, for GPUs whose
+ * native FP64 rate caps the streaming kernels well below memory bandwidth;
+ * the least squares, SVD and Hessenberg stay native FP64.  The batched form
+ * checks convergence on the true FP64 residual b - A x. */
 typedef struct gdmr_system gdmr_system;
 int gdmr_system_create(gdmr_system **out, int n, const int *rowPtr, const int *colIdx, const double *vals_ri,
                        int basisDim, int deflatDim, int capacity, int precision, int device);
@@ -117,7 +121,7 @@ int gdmr_system_svd_sweeps(const gdmr_system *sys);
 int gdmr_system_set_graphs(gdmr_system *sys, int on);
 
 /* Reference-semantics solve of one right-hand side (solverDMR's algorithm,
- * complex128 or complex64 per the system's precision), then the true FP64
+ * complex128, complex64 or double-float per the system's precision), then the true FP64
  * residual.  b, x: interleaved complex128, on the host (on_device = 0) or the
  * device (on_device = 1); x is the initial guess on entry. */
 int gdmr_solve(gdmr_system *sys, int mode, const double *b, double *x, double tol, int matRank, int on_device,

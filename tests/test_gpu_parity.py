@@ -8,7 +8,10 @@ sparse direct solve.  Tolerances:
     (+-2 later in a recycled sequence, whose deflation space is sensitive to
     rounding), x within 1e-8 relative of the oracle, true FP64 residual
     <= 2x the requested tolerance;
-  * complex64 (reference precision) forms: cycles +-2, x within 1e-3.
+  * complex64 (reference precision) forms: cycles +-2, x within 1e-3;
+  * fp64e (the complex128 iteration in double-float arithmetic on the FP32
+    pipes, about 48 significant bits): as complex128, with one cycle of slack
+    on a first solve and 1e-11 on the breakdown fixture.
 """
 import os
 
@@ -44,27 +47,35 @@ def c1():
     return A, rhs, cfg, [lu.solve(b) for b in rhs]
 
 
-def test_fp64_first_solve_matches_oracle(c1, oracle_mod):
+# fp64e: the same iteration in double-float arithmetic (about 48 significant bits), so the
+# first solve may end one cycle apart from the oracle; everything else holds as for fp64.
+CYCLE_SLACK = {"fp64": 0, "fp64e": 1}
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64e"])
+def test_fp64_first_solve_matches_oracle(c1, oracle_mod, precision):
     A, rhs, cfg, direct = c1
-    sys_ = gdmr.System(A, cfg["m"], cfg["k"], capacity=1, precision="fp64")
+    sys_ = gdmr.System(A, cfg["m"], cfg["k"], capacity=1, precision=precision)
     x, st = sys_.solve(rhs[0], mode=0, tol=1e-10, mat_rank=2000)
     o = oracle_mod.Oracle(A, cfg["m"], cfg["k"], fuse_deflation=True)
     r = o.solve(rhs[0], mode=0, tol=1e-10, mat_rank=2000)
     assert st["status"] == 0
-    assert st["cycles"] == r["cycles"]
-    assert st["its"] == r["its"] == r["cycles"] - 1
+    assert abs(st["cycles"] - r["cycles"]) <= CYCLE_SLACK[precision]
+    assert st["its"] == st["cycles"] - 1 and r["its"] == r["cycles"] - 1
     # the last cycle works near 1e-10, where the recursive residual carries rounding of
     # order eps / (relative residual): two correct implementations differ by ~1% there
-    assert abs(st["rel_res"] - r["ret"]) <= 5e-2 * r["ret"]
+    if st["cycles"] == r["cycles"]:
+        assert abs(st["rel_res"] - r["ret"]) <= 5e-2 * r["ret"]
     assert _rel(x, r["x"]) < 1e-8
     assert st["true_rel_res"] <= 2e-10
     assert _true(A, rhs[0], x) <= 2e-10
     assert _rel(x, direct[0]) < 1e-8
 
 
-def test_fp64_recycled_sequence(c1, oracle_mod):
+@pytest.mark.parametrize("precision", ["fp64", "fp64e"])
+def test_fp64_recycled_sequence(c1, oracle_mod, precision):
     A, rhs, cfg, direct = c1
-    sys_ = gdmr.System(A, cfg["m"], cfg["k"], capacity=1, precision="fp64")
+    sys_ = gdmr.System(A, cfg["m"], cfg["k"], capacity=1, precision=precision)
     o = oracle_mod.Oracle(A, cfg["m"], cfg["k"], fuse_deflation=True)
     total_gpu = total_orc = 0
     for i, b in enumerate(rhs):
@@ -79,9 +90,10 @@ def test_fp64_recycled_sequence(c1, oracle_mod):
     assert abs(total_gpu - total_orc) <= 2 * len(rhs)
 
 
-def test_fp64_golden_sequence():
+@pytest.mark.parametrize("precision", ["fp64", "fp64e"])
+def test_fp64_golden_sequence(precision):
     A, d = _golden("helmholtz10.npz")
-    sys_ = gdmr.System(A, int(d["m"]), int(d["k"]), capacity=1, precision="fp64")
+    sys_ = gdmr.System(A, int(d["m"]), int(d["k"]), capacity=1, precision=precision)
     for i in range(int(d["nrhs"])):
         x, st = sys_.solve(d[f"b{i}"], mode=0 if i == 0 else 1, tol=float(d["tol"]), mat_rank=int(d["mat_rank"]))
         assert st["status"] == 0
@@ -90,12 +102,13 @@ def test_fp64_golden_sequence():
         assert _rel(x, d[f"direct{i}"]) < 1e-8
 
 
-def test_fp64_breakdown_identity_tail():
+@pytest.mark.parametrize("precision,xtol", [("fp64", 1e-12), ("fp64e", 1e-11)])
+def test_fp64_breakdown_identity_tail(precision, xtol):
     A, d = _golden("breakdown30.npz")
-    sys_ = gdmr.System(A, int(d["m"]), int(d["k"]), capacity=1, precision="fp64")
+    sys_ = gdmr.System(A, int(d["m"]), int(d["k"]), capacity=1, precision=precision)
     x, st = sys_.solve(d["b0"], mode=0, tol=float(d["tol"]), mat_rank=int(d["mat_rank"]))
     assert st["status"] == 0 and st["cycles"] == 1 and st["breakdowns"] == 1
-    assert _rel(x, d["direct0"]) < 1e-12
+    assert _rel(x, d["direct0"]) < xtol
 
 
 def test_legacy_complex64_plugin_csr(c1, oracle_mod):
@@ -181,7 +194,7 @@ def test_legacy_complex128_plugin(c1, oracle_mod):
         ls.close()
 
 
-@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("precision", ["mixed", "fp64", "fp64e"])
 def test_refined_batch_reaches_fp64_tolerance(c1, precision):
     A, rhs, cfg, direct = c1
     sys_ = gdmr.System(A, cfg["m"], cfg["k"], capacity=8, precision=precision)
@@ -251,7 +264,7 @@ def test_cycle_cap_reports_no_convergence(c1):
     assert "converge" in gdmr.last_error()
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp64e"])
 def test_graph_replay_matches_eager_launches(c1, precision):
     """Restart cycles replayed as CUDA graphs give the same iterates as eager launches."""
     A, rhs, cfg, direct = c1
@@ -259,7 +272,7 @@ def test_graph_replay_matches_eager_launches(c1, precision):
     for graphs in (False, True):
         s = gdmr.System(A, cfg["m"], cfg["k"], capacity=2, precision=precision)
         s.set_graphs(graphs)
-        if precision == "fp64":
+        if precision in ("fp64", "fp64e"):
             x0, st0 = s.solve(rhs[0], mode=0, tol=1e-10, mat_rank=2000)
             x1, st1 = s.solve(rhs[1], mode=1, tol=1e-10, mat_rank=2000)
             res.append((np.stack([x0, x1]), [st0["cycles"], st1["cycles"]]))
