@@ -381,20 +381,35 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
 }
 
-// coef_s[p] = sum over the G CTAs of part[g][p*nsys + s], one thread per (p, s), fixed order.
+// coef_s[p] = sum over the G CTAs of part[g][p*nsys + s]: 32 outputs per CTA, lane = output
+// (coalesced reads across outputs), warp w sums the CTAs g = w, w + 8, ... in order, and the
+// eight warp sums are added in warp order (deterministic).
 __global__ void __launch_bounds__(256) k_wproj_tc_reduce(int kk, int nsys, int G, const double *__restrict__ part,
                                                          const int *__restrict__ act, double2 *__restrict__ coef0,
                                                          size_t strideC) {
-    const int o = blockIdx.x * blockDim.x + threadIdx.x, O = kk * nsys;
-    if (o >= O) return;
+    __shared__ double2 red[8][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int o = blockIdx.x * 32 + lane, O = kk * nsys;
     double re = 0, im = 0;
-#pragma unroll 8
-    for (int g = 0; g < G; ++g) {
-        const double2 v = *reinterpret_cast<const double2 *>(part + ((size_t)g * O + o) * 2);
-        re += v.x;
-        im += v.y;
+    if (o < O) {
+#pragma unroll 4
+        for (int g = warp; g < G; g += 8) {
+            const double2 v = *reinterpret_cast<const double2 *>(part + ((size_t)g * O + o) * 2);
+            re += v.x;
+            im += v.y;
+        }
     }
-    coef0[(size_t)act[o % nsys] * strideC + o / nsys] = make_double2(re, im);
+    red[warp][lane] = make_double2(re, im);
+    __syncthreads();
+    if (warp == 0 && o < O) {
+        double2 t = red[0][lane];
+#pragma unroll
+        for (int w = 1; w < 8; ++w) {
+            t.x += red[w][lane].x;
+            t.y += red[w][lane].y;
+        }
+        coef0[(size_t)act[o % nsys] * strideC + o / nsys] = t;
+    }
 }
 
 std::mutex g_tc_mu;
@@ -442,7 +457,7 @@ int launch_wproj_tc(int n, int kk, const float2 *W, const float2 *Y, size_t stri
     }
     k_wproj_tc<<<G, TC_THREADS, smem, st>>>(n, kk, W, Y, strideY, act, nsys, np, part);
     const int O = kk * nsys;
-    k_wproj_tc_reduce<<<(O + 255) / 256, 256, 0, st>>>(kk, nsys, G, part, act, coef, strideC);
+    k_wproj_tc_reduce<<<(O + 31) / 32, 256, 0, st>>>(kk, nsys, G, part, act, coef, strideC);
     return 2;
 }
 
