@@ -2078,7 +2078,8 @@ std::string tune_report() {
 // Variant tables: (EPT, PU, VEC), or grp(EPT, SB) for the system-grouped kernels.
 //   complex64:  0 (8,2,1)  1 (8,2,2)  2 (16,2,2)  3 (8,4,2)  4 (2,2,1)  5 (1,4,1)  6 grp(4,4)  7 grp(4,2)
 //               projection only: 8 split-vector(4); 9 batched shared-W (CUDA cores);
-//               10 batched shared-W on the tensor cores (tcgen05, 3xTF32); update: 8 batched shared-W
+//               10 batched shared-W on the tensor cores (tcgen05, 3xTF32);
+//               update only: 8 batched shared-W (CUDA cores), 9 shared part on the tensor cores
 //   complex128: 0 (4,2,1)  1 (8,2,1)  2 (4,4,1)  3 (1,4,1)  4 (2,2,1)  5 grp(4,2)
 //               projection only: 6 split-vector(4)
 template <class R, int EPT, int PU, int VEC>
@@ -2285,63 +2286,99 @@ void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT
     L_.add(launched);
 }
 
+// The update variants; returns the number of kernels launched.
+template <class R>
+int update_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB,
+                    size_t strideB, int qb, const typename CT<R>::t *w, size_t strideW, typename CT<R>::t *out,
+                    size_t strideO, const int *act, int nsys, const double2 *coef, size_t strideC, double2 *partials,
+                    unsigned *tickets, SysState *state, FinishArgs fin, bool skip_broken, cudaStream_t st) {
+    const size_t cap = scratch_capacity(partials);
+    auto fits = [&](int ept) { return (size_t)nsys * 3 * (((size_t)n + NT * ept - 1) / (NT * ept)) <= cap; };
+    constexpr int VW = sizeof(R) == 4 ? 8 : 6;   // batched shared-W variant
+    if constexpr (sizeof(R) == 4) {
+        // 9: the shared part W c on the tensor cores into the free slot segB_s[qb] (the next
+        // Krylov vector's), then the per-system update with that slot as one more basis vector
+        // of coefficient 1 (written by the apply kernel at coef_s[qa + qb])
+        if (v == 9) {
+            if (qa > 0 && qb > 0 && segB && wapply_tc_ok(n, qa, nsys) && fits(8)) {
+                launch_wapply_tc(n, qa, segA, const_cast<double2 *>(coef), strideC, act, nsys,
+                                 const_cast<typename CT<R>::t *>(segB) + (size_t)qb * n, strideB, qa + qb, st);
+                int vown = 0;
+                {
+                    std::lock_guard<std::mutex> lk(g_tune_mu);
+                    for (auto &e : g_tuned)
+                        if (e.key == TuneKey{prec_key<R>(), 1, n, bucket_of(nsys, 0)}) vown = e.variant;
+                }
+                if (vown >= VW) vown = 0;
+                return 1 + update_dispatch<R>(vown, n, nullptr, 0, segB, strideB, qb + 1, w, strideW, out, strideO,
+                                              act, nsys, coef + qa, strideC, partials, tickets, state, fin,
+                                              skip_broken, st);
+            }
+            v = 0;
+        }
+    }
+    if (v == VW && std::is_same<R, dfr>::value) v = 0;   // no double-float form of the batched pair
+    if constexpr (!std::is_same<R, dfr>::value) {
+        if (v == VW) {
+            if (qa > 0 && batched_w_ok(qa, nsys) && qa <= wreg_max<R>() && fits(1) && (n + NT - 1) / NT <= 65535) {
+                update_wreg_run<R>(n, qa, segA, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC,
+                                   partials, tickets, state, fin, skip_broken, st);
+                return 1;
+            }
+            v = 0;
+        }
+    }
+    if constexpr (sizeof(R) == 4) {
+        static const int ept_of[8] = {8, 8, 16, 8, 2, 1, 4, 4};
+        if (v < 0 || v > 7 || !fits(ept_of[v])) v = 0;
+    } else {
+        static const int ept_of[6] = {4, 8, 4, 1, 2, 4};
+        if (v < 0 || v > 5 || !fits(ept_of[v])) v = 0;
+    }
+    if constexpr (sizeof(R) == 4) {
+        const bool v2 = vec2_ok(n, strideB, strideW) && strideO % 2 == 0;
+        if (v == 1 && v2) update_v<R, 8, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+        else if (v == 2 && v2) update_v<R, 16, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+        else if (v == 3 && v2) update_v<R, 8, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+        else if (v == 4) update_v<R, 2, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+        else if (v == 5) update_v<R, 1, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+        else if (v == 6) update_g<R, 4, 4>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+        else if (v == 7) update_g<R, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+        else update_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+    } else {
+        if (v == 1) update_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+        else if (v == 2) update_v<R, 4, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+        else if (v == 3) update_v<R, 1, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+        else if (v == 4) update_v<R, 2, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+        else if (v == 5) update_g<R, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+        else update_v<R, 4, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
+    }
+    return 1;
+}
+
 template <class R>
 void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
                    const typename CT<R>::t *w, size_t strideW, typename CT<R>::t *out, size_t strideO, const int *act,
                    int nsys, const double2 *coef, size_t strideC, double2 *partials, unsigned *tickets,
                    SysState *state, FinishArgs fin, bool skip_broken, cudaStream_t st) {
     if (nsys <= 0) return;
-    Launch L_(KC_UPDATE, (double)sizeof(typename CT<R>::t) * n * ((double)qa + (double)nsys * (qb + 2)), st, 1);
-    const size_t cap = scratch_capacity(partials);
-    auto fits = [&](int ept) { return (size_t)nsys * 3 * (((size_t)n + NT * ept - 1) / (NT * ept)) <= cap; };
-    constexpr int VW = sizeof(R) == 4 ? 8 : 6;   // batched shared-W variant
+    Launch L_(KC_UPDATE, (double)sizeof(typename CT<R>::t) * n * ((double)qa + (double)nsys * (qb + 2)), st, 0);
+    int launched = 0;
     auto run = [&](int v) {
-        if (v == VW && std::is_same<R, dfr>::value) v = 0;   // no double-float form of the batched pair
-        if constexpr (!std::is_same<R, dfr>::value) {
-          if (v == VW) {
-            if (qa > 0 && batched_w_ok(qa, nsys) && qa <= wreg_max<R>() && fits(1) && (n + NT - 1) / NT <= 65535) {
-                update_wreg_run<R>(n, qa, segA, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC,
-                                  partials, tickets, state, fin, skip_broken, st);
-                return;
-            }
-            v = 0;
-          }
-        }
-        if constexpr (sizeof(R) == 4) {
-            static const int ept_of[8] = {8, 8, 16, 8, 2, 1, 4, 4};
-            if (v < 0 || v > 7 || !fits(ept_of[v])) v = 0;
-        } else {
-            static const int ept_of[6] = {4, 8, 4, 1, 2, 4};
-            if (v < 0 || v > 5 || !fits(ept_of[v])) v = 0;
-        }
-        if constexpr (sizeof(R) == 4) {
-            const bool v2 = vec2_ok(n, strideB, strideW) && strideO % 2 == 0;
-            if (v == 1 && v2) update_v<R, 8, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
-            else if (v == 2 && v2) update_v<R, 16, 2, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
-            else if (v == 3 && v2) update_v<R, 8, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
-            else if (v == 4) update_v<R, 2, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
-            else if (v == 5) update_v<R, 1, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
-            else if (v == 6) update_g<R, 4, 4>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
-            else if (v == 7) update_g<R, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
-            else update_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
-        } else {
-            if (v == 1) update_v<R, 8, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
-            else if (v == 2) update_v<R, 4, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
-            else if (v == 3) update_v<R, 1, 4, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
-            else if (v == 4) update_v<R, 2, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
-            else if (v == 5) update_g<R, 4, 2>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
-            else update_v<R, 4, 2, 1>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC, partials, tickets, state, fin, skip_broken, st);
-        }
+        launched = update_dispatch<R>(v, n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef,
+                                      strideC, partials, tickets, state, fin, skip_broken, st);
     };
     int v = 0;
     if (forced_variant(1) >= 0) v = forced_variant(1);
-    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(prec_key<R>(), 1, n, nsys, qa, VW + 1, st, run);
+    else if (representative(nsys, qa, qb) && !profile_enabled())
+        v = tuned_variant(prec_key<R>(), 1, n, nsys, qa, sizeof(R) == 4 ? 10 : 7, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)
             if (e.key == TuneKey{prec_key<R>(), 1, n, bucket_of(nsys, qa)}) v = e.variant;
     }
     run(v);
+    L_.add(launched);
 }
 
 template <class R>

@@ -182,7 +182,14 @@ bool wproj_tc_ok(int n, int kk, int nsys, const void *W, const void *Y, size_t s
 int wproj_tc_grid(int n);
 int launch_wproj_tc(int n, int kk, const float2 *W, const float2 *Y, size_t strideY, const int *act, int nsys,
                     double *part, double2 *coef, size_t strideC, cudaStream_t st);
-// mbarrier waits of the tensor-core kernel that ran out of time (0 in a healthy process).
+// Tensor-core apply of the shared deflation vectors for a batch (complex64; gdmr_tc.cu):
+// P[act[s]*strideP + i] = sum_p coef[act[s]*strideC + p] W_p[i] for p < kk, and
+// coef[act[s]*strideC + unit_idx] = 1, so that a per-system update with P as one more basis
+// vector subtracts W c_s.  wapply_tc_ok: kk <= 32, 8 <= nsys <= 64.
+bool wapply_tc_ok(int n, int kk, int nsys);
+int launch_wapply_tc(int n, int kk, const float2 *W, double2 *coef, size_t strideC, const int *act, int nsys,
+                     float2 *P, size_t strideP, int unit_idx, cudaStream_t st);
+// mbarrier waits of the tensor-core kernels that ran out of time (0 in a healthy process).
 unsigned wproj_tc_timeouts();
 
 // out1 (and out2 if non-null) = alpha_s * in; zeros when the system broke down.

@@ -412,6 +412,207 @@ __global__ void __launch_bounds__(256) k_wproj_tc_reduce(int kk, int nsys, int G
     }
 }
 
+// ================================================================ batched shared-basis apply
+// P_s = W c_s for every active system s (c_s = coef_s[0:kk], the projection onto the shared
+// deflation vectors), written into the caller's slot for s (the next Krylov vector's slot),
+// so that the update out_s = y_s - P_s - V_s c_s^V runs as a per-system update with P_s as one
+// more basis vector of coefficient 1 (written here at coef_s[unit_idx]).
+//
+// Real GEMM on the tensor cores (kind::tf32), one 128-element tile of W per step:
+//   A (M = 128 rows = elements, K = 2kk reals (wr_p, wi_p)), split big/small into two operands;
+//   B (N = 4 NSp rows, K = 2kk): rows [big | small] x system x (re, im output) with
+//     re row: (cr_p, -ci_p), im row: (ci_p, cr_p), so D[i][(s,re)] = Re(w_i c_s), D[i][(s,im)] = Im;
+//   per K step: A_big x B (N = 4 NSp) and A_small x B_big (N = 2 NSp) into one TMEM tile, and
+//   P = D[:, big block] + D[:, small block].
+// Warp roles: warps 0-3 epilogue (TMEM lanes 0-127 -> P stores), warps 4-11 producers (W tile
+// -> split, swizzled A operands), warp 12 issues the MMAs.  A and the TMEM tile are
+// double-buffered; mbarriers only.
+constexpr int WA_EPI = 4, WA_PROD = 8;
+constexpr int WA_MMA_WARP = WA_EPI + WA_PROD;
+constexpr int WA_THREADS = (WA_MMA_WARP + 1) * 32;
+constexpr int WA_TILE = 128;                      // elements per tile (MMA M)
+constexpr int WA_AOP = WA_TILE * 2 * TC_ROW;      // bytes of one A operand (2 swizzle atom columns)
+constexpr int WA_ITEMS = TC_KMAX * WA_TILE / (WA_PROD * 32);   // W values per producer per tile
+
+__device__ __forceinline__ int swz(int r, int kf, int rows) {   // float offset of (row, K float)
+    return ((kf >> 5) * rows * TC_ROW + r * TC_ROW + ((((kf >> 2) & 7) ^ (r & 7)) << 4) + ((kf & 3) << 2)) >> 2;
+}
+
+__global__ void __launch_bounds__(WA_THREADS, 1)
+    k_wapply_tc(int n, int kk, const float2 *__restrict__ W, double2 *__restrict__ coef0, size_t strideC,
+                const int *__restrict__ act, int nsys, int nsp, float2 *__restrict__ P0, size_t strideP,
+                int unit_idx) {
+    extern __shared__ __align__(1024) unsigned char wa_sm[];
+    unsigned char *base = wa_sm + ((1024u - (smem_u32(wa_sm) & 1023u)) & 1023u);
+    float *A = reinterpret_cast<float *>(base);                       // [buf][big|small] operands
+    float *B = reinterpret_cast<float *>(base + 4 * WA_AOP);          // 4 nsp rows x 2 atom columns
+    const int brows = 4 * nsp;
+    __shared__ __align__(8) uint64_t full[2], mdone[2], tempty[2], done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_act[TC_NMAX];
+    __shared__ volatile int s_abort;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, G = gridDim.x;
+    const long ntiles = ((long)n + WA_TILE - 1) / WA_TILE;
+    const int my_tiles = (int)((ntiles - blockIdx.x + G - 1) / G);
+
+    // zero both A buffers (padded K stays zero) and B, then fill B from the coefficients
+    for (int e = tid; e < (4 * WA_AOP + brows * 2 * TC_ROW) / 16; e += WA_THREADS)
+        reinterpret_cast<float4 *>(base)[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (tid < nsys) s_act[tid] = act[tid];
+    if (tid == 0) {
+        s_abort = 0;
+        for (int b = 0; b < 2; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&full[b])), "r"(WA_PROD));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mdone[b])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&tempty[b])), "r"(WA_EPI));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&done)));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
+                     "n"(TC_TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    __syncthreads();
+    for (int e = tid; e < nsys * kk; e += WA_THREADS) {
+        const int sl = e / kk, p = e % kk;
+        const double2 c = coef0[(size_t)s_act[sl] * strideC + p];
+        const float cr = (float)c.x, ci = (float)c.y;
+        const float vals[2][2] = {{cr, -ci}, {ci, cr}};   // [output re|im][K 2p, 2p+1]
+#pragma unroll
+        for (int o = 0; o < 2; ++o)
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const float v = vals[o][q], big = tf32_big(v);
+                B[swz(2 * sl + o, 2 * p + q, brows)] = big;
+                B[swz(2 * nsp + 2 * sl + o, 2 * p + q, brows)] = v - big;
+            }
+    }
+    if (blockIdx.x == 0 && tid < nsys) coef0[(size_t)s_act[tid] * strideC + unit_idx] = make_double2(1.0, 0.0);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t taddr = tmem_base;
+
+    if (warp >= WA_EPI && warp < WA_MMA_WARP) {
+        // ---- producers: W tile (kk vectors x 128 elements, lane = element: coalesced) ->
+        // big/small A operands, K position 2p (re) and 2p + 1 (im) of row = element
+        const int ptid = tid - WA_EPI * 32;
+        float2 cur[WA_ITEMS], nxt[WA_ITEMS];
+        auto load = [&](long t, float2(&dst)[WA_ITEMS]) {
+#pragma unroll
+            for (int u = 0; u < WA_ITEMS; ++u) {
+                const int e = ptid + u * WA_PROD * 32, p = e / WA_TILE, i = e % WA_TILE;
+                const long g = t * WA_TILE + i;
+                dst[u] = (p < kk && g < n) ? W[(size_t)p * n + g] : make_float2(0.f, 0.f);
+            }
+        };
+        const long t0 = blockIdx.x;
+        if (my_tiles > 0) load(t0, cur);
+        for (int i = 0; i < my_tiles; ++i) {
+            const int buf = i & 1;
+            if (i + 1 < my_tiles) load(t0 + (long)(i + 1) * G, nxt);
+            if (i >= 2) {   // the MMAs of tile i - 2 read this A buffer
+                int ok = 1;
+                if (lane == 0) {
+                    ok = mbar_wait(smem_u32(&mdone[buf]), ((i >> 1) - 1) & 1, &s_abort);
+                    if (!ok && !s_abort) { atomicAdd(&g_tc_timeouts, 1u); s_abort = 1; }
+                }
+                if (!__shfl_sync(0xffffffffu, ok, 0)) break;
+            }
+            float *Ab = A + (size_t)buf * 2 * (WA_AOP / 4), *As = Ab + WA_AOP / 4;
+#pragma unroll
+            for (int u = 0; u < WA_ITEMS; ++u) {
+                const int e = ptid + u * WA_PROD * 32, p = e / WA_TILE, r = e % WA_TILE;
+                if (p >= kk) continue;
+                const float br = tf32_big(cur[u].x), bi = tf32_big(cur[u].y);
+                const int o = swz(r, 2 * p, WA_TILE);   // 2p and 2p + 1 share a 16-byte chunk
+                *reinterpret_cast<float2 *>(Ab + o) = make_float2(br, bi);
+                *reinterpret_cast<float2 *>(As + o) = make_float2(cur[u].x - br, cur[u].y - bi);
+            }
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&full[buf]));
+#pragma unroll
+            for (int u = 0; u < WA_ITEMS; ++u) cur[u] = nxt[u];
+        }
+    } else if (warp == WA_MMA_WARP) {
+        if (lane == 0) {
+            const int ksteps = (2 * kk + 7) / 8;
+            const uint32_t id_all = idesc_tf32(TC_M, 4 * nsp), id_big = idesc_tf32(TC_M, 2 * nsp);
+            const uint64_t a0 = sdesc(smem_u32(A)), b0 = sdesc(smem_u32(B));
+            const uint64_t abuf = (uint64_t)(2 * WA_AOP) >> 4, asmall = (uint64_t)WA_AOP >> 4;
+            const uint64_t acol = (uint64_t)(WA_TILE * TC_ROW) >> 4, bcol = (uint64_t)(brows * TC_ROW) >> 4;
+            for (int i = 0; i < my_tiles; ++i) {
+                const int buf = i & 1;
+                if (!mbar_wait(smem_u32(&full[buf]), (i >> 1) & 1, &s_abort) ||
+                    (i >= 2 && !mbar_wait(smem_u32(&tempty[buf]), ((i >> 1) - 1) & 1, &s_abort))) {
+                    if (!s_abort) { atomicAdd(&g_tc_timeouts, 1u); s_abort = 1; }
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t d = taddr + (uint32_t)(buf * 256);
+                for (int ks = 0; ks < ksteps; ++ks) {
+                    const uint64_t koff = (uint64_t)((ks & 3) * 32) >> 4;
+                    const uint64_t ab = a0 + buf * abuf + (ks >> 2) * acol + koff;
+                    const uint64_t bd = b0 + (ks >> 2) * bcol + koff;
+                    asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+                                 "l"(ab), "l"(bd), "r"(id_all), "r"(ks > 0 ? 1u : 0u));
+                    asm volatile("tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, 1;\n" ::"r"(d),
+                                 "l"(ab + asmall), "l"(bd), "r"(id_big));
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                 smem_u32(&mdone[buf]))
+                             : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             smem_u32(&done))
+                         : "memory");
+        }
+    } else {
+        // ---- epilogue: warp w reads TMEM lanes 32w..32w+31 = elements of the tile, sums the big
+        // and small blocks and stores P_s for every system (lanes = consecutive elements)
+        for (int i = 0; i < my_tiles; ++i) {
+            const int buf = i & 1;
+            int ok = 1;
+            if (lane == 0) {
+                ok = mbar_wait(smem_u32(&mdone[buf]), (i >> 1) & 1, &s_abort);
+                if (!ok && !s_abort) { atomicAdd(&g_tc_timeouts, 1u); s_abort = 1; }
+            }
+            if (!__shfl_sync(0xffffffffu, ok, 0)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const long g = ((long)blockIdx.x + (long)i * G) * WA_TILE + warp * 32 + lane;
+            const uint32_t row = taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)(buf * 256);
+            for (int c0 = 0; c0 < 2 * nsp; c0 += 16) {
+                uint32_t vb[16], vs[16];
+                tmem_ld16(row + (uint32_t)c0, vb);
+                tmem_ld16(row + (uint32_t)(2 * nsp + c0), vs);
+                if (g < n) {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const int sl = c0 / 2 + j;
+                        if (sl < nsys)
+                            P0[(size_t)s_act[sl] * strideP + g] =
+                                make_float2(__uint_as_float(vb[2 * j]) + __uint_as_float(vs[2 * j]),
+                                            __uint_as_float(vb[2 * j + 1]) + __uint_as_float(vs[2 * j + 1]));
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&tempty[buf]));
+        }
+    }
+    __syncthreads();
+    if (!mbar_wait(smem_u32(&done), 0, nullptr) && tid == 0) atomicAdd(&g_tc_timeouts, 1u);
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "n"(TC_TMEM_COLS));
+}
+
 std::mutex g_tc_mu;
 std::vector<int> g_tc_sms;       // per device
 std::vector<char> g_tc_smem_set;
@@ -459,6 +660,33 @@ int launch_wproj_tc(int n, int kk, const float2 *W, const float2 *Y, size_t stri
     const int O = kk * nsys;
     k_wproj_tc_reduce<<<(O + 31) / 32, 256, 0, st>>>(kk, nsys, G, part, act, coef, strideC);
     return 2;
+}
+
+size_t wapply_smem_bytes(int nsp) { return (size_t)4 * WA_AOP + (size_t)4 * nsp * 2 * TC_ROW + 1024; }
+
+bool wapply_tc_ok(int n, int kk, int nsys) { return kk > 0 && kk <= TC_KMAX && nsys >= 8 && nsys <= TC_NMAX && n > 0; }
+
+int launch_wapply_tc(int n, int kk, const float2 *W, double2 *coef, size_t strideC, const int *act, int nsys,
+                     float2 *P, size_t strideP, int unit_idx, cudaStream_t st) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const long ntiles = ((long)n + WA_TILE - 1) / WA_TILE;
+    const int sms = device_sms(dev);
+    const int G = (int)(ntiles < sms ? ntiles : sms);
+    const int nsp = ((nsys + 7) / 8) * 8;
+    static std::vector<char> set;
+    {
+        std::lock_guard<std::mutex> lk(g_tc_mu);
+        if ((int)set.size() <= dev) set.resize(dev + 1, 0);
+        if (!set[dev]) {
+            cudaFuncSetAttribute(k_wapply_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)wapply_smem_bytes(TC_NMAX));
+            set[dev] = 1;
+        }
+    }
+    k_wapply_tc<<<G, WA_THREADS, wapply_smem_bytes(nsp), st>>>(n, kk, W, coef, strideC, act, nsys, nsp, P, strideP,
+                                                               unit_idx);
+    return 1;
 }
 
 unsigned wproj_tc_timeouts() {

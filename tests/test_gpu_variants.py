@@ -9,7 +9,9 @@ true FP64 residual (<= 1.5e-10).  The last index of each list is the batched
 shared-basis pair (split-K projection of W for the whole batch, update with
 W in registers for 16 systems at a time), which only runs while 8 or more
 systems are active; complex64 projection variant 10 is the same shared-W
-projection on the tensor cores (tcgen05, TF32 operands split big + small).
+projection on the tensor cores (tcgen05, TF32 operands split big + small), and
+complex64 update variant 9 applies W c on the tensor cores into the next Krylov
+vector's slot before the per-system update.
 """
 import numpy as np
 import pytest
@@ -21,7 +23,7 @@ pytestmark = pytest.mark.gpu
 
 NRHS = 20
 PAIRS = {
-    "mixed": [(i, i) for i in range(9)] + [(9, 8), (10, 0), (10, 8)],
+    "mixed": [(i, i) for i in range(9)] + [(9, 8), (10, 0), (10, 8), (0, 9), (10, 9)],
     "fp64": [(i, i) for i in range(7)] + [(7, 6)],
 }
 
