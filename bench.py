@@ -49,11 +49,10 @@ KAPPA, DAMPING, M, K, TOL = 24.0, 0.1, 48, 24, 1e-10
 
 
 # DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic byte, per kernel
-# class, from one capture of every launch of three batched cycles on the same operator
-# (profiles/dram_traffic_mixed96_8rhs.md).  The ratio does not depend on the batch size: every
-# system's vectors are separate streams and the shared deflation vectors are counted once.
-TRAFFIC_PER_ALGORITHMIC_BYTE = {"projection": 1.003, "update": 0.991, "operator": 0.847, "combine": 0.994,
-                                "deflation_update": 1.329, "residual64": 1.312, "other": 0.595}
+# class, from one capture of every launch of three batched cycles of this same workload
+# (profiles/dram_traffic_mixed96_64rhs.md, tensor-core shared-basis kernels in use).
+TRAFFIC_PER_ALGORITHMIC_BYTE = {"projection": 1.027, "update": 1.043, "operator": 0.957, "combine": 1.001,
+                                "deflation_update": 1.328, "residual64": 1.469, "other": 0.946}
 
 
 def peaks():
@@ -499,7 +498,7 @@ def main():
                 "algorithmic_bytes_per_launch": per_launch,
                 "traffic": ratio * per_launch if ratio is not None else None,
                 "traffic_basis": (f"ncu DRAM bytes = {ratio} x algorithmic bytes for this class "
-                                  "(every launch of 3 cycles, 96^3, 8 RHS), times this run's mean "
+                                  "(every launch of 3 cycles of this workload), times this run's mean "
                                   "algorithmic bytes per launch") if ratio is not None else None,
                 "share": d["ms"] / tot_ms, "classes": class_table(prof, hbm_peak)}
 
