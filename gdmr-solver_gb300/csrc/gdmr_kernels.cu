@@ -252,6 +252,44 @@ template <class C, int VEC> __device__ __forceinline__ void store_pack(C *p, lon
     for (int j = 0; j < VEC; ++j)
         if (i0 + j < n) p[i0 + j] = r.v[j];
 }
+// Warp sum of PU complex double-float partials as a reduce-scatter butterfly: at offsets 16, 8,
+// ... each lane keeps half of its components (chosen by its lane bit) and adds the partner's
+// copy of that half, so the 2*PU components take log2(2 PU) halving levels and then full
+// levels for the rest, instead of 5 full levels each.  Component c = 2u + (0 re | 1 im) ends in
+// the lanes whose top bits spell c; the first of them writes dst[p0 + u].
+template <int PU> __device__ __forceinline__ void df_reduce_scatter(dfc (&a)[PU], dfc *dst, int p0, int q, int lane) {
+    constexpr int Q = 2 * PU;
+    dfr v[Q];
+#pragma unroll
+    for (int u = 0; u < PU; ++u) {
+        v[2 * u] = a[u].x;
+        v[2 * u + 1] = a[u].y;
+    }
+    int off = 16;
+#pragma unroll
+    for (int cnt = Q; cnt > 1; cnt >>= 1, off >>= 1) {
+        const bool hi = (lane & off) != 0;
+        const int half = cnt >> 1;
+#pragma unroll
+        for (int i = 0; i < half; ++i) {
+            const dfr keep = hi ? v[half + i] : v[i], send = hi ? v[i] : v[half + i];
+            const dfr got(__shfl_xor_sync(0xffffffffu, send.hi, off), __shfl_xor_sync(0xffffffffu, send.lo, off));
+            v[i] = keep + got;
+        }
+    }
+    for (; off > 0; off >>= 1)
+        v[0] = v[0] + dfr(__shfl_xor_sync(0xffffffffu, v[0].hi, off), __shfl_xor_sync(0xffffffffu, v[0].lo, off));
+    // lanes 32/Q * c hold component c
+    constexpr int SPAN = 32 / Q;
+    if ((lane & (SPAN - 1)) == 0) {
+        const int c = lane / SPAN, u = c >> 1;
+        if (p0 + u < q) {
+            if (c & 1) dst[p0 + u].y = v[0];
+            else dst[p0 + u].x = v[0];
+        }
+    }
+}
+
 template <class C> __host__ __device__ constexpr int min_blocks(int ept, int pu) {
     // double-float values carry two FP32 words per component plus two-sum temporaries
     return std::is_same<C, dfc>::value || ept * pu * (int)sizeof(C) > 128 ? 2 : 3;
@@ -260,8 +298,10 @@ template <class C> __host__ __device__ constexpr int min_blocks(int ept, int pu)
 // coef_s[p] = <B_p, w_s> for B = [segA (qa vectors) | segB_s (qb vectors)].
 // Grid (systems, chunks), w in registers, PU basis vectors in flight per thread, warp
 // reductions in the working precision, last CTA of each system sums the chunk partials.
-template <class R, int EPT, int PU, int VEC>
-__global__ void __launch_bounds__(NT, min_blocks<typename CT<R>::t>(EPT, PU))
+// PF: the next group's basis vectors are loaded before the current group is reduced, so the
+// double-float forms (about 44 FP32 operations per element and vector) keep their loads in flight.
+template <class R, int EPT, int PU, int VEC, bool PF = false>
+__global__ void __launch_bounds__(NT, PF ? 2 : min_blocks<typename CT<R>::t>(EPT, PU))
     k_mdot(int n, const typename CT<R>::t *__restrict__ segA, int qa, const typename CT<R>::t *__restrict__ segB0,
            size_t strideB, int qb, const typename CT<R>::t *__restrict__ w0, size_t strideW,
            const int *__restrict__ act, double2 *__restrict__ partials, int qmax, unsigned *tickets,
@@ -278,25 +318,54 @@ __global__ void __launch_bounds__(NT, min_blocks<typename CT<R>::t>(EPT, PU))
     Pack<C, VEC> wv[NP];
 #pragma unroll
     for (int e = 0; e < NP; ++e) wv[e] = load_pack<C, VEC>(w, c0 + ((long)e * NT + tid) * VEC, n);
-    for (int p0 = 0; p0 < q; p0 += PU) {
-        Pack<C, VEC> vv[PU][NP];
+    Pack<C, VEC> vv[PU][NP], nx[PU][NP];
+    auto load_group = [&](int g0, Pack<C, VEC>(&dst)[PU][NP]) {
 #pragma unroll
         for (int u = 0; u < PU; ++u) {
-            const int p = p0 + u < q ? p0 + u : q - 1;   // duplicate the last vector; its result is dropped
+            const int p = g0 + u < q ? g0 + u : q - 1;   // duplicate the last vector; its result is dropped
             const C *vp = p < qa ? segA + (size_t)p * n : segB + (size_t)(p - qa) * n;
 #pragma unroll
-            for (int e = 0; e < NP; ++e) vv[u][e] = load_pack<C, VEC>(vp, c0 + ((long)e * NT + tid) * VEC, n);
+            for (int e = 0; e < NP; ++e) dst[u][e] = load_pack<C, VEC>(vp, c0 + ((long)e * NT + tid) * VEC, n);
         }
+    };
+    if constexpr (PF) load_group(0, vv);
+    for (int p0 = 0; p0 < q; p0 += PU) {
+        if constexpr (PF) {
+            if (p0 + PU < q) load_group(p0 + PU, nx);
+        } else {
+            load_group(p0, vv);
+        }
+        if constexpr (std::is_same<C, dfc>::value) {
+            // double-float: all PU partials first, then one reduce-scatter butterfly over the
+            // 2*PU real components (each lane keeps half of what it holds at every level)
+            C a[PU];
 #pragma unroll
-        for (int u = 0; u < PU; ++u) {
-            C a = czero<C>();
+            for (int u = 0; u < PU; ++u) {
+                a[u] = czero<C>();
 #pragma unroll
-            for (int e = 0; e < NP; ++e)
+                for (int e = 0; e < NP; ++e)
 #pragma unroll
-                for (int j = 0; j < VEC; ++j) cdotacc(a, vv[u][e].v[j], wv[e].v[j]);
-            a.x = warp_sum(a.x);
-            a.y = warp_sum(a.y);
-            if (lane == 0 && p0 + u < q) wsum[warp][p0 + u] = a;
+                    for (int j = 0; j < VEC; ++j) cdotacc(a[u], vv[u][e].v[j], wv[e].v[j]);
+            }
+            df_reduce_scatter<PU>(a, &wsum[warp][0], p0, q, lane);
+        } else {
+#pragma unroll
+            for (int u = 0; u < PU; ++u) {
+                C a = czero<C>();
+#pragma unroll
+                for (int e = 0; e < NP; ++e)
+#pragma unroll
+                    for (int j = 0; j < VEC; ++j) cdotacc(a, vv[u][e].v[j], wv[e].v[j]);
+                a.x = warp_sum(a.x);
+                a.y = warp_sum(a.y);
+                if (lane == 0 && p0 + u < q) wsum[warp][p0 + u] = a;
+            }
+        }
+        if constexpr (PF) {
+#pragma unroll
+            for (int u = 0; u < PU; ++u)
+#pragma unroll
+                for (int e = 0; e < NP; ++e) vv[u][e] = nx[u][e];
         }
     }
     __syncthreads();
@@ -324,8 +393,8 @@ __global__ void __launch_bounds__(NT, min_blocks<typename CT<R>::t>(EPT, PU))
 }
 
 // ----------------------------------------------------------------- update + norms
-template <class R, int EPT, int PU, int VEC>
-__global__ void __launch_bounds__(NT, min_blocks<typename CT<R>::t>(EPT, PU))
+template <class R, int EPT, int PU, int VEC, bool PF = false>
+__global__ void __launch_bounds__(NT, PF ? 2 : min_blocks<typename CT<R>::t>(EPT, PU))
     k_update(int n, const typename CT<R>::t *__restrict__ segA, int qa, const typename CT<R>::t *__restrict__ segB0,
              size_t strideB, int qb, const typename CT<R>::t *__restrict__ w0, size_t strideW,
              typename CT<R>::t *__restrict__ out0, size_t strideO, const int *__restrict__ act,
@@ -351,14 +420,24 @@ __global__ void __launch_bounds__(NT, min_blocks<typename CT<R>::t>(EPT, PU))
         org[e] = load_pack<C, VEC>(w, c0 + ((long)e * NT + tid) * VEC, n);
         acc[e] = org[e];
     }
-    for (int p0 = 0; p0 < q; p0 += PU) {
-        Pack<C, VEC> vv[PU][NP];
+    Pack<C, VEC> vv[PU][NP], nx[PU][NP];
+    auto load_group = [&](int g0, Pack<C, VEC>(&dst)[PU][NP]) {
 #pragma unroll
         for (int u = 0; u < PU; ++u) {
-            const int p = p0 + u < q ? p0 + u : q - 1;
+            const int p = g0 + u < q ? g0 + u : q - 1;
             const C *vp = p < qa ? segA + (size_t)p * n : segB + (size_t)(p - qa) * n;
 #pragma unroll
-            for (int e = 0; e < NP; ++e) vv[u][e] = load_pack<C, VEC>(vp, c0 + ((long)e * NT + tid) * VEC, n);
+            for (int e = 0; e < NP; ++e) dst[u][e] = load_pack<C, VEC>(vp, c0 + ((long)e * NT + tid) * VEC, n);
+        }
+    };
+    if constexpr (PF) {
+        if (q > 0) load_group(0, vv);
+    }
+    for (int p0 = 0; p0 < q; p0 += PU) {
+        if constexpr (PF) {
+            if (p0 + PU < q) load_group(p0 + PU, nx);
+        } else {
+            load_group(p0, vv);
         }
 #pragma unroll
         for (int u = 0; u < PU; ++u) {
@@ -375,6 +454,12 @@ __global__ void __launch_bounds__(NT, min_blocks<typename CT<R>::t>(EPT, PU))
             for (int e = 0; e < NP; ++e)
 #pragma unroll
                 for (int j = 0; j < VEC; ++j) acc[e].v[j] = canon(acc[e].v[j]);
+        }
+        if constexpr (PF) {
+#pragma unroll
+            for (int u = 0; u < PU; ++u)
+#pragma unroll
+                for (int e = 0; e < NP; ++e) vv[u][e] = nx[u][e];
         }
     }
     C ln = czero<C>(), lc = czero<C>();
@@ -1591,6 +1676,65 @@ __global__ void __launch_bounds__(1024) k_svd(int m, int k, const double2 *__res
 }
 
 // ----------------------------------------------------------------- SELL-32 SpMM
+// One system: two rows a thread (row r and r + NT of a 2*NT-row chunk), both rows' entries
+// loaded before any gather, so the two dependent trips (column index, then x) overlap across
+// the rows; rows wider than WMAX take the generic loop.
+template <class R>
+__global__ void __launch_bounds__(NT) k_spmv2(int n, const int *__restrict__ slice_ptr, const int *__restrict__ cols,
+                                              const typename CT<R>::t *__restrict__ vals,
+                                              const typename CT<R>::t *__restrict__ x0, size_t strideX,
+                                              typename CT<R>::t *__restrict__ y0, size_t strideY,
+                                              const int *__restrict__ act) {
+    using C = typename CT<R>::t;
+    constexpr int WMAX = 8;
+    const int sys = act[0];
+    const C *x = x0 + (size_t)sys * strideX;
+    C *y = y0 + (size_t)sys * strideY;
+    const long rbase = (long)blockIdx.x * 2 * NT + threadIdx.x;
+    C v[2][WMAX];
+    int c[2][WMAX], width[2];
+    bool ok[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const long row = rbase + (long)h * NT;
+        ok[h] = row < n;
+        width[h] = 0;
+        if (ok[h]) {
+            const int slice = (int)(row >> 5), lane = (int)(row & 31);
+            const int beg = slice_ptr[slice];
+            width[h] = (slice_ptr[slice + 1] - beg) >> 5;
+#pragma unroll
+            for (int e = 0; e < WMAX; ++e) {
+                const bool in = e < width[h];
+                v[h][e] = in ? vals[beg + e * 32 + lane] : czero<C>();
+                c[h][e] = in ? cols[beg + e * 32 + lane] : (int)row;
+            }
+        }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        if (!ok[h]) continue;
+        const long row = rbase + (long)h * NT;
+        C acc = czero<C>();
+        if (width[h] <= WMAX) {
+            C g[WMAX];
+#pragma unroll
+            for (int e = 0; e < WMAX; ++e) g[e] = e < width[h] ? x[c[h][e]] : czero<C>();
+#pragma unroll
+            for (int e = 0; e < WMAX; ++e)
+                if (e < width[h]) cfma(acc, v[h][e], g[e]);
+        } else {
+            const int slice = (int)(row >> 5), lane = (int)(row & 31), beg = slice_ptr[slice];
+            for (int e = 0; e < width[h]; ++e) {
+                const int idx = beg + e * 32 + lane;
+                cfma(acc, vals[idx], x[cols[idx]]);
+                acc = canon(acc);
+            }
+        }
+        y[row] = canon(acc);
+    }
+}
+
 // Grid (system groups, row chunks): the groups of one row chunk run together, so the
 // matrix slice is read from HBM once and from L2 for the other groups.
 template <class R, int SG>
@@ -2080,26 +2224,28 @@ std::string tune_report() {
 //               projection only: 8 split-vector(4); 9 batched shared-W (CUDA cores);
 //               10 batched shared-W on the tensor cores (tcgen05, 3xTF32);
 //               update only: 8 batched shared-W (CUDA cores), 9 shared part on the tensor cores
-//   complex128: 0 (4,2,1)  1 (8,2,1)  2 (4,4,1)  3 (1,4,1)  4 (2,2,1)  5 grp(4,2)
-//               projection only: 6 split-vector(4)
-template <class R, int EPT, int PU, int VEC>
+//   complex128 and double-float: 0 (4,2,1)  1 (8,2,1)  2 (4,4,1)  3 (1,4,1)  4 (2,2,1)  5 grp(4,2)
+//               projection: 6 split-vector(4), 7 batched shared-W (complex128), 8 (4,2,1) prefetching
+//               update: 6 batched shared-W (complex128), 7 (4,2,1) prefetching
+template <class R, int EPT, int PU, int VEC, bool PF = false>
 void mdot_v(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
             const typename CT<R>::t *w, size_t strideW, const int *act, int nsys, double2 *partials, int qmax,
             unsigned *tickets, double2 *coef, size_t strideC, SysState *state, bool skip_broken, cudaStream_t st) {
     const int G = (n + NT * EPT - 1) / (NT * EPT);
-    k_mdot<R, EPT, PU, VEC><<<grid2(nsys, G > 0 ? G : 1), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW, act,
-                                                                     partials, qmax, tickets, coef, strideC, state,
-                                                                     skip_broken ? 1 : 0);
+    k_mdot<R, EPT, PU, VEC, PF><<<grid2(nsys, G > 0 ? G : 1), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW,
+                                                                         act, partials, qmax, tickets, coef, strideC,
+                                                                         state, skip_broken ? 1 : 0);
 }
-template <class R, int EPT, int PU, int VEC>
+template <class R, int EPT, int PU, int VEC, bool PF = false>
 void update_v(int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB, int qb,
               const typename CT<R>::t *w, size_t strideW, typename CT<R>::t *out, size_t strideO, const int *act,
               int nsys, const double2 *coef, size_t strideC, double2 *partials, unsigned *tickets, SysState *state,
               FinishArgs fin, bool skip_broken, cudaStream_t st) {
     const int G = (n + NT * EPT - 1) / (NT * EPT);
-    k_update<R, EPT, PU, VEC><<<grid2(nsys, G > 0 ? G : 1), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW,
-                                                                       out, strideO, act, coef, strideC, partials,
-                                                                       tickets, state, fin, skip_broken ? 1 : 0);
+    k_update<R, EPT, PU, VEC, PF><<<grid2(nsys, G > 0 ? G : 1), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w,
+                                                                           strideW, out, strideO, act, coef, strideC,
+                                                                           partials, tickets, state, fin,
+                                                                           skip_broken ? 1 : 0);
 }
 
 template <class R, int VPG>
@@ -2233,6 +2379,13 @@ int mdot_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const typ
         }
         v = 0;
     }
+    if constexpr (sizeof(R) != 4) {
+        if (v == 8) {   // (4, 2, 1) with the next group prefetched
+            mdot_v<R, 4, 2, 1, true>(n, segA, qa, segB, strideB, qb, w, strideW, act, nsys, partials, qmax, tickets,
+                                     coef, strideC, state, skip_broken, st);
+            return 1;
+        }
+    }
     if constexpr (sizeof(R) == 4) {
         static const int ept_of[9] = {8, 8, 16, 8, 2, 1, 4, 4, 1};
         if (v < 0 || v > 8 || !fits(ept_of[v])) v = 0;
@@ -2276,7 +2429,7 @@ void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT
     };
     int v = 0;
     if (forced_variant(0) >= 0) v = forced_variant(0);
-    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(prec_key<R>(), 0, n, nsys, qa, sizeof(R) == 4 ? 11 : 8, st, run);
+    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(prec_key<R>(), 0, n, nsys, qa, sizeof(R) == 4 ? 11 : 9, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)
@@ -2328,6 +2481,13 @@ int update_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const t
             v = 0;
         }
     }
+    if constexpr (sizeof(R) != 4) {
+        if (v == 7) {   // (4, 2, 1) with the next group prefetched
+            update_v<R, 4, 2, 1, true>(n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef,
+                                       strideC, partials, tickets, state, fin, skip_broken, st);
+            return 1;
+        }
+    }
     if constexpr (sizeof(R) == 4) {
         static const int ept_of[8] = {8, 8, 16, 8, 2, 1, 4, 4};
         if (v < 0 || v > 7 || !fits(ept_of[v])) v = 0;
@@ -2371,7 +2531,7 @@ void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename 
     int v = 0;
     if (forced_variant(1) >= 0) v = forced_variant(1);
     else if (representative(nsys, qa, qb) && !profile_enabled())
-        v = tuned_variant(prec_key<R>(), 1, n, nsys, qa, sizeof(R) == 4 ? 10 : 7, st, run);
+        v = tuned_variant(prec_key<R>(), 1, n, nsys, qa, sizeof(R) == 4 ? 10 : 8, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)
@@ -2457,6 +2617,12 @@ void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX
                  const int *act, int nsys, cudaStream_t st) {
     if (nsys <= 0) return;
     Launch L_(KC_SPMM, spmm_bytes(A, sizeof(typename CT<R>::t), nsys), st, 1);
+    if (nsys == 1) {
+        const long chunks = ((long)A.n + 2 * NT - 1) / (2 * NT);
+        k_spmv2<R><<<(unsigned)chunks, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const typename CT<R>::t *)A.vals, x,
+                                                    strideX, y, strideY, act);
+        return;
+    }
     constexpr int SG = 8;
     int rows = (A.n + NT - 1) / NT;
     dim3 grid((nsys + SG - 1) / SG, rows < 65535 ? rows : 65535);

@@ -94,7 +94,8 @@ void gdmrTune(int on);
 const char *gdmrTuneReport(void);
 /* Pins the Gram-Schmidt variants by their index in the tuner report (-1: tuner).  Used to
  * check every variant against the others; an index a launch cannot use falls back to 0.
- * complex64 projection 0-10, update 0-9; complex128 and fp64e projection 0-7, update 0-6.
+ * complex64 projection 0-10, update 0-9; complex128 and fp64e projection 0-8, update 0-7
+ * (projection 8 and update 7 prefetch the next group of basis vectors).
  * Batched shared-deflation-basis variants (8 to 64 systems, k <= 32): complex64 projection 9
  * (CUDA cores) and 10 (tensor cores), update 8 (CUDA cores) and 9 (tensor cores); complex128
  * projection 7 and update 6 (CUDA cores). */

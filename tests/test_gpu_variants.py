@@ -11,7 +11,8 @@ W in registers for 16 systems at a time), which only runs while 8 or more
 systems are active; complex64 projection variant 10 is the same shared-W
 projection on the tensor cores (tcgen05, TF32 operands split big + small), and
 complex64 update variant 9 applies W c on the tensor cores into the next Krylov
-vector's slot before the per-system update.
+vector's slot before the per-system update; complex128 / fp64e projection 8 and
+update 7 prefetch the next group of basis vectors.
 """
 import numpy as np
 import pytest
@@ -24,7 +25,8 @@ pytestmark = pytest.mark.gpu
 NRHS = 20
 PAIRS = {
     "mixed": [(i, i) for i in range(9)] + [(9, 8), (10, 0), (10, 8), (0, 9), (10, 9)],
-    "fp64": [(i, i) for i in range(7)] + [(7, 6)],
+    "fp64": [(i, i) for i in range(7)] + [(7, 6), (8, 7)],
+    "fp64e": [(0, 0), (1, 1), (2, 2), (6, 5), (8, 7)],
 }
 
 
