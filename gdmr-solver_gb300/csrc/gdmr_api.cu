@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -621,6 +622,68 @@ extern "C" long long gdmr_system_bytes(const gdmr_system *S) {
     if (!S) return 0;
     return (long long)(S->A.bytes() + S->e32.device_bytes() + S->e64.device_bytes() + S->edf.device_bytes() +
                        2 * sizeof(double2) * (size_t)S->n * std::max(S->cap, 2));
+}
+
+// Switches the inner operator of the system's engine to the matrix-free stencil after checking,
+// in FP64, that it reproduces the system's CSR operator on a fixed pseudo-random vector.  The
+// FP64 true residual keeps using the CSR operator.
+extern "C" int gdmr_system_set_stencil(gdmr_system *S, int nx, int ny, int nz, const double *coef_ri) {
+    if (!S || !coef_ri) return fail(GDMR_EINVAL, "gdmr_system_set_stencil", "null argument");
+    if (nx < 1 || ny < 1 || nz < 1 || (long)nx * ny * nz != (long)S->n)
+        return fail(GDMR_EINVAL, "gdmr_system_set_stencil", "nx * ny * nz must equal the system size");
+    std::lock_guard<std::mutex> lk(S->mu);
+    cudaSetDevice(S->device);
+    Stencil7 st{nx, ny, nz, make_double2(coef_ri[0], coef_ri[1]), make_double2(coef_ri[2], coef_ri[3]),
+                make_double2(coef_ri[4], coef_ri[5]), make_double2(coef_ri[6], coef_ri[7])};
+    const int n = S->n;
+    std::vector<double2> hx(n), h1(n), h2(n);
+    uint64_t z = 0x2545F4914F6CDD1DULL;
+    for (int i = 0; i < n; ++i) {   // xorshift64*: values in [-1, 1)
+        z ^= z >> 12; z ^= z << 25; z ^= z >> 27;
+        const uint64_t r = z * 0x2545F4914F6CDD1DULL;
+        hx[i] = make_double2((double)(r >> 11) * 0x1.0p-52 - 1.0, (double)((r >> 11) ^ 0x5555555555555ULL) * 0x1.0p-52 - 1.0);
+    }
+    int *dact = nullptr;
+    const int zero = 0;
+    double2 *x = S->db, *y1 = S->dx, *y2 = S->dx + (size_t)n;
+    if (cudaMalloc(&dact, sizeof(int)) != cudaSuccess) return fail(GDMR_ENOMEM, "gdmr_system_set_stencil", "scratch");
+    cudaMemcpyAsync(dact, &zero, sizeof(int), cudaMemcpyHostToDevice, S->st);
+    cudaMemcpyAsync(x, hx.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, S->st);
+    launch_spmm<double>(S->A.view64(), x, 0, y1, 0, dact, 1, S->st);
+    launch_stencil<double>(st, x, 0, y2, 0, dact, 1, S->st);
+    cudaMemcpyAsync(h1.data(), y1, sizeof(double2) * n, cudaMemcpyDeviceToHost, S->st);
+    cudaMemcpyAsync(h2.data(), y2, sizeof(double2) * n, cudaMemcpyDeviceToHost, S->st);
+    const cudaError_t e = cudaStreamSynchronize(S->st);
+    cudaFree(dact);
+    if (e != cudaSuccess) return fail(GDMR_ECUDA, "gdmr_system_set_stencil", cudaGetErrorString(e));
+    double err = 0, mag = 0;
+    for (int i = 0; i < n; ++i) {
+        err = std::max(err, std::hypot(h1[i].x - h2[i].x, h1[i].y - h2[i].y));
+        mag = std::max(mag, std::hypot(h1[i].x, h1[i].y));
+    }
+    if (!(err <= 1e-12 * mag))
+        return fail(GDMR_EINVAL, "gdmr_system_set_stencil", "the stencil does not reproduce the system's operator");
+    if (S->precision == 1) {
+        S->e32.op.kind = Operator<float>::STENCIL;
+        S->e32.op.stencil = st;
+    } else if (S->precision == 2) {
+        S->edf.op.kind = Operator<dfr>::STENCIL;
+        S->edf.op.stencil = st;
+    } else {
+        S->e64.op.kind = Operator<double>::STENCIL;
+        S->e64.op.stencil = st;
+    }
+    set_last_error(GDMR_OK, "ok");
+    return GDMR_OK;
+}
+
+extern "C" int gdmr_system_clear_stencil(gdmr_system *S) {
+    if (!S) return fail(GDMR_EINVAL, "gdmr_system_clear_stencil", "null system");
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (S->precision == 1) S->e32.op.kind = Operator<float>::SELL;
+    else if (S->precision == 2) S->edf.op.kind = Operator<dfr>::SELL;
+    else S->e64.op.kind = Operator<double>::SELL;
+    return GDMR_OK;
 }
 
 extern "C" int gdmr_system_set_graphs(gdmr_system *S, int on) {

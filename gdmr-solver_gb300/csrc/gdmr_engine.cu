@@ -326,6 +326,9 @@ void Engine<R>::apply(const C *x0, size_t strideX, C *y0, size_t strideY, int ns
     case Operator<R>::SELL:
         launch_spmm<R>(op.sell, x0, strideX, y0, strideY, act_, nsys, stream);
         break;
+    case Operator<R>::STENCIL:
+        launch_stencil<R>(op.stencil, x0, strideX, y0, strideY, act_, nsys, stream);
+        break;
     case Operator<R>::DENSE:
         for (int i = 0; i < nsys; ++i) {
             const int s = act_h_[i];
@@ -426,6 +429,9 @@ template <class R> int Engine<R>::enqueue_cycle(int kk, int nsys, double tol, lo
             if (op.kind == Operator<R>::SELL) {
                 *matvecs += 1;
                 launch_spmm<R>(op.sell, Z_ + (size_t)i * n, 0, az, 0, ident_, 1, stream);
+            } else if (op.kind == Operator<R>::STENCIL) {
+                *matvecs += 1;
+                launch_stencil<R>(op.stencil, Z_ + (size_t)i * n, 0, az, 0, ident_, 1, stream);
             } else {
                 std::vector<int> keep = act_h_;
                 act_h_ = {0};
@@ -608,8 +614,8 @@ template <class R> int Engine<R>::refine_setup(const SellMatrix &A64) {
         set_last_error(GDMR_ENOTINIT, "solver used before initialisation");
         return GDMR_ENOTINIT;
     }
-    if (op.kind != Operator<R>::SELL || !A64.vals) {
-        set_last_error(GDMR_EINVAL, "refined solve: needs a SELL operator with FP64 values");
+    if ((op.kind != Operator<R>::SELL && op.kind != Operator<R>::STENCIL) || !A64.vals) {
+        set_last_error(GDMR_EINVAL, "refined solve: needs a SELL or stencil operator and FP64 SELL values");
         return GDMR_EINVAL;
     }
     A64_ = A64;

@@ -51,7 +51,8 @@ void sell_free(DeviceSell &s);
 // Operator seen by an engine of precision R.
 template <class R> struct Operator {
     using C = typename CT<R>::t;
-    enum Kind { NONE, HOOK, SELL, DENSE } kind = NONE;
+    enum Kind { NONE, HOOK, SELL, DENSE, STENCIL } kind = NONE;
+    Stencil7 stencil{};             // STENCIL: matrix-free constant-coefficient operator
     void (*hook)(void) = nullptr;   // reference hook: applies A in place to `ext`
     C *ext = nullptr;
     SellMatrix sell{};

@@ -1676,6 +1676,55 @@ __global__ void __launch_bounds__(1024) k_svd(int m, int k, const double2 *__res
 }
 
 // ----------------------------------------------------------------- SELL-32 SpMM
+// ----------------------------------------------------------------- matrix-free stencil
+// Thread (x, y) of a 32 x 8 tile marches over ZC planes, keeping the planes below, at and
+// above in registers: each x value comes from memory once for the z direction, the in-plane
+// neighbours come from the same or adjacent rows of the tile (L1).  Grid (tiles, z chunks,
+// systems).
+template <class C> __device__ __forceinline__ C cadd(C a, C b) {
+    C r;
+    r.x = a.x + b.x;
+    r.y = a.y + b.y;
+    return r;
+}
+constexpr int ST_ZC = 8;
+template <class R>
+__global__ void __launch_bounds__(NT) k_stencil(int nx, int ny, int nz, double2 dd, double2 wxd, double2 wyd,
+                                                double2 wzd, const typename CT<R>::t *__restrict__ x0, size_t strideX,
+                                                typename CT<R>::t *__restrict__ y0, size_t strideY,
+                                                const int *__restrict__ act) {
+    using C = typename CT<R>::t;
+    const int sys = act[blockIdx.z];
+    const C *x = x0 + (size_t)sys * strideX;
+    C *y = y0 + (size_t)sys * strideY;
+    const int tilesx = (nx + 31) / 32;
+    const int ix = (blockIdx.x % tilesx) * 32 + (threadIdx.x & 31);
+    const int iy = (blockIdx.x / tilesx) * 8 + (threadIdx.x >> 5);
+    if (ix >= nx || iy >= ny) return;
+    const C d = from_d<C>(dd), wx = from_d<C>(wxd), wy = from_d<C>(wyd), wz = from_d<C>(wzd);
+    const long plane = (long)nx * ny;
+    const int z0 = blockIdx.y * ST_ZC, z1 = min(nz, z0 + ST_ZC);
+    long idx = (long)iy * nx + ix + (long)z0 * plane;
+    C below = z0 > 0 ? x[idx - plane] : czero<C>();
+    C cur = x[idx];
+    for (int z = z0; z < z1; ++z, idx += plane) {
+        const C above = z + 1 < nz ? x[idx + plane] : czero<C>();
+        C sx = czero<C>(), sy = czero<C>();
+        if (ix > 0) sx = x[idx - 1];
+        if (ix + 1 < nx) sx = cadd(sx, x[idx + 1]);
+        if (iy > 0) sy = x[idx - nx];
+        if (iy + 1 < ny) sy = cadd(sy, x[idx + nx]);
+        C acc = czero<C>();
+        cfma(acc, d, cur);
+        cfma(acc, wx, sx);
+        cfma(acc, wy, sy);
+        cfma(acc, wz, cadd(below, above));
+        y[idx] = canon(acc);
+        below = cur;
+        cur = above;
+    }
+}
+
 // One system: two rows a thread (row r and r + NT of a 2*NT-row chunk), both rows' entries
 // loaded before any gather, so the two dependent trips (column index, then x) overlap across
 // the rows; rows wider than WMAX take the generic loop.
@@ -2630,6 +2679,17 @@ void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX
                                        strideY, act, nsys);
 }
 
+template <class R>
+void launch_stencil(const Stencil7 &S, const typename CT<R>::t *x, size_t strideX, typename CT<R>::t *y,
+                    size_t strideY, const int *act, int nsys, cudaStream_t st) {
+    if (nsys <= 0) return;
+    const double n = (double)S.nx * S.ny * S.nz;
+    Launch L_(KC_SPMM, 2.0 * nsys * n * sizeof(typename CT<R>::t), st, 1);   // x read once, y written
+    const int tiles = ((S.nx + 31) / 32) * ((S.ny + 7) / 8);
+    const dim3 grid(tiles, (S.nz + ST_ZC - 1) / ST_ZC, nsys);
+    k_stencil<R><<<grid, NT, 0, st>>>(S.nx, S.ny, S.nz, S.d, S.wx, S.wy, S.wz, x, strideX, y, strideY, act);
+}
+
 void launch_residual64(const SellMatrix &A, const double2 *b, size_t strideB, const double2 *x, size_t strideX,
                        double2 *r, size_t strideR, const int *act, int nsys, double2 *partials, unsigned *tickets,
                        SysState *state, cudaStream_t st) {
@@ -2702,6 +2762,8 @@ void launch_broadcast_hdef(int m, int kk, const double2 *Hd, double2 *H, size_t 
     template void launch_znormalise<R>(int, int, const CT<R>::t *, const double *, CT<R>::t *, cudaStream_t);          \
     template void launch_spmm<R>(const SellMatrix &, const CT<R>::t *, size_t, CT<R>::t *, size_t, const int *, int,  \
                                  cudaStream_t);                                                                        \
+    template void launch_stencil<R>(const Stencil7 &, const CT<R>::t *, size_t, CT<R>::t *, size_t, const int *, int, \
+                                    cudaStream_t);                                                                     \
     template void launch_dense_gemv<R>(int, const CT<R>::t *, const CT<R>::t *, CT<R>::t *, cudaStream_t);             \
     template void launch_copy_vec<R>(int, const CT<R>::t *, size_t, CT<R>::t *, size_t, const int *, int,              \
                                      cudaStream_t);                                                                    \

@@ -234,6 +234,17 @@ struct SellMatrix {
     const void *vals;       // padded values (float2 or double2)
     long nnz;               // non-zeros of the source matrix (for algorithmic byte counts)
 };
+// Matrix-free constant-coefficient stencil on an nx x ny x nz grid (nz = 1: 5-point 2D),
+// unknowns numbered i + nx (j + ny l), Dirichlet boundary (neighbours outside are dropped):
+//   y = d x + wx (x[i-1] + x[i+1]) + wy (x[j-1] + x[j+1]) + wz (x[l-1] + x[l+1]).
+struct Stencil7 {
+    int nx, ny, nz;
+    double2 d, wx, wy, wz;
+};
+template <class R>
+void launch_stencil(const Stencil7 &S, const typename CT<R>::t *x, size_t strideX, typename CT<R>::t *y,
+                    size_t strideY, const int *act, int nsys, cudaStream_t st);
+
 template <class R>
 void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX, typename CT<R>::t *y,
                  size_t strideY, const int *act, int nsys, cudaStream_t st);

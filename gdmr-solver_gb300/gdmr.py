@@ -58,6 +58,8 @@ SIGNATURES = {
     "gdmrTune": (None, [I]),
     "gdmrTuneReport": (ctypes.c_char_p, []),
     "gdmrTuneForce": (None, [I, I]),
+    "gdmr_system_set_stencil": (I, [P, I, I, I, P]),
+    "gdmr_system_clear_stencil": (I, [P]),
     "gdmr_system_create": (I, [P, I, P, P, P, I, I, I, I, I]),
     "gdmr_system_destroy": (I, [P]),
     "gdmr_system_bytes": (LL, [P]),
@@ -313,6 +315,18 @@ class System:
 
     def set_graphs(self, on: bool) -> None:
         _check(self.L.gdmr_system_set_graphs(self._h, 1 if on else 0), "gdmr_system_set_graphs")
+
+    def set_stencil(self, shape, d, wx, wy, wz=0.0) -> None:
+        """Matrix-free inner operator: the constant-coefficient stencil on a grid of `shape`
+        (2 or 3 edge lengths, first fastest).  Checked in FP64 against the system's CSR
+        operator; raises GDMRError if it does not reproduce it."""
+        nx, ny = int(shape[0]), int(shape[1])
+        nz = int(shape[2]) if len(shape) > 2 else 1
+        coef = np.array([d, wx, wy, wz], dtype=np.complex128)
+        _check(self.L.gdmr_system_set_stencil(self._h, nx, ny, nz, _ptr(coef)), "gdmr_system_set_stencil")
+
+    def clear_stencil(self) -> None:
+        _check(self.L.gdmr_system_clear_stencil(self._h), "gdmr_system_clear_stencil")
 
     def svd_sweeps(self) -> dict:
         v = int(self.L.gdmr_system_svd_sweeps(self._h))

@@ -121,6 +121,14 @@ def helmholtz(shape: tuple, kappa: float, damping: float) -> CSR:
     return A
 
 
+def helmholtz_stencil(shape: tuple, kappa: float, damping: float) -> tuple:
+    """(d, wx, wy, wz) of the matrix-free form of helmholtz(shape, kappa, damping)."""
+    inv_h2 = [(L + 1) ** 2 for L in shape]
+    d = sum(2.0 * s for s in inv_h2) - kappa * kappa * complex(1.0, damping)
+    w = [-float(s) for s in inv_h2] + [0.0] * (3 - len(shape))
+    return complex(d), complex(w[0]), complex(w[1]), complex(w[2])
+
+
 def variable_helmholtz(shape: tuple, kappa: float, damping: float, seed: int, block: int = 8) -> CSR:
     """3D 7-point -div(a grad u) - kappa^2 (1 + i damping) u with piecewise-constant a.
 

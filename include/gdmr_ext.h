@@ -119,6 +119,15 @@ int gdmr_system_destroy(gdmr_system *sys);
 long long gdmr_system_bytes(const gdmr_system *sys);
 /* Jacobi sweeps of the last deflation-space SVD: 1000 * (FP32 sweeps) + (FP64 sweeps). */
 int gdmr_system_svd_sweeps(const gdmr_system *sys);
+/* Matrix-free operator: a constant-coefficient stencil on an nx x ny x nz grid (nz = 1 for the
+ * 5-point 2D form), unknowns numbered i + nx (j + ny l), Dirichlet boundary:
+ *   y = d x + wx (x[i-1] + x[i+1]) + wy (x[j-1] + x[j+1]) + wz (x[l-1] + x[l+1]),
+ * coef_ri = {d, wx, wy, wz} as interleaved complex128.  It replaces the inner operator of the
+ * system (the FP64 true residual keeps the CSR operator) after an FP64 check that it reproduces
+ * the CSR operator on a pseudo-random vector (GDMR_EINVAL if not, to 1e-12 relative).
+ * gdmr_system_clear_stencil returns to the CSR operator. */
+int gdmr_system_set_stencil(gdmr_system *sys, int nx, int ny, int nz, const double *coef_ri);
+int gdmr_system_clear_stencil(gdmr_system *sys);
 /* Restart cycles of small systems (n x batch <= 2^20) replay as CUDA graphs after the first
  * cycle (on by default); 0 launches every kernel eagerly. */
 int gdmr_system_set_graphs(gdmr_system *sys, int on);
