@@ -522,6 +522,21 @@ def main():
            "h2d_bytes_per_step": int(2 * B.nbytes), "d2h_bytes_per_step": int(B.nbytes)}
     e2e_ok = all(s["status"] == 0 and s["true_rel_res"] <= TOL for s in st_e2e)
 
+    # the same step with the matrix-free stencil as the inner operator (gdmr_system_set_stencil)
+    matrix_free = None
+    if not args.stencil:
+        sysm.set_stencil(shape, *problems.helmholtz_stencil(shape, KAPPA, DAMPING))
+        torch.cuda.synchronize()
+        ev0.record()
+        st_mf = step()
+        ev1.record()
+        torch.cuda.synchronize()
+        mf_ms = max_over_ranks(ev0.elapsed_time(ev1), world)
+        sysm.clear_stencil()
+        matrix_free = {"value": world * nrhs / (mf_ms / 1e3), "unit": "solves/s", "steps": 1,
+                       "verified": all(x["status"] == 0 and x["true_rel_res"] <= TOL for x in st_mf),
+                       "operator": "matrix-free 7-point stencil (k_stencil); FP64 residual on the CSR operator"}
+
     # plain forms, one right-hand side at a time (reference algorithm): native complex128
     # (the drop-in) and fp64e (the same iteration in double-float arithmetic on the FP32 pipes)
     def plain_form(precision, max_cycles):
@@ -563,7 +578,7 @@ def main():
         "verified": bool(verified), "worst_true_rel_res": worst_res,
         "plain_fp64": plain, "mixed_over_plain": value / world / plain["value"],
         "plain_fp64e": plain_e, "mixed_over_plain_fp64e": value / world / plain_e["value"],
-        "e2e": e2e, "e2e_verified": bool(e2e_ok),
+        "e2e": e2e, "e2e_verified": bool(e2e_ok), "matrix_free": matrix_free,
         "gpu_launches": int(launches), "clocks": clocks, "roofline": roofline,
         "tuning": gdmr.tune_report().strip().splitlines(),
     }

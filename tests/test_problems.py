@@ -2,6 +2,7 @@
 import os
 
 import numpy as np
+import pytest
 
 import problems
 
@@ -67,3 +68,28 @@ def test_gaussian_source_noise_level():
     s = problems.gaussian_source_rhs((24, 24, 24), 101)
     assert s.shape == (24**3,)
     assert np.abs(s).max() > 0.5
+
+
+def _stencil_apply(shape, coef, x):
+    """y = d x + w_axis (x[-1] + x[+1]) along every axis, Dirichlet (the k_stencil formula)."""
+    d, wx, wy, wz = coef
+    X = x.reshape(tuple(reversed(shape)))          # numbering i + nx (j + ny l): x fastest
+    Y = d * X
+    for axis, w in zip(range(X.ndim - 1, -1, -1), (wx, wy, wz)):
+        sl_lo = [slice(None)] * X.ndim
+        sl_hi = [slice(None)] * X.ndim
+        sl_lo[axis] = slice(0, -1)
+        sl_hi[axis] = slice(1, None)
+        Y[tuple(sl_lo)] += w * X[tuple(sl_hi)]
+        Y[tuple(sl_hi)] += w * X[tuple(sl_lo)]
+    return Y.reshape(-1)
+
+
+@pytest.mark.parametrize("shape,kappa,damping", [((64, 64), 20.0, 0.05), ((7, 5, 6), 3.0, 0.1)])
+def test_helmholtz_stencil_matches_csr(shape, kappa, damping):
+    A = problems.helmholtz(shape, kappa, damping)
+    coef = problems.helmholtz_stencil(shape, kappa, damping)
+    x = problems.complex_gaussian(3, A.n)
+    y_csr = A.to_scipy() @ x
+    y_st = _stencil_apply(shape, coef, x)
+    assert np.max(np.abs(y_csr - y_st)) <= 1e-12 * np.max(np.abs(y_csr))
