@@ -1368,186 +1368,501 @@ __global__ void __launch_bounds__(128) k_ls(int m, const double2 *__restrict__ H
     }
 }
 
-// ----------------------------------------------------------------- SVD (one-sided Jacobi, FP32 then FP64)
+// ----------------------------------------------------------------- SVD (one-sided Jacobi, FP32 then double-float)
 // Right singular vectors of H ((m+1) x m) by one-sided Jacobi (Hestenes 1958) with the
-// round-robin ("circle") ordering of disjoint column pairs:
-//   1. FP32 sweeps to FP32 convergence (cheap: GB300 issues FP32 at ~64x its FP64 rate);
-//   2. FP64: V re-orthonormalised by two passes of Gram-Schmidt, A = H V;
-//   3. FP64 sweeps to FP64 convergence (typically one or two).
-// In FP64 the scalar rotation parameters of a round are computed one pair per lane of
-// warp 0, so a round pays for them once instead of once per pair in every lane.
-template <class T> struct CX;
-template <> struct CX<float> { using t = float2; };
-template <> struct CX<double> { using t = double2; };
+// round-robin ("circle") ordering of disjoint column pairs, in one CTA:
+//   1. FP32 sweeps to FP32 convergence;
+//   2. double-float (the FP32 pipes): V made unitary to double-float precision by the
+//      second-order polar correction V <- V (I - E/2 + 3 E^2/8), E = V^H V - I, then A = H V;
+//   3. double-float sweeps restricted to the pairs with a column of the k smallest singular
+//      values, to the FP64 tolerance.
+// GB300 retires FP64 at about 1/64 of its FP32 rate; in one CTA that is about one FP64 warp
+// instruction per 80 clocks per scheduler, and phases 2 and 3 in native FP64 took 1.4 of the
+// 2.0 ms of an m = 40 SVD.
 
-// Pair of slot pi in round r of the circle method over mm (even) slots.
+// Pair (p < q) of slot pi in round r (0 <= r < mm - 1) of the circle method over mm (even)
+// slots.
 __device__ __forceinline__ void circle_pair(int r, int pi, int mm, int &p, int &q) {
-    auto pos = [&](int i) { return i == 0 ? 0 : 1 + ((i - 1 + r) % (mm - 1)); };
+    auto pos = [&](int i) {
+        if (i == 0) return 0;
+        int x = i - 1 + r;                  // < 2 (mm - 1): one conditional subtraction
+        if (x >= mm - 1) x -= mm - 1;
+        return 1 + x;
+    };
     p = pos(pi);
     q = pos(mm - 1 - pi);
+    if (p > q) { const int t = p; p = q; q = t; }
 }
 
-// Sweeps of one-sided Jacobi on A ((m+1) x m) accumulating V (m x m).  `only` (optional, m
-// flags) restricts the rotations to pairs with at least one flagged column: the columns of
-// the k smallest singular values, the only ones the deflation update uses.  Rotating a
-// flagged column against every other one makes it orthogonal to all columns of A, which
-// decouples the flagged block exactly; rotations among unflagged columns cannot change it.
-// SPLIT: compute each round's rotation parameters one pair per lane of one warp (FP64, where
-// scalar arithmetic is expensive) instead of in every lane of each pair's warp (FP32).
-template <class T, bool SPLIT>
-__device__ int jacobi_sweeps(int m, typename CX<T>::t *A, typename CX<T>::t *V, T *nrm, double2 *rot, T tol,
-                             int max_sweeps, int *s_flag, float *s_off, const unsigned char *only) {
-    using C = typename CX<T>::t;
+// QR with column pivoting (Businger and Golub 1965) of A ((m+1) x m, column-major, FP32) in
+// place, by Householder reflections in the conventions of LAPACK's xLARFG: on return the upper
+// triangle holds R, and column j of R comes from column perm[j] of A.  Pivoting on the largest
+// remaining column norm grades R, which lets one-sided Jacobi on R^H converge in about half
+// the sweeps it takes on A (Drmac and Veselic 2008).  The partial norms are recomputed after
+// each step, not downdated.  pn (m) is scratch; s_c a shared scalar.
+__device__ void qrcp_f32(int m, float2 *A, int *perm, float *pn, float2 *s_c) {
     const int rows = m + 1, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    for (int c = warp; c < m; c += nwarps) {
+        float a = 0.f;
+        for (int r = lane; r < rows; r += 32) { const float2 v = A[(size_t)c * rows + r]; a += v.x * v.x + v.y * v.y; }
+        a = warp_sum(a);
+        if (lane == 0) { pn[c] = a; perm[c] = c; }
+    }
+    __syncthreads();
+    for (int j = 0; j < m; ++j) {
+        float2 *aj = A + (size_t)j * rows;
+        if (warp == 0) {
+            // pivot: the largest remaining norm, lowest index on ties; swap it into column j
+            float best = -1.f;
+            int bi = j;
+            for (int c = j + lane; c < m; c += 32)
+                if (pn[c] > best) { best = pn[c]; bi = c; }
+            for (int o = 16; o > 0; o >>= 1) {
+                const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (bi != j) {
+                float2 *ap = A + (size_t)bi * rows;
+                for (int r = lane; r < rows; r += 32) { const float2 t = aj[r]; aj[r] = ap[r]; ap[r] = t; }
+                if (lane == 0) {
+                    const int t = perm[j]; perm[j] = perm[bi]; perm[bi] = t;
+                    const float u = pn[j]; pn[j] = pn[bi]; pn[bi] = u;
+                }
+                __syncwarp();
+            }
+            // reflector H = I - tau v v^H, v = (1, x / (alpha - beta))
+            float xn = 0.f;
+            for (int r = j + 1 + lane; r < rows; r += 32) xn += aj[r].x * aj[r].x + aj[r].y * aj[r].y;
+            xn = warp_sum(xn);
+            const float2 al = aj[j];
+            float2 tau = make_float2(0.f, 0.f);
+            if (xn > 0.f || al.y != 0.f) {
+                const float beta = -copysignf(sqrtf(al.x * al.x + al.y * al.y + xn), al.x);
+                tau = make_float2((beta - al.x) / beta, -al.y / beta);
+                const float2 d = make_float2(al.x - beta, al.y);                  // 1 / (alpha - beta)
+                const float id = 1.f / (d.x * d.x + d.y * d.y);
+                const float2 sc = make_float2(d.x * id, -d.y * id);
+                for (int r = j + 1 + lane; r < rows; r += 32) {
+                    const float2 x = aj[r];
+                    aj[r] = make_float2(x.x * sc.x - x.y * sc.y, x.x * sc.y + x.y * sc.x);
+                }
+                __syncwarp();
+                if (lane == 0) aj[j] = make_float2(beta, 0.f);
+            }
+            if (lane == 0) *s_c = tau;
+        }
+        __syncthreads();
+        const float2 tau = *s_c;
+        for (int c = j + 1 + warp; c < m; c += nwarps) {   // a_c <- (I - conj(tau) v v^H) a_c
+            float2 *ac = A + (size_t)c * rows;
+            float wr = 0.f, wi = 0.f;
+            for (int r = j + lane; r < rows; r += 32) {
+                const float2 v = (r == j) ? make_float2(1.f, 0.f) : aj[r], a = ac[r];
+                wr += v.x * a.x + v.y * a.y;
+                wi += v.x * a.y - v.y * a.x;
+            }
+            wr = warp_sum(wr);
+            wi = warp_sum(wi);
+            const float fr = tau.x * wr + tau.y * wi, fi = tau.x * wi - tau.y * wr;   // conj(tau) w
+            float s = 0.f;
+            for (int r = j + lane; r < rows; r += 32) {
+                const float2 v = (r == j) ? make_float2(1.f, 0.f) : aj[r];
+                float2 a = ac[r];
+                a.x -= fr * v.x - fi * v.y;
+                a.y -= fr * v.y + fi * v.x;
+                ac[r] = a;
+                if (r > j) s += a.x * a.x + a.y * a.y;
+            }
+            s = warp_sum(s);
+            if (lane == 0) pn[c] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// The circle schedule as a table: entry round * (mm/2) + pi = p | q << 8 (p < q < mm <= 256).
+// With `only`, each round keeps just the pairs with a flagged column, packed to the front, and
+// cnt[round] says how many.
+__device__ void pair_table(int m, unsigned short *tab, int *cnt, const unsigned char *only) {
     const int mm = m + (m & 1), npairs = mm / 2;
+    for (int r = threadIdx.x; r < mm - 1; r += blockDim.x) {
+        int n = 0;
+        for (int pi = 0; pi < npairs; ++pi) {
+            int p, q;
+            circle_pair(r, pi, mm, p, q);
+            if (!only || (q < m && (only[p] || only[q]))) tab[r * npairs + n++] = (unsigned short)(p | (q << 8));
+        }
+        if (cnt) cnt[r] = n;
+    }
+}
+
+// 1/sqrt(x) in FP32 to about an ulp: the hardware estimate and one Newton step.
+__device__ __forceinline__ float rsqrt_nr(float x) {
+    const float r = rsqrtf(x);
+    return r * fmaf(-0.5f * x * r, r, 1.5f);
+}
+
+// Jacobi rotation tangent t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)), zeta = (b - a) / (2 |gamma|):
+// the root of t^2 + 2 zeta t - 1 of smaller magnitude.  Above 2^40, t = 1 / (2 zeta) to FP32
+// precision (and zeta^2 could overflow).
+__device__ __forceinline__ float jacobi_t(float zeta) {
+    const float az = fabsf(zeta);
+    if (az > 0x1p40f) return __fdividef(0.5f, zeta);
+    const float z2 = fmaf(az, az, 1.f);
+    return __fdividef((zeta >= 0.f) ? 1.f : -1.f, az + z2 * rsqrtf(z2));
+}
+
+// Sweeps of FP32 one-sided Jacobi on A (rows x m) accumulating V (m x m; none when V is null),
+// both column-major with leading dimensions rows and m.  One warp per column pair, every lane
+// computing the
+// rotation parameters; the pairs of each round come from `tab` (p | q << 8, p < q, built by
+// pair_table), which takes the schedule arithmetic off the critical path of a round.  The angle only has to shrink the off-diagonal element (the
+// double-float phase finishes the job), so it uses the hardware estimates; c and the phase of
+// gamma are Newton-refined, which keeps each rotation unitary to about an ulp.
+__device__ int jacobi_sweeps_f32(int m, int rows, float2 *A, float2 *V, float *nrm, float tol, int max_sweeps,
+                                 int *s_flag, float *s_off, const unsigned short *tab) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const int mm = m + (m & 1), npairs = mm / 2;
+    const float tol2 = tol * tol;
     int sweep = 0;
     for (; sweep < max_sweeps; ++sweep) {
         for (int c = warp; c < m; c += nwarps) {   // column norms, refreshed every sweep
-            T a = 0;
-            for (int r = lane; r < rows; r += 32) { C v = A[(size_t)c * rows + r]; a += v.x * v.x + v.y * v.y; }
+            float a = 0;
+            for (int r = lane; r < rows; r += 32) { float2 v = A[(size_t)c * rows + r]; a += v.x * v.x + v.y * v.y; }
             a = warp_sum(a);
             if (lane == 0) nrm[c] = a;
         }
         if (tid == 0) { *s_flag = 0; *s_off = 0.f; }
         __syncthreads();
+        float wmax = 0.f;                           // largest relative off-diagonal this warp saw
         for (int round = 0; round < mm - 1; ++round) {
-            // (1) gamma of every pair, one warp per pair; in the fused form also (2) and (3)
             for (int pi = warp; pi < npairs; pi += nwarps) {
-                int p, q;
-                circle_pair(round, pi, mm, p, q);
-                const bool skip = p >= m || q >= m || (only && !only[p] && !only[q]);
-                if (skip) { if (SPLIT && lane == 0) rot[pi] = make_double2(0, 0); continue; }
-                if (p > q) { int t = p; p = q; q = t; }
-                T gr = 0, gi = 0;
+                const unsigned e = tab[round * npairs + pi];
+                const int p = e & 0xff, q = e >> 8;
+                if (q >= m) continue;
+                float gr = 0, gi = 0;
                 for (int r = lane; r < rows; r += 32) {
-                    C ap = A[(size_t)p * rows + r], aq = A[(size_t)q * rows + r];
+                    float2 ap = A[(size_t)p * rows + r], aq = A[(size_t)q * rows + r];
                     gr += ap.x * aq.x + ap.y * aq.y;
                     gi += ap.x * aq.y - ap.y * aq.x;
                 }
                 gr = warp_sum(gr);
                 gi = warp_sum(gi);
-                if (SPLIT) {
-                    if (lane == 0) rot[pi] = make_double2((double)gr, (double)gi);
-                    continue;
-                }
-                // fused: every lane computes the (cheap) FP32 parameters and applies them
-                const T a = nrm[p], b = nrm[q];
-                const T ag = sqrt(gr * gr + gi * gi);
-                const T rel = ag / sqrt(a * b);
-                if (!(ag > (T)0 && rel > tol)) continue;
-                if (lane == 0) {
-                    *s_flag = 1;
-                    atomicMax((int *)s_off, __float_as_int((float)rel));
-                }
-                const T pr = gr / ag, pim = -gi / ag;
-                const T zeta = (b - a) / ((T)2 * ag);
-                const T tt = ((zeta >= (T)0) ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
-                const T c = (T)1 / sqrt((T)1 + tt * tt), sn = c * tt;
+                const float a = nrm[p], b = nrm[q];
+                const float g2 = gr * gr + gi * gi;
+                if (!(g2 > tol2 * a * b)) continue;   // |gamma| / sqrt(a b) <= tol, or zero
+                const float ig = rsqrt_nr(g2), ag = g2 * ig;
+                wmax = fmaxf(wmax, ag * rsqrtf(a * b));
+                const float pr = gr * ig, pim = -gi * ig;
+                const float zeta = (b - a) * 0.5f * ig;
+                const float tt = jacobi_t(zeta);
+                const float c = rsqrt_nr(fmaf(tt, tt, 1.f)), sn = c * tt;
                 for (int r = lane; r < rows; r += 32) {
-                    C ap = A[(size_t)p * rows + r], aq0 = A[(size_t)q * rows + r];
-                    C aq;
-                    aq.x = aq0.x * pr - aq0.y * pim;
-                    aq.y = aq0.x * pim + aq0.y * pr;
-                    C np_, nq_;
-                    np_.x = c * ap.x - sn * aq.x; np_.y = c * ap.y - sn * aq.y;
-                    nq_.x = sn * ap.x + c * aq.x; nq_.y = sn * ap.y + c * aq.y;
-                    A[(size_t)p * rows + r] = np_;
-                    A[(size_t)q * rows + r] = nq_;
+                    float2 ap = A[(size_t)p * rows + r], aq0 = A[(size_t)q * rows + r];
+                    const float2 aq = make_float2(aq0.x * pr - aq0.y * pim, aq0.x * pim + aq0.y * pr);
+                    A[(size_t)p * rows + r] = make_float2(c * ap.x - sn * aq.x, c * ap.y - sn * aq.y);
+                    A[(size_t)q * rows + r] = make_float2(sn * ap.x + c * aq.x, sn * ap.y + c * aq.y);
                 }
-                for (int r = lane; r < m; r += 32) {
-                    C vp = V[(size_t)p * m + r], vq0 = V[(size_t)q * m + r];
-                    C vq;
-                    vq.x = vq0.x * pr - vq0.y * pim;
-                    vq.y = vq0.x * pim + vq0.y * pr;
-                    C np_, nq_;
-                    np_.x = c * vp.x - sn * vq.x; np_.y = c * vp.y - sn * vq.y;
-                    nq_.x = sn * vp.x + c * vq.x; nq_.y = sn * vp.y + c * vq.y;
-                    V[(size_t)p * m + r] = np_;
-                    V[(size_t)q * m + r] = nq_;
+                for (int r = lane; V && r < m; r += 32) {
+                    float2 vp = V[(size_t)p * m + r], vq0 = V[(size_t)q * m + r];
+                    const float2 vq = make_float2(vq0.x * pr - vq0.y * pim, vq0.x * pim + vq0.y * pr);
+                    V[(size_t)p * m + r] = make_float2(c * vp.x - sn * vq.x, c * vp.y - sn * vq.y);
+                    V[(size_t)q * m + r] = make_float2(sn * vp.x + c * vq.x, sn * vp.y + c * vq.y);
                 }
                 if (lane == 0) {
                     nrm[p] = a - tt * ag;
                     nrm[q] = b + tt * ag;
                 }
             }
-            if (SPLIT) {
-                __syncthreads();
-                // (2) rotation parameters, one pair per lane: (c, t), phase e^{-i phi}, |gamma|
-                for (int pi = tid; pi < npairs; pi += blockDim.x) {
-                    int p, q;
-                    circle_pair(round, pi, mm, p, q);
-                    const double2 gd = rot[pi];
-                    T gx = (T)gd.x, gy = (T)gd.y;
-                    T cc = 1, tt = 0, phr = 1, phi = 0, ag = 0;
-                    if (p < m && q < m && !(only && !only[p] && !only[q])) {
-                        const T a = nrm[p < q ? p : q], b = nrm[p < q ? q : p];
-                        ag = sqrt(gx * gx + gy * gy);
-                        const T rel = ag / sqrt(a * b);
-                        if (ag > (T)0 && rel > tol) {
-                            *s_flag = 1;
-                            atomicMax((int *)s_off, __float_as_int((float)rel));
-                            phr = gx / ag;
-                            phi = -gy / ag;
-                            const T zeta = (b - a) / ((T)2 * ag);
-                            tt = ((zeta >= (T)0) ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
-                            cc = (T)1 / sqrt((T)1 + tt * tt);
-                        }
-                    }
-                    rot[pi] = make_double2((double)cc, (double)tt);
-                    rot[npairs + pi] = make_double2((double)phr, (double)phi);
-                    rot[2 * npairs + pi] = make_double2((double)ag, 0.0);
-                }
-                __syncthreads();
-                // (3) apply: one warp per pair, columns (min, max); incremental norms
-                for (int pi = warp; pi < npairs; pi += nwarps) {
-                    int p, q;
-                    circle_pair(round, pi, mm, p, q);
-                    if (p >= m || q >= m) continue;
-                    if (p > q) { int t = p; p = q; q = t; }
-                    const double2 ct = rot[pi];
-                    if (ct.y == 0.0) continue;
-                    const double2 ph = rot[npairs + pi];
-                    const T c = (T)ct.x, sn = (T)(ct.x * ct.y), pr = (T)ph.x, pim = (T)ph.y;
-                    for (int r = lane; r < rows; r += 32) {
-                        C ap = A[(size_t)p * rows + r], aq0 = A[(size_t)q * rows + r];
-                        C aq;
-                        aq.x = aq0.x * pr - aq0.y * pim;
-                        aq.y = aq0.x * pim + aq0.y * pr;
-                        C np_, nq_;
-                        np_.x = c * ap.x - sn * aq.x; np_.y = c * ap.y - sn * aq.y;
-                        nq_.x = sn * ap.x + c * aq.x; nq_.y = sn * ap.y + c * aq.y;
-                        A[(size_t)p * rows + r] = np_;
-                        A[(size_t)q * rows + r] = nq_;
-                    }
-                    for (int r = lane; r < m; r += 32) {
-                        C vp = V[(size_t)p * m + r], vq0 = V[(size_t)q * m + r];
-                        C vq;
-                        vq.x = vq0.x * pr - vq0.y * pim;
-                        vq.y = vq0.x * pim + vq0.y * pr;
-                        C np_, nq_;
-                        np_.x = c * vp.x - sn * vq.x; np_.y = c * vp.y - sn * vq.y;
-                        nq_.x = sn * vp.x + c * vq.x; nq_.y = sn * vp.y + c * vq.y;
-                        V[(size_t)p * m + r] = np_;
-                        V[(size_t)q * m + r] = nq_;
-                    }
-                    if (lane == 0) {
-                        const T tg = (T)(ct.y * rot[2 * npairs + pi].x);
-                        nrm[p] = nrm[p] - tg;
-                        nrm[q] = nrm[q] + tg;
-                    }
-                }
-            }
             __syncthreads();
         }
+        if (lane == 0 && wmax > 0.f) {
+            *s_flag = 1;
+            atomicMax((int *)s_off, __float_as_int(wmax));
+        }
+        __syncthreads();
         if (!*s_flag) break;
         // quadratic convergence: after a sweep whose largest relative off-diagonal was d,
         // the next is of order d^2; stop once that is below the tolerance
         const float d = *s_off;
         __syncthreads();
-        if ((double)d * (double)d < (double)tol * 1e-2) { ++sweep; break; }
+        if (d * d < tol * 1e-2f) { ++sweep; break; }
     }
     return sweep + 1;
 }
+
+// Exact float product as a double-float (FMA two-product).
+__device__ __forceinline__ dfr df_prod(float a, float b) {
+    const float p = a * b;
+    return dfr(p, fmaf(a, b, -p));
+}
+// acc + a * b for floats a, b, the product exact.
+__device__ __forceinline__ dfr df_acc(dfr acc, float a, float b) {
+    const float p = a * b, pe = fmaf(a, b, -p);
+    const float s = p + acc.hi, bb = s - p;
+    return df_renorm(s, ((p - (s - bb)) + (acc.hi - bb)) + (pe + acc.lo));
+}
+// 1 / sqrt(x) for a double-float x > 0: the FP32 estimate r0 times 1 - e/2 + 3e^2/8 (the
+// binomial series of (1 + e)^(-1/2)), e = x r0^2 - 1 kept as the exact pair (hi - 1, lo)
+// (hi - 1 is exact for hi in [1/2, 2], Sterbenz).  |e| < 1e-6, so the truncation is O(1e-19).
+__device__ __forceinline__ dfr df_rsqrt(dfr x) {
+    const float r0 = rsqrtf(x.hi);
+    const dfr u = x * df_prod(r0, r0);
+    const float eh = u.hi - 1.0f, el = u.lo;
+    return dfr(r0, 0.0f) * (dfr(1.0f, 0.0f) + dfr(-0.5f * eh, fmaf(0.375f * eh, eh, -0.5f * el)));
+}
+__device__ __forceinline__ dfc to_dfc(double2 a) {
+    dfc c;
+    c.x = dfr(a.x);
+    c.y = dfr(a.y);
+    return c;
+}
+
+// Columns P, Q (length len) <- (c P - s w Q, s P + c w Q), w = wr + i wi.
+__device__ __forceinline__ void rotate_df(dfc *P, dfc *Q, int len, int lane, dfr c, dfr s, dfr wr, dfr wi) {
+    for (int r = lane; r < len; r += 32) {
+        const dfc ap = P[r], q0 = Q[r];
+        const dfr qx = q0.x * wr - q0.y * wi, qy = q0.x * wi + q0.y * wr;
+        dfc np_, nq_;
+        np_.x = c * ap.x - s * qx;
+        np_.y = c * ap.y - s * qy;
+        nq_.x = s * ap.x + c * qx;
+        nq_.y = s * ap.y + c * qy;
+        P[r] = np_;
+        Q[r] = nq_;
+    }
+}
+// a + b for a double-float a and a float b.
+__device__ __forceinline__ dfr df_addf(dfr a, float b) {
+    const float s = a.hi + b, bb = s - a.hi;
+    return df_renorm(s, ((a.hi - (s - bb)) + (b - bb)) + a.lo);
+}
+// Small-angle rotation, |t| < 2^-30: c = 1 and s = t to double-float precision, and column Q
+// takes the unit phase conj(w), so (P, Q) <- (P - g Q, Q + conj(g) P) with g = t w, unitary up
+// to |t|^2 < 1e-18.  g Q and conj(g) P are below 1e-9 of the columns, so FP32 products of
+// the leading halves are exact enough.
+__device__ __forceinline__ void rotate_small_df(dfc *P, dfc *Q, int len, int lane, float gr, float gi) {
+    for (int r = lane; r < len; r += 32) {
+        const dfc ap = P[r], aq = Q[r];
+        dfc np_, nq_;
+        np_.x = df_addf(ap.x, -fmaf(gr, aq.x.hi, -gi * aq.y.hi));
+        np_.y = df_addf(ap.y, -fmaf(gr, aq.y.hi, gi * aq.x.hi));
+        nq_.x = df_addf(aq.x, fmaf(gr, ap.x.hi, gi * ap.y.hi));
+        nq_.y = df_addf(aq.y, fmaf(gr, ap.y.hi, -gi * ap.x.hi));
+        P[r] = np_;
+        Q[r] = nq_;
+    }
+}
+// Rotation parameters of the pair (p, q) from gamma = <a_p, a_q> and the squared column norms
+// a, b (double-float).  Returns false when the pair needs no rotation (relative off-diagonal
+// at most tol, or zero).  Otherwise t is the tangent of the rotation (FP32 accuracy), ag =
+// |gamma|, and (gx, gy) * igs is the unit complex gamma / |gamma|: gamma is scaled by a power
+// of two into [1/2, 2) first, so nothing underflows.
+__device__ __forceinline__ bool polish_params(dfr gr, dfr gi, dfr a, dfr b, float tol, float &t, float &ag,
+                                              float &gx, float &gy, float &igs) {
+    const int ex = max(-120, min(120, ilogbf(fmaxf(fabsf(gr.hi), fabsf(gi.hi)))));
+    const float down = __int_as_float((127 - ex) << 23), up = __int_as_float((127 + ex) << 23);
+    gx = gr.hi * down;
+    gy = gi.hi * down;
+    const float g2 = gx * gx + gy * gy;
+    if (!(g2 > 0.f)) return false;
+    igs = rsqrt_nr(g2);
+    ag = g2 * igs * up;
+    if (!(ag * rsqrtf(a.hi) * rsqrtf(b.hi) > tol)) return false;
+    t = jacobi_t((b - a).hi * 0.5f * igs * down);   // zeta = (b - a) / (2 |gamma|)
+    return true;
+}
+
+// gamma = <a_p, a_q> over len rows, one thread, in double-float.
+__device__ __forceinline__ void dot_df(const dfc *P, const dfc *Q, int len, dfr &gr, dfr &gi) {
+    gr = dfr(0.f, 0.f);
+    gi = dfr(0.f, 0.f);
+    for (int r = 0; r < len; ++r) {
+        const dfc ap = P[r], aq = Q[r];
+        gr = rfma(ap.x, aq.x, gr);
+        gr = rfma(ap.y, aq.y, gr);
+        gi = rfma(ap.x, aq.y, gi);
+        gi = rfma(-ap.y, aq.x, gi);
+    }
+    gr = df_renorm(gr.hi, gr.lo);
+    gi = df_renorm(gi.hi, gi.lo);
+}
+
+// One sweep's worth of small rotations applied at once.  When every rotation of a sweep has
+// |t| < 2^-26, the sweep is V <- V (I + T + T^2/2 + ...) with T skew-Hermitian and
+// T[q][p] = -g, T[p][q] = conj(g), g = t conj(gamma) / |gamma|, for every pair p < q with a
+// flagged column.  Products of two rotations are O(t^2) < 2e-16, so all gammas can come from
+// the current A and all updates can be applied together, with no rounds; the diagonal of T^2/2
+// (-sum |g|^2 / 2 per column) is kept, which makes the update unitary to O(t^3).  The sums run
+// in double-float (the FP32 coefficients times the leading halves of V, exactly).  Only the
+// flagged columns of V are updated: they are the output, and A is not needed again (its norms
+// move by O(t |gamma|), so the norms the sweep started from stay exact to that order).  fl lists
+// the k flagged columns; C (k x m) is scratch, and the k x m sums go in place of A once every
+// gamma is formed.  Returns false, having changed nothing, when some rotation is not small
+// (the caller then runs an ordinary sweep).
+__device__ bool polish_small_all(int m, dfc *A, dfc *V, int ldv, const dfr *nrm, float tol, const int *fl, int k,
+                                 float2 *C, int *s_big) {
+    const int rows = m + 1, tid = threadIdx.x, nt = blockDim.x;
+    dfc *D = A;
+    if (tid == 0) *s_big = 0;
+    __syncthreads();
+    for (int e = tid; e < k * m; e += nt) {   // C[f][q]: coefficient of column q added to flagged f
+        const int f = fl[e / m], q0 = e % m;
+        float2 coef = make_float2(0.f, 0.f);
+        if (q0 != f) {
+            const int p = min(f, q0), q = max(f, q0);
+            dfr gr, gi;
+            dot_df(A + (size_t)p * rows, A + (size_t)q * rows, rows, gr, gi);
+            float t, ag, gx, gy, igs;
+            if (polish_params(gr, gi, nrm[p], nrm[q], tol, t, ag, gx, gy, igs)) {
+                if (!(fabsf(t) < 0x1p-26f)) atomicOr(s_big, 1);
+                const float g_r = t * gx * igs, g_i = -t * gy * igs;   // g = t conj(gamma) / |gamma|
+                coef = (f == p) ? make_float2(-g_r, -g_i) : make_float2(g_r, -g_i);
+            }
+        }
+        C[e] = coef;
+    }
+    __syncthreads();
+    if (*s_big) return false;
+    for (int e = tid; e < k * m; e += nt) {   // D[f][r] = sum_q C[f][q] V[r][q] - |C[f]|^2 / 2 V[r][f]
+        const int fi = e / m, r = e % m;
+        dfr dx(0.f, 0.f), dy(0.f, 0.f);
+        float lx = 0.f, ly = 0.f, kap = 0.f;
+        for (int q = 0; q < m; ++q) {
+            const float2 c = C[(size_t)fi * m + q];
+            const dfc v = V[(size_t)q * ldv + r];
+            dx = df_acc(df_acc(dx, c.x, v.x.hi), -c.y, v.y.hi);
+            dy = df_acc(df_acc(dy, c.x, v.y.hi), c.y, v.x.hi);
+            lx = fmaf(c.x, v.x.lo, fmaf(-c.y, v.y.lo, lx));
+            ly = fmaf(c.x, v.y.lo, fmaf(c.y, v.x.lo, ly));
+            kap = fmaf(c.x, c.x, fmaf(c.y, c.y, kap));
+        }
+        const dfc vf = V[(size_t)fl[fi] * ldv + r];
+        dfc d;
+        d.x = df_addf(dx, fmaf(-0.5f * kap, vf.x.hi, lx));
+        d.y = df_addf(dy, fmaf(-0.5f * kap, vf.y.hi, ly));
+        D[e] = d;
+    }
+    __syncthreads();
+    for (int e = tid; e < k * m; e += nt) {
+        dfc &v = V[(size_t)fl[e / m] * ldv + e % m];
+        v.x = v.x + D[e].x;
+        v.y = v.y + D[e].y;
+    }
+    __syncthreads();
+    return true;
+}
+
+// Double-float one-sided Jacobi sweeps on A ((m+1) x m, leading dimension m+1) accumulating V
+// (m x m, leading dimension ldv), restricted to the pairs with a flagged column: rotating each
+// flagged column against every other one makes it orthogonal to all columns of A, which
+// decouples the flagged block exactly; rotations among unflagged columns cannot change it.
+// tab / cnt hold each round's pairs with a flagged column, packed (pair_table), so the active
+// pairs go to consecutive warps and spread evenly over the four schedulers.  The angle comes
+// from FP32-rounded parameters (b - a formed in double-float first), so a rotation leaves
+// about 1e-7 of its off-diagonal element and a sweep still squares the largest one; c, s and
+// the phase of gamma are unitary to double-float precision, which keeps V unitary.  From the
+// second sweep on, a sweep of small rotations is applied at once (polish_small_all).
+// Returns the number of sweeps.
+// Returns the number of sweeps; nrm then holds the squared column norms of the result (A itself
+// may have been overwritten).
+__device__ int jacobi_polish_df(int m, dfc *A, dfc *V, int ldv, dfr *nrm, float tol, int max_sweeps, int *s_flag,
+                                float *s_off, const unsigned short *tab, const int *cnt, const int *fl, int k,
+                                float2 *C) {
+    const int rows = m + 1, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const int mm = m + (m & 1), npairs = mm / 2;
+    __shared__ int s_big;
+    auto column_norms = [&]() {
+        for (int c = warp; c < m; c += nwarps) {
+            dfr a(0.f, 0.f);
+            for (int r = lane; r < rows; r += 32) {
+                const dfc v = A[(size_t)c * rows + r];
+                a = fma(v.x, v.x, a);
+                a = fma(v.y, v.y, a);
+            }
+            a = warp_sum(a);
+            if (lane == 0) nrm[c] = a;
+        }
+    };
+    int sweep = 0;
+    bool fresh = false;                     // nrm matches the current A
+    for (; sweep < max_sweeps; ++sweep) {
+        column_norms();
+        if (tid == 0) { *s_flag = 0; *s_off = 0.f; }
+        __syncthreads();
+        if (sweep > 0 && polish_small_all(m, A, V, ldv, nrm, tol, fl, k, C, &s_big)) {
+            ++sweep;
+            fresh = true;
+            break;
+        }
+        float wmax = 0.f;
+        for (int round = 0; round < mm - 1; ++round) {
+            for (int j = warp; j < cnt[round]; j += nwarps) {
+                const unsigned e = tab[round * npairs + j];
+                const int p = e & 0xff, q = e >> 8;
+                dfc *Ap = A + (size_t)p * rows, *Aq = A + (size_t)q * rows;
+                dfr gr(0.f, 0.f), gi(0.f, 0.f);
+                for (int r = lane; r < rows; r += 32) {   // unnormalised chains, canonical below
+                    const dfc ap = Ap[r], aq = Aq[r];
+                    gr = rfma(ap.x, aq.x, gr);
+                    gr = rfma(ap.y, aq.y, gr);
+                    gi = rfma(ap.x, aq.y, gi);
+                    gi = rfma(-ap.y, aq.x, gi);
+                }
+                gr = warp_sum(df_renorm(gr.hi, gr.lo));   // identical in every lane: the two-sum is symmetric
+                gi = warp_sum(df_renorm(gi.hi, gi.lo));
+                const dfr a = nrm[p], b = nrm[q];
+                float t, ag, gx, gy, igs;
+                if (!polish_params(gr, gi, a, b, tol, t, ag, gx, gy, igs)) continue;
+                wmax = fmaxf(wmax, ag * rsqrtf(a.hi) * rsqrtf(b.hi));
+                if (fabsf(t) < 0x1p-30f) {
+                    const float wr = gx * igs, wi = -gy * igs;
+                    rotate_small_df(Ap, Aq, rows, lane, t * wr, t * wi);
+                    rotate_small_df(V + (size_t)p * ldv, V + (size_t)q * ldv, m, lane, t * wr, t * wi);
+                } else {
+                    const dfr c = df_rsqrt(dfr(1.f, 0.f) + df_prod(t, t));
+                    const dfr s = c * dfr(t, 0.f);
+                    const dfr ig = df_rsqrt(df_prod(gx, gx) + df_prod(gy, gy));
+                    const dfr wr = dfr(gx, 0.f) * ig, wi = dfr(-gy, 0.f) * ig;
+                    rotate_df(Ap, Aq, rows, lane, c, s, wr, wi);
+                    rotate_df(V + (size_t)p * ldv, V + (size_t)q * ldv, m, lane, c, s, wr, wi);
+                }
+                if (lane == 0) {
+                    const dfr tg = df_prod(t, ag);
+                    nrm[p] = a - tg;
+                    nrm[q] = b + tg;
+                }
+            }
+            __syncthreads();
+        }
+        if (lane == 0 && wmax > 0.f) {
+            *s_flag = 1;
+            atomicMax((int *)s_off, __float_as_int(wmax));
+        }
+        __syncthreads();
+        if (!*s_flag) {                     // no rotation: the norms are the ones computed above
+            fresh = true;
+            break;
+        }
+        const float d = *s_off;
+        __syncthreads();
+        if (d * d < tol * 1e-2f) { ++sweep; break; }
+    }
+    if (!fresh) {
+        column_norms();
+        __syncthreads();
+    }
+    return sweep + 1;
+}
+
+// Working storage of k_svd, three regions of 16 (m+1) m bytes (shared memory when it fits):
+//   Ad  (m+1) x m double-float complex, A = H V;
+//   Vd  m x m, leading dimension m | 1 (odd, so the column-strided reads of V^H V hit
+//       distinct banks);
+//   Sc  scratch: the FP32 A and V of phase 1, then the FP32 E and E^2, then V F, then H as
+//       double-float (E and F live in Ad until A is formed).
+__host__ __device__ inline size_t svd_work_bytes(int m) { return 3 * sizeof(dfc) * (size_t)(m + 1) * m; }
 
 __global__ void __launch_bounds__(1024) k_svd(int m, int k, const double2 *__restrict__ H0, size_t strideH,
                                               const int *__restrict__ lead, double2 *__restrict__ vs,
@@ -1555,124 +1870,229 @@ __global__ void __launch_bounds__(1024) k_svd(int m, int k, const double2 *__res
                                               int *sweeps_out) {
     const double2 *__restrict__ H = H0 + (size_t)(*lead) * strideH;
     extern __shared__ __align__(16) unsigned char svd_sm[];
-    const int rows = m + 1, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const int rows = m + 1, tid = threadIdx.x, nt = blockDim.x, ldv = m | 1;
     unsigned char *base = use_smem ? svd_sm : (unsigned char *)gwork;
-    double2 *A64 = (double2 *)base;
-    double2 *V64 = A64 + (size_t)rows * m;
-    float2 *A32 = (float2 *)(V64 + (size_t)m * m);
+    dfc *Ad = (dfc *)base;
+    dfc *Vd = Ad + (size_t)rows * m;
+    dfc *Sc = Vd + (size_t)rows * m;
+    float2 *A32 = (float2 *)Sc;
     float2 *V32 = A32 + (size_t)rows * m;
-    __shared__ double nrm64[168];
+    __shared__ dfr nrmd[168];
     __shared__ float nrm32[168];
-    __shared__ double2 rot[3 * 84];
-    __shared__ int s_flag;
+    __shared__ int s_flag, slot_col[168];
     __shared__ float s_off;
-    for (int i = tid; i < rows * m; i += blockDim.x) A32[i] = make_float2((float)H[i].x, (float)H[i].y);
-    for (int i = tid; i < m * m; i += blockDim.x) V32[i] = make_float2((i % m) == (i / m) ? 1.f : 0.f, 0.f);
-    __syncthreads();
-    const int s32 = jacobi_sweeps<float, false>(m, A32, V32, nrm32, rot, 4.0f * 1.1920929e-7f * m, 40, &s_flag, &s_off,
-                                                nullptr);
-    // the k columns of smallest norm (smallest singular values) after the FP32 phase
     __shared__ unsigned char small_col[168];
-    for (int c = tid; c < m; c += blockDim.x) {
-        const float sc = nrm32[c];
+    __shared__ int s_emax, s_bad, flag_list[168], perm[168];
+    __shared__ float2 s_c;
+    // H scaled by the power of two that brings its largest entry into [1, 2): exact, and it
+    // keeps the FP32 phase clear of overflow and underflow whatever the operator's scale
+    if (tid == 0) s_emax = 0;
+    __syncthreads();
+    int em = 0;
+    for (int i = tid; i < rows * m; i += nt) {
+        const double2 h = H[i];
+        em = max(em, (int)((__double_as_longlong(h.x) >> 52) & 0x7ff));
+        em = max(em, (int)((__double_as_longlong(h.y) >> 52) & 0x7ff));
+    }
+    atomicMax(&s_emax, em);
+    __syncthreads();
+    const int eb = (s_emax == 0 || s_emax == 0x7ff) ? 1023 : min(max(2046 - s_emax, 1), 2046);
+    const double sc = __longlong_as_double((long long)eb << 52);
+    for (int i = tid; i < rows * m; i += nt) A32[i] = make_float2((float)(H[i].x * sc), (float)(H[i].y * sc));
+    pair_table(m, (unsigned short *)Vd, nullptr, nullptr);   // Vd is free until phase 2
+    if (tid == 0) s_bad = 0;
+    __syncthreads();
+    // 1. FP32.  H P = Q R (column pivoting), then one-sided Jacobi on X = R^H with no
+    // accumulation: R^H U = V_R Sigma, so the columns of the result are the right singular
+    // vectors of R scaled by the singular values, and H's are V = P V_R.  Should a column come
+    // out too small to normalise (singular values below ~1e-15 of the largest), the phase is
+    // redone as Jacobi on H accumulating V.
+    const float tol32 = 4.0f * 1.1920929e-7f * m;
+    const unsigned short *tab32 = (const unsigned short *)Vd;
+    qrcp_f32(m, A32, perm, nrm32, &s_c);
+    float2 *X = V32;                        // m x m, leading dimension m
+    for (int e = tid; e < m * m; e += nt) { // X[i][j] = conj(R[j][i]), lower triangular
+        const int i = e % m, j = e / m;
+        const float2 r = A32[(size_t)i * rows + j];
+        X[e] = i >= j ? make_float2(r.x, -r.y) : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    int s32 = jacobi_sweeps_f32(m, m, X, nullptr, nrm32, tol32, 40, &s_flag, &s_off, tab32);
+    {
+        const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+        for (int c = warp; c < m; c += nwarps) {
+            float a = 0.f;
+            for (int r = lane; r < m; r += 32) { const float2 v = X[(size_t)c * m + r]; a += v.x * v.x + v.y * v.y; }
+            a = warp_sum(a);
+            if (lane == 0) {
+                nrm32[c] = a;
+                if (!(a > 1e-30f)) s_bad = 1;
+            }
+        }
+    }
+    __syncthreads();
+    float2 *V1 = A32;                       // the FP32 right singular vectors, m x m, leading dimension m
+    if (!s_bad) {
+        for (int e = tid; e < m * m; e += nt) {   // V[perm[j]][c] = X[j][c] / |x_c|
+            const int j = e % m, c = e / m;
+            const float2 x = X[e];
+            const float s = rsqrt_nr(nrm32[c]);
+            V1[(size_t)c * m + perm[j]] = make_float2(x.x * s, x.y * s);
+        }
+    } else {
+        for (int i = tid; i < rows * m; i += nt) A32[i] = make_float2((float)(H[i].x * sc), (float)(H[i].y * sc));
+        for (int i = tid; i < m * m; i += nt) V32[i] = make_float2((i % m) == (i / m) ? 1.f : 0.f, 0.f);
+        __syncthreads();
+        s32 = 100 + jacobi_sweeps_f32(m, rows, A32, V32, nrm32, tol32, 40, &s_flag, &s_off, tab32);
+        V1 = V32;
+    }
+    __syncthreads();
+    // the k columns of smallest norm (smallest singular values) after the FP32 phase
+    for (int c = tid; c < m; c += nt) {
+        const float s = nrm32[c];
         int below = 0;
         for (int c2 = 0; c2 < m; ++c2) {
             const float s2 = nrm32[c2];
-            below += (s2 < sc) || (s2 == sc && c2 < c);
+            below += (s2 < s) || (s2 == s && c2 < c);
         }
         small_col[c] = below < k ? 1 : 0;
     }
-    // V64 = V32 re-orthonormalised in FP64 by Cholesky QR: S = V^H V = L L^H, V <- V L^{-H}.
-    // V32 is orthonormal to FP32 accuracy, so S is within ~1e-6 of I and the factorisation
-    // is well conditioned.  S lives in the FP32 scratch region, free after phase 1.
-    for (int i = tid; i < m * m; i += blockDim.x) V64[i] = make_double2(V32[i].x, V32[i].y);
-    __syncthreads();
-    double2 *S = (double2 *)A32;            // m x m, column-major
-    for (int e = tid; e < m * m; e += blockDim.x) {
-        const int i = e % m, j = e / m;
-        if (i < j) continue;                // lower triangle S[i][j], i >= j
-        double gr = 0, gi = 0;
-        for (int r = 0; r < m; ++r) {       // S_ij = sum_r conj(V_ri) V_rj
-            const double2 a = V64[(size_t)i * m + r], b = V64[(size_t)j * m + r];
-            gr += a.x * b.x + a.y * b.y;
-            gi += a.x * b.y - a.y * b.x;
-        }
-        S[(size_t)j * m + i] = make_double2(gr, gi);
+    // 2. Vd = V32 (exact); E = V^H V - I; V <- V (I + F), F = -E/2 + 3/8 E^2 - 5/16 E^3 (the
+    // binomial series of (I + E)^(-1/2)): V^H V = I + O(|E|^4).  |E| is about 1e-5 after the
+    // FP32 phase, so E^2 and E^3 need only FP32; E itself is double-float.
+    for (int i = tid; i < m * m; i += nt) {
+        const float2 v = V1[i];
+        dfc d;
+        d.x = dfr(v.x, 0.f);
+        d.y = dfr(v.y, 0.f);
+        Vd[(size_t)(i / m) * ldv + i % m] = d;
     }
     __syncthreads();
-    for (int j = 0; j < m; ++j) {           // right-looking Cholesky, lower triangle in place
-        if (tid == 0) {
-            const double d = sqrt(S[(size_t)j * m + j].x);
-            S[(size_t)j * m + j] = make_double2(d, 0.0);
-            nrm64[0] = 1.0 / d;
+    dfc *E = Ad;                            // m x m, leading dimension m; E[i][j] = <v_i, v_j> - d_ij
+    float2 *Eh = (float2 *)Sc, *E2 = Eh + (size_t)m * m;   // its leading halves, and E^2
+    for (int idx = tid; idx < m * (m + 1) / 2; idx += nt) {
+        int j = 0, i = idx;                 // lower triangle i >= j, column by column
+        while (i >= m - j) { i -= m - j; ++j; }
+        i += j;                             // lanes over i: columns i at stride ldv (odd)
+        const dfc *vi = Vd + (size_t)i * ldv, *vj = Vd + (size_t)j * ldv;
+        dfr gr(i == j ? -1.f : 0.f, 0.f), gi(0.f, 0.f);
+        for (int r = 0; r < m; ++r) {       // conj(v_ri) v_rj; the entries are floats (lo = 0)
+            const dfc x = vi[r], y = vj[r]; // whole 16-byte elements: 4 wavefronts, no conflict
+            gr = df_acc(df_acc(gr, x.x.hi, y.x.hi), x.y.hi, y.y.hi);
+            gi = df_acc(df_acc(gi, x.x.hi, y.y.hi), -x.y.hi, y.x.hi);
         }
-        __syncthreads();
-        const double inv = nrm64[0];
-        for (int i = j + 1 + tid; i < m; i += blockDim.x) {
-            double2 v = S[(size_t)j * m + i];
-            S[(size_t)j * m + i] = make_double2(v.x * inv, v.y * inv);
-        }
-        __syncthreads();
-        const int tail = m - j - 1;
-        for (int e = tid; e < tail * tail; e += blockDim.x) {
-            const int i = j + 1 + e % tail, kcol = j + 1 + e / tail;
-            if (i < kcol) continue;
-            const double2 lij = S[(size_t)j * m + i], lkj = S[(size_t)j * m + kcol];
-            double2 v = S[(size_t)kcol * m + i];   // S_ik -= L_ij conj(L_kj)
-            v.x -= lij.x * lkj.x + lij.y * lkj.y;
-            v.y -= lij.y * lkj.x - lij.x * lkj.y;
-            S[(size_t)kcol * m + i] = v;
-        }
-        __syncthreads();
+        dfc eij, eji;                       // E[i][j] = <v_i, v_j>, E[j][i] its conjugate
+        eij.x = gr;
+        eij.y = gi;
+        eji.x = gr;
+        eji.y = -gi;
+        E[(size_t)j * m + i] = eij;         // column-major
+        E[(size_t)i * m + j] = eji;
+        Eh[(size_t)j * m + i] = make_float2(gr.hi, gi.hi);
+        Eh[(size_t)i * m + j] = make_float2(gr.hi, -gi.hi);
     }
-    for (int j = 0; j < m; ++j) {           // V[:, j] <- (V[:, j] - sum_{k<j} V[:, k] conj(L_jk)) / L_jj
-        const double inv = 1.0 / S[(size_t)j * m + j].x;
-        for (int r = tid; r < m; r += blockDim.x) {
-            double2 v = V64[(size_t)j * m + r];
-            for (int kc = 0; kc < j; ++kc) {
-                const double2 l = S[(size_t)kc * m + j], a = V64[(size_t)kc * m + r];
-                v.x -= a.x * l.x + a.y * l.y;
-                v.y -= a.y * l.x - a.x * l.y;
-            }
-            V64[(size_t)j * m + r] = make_double2(v.x * inv, v.y * inv);
+    __syncthreads();
+    for (int e = tid; e < m * m; e += nt) {
+        const int i = e % m, j = e / m;     // (E E)[i][j] = sum_l E[i][l] E[l][j], lanes over i
+        float sx = 0.f, sy = 0.f;
+        for (int l = 0; l < m; ++l) {
+            const float2 x = Eh[(size_t)l * m + i], y = Eh[(size_t)j * m + l];
+            sx = fmaf(x.x, y.x, fmaf(-x.y, y.y, sx));
+            sy = fmaf(x.x, y.y, fmaf(x.y, y.x, sy));
         }
-        __syncthreads();
+        E2[e] = make_float2(sx, sy);
     }
-    // A64 = H V64
-    for (int i = tid; i < rows * m; i += blockDim.x) {
-        const int r = i % rows, c = i / rows;
-        double2 acc = make_double2(0, 0);
+    __syncthreads();
+    for (int e = tid; e < m * m; e += nt) { // F in place of E
+        const int i = e % m, j = e / m;     // (E E^2)[i][j]
+        float sx = 0.f, sy = 0.f;
+        for (int l = 0; l < m; ++l) {
+            const float2 x = Eh[(size_t)l * m + i], y = E2[(size_t)j * m + l];
+            sx = fmaf(x.x, y.x, fmaf(-x.y, y.y, sx));
+            sy = fmaf(x.x, y.y, fmaf(x.y, y.x, sy));
+        }
+        const float2 q = E2[e];
+        dfc f = E[e];
+        f.x = dfr(-0.5f * f.x.hi, -0.5f * f.x.lo) + dfr(fmaf(0.375f, q.x, -0.3125f * sx), 0.f);
+        f.y = dfr(-0.5f * f.y.hi, -0.5f * f.y.lo) + dfr(fmaf(0.375f, q.y, -0.3125f * sy), 0.f);
+        E[e] = f;
+    }
+    __syncthreads();
+    dfc *T = Sc;                            // m x m, leading dimension m
+    for (int e = tid; e < m * m; e += nt) {
+        const int i = e % m, j = e / m;     // T[i][j] = sum_l V[i][l] F[l][j]
+        dfr sx(0.f, 0.f), sy(0.f, 0.f);
+        for (int l = 0; l < m; ++l) {
+            const dfc v = Vd[(size_t)l * ldv + i], f = E[(size_t)j * m + l];
+            sx = fma(dfr(v.x.hi, 0.f), f.x, sx);
+            sx = fma(dfr(-v.y.hi, 0.f), f.y, sx);
+            sy = fma(dfr(v.x.hi, 0.f), f.y, sy);
+            sy = fma(dfr(v.y.hi, 0.f), f.x, sy);
+        }
+        T[e].x = sx;
+        T[e].y = sy;
+    }
+    __syncthreads();
+    for (int e = tid; e < m * m; e += nt) {
+        dfc &v = Vd[(size_t)(e / m) * ldv + e % m];
+        v.x = v.x + T[e].x;
+        v.y = v.y + T[e].y;
+    }
+    __syncthreads();
+    dfc *Hd = Sc;                           // H as double-float, (m+1) x m
+    for (int i = tid; i < rows * m; i += nt) Hd[i] = to_dfc(make_double2(H[i].x * sc, H[i].y * sc));
+    __syncthreads();
+    for (int e = tid; e < rows * m; e += nt) {
+        const int r = e % rows, c = e / rows;   // A[r][c] = sum_p H[r][p] V[p][c]
+        dfr sx(0.f, 0.f), sy(0.f, 0.f);
         for (int p = 0; p < m; ++p) {
-            const double2 h = H[(size_t)p * rows + r], v = V64[(size_t)c * m + p];
-            acc.x += h.x * v.x - h.y * v.y;
-            acc.y += h.x * v.y + h.y * v.x;
+            const dfc h = Hd[(size_t)p * rows + r], v = Vd[(size_t)c * ldv + p];
+            sx = fma(h.x, v.x, sx);
+            sx = fma(-h.y, v.y, sx);
+            sy = fma(h.x, v.y, sy);
+            sy = fma(h.y, v.x, sy);
         }
-        A64[i] = acc;
+        Ad[e].x = sx;
+        Ad[e].y = sy;
     }
     __syncthreads();
-    const int s64 = jacobi_sweeps<double, true>(m, A64, V64, nrm64, rot, 4.0 * 2.220446049250313e-16 * m, 3, &s_flag,
-                                                &s_off, small_col);
-    for (int c = warp; c < m; c += nwarps) {
-        double a = 0;
-        for (int r = lane; r < rows; r += 32) { double2 v = A64[(size_t)c * rows + r]; a += v.x * v.x + v.y * v.y; }
-        a = warp_sum(a);
-        if (lane == 0) nrm64[c] = a;
-    }
+    // 3. double-float polish of the k smallest.  Sc (H no longer needed) takes the packed pair
+    // table of the flagged pairs, its counts, and the k x m coefficients of polish_small_all.
+    const int mm = m + (m & 1);
+    unsigned short *ptab = (unsigned short *)Sc;
+    int *pcnt = (int *)(((uintptr_t)(ptab + (size_t)(mm - 1) * (mm / 2)) + 15) & ~(uintptr_t)15);
+    float2 *coefs = (float2 *)(((uintptr_t)(pcnt + mm) + 15) & ~(uintptr_t)15);
+    pair_table(m, ptab, pcnt, small_col);
+    for (int c = tid; c < m; c += nt)
+        if (small_col[c]) {
+            int idx = 0;
+            for (int c2 = 0; c2 < c; ++c2) idx += small_col[c2];
+            flag_list[idx] = c;
+        }
     __syncthreads();
-    // rank in descending order (ties broken by column index)
-    for (int c = tid; c < m; c += blockDim.x) {
-        const double sc = nrm64[c];
-        int rank = 0;
+    const int sdf = jacobi_polish_df(m, Ad, Vd, ldv, nrmd, 4.0f * 2.220446e-16f * m, 3, &s_flag, &s_off, ptab, pcnt,
+                                     flag_list, k, coefs);
+    // singular values in descending order (ties broken by column index); the output vectors are
+    // the flagged columns, the only ones polished, in descending order of their values
+    auto greater = [](dfr x, dfr y) { return x.hi > y.hi || (x.hi == y.hi && x.lo > y.lo); };
+    auto same = [](dfr x, dfr y) { return x.hi == y.hi && x.lo == y.lo; };
+    for (int c = tid; c < m; c += nt) {
+        const dfr s = nrmd[c];
+        int rank = 0, rank_f = 0;
         for (int c2 = 0; c2 < m; ++c2) {
-            const double s2 = nrm64[c2];
-            rank += (s2 > sc) || (s2 == sc && c2 < c);
+            const bool before = greater(nrmd[c2], s) || (same(nrmd[c2], s) && c2 < c);
+            rank += before;
+            rank_f += before && small_col[c2];
         }
-        sigma[rank] = sqrt(sc);
-        const int t = rank - (m - k);
-        if (t >= 0)
-            for (int r = 0; r < m; ++r) vs[(size_t)t * m + r] = V64[(size_t)c * m + r];
+        sigma[rank] = sqrt((double)s) / sc;
+        if (small_col[c]) slot_col[rank_f] = c;
     }
-    if (tid == 0 && sweeps_out) *sweeps_out = s32 * 1000 + s64;
+    __syncthreads();
+    for (int e = tid; e < k * m; e += nt) {
+        const dfc v = Vd[(size_t)slot_col[e / m] * ldv + e % m];
+        vs[e] = make_double2((double)v.x, (double)v.y);
+    }
+    if (tid == 0 && sweeps_out) *sweeps_out = s32 * 1000 + sdf;
 }
 
 // ----------------------------------------------------------------- SELL-32 SpMM
@@ -2645,9 +3065,7 @@ void launch_ls(int m, const double2 *H, size_t strideH, const double2 *g, double
     k_ls<<<nsys, 128, smem, st>>>(m, H, strideH, g, y, t, strideC, act);
 }
 
-size_t svd_smem_bytes(int m) {
-    return (sizeof(double2) + sizeof(float2)) * ((size_t)(m + 1) * m + (size_t)m * m);
-}
+size_t svd_smem_bytes(int m) { return svd_work_bytes(m); }
 
 void launch_svd_smallest(int m, int k, const double2 *H, size_t strideH, const int *lead, double2 *vs, double *sigma,
                          double2 *work, int *sweeps,
