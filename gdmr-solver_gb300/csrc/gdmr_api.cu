@@ -398,6 +398,43 @@ extern "C" int gdmrProfileRead(int kernelClass, double *bytes, double *ms, long 
     return GDMR_OK;
 }
 
+// The deflation update's SVD on its own (svDecompHessDMR, gDMR.cu:638): host buffers in and
+// out, device scratch for the call, the current device and the null stream.
+extern "C" int gdmr_hessenberg_svd(int m, int k, const double *H_ri, double *sigma, double *vs_ri, int *sweeps) {
+    const char *W = "gdmr_hessenberg_svd";
+    if (m < 1 || m > 160 || k < 1 || k > m) return fail(GDMR_EINVAL, W, "need 1 <= k <= m <= 160");
+    if (!H_ri || !sigma || !vs_ri) return fail(GDMR_EINVAL, W, "null buffer");
+    const size_t hb = sizeof(double2) * (size_t)(m + 1) * m, vb = sizeof(double2) * (size_t)k * m;
+    double2 *Hd = nullptr, *vsd = nullptr, *work = nullptr;
+    double *sd = nullptr;
+    int *ints = nullptr;                    // [0] = lead system (0), [1] = sweeps
+    auto release = [&]() {
+        cudaFree(Hd);
+        cudaFree(vsd);
+        cudaFree(work);
+        cudaFree(sd);
+        cudaFree(ints);
+    };
+    if (cudaMalloc(&Hd, hb) != cudaSuccess || cudaMalloc(&vsd, vb) != cudaSuccess ||
+        cudaMalloc(&work, svd_smem_bytes(m)) != cudaSuccess || cudaMalloc(&sd, sizeof(double) * m) != cudaSuccess ||
+        cudaMalloc(&ints, 2 * sizeof(int)) != cudaSuccess) {
+        release();
+        return fail(GDMR_ENOMEM, W, "device allocation failed");
+    }
+    cudaError_t e = cudaMemcpy(Hd, H_ri, hb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(ints, 0, 2 * sizeof(int));
+    if (e == cudaSuccess) {
+        launch_svd_smallest(m, k, Hd, 0, ints, vsd, sd, work, ints + 1, 0);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(sigma, sd, sizeof(double) * m, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(vs_ri, vsd, vb, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && sweeps) e = cudaMemcpy(sweeps, ints + 1, sizeof(int), cudaMemcpyDeviceToHost);
+    release();
+    if (e != cudaSuccess) return fail(GDMR_ECUDA, W, cudaGetErrorString(e));
+    return GDMR_OK;
+}
+
 // ================================================================ context API
 // complex128 <-> complex64 helpers used by the context API
 namespace {

@@ -1207,6 +1207,59 @@ __global__ void __launch_bounds__(NT) k_combine(int n, int kk, int m, const type
 }
 
 // ----------------------------------------------------------------- deflation-space update
+// Z_new = [Z V_lead] vs: m x k complex multiply-adds per element, a compute-bound GEMM.  The
+// complex128 engine runs it in double-float on the FP32 pipes (about 2^-48 per operation):
+// m k = 1152 complex FP64 multiply-adds per element at GB300's 1 TFLOP/s FP64 rate took 6.5 ms
+// a cycle on the 96^3 operator, a fifth of the plain FP64 form's kernel time.  The FP64 operands
+// are split into double-float and the results joined back by bit operations, so no FP64
+// instruction sits in the element loop.
+
+// Exact float -> double by bit operations (normal floats, zero, inf/nan; subnormals flush to 0).
+__device__ __forceinline__ double f2d_bits(float f) {
+    const unsigned u = __float_as_uint(f), e = (u >> 23) & 0xffu;
+    const unsigned long long sgn = (unsigned long long)(u >> 31) << 63;
+    if (e == 0) return __longlong_as_double((long long)sgn);
+    const unsigned long long de = e == 0xffu ? 0x7ffull : (unsigned long long)(e - 127u + 1023u);
+    return __longlong_as_double((long long)(sgn | de << 52 | (unsigned long long)(u & 0x7fffffu) << 29));
+}
+// double -> double-float by bit operations: hi = x truncated to 24 significant bits, lo = the
+// remaining 29 bits rounded to float (so hi + lo = x to 2^-47 relative; lo has the sign of hi
+// and is below ulp(hi), a valid, if unnormalised, pair).  |x| outside [2^-70, 2^70) and zero
+// take the conversion instructions.
+__device__ __forceinline__ dfr d2df_bits(double x) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const unsigned hw = (unsigned)(u >> 32), lw = (unsigned)u;
+    const int e = (int)((hw >> 20) & 0x7ffu);
+    if (e < 1023 - 70 || e >= 1023 + 70) {
+        const float h = (float)x;
+        return dfr(h, (float)(x - (double)h));
+    }
+    const unsigned sgn = hw & 0x80000000u;
+    const float hi = __uint_as_float(sgn | (unsigned)(e - 1023 + 127) << 23 | ((hw & 0xfffffu) << 3) | (lw >> 29));
+    const float scale = __uint_as_float((unsigned)(e - 1075 + 127) << 23);   // 2^(e - 1075), a normal float
+    const float lo = (float)(lw & 0x1fffffffu) * scale;
+    return dfr(hi, sgn ? -lo : lo);
+}
+
+// Working type of the deflation GEMM and the conversions in and out of it.
+template <class C> struct ZW { using t = C; };
+template <> struct ZW<double2> { using t = dfc; };
+__device__ __forceinline__ float2 zin(float2 a) { return a; }
+__device__ __forceinline__ dfc zin(dfc a) { return a; }
+__device__ __forceinline__ dfc zin(double2 a) {
+    dfc c;
+    c.x = d2df_bits(a.x);
+    c.y = d2df_bits(a.y);
+    return c;
+}
+template <class C> __device__ __forceinline__ C zout(typename ZW<C>::t a) { return a; }
+template <> __device__ __forceinline__ double2 zout<double2>(dfc a) {
+    return make_double2(f2d_bits(a.x.hi) + f2d_bits(a.x.lo), f2d_bits(a.y.hi) + f2d_bits(a.y.lo));
+}
+// |a|^2 accumulated in the working real type; converted to double once per thread
+__device__ __forceinline__ void zacc_norm(float &s, float2 a) { s = fmaf(a.x, a.x, fmaf(a.y, a.y, s)); }
+__device__ __forceinline__ void zacc_norm(dfr &s, dfc a) { s = rfma(a.x, a.x, rfma(a.y, a.y, s)); }
+
 template <class R, int KB>
 __global__ void __launch_bounds__(NT) k_zupdate(int n, int kk, int m, int k, int t0, const typename CT<R>::t *__restrict__ Z,
                                                 const typename CT<R>::t *__restrict__ V0, size_t strideV,
@@ -1214,39 +1267,46 @@ __global__ void __launch_bounds__(NT) k_zupdate(int n, int kk, int m, int k, int
                                                 typename CT<R>::t *__restrict__ Znew, double2 *__restrict__ partials,
                                                 unsigned *ticket, double *znorm2) {
     using C = typename CT<R>::t;
-    const typename CT<R>::t *__restrict__ V = V0 + (size_t)(*lead) * strideV;
+    using W = typename ZW<C>::t;
+    using WR = decltype(W::x);
+    constexpr bool DF = std::is_same<W, dfc>::value;
+    const C *__restrict__ V = V0 + (size_t)(*lead) * strideV;
     extern __shared__ unsigned char smraw[];
-    C *cs = reinterpret_cast<C *>(smraw);            // m x KB coefficients
+    W *cs = reinterpret_cast<W *>(smraw);            // m x KB coefficients
     __shared__ double red[KB][NW];
     const int nt = min(KB, k - t0), G = gridDim.x, tid = threadIdx.x;
     for (int i = tid; i < m * KB; i += NT) {
         int p = i / KB, t = i % KB;
-        cs[i] = t < nt ? from_d<C>(vs[(size_t)(t0 + t) * m + p]) : czero<C>();
+        cs[i] = t < nt ? from_d<W>(vs[(size_t)(t0 + t) * m + p]) : czero<W>();
     }
     __syncthreads();
-    double nrm[KB];
+    WR nrm_w[KB];
 #pragma unroll
-    for (int t = 0; t < KB; ++t) nrm[t] = 0;
+    for (int t = 0; t < KB; ++t) nrm_w[t] = WR(0.f);
     for (long i = (long)blockIdx.x * NT + tid; i < n; i += (long)G * NT) {
-        C acc[KB];
+        W acc[KB];
 #pragma unroll
-        for (int t = 0; t < KB; ++t) acc[t] = czero<C>();
+        for (int t = 0; t < KB; ++t) acc[t] = czero<W>();
         for (int p = 0; p < m; ++p) {
-            const C b = p < kk ? Z[(size_t)p * n + i] : V[(size_t)(p - kk) * n + i];
+            const W b = zin(p < kk ? Z[(size_t)p * n + i] : V[(size_t)(p - kk) * n + i]);
 #pragma unroll
             for (int t = 0; t < KB; ++t) {
                 cfma(acc[t], cs[p * KB + t], b);
-                if constexpr (std::is_same<C, dfc>::value)
+                if constexpr (DF)
                     if ((p & 3) == 3) acc[t] = canon(acc[t]);
             }
         }
 #pragma unroll
         for (int t = 0; t < KB; ++t) {
             acc[t] = canon(acc[t]);
-            if (t < nt) Znew[(size_t)(t0 + t) * n + i] = acc[t];
-            nrm[t] += abs2_d(acc[t]);
+            if (t < nt) Znew[(size_t)(t0 + t) * n + i] = zout<C>(acc[t]);
+            zacc_norm(nrm_w[t], acc[t]);
+            if constexpr (DF) nrm_w[t] = canon(dfc{nrm_w[t], dfr(0.f, 0.f)}).x;
         }
     }
+    double nrm[KB];
+#pragma unroll
+    for (int t = 0; t < KB; ++t) nrm[t] = (double)nrm_w[t];
     block_sum<KB>(nrm, red);
     double *part = (double *)partials;
     if (tid == 0)
@@ -2070,7 +2130,10 @@ __global__ void __launch_bounds__(1024) k_svd(int m, int k, const double2 *__res
             flag_list[idx] = c;
         }
     __syncthreads();
-    const int sdf = jacobi_polish_df(m, Ad, Vd, ldv, nrmd, 4.0f * 2.220446e-16f * m, 3, &s_flag, &s_off, ptab, pcnt,
+    // Two sweeps when the FP32 vectors are good (the 64 x 64 Helmholtz Hessenbergs); where FP32
+    // could not resolve the small singular values (condition ~1e6 and up) it takes more: 11 for
+    // m = 96 over six decades.
+    const int sdf = jacobi_polish_df(m, Ad, Vd, ldv, nrmd, 4.0f * 2.220446e-16f * m, 30, &s_flag, &s_off, ptab, pcnt,
                                      flag_list, k, coefs);
     // singular values in descending order (ties broken by column index); the output vectors are
     // the flagged columns, the only ones polished, in descending order of their values
@@ -3042,7 +3105,7 @@ void launch_zupdate(int n, int kk, int m, int k, const typename CT<R>::t *Z, con
     int G = num_sms() * 4;
     if (G > chunks) G = chunks;
     for (int t0 = 0; t0 < k; t0 += KB) {
-        size_t smem = (size_t)m * KB * sizeof(C);
+        size_t smem = (size_t)m * KB * sizeof(typename ZW<C>::t);
         k_zupdate<R, KB><<<G, NT, smem, st>>>(n, kk, m, k, t0, Z, V, strideV, lead, vs, Znew, partials, ticket,
                                               znorm2);
     }

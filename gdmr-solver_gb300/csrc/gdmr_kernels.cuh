@@ -219,11 +219,15 @@ void launch_znormalise(int n, int k, const typename CT<R>::t *Znew, const double
 // Batched least squares min ||H_s y - g_s|| (FP64 Givens), t_s = H_s y_s.
 void launch_ls(int m, const double2 *H, size_t strideH, const double2 *g, double2 *y, double2 *t, size_t strideC,
                const int *act, int nsys, cudaStream_t st);
-// Right singular vectors of the k smallest singular values of H ((m+1) x m), FP64 one-sided Jacobi.
-// vs: m x k column-major; sigma: m values (descending); work: global scratch of 3*m*(m+1) double2.
+// Right singular vectors of the k smallest singular values of H ((m+1) x m) in one CTA: FP32
+// pivoted QR and one-sided Jacobi, then a double-float polar correction and restricted Jacobi
+// (about 1e-13).  vs: m x k column-major, vector t for the (m-k+t)-th largest value; sigma: m
+// values (descending); work: global scratch of svd_smem_bytes(m) = 3*m*(m+1) double2.
 // H: Hessenberg of system 0 (system s at H + s*strideH); the lead system is read from device memory.
+// sweeps: 1000 * (FP32 sweeps, +100 when the unpivoted fallback ran) + double-float sweeps.
 void launch_svd_smallest(int m, int k, const double2 *H, size_t strideH, const int *lead, double2 *vs, double *sigma,
                          double2 *work, int *sweeps, cudaStream_t st);
+size_t svd_smem_bytes(int m);
 
 // SELL-32 sparse matrix times a batch of vectors: y_s = A x_s over the active systems.
 struct SellMatrix {

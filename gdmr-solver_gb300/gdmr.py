@@ -58,6 +58,7 @@ SIGNATURES = {
     "gdmrTune": (None, [I]),
     "gdmrTuneReport": (ctypes.c_char_p, []),
     "gdmrTuneForce": (None, [I, I]),
+    "gdmr_hessenberg_svd": (I, [I, I, P, P, P, P]),
     "gdmr_system_set_stencil": (I, [P, I, I, I, P]),
     "gdmr_system_clear_stencil": (I, [P]),
     "gdmr_system_create": (I, [P, I, P, P, P, I, I, I, I, I]),
@@ -127,6 +128,26 @@ def tune(on: bool) -> None:
 def tune_force(projection: int = -1, update: int = -1) -> None:
     """Pins the Gram-Schmidt variants (index as in tune_report; -1 hands back to the tuner)."""
     load().gdmrTuneForce(int(projection), int(update))
+
+
+def hessenberg_svd(H: np.ndarray, k: int, with_sweeps: bool = False):
+    """The deflation update's SVD of a (m+1) x m complex Hessenberg (gdmr_hessenberg_svd):
+    the m singular values in descending order and, as the columns of an m x k array, the right
+    singular vectors of the k smallest (column t belongs to the (m-k+t)-th largest value);
+    with_sweeps adds (FP32 sweeps, double-float sweeps)."""
+    H = np.asarray(H, dtype=np.complex128)
+    rows, m = H.shape
+    if rows != m + 1:
+        raise ValueError("H must be (m+1) x m")
+    Hc = np.ascontiguousarray(H.T)                   # column-major: column j contiguous
+    sigma = np.empty(m, dtype=np.float64)
+    vs = np.empty((k, m), dtype=np.complex128)
+    sw = ctypes.c_int(0)
+    _check(load().gdmr_hessenberg_svd(int(m), int(k), _ptr(Hc), _ptr(sigma), _ptr(vs), ctypes.byref(sw)),
+           "gdmr_hessenberg_svd")
+    if with_sweeps:
+        return sigma, vs.T.copy(), (sw.value // 1000, sw.value % 1000)
+    return sigma, vs.T.copy()
 
 
 def profile_read() -> dict:

@@ -87,6 +87,15 @@ long long gdmrKernelLaunches(void);
 void gdmrProfile(int on);
 void gdmrProfileReset(void);
 int gdmrProfileRead(int kernelClass, double *bytes, double *ms, long long *launches);
+/* The singular value decomposition of the deflation update on its own (svDecompHessDMR,
+ * gDMR.cu:638): H is (m+1) x m complex128 (re, im interleaved), column-major with leading
+ * dimension m+1, in host memory; sigma receives the m singular values in descending order and
+ * vs the right singular vectors of the k smallest (k x m: vector t, of the (m-k+t)-th
+ * largest value, contiguous).  The vectors are accurate to about 1e-13 (double-float), the
+ * other values to FP32 refinement.  sweeps (may be NULL) receives 1000 * (FP32 Jacobi sweeps,
+ * plus 100 if the unpivoted fallback ran) + double-float sweeps.  Runs on the current device
+ * with device scratch of its own.  1 <= k <= m <= 160, else GDMR_EINVAL. */
+int gdmr_hessenberg_svd(int m, int k, const double *H, double *sigma, double *vs, int *sweeps);
 /* Gram-Schmidt kernel autotuning: the first launch of a shape times the kernel variants
  * and keeps the fastest for the process (on by default; off selects the first variant).
  * The report lists one line per tuned shape with the time of every variant. */
