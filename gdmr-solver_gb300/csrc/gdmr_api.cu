@@ -380,6 +380,7 @@ extern "C" void gdmrLastStats(gdmr_stats *out) {
 
 // ================================================================ instrumentation
 extern "C" long long gdmrKernelLaunches(void) { return launch_count(); }
+extern "C" unsigned gdmrAsyncTimeouts(void) { return wproj_tc_timeouts() + bulk_timeouts(); }
 extern "C" void gdmrProfile(int on) { profile_enable(on != 0); }
 extern "C" void gdmrProfileReset(void) { profile_reset(); }
 extern "C" void gdmrTune(int on) { tune_enable(on != 0); }

@@ -492,6 +492,505 @@ __global__ void __launch_bounds__(NT, PF ? 2 : min_blocks<typename CT<R>::t>(EPT
     }
 }
 
+// ----------------------------------------------------------------- persistent Gram-Schmidt
+// The two Gram-Schmidt kernels for a few systems at 16 bytes an element (complex128, double-
+// float): grid (systems, G) with about two CTAs per SM in all, each CTA striding over the
+// element chunks of NT x EPT.  A projection group of PU basis vectors accumulates over every
+// chunk of its CTA before its one warp reduction, and the update's norm and cross term are
+// summed once per CTA.  In the chunked kernels above, one CTA per chunk, those reductions came
+// once per 4 elements a thread: the double-float warp butterflies and the FP64 block sums
+// (one FP64 warp instruction is ~64 clocks of a scheduler on GB300) were about half of the
+// double-float projection's 93 instructions per complex multiply-add.
+inline int persist_grid(int n, int ept, int nsys) {
+    const long nch = ((long)n + (long)NT * ept - 1) / ((long)NT * ept);
+    long G = (2L * num_sms() + nsys - 1) / nsys;
+    if (G > nch) G = nch;
+    return G < 1 ? 1 : (int)G;
+}
+
+template <class R, int EPT, int PU>
+__global__ void __launch_bounds__(NT, 2)
+    k_mdot_persist(int n, const typename CT<R>::t *__restrict__ segA, int qa,
+                   const typename CT<R>::t *__restrict__ segB0, size_t strideB, int qb,
+                   const typename CT<R>::t *__restrict__ w0, size_t strideW, const int *__restrict__ act,
+                   double2 *__restrict__ partials, int qmax, unsigned *tickets, double2 *__restrict__ coef0,
+                   size_t strideC, SysState *state, int skip_broken) {
+    using C = typename CT<R>::t;
+    const int slot = blockIdx.x, s = act[slot], G = gridDim.y;
+    if (skip_broken && state[s].broken) return;
+    const C *segB = segB0 + (size_t)s * strideB;
+    const C *w = w0 + (size_t)s * strideW;
+    const int q = qa + qb, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __shared__ C wsum[NW][QMAX];
+    const long span = (long)NT * EPT, nch = ((long)n + span - 1) / span;
+    for (int p0 = 0; p0 < q; p0 += PU) {
+        const C *vp[PU];
+#pragma unroll
+        for (int u = 0; u < PU; ++u) {
+            const int p = p0 + u < q ? p0 + u : q - 1;   // duplicate the last vector; its result is dropped
+            vp[u] = p < qa ? segA + (size_t)p * n : segB + (size_t)(p - qa) * n;
+        }
+        C a[PU];
+#pragma unroll
+        for (int u = 0; u < PU; ++u) a[u] = czero<C>();
+        for (long ch = blockIdx.y; ch < nch; ch += G) {
+            const long c0 = ch * span + tid;
+            C wv[EPT], vv[PU][EPT];
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) wv[e] = c0 + (long)e * NT < n ? w[c0 + (long)e * NT] : czero<C>();
+#pragma unroll
+            for (int u = 0; u < PU; ++u)
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) vv[u][e] = c0 + (long)e * NT < n ? vp[u][c0 + (long)e * NT] : czero<C>();
+#pragma unroll
+            for (int u = 0; u < PU; ++u) {
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) cdotacc(a[u], vv[u][e], wv[e]);
+                a[u] = canon(a[u]);
+            }
+        }
+        if constexpr (std::is_same<C, dfc>::value) {
+            df_reduce_scatter<PU>(a, &wsum[warp][0], p0, q, lane);
+        } else {
+#pragma unroll
+            for (int u = 0; u < PU; ++u) {
+                a[u].x = warp_sum(a[u].x);
+                a[u].y = warp_sum(a[u].y);
+                if (lane == 0 && p0 + u < q) wsum[warp][p0 + u] = a[u];
+            }
+        }
+    }
+    __syncthreads();
+    const int chunk = blockIdx.y;
+    double *part = (double *)partials + (size_t)slot * qmax * 2 * G;   // [p][re|im][G]
+    for (int p = tid; p < q; p += NT) {
+        double re = 0, im = 0;
+#pragma unroll
+        for (int ww = 0; ww < NW; ++ww) { re += (double)wsum[ww][p].x; im += (double)wsum[ww][p].y; }
+        double *pp = part + (size_t)p * 2 * G;
+        pp[chunk] = re;
+        pp[G + chunk] = im;
+    }
+    if (!arrive_last(&tickets[slot], G)) return;
+    double2 *coef = coef0 + (size_t)s * strideC;
+    for (int p = warp; p < q; p += NW) {
+        const double *pp = part + (size_t)p * 2 * G;
+        double re = 0, im = 0;
+        for (int g = lane; g < G; g += 32) { re += __ldcg(pp + g); im += __ldcg(pp + G + g); }
+        re = warp_sum(re);
+        im = warp_sum(im);
+        if (lane == 0) coef[p] = make_double2(re, im);
+    }
+    if (tid == 0) tickets[slot] = 0;
+}
+
+template <class R, int EPT, int PU>
+__global__ void __launch_bounds__(NT, 2)
+    k_update_persist(int n, const typename CT<R>::t *__restrict__ segA, int qa,
+                     const typename CT<R>::t *__restrict__ segB0, size_t strideB, int qb,
+                     const typename CT<R>::t *__restrict__ w0, size_t strideW, typename CT<R>::t *__restrict__ out0,
+                     size_t strideO, const int *__restrict__ act, const double2 *__restrict__ coef0, size_t strideC,
+                     double2 *__restrict__ partials, unsigned *tickets, SysState *state, FinishArgs fin,
+                     int skip_broken) {
+    using C = typename CT<R>::t;
+    const int slot = blockIdx.x, s = act[slot], G = gridDim.y;
+    if (skip_broken && state[s].broken) return;
+    const C *segB = segB0 + (size_t)s * strideB;
+    const C *w = w0 + (size_t)s * strideW;
+    C *out = out0 + (size_t)s * strideO;
+    const int q = qa + qb, tid = threadIdx.x;
+    __shared__ C cs[QMAX];
+    __shared__ double red[3][NW];
+    const double2 *coef = coef0 + (size_t)s * strideC;
+    for (int p = tid; p < q; p += NT) cs[p] = from_d<C>(coef[p]);
+    __syncthreads();
+    const long span = (long)NT * EPT, nch = ((long)n + span - 1) / span;
+    C ln = czero<C>(), lc = czero<C>();
+    for (long ch = blockIdx.y; ch < nch; ch += G) {
+        const long c0 = ch * span + tid;
+        C org[EPT], acc[EPT];
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            org[e] = c0 + (long)e * NT < n ? w[c0 + (long)e * NT] : czero<C>();
+            acc[e] = org[e];
+        }
+        for (int p0 = 0; p0 < q; p0 += PU) {
+            C vv[PU][EPT];
+#pragma unroll
+            for (int u = 0; u < PU; ++u) {
+                const int p = p0 + u < q ? p0 + u : q - 1;
+                const C *vp = p < qa ? segA + (size_t)p * n : segB + (size_t)(p - qa) * n;
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) vv[u][e] = c0 + (long)e * NT < n ? vp[c0 + (long)e * NT] : czero<C>();
+            }
+#pragma unroll
+            for (int u = 0; u < PU; ++u) {
+                if (p0 + u < q) {
+                    const C c = cs[p0 + u];
+#pragma unroll
+                    for (int e = 0; e < EPT; ++e) cfms(acc[e], c, vv[u][e]);
+                }
+            }
+            if constexpr (std::is_same<C, dfc>::value) {   // keep double-float chains short
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) acc[e] = canon(acc[e]);
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            acc[e] = canon(acc[e]);
+            if (c0 + (long)e * NT < n) out[c0 + (long)e * NT] = acc[e];
+            cdotacc(ln, acc[e], acc[e]);
+            cdotacc(lc, acc[e], org[e]);
+        }
+        ln = canon(ln);
+        lc = canon(lc);
+    }
+    double v[3] = {(double)ln.x, (double)lc.x, (double)lc.y};
+    block_sum<3>(v, red);
+    const int chunk = blockIdx.y;
+    double *part = (double *)partials + (size_t)slot * 3 * G;
+    if (tid == 0) {
+        part[chunk] = v[0];
+        part[G + chunk] = v[1];
+        part[2 * G + chunk] = v[2];
+    }
+    if (!arrive_last(&tickets[slot], G)) return;
+    double tot[3];
+    __syncthreads();
+    sum_partials<3>(part, G, tot, red);
+    if (tid == 0) {
+        run_finish(fin, s, state[s], tot[0], tot[1], tot[2]);
+        tickets[slot] = 0;
+    }
+}
+
+// ----------------------------------------------------------------- bulk-copy Gram-Schmidt (double-float)
+// The double-float projection and update as copy/compute pipelines: one CTA per SM, a producer
+// warp streams 8 KB vector tiles (512 complex double-float elements) into shared memory with
+// cp.async.bulk (the TMA engine, no tensor map), and eight consumer warps compute from shared
+// memory behind "full"/"empty" mbarriers.  The register-tiled kernels above issue their loads
+// and then wait for them (ncu: 3.3 long-scoreboard stalls per issue); here 4-5 stages (~160 KB)
+// are in flight per SM while the consumers work (0.5 long-scoreboard stalls per issue).
+// Measured on the 96^3 plain fp64e solve (8 vectors): 38.8 us against 32.7 us for the
+// persistent register-tiled projection, 63 against 45 us for the update; the consumers'
+// double-float arithmetic (44 FP32 instructions per complex multiply-add) issues at ~39% with
+// 2 warps a scheduler, and 16 consumer warps measured slower still (42.8 us).  They stay as
+// tuner candidates.  Every mbarrier wait is bounded (about two seconds
+// of clock): a timeout is counted in g_bulk_timeouts, the kernel stops issuing and consuming,
+// and the producer waits (bounded) for the copies it issued before the CTA exits.
+constexpr int BK_TILE = 512;                   // elements per vector tile (8 KB)
+constexpr int BK_CONS = 256;                   // consumer threads, 8 warps; warp 8 produces
+constexpr int BK_CW = BK_CONS / 32;            // consumer warps
+constexpr int BK_THREADS = BK_CONS + 32;
+constexpr int BK_EPT = BK_TILE / BK_CONS;      // elements per consumer thread and tile
+constexpr int BK_PU = 4;                       // vector tiles per stage
+constexpr int BK_MSTAGES = 4, BK_USTAGES = 5;
+constexpr long long BK_WAIT_CYCLES = 4000000000LL;
+__device__ unsigned g_bulk_timeouts = 0;
+
+__device__ __forceinline__ uint32_t bk_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void bk_init(uint32_t a, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void bk_arrive(uint32_t a) {
+    asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(a) : "memory");
+}
+__device__ __forceinline__ void bk_arrive_tx(uint32_t a, uint32_t bytes) {
+    asm volatile("{\n.reg .b64 st;\nmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n" ::"r"(a), "r"(bytes)
+                 : "memory");
+}
+// global -> shared bulk copy: 16-byte aligned addresses, size a multiple of 16
+__device__ __forceinline__ void bk_copy(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ bool bk_wait(uint32_t a, uint32_t parity, volatile int *abort) {
+    const long long t0 = clock64();
+    while (true) {
+        uint32_t ok;
+        asm volatile("{\n.reg .pred P;\nmbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\nselp.b32 %0, 1, 0, P;\n}\n"
+                     : "=r"(ok) : "r"(a), "r"(parity) : "memory");
+        if (ok) return true;
+        if ((abort && *abort) || clock64() - t0 > BK_WAIT_CYCLES) return false;
+    }
+}
+// lane 0 waits, the warp follows its verdict; a timeout raises the CTA's abort flag
+__device__ __forceinline__ bool bk_warp_wait(uint32_t a, uint32_t parity, volatile int *abort, int lane) {
+    int ok = 1;
+    if (lane == 0) {
+        ok = bk_wait(a, parity, abort);
+        if (!ok && !*abort) {
+            atomicAdd(&g_bulk_timeouts, 1u);
+            *abort = 1;
+        }
+    }
+    return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+// Sum of three doubles over the warps of a pipeline CTA; the result is valid in thread 0.
+__device__ __forceinline__ void bk_block_sum3(double (&v)[3], double (*red)[BK_CW + 1]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) v[j] = warp_sum(v[j]);
+    if (lane == 0)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) red[j][warp] = v[j];
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            double t = 0;
+            for (int ww = 0; ww < BK_CW + 1; ++ww) t += red[j][ww];
+            v[j] = t;
+        }
+}
+__host__ __device__ constexpr size_t bk_mdot_smem() { return (size_t)BK_MSTAGES * (BK_PU + 1) * BK_TILE * sizeof(dfc); }
+__host__ __device__ constexpr size_t bk_update_smem() { return (size_t)BK_USTAGES * BK_PU * BK_TILE * sizeof(dfc); }
+
+// The producer's side of a pipeline over `total` stages: stage k goes to buffer k % NS after
+// the consumers released that buffer's previous use; items(k, j) gives the source of tile j of
+// stage k (nullptr: no tile) and bytes(k) the size of every tile of the stage.  Afterwards it
+// waits for the last use of each buffer, so no copy is in flight when the CTA exits.
+template <int NS, int PER, class Items, class Bytes>
+__device__ void bk_produce(long total, unsigned char *base, unsigned long long *full, unsigned long long *empty,
+                           volatile int *abort, Items items, Bytes bytes) {
+    long last[NS];
+#pragma unroll
+    for (int b = 0; b < NS; ++b) last[b] = -1;
+    for (long k = 0; k < total && !*abort; ++k) {
+        const int b = (int)(k % NS);
+        const long use = k / NS;
+        if (use > 0 && !bk_wait(bk_u32(&empty[b]), (uint32_t)((use - 1) & 1), abort)) {
+            if (!*abort) { atomicAdd(&g_bulk_timeouts, 1u); *abort = 1; }
+            break;
+        }
+        const uint32_t nb = bytes(k);
+        int cnt = 0;
+#pragma unroll
+        for (int j = 0; j < PER; ++j) cnt += items(k, j) != nullptr;
+        bk_arrive_tx(bk_u32(&full[b]), nb * cnt);
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            const void *src = items(k, j);
+            if (src) bk_copy(bk_u32(base + ((size_t)b * PER + j) * BK_TILE * sizeof(dfc)), src, nb, bk_u32(&full[b]));
+        }
+        last[b] = use;
+    }
+#pragma unroll
+    for (int b = 0; b < NS; ++b)
+        if (last[b] >= 0 && !bk_wait(bk_u32(&full[b]), (uint32_t)(last[b] & 1), nullptr)) atomicAdd(&g_bulk_timeouts, 1u);
+}
+
+__global__ void __launch_bounds__(BK_THREADS, 1)
+    k_mdot_bulk(int n, const dfc *__restrict__ segA, int qa, const dfc *__restrict__ segB0, size_t strideB, int qb,
+                const dfc *__restrict__ w0, size_t strideW, const int *__restrict__ act, double2 *__restrict__ partials,
+                int qmax, unsigned *tickets, double2 *__restrict__ coef0, size_t strideC, SysState *state,
+                int skip_broken) {
+    extern __shared__ __align__(128) unsigned char bk_sm[];
+    __shared__ __align__(8) unsigned long long full[BK_MSTAGES], empty[BK_MSTAGES];
+    __shared__ int s_abort;
+    __shared__ dfc wsum[BK_CW][QMAX];
+    const int slot = blockIdx.x, s = act[slot], G = gridDim.y, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (skip_broken && state[s].broken) return;
+    const dfc *segB = segB0 + (size_t)s * strideB;
+    const dfc *w = w0 + (size_t)s * strideW;
+    const int q = qa + qb, ngroups = (q + BK_PU - 1) / BK_PU;
+    const long ntiles = ((long)n + BK_TILE - 1) / BK_TILE;
+    const long my = blockIdx.y < ntiles ? (ntiles - blockIdx.y + G - 1) / G : 0;   // tiles of this CTA
+    const long total = (long)ngroups * my;                                         // stages, group-major
+    if (tid == 0) {
+        for (int b = 0; b < BK_MSTAGES; ++b) {
+            bk_init(bk_u32(&full[b]), 1);
+            bk_init(bk_u32(&empty[b]), BK_CW);
+        }
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    auto vec = [&](int p) { return p < qa ? segA + (size_t)p * n : segB + (size_t)(p - qa) * n; };
+    if (warp == BK_CW) {
+        if (lane == 0)
+            bk_produce<BK_MSTAGES, BK_PU + 1>(
+                total, bk_sm, full, empty, &s_abort,
+                [&](long k, int j) -> const void * {
+                    const int g = (int)(k / my);
+                    const long e0 = (blockIdx.y + (k % my) * G) * (long)BK_TILE;
+                    if (j == 0) return w + e0;
+                    const int p = g * BK_PU + j - 1;
+                    return vec(p < q ? p : q - 1) + e0;   // the last group repeats the last vector
+                },
+                [&](long k) -> uint32_t {
+                    const long e0 = (blockIdx.y + (k % my) * G) * (long)BK_TILE;
+                    return (uint32_t)((n - e0 < BK_TILE ? n - e0 : BK_TILE) * sizeof(dfc));
+                });
+    } else {
+        bool ok = true;
+        for (int g = 0; g < ngroups && ok; ++g) {
+            dfc a[BK_PU];
+#pragma unroll
+            for (int u = 0; u < BK_PU; ++u) a[u] = czero<dfc>();
+            for (long i = 0; i < my; ++i) {
+                const long k = (long)g * my + i;
+                const int b = (int)(k % BK_MSTAGES);
+                if (!bk_warp_wait(bk_u32(&full[b]), (uint32_t)((k / BK_MSTAGES) & 1), &s_abort, lane)) { ok = false; break; }
+                const dfc *st = reinterpret_cast<const dfc *>(bk_sm) + (size_t)b * (BK_PU + 1) * BK_TILE;
+                const long e0 = (blockIdx.y + i * G) * (long)BK_TILE;
+#pragma unroll
+                for (int e = 0; e < BK_EPT; ++e) {
+                    const int idx = e * BK_CONS + tid;
+                    if (e0 + idx < n) {
+                        const dfc wv = st[idx];
+#pragma unroll
+                        for (int u = 0; u < BK_PU; ++u) cdotacc(a[u], st[(size_t)(u + 1) * BK_TILE + idx], wv);
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) bk_arrive(bk_u32(&empty[b]));
+#pragma unroll
+                for (int u = 0; u < BK_PU; ++u) a[u] = canon(a[u]);
+            }
+            if (ok) df_reduce_scatter<BK_PU>(a, &wsum[warp][0], g * BK_PU, q, lane);
+        }
+    }
+    __syncthreads();
+    const int chunk = blockIdx.y;
+    double *part = (double *)partials + (size_t)slot * qmax * 2 * G;   // [p][re|im][G]
+    for (int p = tid; p < q; p += blockDim.x) {
+        double re = 0, im = 0;
+#pragma unroll
+        for (int ww = 0; ww < BK_CW; ++ww) { re += (double)wsum[ww][p].x; im += (double)wsum[ww][p].y; }
+        double *pp = part + (size_t)p * 2 * G;
+        pp[chunk] = re;
+        pp[G + chunk] = im;
+    }
+    if (!arrive_last(&tickets[slot], G)) return;
+    double2 *coef = coef0 + (size_t)s * strideC;
+    for (int p = warp; p < q; p += BK_CW + 1) {
+        const double *pp = part + (size_t)p * 2 * G;
+        double re = 0, im = 0;
+        for (int g = lane; g < G; g += 32) { re += __ldcg(pp + g); im += __ldcg(pp + G + g); }
+        re = warp_sum(re);
+        im = warp_sum(im);
+        if (lane == 0) coef[p] = make_double2(re, im);
+    }
+    if (tid == 0) tickets[slot] = 0;
+}
+
+__global__ void __launch_bounds__(BK_THREADS, 1)
+    k_update_bulk(int n, const dfc *__restrict__ segA, int qa, const dfc *__restrict__ segB0, size_t strideB, int qb,
+                  const dfc *__restrict__ w0, size_t strideW, dfc *__restrict__ out0, size_t strideO,
+                  const int *__restrict__ act, const double2 *__restrict__ coef0, size_t strideC,
+                  double2 *__restrict__ partials, unsigned *tickets, SysState *state, FinishArgs fin,
+                  int skip_broken) {
+    extern __shared__ __align__(128) unsigned char bk_sm[];
+    __shared__ __align__(8) unsigned long long full[BK_USTAGES], empty[BK_USTAGES];
+    __shared__ int s_abort;
+    __shared__ dfc cs[QMAX];
+    __shared__ double red9[3][BK_CW + 1];
+    const int slot = blockIdx.x, s = act[slot], G = gridDim.y, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (skip_broken && state[s].broken) return;
+    const dfc *segB = segB0 + (size_t)s * strideB;
+    const dfc *w = w0 + (size_t)s * strideW;
+    dfc *out = out0 + (size_t)s * strideO;
+    const int q = qa + qb, per_tile = (q + 1 + BK_PU - 1) / BK_PU;   // stages per tile: [w, v_0 .. v_q-1]
+    const long ntiles = ((long)n + BK_TILE - 1) / BK_TILE;
+    const long my = blockIdx.y < ntiles ? (ntiles - blockIdx.y + G - 1) / G : 0;
+    const long total = (long)per_tile * my;                                        // stages, tile-major
+    const double2 *coef = coef0 + (size_t)s * strideC;
+    for (int p = tid; p < q; p += blockDim.x) cs[p] = from_d<dfc>(coef[p]);
+    if (tid == 0) {
+        for (int b = 0; b < BK_USTAGES; ++b) {
+            bk_init(bk_u32(&full[b]), 1);
+            bk_init(bk_u32(&empty[b]), BK_CW);
+        }
+        s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    dfc ln = czero<dfc>(), lc = czero<dfc>();
+    if (warp == BK_CW) {
+        if (lane == 0)
+            bk_produce<BK_USTAGES, BK_PU>(
+                total, bk_sm, full, empty, &s_abort,
+                [&](long k, int j) -> const void * {
+                    const long e0 = (blockIdx.y + (k / per_tile) * G) * (long)BK_TILE;
+                    const int li = (int)(k % per_tile) * BK_PU + j;   // 0: w, 1 + p: v_p
+                    if (li > q) return nullptr;
+                    if (li == 0) return w + e0;
+                    const int p = li - 1;
+                    return (p < qa ? segA + (size_t)p * n : segB + (size_t)(p - qa) * n) + e0;
+                },
+                [&](long k) -> uint32_t {
+                    const long e0 = (blockIdx.y + (k / per_tile) * G) * (long)BK_TILE;
+                    return (uint32_t)((n - e0 < BK_TILE ? n - e0 : BK_TILE) * sizeof(dfc));
+                });
+    } else {
+        bool ok = true;
+        for (long i = 0; i < my && ok; ++i) {
+            const long e0 = (blockIdx.y + i * G) * (long)BK_TILE;
+            dfc org[BK_EPT], acc[BK_EPT];
+            for (int c = 0; c < per_tile; ++c) {
+                const long k = i * per_tile + c;
+                const int b = (int)(k % BK_USTAGES);
+                if (!bk_warp_wait(bk_u32(&full[b]), (uint32_t)((k / BK_USTAGES) & 1), &s_abort, lane)) { ok = false; break; }
+                const dfc *st = reinterpret_cast<const dfc *>(bk_sm) + (size_t)b * BK_PU * BK_TILE;
+#pragma unroll
+                for (int j = 0; j < BK_PU; ++j) {
+                    const int li = c * BK_PU + j;
+                    if (li > q) break;
+#pragma unroll
+                    for (int e = 0; e < BK_EPT; ++e) {
+                        const dfc v = st[(size_t)j * BK_TILE + e * BK_CONS + tid];
+                        if (li == 0) {
+                            org[e] = v;
+                            acc[e] = v;
+                        } else {
+                            cfms(acc[e], cs[li - 1], v);
+                        }
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) bk_arrive(bk_u32(&empty[b]));
+#pragma unroll
+                for (int e = 0; e < BK_EPT; ++e) acc[e] = canon(acc[e]);
+            }
+            if (!ok) break;
+#pragma unroll
+            for (int e = 0; e < BK_EPT; ++e) {
+                const long idx = e0 + e * BK_CONS + tid;
+                if (idx < n) {
+                    out[idx] = acc[e];
+                    cdotacc(ln, acc[e], acc[e]);
+                    cdotacc(lc, acc[e], org[e]);
+                }
+            }
+            ln = canon(ln);
+            lc = canon(lc);
+        }
+    }
+    double v[3] = {(double)ln.x, (double)lc.x, (double)lc.y};   // the producer warp adds zeros
+    bk_block_sum3(v, red9);
+    const int chunk = blockIdx.y;
+    double *part = (double *)partials + (size_t)slot * 3 * G;
+    if (tid == 0) {
+        part[chunk] = v[0];
+        part[G + chunk] = v[1];
+        part[2 * G + chunk] = v[2];
+    }
+    if (!arrive_last(&tickets[slot], G)) return;
+    double tot[3] = {0, 0, 0};
+    if (tid < BK_CONS)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            for (int g = tid; g < G; g += BK_CONS) tot[j] += __ldcg(part + (size_t)j * G + g);
+    bk_block_sum3(tot, red9);
+    if (tid == 0) {
+        run_finish(fin, s, state[s], tot[0], tot[1], tot[2]);
+        tickets[slot] = 0;
+    }
+}
+
 // ----------------------------------------------------------------- batched W projection
 // coef_s[p] = <W_p, y_s> for every active system s and deflation vector p: the shared part
 // of a batched projection as one split-K product, so W is read once for the whole batch
@@ -2588,6 +3087,12 @@ size_t scratch_doubles(int qmax, int nsys, int n) {
     return per_chunk + grid_stride;
 }
 
+unsigned bulk_timeouts() {
+    unsigned v = 0;
+    cudaMemcpyFromSymbol(&v, g_bulk_timeouts, sizeof v);
+    return v;
+}
+
 namespace {
 // Raises a kernel's dynamic shared-memory limit once per (kernel, device) to the most the
 // device allows next to the kernel's static shared memory, so no attribute call happens
@@ -2917,6 +3422,37 @@ int mdot_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const typ
                                      coef, strideC, state, skip_broken, st);
             return 1;
         }
+        if constexpr (std::is_same<R, dfr>::value) {
+            if (v == 11) {   // bulk-copy pipeline, one CTA per SM
+                const long ntiles = ((long)n + BK_TILE - 1) / BK_TILE;
+                long G = num_sms() / nsys;
+                if (G > ntiles) G = ntiles;
+                if (G < 1) G = 1;
+                if ((size_t)nsys * qmax * 2 * G <= cap) {
+                    allow_smem(k_mdot_bulk, bk_mdot_smem());
+                    k_mdot_bulk<<<grid2(nsys, (int)G), BK_THREADS, bk_mdot_smem(), st>>>(
+                        n, segA, qa, segB, strideB, qb, w, strideW, act, partials, qmax, tickets, coef, strideC, state,
+                        skip_broken ? 1 : 0);
+                    return 1;
+                }
+                v = 0;
+            }
+        }
+        if (v == 9 || v == 10) {   // persistent: (4 elements, 2 vectors) or (2, 4)
+            const int ept = v == 9 ? 4 : 2, G = persist_grid(n, ept, nsys);
+            if ((size_t)nsys * qmax * 2 * G <= cap) {
+                if (v == 9)
+                    k_mdot_persist<R, 4, 2><<<grid2(nsys, G), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW,
+                                                                           act, partials, qmax, tickets, coef, strideC,
+                                                                           state, skip_broken ? 1 : 0);
+                else
+                    k_mdot_persist<R, 2, 4><<<grid2(nsys, G), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w, strideW,
+                                                                           act, partials, qmax, tickets, coef, strideC,
+                                                                           state, skip_broken ? 1 : 0);
+                return 1;
+            }
+            v = 0;
+        }
     }
     if constexpr (sizeof(R) == 4) {
         static const int ept_of[9] = {8, 8, 16, 8, 2, 1, 4, 4, 1};
@@ -2961,7 +3497,7 @@ void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT
     };
     int v = 0;
     if (forced_variant(0) >= 0) v = forced_variant(0);
-    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(prec_key<R>(), 0, n, nsys, qa, sizeof(R) == 4 ? 11 : 9, st, run);
+    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(prec_key<R>(), 0, n, nsys, qa, sizeof(R) == 4 ? 11 : std::is_same<R, dfr>::value ? 12 : 11, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)
@@ -3019,6 +3555,39 @@ int update_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const t
                                        strideC, partials, tickets, state, fin, skip_broken, st);
             return 1;
         }
+        if constexpr (std::is_same<R, dfr>::value) {
+            if (v == 10) {   // bulk-copy pipeline, one CTA per SM
+                const long ntiles = ((long)n + BK_TILE - 1) / BK_TILE;
+                long G = num_sms() / nsys;
+                if (G > ntiles) G = ntiles;
+                if (G < 1) G = 1;
+                if ((size_t)nsys * 3 * G <= cap) {
+                    allow_smem(k_update_bulk, bk_update_smem());
+                    k_update_bulk<<<grid2(nsys, (int)G), BK_THREADS, bk_update_smem(), st>>>(
+                        n, segA, qa, segB, strideB, qb, w, strideW, out, strideO, act, coef, strideC, partials, tickets,
+                        state, fin, skip_broken ? 1 : 0);
+                    return 1;
+                }
+                v = 0;
+            }
+        }
+        if (v == 8 || v == 9) {   // persistent: (4 elements, 2 vectors) or (2, 4)
+            const int ept = v == 8 ? 4 : 2, G = persist_grid(n, ept, nsys);
+            if ((size_t)nsys * 3 * G <= cap) {
+                if (v == 8)
+                    k_update_persist<R, 4, 2><<<grid2(nsys, G), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w,
+                                                                             strideW, out, strideO, act, coef, strideC,
+                                                                             partials, tickets, state, fin,
+                                                                             skip_broken ? 1 : 0);
+                else
+                    k_update_persist<R, 2, 4><<<grid2(nsys, G), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w,
+                                                                             strideW, out, strideO, act, coef, strideC,
+                                                                             partials, tickets, state, fin,
+                                                                             skip_broken ? 1 : 0);
+                return 1;
+            }
+            v = 0;
+        }
     }
     if constexpr (sizeof(R) == 4) {
         static const int ept_of[8] = {8, 8, 16, 8, 2, 1, 4, 4};
@@ -3063,7 +3632,7 @@ void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename 
     int v = 0;
     if (forced_variant(1) >= 0) v = forced_variant(1);
     else if (representative(nsys, qa, qb) && !profile_enabled())
-        v = tuned_variant(prec_key<R>(), 1, n, nsys, qa, sizeof(R) == 4 ? 10 : 8, st, run);
+        v = tuned_variant(prec_key<R>(), 1, n, nsys, qa, sizeof(R) == 4 ? 10 : std::is_same<R, dfr>::value ? 11 : 10, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)

@@ -191,6 +191,8 @@ int launch_wapply_tc(int n, int kk, const float2 *W, double2 *coef, size_t strid
                      float2 *P, size_t strideP, int unit_idx, cudaStream_t st);
 // mbarrier waits of the tensor-core kernels that ran out of time (0 in a healthy process).
 unsigned wproj_tc_timeouts();
+// Bounded mbarrier waits of the bulk-copy Gram-Schmidt pipelines that ran out (0 in a healthy run).
+unsigned bulk_timeouts();
 
 // out1 (and out2 if non-null) = alpha_s * in; zeros when the system broke down.
 template <class R>

@@ -58,6 +58,7 @@ SIGNATURES = {
     "gdmrTune": (None, [I]),
     "gdmrTuneReport": (ctypes.c_char_p, []),
     "gdmrTuneForce": (None, [I, I]),
+    "gdmrAsyncTimeouts": (ctypes.c_uint, []),
     "gdmr_hessenberg_svd": (I, [I, I, P, P, P, P]),
     "gdmr_system_set_stencil": (I, [P, I, I, I, P]),
     "gdmr_system_clear_stencil": (I, [P]),
@@ -123,6 +124,11 @@ def tune_report() -> str:
 
 def tune(on: bool) -> None:
     load().gdmrTune(1 if on else 0)
+
+
+def async_timeouts() -> int:
+    """Bounded mbarrier waits of the pipelined kernels that ran out since load (0 when healthy)."""
+    return int(load().gdmrAsyncTimeouts())
 
 
 def tune_force(projection: int = -1, update: int = -1) -> None:

@@ -84,6 +84,10 @@ void gdmrLastStats(gdmr_stats *out);
  * w - [W V] c, 2 operator products, 3 cycle-end combinations, 4 deflation
  * update, 5 FP64 true residual, 6 least squares, 7 SVD, 8 other. */
 long long gdmrKernelLaunches(void);
+/* Bounded mbarrier waits (tensor-core and bulk-copy pipelines) that ran out since load: every
+ * such wait gives up after about two seconds and the kernel returns with its results unset, so
+ * a nonzero count means a result of this process is not to be trusted. */
+unsigned gdmrAsyncTimeouts(void);
 void gdmrProfile(int on);
 void gdmrProfileReset(void);
 int gdmrProfileRead(int kernelClass, double *bytes, double *ms, long long *launches);
