@@ -508,7 +508,7 @@ inline int persist_grid(int n, int ept, int nsys) {
     return G < 1 ? 1 : (int)G;
 }
 
-template <class R, int EPT, int PU>
+template <class R, int EPT, int PU, bool PF = false>
 __global__ void __launch_bounds__(NT, 2)
     k_mdot_persist(int n, const typename CT<R>::t *__restrict__ segA, int qa,
                    const typename CT<R>::t *__restrict__ segB0, size_t strideB, int qb,
@@ -533,20 +533,38 @@ __global__ void __launch_bounds__(NT, 2)
         C a[PU];
 #pragma unroll
         for (int u = 0; u < PU; ++u) a[u] = czero<C>();
-        for (long ch = blockIdx.y; ch < nch; ch += G) {
+        C wv[EPT], vv[PU][EPT];
+        auto load = [&](long ch, C(&wd)[EPT], C(&vd)[PU][EPT]) {
             const long c0 = ch * span + tid;
-            C wv[EPT], vv[PU][EPT];
 #pragma unroll
-            for (int e = 0; e < EPT; ++e) wv[e] = c0 + (long)e * NT < n ? w[c0 + (long)e * NT] : czero<C>();
+            for (int e = 0; e < EPT; ++e) wd[e] = c0 + (long)e * NT < n ? w[c0 + (long)e * NT] : czero<C>();
 #pragma unroll
             for (int u = 0; u < PU; ++u)
 #pragma unroll
-                for (int e = 0; e < EPT; ++e) vv[u][e] = c0 + (long)e * NT < n ? vp[u][c0 + (long)e * NT] : czero<C>();
+                for (int e = 0; e < EPT; ++e) vd[u][e] = c0 + (long)e * NT < n ? vp[u][c0 + (long)e * NT] : czero<C>();
+        };
+        if constexpr (PF)
+            if (blockIdx.y < nch) load(blockIdx.y, wv, vv);
+        for (long ch = blockIdx.y; ch < nch; ch += G) {
+            C wn[PF ? EPT : 1], vn[PF ? PU : 1][PF ? EPT : 1];
+            if constexpr (PF) {   // the next chunk's loads go out before this chunk's arithmetic
+                if (ch + G < nch) load(ch + G, wn, vn);
+            } else {
+                load(ch, wv, vv);
+            }
 #pragma unroll
             for (int u = 0; u < PU; ++u) {
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) cdotacc(a[u], vv[u][e], wv[e]);
                 a[u] = canon(a[u]);
+            }
+            if constexpr (PF) {
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) wv[e] = wn[e];
+#pragma unroll
+                for (int u = 0; u < PU; ++u)
+#pragma unroll
+                    for (int e = 0; e < EPT; ++e) vv[u][e] = vn[u][e];
             }
         }
         if constexpr (std::is_same<C, dfc>::value) {
@@ -584,7 +602,7 @@ __global__ void __launch_bounds__(NT, 2)
     if (tid == 0) tickets[slot] = 0;
 }
 
-template <class R, int EPT, int PU>
+template <class R, int EPT, int PU, bool PF = false>
 __global__ void __launch_bounds__(NT, 2)
     k_update_persist(int n, const typename CT<R>::t *__restrict__ segA, int qa,
                      const typename CT<R>::t *__restrict__ segB0, size_t strideB, int qb,
@@ -614,14 +632,23 @@ __global__ void __launch_bounds__(NT, 2)
             org[e] = c0 + (long)e * NT < n ? w[c0 + (long)e * NT] : czero<C>();
             acc[e] = org[e];
         }
-        for (int p0 = 0; p0 < q; p0 += PU) {
-            C vv[PU][EPT];
+        C vv[PU][EPT];
+        auto load = [&](int g0, C(&vd)[PU][EPT]) {
 #pragma unroll
             for (int u = 0; u < PU; ++u) {
-                const int p = p0 + u < q ? p0 + u : q - 1;
+                const int p = g0 + u < q ? g0 + u : q - 1;
                 const C *vp = p < qa ? segA + (size_t)p * n : segB + (size_t)(p - qa) * n;
 #pragma unroll
-                for (int e = 0; e < EPT; ++e) vv[u][e] = c0 + (long)e * NT < n ? vp[c0 + (long)e * NT] : czero<C>();
+                for (int e = 0; e < EPT; ++e) vd[u][e] = c0 + (long)e * NT < n ? vp[c0 + (long)e * NT] : czero<C>();
+            }
+        };
+        if constexpr (PF) load(0, vv);
+        for (int p0 = 0; p0 < q; p0 += PU) {
+            C vn[PF ? PU : 1][PF ? EPT : 1];
+            if constexpr (PF) {   // the next group's loads go out before this group's arithmetic
+                if (p0 + PU < q) load(p0 + PU, vn);
+            } else {
+                load(p0, vv);
             }
 #pragma unroll
             for (int u = 0; u < PU; ++u) {
@@ -634,6 +661,12 @@ __global__ void __launch_bounds__(NT, 2)
             if constexpr (std::is_same<C, dfc>::value) {   // keep double-float chains short
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) acc[e] = canon(acc[e]);
+            }
+            if constexpr (PF) {
+#pragma unroll
+                for (int u = 0; u < PU; ++u)
+#pragma unroll
+                    for (int e = 0; e < EPT; ++e) vv[u][e] = vn[u][e];
             }
         }
 #pragma unroll
@@ -3161,7 +3194,7 @@ struct TuneKey {
 struct TuneEntry {
     TuneKey key;
     int variant;
-    float ms[12];
+    float ms[16];
     int nvar;
 };
 std::vector<TuneEntry> g_tuned;
@@ -3438,6 +3471,23 @@ int mdot_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const typ
                 v = 0;
             }
         }
+        if (v == 12 || v == 13) {   // persistent with the next chunk prefetched: (1, 4) or (2, 2)
+            const int ept = v == 12 ? 1 : 2, G = persist_grid(n, ept, nsys);
+            if ((size_t)nsys * qmax * 2 * G <= cap) {
+                if (v == 12)
+                    k_mdot_persist<R, 1, 4, true><<<grid2(nsys, G), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w,
+                                                                                 strideW, act, partials, qmax, tickets,
+                                                                                 coef, strideC, state,
+                                                                                 skip_broken ? 1 : 0);
+                else
+                    k_mdot_persist<R, 2, 2, true><<<grid2(nsys, G), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w,
+                                                                                 strideW, act, partials, qmax, tickets,
+                                                                                 coef, strideC, state,
+                                                                                 skip_broken ? 1 : 0);
+                return 1;
+            }
+            v = 0;
+        }
         if (v == 9 || v == 10) {   // persistent: (4 elements, 2 vectors) or (2, 4)
             const int ept = v == 9 ? 4 : 2, G = persist_grid(n, ept, nsys);
             if ((size_t)nsys * qmax * 2 * G <= cap) {
@@ -3497,7 +3547,7 @@ void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT
     };
     int v = 0;
     if (forced_variant(0) >= 0) v = forced_variant(0);
-    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(prec_key<R>(), 0, n, nsys, qa, sizeof(R) == 4 ? 11 : std::is_same<R, dfr>::value ? 12 : 11, st, run);
+    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(prec_key<R>(), 0, n, nsys, qa, sizeof(R) == 4 ? 11 : 14, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)
@@ -3571,6 +3621,23 @@ int update_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const t
                 v = 0;
             }
         }
+        if (v == 11 || v == 12) {   // persistent with the next group prefetched: (2, 2) or (1, 4)
+            const int ept = v == 11 ? 2 : 1, G = persist_grid(n, ept, nsys);
+            if ((size_t)nsys * 3 * G <= cap) {
+                if (v == 11)
+                    k_update_persist<R, 2, 2, true><<<grid2(nsys, G), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w,
+                                                                                   strideW, out, strideO, act, coef,
+                                                                                   strideC, partials, tickets, state, fin,
+                                                                                   skip_broken ? 1 : 0);
+                else
+                    k_update_persist<R, 1, 4, true><<<grid2(nsys, G), NT, 0, st>>>(n, segA, qa, segB, strideB, qb, w,
+                                                                                   strideW, out, strideO, act, coef,
+                                                                                   strideC, partials, tickets, state, fin,
+                                                                                   skip_broken ? 1 : 0);
+                return 1;
+            }
+            v = 0;
+        }
         if (v == 8 || v == 9) {   // persistent: (4 elements, 2 vectors) or (2, 4)
             const int ept = v == 8 ? 4 : 2, G = persist_grid(n, ept, nsys);
             if ((size_t)nsys * 3 * G <= cap) {
@@ -3632,7 +3699,7 @@ void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename 
     int v = 0;
     if (forced_variant(1) >= 0) v = forced_variant(1);
     else if (representative(nsys, qa, qb) && !profile_enabled())
-        v = tuned_variant(prec_key<R>(), 1, n, nsys, qa, sizeof(R) == 4 ? 10 : std::is_same<R, dfr>::value ? 11 : 10, st, run);
+        v = tuned_variant(prec_key<R>(), 1, n, nsys, qa, sizeof(R) == 4 ? 10 : 13, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)
