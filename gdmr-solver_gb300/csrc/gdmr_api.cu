@@ -733,6 +733,15 @@ extern "C" int gdmr_system_set_graphs(gdmr_system *S, int on) {
     return GDMR_OK;
 }
 
+extern "C" int gdmr_system_set_fused(gdmr_system *S, int on) {
+    if (!S) return fail(GDMR_EINVAL, "gdmr_system_set_fused", "null system");
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->e32.fused_small = on != 0;
+    S->e64.fused_small = on != 0;
+    S->edf.fused_small = on != 0;
+    return GDMR_OK;
+}
+
 extern "C" int gdmr_system_svd_sweeps(const gdmr_system *S) {
     if (!S) return 0;
     return S->precision == 1 ? S->e32.last_svd_sweeps()

@@ -210,6 +210,7 @@ template <class R> void Engine<R>::release() {
     if (partials_) unregister_scratch(partials_);
     partials_side_ = nullptr;
     ticket_side_ = nullptr;
+    ks_bar_ = nullptr;
     for (void *p : allocs_) cudaFree(p);
     allocs_.clear();
     if (hstate_) cudaFreeHost(hstate_);
@@ -274,6 +275,7 @@ template <class R> int Engine<R>::init(int n, int m, int k, int capacity, int de
     A_(partials_side_, sizeof(double) * scratch_doubles(16, 1, 1));
     A_(lead_dev_, sizeof(int));
     A_(ticket_side_, sizeof(unsigned));
+    A_(ks_bar_, 2 * sizeof(unsigned));
 #undef A_
     if (cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ev_krylov_, cudaEventDisableTiming) != cudaSuccess ||
@@ -460,8 +462,13 @@ template <class R> int Engine<R>::enqueue_cycle(int kk, int nsys, double tol, lo
     } else if (hook) {
         cudaMemcpyAsync(op.ext, V_, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
     }
-    // Krylov loop (gDMR.cu:2069-2328): classical Gram-Schmidt against [W V] in one pass.
-    for (int j = 1; j <= m - kk; ++j) {
+    // Krylov loop (gDMR.cu:2069-2328): classical Gram-Schmidt against [W V] in one pass.  One
+    // small system with a SELL operator runs the whole loop as one cooperative kernel.
+    const bool fused = nsys == 1 && op.kind == Operator<R>::SELL && fused_small &&
+                       launch_krylov_small<R>(n, kk, m, op.sell, W_, V_, sV, act_, state_, H_, strideH(), coef_, sC,
+                                              (double *)partials_, qmax(), ks_bar_, tol, compat_eye, stream);
+    if (fused) *matvecs += m - kk;
+    for (int j = 1; !fused && j <= m - kk; ++j) {
         const int col = kk + j - 1;
         if (hook) {
             *matvecs += 1;

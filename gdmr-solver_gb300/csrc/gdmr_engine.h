@@ -86,6 +86,7 @@ template <class R> class Engine {
     Operator<R> op;
     cudaStream_t stream = nullptr;
     bool use_graphs = true;     // capture restart cycles of small systems as CUDA graphs
+    bool fused_small = true;    // one small system: the Krylov loop as one cooperative kernel
     bool compat_eye = true;     // reproduce the reference's breakdown identity tail (gDMR.cu:2275)
 
     // Reference semantics on system 0 (solverDMR): b, x are device vectors of precision R;
@@ -145,6 +146,7 @@ template <class R> class Engine {
     double *sigma_ = nullptr, *znorm2_ = nullptr;
     int *sweeps_ = nullptr;
     unsigned *tickets_ = nullptr;
+    unsigned *ks_bar_ = nullptr;   // grid barrier + abort flag of the fused small-system Krylov loop
     SysState *state_ = nullptr, *hstate_ = nullptr;
     int *act_ = nullptr;        // active list (device)
     int *ident_ = nullptr;      // 0..cap (device), ident_[cap] is the deflation pseudo-system

@@ -1024,6 +1024,233 @@ __global__ void __launch_bounds__(BK_THREADS, 1)
     }
 }
 
+// ----------------------------------------------------------------- fused Krylov loop, one small system
+// The whole Krylov loop of a restart cycle for one system with a SELL operator and n <= 32 x
+// (CTAs that fit on the device at once), in one cooperative launch.  For small n the
+// per-step kernels (operator, projection, update, scaling: four launches with a last-CTA
+// reduction each) are latency: 53 us a step on the 64 x 64 Helmholtz operator, where the data
+// of a step is ~3 MB.  Here CTA b owns rows 32b .. 32b+31 (one SELL slice); warp 0 applies the
+// operator to them, the eight warps split the basis vectors of the projection and the update,
+// and four grid barriers a step exchange the CTAs' partial sums:
+//   projection partials -> | CTA p mod G sums coefficient p -> | update, norm partials -> |
+//   every CTA sums the norms in the same order, CTA 0 runs the step's finish (H column,
+//   breakdown test), all scale their rows into V_j -> | next step.
+// Values other CTAs wrote in this launch are read with ld.global.cg (L2), never from L1.  The
+// barrier is a monotonic counter (zeroed before the launch); its wait is bounded (about two
+// seconds of clock), and a timeout is counted in g_bulk_timeouts and ends every CTA's loop.
+constexpr int KS_THREADS = 256;
+constexpr int KS_WARPS = KS_THREADS / 32;
+constexpr int KS_PCHUNK = 64;   // projection products staged in shared memory per round
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+// Grid barrier: the CTA's writes are ordered before thread 0's release increment by the block
+// barrier (cumulativity), and its acquire loads order what the CTA reads after the closing block
+// barrier, so no separate full fences are needed.
+__device__ bool ks_grid_sync(unsigned *bar, unsigned target, int *abort) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;\n" ::"l"(bar) : "memory");
+        const long long t0 = clock64();
+        int ok = 1;
+        while (ld_acquire_gpu(bar) < target) {
+            if (*(volatile int *)abort) { ok = 0; break; }
+            if (clock64() - t0 > BK_WAIT_CYCLES) {
+                atomicAdd(&g_bulk_timeouts, 1u);
+                atomicExch(abort, 1);
+                ok = 0;
+                break;
+            }
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+template <class C> __device__ __forceinline__ C ldcg_c(const C *p);
+template <> __device__ __forceinline__ double2 ldcg_c<double2>(const double2 *p) { return __ldcg(p); }
+template <> __device__ __forceinline__ dfc ldcg_c<dfc>(const dfc *p) {
+    const float4 f = __ldcg(reinterpret_cast<const float4 *>(p));
+    dfc c;
+    c.x = dfr(f.x, f.y);
+    c.y = dfr(f.z, f.w);
+    return c;
+}
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ dfc csub(dfc a, dfc b) {
+    dfc r;
+    r.x = a.x - b.x;
+    r.y = a.y - b.y;
+    return r;
+}
+
+template <class R> struct KrylovSmallArgs {
+    using C = typename CT<R>::t;
+    int n, kk, m, compat_eye, qmax;
+    double tol;
+    const int *slice_ptr, *cols;
+    const C *vals;
+    const C *W;
+    C *V0;                  // basis of system 0; system s at V0 + s * strideV
+    size_t strideV;
+    const int *act;         // act[0]: the system
+    SysState *state;
+    double2 *H0;            // system s at H0 + s * strideH
+    size_t strideH;
+    double2 *coef0;         // system s at coef0 + s * strideC
+    size_t strideC;
+    double *part;           // G x qmax x 2 projection partials
+    double *npart;          // G x 3 norm partials
+    unsigned *bar;          // [0] barrier counter (zeroed before the launch), [1] abort flag
+};
+
+template <class R>
+__global__ void __launch_bounds__(KS_THREADS) k_krylov_small(KrylovSmallArgs<R> a) {
+    using C = typename CT<R>::t;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, b = blockIdx.x, G = gridDim.x;
+    const int s = a.act[0], n = a.n, kk = a.kk, row = 32 * b + lane;
+    C *V = a.V0 + (size_t)s * a.strideV;
+    double2 *coef = a.coef0 + (size_t)s * a.strideC;
+    SysState *st = a.state + s;
+    int *abort = reinterpret_cast<int *>(a.bar + 1);
+    __shared__ C ys[32], ws[32], upd[KS_WARPS][32], prod[KS_PCHUNK][32];
+    __shared__ double red[3];
+    unsigned k = 0;   // barriers passed
+    for (int j = 1; j <= a.m - kk; ++j) {
+        const int q = kk + j;
+        // (1) y = A v_{j-1} on the CTA's slice; v_{j-1} comes from every CTA: read through L2
+        if (warp == 0) {
+            C acc = czero<C>();
+            if (row < n) {
+                const int beg = a.slice_ptr[b], width = (a.slice_ptr[b + 1] - beg) >> 5;
+                const C *x = V + (size_t)(j - 1) * n;
+                for (int e = 0; e < width; ++e) {
+                    const int idx = beg + e * 32 + lane;
+                    cfma(acc, a.vals[idx], ldcg_c(x + a.cols[idx]));
+                    if constexpr (std::is_same<C, dfc>::value)
+                        if ((e & 3) == 3) acc = canon(acc);
+                }
+            }
+            ys[lane] = canon(acc);
+        }
+        __syncthreads();
+        // (2) projection partials <B_p, y> over the slice: warp w forms the 32 products of
+        // p = w, w + 8, ... into shared memory, then thread p sums its 32 in order (a warp
+        // butterfly would repeat every add in 32 lanes, at GB300's FP64 rate the bulk of a step)
+        for (int p0 = 0; p0 < q; p0 += KS_PCHUNK) {
+            const int pe = min(q, p0 + KS_PCHUNK);
+            for (int p = p0 + warp; p < pe; p += KS_WARPS) {
+                const C *B = p < kk ? a.W + (size_t)p * n : V + (size_t)(p - kk) * n;
+                C acc = czero<C>();
+                if (row < n) cdotacc(acc, B[row], ys[lane]);
+                prod[p - p0][lane] = canon(acc);
+            }
+            __syncthreads();
+            for (int p = p0 + tid; p < pe; p += KS_THREADS) {
+                C acc = czero<C>();
+                for (int l = 0; l < 32; ++l) {
+                    const C v = prod[p - p0][l];
+                    acc.x = acc.x + v.x;
+                    acc.y = acc.y + v.y;
+                }
+                a.part[((size_t)b * a.qmax + p) * 2] = (double)acc.x;
+                a.part[((size_t)b * a.qmax + p) * 2 + 1] = (double)acc.y;
+            }
+            __syncthreads();
+        }
+        if (!ks_grid_sync(a.bar, (++k) * G, abort)) return;
+        // (3) coefficient p summed over the CTAs by CTA p mod G (fixed order: lanes stride, butterfly)
+        if (warp == 0)
+            for (int p = b; p < q; p += G) {
+                double re = 0, im = 0;
+                for (int c = lane; c < G; c += 32) {
+                    re += __ldcg(a.part + ((size_t)c * a.qmax + p) * 2);
+                    im += __ldcg(a.part + ((size_t)c * a.qmax + p) * 2 + 1);
+                }
+                re = warp_sum(re);
+                im = warp_sum(im);
+                if (lane == 0) coef[p] = make_double2(re, im);
+            }
+        if (!ks_grid_sync(a.bar, (++k) * G, abort)) return;
+        // (4) w = y - sum_p c_p B_p, warps splitting p; norm and cross-term partials
+        {
+            C acc = czero<C>();
+            for (int p = warp; p < q; p += KS_WARPS) {
+                const C *B = p < kk ? a.W + (size_t)p * n : V + (size_t)(p - kk) * n;
+                const double2 cd = __ldcg(coef + p);
+                if (row < n) cfma(acc, from_d<C>(cd), B[row]);
+            }
+            upd[warp][lane] = canon(acc);
+        }
+        __syncthreads();
+        if (warp == 0) {
+            C w = ys[lane];
+#pragma unroll
+            for (int u = 0; u < KS_WARPS; ++u) w = csub(w, upd[u][lane]);
+            w = canon(w);
+            if (row >= n) w = czero<C>();
+            ws[lane] = w;
+            C ln = czero<C>(), lc = czero<C>();
+            cdotacc(ln, w, w);
+            cdotacc(lc, w, ys[lane]);
+            double v0 = (double)canon(ln).x, v1 = (double)canon(lc).x, v2 = (double)canon(lc).y;
+            v0 = warp_sum(v0);
+            v1 = warp_sum(v1);
+            v2 = warp_sum(v2);
+            if (lane == 0) {
+                a.npart[(size_t)b * 3] = v0;
+                a.npart[(size_t)b * 3 + 1] = v1;
+                a.npart[(size_t)b * 3 + 2] = v2;
+            }
+        }
+        if (!ks_grid_sync(a.bar, (++k) * G, abort)) return;
+        // (5) the norms, summed by every CTA in the same order; CTA 0 runs the step's finish
+        if (warp == 0) {
+            double v0 = 0, v1 = 0, v2 = 0;
+            for (int c = lane; c < G; c += 32) {
+                v0 += __ldcg(a.npart + (size_t)c * 3);
+                v1 += __ldcg(a.npart + (size_t)c * 3 + 1);
+                v2 += __ldcg(a.npart + (size_t)c * 3 + 2);
+            }
+            v0 = warp_sum(v0);
+            v1 = warp_sum(v1);
+            v2 = warp_sum(v2);
+            if (lane == 0) { red[0] = v0; red[1] = v1; red[2] = v2; }
+        }
+        __syncthreads();
+        const double n2 = red[0], nrm = sqrt(n2);
+        const bool broken = nrm < a.tol;
+        if (b == 0) {
+            // the H column from the coefficients (other CTAs wrote them: through L2), then the
+            // finish proper (subdiagonal, breakdown identity tail, state) with nco = 0
+            double2 *Hs = a.H0 + (size_t)s * a.strideH;
+            for (int p = tid; p < q; p += KS_THREADS) Hs[(size_t)(kk + j - 1) * (a.m + 1) + p] = __ldcg(coef + p);
+            if (tid == 0) {
+                FinishArgs f{};
+                f.mode = FIN_KRYLOV; f.col = kk + j - 1; f.nco = 0; f.ldH = a.m + 1; f.m = a.m; f.kk = kk;
+                f.compat_eye = a.compat_eye; f.tol = a.tol; f.H = a.H0; f.strideH = a.strideH;
+                f.coef = a.coef0; f.strideC = a.strideC;
+                run_finish(f, s, *st, n2, red[1], red[2]);
+            }
+        }
+        // (6) v_j = w / ||w|| (zero after a breakdown, which ends the cycle's Krylov loop)
+        if (warp == 0 && row < n) {
+            C v = ws[lane];
+            const R al = broken ? R(0.f) : R(1.0 / nrm);
+            v.x = v.x * al;
+            v.y = v.y * al;
+            if (broken) v = czero<C>();
+            V[(size_t)j * n + row] = v;
+        }
+        if (broken) return;
+        if (!ks_grid_sync(a.bar, (++k) * G, abort)) return;
+    }
+}
+
 // ----------------------------------------------------------------- batched W projection
 // coef_s[p] = <W_p, y_s> for every active system s and deflation vector p: the shared part
 // of a batched projection as one split-K product, so W is read once for the whole batch
@@ -3778,6 +4005,59 @@ void launch_svd_smallest(int m, int k, const double2 *H, size_t strideH, const i
     k_svd<<<1, threads, use_smem ? smem : 0, st>>>(m, k, H, strideH, lead, vs, sigma, work, use_smem, sweeps);
 }
 
+// Algorithmic bytes of the fused Krylov loop: per step the operator product, the projection
+// against kk + j vectors (and y), the update (the same vectors, y, w) and the scaling.
+double krylov_small_bytes(const SellMatrix &A, size_t vs, int kk, int m) {
+    double b = 0;
+    for (int j = 1; j <= m - kk; ++j)
+        b += spmm_bytes(A, vs, 1) + (double)vs * A.n * ((kk + j + 1.0) + (kk + j + 2.0) + 2.0);
+    return b;
+}
+
+// The fused Krylov loop for one system (k_krylov_small); false when it does not apply: n above
+// 32 x (CTAs resident at once), the scratch too small, or the launch refused.
+template <class R>
+bool launch_krylov_small(int n, int kk, int m, const SellMatrix &A, const typename CT<R>::t *W,
+                         typename CT<R>::t *V, size_t strideV, const int *act, SysState *state, double2 *H,
+                         size_t strideH, double2 *coef, size_t strideC, double *partials, int qmax, unsigned *bar,
+                         double tol, bool compat_eye, cudaStream_t st) {
+    if constexpr (sizeof(R) == 4) {
+        return false;
+    } else {
+        const int G = A.nslices;
+        if (G < 1 || m - kk < 1 || qmax > QMAX) return false;
+        static int resident = -1;
+        if (resident < 0) {
+            int per_sm = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_krylov_small<R>, KS_THREADS, 0) != cudaSuccess)
+                per_sm = 0;
+            resident = per_sm * num_sms();
+        }
+        if (G > resident) return false;
+        const size_t need = (size_t)G * qmax * 2 + (size_t)G * 3;
+        if (need > scratch_capacity(partials)) return false;
+        KrylovSmallArgs<R> a{};
+        a.n = n; a.kk = kk; a.m = m; a.compat_eye = compat_eye ? 1 : 0; a.qmax = qmax; a.tol = tol;
+        a.slice_ptr = A.slice_ptr; a.cols = A.cols; a.vals = (const typename CT<R>::t *)A.vals;
+        a.W = W; a.V0 = V; a.strideV = strideV; a.act = act; a.state = state;
+        a.H0 = H; a.strideH = strideH; a.coef0 = coef; a.strideC = strideC;
+        a.part = partials; a.npart = partials + (size_t)G * qmax * 2; a.bar = bar;
+        Launch L_(KC_UPDATE, krylov_small_bytes(A, sizeof(typename CT<R>::t), kk, m), st, 1);
+        if (cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st) != cudaSuccess) return false;
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3((unsigned)G);
+        cfg.blockDim = dim3(KS_THREADS);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, k_krylov_small<R>, a) == cudaSuccess;
+    }
+}
+
 template <class R>
 void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX, typename CT<R>::t *y, size_t strideY,
                  const int *act, int nsys, cudaStream_t st) {
@@ -3889,7 +4169,10 @@ void launch_broadcast_hdef(int m, int kk, const double2 *Hd, double2 *H, size_t 
     template void launch_demote_unit<R>(int, const double2 *, size_t, CT<R>::t *, size_t, const int *, int,            \
                                         const SysState *, cudaStream_t);                                               \
     template void launch_norm<R>(int, const CT<R>::t *, size_t, const int *, int, double2 *, unsigned *, SysState *,   \
-                                 int, cudaStream_t);
+                                 int, cudaStream_t);                                                                   \
+    template bool launch_krylov_small<R>(int, int, int, const SellMatrix &, const CT<R>::t *, CT<R>::t *, size_t,      \
+                                         const int *, SysState *, double2 *, size_t, double2 *, size_t, double *, int, \
+                                         unsigned *, double, bool, cudaStream_t);
 
 GDMR_INST(float)
 GDMR_INST(double)

@@ -254,6 +254,17 @@ void launch_stencil(const Stencil7 &S, const typename CT<R>::t *x, size_t stride
 template <class R>
 void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX, typename CT<R>::t *y,
                  size_t strideY, const int *act, int nsys, cudaStream_t st);
+
+// The Krylov loop of a restart cycle for one system act[0] with a SELL operator (complex128 or
+// double-float) as one cooperative kernel, CTA b on SELL slice b; partials: the engine's scratch
+// (G x qmax x 2 + G x 3 doubles), bar: 2 unsigned (zeroed here).  Returns false, launching
+// nothing, when it does not apply (complex64, more slices than CTAs resident at once, scratch).
+template <class R>
+bool launch_krylov_small(int n, int kk, int m, const SellMatrix &A, const typename CT<R>::t *W,
+                         typename CT<R>::t *V, size_t strideV, const int *act, SysState *state, double2 *H,
+                         size_t strideH, double2 *coef, size_t strideC, double *partials, int qmax, unsigned *bar,
+                         double tol, bool compat_eye, cudaStream_t st);
+
 // y_s = b_s - A x_s in FP64 with ||y_s||^2 reduced into state[s].nrm2 (refined form).
 void launch_residual64(const SellMatrix &A, const double2 *b, size_t strideB, const double2 *x, size_t strideX,
                        double2 *r, size_t strideR, const int *act, int nsys, double2 *partials, unsigned *tickets,

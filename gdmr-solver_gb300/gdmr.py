@@ -67,6 +67,7 @@ SIGNATURES = {
     "gdmr_system_bytes": (LL, [P]),
     "gdmr_system_svd_sweeps": (I, [P]),
     "gdmr_system_set_graphs": (I, [P, I]),
+    "gdmr_system_set_fused": (I, [P, I]),
     "gdmr_solve": (I, [P, I, P, P, D, I, I, P]),
     "gdmr_solve_batch": (I, [P, I, P, P, P, I, I, P]),
     "gdmr_true_residual": (I, [P, I, P, P, I, P]),
@@ -342,6 +343,10 @@ class System:
 
     def set_graphs(self, on: bool) -> None:
         _check(self.L.gdmr_system_set_graphs(self._h, 1 if on else 0), "gdmr_system_set_graphs")
+
+    def set_fused(self, on: bool) -> None:
+        """One small system: run the Krylov loop as one cooperative kernel (default) or step by step."""
+        _check(self.L.gdmr_system_set_fused(self._h, 1 if on else 0), "gdmr_system_set_fused")
 
     def set_stencil(self, shape, d, wx, wy, wz=0.0) -> None:
         """Matrix-free inner operator: the constant-coefficient stencil on a grid of `shape`

@@ -144,6 +144,10 @@ int gdmr_system_clear_stencil(gdmr_system *sys);
 /* Restart cycles of small systems (n x batch <= 2^20) replay as CUDA graphs after the first
  * cycle (on by default); 0 launches every kernel eagerly. */
 int gdmr_system_set_graphs(gdmr_system *sys, int on);
+/* One system with a CSR operator, complex128 or fp64e, and n up to 32 x (CTAs the device holds
+ * at once): the Krylov loop of a restart cycle runs as one cooperative kernel (on by default;
+ * 0 launches its operator, projection, update and scaling kernels step by step). */
+int gdmr_system_set_fused(gdmr_system *sys, int on);
 
 /* Reference-semantics solve of one right-hand side (solverDMR's algorithm,
  * complex128, complex64 or double-float per the system's precision), then the true FP64
