@@ -78,10 +78,17 @@ template <class C> void sub(int n, const C *a, const C *b, C *out, cudaStream_t 
 
 // ----------------------------------------------------------------- SELL build
 size_t DeviceSell::bytes() const {
-    return sizeof(int) * ((size_t)nslices + 1 + padded) + (vals32 ? sizeof(float2) * padded : 0) +
+    return sizeof(int) * ((size_t)nslices + 1 + padded) + (size_t)nslices + (vals32 ? sizeof(float2) * padded : 0) +
            (vals64 ? sizeof(double2) * padded : 0) + (valsdf ? sizeof(dfc) * padded : 0);
 }
 
+// SELL-32 with an offset pattern.  When the column offsets (column - row) of all non-zeros form
+// a set of at most SELL_PATTERN values (a 5- or 7-point stencil on a lexicographic grid), a
+// slice all of whose rows can use every offset (rows whose neighbours stay inside 0..n-1) is
+// stored "uniform": entry e of row r is A[r][r + off[e]], zero where A has no such entry, so the
+// kernels form the column as r + off[e] instead of loading it (the column-index load, then the
+// dependent gather, was the latency chain of the operator kernels).  The explicit column array
+// is filled for every slice, so kernels that do not use the pattern read the same matrix.
 int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, const double *vals_ri, bool want32,
                   bool want64, cudaStream_t st, bool wantdf) {
     if (n <= 0 || !rowptr || !colidx || !vals_ri) {
@@ -89,16 +96,38 @@ int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, 
         return GDMR_EINVAL;
     }
     const int ns = (n + 31) / 32;
+    // the offset pattern: every distinct column - row, if there are at most SELL_PATTERN of them
+    std::vector<int> pat;
+    for (int r = 0; r < n; ++r) {
+        if (rowptr[r + 1] < rowptr[r]) {
+            set_last_error(GDMR_EINVAL, "sell_from_csr: row pointers are not non-decreasing");
+            return GDMR_EINVAL;
+        }
+        for (int q = rowptr[r]; q < rowptr[r + 1] && pat.size() <= (size_t)SELL_PATTERN; ++q) {
+            const int col = colidx[q];
+            if (col < 0 || col >= n) {
+                set_last_error(GDMR_EINVAL, "sell_from_csr: column index out of range");
+                return GDMR_EINVAL;
+            }
+            if (std::find(pat.begin(), pat.end(), col - r) == pat.end()) pat.push_back(col - r);
+        }
+        if (pat.size() > (size_t)SELL_PATTERN) break;
+    }
+    if (pat.size() > (size_t)SELL_PATTERN) pat.clear();
+    std::sort(pat.begin(), pat.end());
+    const int np = (int)pat.size();
+    std::vector<unsigned char> uni(ns, 0);
     std::vector<int> sp(ns + 1, 0);
     for (int s = 0; s < ns; ++s) {
         int w = 0;
+        bool u = np > 0;
         for (int r = s * 32; r < std::min(n, s * 32 + 32); ++r) {
-            int len = rowptr[r + 1] - rowptr[r];
-            if (len < 0) {
-                set_last_error(GDMR_EINVAL, "sell_from_csr: row pointers are not non-decreasing");
-                return GDMR_EINVAL;
-            }
-            w = std::max(w, len);
+            w = std::max(w, rowptr[r + 1] - rowptr[r]);
+            if (np > 0 && (r + pat.front() < 0 || r + pat.back() >= n)) u = false;
+        }
+        if (u) {
+            uni[s] = 1;
+            w = np;
         }
         long next = (long)sp[s] + 32L * w;
         if (next > 0x7fffffffL) {
@@ -108,34 +137,43 @@ int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, 
         sp[s + 1] = (int)next;
     }
     const long padded = sp[ns];
+    int band = 0;
     std::vector<int> cols(padded);
     std::vector<float2> v32(want32 ? padded : 0);
     std::vector<double2> v64(want64 ? padded : 0);
     std::vector<dfc> vdf(wantdf ? padded : 0);
+    auto put = [&](long e, int col, double re, double im) {
+        cols[e] = col;
+        if (want32) v32[e] = make_float2((float)re, (float)im);
+        if (want64) v64[e] = make_double2(re, im);
+        if (wantdf) {
+            vdf[e].x = dfr(re);
+            vdf[e].y = dfr(im);
+        }
+    };
     for (int s = 0; s < ns; ++s) {
         const int w = (sp[s + 1] - sp[s]) / 32;
         for (int lane = 0; lane < 32; ++lane) {
             const int r = s * 32 + lane;
             const int beg = r < n ? rowptr[r] : 0, len = r < n ? rowptr[r + 1] - rowptr[r] : 0;
-            for (int c = 0; c < w; ++c) {
-                const long e = (long)sp[s] + (long)c * 32 + lane;
-                int col = r < n ? r : 0;
-                double re = 0, im = 0;
-                if (c < len) {
-                    col = colidx[beg + c];
-                    if (col < 0 || col >= n) {
-                        set_last_error(GDMR_EINVAL, "sell_from_csr: column index out of range");
-                        return GDMR_EINVAL;
-                    }
-                    re = vals_ri[2 * (size_t)(beg + c)];
-                    im = vals_ri[2 * (size_t)(beg + c) + 1];
+            for (int q = beg; q < beg + len; ++q) band = std::max(band, std::abs(colidx[q] - r));
+            if (uni[s]) {
+                // pattern order; duplicate entries of one column add up, as in CSR
+                std::vector<double> re(np, 0.0), im(np, 0.0);
+                for (int q = beg; q < beg + len; ++q) {
+                    const int e = (int)(std::find(pat.begin(), pat.end(), colidx[q] - r) - pat.begin());
+                    re[e] += vals_ri[2 * (size_t)q];
+                    im[e] += vals_ri[2 * (size_t)q + 1];
                 }
-                cols[e] = col;
-                if (want32) v32[e] = make_float2((float)re, (float)im);
-                if (want64) v64[e] = make_double2(re, im);
-                if (wantdf) {
-                    vdf[e].x = dfr(re);
-                    vdf[e].y = dfr(im);
+                for (int e = 0; e < np; ++e)
+                    put((long)sp[s] + (long)e * 32 + lane, r < n ? r + pat[e] : 0, re[e], im[e]);
+            } else {
+                for (int c = 0; c < w; ++c) {
+                    const long e = (long)sp[s] + (long)c * 32 + lane;
+                    if (c < len)
+                        put(e, colidx[beg + c], vals_ri[2 * (size_t)(beg + c)], vals_ri[2 * (size_t)(beg + c) + 1]);
+                    else
+                        put(e, r < n ? r : 0, 0.0, 0.0);
                 }
             }
         }
@@ -145,11 +183,16 @@ int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, 
     d.nnz = rowptr[n] - rowptr[0];
     d.padded = padded;
     d.nslices = ns;
+    d.band = band;
+    d.npat = np;
+    for (int e = 0; e < np; ++e) d.pat[e] = pat[e];
     GDMR_CK(cudaGetDevice(&d.device));
     GDMR_CK(cudaMalloc(&d.slice_ptr, sizeof(int) * (ns + 1)));
     GDMR_CK(cudaMalloc(&d.cols, sizeof(int) * std::max<long>(padded, 1)));
+    GDMR_CK(cudaMalloc(&d.uniform, (size_t)ns));
     GDMR_CK(cudaMemcpyAsync(d.slice_ptr, sp.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice, st));
     GDMR_CK(cudaMemcpyAsync(d.cols, cols.data(), sizeof(int) * padded, cudaMemcpyHostToDevice, st));
+    GDMR_CK(cudaMemcpyAsync(d.uniform, uni.data(), (size_t)ns, cudaMemcpyHostToDevice, st));
     if (want32) {
         GDMR_CK(cudaMalloc(&d.vals32, sizeof(float2) * std::max<long>(padded, 1)));
         GDMR_CK(cudaMemcpyAsync(d.vals32, v32.data(), sizeof(float2) * padded, cudaMemcpyHostToDevice, st));
@@ -171,6 +214,7 @@ int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, 
 void sell_free(DeviceSell &s) {
     if (s.slice_ptr) cudaFree(s.slice_ptr);
     if (s.cols) cudaFree(s.cols);
+    if (s.uniform) cudaFree(s.uniform);
     if (s.vals32) cudaFree(s.vals32);
     if (s.vals64) cudaFree(s.vals64);
     if (s.valsdf) cudaFree(s.valsdf);

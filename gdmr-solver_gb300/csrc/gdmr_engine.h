@@ -38,9 +38,20 @@ struct DeviceSell {
     double2 *vals64 = nullptr;
     dfc *valsdf = nullptr;   // double-float values of the fp64e form
     int device = 0;
-    SellMatrix view32() const { return SellMatrix{n, nslices, slice_ptr, cols, vals32, nnz}; }
-    SellMatrix view64() const { return SellMatrix{n, nslices, slice_ptr, cols, vals64, nnz}; }
-    SellMatrix viewdf() const { return SellMatrix{n, nslices, slice_ptr, cols, valsdf, nnz}; }
+    int band = 0;                      // max |column - row|
+    unsigned char *uniform = nullptr;  // per slice: 1 = columns are row + pat[e]
+    int npat = 0;                      // offset pattern (0: none)
+    int pat[SELL_PATTERN] = {};
+    SellMatrix view(const void *v) const {
+        SellMatrix m{n, nslices, slice_ptr, cols, v, nnz};
+        m.uniform = uniform;
+        m.npat = npat;
+        for (int e = 0; e < SELL_PATTERN; ++e) m.pat[e] = pat[e];
+        return m;
+    }
+    SellMatrix view32() const { return view(vals32); }
+    SellMatrix view64() const { return view(vals64); }
+    SellMatrix viewdf() const { return view(valsdf); }
     size_t bytes() const;
 };
 // Builds the SELL-32 form of a CSR matrix (values interleaved re,im doubles).

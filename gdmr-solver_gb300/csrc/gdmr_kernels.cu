@@ -2975,9 +2975,9 @@ __global__ void __launch_bounds__(NT) k_spmv2(int n, const int *__restrict__ sli
                                               const typename CT<R>::t *__restrict__ vals,
                                               const typename CT<R>::t *__restrict__ x0, size_t strideX,
                                               typename CT<R>::t *__restrict__ y0, size_t strideY,
-                                              const int *__restrict__ act) {
+                                              const int *__restrict__ act, SellPattern pat) {
     using C = typename CT<R>::t;
-    constexpr int WMAX = 8;
+    constexpr int WMAX = SELL_PATTERN;
     const int sys = act[0];
     const C *x = x0 + (size_t)sys * strideX;
     C *y = y0 + (size_t)sys * strideY;
@@ -2994,11 +2994,12 @@ __global__ void __launch_bounds__(NT) k_spmv2(int n, const int *__restrict__ sli
             const int slice = (int)(row >> 5), lane = (int)(row & 31);
             const int beg = slice_ptr[slice];
             width[h] = (slice_ptr[slice + 1] - beg) >> 5;
+            const bool uni = pat.uniform && pat.uniform[slice];   // columns row + off[e]
 #pragma unroll
             for (int e = 0; e < WMAX; ++e) {
                 const bool in = e < width[h];
                 v[h][e] = in ? vals[beg + e * 32 + lane] : czero<C>();
-                c[h][e] = in ? cols[beg + e * 32 + lane] : (int)row;
+                c[h][e] = in ? (uni ? (int)row + pat.off[e] : cols[beg + e * 32 + lane]) : (int)row;
             }
         }
     }
@@ -3033,14 +3034,15 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
                                              const typename CT<R>::t *__restrict__ vals,
                                              const typename CT<R>::t *__restrict__ x0, size_t strideX,
                                              typename CT<R>::t *__restrict__ y0, size_t strideY,
-                                             const int *__restrict__ act, int nsys) {
+                                             const int *__restrict__ act, int nsys, SellPattern pat) {
     using C = typename CT<R>::t;
-    constexpr int WMAX = 8;   // stencil rows (7-point) fit; wider slices take the loop below
+    constexpr int WMAX = SELL_PATTERN;   // stencil rows (7-point) fit; wider slices take the loop below
     const int g0 = blockIdx.x * SG;
     const int ng = min(SG, nsys - g0);
     for (long row = (long)blockIdx.y * NT + threadIdx.x; row < n; row += (long)gridDim.y * NT) {
         const int slice = (int)(row >> 5), lane = (int)(row & 31);
         const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
+        const bool uni = pat.uniform && pat.uniform[slice];   // columns row + off[e]: no index loads
         if (width <= WMAX) {
             C v[WMAX];
             int c[WMAX];
@@ -3048,7 +3050,7 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
             for (int e = 0; e < WMAX; ++e) {
                 if (e < width) {
                     v[e] = vals[beg + e * 32 + lane];
-                    c[e] = cols[beg + e * 32 + lane];
+                    c[e] = uni ? (int)row + pat.off[e] : cols[beg + e * 32 + lane];
                 } else {
                     v[e] = czero<C>();
                     c[e] = (int)row;
@@ -4058,6 +4060,13 @@ bool launch_krylov_small(int n, int kk, int m, const SellMatrix &A, const typena
     }
 }
 
+SellPattern sell_pattern(const SellMatrix &A) {
+    SellPattern p{};
+    p.uniform = A.npat > 0 ? A.uniform : nullptr;
+    for (int e = 0; e < SELL_PATTERN; ++e) p.off[e] = A.pat[e];
+    return p;
+}
+
 template <class R>
 void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX, typename CT<R>::t *y, size_t strideY,
                  const int *act, int nsys, cudaStream_t st) {
@@ -4066,14 +4075,14 @@ void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX
     if (nsys == 1) {
         const long chunks = ((long)A.n + 2 * NT - 1) / (2 * NT);
         k_spmv2<R><<<(unsigned)chunks, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const typename CT<R>::t *)A.vals, x,
-                                                    strideX, y, strideY, act);
+                                                    strideX, y, strideY, act, sell_pattern(A));
         return;
     }
     constexpr int SG = 8;
     int rows = (A.n + NT - 1) / NT;
     dim3 grid((nsys + SG - 1) / SG, rows < 65535 ? rows : 65535);
     k_spmm<R, SG><<<grid, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const typename CT<R>::t *)A.vals, x, strideX, y,
-                                       strideY, act, nsys);
+                                       strideY, act, nsys, sell_pattern(A));
 }
 
 template <class R>

@@ -232,6 +232,12 @@ void launch_svd_smallest(int m, int k, const double2 *H, size_t strideH, const i
 size_t svd_smem_bytes(int m);
 
 // SELL-32 sparse matrix times a batch of vectors: y_s = A x_s over the active systems.
+constexpr int SELL_PATTERN = 8;   // most distinct column offsets stored as a pattern
+// Column offsets of a pattern-stored slice, passed to the operator kernels by value.
+struct SellPattern {
+    const unsigned char *uniform;
+    int off[SELL_PATTERN];
+};
 struct SellMatrix {
     int n;              // rows
     int nslices;        // ceil(n/32)
@@ -239,6 +245,9 @@ struct SellMatrix {
     const int *cols;        // padded column indices
     const void *vals;       // padded values (float2 or double2)
     long nnz;               // non-zeros of the source matrix (for algorithmic byte counts)
+    const unsigned char *uniform = nullptr;   // per slice: 1 = column of entry e is row + pat[e]
+    int npat = 0;                              // offset pattern (0: none)
+    int pat[SELL_PATTERN] = {};
 };
 // Matrix-free constant-coefficient stencil on an nx x ny x nz grid (nz = 1: 5-point 2D),
 // unknowns numbered i + nx (j + ny l), Dirichlet boundary (neighbours outside are dropped):
