@@ -512,11 +512,18 @@ template <class R> int Engine<R>::enqueue_cycle(int kk, int nsys, double tol, lo
                        launch_krylov_small<R>(n, kk, m, op.sell, W_, V_, sV, act_, state_, H_, strideH(), coef_, sC,
                                               (double *)partials_, qmax(), ks_bar_, tol, compat_eye, stream);
     if (fused) *matvecs += m - kk;
+    // With a SELL operator, the normalisation of v_{j-1} = a w_{j-1} happens inside the operator
+    // product of step j (launch_spmm with `scale`), which reads w_{j-1} from T anyway; only the
+    // last vector of the cycle is normalised on its own.
+    const bool fold = !fused && op.kind == Operator<R>::SELL;
     for (int j = 1; !fused && j <= m - kk; ++j) {
         const int col = kk + j - 1;
         if (hook) {
             *matvecs += 1;
             op.hook();      // v_{j-1} is already in the hook buffer
+        } else if (fold && j > 1) {
+            *matvecs += nsys;
+            launch_spmm<R>(op.sell, T_, n, Y_, n, act_, nsys, stream, state_, V_ + (size_t)(j - 1) * n, sV);
         } else {
             apply(V_ + (size_t)(j - 1) * n, sV, Y_, n, nsys, matvecs);
         }
@@ -529,7 +536,9 @@ template <class R> int Engine<R>::enqueue_cycle(int kk, int nsys, double tol, lo
         f.compat_eye = compat_eye ? 1 : 0; f.tol = tol; f.H = H_; f.strideH = strideH(); f.coef = coef_; f.strideC = sC;
         launch_update<R>(n, W_, kk, V_, sV, j, w, sW, T_, n, act_, nsys, coef_, sC, partials_, tickets_, state_, f, true,
                          stream);
-        launch_scale<R>(n, T_, n, V_ + (size_t)j * n, sV, hook ? op.ext : nullptr, 0, act_, nsys, state_, true, stream);
+        if (!fold || j == m - kk)
+            launch_scale<R>(n, T_, n, V_ + (size_t)j * n, sV, hook ? op.ext : nullptr, 0, act_, nsys, state_, true,
+                            stream);
     }
     // deflation-space update from the lead system (genDeflatDMR, gDMR.cu:1583-1704), on the
     // side stream: it needs only H_lead and the basis, which nothing below modifies

@@ -2971,16 +2971,21 @@ __global__ void __launch_bounds__(NT) k_stencil(int nx, int ny, int nz, double2 
 // loaded before any gather, so the two dependent trips (column index, then x) overlap across
 // the rows; rows wider than WMAX take the generic loop.
 template <class R>
-__global__ void __launch_bounds__(NT) k_spmv2(int n, const int *__restrict__ slice_ptr, const int *__restrict__ cols,
+__global__ void __launch_bounds__(NT, 2) k_spmv2(int n, const int *__restrict__ slice_ptr, const int *__restrict__ cols,
                                               const typename CT<R>::t *__restrict__ vals,
                                               const typename CT<R>::t *__restrict__ x0, size_t strideX,
                                               typename CT<R>::t *__restrict__ y0, size_t strideY,
-                                              const int *__restrict__ act, SellPattern pat) {
+                                              const int *__restrict__ act, SellPattern pat,
+                                              const SysState *__restrict__ scale,
+                                              typename CT<R>::t *__restrict__ vout0, size_t strideVO) {
     using C = typename CT<R>::t;
     constexpr int WMAX = SELL_PATTERN;
     const int sys = act[0];
     const C *x = x0 + (size_t)sys * strideX;
     C *y = y0 + (size_t)sys * strideY;
+    // pending normalisation, as in k_spmm
+    const R al = scale ? (R)scale[sys].alpha : R(1.0);
+    const bool brk = scale && scale[sys].broken;
     const long rbase = (long)blockIdx.x * 2 * NT + threadIdx.x;
     C v[2][WMAX];
     int c[2][WMAX], width[2];
@@ -3023,6 +3028,15 @@ __global__ void __launch_bounds__(NT) k_spmv2(int n, const int *__restrict__ sli
                 acc = canon(acc);
             }
         }
+        if (scale) {
+            C v = x[row];
+            v.x = v.x * al;
+            v.y = v.y * al;
+            acc.x = acc.x * al;
+            acc.y = acc.y * al;
+            if (brk) v = czero<C>();
+            vout0[(size_t)sys * strideVO + row] = canon(v);
+        }
         y[row] = canon(acc);
     }
 }
@@ -3034,11 +3048,30 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
                                              const typename CT<R>::t *__restrict__ vals,
                                              const typename CT<R>::t *__restrict__ x0, size_t strideX,
                                              typename CT<R>::t *__restrict__ y0, size_t strideY,
-                                             const int *__restrict__ act, int nsys, SellPattern pat) {
+                                             const int *__restrict__ act, int nsys, SellPattern pat,
+                                             const SysState *__restrict__ scale, typename CT<R>::t *__restrict__ vout0,
+                                             size_t strideVO) {
     using C = typename CT<R>::t;
     constexpr int WMAX = SELL_PATTERN;   // stencil rows (7-point) fit; wider slices take the loop below
     const int g0 = blockIdx.x * SG;
     const int ng = min(SG, nsys - g0);
+    // With `scale`, x_s is the unnormalised Krylov vector w_s: y_s = a_s (A w_s) and the row's
+    // basis entry v_s = a_s w_s goes to vout_s (a_s = state[s].alpha; zeros after a breakdown),
+    // which spares the normalisation kernel its pass over w.
+    auto fin = [&](int sys, long row, C acc, const C *x) {
+        if (scale) {
+            const SysState &stt = scale[sys];
+            const R al = (R)stt.alpha;
+            C v = x[row];
+            v.x = v.x * al;
+            v.y = v.y * al;
+            acc.x = acc.x * al;
+            acc.y = acc.y * al;
+            if (stt.broken) v = czero<C>();
+            vout0[(size_t)sys * strideVO + row] = canon(v);
+        }
+        y0[(size_t)sys * strideY + row] = canon(acc);
+    };
     for (long row = (long)blockIdx.y * NT + threadIdx.x; row < n; row += (long)gridDim.y * NT) {
         const int slice = (int)(row >> 5), lane = (int)(row & 31);
         const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
@@ -3068,8 +3101,8 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
                         cfma(a1, v[e], xb[c[e]]);
                     }
                 }
-                y0[(size_t)s0 * strideY + row] = canon(a0);
-                y0[(size_t)s1 * strideY + row] = canon(a1);
+                fin(s0, row, a0, xa);
+                fin(s1, row, a1, xb);
             }
             if (g < ng) {
                 const int s0 = act[g0 + g];
@@ -3078,7 +3111,7 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
 #pragma unroll
                 for (int e = 0; e < WMAX; ++e)
                     if (e < width) cfma(a0, v[e], xa[c[e]]);
-                y0[(size_t)s0 * strideY + row] = canon(a0);
+                fin(s0, row, a0, xa);
             }
         } else {
             for (int g = 0; g < ng; ++g) {
@@ -3089,7 +3122,7 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
                     const int idx = beg + e * 32 + lane;
                     cfma(acc, vals[idx], x[cols[idx]]);
                 }
-                y0[(size_t)s * strideY + row] = canon(acc);
+                fin(s, row, acc, x);
             }
         }
     }
@@ -3474,8 +3507,13 @@ int tuned_variant(int prec, int kernel, int n, int nsys, int qa, int nvar, cudaS
         }
         std::sort(t, t + 3);
         ent.ms[v] = t[1];
-        if (t[1] < best) { best = t[1]; ent.variant = v; }
+        if (t[1] < best) best = t[1];
     }
+    // the lowest-numbered variant within 3% of the fastest: variants that close swap places with
+    // timing noise from one process to the next, and each choice sums in its own order, so a
+    // stable choice keeps a process's results repeatable across runs as well as within one
+    for (int v = 0; v < nvar; ++v)
+        if (ent.ms[v] >= 0.f && ent.ms[v] <= 1.03f * best) { ent.variant = v; break; }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -4069,20 +4107,22 @@ SellPattern sell_pattern(const SellMatrix &A) {
 
 template <class R>
 void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX, typename CT<R>::t *y, size_t strideY,
-                 const int *act, int nsys, cudaStream_t st) {
+                 const int *act, int nsys, cudaStream_t st, const SysState *scale, typename CT<R>::t *vout,
+                 size_t strideVO) {
     if (nsys <= 0) return;
     Launch L_(KC_SPMM, spmm_bytes(A, sizeof(typename CT<R>::t), nsys), st, 1);
     if (nsys == 1) {
         const long chunks = ((long)A.n + 2 * NT - 1) / (2 * NT);
         k_spmv2<R><<<(unsigned)chunks, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const typename CT<R>::t *)A.vals, x,
-                                                    strideX, y, strideY, act, sell_pattern(A));
+                                                    strideX, y, strideY, act, sell_pattern(A), scale, vout,
+                                                    strideVO);
         return;
     }
     constexpr int SG = 8;
     int rows = (A.n + NT - 1) / NT;
     dim3 grid((nsys + SG - 1) / SG, rows < 65535 ? rows : 65535);
     k_spmm<R, SG><<<grid, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const typename CT<R>::t *)A.vals, x, strideX, y,
-                                       strideY, act, nsys, sell_pattern(A));
+                                       strideY, act, nsys, sell_pattern(A), scale, vout, strideVO);
 }
 
 template <class R>
@@ -4167,7 +4207,7 @@ void launch_broadcast_hdef(int m, int kk, const double2 *Hd, double2 *H, size_t 
                                     const double2 *, CT<R>::t *, double2 *, unsigned *, double *, cudaStream_t);       \
     template void launch_znormalise<R>(int, int, const CT<R>::t *, const double *, CT<R>::t *, cudaStream_t);          \
     template void launch_spmm<R>(const SellMatrix &, const CT<R>::t *, size_t, CT<R>::t *, size_t, const int *, int,  \
-                                 cudaStream_t);                                                                        \
+                                 cudaStream_t, const SysState *, CT<R>::t *, size_t);                                 \
     template void launch_stencil<R>(const Stencil7 &, const CT<R>::t *, size_t, CT<R>::t *, size_t, const int *, int, \
                                     cudaStream_t);                                                                     \
     template void launch_dense_gemv<R>(int, const CT<R>::t *, const CT<R>::t *, CT<R>::t *, cudaStream_t);             \

@@ -260,9 +260,12 @@ template <class R>
 void launch_stencil(const Stencil7 &S, const typename CT<R>::t *x, size_t strideX, typename CT<R>::t *y,
                     size_t strideY, const int *act, int nsys, cudaStream_t st);
 
+// With `scale` (the pending normalisation): x holds the unnormalised Krylov vectors w_s, y_s =
+// a_s (A w_s) and v_s = a_s w_s (zero after a breakdown) is written to vout (a_s = scale[s].alpha).
 template <class R>
 void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX, typename CT<R>::t *y,
-                 size_t strideY, const int *act, int nsys, cudaStream_t st);
+                 size_t strideY, const int *act, int nsys, cudaStream_t st, const SysState *scale = nullptr,
+                 typename CT<R>::t *vout = nullptr, size_t strideVO = 0);
 
 // The Krylov loop of a restart cycle for one system act[0] with a SELL operator (complex128 or
 // double-float) as one cooperative kernel, CTA b on SELL slice b; partials: the engine's scratch

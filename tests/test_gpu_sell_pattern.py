@@ -1,0 +1,75 @@
+"""The SELL-32 operator store, with and without its offset pattern, against scipy.
+
+A matrix whose column offsets (column - row) take at most 8 values is stored with the offsets
+as a pattern: the operator kernels form the columns as row + offset instead of loading them, and
+entries the pattern has but a row lacks are stored as zeros.  Through the plugin operator
+(impCsrLS_z, then linOptLS_z: x <- A x on the device, complex128), y must equal scipy's A x to
+1e-13 relative for:
+  * a 2D 5-point operator whose CSR rows are shuffled and carry split (duplicate) entries;
+  * a 3D 7-point operator, whose first and last planes' slices cannot use the pattern;
+  * an unstructured random matrix (more than 8 offsets: no pattern at all).
+"""
+import numpy as np
+import pytest
+
+import gdmr
+import problems
+from problems import CSR
+
+pytestmark = pytest.mark.gpu
+
+
+def _apply(A, x):
+    ls = gdmr.LinearSystem(A.n, 10, 2, precision="c128")
+    try:
+        ls.imp_csr(A)
+        ls.imp_src(x)
+        ls.lin_opt()
+        return ls.exp_src()
+    finally:
+        ls.close()
+
+
+def _shuffled_with_duplicates(A, seed):
+    rng = np.random.default_rng(seed)
+    indptr, indices, data = [0], [], []
+    for r in range(A.n):
+        beg, end = A.indptr[r], A.indptr[r + 1]
+        cols = list(A.indices[beg:end])
+        vals = list(A.data[beg:end])
+        j = int(rng.integers(len(cols)))       # split one entry into two that sum to it
+        w = complex(rng.standard_normal(), rng.standard_normal())
+        cols.append(cols[j])
+        vals.append(w)
+        vals[j] = vals[j] - w
+        order = rng.permutation(len(cols))
+        indices += [cols[i] for i in order]
+        data += [vals[i] for i in order]
+        indptr.append(len(indices))
+    return CSR(A.n, np.array(indptr), np.array(indices), np.array(data, dtype=complex))
+
+
+def _check(A, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal(A.n) + 1j * rng.standard_normal(A.n)
+    y = _apply(A, x)
+    ref = A.to_scipy() @ x
+    assert np.linalg.norm(y - ref) / np.linalg.norm(ref) < 1e-13
+
+
+def test_2d_pattern_with_shuffled_rows_and_duplicates():
+    A = problems.helmholtz((37, 29), 12.0, 0.05)
+    _check(_shuffled_with_duplicates(A, 3), 4)
+
+
+def test_3d_pattern_with_boundary_slices():
+    _check(problems.helmholtz((12, 10, 9), 6.0, 0.1), 5)
+
+
+def test_unstructured_matrix_has_no_pattern():
+    rng = np.random.default_rng(6)
+    n, per_row = 1500, 9
+    indptr = np.arange(0, (n + 1) * per_row, per_row)
+    indices = np.concatenate([np.sort(rng.choice(n, per_row, replace=False)) for _ in range(n)])
+    data = rng.standard_normal(n * per_row) + 1j * rng.standard_normal(n * per_row)
+    _check(CSR(n, indptr, indices, data), 7)
