@@ -512,10 +512,10 @@ template <class R> int Engine<R>::enqueue_cycle(int kk, int nsys, double tol, lo
                        launch_krylov_small<R>(n, kk, m, op.sell, W_, V_, sV, act_, state_, H_, strideH(), coef_, sC,
                                               (double *)partials_, qmax(), ks_bar_, tol, compat_eye, stream);
     if (fused) *matvecs += m - kk;
-    // With a SELL operator, the normalisation of v_{j-1} = a w_{j-1} happens inside the operator
+    // With a SELL or stencil operator, the normalisation of v_{j-1} = a w_{j-1} happens inside the operator
     // product of step j (launch_spmm with `scale`), which reads w_{j-1} from T anyway; only the
     // last vector of the cycle is normalised on its own.
-    const bool fold = !fused && op.kind == Operator<R>::SELL;
+    const bool fold = !fused && (op.kind == Operator<R>::SELL || op.kind == Operator<R>::STENCIL);
     for (int j = 1; !fused && j <= m - kk; ++j) {
         const int col = kk + j - 1;
         if (hook) {
@@ -523,7 +523,10 @@ template <class R> int Engine<R>::enqueue_cycle(int kk, int nsys, double tol, lo
             op.hook();      // v_{j-1} is already in the hook buffer
         } else if (fold && j > 1) {
             *matvecs += nsys;
-            launch_spmm<R>(op.sell, T_, n, Y_, n, act_, nsys, stream, state_, V_ + (size_t)(j - 1) * n, sV);
+            if (op.kind == Operator<R>::SELL)
+                launch_spmm<R>(op.sell, T_, n, Y_, n, act_, nsys, stream, state_, V_ + (size_t)(j - 1) * n, sV);
+            else
+                launch_stencil<R>(op.stencil, T_, n, Y_, n, act_, nsys, stream, state_, V_ + (size_t)(j - 1) * n, sV);
         } else {
             apply(V_ + (size_t)(j - 1) * n, sV, Y_, n, nsys, matvecs);
         }

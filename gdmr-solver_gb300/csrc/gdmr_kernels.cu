@@ -2934,11 +2934,16 @@ template <class R>
 __global__ void __launch_bounds__(NT) k_stencil(int nx, int ny, int nz, double2 dd, double2 wxd, double2 wyd,
                                                 double2 wzd, const typename CT<R>::t *__restrict__ x0, size_t strideX,
                                                 typename CT<R>::t *__restrict__ y0, size_t strideY,
-                                                const int *__restrict__ act) {
+                                                const int *__restrict__ act, const SysState *__restrict__ scale,
+                                                typename CT<R>::t *__restrict__ vout0, size_t strideVO) {
     using C = typename CT<R>::t;
     const int sys = act[blockIdx.z];
     const C *x = x0 + (size_t)sys * strideX;
     C *y = y0 + (size_t)sys * strideY;
+    // pending normalisation, as in k_spmm: x is w, y = a (A w), vout = a w
+    const R al = scale ? (R)scale[sys].alpha : R(1.0);
+    const bool brk = scale && scale[sys].broken;
+    C *vout = scale ? vout0 + (size_t)sys * strideVO : nullptr;
     const int tilesx = (nx + 31) / 32;
     const int ix = (blockIdx.x % tilesx) * 32 + (threadIdx.x & 31);
     const int iy = (blockIdx.x / tilesx) * 8 + (threadIdx.x >> 5);
@@ -2961,6 +2966,15 @@ __global__ void __launch_bounds__(NT) k_stencil(int nx, int ny, int nz, double2 
         cfma(acc, wx, sx);
         cfma(acc, wy, sy);
         cfma(acc, wz, cadd(below, above));
+        if (vout) {
+            C v = cur;
+            v.x = v.x * al;
+            v.y = v.y * al;
+            acc.x = acc.x * al;
+            acc.y = acc.y * al;
+            if (brk) v = czero<C>();
+            vout[idx] = canon(v);
+        }
         y[idx] = canon(acc);
         below = cur;
         cur = above;
@@ -4127,13 +4141,15 @@ void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX
 
 template <class R>
 void launch_stencil(const Stencil7 &S, const typename CT<R>::t *x, size_t strideX, typename CT<R>::t *y,
-                    size_t strideY, const int *act, int nsys, cudaStream_t st) {
+                    size_t strideY, const int *act, int nsys, cudaStream_t st, const SysState *scale,
+                    typename CT<R>::t *vout, size_t strideVO) {
     if (nsys <= 0) return;
     const double n = (double)S.nx * S.ny * S.nz;
     Launch L_(KC_SPMM, 2.0 * nsys * n * sizeof(typename CT<R>::t), st, 1);   // x read once, y written
     const int tiles = ((S.nx + 31) / 32) * ((S.ny + 7) / 8);
     const dim3 grid(tiles, (S.nz + ST_ZC - 1) / ST_ZC, nsys);
-    k_stencil<R><<<grid, NT, 0, st>>>(S.nx, S.ny, S.nz, S.d, S.wx, S.wy, S.wz, x, strideX, y, strideY, act);
+    k_stencil<R><<<grid, NT, 0, st>>>(S.nx, S.ny, S.nz, S.d, S.wx, S.wy, S.wz, x, strideX, y, strideY, act, scale,
+                                      vout, strideVO);
 }
 
 void launch_residual64(const SellMatrix &A, const double2 *b, size_t strideB, const double2 *x, size_t strideX,
@@ -4209,7 +4225,7 @@ void launch_broadcast_hdef(int m, int kk, const double2 *Hd, double2 *H, size_t 
     template void launch_spmm<R>(const SellMatrix &, const CT<R>::t *, size_t, CT<R>::t *, size_t, const int *, int,  \
                                  cudaStream_t, const SysState *, CT<R>::t *, size_t);                                 \
     template void launch_stencil<R>(const Stencil7 &, const CT<R>::t *, size_t, CT<R>::t *, size_t, const int *, int, \
-                                    cudaStream_t);                                                                     \
+                                    cudaStream_t, const SysState *, CT<R>::t *, size_t);                               \
     template void launch_dense_gemv<R>(int, const CT<R>::t *, const CT<R>::t *, CT<R>::t *, cudaStream_t);             \
     template void launch_copy_vec<R>(int, const CT<R>::t *, size_t, CT<R>::t *, size_t, const int *, int,              \
                                      cudaStream_t);                                                                    \

@@ -256,9 +256,11 @@ struct Stencil7 {
     int nx, ny, nz;
     double2 d, wx, wy, wz;
 };
+// `scale` / vout: the pending normalisation, as for launch_spmm.
 template <class R>
 void launch_stencil(const Stencil7 &S, const typename CT<R>::t *x, size_t strideX, typename CT<R>::t *y,
-                    size_t strideY, const int *act, int nsys, cudaStream_t st);
+                    size_t strideY, const int *act, int nsys, cudaStream_t st, const SysState *scale = nullptr,
+                    typename CT<R>::t *vout = nullptr, size_t strideVO = 0);
 
 // With `scale` (the pending normalisation): x holds the unnormalised Krylov vectors w_s, y_s =
 // a_s (A w_s) and v_s = a_s w_s (zero after a breakdown) is written to vout (a_s = scale[s].alpha).
