@@ -4124,7 +4124,9 @@ void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX
                  const int *act, int nsys, cudaStream_t st, const SysState *scale, typename CT<R>::t *vout,
                  size_t strideVO) {
     if (nsys <= 0) return;
-    Launch L_(KC_SPMM, spmm_bytes(A, sizeof(typename CT<R>::t), nsys), st, 1);
+    // with the normalisation folded in, the kernel also writes v_s: one more vector a system
+    Launch L_(KC_SPMM, spmm_bytes(A, sizeof(typename CT<R>::t), nsys) +
+                           (scale ? (double)sizeof(typename CT<R>::t) * A.n * nsys : 0.0), st, 1);
     if (nsys == 1) {
         const long chunks = ((long)A.n + 2 * NT - 1) / (2 * NT);
         k_spmv2<R><<<(unsigned)chunks, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const typename CT<R>::t *)A.vals, x,
@@ -4145,7 +4147,8 @@ void launch_stencil(const Stencil7 &S, const typename CT<R>::t *x, size_t stride
                     typename CT<R>::t *vout, size_t strideVO) {
     if (nsys <= 0) return;
     const double n = (double)S.nx * S.ny * S.nz;
-    Launch L_(KC_SPMM, 2.0 * nsys * n * sizeof(typename CT<R>::t), st, 1);   // x read once, y written
+    // x read once, y written (and v = a x written with the normalisation folded in)
+    Launch L_(KC_SPMM, (scale ? 3.0 : 2.0) * nsys * n * sizeof(typename CT<R>::t), st, 1);
     const int tiles = ((S.nx + 31) / 32) * ((S.ny + 7) / 8);
     const dim3 grid(tiles, (S.nz + ST_ZC - 1) / ST_ZC, nsys);
     k_stencil<R><<<grid, NT, 0, st>>>(S.nx, S.ny, S.nz, S.d, S.wx, S.wy, S.wz, x, strideX, y, strideY, act, scale,
