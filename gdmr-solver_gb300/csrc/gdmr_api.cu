@@ -387,6 +387,7 @@ extern "C" void gdmrTune(int on) { tune_enable(on != 0); }
 extern "C" void gdmrTuneForce(int projectionVariant, int updateVariant) {
     tune_force(projectionVariant, updateVariant);
 }
+extern "C" void gdmrGridOperator(int enable) { set_grid_operator(enable); }
 extern "C" const char *gdmrTuneReport(void) {
     static thread_local std::string rep;
     rep = tune_report();
@@ -740,6 +741,21 @@ extern "C" int gdmr_system_set_fused(gdmr_system *S, int on) {
     S->e64.fused_small = on != 0;
     S->edf.fused_small = on != 0;
     return GDMR_OK;
+}
+
+extern "C" int gdmr_system_grid(const gdmr_system *S, int *dims) {
+    if (!S || !dims) return fail(GDMR_EINVAL, "gdmr_system_grid", "null system or dims");
+    dims[0] = S->A.gx;
+    dims[1] = S->A.gy;
+    dims[2] = S->A.gz;
+    return GDMR_OK;
+}
+
+extern "C" int gdmr_csr_grid_form(int n, const int *rowPtr, const int *colIdx, const double *vals_ri, int *dims) {
+    if (!dims) return fail(GDMR_EINVAL, "gdmr_csr_grid_form", "null dims");
+    const int rc = csr_grid_form(n, rowPtr, colIdx, vals_ri, dims);
+    if (rc == GDMR_OK) set_last_error(GDMR_OK, "ok");
+    return rc;
 }
 
 extern "C" int gdmr_system_svd_sweeps(const gdmr_system *S) {

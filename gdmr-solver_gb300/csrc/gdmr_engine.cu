@@ -79,7 +79,89 @@ template <class C> void sub(int n, const C *a, const C *b, C *out, cudaStream_t 
 // ----------------------------------------------------------------- SELL build
 size_t DeviceSell::bytes() const {
     return sizeof(int) * ((size_t)nslices + 1 + padded) + (size_t)nslices + (vals32 ? sizeof(float2) * padded : 0) +
-           (vals64 ? sizeof(double2) * padded : 0) + (valsdf ? sizeof(dfc) * padded : 0);
+           (vals64 ? sizeof(double2) * padded : 0) + (valsdf ? sizeof(dfc) * padded : 0) +
+           (size_t)grid_planes() * n * ((grid32 ? sizeof(float2) : 0) + (grid64 ? sizeof(double2) : 0) +
+                                        (griddf ? sizeof(dfc) : 0));
+}
+
+// Checks a CSR matrix's arrays (row pointers from 0 up, non-decreasing; columns in 0..n-1) and
+// collects its offset pattern: every distinct column - row, ascending, if there are at most
+// SELL_PATTERN of them (else none).
+static int csr_offsets(int n, const int *rowptr, const int *colidx, std::vector<int> &pat, const char *who) {
+    pat.clear();
+    if (n <= 0 || !rowptr || !colidx) {
+        set_last_error(GDMR_EINVAL, std::string(who) + ": empty matrix or null arrays");
+        return GDMR_EINVAL;
+    }
+    if (rowptr[0] < 0) {
+        set_last_error(GDMR_EINVAL, std::string(who) + ": negative row pointer");
+        return GDMR_EINVAL;
+    }
+    bool over = false;
+    for (int r = 0; r < n; ++r) {
+        if (rowptr[r + 1] < rowptr[r]) {
+            set_last_error(GDMR_EINVAL, std::string(who) + ": row pointers are not non-decreasing");
+            return GDMR_EINVAL;
+        }
+        for (int q = rowptr[r]; q < rowptr[r + 1]; ++q) {
+            const int col = colidx[q];
+            if (col < 0 || col >= n) {
+                set_last_error(GDMR_EINVAL, std::string(who) + ": column index out of range");
+                return GDMR_EINVAL;
+            }
+            if (!over && std::find(pat.begin(), pat.end(), col - r) == pat.end()) {
+                pat.push_back(col - r);
+                over = pat.size() > (size_t)SELL_PATTERN;
+            }
+        }
+    }
+    if (over) pat.clear();
+    std::sort(pat.begin(), pat.end());
+    return GDMR_OK;
+}
+
+// Structured-grid form: the pattern is the 7-point (-P, -Q, -1, 0, 1, Q, P) or 5-point
+// (-Q, -1, 0, 1, Q) offset set of a lexicographic grid, nx = Q, P = nx ny, n = P nz, and no
+// non-zero couples two rows across the grid's edge (the grid kernel leaves those terms out).
+// dims <- {nx, ny, nz}, zeros if the matrix has no such form.
+static void grid_form(int n, const int *rowptr, const int *colidx, const double *vals_ri, const std::vector<int> &pat,
+                      int dims[3]) {
+    dims[0] = dims[1] = dims[2] = 0;
+    const int np = (int)pat.size();
+    if (np != 7 && np != 5) return;
+    const int b = np == 7 ? 1 : 0;
+    const long Q = -(long)pat[b], P = np == 7 ? -(long)pat[0] : (long)n;
+    bool ok = Q > 1 && pat[b + 1] == -1 && pat[b + 2] == 0 && pat[b + 3] == 1 && pat[b + 4] == Q && P % Q == 0 &&
+              n % P == 0 && P / Q > 1;
+    if (np == 7) ok = ok && pat[6] == P && n / P > 1;
+    if (!ok) return;
+    const int gx = (int)Q, gy = (int)(P / Q), gz = (int)(n / P);
+    for (int r = 0; r < n; ++r) {
+        const int ix = r % gx, iy = (r / gx) % gy, iz = (int)(r / P);
+        for (int q = rowptr[r]; q < rowptr[r + 1]; ++q) {
+            const long dlt = (long)colidx[q] - r;
+            if (vals_ri[2 * (size_t)q] == 0.0 && vals_ri[2 * (size_t)q + 1] == 0.0) continue;
+            if ((dlt == -1 && ix == 0) || (dlt == 1 && ix == gx - 1) || (dlt == -Q && iy == 0) ||
+                (dlt == Q && iy == gy - 1) || (np == 7 && ((dlt == -P && iz == 0) || (dlt == P && iz == gz - 1))))
+                return;
+        }
+    }
+    dims[0] = gx;
+    dims[1] = gy;
+    dims[2] = gz;
+}
+
+int csr_grid_form(int n, const int *rowptr, const int *colidx, const double *vals_ri, int dims[3]) {
+    dims[0] = dims[1] = dims[2] = 0;
+    std::vector<int> pat;
+    const int rc = csr_offsets(n, rowptr, colidx, pat, "csr_grid_form");
+    if (rc != GDMR_OK) return rc;
+    if (!vals_ri) {
+        set_last_error(GDMR_EINVAL, "csr_grid_form: null values");
+        return GDMR_EINVAL;
+    }
+    grid_form(n, rowptr, colidx, vals_ri, pat, dims);
+    return GDMR_OK;
 }
 
 // SELL-32 with an offset pattern.  When the column offsets (column - row) of all non-zeros form
@@ -88,33 +170,18 @@ size_t DeviceSell::bytes() const {
 // stored "uniform": entry e of row r is A[r][r + off[e]], zero where A has no such entry, so the
 // kernels form the column as r + off[e] instead of loading it (the column-index load, then the
 // dependent gather, was the latency chain of the operator kernels).  The explicit column array
-// is filled for every slice, so kernels that do not use the pattern read the same matrix.
+// is filled for every slice, so kernels that do not use the pattern read the same matrix.  A
+// matrix with the structured-grid form also gets its coefficient planes (SellMatrix::grid).
 int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, const double *vals_ri, bool want32,
                   bool want64, cudaStream_t st, bool wantdf) {
-    if (n <= 0 || !rowptr || !colidx || !vals_ri) {
-        set_last_error(GDMR_EINVAL, "sell_from_csr: empty matrix or null arrays");
+    std::vector<int> pat;
+    int rc = csr_offsets(n, rowptr, colidx, pat, "sell_from_csr");
+    if (rc != GDMR_OK) return rc;
+    if (!vals_ri) {
+        set_last_error(GDMR_EINVAL, "sell_from_csr: null values");
         return GDMR_EINVAL;
     }
     const int ns = (n + 31) / 32;
-    // the offset pattern: every distinct column - row, if there are at most SELL_PATTERN of them
-    std::vector<int> pat;
-    for (int r = 0; r < n; ++r) {
-        if (rowptr[r + 1] < rowptr[r]) {
-            set_last_error(GDMR_EINVAL, "sell_from_csr: row pointers are not non-decreasing");
-            return GDMR_EINVAL;
-        }
-        for (int q = rowptr[r]; q < rowptr[r + 1] && pat.size() <= (size_t)SELL_PATTERN; ++q) {
-            const int col = colidx[q];
-            if (col < 0 || col >= n) {
-                set_last_error(GDMR_EINVAL, "sell_from_csr: column index out of range");
-                return GDMR_EINVAL;
-            }
-            if (std::find(pat.begin(), pat.end(), col - r) == pat.end()) pat.push_back(col - r);
-        }
-        if (pat.size() > (size_t)SELL_PATTERN) break;
-    }
-    if (pat.size() > (size_t)SELL_PATTERN) pat.clear();
-    std::sort(pat.begin(), pat.end());
     const int np = (int)pat.size();
     std::vector<unsigned char> uni(ns, 0);
     std::vector<int> sp(ns + 1, 0);
@@ -178,7 +245,30 @@ int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, 
             }
         }
     }
+    int gdims[3];
+    grid_form(n, rowptr, colidx, vals_ri, pat, gdims);
+    const int gx = gdims[0], gy = gdims[1], gz = gdims[2];
+    // coefficient planes, duplicates of one column added in CSR order as for uniform slices
+    const size_t gsz = gx ? (size_t)np * n : 0;
+    std::vector<double> gre(gsz, 0.0), gim(gsz, 0.0);
+    if (gx)
+        for (int r = 0; r < n; ++r)
+            for (int q = rowptr[r]; q < rowptr[r + 1]; ++q) {
+                const size_t e = (size_t)(std::find(pat.begin(), pat.end(), colidx[q] - r) - pat.begin());
+                gre[e * n + r] += vals_ri[2 * (size_t)q];
+                gim[e * n + r] += vals_ri[2 * (size_t)q + 1];
+            }
     DeviceSell d;
+    // a failed allocation or copy frees what was already allocated
+#define SELL_CK_(call)                                                                                                 \
+    do {                                                                                                               \
+        cudaError_t e_ = (call);                                                                                       \
+        if (e_ != cudaSuccess) {                                                                                       \
+            sell_free(d);                                                                                              \
+            set_last_error(GDMR_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));                            \
+            return GDMR_ECUDA;                                                                                         \
+        }                                                                                                              \
+    } while (0)
     d.n = n;
     d.nnz = rowptr[n] - rowptr[0];
     d.padded = padded;
@@ -186,26 +276,57 @@ int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, 
     d.band = band;
     d.npat = np;
     for (int e = 0; e < np; ++e) d.pat[e] = pat[e];
-    GDMR_CK(cudaGetDevice(&d.device));
-    GDMR_CK(cudaMalloc(&d.slice_ptr, sizeof(int) * (ns + 1)));
-    GDMR_CK(cudaMalloc(&d.cols, sizeof(int) * std::max<long>(padded, 1)));
-    GDMR_CK(cudaMalloc(&d.uniform, (size_t)ns));
-    GDMR_CK(cudaMemcpyAsync(d.slice_ptr, sp.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice, st));
-    GDMR_CK(cudaMemcpyAsync(d.cols, cols.data(), sizeof(int) * padded, cudaMemcpyHostToDevice, st));
-    GDMR_CK(cudaMemcpyAsync(d.uniform, uni.data(), (size_t)ns, cudaMemcpyHostToDevice, st));
+    SELL_CK_(cudaGetDevice(&d.device));
+    SELL_CK_(cudaMalloc(&d.slice_ptr, sizeof(int) * (ns + 1)));
+    SELL_CK_(cudaMalloc(&d.cols, sizeof(int) * std::max<long>(padded, 1)));
+    SELL_CK_(cudaMalloc(&d.uniform, (size_t)ns));
+    SELL_CK_(cudaMemcpyAsync(d.slice_ptr, sp.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice, st));
+    SELL_CK_(cudaMemcpyAsync(d.cols, cols.data(), sizeof(int) * padded, cudaMemcpyHostToDevice, st));
+    SELL_CK_(cudaMemcpyAsync(d.uniform, uni.data(), (size_t)ns, cudaMemcpyHostToDevice, st));
     if (want32) {
-        GDMR_CK(cudaMalloc(&d.vals32, sizeof(float2) * std::max<long>(padded, 1)));
-        GDMR_CK(cudaMemcpyAsync(d.vals32, v32.data(), sizeof(float2) * padded, cudaMemcpyHostToDevice, st));
+        SELL_CK_(cudaMalloc(&d.vals32, sizeof(float2) * std::max<long>(padded, 1)));
+        SELL_CK_(cudaMemcpyAsync(d.vals32, v32.data(), sizeof(float2) * padded, cudaMemcpyHostToDevice, st));
     }
     if (want64) {
-        GDMR_CK(cudaMalloc(&d.vals64, sizeof(double2) * std::max<long>(padded, 1)));
-        GDMR_CK(cudaMemcpyAsync(d.vals64, v64.data(), sizeof(double2) * padded, cudaMemcpyHostToDevice, st));
+        SELL_CK_(cudaMalloc(&d.vals64, sizeof(double2) * std::max<long>(padded, 1)));
+        SELL_CK_(cudaMemcpyAsync(d.vals64, v64.data(), sizeof(double2) * padded, cudaMemcpyHostToDevice, st));
     }
     if (wantdf) {
-        GDMR_CK(cudaMalloc(&d.valsdf, sizeof(dfc) * std::max<long>(padded, 1)));
-        GDMR_CK(cudaMemcpyAsync(d.valsdf, vdf.data(), sizeof(dfc) * padded, cudaMemcpyHostToDevice, st));
+        SELL_CK_(cudaMalloc(&d.valsdf, sizeof(dfc) * std::max<long>(padded, 1)));
+        SELL_CK_(cudaMemcpyAsync(d.valsdf, vdf.data(), sizeof(dfc) * padded, cudaMemcpyHostToDevice, st));
     }
-    GDMR_CK(cudaStreamSynchronize(st));
+    if (gx) {
+        d.gx = gx;
+        d.gy = gy;
+        d.gz = gz;
+        // one precision at a time, each host copy released after its upload
+        if (want32) {
+            std::vector<float2> g(gsz);
+            for (size_t e = 0; e < gsz; ++e) g[e] = make_float2((float)gre[e], (float)gim[e]);
+            SELL_CK_(cudaMalloc(&d.grid32, sizeof(float2) * gsz));
+            SELL_CK_(cudaMemcpyAsync(d.grid32, g.data(), sizeof(float2) * gsz, cudaMemcpyHostToDevice, st));
+            SELL_CK_(cudaStreamSynchronize(st));
+        }
+        if (want64) {
+            std::vector<double2> g(gsz);
+            for (size_t e = 0; e < gsz; ++e) g[e] = make_double2(gre[e], gim[e]);
+            SELL_CK_(cudaMalloc(&d.grid64, sizeof(double2) * gsz));
+            SELL_CK_(cudaMemcpyAsync(d.grid64, g.data(), sizeof(double2) * gsz, cudaMemcpyHostToDevice, st));
+            SELL_CK_(cudaStreamSynchronize(st));
+        }
+        if (wantdf) {
+            std::vector<dfc> g(gsz);
+            for (size_t e = 0; e < gsz; ++e) {
+                g[e].x = dfr(gre[e]);
+                g[e].y = dfr(gim[e]);
+            }
+            SELL_CK_(cudaMalloc(&d.griddf, sizeof(dfc) * gsz));
+            SELL_CK_(cudaMemcpyAsync(d.griddf, g.data(), sizeof(dfc) * gsz, cudaMemcpyHostToDevice, st));
+            SELL_CK_(cudaStreamSynchronize(st));
+        }
+    }
+    SELL_CK_(cudaStreamSynchronize(st));
+#undef SELL_CK_
     sell_free(out);
     out = d;
     return GDMR_OK;
@@ -218,6 +339,9 @@ void sell_free(DeviceSell &s) {
     if (s.vals32) cudaFree(s.vals32);
     if (s.vals64) cudaFree(s.vals64);
     if (s.valsdf) cudaFree(s.valsdf);
+    if (s.grid32) cudaFree(s.grid32);
+    if (s.grid64) cudaFree(s.grid64);
+    if (s.griddf) cudaFree(s.griddf);
     s = DeviceSell();
 }
 

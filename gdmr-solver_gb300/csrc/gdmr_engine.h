@@ -42,22 +42,34 @@ struct DeviceSell {
     unsigned char *uniform = nullptr;  // per slice: 1 = columns are row + pat[e]
     int npat = 0;                      // offset pattern (0: none)
     int pat[SELL_PATTERN] = {};
-    SellMatrix view(const void *v) const {
+    // structured-grid coefficient planes per precision (null: the matrix is not a grid stencil)
+    float2 *grid32 = nullptr;
+    double2 *grid64 = nullptr;
+    dfc *griddf = nullptr;
+    int gx = 0, gy = 0, gz = 0;
+    SellMatrix view(const void *v, const void *g) const {
         SellMatrix m{n, nslices, slice_ptr, cols, v, nnz};
         m.uniform = uniform;
         m.npat = npat;
         for (int e = 0; e < SELL_PATTERN; ++e) m.pat[e] = pat[e];
+        m.grid = g;
+        m.gx = gx;
+        m.gy = gy;
+        m.gz = gz;
         return m;
     }
-    SellMatrix view32() const { return view(vals32); }
-    SellMatrix view64() const { return view(vals64); }
-    SellMatrix viewdf() const { return view(valsdf); }
+    SellMatrix view32() const { return view(vals32, grid32); }
+    SellMatrix view64() const { return view(vals64, grid64); }
+    SellMatrix viewdf() const { return view(valsdf, griddf); }
+    int grid_planes() const { return gx == 0 ? 0 : (gz > 1 ? 7 : 5); }
     size_t bytes() const;
 };
 // Builds the SELL-32 form of a CSR matrix (values interleaved re,im doubles).
 int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, const double *vals_ri, bool want32,
                   bool want64, cudaStream_t st, bool wantdf = false);
 void sell_free(DeviceSell &s);
+// Host check of a CSR matrix for the structured-grid form: dims <- {nx, ny, nz}, zeros if none.
+int csr_grid_form(int n, const int *rowptr, const int *colidx, const double *vals_ri, int dims[3]);
 
 // Operator seen by an engine of precision R.
 template <class R> struct Operator {

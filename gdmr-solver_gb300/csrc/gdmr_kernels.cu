@@ -2981,6 +2981,89 @@ __global__ void __launch_bounds__(NT) k_stencil(int nx, int ny, int nz, double2 
     }
 }
 
+// ----------------------------------------------------------------- structured-grid operator
+// The SELL matrix's grid form (coefficient planes, SellMatrix::grid) on the stencil kernel's
+// schedule: a CTA is a 32 x 8 tile of (x, y) and a chunk of GR_ZC planes, each thread marches
+// up z holding, per system, the x values of the plane below and of its own row in registers;
+// in-plane neighbours come from the tile's other rows (L1).  A thread loads its row's
+// coefficients once per plane and applies them to SG systems.  Blocks are numbered system group
+// fastest, so the groups of one tile run side by side and its coefficients come from DRAM once
+// and from L2 for the other groups.  Terms are added in ascending offset order (-P, -Q, -1, 0,
+// +1, +Q, +P), the order in which the SELL kernels add a stencil row; a term whose neighbour
+// lies outside the grid is left out where the SELL kernels add a stored zero times x.  So both
+// forms give the same values for a matrix whose CSR rows are sorted and free of duplicates.
+constexpr int GR_ZC = 8;
+template <class R, int SG>
+__global__ void __launch_bounds__(NT) k_grid_spmm(int nx, int ny, int nz, int ngroups, int ntiles,
+                                                  const typename CT<R>::t *__restrict__ coef,
+                                                  const typename CT<R>::t *__restrict__ x0, size_t strideX,
+                                                  typename CT<R>::t *__restrict__ y0, size_t strideY,
+                                                  const int *__restrict__ act, int nsys,
+                                                  const SysState *__restrict__ scale,
+                                                  typename CT<R>::t *__restrict__ vout0, size_t strideVO) {
+    using C = typename CT<R>::t;
+    const int grp = (int)(blockIdx.x % (unsigned)ngroups);
+    const int rest = (int)(blockIdx.x / (unsigned)ngroups);
+    const int tile = rest % ntiles, zc = rest / ntiles;
+    const int tilesx = (nx + 31) / 32;
+    const int ix = (tile % tilesx) * 32 + (int)(threadIdx.x & 31);
+    const int iy = (tile / tilesx) * 8 + (int)(threadIdx.x >> 5);
+    if (ix >= nx || iy >= ny) return;
+    const int g0 = grp * SG, ng = min(SG, nsys - g0);
+    const long plane = (long)nx * ny, n = plane * nz;
+    const bool d3 = nz > 1;
+    const C *cf = coef + (d3 ? n : 0);   // the -Q plane (the -P plane precedes it in 3D)
+    const int z0 = zc * GR_ZC, z1 = min(nz, z0 + GR_ZC);
+    long idx = (long)iy * nx + ix + (long)z0 * plane;
+    const C *xs[SG];
+    C below[SG], cur[SG];
+#pragma unroll
+    for (int g = 0; g < SG; ++g) {
+        if (g < ng) {
+            xs[g] = x0 + (size_t)act[g0 + g] * strideX;
+            below[g] = z0 > 0 ? xs[g][idx - plane] : czero<C>();
+            cur[g] = xs[g][idx];
+        }
+    }
+    const bool xl = ix > 0, xh = ix + 1 < nx, yl = iy > 0, yh = iy + 1 < ny;
+    for (int z = z0; z < z1; ++z, idx += plane) {
+        const bool zl = z > 0, zh = z + 1 < nz;
+        const C amP = zl ? coef[idx] : czero<C>();
+        const C amQ = cf[idx], am1 = cf[n + idx], a00 = cf[2 * n + idx], ap1 = cf[3 * n + idx], apQ = cf[4 * n + idx];
+        const C apP = zh ? cf[5 * n + idx] : czero<C>();
+#pragma unroll
+        for (int g = 0; g < SG; ++g) {
+            if (g < ng) {
+                const C *x = xs[g];
+                const C above = zh ? x[idx + plane] : czero<C>();
+                C acc = czero<C>();
+                if (zl) cfma(acc, amP, below[g]);
+                if (yl) cfma(acc, amQ, x[idx - nx]);
+                if (xl) cfma(acc, am1, x[idx - 1]);
+                cfma(acc, a00, cur[g]);
+                if (xh) cfma(acc, ap1, x[idx + 1]);
+                if (yh) cfma(acc, apQ, x[idx + nx]);
+                if (zh) cfma(acc, apP, above);
+                const int sys = act[g0 + g];
+                if (scale) {   // pending normalisation, as in k_spmm
+                    const SysState &stt = scale[sys];
+                    const R al = (R)stt.alpha;
+                    C v = cur[g];
+                    v.x = v.x * al;
+                    v.y = v.y * al;
+                    acc.x = acc.x * al;
+                    acc.y = acc.y * al;
+                    if (stt.broken) v = czero<C>();
+                    vout0[(size_t)sys * strideVO + idx] = canon(v);
+                }
+                y0[(size_t)sys * strideY + idx] = canon(acc);
+                below[g] = cur[g];
+                cur[g] = above;
+            }
+        }
+    }
+}
+
 // One system: two rows a thread (row r and r + NT of a 2*NT-row chunk), both rows' entries
 // loaded before any gather, so the two dependent trips (column index, then x) overlap across
 // the rows; rows wider than WMAX take the generic loop.
@@ -4112,6 +4195,10 @@ bool launch_krylov_small(int n, int kk, int m, const SellMatrix &A, const typena
     }
 }
 
+static std::atomic<int> g_grid_operator{1};
+void set_grid_operator(int enable) { g_grid_operator.store(enable ? 1 : 0); }
+int grid_operator() { return g_grid_operator.load(); }
+
 SellPattern sell_pattern(const SellMatrix &A) {
     SellPattern p{};
     p.uniform = A.npat > 0 ? A.uniform : nullptr;
@@ -4127,6 +4214,22 @@ void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX
     // with the normalisation folded in, the kernel also writes v_s: one more vector a system
     Launch L_(KC_SPMM, spmm_bytes(A, sizeof(typename CT<R>::t), nsys) +
                            (scale ? (double)sizeof(typename CT<R>::t) * A.n * nsys : 0.0), st, 1);
+    if (A.grid && grid_operator()) {
+        const int ntiles = ((A.gx + 31) / 32) * ((A.gy + 7) / 8), nzc = (A.gz + GR_ZC - 1) / GR_ZC;
+        const int sg = nsys == 1 ? 1 : 4;
+        const int ngroups = (nsys + sg - 1) / sg;
+        const long blocks = (long)ngroups * ntiles * nzc;
+        if (blocks <= 0x7fffffffL) {
+            const auto *cf = (const typename CT<R>::t *)A.grid;
+            if (sg == 1)
+                k_grid_spmm<R, 1><<<(unsigned)blocks, NT, 0, st>>>(A.gx, A.gy, A.gz, ngroups, ntiles, cf, x, strideX, y,
+                                                                   strideY, act, nsys, scale, vout, strideVO);
+            else
+                k_grid_spmm<R, 4><<<(unsigned)blocks, NT, 0, st>>>(A.gx, A.gy, A.gz, ngroups, ntiles, cf, x, strideX, y,
+                                                                   strideY, act, nsys, scale, vout, strideVO);
+            return;
+        }
+    }
     if (nsys == 1) {
         const long chunks = ((long)A.n + 2 * NT - 1) / (2 * NT);
         k_spmv2<R><<<(unsigned)chunks, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const typename CT<R>::t *)A.vals, x,

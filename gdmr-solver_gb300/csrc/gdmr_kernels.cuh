@@ -248,7 +248,16 @@ struct SellMatrix {
     const unsigned char *uniform = nullptr;   // per slice: 1 = column of entry e is row + pat[e]
     int npat = 0;                              // offset pattern (0: none)
     int pat[SELL_PATTERN] = {};
+    // Structured-grid form (null: none): the same matrix as coefficient planes on a gx x gy x gz
+    // grid, plane p = A[r][r + off_p] for every row r, offsets ascending (-P, -Q, -1, 0, +1, +Q,
+    // +P with Q = gx, P = gx gy; 2D (gz = 1): the middle five), values of the same type as `vals`.
+    const void *grid = nullptr;
+    int gx = 0, gy = 0, gz = 0;
 };
+// Process-wide switch for the structured-grid operator kernel (on by default); launch_spmm
+// takes the SELL kernels when it is off or the matrix has no grid form.
+void set_grid_operator(int enable);
+int grid_operator();
 // Matrix-free constant-coefficient stencil on an nx x ny x nz grid (nz = 1: 5-point 2D),
 // unknowns numbered i + nx (j + ny l), Dirichlet boundary (neighbours outside are dropped):
 //   y = d x + wx (x[i-1] + x[i+1]) + wy (x[j-1] + x[j+1]) + wz (x[l-1] + x[l+1]).

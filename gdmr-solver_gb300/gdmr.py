@@ -58,6 +58,8 @@ SIGNATURES = {
     "gdmrTune": (None, [I]),
     "gdmrTuneReport": (ctypes.c_char_p, []),
     "gdmrTuneForce": (None, [I, I]),
+    "gdmrGridOperator": (None, [I]),
+    "gdmr_csr_grid_form": (I, [I, P, P, P, P]),
     "gdmrAsyncTimeouts": (ctypes.c_uint, []),
     "gdmr_hessenberg_svd": (I, [I, I, P, P, P, P]),
     "gdmr_system_set_stencil": (I, [P, I, I, I, P]),
@@ -68,6 +70,7 @@ SIGNATURES = {
     "gdmr_system_svd_sweeps": (I, [P]),
     "gdmr_system_set_graphs": (I, [P, I]),
     "gdmr_system_set_fused": (I, [P, I]),
+    "gdmr_system_grid": (I, [P, P]),
     "gdmr_solve": (I, [P, I, P, P, D, I, I, P]),
     "gdmr_solve_batch": (I, [P, I, P, P, P, I, I, P]),
     "gdmr_true_residual": (I, [P, I, P, P, I, P]),
@@ -135,6 +138,24 @@ def async_timeouts() -> int:
 def tune_force(projection: int = -1, update: int = -1) -> None:
     """Pins the Gram-Schmidt variants (index as in tune_report; -1 hands back to the tuner)."""
     load().gdmrTuneForce(int(projection), int(update))
+
+
+def grid_operator(enable: bool) -> None:
+    """Structured-grid operator kernel for matrices with a grid form (on by default); off sends
+    the products launched afterwards to the SELL-32 kernels."""
+    load().gdmrGridOperator(1 if enable else 0)
+
+
+def csr_grid_form(A):
+    """(nx, ny, nz) if the CSR matrix A (n, indptr, indices, data) has the structured-grid form
+    of the grid operator kernel, else None.  Host-only."""
+    indptr = np.ascontiguousarray(A.indptr, dtype=np.int32)
+    indices = np.ascontiguousarray(A.indices, dtype=np.int32)
+    vals = np.ascontiguousarray(np.asarray(A.data, dtype=np.complex128).view(np.float64))
+    dims = np.zeros(3, dtype=np.int32)
+    _check(load().gdmr_csr_grid_form(int(A.n), _ptr(indptr), _ptr(indices), _ptr(vals), _ptr(dims)),
+           "gdmr_csr_grid_form")
+    return tuple(int(d) for d in dims) if dims[0] > 0 else None
 
 
 def hessenberg_svd(H: np.ndarray, k: int, with_sweeps: bool = False):
@@ -347,6 +368,12 @@ class System:
     def set_fused(self, on: bool) -> None:
         """One small system: run the Krylov loop as one cooperative kernel (default) or step by step."""
         _check(self.L.gdmr_system_set_fused(self._h, 1 if on else 0), "gdmr_system_set_fused")
+
+    def grid_shape(self):
+        """(nx, ny, nz) if the CSR operator has the structured-grid form, else None."""
+        dims = np.zeros(3, dtype=np.int32)
+        _check(self.L.gdmr_system_grid(self._h, _ptr(dims)), "gdmr_system_grid")
+        return tuple(int(d) for d in dims) if dims[0] > 0 else None
 
     def set_stencil(self, shape, d, wx, wy, wz=0.0) -> None:
         """Matrix-free inner operator: the constant-coefficient stencil on a grid of `shape`

@@ -114,6 +114,20 @@ const char *gdmrTuneReport(void);
  * projection 7 and update 6 (CUDA cores). */
 void gdmrTuneForce(int projectionVariant, int updateVariant);
 
+/* Structured-grid operator kernel (on by default).  A CSR matrix whose non-zeros all lie on the
+ * 5- or 7-point offsets (-nx ny, -nx, -1, 0, +1, +nx, +nx ny) of a lexicographic nx x ny (x nz)
+ * grid, none coupling two rows across the grid's edge, is also kept as coefficient planes, and
+ * its products run on a kernel that walks the grid's planes with the x values in registers
+ * instead of gathering them per row.  It adds the terms in the order the SELL-32 kernels do, so
+ * a matrix with sorted, duplicate-free CSR rows gives the same values either way.  0 sends the
+ * products launched after the call to the SELL-32 kernels (CUDA graphs already captured keep
+ * the kernels they captured). */
+void gdmrGridOperator(int enable);
+
+/* Host-only check of a CSR matrix (complex values interleaved re, im) for the structured-grid
+ * form: dims[0..2] <- (nx, ny, nz), zeros if it has none.  GDMR_EINVAL for malformed arrays. */
+int gdmr_csr_grid_form(int n, const int *rowPtr, const int *colIdx, const double *vals_ri, int *dims);
+
 /* ---- context API: one resident operator, many right-hand sides -------------
  * A gdmr_system holds a CSR operator on the device (SELL-32, complex64 and
  * complex128 values), a solver engine of `capacity` systems and one recycled
@@ -148,6 +162,10 @@ int gdmr_system_set_graphs(gdmr_system *sys, int on);
  * at once): the Krylov loop of a restart cycle runs as one cooperative kernel (on by default;
  * 0 launches its operator, projection, update and scaling kernels step by step). */
 int gdmr_system_set_fused(gdmr_system *sys, int on);
+
+/* dims[0..2] <- the grid's edge lengths (nx, ny, nz) if the system's CSR operator has the
+ * structured-grid form (gdmrGridOperator), zeros if not. */
+int gdmr_system_grid(const gdmr_system *sys, int *dims);
 
 /* Reference-semantics solve of one right-hand side (solverDMR's algorithm,
  * complex128, complex64 or double-float per the system's precision), then the true FP64

@@ -1,4 +1,5 @@
-"""The SELL-32 operator store, with and without its offset pattern, against scipy.
+"""The SELL-32 operator store, with and without its offset pattern, and the structured-grid
+kernel, against scipy.
 
 A matrix whose column offsets (column - row) take at most 8 values is stored with the offsets
 as a pattern: the operator kernels form the columns as row + offset instead of loading them, and
@@ -8,6 +9,8 @@ entries the pattern has but a row lacks are stored as zeros.  Through the plugin
   * a 2D 5-point operator whose CSR rows are shuffled and carry split (duplicate) entries;
   * a 3D 7-point operator, whose first and last planes' slices cannot use the pattern;
   * an unstructured random matrix (more than 8 offsets: no pattern at all).
+The two stencil matrices also have the structured-grid form: each case runs with the grid
+kernel on (the default) and off.
 """
 import numpy as np
 import pytest
@@ -17,6 +20,13 @@ import problems
 from problems import CSR
 
 pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(params=[True, False], ids=["grid", "sell"])
+def grid(request):
+    gdmr.grid_operator(request.param)
+    yield request.param
+    gdmr.grid_operator(True)
 
 
 def _apply(A, x):
@@ -57,12 +67,12 @@ def _check(A, seed):
     assert np.linalg.norm(y - ref) / np.linalg.norm(ref) < 1e-13
 
 
-def test_2d_pattern_with_shuffled_rows_and_duplicates():
+def test_2d_pattern_with_shuffled_rows_and_duplicates(grid):
     A = problems.helmholtz((37, 29), 12.0, 0.05)
     _check(_shuffled_with_duplicates(A, 3), 4)
 
 
-def test_3d_pattern_with_boundary_slices():
+def test_3d_pattern_with_boundary_slices(grid):
     _check(problems.helmholtz((12, 10, 9), 6.0, 0.1), 5)
 
 
