@@ -392,6 +392,9 @@ def main():
     ap.add_argument("--m", type=int, default=M, help="basis size m (profiling captures)")
     ap.add_argument("--stencil", action="store_true",
                     help="matrix-free 7-point operator for the inner cycles (default: the CSR operator)")
+    ap.add_argument("--grid-batch", type=int, default=0, choices=[0, 1, 2, 4],
+                    help="batched operator products on the structured-grid kernel with this many systems a "
+                         "thread (0: the SELL-32 kernel, the library's default for batches)")
     ap.add_argument("--sell", action="store_true",
                     help="CSR operator products on the SELL-32 kernels (default: the structured-grid kernel, "
                          "which the 7-point CSR operator qualifies for)")
@@ -427,6 +430,8 @@ def main():
         gdmr.tune_force(*(int(v) for v in args.force_variants.split(",")))
     if args.sell:
         gdmr.grid_operator(False)
+    if args.grid_batch:
+        gdmr.grid_batch(args.grid_batch)
     shape = (args.grid,) * 3
     A, B = build_workload(args.nrhs, rank, shape)
     nrhs, n = B.shape
@@ -441,7 +446,10 @@ def main():
     if args.stencil:
         sysm.set_stencil(shape, *problems.helmholtz_stencil(shape, KAPPA, DAMPING))
     op_kernel = ("matrix-free stencil (k_stencil)" if args.stencil else
-                 "structured grid (k_grid_spmm)" if sysm.grid_shape() and not args.sell else "SELL-32 (k_spmm)")
+                 f"structured grid (k_grid_spmm, {args.grid_batch} systems a thread)"
+                 if sysm.grid_shape() and not args.sell and args.grid_batch else
+                 "SELL-32 (k_spmm) for the batch, structured grid (k_grid_spmm) for single vectors"
+                 if sysm.grid_shape() and not args.sell else "SELL-32 (k_spmm, k_spmv2)")
     Bd = torch.from_numpy(B).to(f"cuda:{local}")
     Xd = torch.zeros_like(Bd)
     tols = [TOL] * nrhs

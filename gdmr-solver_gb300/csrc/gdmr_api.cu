@@ -388,6 +388,7 @@ extern "C" void gdmrTuneForce(int projectionVariant, int updateVariant) {
     tune_force(projectionVariant, updateVariant);
 }
 extern "C" void gdmrGridOperator(int enable) { set_grid_operator(enable); }
+extern "C" void gdmrGridBatch(int systemsPerThread) { set_grid_batch(systemsPerThread); }
 extern "C" const char *gdmrTuneReport(void) {
     static thread_local std::string rep;
     rep = tune_report();

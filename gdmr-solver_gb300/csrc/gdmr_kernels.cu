@@ -4196,8 +4196,11 @@ bool launch_krylov_small(int n, int kk, int m, const SellMatrix &A, const typena
 }
 
 static std::atomic<int> g_grid_operator{1};
+static std::atomic<int> g_grid_batch{0};
 void set_grid_operator(int enable) { g_grid_operator.store(enable ? 1 : 0); }
 int grid_operator() { return g_grid_operator.load(); }
+void set_grid_batch(int sg) { g_grid_batch.store(sg == 1 || sg == 2 || sg == 4 ? sg : 0); }
+int grid_batch() { return g_grid_batch.load(); }
 
 SellPattern sell_pattern(const SellMatrix &A) {
     SellPattern p{};
@@ -4214,19 +4217,23 @@ void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX
     // with the normalisation folded in, the kernel also writes v_s: one more vector a system
     Launch L_(KC_SPMM, spmm_bytes(A, sizeof(typename CT<R>::t), nsys) +
                            (scale ? (double)sizeof(typename CT<R>::t) * A.n * nsys : 0.0), st, 1);
-    if (A.grid && grid_operator()) {
+    const int sg = nsys == 1 ? 1 : grid_batch();
+    if (A.grid && grid_operator() && sg > 0) {
         const int ntiles = ((A.gx + 31) / 32) * ((A.gy + 7) / 8), nzc = (A.gz + GR_ZC - 1) / GR_ZC;
-        const int sg = nsys == 1 ? 1 : 4;
         const int ngroups = (nsys + sg - 1) / sg;
         const long blocks = (long)ngroups * ntiles * nzc;
         if (blocks <= 0x7fffffffL) {
             const auto *cf = (const typename CT<R>::t *)A.grid;
+#define GRID_LAUNCH_(SGV)                                                                                              \
+    k_grid_spmm<R, SGV><<<(unsigned)blocks, NT, 0, st>>>(A.gx, A.gy, A.gz, ngroups, ntiles, cf, x, strideX, y, strideY, \
+                                                         act, nsys, scale, vout, strideVO)
             if (sg == 1)
-                k_grid_spmm<R, 1><<<(unsigned)blocks, NT, 0, st>>>(A.gx, A.gy, A.gz, ngroups, ntiles, cf, x, strideX, y,
-                                                                   strideY, act, nsys, scale, vout, strideVO);
+                GRID_LAUNCH_(1);
+            else if (sg == 2)
+                GRID_LAUNCH_(2);
             else
-                k_grid_spmm<R, 4><<<(unsigned)blocks, NT, 0, st>>>(A.gx, A.gy, A.gz, ngroups, ntiles, cf, x, strideX, y,
-                                                                   strideY, act, nsys, scale, vout, strideVO);
+                GRID_LAUNCH_(4);
+#undef GRID_LAUNCH_
             return;
         }
     }

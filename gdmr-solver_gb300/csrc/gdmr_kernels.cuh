@@ -255,9 +255,13 @@ struct SellMatrix {
     int gx = 0, gy = 0, gz = 0;
 };
 // Process-wide switch for the structured-grid operator kernel (on by default); launch_spmm
-// takes the SELL kernels when it is off or the matrix has no grid form.
+// takes the SELL kernels when it is off or the matrix has no grid form.  grid_batch: systems a
+// thread of a launch over several systems (1, 2 or 4); 0 (default) keeps those launches on the
+// SELL kernel.
 void set_grid_operator(int enable);
 int grid_operator();
+void set_grid_batch(int sg);
+int grid_batch();
 // Matrix-free constant-coefficient stencil on an nx x ny x nz grid (nz = 1: 5-point 2D),
 // unknowns numbered i + nx (j + ny l), Dirichlet boundary (neighbours outside are dropped):
 //   y = d x + wx (x[i-1] + x[i+1]) + wy (x[j-1] + x[j+1]) + wz (x[l-1] + x[l+1]).

@@ -59,6 +59,7 @@ SIGNATURES = {
     "gdmrTuneReport": (ctypes.c_char_p, []),
     "gdmrTuneForce": (None, [I, I]),
     "gdmrGridOperator": (None, [I]),
+    "gdmrGridBatch": (None, [I]),
     "gdmr_csr_grid_form": (I, [I, P, P, P, P]),
     "gdmrAsyncTimeouts": (ctypes.c_uint, []),
     "gdmr_hessenberg_svd": (I, [I, I, P, P, P, P]),
@@ -144,6 +145,12 @@ def grid_operator(enable: bool) -> None:
     """Structured-grid operator kernel for matrices with a grid form (on by default); off sends
     the products launched afterwards to the SELL-32 kernels."""
     load().gdmrGridOperator(1 if enable else 0)
+
+
+def grid_batch(systems_per_thread: int) -> None:
+    """Batched operator products on the grid kernel with 1, 2 or 4 systems a thread; 0 (the
+    default) keeps them on the SELL-32 kernel."""
+    load().gdmrGridBatch(int(systems_per_thread))
 
 
 def csr_grid_form(A):

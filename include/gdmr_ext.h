@@ -123,6 +123,10 @@ void gdmrTuneForce(int projectionVariant, int updateVariant);
  * products launched after the call to the SELL-32 kernels (CUDA graphs already captured keep
  * the kernels they captured). */
 void gdmrGridOperator(int enable);
+/* Products over several systems at once (the batched solves) take the grid kernel only when
+ * this is 1, 2 or 4 (systems a thread; the coefficients are loaded once for them); 0, the
+ * default, keeps them on the SELL-32 kernel, which measured faster for the 64-system batch. */
+void gdmrGridBatch(int systemsPerThread);
 
 /* Host-only check of a CSR matrix (complex values interleaved re, im) for the structured-grid
  * form: dims[0..2] <- (nx, ny, nz), zeros if it has none.  GDMR_EINVAL for malformed arrays. */

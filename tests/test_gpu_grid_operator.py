@@ -5,10 +5,11 @@ products run on the grid kernel (gdmrGridOperator, on by default).  The kernel a
 terms in the order the SELL kernels do and leaves out only terms whose neighbour lies outside
 the grid (where SELL adds a stored zero times x), so for a matrix with sorted, duplicate-free
 CSR rows every product, and with it every solve, must come out identical:
-  * mixed batched solves of 7 and 5 right-hand sides (system groups of 4, the last one partial;
-    batches that shrink as systems converge), on a 3D grid whose x and y edges leave partial
-    tiles and whose z edge a partial chunk of planes, and on a 2D grid with variable
-    coefficients;
+  * mixed batched solves of 7 and 5 right-hand sides, with the batched products on the grid
+    kernel at 1, 2 and 4 systems a thread (the last group partial; batches that shrink as
+    systems converge) and on SELL (the default, where only single-vector products take the grid
+    kernel), on a 3D grid whose x and y edges leave partial tiles and whose z edge a partial
+    chunk of planes, and on a 2D grid with variable coefficients;
   * plain complex128 and double-float solves of one right-hand side (step-by-step Krylov loop).
 The tuner is settled by a first solve, so both runs take the same Gram-Schmidt variants.
 """
@@ -21,8 +22,9 @@ import problems
 pytestmark = pytest.mark.gpu
 
 
-def _batch(A, B, m, k, precision, grid):
+def _batch(A, B, m, k, precision, grid, sg=0):
     gdmr.grid_operator(grid)
+    gdmr.grid_batch(sg)
     try:
         s = gdmr.System(A, m, k, capacity=B.shape[0], precision=precision)
         try:
@@ -32,6 +34,7 @@ def _batch(A, B, m, k, precision, grid):
             s.close()
     finally:
         gdmr.grid_operator(True)
+        gdmr.grid_batch(0)
     return shape, X, stats
 
 
@@ -55,13 +58,14 @@ CASES = {
 }
 
 
+@pytest.mark.parametrize("sgt", [0, 1, 2, 4])
 @pytest.mark.parametrize("case", sorted(CASES))
-def test_mixed_batch_is_identical_on_both_kernels(case):
+def test_mixed_batch_is_identical_on_both_kernels(case, sgt):
     make, shape, nrhs = CASES[case]
     A = make()
     B = np.array([problems.unit_gaussian_rhs(A.n, 40 + i) for i in range(nrhs)])
-    _batch(A, B, 30, 10, "mixed", True)                      # settles the tuner
-    g_shape, Xg, sg = _batch(A, B, 30, 10, "mixed", True)
+    _batch(A, B, 30, 10, "mixed", True, sgt)                 # settles the tuner
+    g_shape, Xg, sg = _batch(A, B, 30, 10, "mixed", True, sgt)
     s_shape, Xs, ss = _batch(A, B, 30, 10, "mixed", False)
     assert g_shape == shape and s_shape == shape
     for i in range(nrhs):
