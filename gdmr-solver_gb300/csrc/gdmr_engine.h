@@ -47,7 +47,6 @@ struct DeviceSell {
     double2 *grid64 = nullptr;
     dfc *griddf = nullptr;
     int gx = 0, gy = 0, gz = 0;
-    unsigned greal = 0;                // bit p: plane p is real (imaginary parts all zero)
     SellMatrix view(const void *v, const void *g) const {
         SellMatrix m{n, nslices, slice_ptr, cols, v, nnz};
         m.uniform = uniform;
@@ -57,7 +56,6 @@ struct DeviceSell {
         m.gx = gx;
         m.gy = gy;
         m.gz = gz;
-        m.greal = greal;
         return m;
     }
     SellMatrix view32() const { return view(vals32, grid32); }
