@@ -221,7 +221,7 @@ def run_reference(args, world, rank):
 
 
 def run_serve(args, rank):
-    """Serving workload (BASELINE configs[4]): six resident operators (7-point Helmholtz 64^3 /
+    """Serving workload: six resident operators (7-point Helmholtz 64^3 /
     96^3 / 128^3 with kappa 16 / 24 / 32, each at damping 0.05 and 0.2), Poisson arrivals,
     each request picks an operator uniformly and brings one Gaussian-source right-hand side
     with a tolerance drawn from {1e-6, 1e-8, 1e-10}; m = 48, k = 24 per operator; device
@@ -276,7 +276,7 @@ def run_serve(args, rank):
 
 
 def run_multi_operator(args, rank):
-    """BASELINE configs[3]: 48 independent operators, 3D 7-point -div(a grad u) - kappa^2 (1+0.1i) u
+    """Many-operator workload: 48 independent operators, 3D 7-point -div(a grad u) - kappa^2 (1+0.1i) u
     with per-axis edge lengths log-uniform in [32, 128] (seeded), a piecewise constant on 8^3
     blocks (Re U[1,4], Im U[0,0.2]), kappa 16; 4 complex Gaussian right-hand sides each;
     m = 40, k = 16, tolerance 1e-9.  All 48 operators are resident at once, each with its own
@@ -315,7 +315,7 @@ def run_multi_operator(args, rank):
 
 
 def run_small(args, rank):
-    """BASELINE configs[0] (the reference-parity case): 2D 5-point Helmholtz 64x64, kappa 20,
+    """The reference-parity case: 2D 5-point Helmholtz 64x64, kappa 20,
     damping 0.05; 8 unit Gaussian right-hand sides solved in sequence with the recycled
     deflation space (mode 0 then 1); m = 40, k = 10, tol 1e-10; the plain FP64 drop-in
     (reference algorithm in complex128) through gdmr_solve, with and without CUDA graphs,
