@@ -2334,11 +2334,11 @@ __device__ __forceinline__ float jacobi_t(float zeta) {
 
 // Sweeps of FP32 one-sided Jacobi on A (rows x m) accumulating V (m x m; none when V is null),
 // both column-major with leading dimensions rows and m.  One warp per column pair, every lane
-// computing the
-// rotation parameters; the pairs of each round come from `tab` (p | q << 8, p < q, built by
-// pair_table), which takes the schedule arithmetic off the critical path of a round.  The angle only has to shrink the off-diagonal element (the
-// double-float phase finishes the job), so it uses the hardware estimates; c and the phase of
-// gamma are Newton-refined, which keeps each rotation unitary to about an ulp.
+// computing the rotation parameters; the pairs of each round come from `tab` (p | q << 8,
+// p < q, built by pair_table), which takes the schedule arithmetic off the critical path of a
+// round.  The angle only has to shrink the off-diagonal element (the double-float phase
+// finishes the job), so it uses the hardware estimates; c and the phase of gamma are
+// Newton-refined, which keeps each rotation unitary to about an ulp.
 __device__ int jacobi_sweeps_f32(int m, int rows, float2 *A, float2 *V, float *nrm, float tol, int max_sweeps,
                                  int *s_flag, float *s_off, const unsigned short *tab) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
