@@ -2766,12 +2766,15 @@ __global__ void __launch_bounds__(1024) k_svd(int m, int k, const double2 *__res
         V1 = V32;
     }
     __syncthreads();
-    // the k columns of smallest norm (smallest singular values) after the FP32 phase
+    // the k columns of smallest norm (smallest singular values) after the FP32 phase; a NaN
+    // (from a non-finite Hessenberg) sorts as -inf, so the order stays total and exactly k
+    // columns are flagged whatever the input
+    auto key32 = [](float v) { return v == v ? v : -INFINITY; };
     for (int c = tid; c < m; c += nt) {
-        const float s = nrm32[c];
+        const float s = key32(nrm32[c]);
         int below = 0;
         for (int c2 = 0; c2 < m; ++c2) {
-            const float s2 = nrm32[c2];
+            const float s2 = key32(nrm32[c2]);
             below += (s2 < s) || (s2 == s && c2 < c);
         }
         small_col[c] = below < k ? 1 : 0;
@@ -2896,22 +2899,26 @@ __global__ void __launch_bounds__(1024) k_svd(int m, int k, const double2 *__res
                                      flag_list, k, coefs);
     // singular values in descending order (ties broken by column index); the output vectors are
     // the flagged columns, the only ones polished, in descending order of their values
+    // (NaN values sort as -inf: ranks and slots stay permutations, every slot is written)
+    auto keyd = [](dfr v) { return v.hi == v.hi && v.lo == v.lo ? v : dfr(-INFINITY, 0.f); };
     auto greater = [](dfr x, dfr y) { return x.hi > y.hi || (x.hi == y.hi && x.lo > y.lo); };
     auto same = [](dfr x, dfr y) { return x.hi == y.hi && x.lo == y.lo; };
     for (int c = tid; c < m; c += nt) {
-        const dfr s = nrmd[c];
+        const dfr s = keyd(nrmd[c]);
         int rank = 0, rank_f = 0;
         for (int c2 = 0; c2 < m; ++c2) {
-            const bool before = greater(nrmd[c2], s) || (same(nrmd[c2], s) && c2 < c);
+            const dfr s2 = keyd(nrmd[c2]);
+            const bool before = greater(s2, s) || (same(s2, s) && c2 < c);
             rank += before;
             rank_f += before && small_col[c2];
         }
-        sigma[rank] = sqrt((double)s) / sc;
+        sigma[rank] = sqrt((double)nrmd[c]) / sc;
         if (small_col[c]) slot_col[rank_f] = c;
     }
     __syncthreads();
     for (int e = tid; e < k * m; e += nt) {
-        const dfc v = Vd[(size_t)slot_col[e / m] * ldv + e % m];
+        const int col = min(max(slot_col[e / m], 0), m - 1);
+        const dfc v = Vd[(size_t)col * ldv + e % m];
         vs[e] = make_double2((double)v.x, (double)v.y);
     }
     if (tid == 0 && sweeps_out) *sweeps_out = s32 * 1000 + sdf;

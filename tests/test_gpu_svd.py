@@ -104,6 +104,20 @@ def test_near_degenerate_pair_at_the_boundary():
         assert np.linalg.norm(vs[:, t] - P @ (P.conj().T @ vs[:, t])) < 1e-13 / gap
 
 
+@pytest.mark.parametrize("m", [40, 96])
+def test_non_finite_hessenberg_returns_without_fault(m):
+    # a Hessenberg holding a NaN (an inner cycle that overflowed) must give NaN singular values
+    # and in-range output, not an out-of-range gather: the ranking keeps NaN in a total order
+    # and every output slot written; the next call on a finite matrix is still right
+    k = 10
+    H = _graded(m, 5, decades=3.0)
+    H[3, 2] = np.nan
+    sigma, vs = gdmr.hessenberg_svd(H, k)
+    assert sigma.shape == (m,) and vs.shape == (m, k)
+    assert np.isnan(sigma).any()
+    _check(_graded(m, 7 + m, decades=6.0), k if m == 40 else 24)
+
+
 def test_rejects_bad_sizes():
     with pytest.raises(gdmr.GDMRError):
         gdmr.hessenberg_svd(np.zeros((162, 161), complex), 4)
