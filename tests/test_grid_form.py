@@ -88,3 +88,19 @@ def test_malformed_csr_is_rejected():
     bad = CSR(A.n, A.indptr, np.where(np.arange(A.nnz) == 7, A.n, A.indices), A.data)
     with pytest.raises(gdmr.GDMRError):
         gdmr.csr_grid_form(bad)
+
+
+def test_column_check_covers_rows_after_the_pattern_overflows():
+    # an unstructured matrix has more than 8 offsets by its first rows; a bad column in the
+    # last row must still be caught (the operator kernels would gather through it)
+    rng = np.random.default_rng(4)
+    n, per = 300, 6
+    indptr = np.arange(0, (n + 1) * per, per)
+    indices = np.concatenate([np.sort(rng.choice(n, per, replace=False)) for _ in range(n)])
+    indices[-1] = n + 5
+    U = CSR(n, indptr, indices, rng.standard_normal(n * per) + 0j)
+    with pytest.raises(gdmr.GDMRError):
+        gdmr.csr_grid_form(U)
+    indices[-1] = -1
+    with pytest.raises(gdmr.GDMRError):
+        gdmr.csr_grid_form(CSR(n, indptr, indices, U.data))
