@@ -136,6 +136,7 @@ template <class R> struct Plugin {
     using C = typename CT<R>::t;
     int n = 0, dev = 0;
     C *src = nullptr, *img = nullptr, *tmp = nullptr, *opt = nullptr;
+    int *zero = nullptr;   // active list {0} of the one-system operator product, on this device
     DeviceSell csr;
     bool use_csr = false;
     cudaStream_t st = nullptr;
@@ -158,14 +159,8 @@ template <class R> void plugin_apply(Plugin<R> &P) {
     cudaSetDevice(P.dev);
     // y = A x into a separate buffer, then copy back: the reference's hook aliases input and output
     if (P.use_csr) {
-        int zero = 0;
-        static thread_local int *d_zero = nullptr;
-        if (!d_zero) {
-            cudaMalloc(&d_zero, sizeof(int));
-            cudaMemcpy(d_zero, &zero, sizeof(int), cudaMemcpyHostToDevice);
-        }
         SellMatrix A = sizeof(R) == 4 ? P.csr.view32() : P.csr.view64();
-        launch_spmm<R>(A, P.src, 0, P.tmp, 0, d_zero, 1, P.st);
+        launch_spmm<R>(A, P.src, 0, P.tmp, 0, P.zero, 1, P.st);
     } else {
         launch_dense_gemv<R>(P.n, P.opt, P.src, P.tmp, P.st);
     }
@@ -180,6 +175,7 @@ template <class R> void plugin_free(Plugin<R> &P) {
     if (P.img) cudaFree(P.img);
     if (P.tmp) cudaFree(P.tmp);
     if (P.opt) cudaFree(P.opt);
+    if (P.zero) cudaFree(P.zero);
     sell_free(P.csr);
     if (P.st) cudaStreamDestroy(P.st);
     P = Plugin<R>();
@@ -195,13 +191,15 @@ bool plugin_init(Plugin<R> &P, const char *name, int devNumLO, int cells) {
     if (cudaSetDevice(devNumLO) != cudaSuccess) { fail(GDMR_ECUDA, name, "Failed to set device"); return false; }
     const size_t vb = sizeof(C) * (size_t)cells;
     if (cudaMalloc(&P.src, vb) != cudaSuccess || cudaMalloc(&P.img, vb) != cudaSuccess ||
-        cudaMalloc(&P.tmp, vb) != cudaSuccess || cudaMalloc(&P.opt, vb * (size_t)cells) != cudaSuccess) {
+        cudaMalloc(&P.tmp, vb) != cudaSuccess || cudaMalloc(&P.opt, vb * (size_t)cells) != cudaSuccess ||
+        cudaMalloc(&P.zero, sizeof(int)) != cudaSuccess) {
         plugin_free(P);
         fail(GDMR_ENOMEM, name, "Failed to allocate device memory");
         return false;
     }
     cudaMemset(P.src, 0, vb);
     cudaMemset(P.img, 0, vb);
+    cudaMemset(P.zero, 0, sizeof(int));
     if (cudaStreamCreate(&P.st) != cudaSuccess) { plugin_free(P); fail(GDMR_ECUDA, name, "stream"); return false; }
     k_identity<C><<<1024, 256, 0, P.st>>>(cells, P.opt);
     cudaStreamSynchronize(P.st);
