@@ -205,7 +205,7 @@ _lib = None
 
 
 def load(path: str = LIB_PATH):
-    """Loads the library (building it first if the sources are newer)."""
+    """Loads the library, building it first if it is missing (`build.py` rebuilds a stale one)."""
     global _lib
     if _lib is not None:
         return _lib
