@@ -49,8 +49,8 @@ KAPPA, DAMPING, M, K, TOL = 24.0, 0.1, 48, 24, 1e-10
 
 
 # DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic byte, per kernel
-# class, from one capture of every launch of three batched cycles of this same workload
-# (profiles/dram_traffic_mixed96_64rhs.md, tensor-core shared-basis kernels in use).
+# class, measured by ncu over three batched cycles of this same workload with the tensor-core
+# shared-basis kernels in use.
 TRAFFIC_PER_ALGORITHMIC_BYTE = {"projection": 1.027, "update": 1.043, "operator": 0.938, "combine": 1.000,
                                 "deflation_update": 1.303, "residual64": 1.478, "other": 0.949}
 

@@ -869,10 +869,10 @@ extern "C" int gdmr_drop_deflation(gdmr_system *S) {
 
 // ================================================================ allocation-free residual check
 // gdmr_true_residual_noalloc: the FP64 relative residual ||b_s - A x_s|| / ||b_s|| of up to
-// GDMR_NOALLOC_MAX_RHS pairs on the caller's device buffers, for callers that must not allocate
-// device memory: code running while a stream is being captured into a CUDA graph (cudaMalloc
-// is not a capturable operation), hosts that own the whole device-memory pool, and
-// latency-critical loops where an allocation could stall.  It allocates nothing: the
+// 64 pairs on the caller's device buffers, for callers that must not allocate device memory:
+// hosts whose own allocator owns the whole device-memory pool (a fixed arena carved up at
+// start-up, where a cudaMalloc from a library would fail or fragment it), and latency-critical
+// loops, where a cudaMalloc can synchronise the device and stall.  It allocates nothing: the
 // cross-CTA reduction scratch is the file-scope array below (256 KB of partial sums plus the
 // arrival counters), which every GPU that loads this library holds until the process exits.
 //

@@ -194,8 +194,9 @@ int gdmr_true_residual(gdmr_system *sys, int nrhs, const double *b, const double
  * ||b_s - A x_s|| / ||b_s|| of nrhs <= 64 pairs, b, x and relres all caller-owned device
  * buffers (complex128 interleaved; relres nrhs doubles), enqueued on `stream` (a
  * cudaStream_t, NULL for the default stream) without synchronising.  For callers that
- * cannot call cudaMalloc: code inside a CUDA-graph stream capture, hosts that own the
- * device-memory pool, latency-critical loops.  It uses a 256 KB static device array as
+ * cannot call cudaMalloc: hosts whose own allocator owns the device-memory pool (a library
+ * cudaMalloc would fail or fragment it) and latency-critical loops (a cudaMalloc can
+ * synchronise the device).  It uses a 256 KB static device array as
  * reduction scratch instead of allocating; the first call on a device sets that up
  * (cudaGetSymbolAddress), so make it before any stream capture.  Calls share the array:
  * calls that overlap on the GPU race.  nrhs above 64 is rejected with GDMR_EINVAL. */

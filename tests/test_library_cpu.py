@@ -13,7 +13,10 @@ import gdmr
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INCLUDE = os.path.join(ROOT, "include")
-REFERENCE_PROG = "/root/reference/progDMR.c"
+# The reference source tree (holding progDMR.c) is named by GDMR_REFERENCE_DIR; the link test
+# skips when it is unset.
+REFERENCE_DIR = os.environ.get("GDMR_REFERENCE_DIR", "")
+REFERENCE_PROG = os.path.join(REFERENCE_DIR, "progDMR.c") if REFERENCE_DIR else ""
 
 
 def declared_functions():
@@ -72,8 +75,8 @@ def test_solver_before_init_reports_not_initialised(lib):
     assert lib.gdmrLastStatus() == 6
 
 
-@pytest.mark.skipif(not os.path.exists(REFERENCE_PROG) or shutil.which("gcc") is None,
-                    reason="reference control program not available")
+@pytest.mark.skipif(not REFERENCE_PROG or not os.path.exists(REFERENCE_PROG) or shutil.which("gcc") is None,
+                    reason="GDMR_REFERENCE_DIR unset or without progDMR.c, or no gcc")
 def test_reference_control_program_links_unchanged(tmp_path):
     """progDMR.c, compiled from the reference tree as it is, against this library's
     gDMRC.h, links with -lgDMR (it is not run: it needs a GPU)."""

@@ -1,8 +1,8 @@
 """gdmr_true_residual_noalloc through the C ABI.
 
-The allocation-free residual check exists for callers that cannot call cudaMalloc (code
-inside a CUDA-graph stream capture, hosts that own the device-memory pool, latency-critical
-loops).  It must give what the allocating entry point gdmr_true_residual gives, on two calls
+The allocation-free residual check exists for callers that cannot call cudaMalloc: hosts
+whose own allocator owns the device-memory pool (a library allocation would fail or fragment
+it) and latency-critical loops (an allocation can synchronise the device).  It must give what the allocating entry point gdmr_true_residual gives, on two calls
 in a row (the static scratch keeps state between calls), and refuse sizes beyond its static
 scratch.  This file is collected last so a stop-at-first-failure run has already run
 everything else; it also passes alone in a fresh process.
