@@ -328,7 +328,9 @@ __global__ void __launch_bounds__(NT, PF ? 2 : min_blocks<typename CT<R>::t>(EPT
             for (int e = 0; e < NP; ++e) dst[u][e] = load_pack<C, VEC>(vp, c0 + ((long)e * NT + tid) * VEC, n);
         }
     };
-    if constexpr (PF) load_group(0, vv);
+    // with no basis vectors (q = 0) the clamped index q - 1 would address 16n bytes before segA
+    if constexpr (PF)
+        if (q > 0) load_group(0, vv);
     for (int p0 = 0; p0 < q; p0 += PU) {
         if constexpr (PF) {
             if (p0 + PU < q) load_group(p0 + PU, nx);
@@ -642,7 +644,10 @@ __global__ void __launch_bounds__(NT, 2)
                 for (int e = 0; e < EPT; ++e) vd[u][e] = c0 + (long)e * NT < n ? vp[c0 + (long)e * NT] : czero<C>();
             }
         };
-        if constexpr (PF) load(0, vv);
+        // an update with no basis vectors (q = 0: the deflation loop's first vector) loads
+        // nothing; the clamped index q - 1 would address 16n bytes before segA
+        if constexpr (PF)
+            if (q > 0) load(0, vv);
         for (int p0 = 0; p0 < q; p0 += PU) {
             C vn[PF ? PU : 1][PF ? EPT : 1];
             if constexpr (PF) {   // the next group's loads go out before this group's arithmetic

@@ -117,8 +117,7 @@ def test_legacy_complex64_plugin_csr(c1, oracle_mod):
     The first solve (no deflation space yet) matches the oracle's cycle count within 2.  Later
     solves run on a recycled space built from complex64 residual directions, which carry
     rounding of order eps32 / tol = 6e-8 / 1e-5, about 6e-3 relative (1e-6 for the FP64 form
-    at 1e-10); the reduction order of the Gram-Schmidt variant the tuner picks on a given
-    device moves the cycle count by up to about 20%, so those take 2 + 20% slack.
+    at 1e-10), so two correct implementations agree on their cycle counts only to 2 + 10%.
     """
     A, rhs, cfg, direct = c1
     ls = gdmr.LinearSystem(A.n, cfg["m"], cfg["k"], precision="c64")
@@ -132,7 +131,7 @@ def test_legacy_complex64_plugin_csr(c1, oracle_mod):
             x = ls.exp_src()
             r = o.solve(b, mode=0 if i == 0 else 1, tol=1e-5, mat_rank=2000)
             assert ret < 1e-5
-            assert abs(its - r["its"]) <= (2 if i == 0 else 2 + r["its"] // 5), (i, its, r["its"])
+            assert abs(its - r["its"]) <= (2 if i == 0 else 2 + r["its"] // 10), (i, its, r["its"])
             assert _rel(x, direct[i]) < 1e-3
             assert _rel(x, r["x"]) < 1e-3
         Z = ls.exp_sv()
