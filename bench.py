@@ -164,58 +164,86 @@ def class_table(prof: dict, hbm_peak: float) -> dict:
     return out
 
 
-def cpu_baseline(A, b, cycles: int, plain_cycles_per_solve: float):
-    """The host oracle (complex128 DMR, all host threads) on `cycles` restart cycles of one
-    right-hand side of the same workload; solves/s extrapolated with the plain GPU form's
-    cycles per solve."""
+def workload_config(A, nrhs: int, shape=SHAPE, m_basis: int = M) -> dict:
+    """The workload as both arms name it (the same dict in the reference arm's line)."""
+    return {"workload": f"helmholtz{shape[0]}_{nrhs}rhs", "grid": list(shape), "n": int(A.n), "nnz": int(A.nnz),
+            "kappa": KAPPA, "damping": DAMPING, "nrhs_per_gpu": nrhs, "m": m_basis, "k": K, "tol": TOL,
+            "form": "mixed batched (complex64 inner DMR, FP64 true residual each cycle)",
+            "l2": "working set ~27 GB >> 129 MB L2; no flush"}
+
+
+def oracle_deflated_cycles(o, b, cycles: int, warm: bool):
+    """`cycles` deflated restart cycles of the host oracle on one right-hand side, each timed by
+    the oracle itself.  warm: the oracle already holds a deflation space (every cycle of a mode-1
+    solve is deflated); otherwise one undeflated cycle builds it first and is not counted."""
+    if warm:
+        r = o.solve(b, mode=1, tol=TOL, mat_rank=cycles - 1)
+        ms = r["cycle_ms"]
+    else:
+        r = o.solve(b, mode=0, tol=TOL, mat_rank=cycles)
+        ms = r["cycle_ms"][1:]
+    return float(np.mean(ms)) / 1e3, len(ms)
+
+
+def cpu_baseline(A, b, cycles: int, cycles_per_solve: int, rhs_seed: int):
+    """The host oracle (complex128 DMR, all host threads) on `cycles` deflated restart cycles of
+    one right-hand side of the same workload; solves/s = 1 / (seconds per deflated cycle x the
+    cycles the plain FP64 GPU form took to solve that right-hand side in this run)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     threads = os.cpu_count() or 1
     o = oracle.Oracle(A, M, K, threads=threads, fuse_deflation=True)
     t = time.perf_counter()
-    r = o.solve(b, mode=0, tol=TOL, mat_rank=cycles - 1)
+    per_cycle, timed = oracle_deflated_cycles(o, b, cycles, warm=False)
     el = time.perf_counter() - t
-    per_cycle = el / max(1, r["cycles"])
-    return {"value": 1.0 / (per_cycle * plain_cycles_per_solve), "unit": "solves/s", "cores": threads,
-            "kind": "port",
-            "sample": f"{r['cycles']} restart cycles of one right-hand side on the full 96^3 operator "
-                      f"({el:.1f} s, {per_cycle:.2f} s/cycle), extrapolated to {plain_cycles_per_solve:.0f} "
-                      f"cycles per solve (plain FP64 GPU form)"}
+    return {"value": 1.0 / (per_cycle * cycles_per_solve), "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": f"right-hand side seed {rhs_seed} of the full workload: one undeflated restart cycle, "
+                      f"then {timed} deflated cycles timed one by one ({per_cycle:.3f} s each; {el:.1f} s in all); "
+                      f"x {cycles_per_solve} cycles, the plain FP64 GPU form's count for this right-hand side"}
 
 
 def run_reference(args, world, rank):
-    """Reference arm: the host oracle (the reference has no CPU implementation of this path)
-    on the same workload, every step a bounded sample of restart cycles, extrapolated."""
+    """Reference arm: the host oracle (the reference has no CPU implementation of this path) on
+    the same workload.  Calibration, untimed: one full solve of right-hand side seed 100, whose
+    cycle count converts seconds per cycle into solves/s.  Each step: `ref_cycles` deflated
+    restart cycles of the same right-hand side (a mode-1 solve on the calibration's deflation
+    space), timed cycle by cycle by the oracle."""
     if rank != 0:
         return
-    A = problems.helmholtz(SHAPE, KAPPA, DAMPING)
-    b = problems.gaussian_source_rhs(SHAPE, 100)
+    shape = (args.grid,) * 3
+    A = problems.helmholtz(shape, KAPPA, DAMPING)
+    seed = problems.shard_seeds(1, 0)[0]
+    b = problems.gaussian_source_rhs(shape, seed)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     threads = os.cpu_count() or 1
     o = oracle.Oracle(A, M, K, threads=threads, fuse_deflation=True)
+    t = time.perf_counter()
+    full = o.solve(b, mode=0, tol=TOL, mat_rank=args.max_cycles)
+    full_s = time.perf_counter() - t
+    cycles_per_solve = int(full["cycles"])
     per = []
-    rhos = []
+    step_s = []
     for step in range(args.warmup + args.steps):
         t = time.perf_counter()
-        r = o.solve(b, mode=0, tol=TOL, mat_rank=args.ref_cycles - 1)
+        pc, _ = oracle_deflated_cycles(o, b, args.ref_cycles, warm=True)
         el = time.perf_counter() - t
         if step >= args.warmup:
-            per.append(el / max(1, r["cycles"]))
-            rhos.extend(list(r["rho"][1:]))
+            per.append(pc)
+            step_s.append(el)
     per_cycle = float(np.mean(per))
-    rho = float(np.exp(np.mean(np.log(rhos)))) if rhos else 0.84
-    cycles_needed = max(1.0, math.log(TOL) / math.log(rho))
-    value = 1.0 / (per_cycle * cycles_needed)
+    value = 1.0 / (per_cycle * cycles_per_solve)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_cycle * args.ref_cycles * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(step_s)) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
-            "data": "synthetic", "config": {"workload": "helmholtz96_64rhs", "grid": list(SHAPE), "m": M, "k": K,
-                                            "tol": TOL},
+            "data": "synthetic", "config": workload_config(A, args.nrhs, shape),
+            "calibration": {"rhs_seed": seed, "cycles": cycles_per_solve, "status": int(full["status"]),
+                            "relative_residual": float(full["ret"]), "full_solve_s": full_s,
+                            "full_solve_solves_s": 1.0 / full_s},
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
-                             "sample": f"{args.ref_cycles} restart cycles of one right-hand side per step; "
-                                       f"solves/s extrapolated to {cycles_needed:.0f} cycles from the observed "
-                                       f"mean cycle reduction {rho:.3f}"},
+                             "sample": f"{args.ref_cycles} deflated restart cycles of right-hand side seed {seed} per "
+                                       f"step ({per_cycle:.3f} s each), x {cycles_per_solve} cycles, the count of "
+                                       f"one full oracle solve of it ({full_s:.1f} s, untimed calibration)"},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -371,8 +399,8 @@ def main():
     ap.add_argument("--nrhs", type=int, default=64)
     ap.add_argument("--plain-sample", type=int, default=2, help="right-hand sides timed in the plain FP64 form")
     ap.add_argument("--e2e-steps", type=int, default=1)
-    ap.add_argument("--cpu-cycles", type=int, default=3)
-    ap.add_argument("--ref-cycles", type=int, default=2)
+    ap.add_argument("--cpu-cycles", type=int, default=12, help="deflated oracle cycles timed for cpu_baseline")
+    ap.add_argument("--ref-cycles", type=int, default=2, help="deflated oracle cycles per reference-arm step")
     ap.add_argument("--max-cycles", type=int, default=3000)
     ap.add_argument("--serve", action="store_true", help="serving workload instead of the batched bench")
     ap.add_argument("--multi-operator", action="store_true", help="48-operator workload instead of the batched bench")
@@ -488,6 +516,9 @@ def main():
     elapsed_ms = max_over_ranks(ev0.elapsed_time(ev1), world)
     value = world * nrhs * args.steps / (elapsed_ms / 1e3)
     clocks = clk.summary()
+    # the last timed step's solutions, checked on the host in FP64 (SciPy CSR), independently of
+    # the library's own residual kernel
+    host_worst, host_check = host_residuals(A, B, Xd.cpu().numpy())
     if args.solve_only:
         out = {"mode": "solve-only", "operator": "stencil" if args.stencil else "csr", "operator_kernel": op_kernel,
                "value": value,
@@ -584,11 +615,9 @@ def main():
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64-inner/f64-refine", "data": "synthetic",
-        "config": {"workload": f"helmholtz{shape[0]}_{nrhs}rhs", "operator": "stencil" if args.stencil else "csr",
-                   "operator_kernel": op_kernel, "grid": list(shape), "n": n, "nnz": A.nnz,
-                   "kappa": KAPPA, "damping": DAMPING, "nrhs_per_gpu": nrhs, "m": m_basis, "k": K, "tol": TOL,
-                   "form": "mixed batched (complex64 inner DMR, FP64 true residual each cycle)",
-                   "l2": "working set ~27 GB >> 129 MB L2; no flush"},
+        "config": workload_config(A, nrhs, shape, m_basis),
+        "operator": "stencil" if args.stencil else "csr", "operator_kernel": op_kernel,
+        "host_worst_true_rel_res": host_worst, "host_check": host_check,
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
         "cycles": {"mean": float(np.mean(cycles)), "max": int(np.max(cycles))},
         "verified": bool(verified), "worst_true_rel_res": worst_res,
@@ -599,9 +628,18 @@ def main():
         "tuning": gdmr.tune_report().strip().splitlines(),
     }
     if rank == 0 and args.cpu_cycles > 0:
-        line["cpu_baseline"] = cpu_baseline(A, B[0], args.cpu_cycles, float(np.mean(plain["cycles"])))
+        line["cpu_baseline"] = cpu_baseline(A, B[0], args.cpu_cycles, int(plain["cycles"][0]),
+                                            problems.shard_seeds(nrhs, rank)[0])
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def host_residuals(A, B, X):
+    """max over right-hand sides of ||b - A x|| / ||b||, in FP64 on the host (SciPy CSR)."""
+    S = A.to_scipy()
+    rel = [float(np.linalg.norm(b - S @ x) / np.linalg.norm(b)) for b, x in zip(B, X)]
+    return max(rel), {"how": "SciPy CSR FP64 product on the host, every right-hand side of the last timed step",
+                      "count": len(rel), "median": float(np.median(rel))}
 
 
 def plain_form_only(args, A, B, m_basis, device, hbm_peak):

@@ -27,6 +27,13 @@ namespace {
 
 std::mutex g_api_mu;     // the legacy entry points are process-global, as in the reference
 gdmr_stats g_last_stats{0, 0, 0, 0.0, -1.0, GDMR_OK, 0, 0.0};
+std::mutex g_hist_mu;
+std::vector<CycleRecord> g_last_history;
+
+void record_history(const std::vector<CycleRecord> &h) {
+    std::lock_guard<std::mutex> lk(g_hist_mu);
+    g_last_history = h;
+}
 
 void record(const SolveStats &s) {
     g_last_stats.cycles = s.cycles;
@@ -108,6 +115,7 @@ double legacy_solve(LegacySolver<R> &S, const char *name, int mode, typename CT<
     double r = S.eng.solve_reference(mode, img, src, tol, matRank, &stats);
     if (numIts) *numIts = stats.its;
     record(stats);
+    record_history(S.eng.history());
     if (stats.status == GDMR_ENOCONV)
         fprintf(stderr, "%s Inverse Solve Error: failed to converge to a solution after %d iterations.\n", name,
                 stats.cycles);
@@ -377,8 +385,29 @@ extern "C" void gdmrLastStats(gdmr_stats *out) {
 }
 
 // ================================================================ instrumentation
+extern "C" int gdmrLastHistory(gdmr_cycle *out, int max) {
+    std::lock_guard<std::mutex> lk(g_hist_mu);
+    const int cnt = (int)g_last_history.size();
+    for (int i = 0; out && i < cnt && i < max; ++i) {
+        const CycleRecord &c = g_last_history[i];
+        out[i].rho = c.rho;
+        out[i].rel_res = c.rel_res;
+        out[i].kk = c.kk;
+        out[i].restart = c.restart;
+        out[i].breakdown = c.breakdown;
+        out[i].stagnated = c.stagnated;
+    }
+    return cnt;
+}
+
 extern "C" long long gdmrKernelLaunches(void) { return launch_count(); }
 extern "C" unsigned gdmrAsyncTimeouts(void) { return wproj_tc_timeouts() + bulk_timeouts(); }
+extern "C" double gdmrWaitLimit(double ms) {
+    const double prev = wait_limit_ms();
+    if (ms >= 0) set_wait_limit_ms(ms);
+    return prev;
+}
+extern "C" void gdmrInjectAllocFailure(int nth) { inject_alloc_failure(nth); }
 extern "C" void gdmrProfile(int on) { profile_enable(on != 0); }
 extern "C" void gdmrProfileReset(void) { profile_reset(); }
 extern "C" void gdmrTune(int on) { tune_enable(on != 0); }
@@ -436,6 +465,70 @@ extern "C" int gdmr_hessenberg_svd(int m, int k, const double *H_ri, double *sig
     return GDMR_OK;
 }
 
+// ================================================================ shared-basis kernels on their own
+// The tensor-core kernels of a batched cycle's shared deflation segment (the deflator of the
+// reference, gDMR.cu:1710-1787, for a batch of systems that share W): the split-K projection
+// coef_s = W^H y_s (k_wproj_tc) and the apply P_s = W c_s (k_wapply_tc), run once on the
+// caller's host data so that a test can check them against a host product.
+extern "C" int gdmr_shared_basis_check(int n, int k, int nsys, const float *W_ri, const float *Y_ri,
+                                       const double *c_ri, double *coef_ri, float *P_ri) {
+    const char *F = "gdmr_shared_basis_check";
+    if (n < 2 || n % 2 != 0 || k < 1 || k > 32 || nsys < 8 || nsys > 64)
+        return fail(GDMR_EINVAL, F, "need an even n >= 2, 1 <= k <= 32 and 8 <= nsys <= 64");
+    if (!W_ri || !Y_ri || !c_ri || !coef_ri || !P_ri) return fail(GDMR_EINVAL, F, "null buffer");
+    const size_t ldc = (size_t)k + 1;   // the apply writes a unit coefficient at index k
+    float2 *Wd = nullptr, *Yd = nullptr, *Pd = nullptr;
+    double2 *coef = nullptr, *capp = nullptr;
+    double *part = nullptr;
+    int *act = nullptr;
+    auto release = [&]() {
+        cudaFree(Wd);
+        cudaFree(Yd);
+        cudaFree(Pd);
+        cudaFree(coef);
+        cudaFree(capp);
+        cudaFree(part);
+        cudaFree(act);
+    };
+    const size_t wb = sizeof(float2) * (size_t)k * n, yb = sizeof(float2) * (size_t)nsys * n;
+    const size_t pb = sizeof(double) * (size_t)wproj_tc_grid(n) * k * nsys * 2;
+    if (cudaMalloc(&Wd, wb) != cudaSuccess || cudaMalloc(&Yd, yb) != cudaSuccess || cudaMalloc(&Pd, yb) != cudaSuccess ||
+        cudaMalloc(&coef, sizeof(double2) * ldc * nsys) != cudaSuccess ||
+        cudaMalloc(&capp, sizeof(double2) * ldc * nsys) != cudaSuccess || cudaMalloc(&part, pb) != cudaSuccess ||
+        cudaMalloc(&act, sizeof(int) * nsys) != cudaSuccess) {
+        release();
+        return fail(GDMR_ENOMEM, F, "device allocation failed");
+    }
+    std::vector<int> ident(nsys);
+    for (int i = 0; i < nsys; ++i) ident[i] = i;
+    if (!wproj_tc_ok(n, k, nsys, Wd, Yd, (size_t)n) || !wapply_tc_ok(n, k, nsys)) {
+        release();
+        return fail(GDMR_EINVAL, F, "the tensor-core kernels do not apply to these sizes");
+    }
+    const unsigned t0 = wproj_tc_timeouts();
+    cudaError_t e = cudaMemcpy(Wd, W_ri, wb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(Yd, Y_ri, yb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(act, ident.data(), sizeof(int) * nsys, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy2D(capp, sizeof(double2) * ldc, c_ri, sizeof(double2) * k, sizeof(double2) * k, nsys,
+                         cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && push_wait_limit() != 0) e = cudaErrorUnknown;
+    if (e == cudaSuccess) {
+        launch_wproj_tc(n, k, Wd, Yd, (size_t)n, act, nsys, part, coef, ldc, 0);
+        launch_wapply_tc(n, k, Wd, capp, ldc, act, nsys, Pd, (size_t)n, k, 0);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess)
+        e = cudaMemcpy2D(coef_ri, sizeof(double2) * k, coef, sizeof(double2) * ldc, sizeof(double2) * k, nsys,
+                         cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(P_ri, Pd, yb, cudaMemcpyDeviceToHost);
+    release();
+    if (e != cudaSuccess) return fail(GDMR_ECUDA, F, cudaGetErrorString(e));
+    if (wproj_tc_timeouts() != t0) return fail(GDMR_ETIMEOUT, F, "a pipeline wait ran out");
+    return GDMR_OK;
+}
+
 // ================================================================ context API
 // complex128 <-> complex64 helpers used by the context API
 namespace {
@@ -482,6 +575,18 @@ struct gdmr_system {
     cudaStream_t st = nullptr;
     double2 *db = nullptr, *dx = nullptr;   // staging for host-buffer calls (cap vectors each)
     std::mutex mu;
+    // frees everything, also when creation failed part of the way
+    ~gdmr_system() {
+        cudaSetDevice(device);
+        if (st) cudaStreamSynchronize(st);
+        e32.release();
+        e64.release();
+        edf.release();
+        sell_free(A);
+        if (db) cudaFree(db);
+        if (dx) cudaFree(dx);
+        if (st) cudaStreamDestroy(st);
+    }
 };
 
 namespace {
@@ -549,7 +654,10 @@ int batch_impl(gdmr_system *S, int nrhs, const double *b, double *x, const doubl
         }
     }
     if (cudaStreamSynchronize(S->st) != cudaSuccess) return fail(GDMR_ECUDA, "gdmr_solve_batch", "synchronise");
-    if (worst != GDMR_OK) set_last_error(worst, "gdmr_solve_batch: some right-hand sides did not converge");
+    if (worst != GDMR_OK)
+        set_last_error(worst, worst == GDMR_ETIMEOUT
+                                  ? "gdmr_solve_batch: a bounded device wait ran out (gdmrWaitLimit); see the stats"
+                                  : "gdmr_solve_batch: some right-hand sides did not converge; see the stats");
     else set_last_error(GDMR_OK, "ok");
     return worst;
 }
@@ -598,6 +706,7 @@ int single_impl(gdmr_system *S, int mode, const double *b, double *x, double tol
     cudaStreamSynchronize(S->st);
     if (stats) to_stats(st, stats);
     record(st);
+    record_history(E.history());
     return st.status;
 }
 
@@ -642,17 +751,7 @@ extern "C" int gdmr_system_create(gdmr_system **out, int n, const int *rowPtr, c
 }
 
 extern "C" int gdmr_system_destroy(gdmr_system *S) {
-    if (!S) return GDMR_OK;
-    cudaSetDevice(S->device);
-    if (S->st) cudaStreamSynchronize(S->st);
-    S->e32.release();
-    S->e64.release();
-    S->edf.release();
-    sell_free(S->A);
-    if (S->db) cudaFree(S->db);
-    if (S->dx) cudaFree(S->dx);
-    if (S->st) cudaStreamDestroy(S->st);
-    delete S;
+    delete S;   // the destructor frees the engines, the matrix, the staging buffers and the stream
     return GDMR_OK;
 }
 

@@ -1,7 +1,10 @@
 // Host engine of the GB300 DMR solver.  See gdmr_engine.h.
 #include "gdmr_engine.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -31,6 +34,17 @@ const char *last_error() {
     copy = g_msg;
     return copy.c_str();
 }
+
+namespace {
+std::atomic<int> g_alloc_countdown{0};   // > 0: the allocation that takes it to 0 fails
+}
+void inject_alloc_failure(int nth) { g_alloc_countdown.store(nth > 0 ? nth : 0); }
+
+// NVTX ranges around the phases of a solve (free when no tool is attached).
+struct Range {
+    explicit Range(const char *name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+};
 
 #define GDMR_CK(call)                                                                                                  \
     do {                                                                                                               \
@@ -349,6 +363,15 @@ void sell_free(DeviceSell &s) {
 template <class R> Engine<R>::~Engine() { release(); }
 
 template <class R> int Engine<R>::alloc(void **p, size_t bytes) {
+    int c = g_alloc_countdown.load();
+    while (c > 0 && !g_alloc_countdown.compare_exchange_weak(c, c - 1)) {
+    }
+    if (c == 1) {   // an injected failure (failure-path tests)
+        *p = nullptr;
+        set_last_error(GDMR_ENOMEM, std::string("cudaMalloc of ") + std::to_string(bytes) +
+                                        " bytes: injected allocation failure");
+        return GDMR_ENOMEM;
+    }
     cudaError_t e = cudaMalloc(p, bytes > 0 ? bytes : 16);
     if (e != cudaSuccess) {
         set_last_error(GDMR_ENOMEM, std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes: " +
@@ -383,6 +406,9 @@ template <class R> void Engine<R>::release() {
     allocs_.clear();
     if (hstate_) cudaFreeHost(hstate_);
     hstate_ = nullptr;
+    if (hto_) cudaFreeHost(hto_);
+    hto_ = nullptr;
+    hist_.clear();
     V_ = W_ = Z_ = Znew_ = R_ = X_ = Y_ = T_ = AZ_ = nullptr;
     H_ = Hd_ = coef_ = coefD_ = g_ = y_ = t_ = vs_ = svdwork_ = partials_ = r64_ = b64_ = x64_ = nullptr;
     slot_.clear();
@@ -452,11 +478,13 @@ template <class R> int Engine<R>::init(int n, int m, int k, int capacity, int de
         set_last_error(GDMR_ECUDA, "engine: side stream or events");
         return GDMR_ECUDA;
     }
-    if (cudaMallocHost(&hstate_, sizeof(SysState) * (capacity + 1)) != cudaSuccess) {
+    if (cudaMallocHost(&hstate_, sizeof(SysState) * (capacity + 1)) != cudaSuccess ||
+        cudaMallocHost(&hto_, 2 * sizeof(unsigned)) != cudaSuccess) {
         release();
         set_last_error(GDMR_ENOMEM, "engine: pinned host state");
         return GDMR_ENOMEM;
     }
+    hto_[0] = hto_[1] = 0;
     std::vector<int> id(capacity + 1);
     for (int i = 0; i <= capacity; ++i) id[i] = i;
     GDMR_CK(cudaMemcpy(ident_, id.data(), sizeof(int) * (capacity + 1), cudaMemcpyHostToDevice));
@@ -482,9 +510,23 @@ template <class R> int Engine<R>::set_active(const std::vector<int> &act) {
 template <class R> int Engine<R>::read_state(int count) {
     GDMR_CK(cudaMemcpyAsync(hstate_, state_, sizeof(SysState) * count, cudaMemcpyDeviceToHost, stream));
     if (k_ > 0) GDMR_CK(cudaMemcpyAsync(&hsweeps_, sweeps_, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    enqueue_timeout_read(hto_, stream);
     GDMR_CK(cudaStreamSynchronize(stream));
     svd_sweeps_ = hsweeps_;
     if (profile_enabled()) profile_flush();
+    return GDMR_OK;
+}
+
+// A solve begins: the process's wait limit goes to this device and the timeout counters are
+// read, so that a wait that runs out during the solve shows up as a rise above this baseline.
+template <class R> int Engine<R>::begin_solve() {
+    if (push_wait_limit() != 0) {
+        set_last_error(GDMR_ECUDA, "engine: copying the wait limit to the device failed");
+        return GDMR_ECUDA;
+    }
+    enqueue_timeout_read(hto_, stream);
+    GDMR_CK(cudaStreamSynchronize(stream));
+    to_base_ = timeouts_now();
     return GDMR_OK;
 }
 
@@ -710,9 +752,24 @@ double Engine<R>::solve_reference(int mode, const C *b, C *x, double tol, int ma
         S.status = GDMR_ENOTINIT;
         return 1.0;
     }
+    Range range("gdmr solve");
+    hist_.clear();
     S.its = mat_rank * mat_rank;
     const bool hook = op.kind == Operator<R>::HOOK;
     if (set_active({0}) != GDMR_OK) return fail(1.0);
+    if (begin_solve() != GDMR_OK) return fail(1.0);
+    // ends the solve with x~ exported, for the exits after the restart loop has started
+    auto stop = [&](int status, const char *msg, int cycle, double ret) {
+        sync_deflation();
+        set_last_error(status, msg);
+        S.its = cycle;
+        S.cycles = cycle;
+        S.status = status;
+        S.rel_res = ret;
+        cudaMemcpyAsync(x, X_, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
+        cudaStreamSynchronize(stream);
+        return ret;
+    };
     // ||b||
     launch_norm<R>(n, b, 0, act_, 1, partials_, tickets_, state_, 1, stream);
     // x~ = x0; r = b - A x0  (the hook overwrites x with A x0, as the reference's does)
@@ -723,6 +780,15 @@ double Engine<R>::solve_reference(int mode, const C *b, C *x, double tol, int ma
     if (read_state(1) != GDMR_OK) return fail(1.0);
     const double bnorm = hstate_[0].bnorm;
     double rho_abs = hstate_[0].rho_abs;
+    if (!std::isfinite(bnorm) || !std::isfinite(rho_abs)) {
+        // the reference's loop test is false for NaN, so it returns NaN as if converged, with
+        // numIts = -1; the same value is returned here, with a status that says what happened
+        const double ret = stop(GDMR_ENONFINITE,
+                                "non-finite residual: the operator or the right-hand side produced NaN or Inf", 0,
+                                rho_abs / bnorm);
+        S.its = -1;
+        return ret;
+    }
     if (rho_abs < bnorm * tol) {     // gDMR.cu:2785-2796: absolute norm returned, x unchanged
         cudaMemcpyAsync(x, X_, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
         cudaStreamSynchronize(stream);
@@ -733,45 +799,39 @@ double Engine<R>::solve_reference(int mode, const C *b, C *x, double tol, int ma
     launch_scale<R>(n, R_, 0, R_, 0, nullptr, 0, act_, 1, state_, false, stream);
     const int first_def = mode == 0 ? 0 : k;
     int loop_flag = 0, cycle = 0, kk_prev = 0;
-    if (mode != 0 && !have_z_ && k > 0) {
-        // the reference would use whatever its deflation buffers hold (zeros after init)
-    }
     while (rho_abs > tol * bnorm) {
-        if (cycle > mat_rank) {
-            sync_deflation();
-            set_last_error(GDMR_ENOCONV, "solver failed to converge within matRank restart cycles");
-            S.its = cycle;
-            S.cycles = cycle;
-            S.status = GDMR_ENOCONV;
-            S.rel_res = rho_abs / bnorm;
-            cudaMemcpyAsync(x, X_, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
-            cudaStreamSynchronize(stream);
-            return rho_abs / bnorm;
-        }
-        if (rho_abs / bnorm > 1.0) {
-            sync_deflation();
-            set_last_error(GDMR_ERUNAWAY, "solver runaway: residual above the right-hand side norm");
-            S.its = cycle;
-            S.cycles = cycle;
-            S.status = GDMR_ERUNAWAY;
-            S.rel_res = rho_abs / bnorm;
-            cudaMemcpyAsync(x, X_, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
-            cudaStreamSynchronize(stream);
-            return rho_abs / bnorm;
-        }
+        if (cycle > mat_rank)
+            return stop(GDMR_ENOCONV, "solver failed to converge within matRank restart cycles", cycle,
+                        rho_abs / bnorm);
+        if (rho_abs / bnorm > 1.0)
+            return stop(GDMR_ERUNAWAY, "solver runaway: residual above the right-hand side norm", cycle,
+                        rho_abs / bnorm);
         const int kk = (cycle == 0 && first_def == 0) ? 0 : k;
         if (sync_deflation() != GDMR_OK) return fail(1.0);
         // restart vector (arnoldiSetupDMR, gDMR.cu:2600-2621); a zero period would divide by zero there
+        CycleRecord rec;
+        rec.kk = kk;
         const int period = (2 * mat_rank) / (m - k);
         if (loop_flag == 0 || (period != 0 && flag_count_ % period == 0)) {
             cudaMemcpyAsync(V_, R_, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
         } else {
             const int idx = kk + (m - k) / 2 - kk_prev;   // the reference indexes its [W|V] storage
+            rec.restart = kk + (m - k) / 2;
             if (idx > 0 && idx <= m) cudaMemcpyAsync(V_, V_ + (size_t)idx * n, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
         }
-        if (run_cycle(kk, 1, 0, tol, &S.matvecs) != GDMR_OK) return fail(1.0);
-        if (read_state(1) != GDMR_OK) return fail(1.0);
+        {
+            Range rc("gdmr cycle");
+            if (run_cycle(kk, 1, 0, tol, &S.matvecs) != GDMR_OK) return fail(1.0);
+            if (read_state(1) != GDMR_OK) return fail(1.0);
+        }
         const SysState &st = hstate_[0];
+        if (timed_out()) {
+            // a bounded wait ran out: this cycle's results, and the deflation space it updated,
+            // are not to be trusted
+            drop_deflation();
+            return stop(GDMR_ETIMEOUT, "a bounded device wait ran out during the solve (gdmrWaitLimit)", cycle + 1,
+                        rho_abs / bnorm);
+        }
         if (st.broken) S.breakdowns++;
         const double rho = st.rho;
         if (rho > 0.995) {            // gDMR.cu:2506-2514
@@ -781,8 +841,16 @@ double Engine<R>::solve_reference(int mode, const C *b, C *x, double tol, int ma
             loop_flag = 0;
         }
         rho_abs = st.rho_abs;
+        rec.rho = rho;
+        rec.rel_res = rho_abs / bnorm;
+        rec.breakdown = st.broken;
+        rec.stagnated = loop_flag;
+        hist_.push_back(rec);
         kk_prev = kk;
         ++cycle;
+        if (!std::isfinite(rho_abs))
+            return stop(GDMR_ENONFINITE, "non-finite residual: the operator produced NaN or Inf", cycle,
+                        rho_abs / bnorm);
     }
     S.its = cycle - 1;
     S.cycles = cycle;
@@ -816,7 +884,7 @@ template <class R> int Engine<R>::refine_setup(const SellMatrix &A64) {
     act_h_.clear();
     kk_prev_ = 0;
     GDMR_CK(cudaMemsetAsync(X_, 0, sizeof(C) * (size_t)n_ * cap_, stream));
-    return GDMR_OK;
+    return begin_solve();
 }
 
 template <class R>
@@ -856,8 +924,17 @@ template <class R> int Engine<R>::refine_cycle(std::vector<int> *done) {
         if (set_active(act) != GDMR_OK) return GDMR_ECUDA;
     }
     // true FP64 residual of every active system
+    Range range("gdmr refined cycle");
     launch_residual64(A64_, b64_, n, x64_, n, r64_, n, act_, na, partials_, tickets_, state_, stream);
     if (read_state(cap_) != GDMR_OK) return GDMR_ECUDA;
+    // a bounded wait that ran out since the last look (the previous cycle's kernels) leaves
+    // every system in flight, and the shared deflation space, untrustworthy
+    const bool lost = timed_out();
+    if (lost) {
+        to_base_ = timeouts_now();
+        drop_deflation();
+        set_last_error(GDMR_ETIMEOUT, "a bounded device wait ran out during the solve (gdmrWaitLimit)");
+    }
     std::vector<int> next;
     int lead = -1;
     double worst = -1;
@@ -870,7 +947,8 @@ template <class R> int Engine<R>::refine_cycle(std::vector<int> *done) {
         S.stats.rel_res = rel;
         S.stats.matvecs += 1;   // the FP64 residual product
         int fin = -1;
-        if (st.bad || !std::isfinite(rel)) fin = GDMR_ERUNAWAY;
+        if (lost && S.stats.cycles > 0) fin = GDMR_ETIMEOUT;
+        else if (st.bad || !std::isfinite(rel)) fin = GDMR_ENONFINITE;
         else if (rel <= S.tol) fin = GDMR_OK;
         else if (S.stats.cycles >= S.max_cycles) fin = GDMR_ENOCONV;
         if (fin >= 0) {

@@ -24,6 +24,8 @@ namespace gdmr {
 void set_last_error(int status, const std::string &msg);
 int last_status();
 const char *last_error();
+// Failure-path testing: the nth device allocation an engine makes from now on fails (0: none).
+void inject_alloc_failure(int nth);
 
 // A sparse operator resident on the device in SELL-32 form, with values in
 // complex64 and (optionally) complex128 sharing one index structure.
@@ -80,6 +82,17 @@ template <class R> struct Operator {
     C *ext = nullptr;
     SellMatrix sell{};
     const C *dense = nullptr;      // column-major n x n
+};
+
+// One restart cycle of a reference-semantics solve, as the host saw it.
+struct CycleRecord {
+    double rho = 0;       // ||r_new|| / ||r_old|| of the cycle (the recursion's reduction factor)
+    double rel_res = 0;   // the recursive residual over ||b|| after the cycle
+    int kk = 0;           // deflation vectors the cycle used
+    int restart = 0;      // 0: started from the residual; else the reference's basis-storage index of
+                          // the mid-Krylov vector it restarted from (gDMR.cu:2600-2621)
+    int breakdown = 0;    // Krylov step of a breakdown, 0 if none
+    int stagnated = 0;    // 1: rho > 0.995, the reference's stagnation flag (gDMR.cu:2506)
 };
 
 struct SolveStats {
@@ -147,6 +160,8 @@ template <class R> class Engine {
     }
     // The reference keeps its stagnation counter across solves (gDMR.cu:2646-2655); reset on init.
     int flag_count() const { return flag_count_; }
+    // Cycles of the last solve_reference call.
+    const std::vector<CycleRecord> &history() const { return hist_; }
 
     // FP32 and FP64 Jacobi sweeps of the last deflation update (read after a cycle).
     int last_svd_sweeps() const { return svd_sweeps_; }
@@ -158,6 +173,14 @@ template <class R> class Engine {
   private:
     int n_ = 0, m_ = 0, k_ = 0, cap_ = 0, dev_ = 0;
     size_t bytes_ = 0;
+    std::vector<CycleRecord> hist_;
+    // bounded device waits that ran out (process-wide counters, read with every state read):
+    // the value at the start of the current solve and the latest one
+    unsigned *hto_ = nullptr;     // pinned: [tensor-core, bulk-copy and grid barriers]
+    unsigned to_base_ = 0;
+    unsigned timeouts_now() const { return hto_ ? hto_[0] + hto_[1] : 0; }
+    int begin_solve();            // pushes the wait limit, takes the timeout baseline
+    bool timed_out() const { return timeouts_now() != to_base_; }
     bool have_z_ = false;
     int flag_count_ = 0;        // reference kryFlagCountDMR (system 0)
     // device buffers

@@ -724,8 +724,10 @@ constexpr int BK_THREADS = BK_CONS + 32;
 constexpr int BK_EPT = BK_TILE / BK_CONS;      // elements per consumer thread and tile
 constexpr int BK_PU = 4;                       // vector tiles per stage
 constexpr int BK_MSTAGES = 4, BK_USTAGES = 5;
-constexpr long long BK_WAIT_CYCLES = 4000000000LL;
+constexpr long long BK_WAIT_CYCLES = 4000000000LL;   // drain waits: ~2 s at 2 GHz, fixed
 __device__ unsigned g_bulk_timeouts = 0;
+// stage waits and grid barriers: the process's wait limit (set_wait_limit_ms), in clock cycles
+__constant__ long long c_wait_cycles = BK_WAIT_CYCLES;
 
 __device__ __forceinline__ uint32_t bk_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void bk_init(uint32_t a, int count) {
@@ -744,21 +746,21 @@ __device__ __forceinline__ void bk_copy(uint32_t dst, const void *src, uint32_t 
                  "l"(src), "r"(bytes), "r"(bar)
                  : "memory");
 }
-__device__ __forceinline__ bool bk_wait(uint32_t a, uint32_t parity, volatile int *abort) {
+__device__ __forceinline__ bool bk_wait(uint32_t a, uint32_t parity, volatile int *abort, long long limit) {
     const long long t0 = clock64();
     while (true) {
         uint32_t ok;
         asm volatile("{\n.reg .pred P;\nmbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\nselp.b32 %0, 1, 0, P;\n}\n"
                      : "=r"(ok) : "r"(a), "r"(parity) : "memory");
         if (ok) return true;
-        if ((abort && *abort) || clock64() - t0 > BK_WAIT_CYCLES) return false;
+        if ((abort && *abort) || clock64() - t0 > limit) return false;
     }
 }
 // lane 0 waits, the warp follows its verdict; a timeout raises the CTA's abort flag
 __device__ __forceinline__ bool bk_warp_wait(uint32_t a, uint32_t parity, volatile int *abort, int lane) {
     int ok = 1;
     if (lane == 0) {
-        ok = bk_wait(a, parity, abort);
+        ok = bk_wait(a, parity, abort, c_wait_cycles);
         if (!ok && !*abort) {
             atomicAdd(&g_bulk_timeouts, 1u);
             *abort = 1;
@@ -799,7 +801,7 @@ __device__ void bk_produce(long total, unsigned char *base, unsigned long long *
     for (long k = 0; k < total && !*abort; ++k) {
         const int b = (int)(k % NS);
         const long use = k / NS;
-        if (use > 0 && !bk_wait(bk_u32(&empty[b]), (uint32_t)((use - 1) & 1), abort)) {
+        if (use > 0 && !bk_wait(bk_u32(&empty[b]), (uint32_t)((use - 1) & 1), abort, c_wait_cycles)) {
             if (!*abort) { atomicAdd(&g_bulk_timeouts, 1u); *abort = 1; }
             break;
         }
@@ -817,7 +819,8 @@ __device__ void bk_produce(long total, unsigned char *base, unsigned long long *
     }
 #pragma unroll
     for (int b = 0; b < NS; ++b)
-        if (last[b] >= 0 && !bk_wait(bk_u32(&full[b]), (uint32_t)(last[b] & 1), nullptr)) atomicAdd(&g_bulk_timeouts, 1u);
+        if (last[b] >= 0 && !bk_wait(bk_u32(&full[b]), (uint32_t)(last[b] & 1), nullptr, BK_WAIT_CYCLES))
+            atomicAdd(&g_bulk_timeouts, 1u);   // drain: the fixed bound, whatever the process limit
 }
 
 __global__ void __launch_bounds__(BK_THREADS, 1)
@@ -1064,7 +1067,7 @@ __device__ bool ks_grid_sync(unsigned *bar, unsigned target, int *abort) {
         int ok = 1;
         while (ld_acquire_gpu(bar) < target) {
             if (*(volatile int *)abort) { ok = 0; break; }
-            if (clock64() - t0 > BK_WAIT_CYCLES) {
+            if (clock64() - t0 > c_wait_cycles) {
                 atomicAdd(&g_bulk_timeouts, 1u);
                 atomicExch(abort, 1);
                 ok = 0;
@@ -3495,6 +3498,41 @@ unsigned bulk_timeouts() {
     unsigned v = 0;
     cudaMemcpyFromSymbol(&v, g_bulk_timeouts, sizeof v);
     return v;
+}
+
+void enqueue_timeout_read_tc(unsigned *host, cudaStream_t st);   // gdmr_tc.cu
+void enqueue_timeout_read(unsigned *host2, cudaStream_t st) {
+    enqueue_timeout_read_tc(host2, st);
+    cudaMemcpyFromSymbolAsync(host2 + 1, g_bulk_timeouts, sizeof(unsigned), 0, cudaMemcpyDeviceToHost, st);
+}
+
+namespace {
+constexpr double CYCLES_PER_MS = 2.07e6;   // the GB300's maximum SM clock
+std::mutex g_wait_mu;
+double g_wait_ms = 2000.0;
+std::vector<long long> g_wait_pushed;      // per device: the cycles it holds
+}  // namespace
+
+void set_wait_limit_ms(double ms) {
+    std::lock_guard<std::mutex> lk(g_wait_mu);
+    g_wait_ms = ms < 0 ? 0 : ms;
+}
+double wait_limit_ms() {
+    std::lock_guard<std::mutex> lk(g_wait_mu);
+    return g_wait_ms;
+}
+// 0 on success, -1 if a CUDA call failed
+int push_wait_limit() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    std::lock_guard<std::mutex> lk(g_wait_mu);
+    const long long cycles = g_wait_ms == 2000.0 ? BK_WAIT_CYCLES : (long long)(g_wait_ms * CYCLES_PER_MS);
+    if ((int)g_wait_pushed.size() <= dev) g_wait_pushed.resize(dev + 1, BK_WAIT_CYCLES);
+    if (g_wait_pushed[dev] == cycles) return 0;
+    if (cudaMemcpyToSymbol(c_wait_cycles, &cycles, sizeof cycles) != cudaSuccess) return -1;
+    if (push_wait_limit_tc(cycles) != 0) return -1;
+    g_wait_pushed[dev] = cycles;
+    return 0;
 }
 
 namespace {

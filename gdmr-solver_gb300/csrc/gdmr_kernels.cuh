@@ -191,8 +191,26 @@ int launch_wapply_tc(int n, int kk, const float2 *W, double2 *coef, size_t strid
                      float2 *P, size_t strideP, int unit_idx, cudaStream_t st);
 // mbarrier waits of the tensor-core kernels that ran out of time (0 in a healthy process).
 unsigned wproj_tc_timeouts();
-// Bounded mbarrier waits of the bulk-copy Gram-Schmidt pipelines that ran out (0 in a healthy run).
+// Bounded mbarrier waits of the bulk-copy Gram-Schmidt pipelines and grid barriers of the fused
+// Krylov kernel that ran out (0 in a healthy run).
 unsigned bulk_timeouts();
+// The same two counters read on `st` into pinned host memory: host2[0] tensor-core kernels,
+// host2[1] bulk-copy pipelines and grid barriers (valid once `st` is synchronised).
+void enqueue_timeout_read(unsigned *host2, cudaStream_t st);
+
+// Bound of the waits a kernel makes on other parts of the GPU: the stage waits of the
+// tensor-core and bulk-copy pipelines and the grid barriers of the fused Krylov kernel, in
+// milliseconds at the GB300's 2.07 GHz clock (default 2000).  A wait that runs out makes its
+// kernel stop and return, and counts in the timeout counters.  The drain waits, where a kernel
+// waits for its own copies and tensor-core operations in flight before it frees TMEM and exits,
+// keep a fixed bound of about two seconds whatever this is set to.
+void set_wait_limit_ms(double ms);
+double wait_limit_ms();
+// Copies the process's wait limit to the current device if it differs from what that device
+// holds (a synchronous copy: never call it while a stream capture is open on this thread).
+int push_wait_limit();
+// The tensor-core translation unit's copy of the limit (clock cycles) on the current device.
+int push_wait_limit_tc(long long cycles);
 
 // out1 (and out2 if non-null) = alpha_s * in; zeros when the system broke down.
 template <class R>

@@ -26,8 +26,10 @@
 //     back (tcgen05.ld) and summed in double-float, the CTA's partials are written as doubles
 //     and k_wproj_tc_reduce sums them over CTAs in a fixed order (deterministic).
 //
-// Every wait on an mbarrier is bounded (about two seconds of clock); a timeout is counted
-// in g_tc_timeouts, the kernel skips its remaining work and still frees its TMEM.
+// Every wait on an mbarrier is bounded: the pipeline's stage waits by the process's wait limit
+// (about two seconds of clock by default), the final wait for every issued MMA by a fixed two
+// seconds.  A timeout is counted in g_tc_timeouts; the kernel skips its remaining work, waits
+// for the MMAs it issued and still frees its TMEM.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -60,6 +62,9 @@ constexpr int TC_A_FLOATS = TC_M * 2 * TC_KT;
 constexpr long long TC_WAIT_CYCLES = 4000000000LL;                       // ~2 s at 2 GHz
 
 __device__ unsigned g_tc_timeouts = 0;
+// bound of the pipeline stage waits: the process's wait limit in clock cycles; the waits on
+// `done` (every MMA issued has finished, before TMEM is read and freed) keep TC_WAIT_CYCLES
+__constant__ long long c_tc_wait_cycles = TC_WAIT_CYCLES;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -92,7 +97,8 @@ __device__ __forceinline__ float tf32_big(float x) {
     return __uint_as_float(r);
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity, volatile int *abort) {
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity, volatile int *abort,
+                                          long long limit = c_tc_wait_cycles) {
     const long long t0 = clock64();
     while (true) {
         uint32_t ok;
@@ -100,7 +106,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity, volati
         asm volatile("{\n.reg .pred P;\nmbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2, %3;\nselp.b32 %0, 1, 0, P;\n}\n"
                      : "=r"(ok) : "r"(addr), "r"(parity), "r"(20000) : "memory");
         if (ok) return true;
-        if ((abort && *abort) || clock64() - t0 > TC_WAIT_CYCLES) return false;
+        if ((abort && *abort) || clock64() - t0 > limit) return false;
     }
 }
 
@@ -325,7 +331,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
     }
     __syncthreads();
-    if (!mbar_wait(smem_u32(&done), 0, nullptr) && tid == 0) {
+    if (!mbar_wait(smem_u32(&done), 0, nullptr, TC_WAIT_CYCLES) && tid == 0) {
         atomicAdd(&g_tc_timeouts, 1u);
         s_abort = 1;
     }
@@ -607,7 +613,7 @@ __global__ void __launch_bounds__(WA_THREADS, 1)
         }
     }
     __syncthreads();
-    if (!mbar_wait(smem_u32(&done), 0, nullptr) && tid == 0) atomicAdd(&g_tc_timeouts, 1u);
+    if (!mbar_wait(smem_u32(&done), 0, nullptr, TC_WAIT_CYCLES) && tid == 0) atomicAdd(&g_tc_timeouts, 1u);
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "n"(TC_TMEM_COLS));
@@ -693,6 +699,14 @@ unsigned wproj_tc_timeouts() {
     unsigned v = 0;
     cudaMemcpyFromSymbol(&v, g_tc_timeouts, sizeof v);
     return v;
+}
+
+void enqueue_timeout_read_tc(unsigned *host, cudaStream_t st) {
+    cudaMemcpyFromSymbolAsync(host, g_tc_timeouts, sizeof(unsigned), 0, cudaMemcpyDeviceToHost, st);
+}
+
+int push_wait_limit_tc(long long cycles) {
+    return cudaMemcpyToSymbol(c_tc_wait_cycles, &cycles, sizeof cycles) == cudaSuccess ? 0 : -1;
 }
 
 }  // namespace gdmr

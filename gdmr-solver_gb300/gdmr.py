@@ -38,6 +38,9 @@ SIGNATURES = {
     "gdmrLastError": (ctypes.c_char_p, []),
     "gdmrVersion": (ctypes.c_char_p, []),
     "gdmrLastStats": (None, [P]),
+    "gdmrLastHistory": (I, [P, I]),
+    "gdmrWaitLimit": (D, [D]),
+    "gdmrInjectAllocFailure": (None, [I]),
     "initDMR_z": (None, [I, I, P, I, I, I, I, P]),
     "freeDMR_z": (None, []),
     "solverDMR_z": (D, [I, P, P, P, I, D, I, P]),
@@ -63,6 +66,7 @@ SIGNATURES = {
     "gdmr_csr_grid_form": (I, [I, P, P, P, P]),
     "gdmrAsyncTimeouts": (ctypes.c_uint, []),
     "gdmr_hessenberg_svd": (I, [I, I, P, P, P, P]),
+    "gdmr_shared_basis_check": (I, [I, I, I, P, P, P, P, P]),
     "gdmr_system_set_stencil": (I, [P, I, I, I, P]),
     "gdmr_system_clear_stencil": (I, [P]),
     "gdmr_system_create": (I, [P, I, P, P, P, I, I, I, I, I]),
@@ -96,7 +100,7 @@ SIGNATURES = {
 }
 
 STATUS = {0: "GDMR_OK", 1: "GDMR_EINVAL", 2: "GDMR_ENOMEM", 3: "GDMR_ENOCONV", 4: "GDMR_ERUNAWAY",
-          5: "GDMR_ECUDA", 6: "GDMR_ENOTINIT", 7: "GDMR_EBREAKDOWN"}
+          5: "GDMR_ECUDA", 6: "GDMR_ENOTINIT", 7: "GDMR_EBREAKDOWN", 8: "GDMR_ETIMEOUT", 9: "GDMR_ENONFINITE"}
 
 
 class Stats(ctypes.Structure):
@@ -105,6 +109,34 @@ class Stats(ctypes.Structure):
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class Cycle(ctypes.Structure):
+    _fields_ = [("rho", D), ("rel_res", D), ("kk", I), ("restart", I), ("breakdown", I), ("stagnated", I)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+def last_history() -> list:
+    """Per restart cycle of the last reference-semantics solve: rho, rel_res, kk, restart (0 or the
+    [W V] storage index of the mid-Krylov restart vector), breakdown step, stagnated flag."""
+    L = load()
+    cnt = int(L.gdmrLastHistory(None, 0))
+    buf = (Cycle * max(cnt, 1))()
+    L.gdmrLastHistory(buf, cnt)
+    return [buf[i].as_dict() for i in range(cnt)]
+
+
+def wait_limit(ms: float = -1.0) -> float:
+    """Bound (ms at 2.07 GHz) of the kernels' stage waits and grid barriers; sets it when ms >= 0
+    and returns the previous value."""
+    return float(load().gdmrWaitLimit(float(ms)))
+
+
+def inject_alloc_failure(nth: int) -> None:
+    """Failure-path testing: the nth engine allocation from now on fails (0 disarms)."""
+    load().gdmrInjectAllocFailure(int(nth))
 
 
 KERNEL_CLASSES = ["projection", "update", "operator", "combine", "deflation_update", "residual64",
@@ -183,6 +215,22 @@ def hessenberg_svd(H: np.ndarray, k: int, with_sweeps: bool = False):
     if with_sweeps:
         return sigma, vs.T.copy(), (sw.value // 1000, sw.value % 1000)
     return sigma, vs.T.copy()
+
+
+def shared_basis_check(W, Y, c):
+    """The batched shared-basis tensor-core kernels on their own (gdmr_shared_basis_check):
+    W (k, n) and Y (nsys, n) complex64, c (nsys, k) complex128.  Returns (coef, P): coef (nsys, k)
+    complex128 with coef[s, p] = <W_p, Y_s>, and P (nsys, n) complex64 with P[s] = sum_p c[s, p] W_p."""
+    W = np.ascontiguousarray(W, dtype=np.complex64)
+    Y = np.ascontiguousarray(Y, dtype=np.complex64)
+    c = np.ascontiguousarray(c, dtype=np.complex128)
+    k, n = W.shape
+    nsys = Y.shape[0]
+    coef = np.empty((nsys, k), np.complex128)
+    P = np.empty((nsys, n), np.complex64)
+    _check(load().gdmr_shared_basis_check(n, k, nsys, _ptr(W), _ptr(Y), _ptr(c), _ptr(coef), _ptr(P)),
+           "gdmr_shared_basis_check")
+    return coef, P
 
 
 def profile_read() -> dict:

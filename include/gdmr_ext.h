@@ -23,7 +23,11 @@ enum {
     GDMR_ERUNAWAY = 4,   /* residual above ||b|| (reference: "Runaway", gDMR.cu:2823) */
     GDMR_ECUDA = 5,      /* CUDA runtime error */
     GDMR_ENOTINIT = 6,   /* used before init */
-    GDMR_EBREAKDOWN = 7
+    GDMR_EBREAKDOWN = 7,
+    GDMR_ETIMEOUT = 8,   /* a bounded device wait ran out during the call (gdmrWaitLimit); its results,
+                            and the deflation space, are dropped */
+    GDMR_ENONFINITE = 9  /* NaN or Inf in a residual: the operator or the data produced it (the
+                            reference's loop test treats NaN as converged, gDMR.cu:2814) */
 };
 
 /* Last status and message of any entry point (process-wide). */
@@ -76,6 +80,21 @@ typedef struct {
     double latency_ms;     /* batched solves: time from the call's start to this solution's return */
 } gdmr_stats;
 void gdmrLastStats(gdmr_stats *out);
+/* One restart cycle of the last reference-semantics solve (solverDMR/solveLS and their _z twins,
+ * gdmr_solve), as the host saw it after the cycle. */
+typedef struct {
+    double rho;        /* ||r_new|| / ||r_old||: the cycle's residual reduction (gDMR.cu:2491-2503) */
+    double rel_res;    /* the recursive residual over ||b|| after the cycle */
+    int kk;            /* deflation vectors the cycle used (0 on a first cycle with mode 0) */
+    int restart;       /* 0: the cycle started from the residual; otherwise the stagnation rule
+                          (arnoldiSetupDMR, gDMR.cu:2600-2621) restarted it from the Krylov vector
+                          at this index of the reference's [W V] storage, kk + (m - k) / 2 */
+    int breakdown;     /* Krylov step of an absolute breakdown in the cycle (gDMR.cu:2256), 0: none */
+    int stagnated;     /* 1 when rho > 0.995, which sets the reference's stagnation flag (gDMR.cu:2506) */
+} gdmr_cycle;
+/* Copies up to max cycles of the last reference-semantics solve into out; returns how many
+ * cycles it had. */
+int gdmrLastHistory(gdmr_cycle *out, int max);
 
 /* ---- instrumentation --------------------------------------------------------
  * Kernel launches issued by this library since load.  With profiling on, each
@@ -88,6 +107,17 @@ long long gdmrKernelLaunches(void);
  * such wait gives up after about two seconds and the kernel returns with its results unset, so
  * a nonzero count means a result of this process is not to be trusted. */
 unsigned gdmrAsyncTimeouts(void);
+/* Bound, in milliseconds at the GB300's 2.07 GHz clock, of every wait a kernel makes on another
+ * part of the GPU: the stage waits of the tensor-core and bulk-copy pipelines and the grid-wide
+ * barriers of the fused small-system Krylov kernel (default 2000).  A wait that runs out stops
+ * its kernel, counts in gdmrAsyncTimeouts, and the solve returns GDMR_ETIMEOUT.  The waits in
+ * which a kernel drains its own copies and tensor-core operations before it frees TMEM keep a
+ * fixed two-second bound.  Takes effect at the next solve (or server start); ms < 0 only reads.
+ * Returns the previous value. */
+double gdmrWaitLimit(double ms);
+/* Failure-path testing: the nth device allocation that a solver engine makes from now on fails
+ * as if cudaMalloc had (GDMR_ENOMEM, everything allocated so far is freed); 0 disarms. */
+void gdmrInjectAllocFailure(int nth);
 void gdmrProfile(int on);
 void gdmrProfileReset(void);
 int gdmrProfileRead(int kernelClass, double *bytes, double *ms, long long *launches);
@@ -100,6 +130,16 @@ int gdmrProfileRead(int kernelClass, double *bytes, double *ms, long long *launc
  * plus 100 if the unpivoted fallback ran) + double-float sweeps.  Runs on the current device
  * with device scratch of its own.  1 <= k <= m <= 160, else GDMR_EINVAL. */
 int gdmr_hessenberg_svd(int m, int k, const double *H, double *sigma, double *vs, int *sweeps);
+/* The tensor-core kernels of a batched cycle's shared deflation segment on their own (the
+ * deflator w -= W W^H w of deflatorDMR, gDMR.cu:1710-1787, for nsys systems that share W), run
+ * once on host data so that their results can be checked against a host product:
+ *   coef[s*k + p] = <W_p, Y_s> = sum_i conj(W_p[i]) Y_s[i]   (split-K projection, 3xTF32)
+ *   P[s*n + i]    = sum_p c[s*k + p] W_p[i]                    (apply, 3xTF32)
+ * W: k x n and Y, P: nsys x n complex64 (interleaved floats); c, coef: nsys x k complex128
+ * (interleaved doubles).  Needs an even n, 1 <= k <= 32, 8 <= nsys <= 64 (GDMR_EINVAL
+ * otherwise).  Allocates its own device buffers and synchronises the device. */
+int gdmr_shared_basis_check(int n, int k, int nsys, const float *W, const float *Y, const double *c, double *coef,
+                            float *P);
 /* Gram-Schmidt kernel autotuning: the first launch of a shape times the kernel variants
  * and keeps the fastest for the process (on by default; off selects the first variant).
  * The report lists one line per tuned shape with the time of every variant. */

@@ -31,6 +31,7 @@
 // through ctypes by tests and bench.py).
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -164,6 +165,9 @@ template <typename R> struct Oracle {
     int flag_count = 0, loop_flag = 0;
     long matvecs = 0;
     std::vector<double> cycle_rho;
+    std::vector<int> cycle_restart;   // 0, or the storage index of the mid-Krylov restart vector
+    std::vector<int> cycle_broken;    // Krylov step of a breakdown, 0 if none
+    std::vector<double> cycle_ms;     // wall time of each cycle (the CPU baseline times deflated ones)
 
     void matvec(const T *x, T *y) {
         ++matvecs;
@@ -285,6 +289,9 @@ template <typename R> struct Oracle {
         R tol = (R)tol_in;
         loop_flag = 0;
         cycle_rho.clear();
+        cycle_restart.clear();
+        cycle_broken.clear();
+        cycle_ms.clear();
         std::vector<T> r(n), t(n), u(n);
         *its = mat_rank * mat_rank;
         *cycles = 0;
@@ -306,14 +313,18 @@ template <typename R> struct Oracle {
         while (rho_abs > tol * bnorm) {
             if (cycle > mat_rank) { *its = cycle; *cycles = cycle; *status = 3; return rho_abs / bnorm; }
             if (rho_abs / bnorm > 1) { *its = cycle; *cycles = cycle; *status = 4; return rho_abs / bnorm; }
+            const auto t_cycle = std::chrono::steady_clock::now();
             int kk = (cycle == 0 && first_def == 0) ? 0 : k;
             int period = (2 * mat_rank) / (m - k);
             T *v0 = &basis[(size_t)kk * n];
-            if (loop_flag == 0 || (period != 0 && flag_count % period == 0))
+            int restart = 0;
+            if (loop_flag == 0 || (period != 0 && flag_count % period == 0)) {
                 std::copy(r.begin(), r.end(), v0);
-            else
-                std::copy(&basis[(size_t)(kk + (m - k) / 2) * n], &basis[(size_t)(kk + (m - k) / 2 + 1) * n], v0);
-            arnoldi(kk, tol);
+            } else {                      // arnoldiSetupDMR, gDMR.cu:2610-2621
+                restart = kk + (m - k) / 2;
+                std::copy(&basis[(size_t)restart * n], &basis[(size_t)(restart + 1) * n], v0);
+            }
+            const int broken = arnoldi(kk, tol);
             project(basis.data(), m + 1, r.data(), cT.data());   // g, gDMR.cu:2334-2408
             for (int p = 0; p <= m; ++p) g[p] = up(cT[p]);
             ls_householder(m + 1, m, H.data(), g.data(), y.data());
@@ -341,6 +352,8 @@ template <typename R> struct Oracle {
             for (int i = 0; i < n; ++i) x[i] = cadd(x[i], u[i]);
             rho_abs = rho * rho_abs;
             cycle_rho.push_back((double)rho);
+            cycle_restart.push_back(restart);
+            cycle_broken.push_back(broken);
             if (k > 0) {                                      // gDMR.cu:1583-1704
                 svd_jacobi(m + 1, m, H.data(), sv.data(), Vs.data());
                 for (int tI = 0; tI < k; ++tI) {
@@ -358,6 +371,8 @@ template <typename R> struct Oracle {
                 }
                 std::swap(Z, Znew);
             }
+            cycle_ms.push_back(
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_cycle).count());
             ++cycle;
         }
         *its = cycle - 1;
@@ -464,6 +479,27 @@ int oracle_cycle_log(void *hp, double *out, int cap) {
     int c = std::min<int>(cap, (int)v.size());
     std::copy(v.begin(), v.begin() + c, out);
     return (int)v.size();
+}
+
+// Wall time (ms) of each cycle of the last solve.
+int oracle_cycle_ms(void *hp, double *out, int cap) {
+    auto *h = (Handle *)hp;
+    const std::vector<double> &v = h->precision == 0 ? h->d->cycle_ms : h->f->cycle_ms;
+    const int c = std::min<int>(cap, (int)v.size());
+    std::copy(v.begin(), v.begin() + c, out);
+    return (int)v.size();
+}
+
+// Per cycle of the last solve: the restart vector's storage index (0: the residual) and the
+// Krylov step of a breakdown (0: none).
+int oracle_cycle_info(void *hp, int *restart, int *broken, int cap) {
+    auto *h = (Handle *)hp;
+    const std::vector<int> &rs = h->precision == 0 ? h->d->cycle_restart : h->f->cycle_restart;
+    const std::vector<int> &bk = h->precision == 0 ? h->d->cycle_broken : h->f->cycle_broken;
+    const int c = std::min<int>(cap, (int)rs.size());
+    std::copy(rs.begin(), rs.begin() + c, restart);
+    std::copy(bk.begin(), bk.begin() + c, broken);
+    return (int)rs.size();
 }
 
 // Deflation basis Z (k x n, vector-contiguous) in and out, interleaved doubles.

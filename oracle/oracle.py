@@ -40,6 +40,10 @@ def lib():
         L.oracle_solve.argtypes = [P, I, P, P, D, I, P, P, P, P]
         L.oracle_cycle_log.restype = I
         L.oracle_cycle_log.argtypes = [P, P, I]
+        L.oracle_cycle_ms.restype = I
+        L.oracle_cycle_ms.argtypes = [P, P, I]
+        L.oracle_cycle_info.restype = I
+        L.oracle_cycle_info.argtypes = [P, P, P, I]
         L.oracle_get_Z.argtypes = [P, P]
         L.oracle_set_Z.argtypes = [P, P]
         L.oracle_ls.argtypes = [I, I, P, P, P]
@@ -83,10 +87,17 @@ class Oracle:
         mv = ctypes.c_long()
         ret = lib().oracle_solve(self._h, int(mode), _ptr(b), _ptr(x), float(tol), int(mat_rank),
                                  ctypes.byref(its), ctypes.byref(cycles), ctypes.byref(status), ctypes.byref(mv))
-        log = np.zeros(max(cycles.value, 1))
-        lib().oracle_cycle_log(self._h, _ptr(log), log.size)
+        nlog = max(cycles.value, 1)
+        log = np.zeros(nlog)
+        got = lib().oracle_cycle_log(self._h, _ptr(log), log.size)
+        restart = np.zeros(nlog, np.int32)
+        broken = np.zeros(nlog, np.int32)
+        lib().oracle_cycle_info(self._h, _ptr(restart), _ptr(broken), nlog)
+        ms = np.zeros(nlog)
+        lib().oracle_cycle_ms(self._h, _ptr(ms), nlog)
+        c = min(got, cycles.value)
         return dict(x=x, ret=ret, its=its.value, cycles=cycles.value, status=status.value,
-                    matvecs=mv.value, rho=log[:cycles.value])
+                    matvecs=mv.value, rho=log[:c], restart=restart[:c], breakdown=broken[:c], cycle_ms=ms[:c])
 
     def get_Z(self) -> np.ndarray:
         out = np.zeros((self.k, self.n), np.complex128)

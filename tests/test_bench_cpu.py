@@ -86,11 +86,11 @@ def test_ranks_solve_disjoint_right_hand_sides(bench):
 
 
 def test_reference_arm_prints_one_json_line():
-    # the reference arm (the oracle port on the host cores), one restart cycle of the 96^3
-    # workload: one JSON line with the contract's keys, e2e equal to its own value, no
-    # host-device traffic
+    # the reference arm (the oracle port on the host cores) on the same workload at a 24^3 grid:
+    # a full calibration solve, then one step of two deflated cycles; one JSON line with the
+    # contract's keys, e2e equal to its own value, no host-device traffic
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "0", "--ref-cycles", "1"],
+                        "--warmup", "0", "--ref-cycles", "2", "--grid", "24"],
                        capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
@@ -100,3 +100,7 @@ def test_reference_arm_prints_one_json_line():
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert np.isfinite(d["ms_per_step"])
+    # solves/s = 1 / (seconds per deflated cycle x the calibration solve's cycle count)
+    cal = d["calibration"]
+    assert cal["status"] == 0 and cal["relative_residual"] <= 1e-10 and cal["cycles"] > 1
+    assert d["config"]["grid"] == [24, 24, 24] and d["config"]["n"] == 24 ** 3

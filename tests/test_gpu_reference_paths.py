@@ -1,0 +1,146 @@
+"""The reference's rarer branches and the headline workload, cycle by cycle against the oracle.
+
+* The stagnation rule (arnoldiSetupDMR, gDMR.cu:2586-2632; flag at gDMR.cu:2506-2514): a cycle
+  that reduces the residual by less than 0.5% sets a flag, and the next cycle restarts from the
+  Krylov vector at storage index kk + (m - k) / 2 of the previous cycle instead of from the
+  residual, except every 2 matRank / (m - k) flagged cycles.  A cyclic shift plus 0.2 I makes a
+  basis of 8 stagnate from the second cycle on.
+* A breakdown inside a deflated cycle (gDMR.cu:2256-2289) with the reference's identity tail,
+  which starts at column j and so overwrites diagonal entries of valid columns when k > 0
+  (quirk Q4): a diagonal operator with 6 distinct eigenvalues and an imported 2-vector
+  deflation space inside the right-hand side's 6-dimensional invariant subspace closes the
+  Krylov space after 4 steps of a basis of 8.
+* The 96^3 Helmholtz operator of the benchmark (kappa 24, damping 0.1, m = 48, k = 24): three
+  restart cycles of the plain complex128 form (cycle 0 undeflated, cycles 1-2 deflated) against
+  the oracle, per-cycle reduction factor within 1e-8 and x within 1e-8.
+* The batched shared-basis tensor-core kernels (k_wproj_tc, k_wapply_tc) on their own at the
+  benchmark's shape (64 systems, k = 24) and n = 262,144, against numpy FP64 products; the
+  bound is the 3xTF32 error, FP32 level.
+
+complex128 ("fp64") must follow the oracle to 1e-8 per cycle (two independent restatements of
+the iteration agree to about 1e-13 over 31 stagnating cycles); the complex64 reference form
+(a "mixed" system's gdmr_solve) to 1e-3, its rounding level over these cycle counts.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import gdmr
+import problems
+from problems import CSR
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-10, "mixed": 1e-5}
+ORACLE_PREC = {"fp64": "c128", "mixed": "c64"}
+RHO_TOL = {"fp64": 1e-8, "mixed": 1e-3}
+X_TOL = {"fp64": 1e-8, "mixed": 1e-3}
+
+
+def _csr(S):
+    S = S.tocsr()
+    S.sort_indices()
+    return CSR(S.shape[0], S.indptr.astype(np.int32), S.indices.astype(np.int32), S.data.astype(np.complex128))
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def cyclic_shift_plus(n, c):
+    P = sp.lil_matrix((n, n), dtype=np.complex128)
+    for i in range(1, n):
+        P[i, i - 1] = 1.0
+    P[0, n - 1] = 1.0
+    return _csr(P.tocsr() + c * sp.eye(n, format="csr"))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_stagnation_restarts_from_the_mid_krylov_vector(oracle_mod, precision):
+    n, m, k, mat_rank = 512, 8, 2, 30
+    A = cyclic_shift_plus(n, 0.2)
+    b = problems.unit_gaussian_rhs(n, 3)
+    s = gdmr.System(A, m, k, capacity=1, precision=precision)
+    x, st = s.solve(b, mode=0, tol=TOL[precision], mat_rank=mat_rank)
+    hist = gdmr.last_history()
+    r = oracle_mod.Oracle(A, m, k, precision=ORACLE_PREC[precision], fuse_deflation=True).solve(
+        b, mode=0, tol=TOL[precision], mat_rank=mat_rank)
+    # the cycle cap ends both: matRank + 1 cycles, status "failed to converge"
+    assert st["status"] == 3 and r["status"] == 3
+    assert st["cycles"] == r["cycles"] == mat_rank + 1 == len(hist)
+    restarts = [h["restart"] for h in hist]
+    # the branch fired, from the Krylov vector at kk + (m - k) / 2, and the period rule
+    # (every 2 matRank / (m - k) = 10th flagged cycle restarts from the residual) fired too
+    assert sum(1 for v in restarts if v) >= 20, restarts
+    assert set(v for v in restarts if v) == {k + (m - k) // 2}
+    assert any(h["stagnated"] and not nxt["restart"] for h, nxt in zip(hist[1:], hist[2:])), restarts
+    assert restarts == [int(v) for v in r["restart"]]
+    assert [h["stagnated"] for h in hist] == [int(v > 0.995) for v in r["rho"]]
+    rho = np.array([h["rho"] for h in hist])
+    assert np.max(np.abs(rho - r["rho"]) / r["rho"]) <= RHO_TOL[precision]
+    assert _rel(x, r["x"]) < X_TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_breakdown_inside_a_deflated_cycle(oracle_mod, precision):
+    n, m, k = 512, 8, 2
+    lam = np.array([0.4, 3 + 1j, -0.6 + 0.5j, 4 - 1j, 1.5 + 2j, -2 - 1j])
+    d = lam[np.arange(n) % 6]
+    A = _csr(sp.diags([d], [0]))
+    b = problems.unit_gaussian_rhs(n, 5)
+    basis = np.zeros((6, n), complex)                  # the invariant subspace holding b
+    for c in range(6):
+        basis[c, c::6] = b[c::6]
+    rng = np.random.default_rng(1)
+    Z = (rng.standard_normal((k, 6)) + 1j * rng.standard_normal((k, 6))) @ basis
+    Z /= np.linalg.norm(Z, axis=1, keepdims=True)
+    s = gdmr.System(A, m, k, capacity=1, precision=precision)
+    s.import_deflation(Z)
+    x, st = s.solve(b, mode=1, tol=TOL[precision], mat_rank=40)
+    hist = gdmr.last_history()
+    o = oracle_mod.Oracle(A, m, k, precision=ORACLE_PREC[precision], fuse_deflation=True)
+    o.set_Z(Z)
+    r = o.solve(b, mode=1, tol=TOL[precision], mat_rank=40)
+    assert st["status"] == 0 and r["status"] == 0
+    assert st["cycles"] == r["cycles"] == 1
+    # a deflated cycle (kk = k) whose Krylov loop broke down at step 4 < m - k
+    assert hist[0]["kk"] == k and hist[0]["breakdown"] == 4 == int(r["breakdown"][0])
+    assert st["breakdowns"] == 1
+    assert _rel(x, r["x"]) < X_TOL[precision]
+    assert _rel(x, b / d) < X_TOL[precision]
+
+
+def test_helmholtz96_plain_cycles_match_the_oracle(oracle_mod):
+    shape = (96, 96, 96)
+    A = problems.helmholtz(shape, 24.0, 0.1)
+    b = problems.gaussian_source_rhs(shape, 100)
+    m, k = 48, 24
+    s = gdmr.System(A, m, k, capacity=1, precision="fp64")
+    x, st = s.solve(b, mode=0, tol=1e-10, mat_rank=2)            # the cycle cap stops it after 3
+    hist = gdmr.last_history()
+    r = oracle_mod.Oracle(A, m, k, fuse_deflation=True).solve(b, mode=0, tol=1e-10, mat_rank=2)
+    assert st["status"] == 3 and r["status"] == 3 and st["cycles"] == r["cycles"] == 3
+    assert [h["kk"] for h in hist] == [0, k, k]
+    rho = np.array([h["rho"] for h in hist])
+    assert np.max(np.abs(rho - r["rho"]) / r["rho"]) <= 1e-8, (rho, r["rho"])
+    assert _rel(x, r["x"]) <= 1e-8
+
+
+def test_shared_basis_tensor_core_kernels_match_fp64_products():
+    n, k, nsys = 262144, 24, 64
+    rng = np.random.default_rng(7)
+
+    def unit_rows(rows):
+        v = rng.standard_normal((rows, n)) + 1j * rng.standard_normal((rows, n))
+        return (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(np.complex64)
+
+    W, Y = unit_rows(k), unit_rows(nsys)
+    c = rng.standard_normal((nsys, k)) + 1j * rng.standard_normal((nsys, k))
+    coef, P = gdmr.shared_basis_check(W, Y, c)
+    W64, Y64 = W.astype(np.complex128), Y.astype(np.complex128)
+    coef_ref = (W64.conj() @ Y64.T).T                      # <W_p, Y_s>, unit-norm rows
+    assert np.max(np.abs(coef - coef_ref)) <= 1e-6
+    P_ref = c @ W64
+    err = np.linalg.norm(P.astype(np.complex128) - P_ref, axis=1) / np.linalg.norm(P_ref, axis=1)
+    assert err.max() <= 1e-6, err.max()
+    assert gdmr.async_timeouts() == 0
