@@ -250,55 +250,123 @@ def run_reference(args, world, rank):
 
 def run_serve(args, rank):
     """Serving workload: six resident operators (7-point Helmholtz 64^3 /
-    96^3 / 128^3 with kappa 16 / 24 / 32, each at damping 0.05 and 0.2), Poisson arrivals,
-    each request picks an operator uniformly and brings one Gaussian-source right-hand side
-    with a tolerance drawn from {1e-6, 1e-8, 1e-10}; m = 48, k = 24 per operator; device
-    memory bounded by a 150 GB budget split evenly across the operators."""
+    96^3 / 128^3 with kappa 16 / 24 / 32, each at damping 0.05 and 0.2), m = 48, k = 24 per
+    operator, device memory bounded by a 150 GB budget split evenly across the operators; each
+    request picks an operator uniformly and brings one Gaussian-source right-hand side with a
+    tolerance drawn from {1e-6, 1e-8, 1e-10}.  Two phases per precision: capacity (a burst of
+    requests submitted at once; solves/s while the queues stay full), then Poisson arrivals at
+    `--load` times that capacity for `--duration` seconds, so that the p50/p99 latencies measure
+    service and the queueing a stated load brings, not an unbounded queue."""
     import gdmr
     gdmr.load()
-    rng = np.random.default_rng(4)
     specs = [((64,) * 3, 16.0), ((96,) * 3, 24.0), ((128,) * 3, 32.0)]
+    mats = [problems.helmholtz(shape, kappa, damping) for shape, kappa in specs for damping in (0.05, 0.2)]
+    shapes = [shape for shape, _ in specs for _ in (0.05, 0.2)]
+    pools = [[problems.gaussian_source_rhs(shapes[i], 7000 + 97 * (i + 1) + j) for j in range(args.serve_pool)]
+             for i in range(len(mats))]
     budget = int(args.budget_gb * (1 << 30))
-    srv = gdmr.Server(budget_bytes=budget, device=0)
-    ops, pools = [], []
-    share = budget // 6
-    for shape, kappa in specs:
-        for damping in (0.05, 0.2):
-            A = problems.helmholtz(shape, kappa, damping)
-            per = gdmr.load().gdmr_server_slot_bytes(A.n, M, 1 if args.serve_precision == "mixed" else 0)
+    forms = ["mixed", "fp64"] if args.serve_precision == "both" else [args.serve_precision]
+    out = {}
+    for form in forms:
+        rng = np.random.default_rng(4)
+        srv = gdmr.Server(budget_bytes=budget, device=0)
+        share = budget // len(mats)
+        ops = []
+        for A in mats:
+            per = gdmr.load().gdmr_server_slot_bytes(A.n, M, 1 if form == "mixed" else 0)
             fixed = A.nnz * 40 + A.n * 16 * (3 * K + 1) + (64 << 20)
             cap = int(max(1, min(args.serve_slots, (share - fixed) // per)))
-            ops.append(srv.add_operator(A, M, K, capacity=cap, precision=args.serve_precision))
-            pools.append([problems.gaussian_source_rhs(shape, 7000 + 97 * len(ops) + j)
-                          for j in range(args.serve_pool)])
-    srv.start()
-    nreq = int(args.rate * args.duration)
-    gaps = rng.exponential(1.0 / args.rate, nreq)
-    choice = rng.integers(0, 6, nreq)
-    tols = rng.choice([1e-6, 1e-8, 1e-10], nreq)
-    tickets = []
-    t0 = time.perf_counter()
-    t_next = t0
-    for i in range(nreq):
-        t_next += gaps[i]
-        delay = t_next - time.perf_counter()
-        if delay > 0:
-            time.sleep(delay)
-        j = int(choice[i])
-        tickets.append((j, float(tols[i]), srv.submit(ops[j], pools[j][i % args.serve_pool], tol=float(tols[i]))))
-    lat, ok = [], True
-    for j, tol, t in tickets:
-        x, st = srv.wait(t, timeout=3600)
-        lat.append(st["latency_ms"])
-        ok &= st["status"] == 0 and st["true_rel_res"] <= tol
-    wall = time.perf_counter() - t0
-    line = {"mode": "serve", "metric": METRIC, "value": nreq / wall, "unit": "solves/s",
-            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
-            "requests": nreq, "rate_req_s": args.rate, "arrival_window_s": args.duration, "wall_s": wall,
-            "verified": bool(ok), "precision": args.serve_precision,
-            "capacity": [srv.capacity(o) for o in ops], "device_bytes": srv.device_bytes,
-            "config": {"workload": "serve6_helmholtz", "budget_gb": args.budget_gb, "m": M, "k": K}}
-    srv.close()
+            ops.append(srv.add_operator(A, M, K, capacity=cap, precision=form))
+        srv.start()
+
+        def run_requests(nreq, gaps):
+            choice = rng.integers(0, len(ops), nreq)
+            tols = rng.choice([1e-6, 1e-8, 1e-10], nreq)
+            tickets = []
+            t0 = time.perf_counter()
+            t_next = t0
+            for i in range(nreq):
+                if gaps is not None:
+                    t_next += gaps[i]
+                    delay = t_next - time.perf_counter()
+                    if delay > 0:
+                        time.sleep(delay)
+                j = int(choice[i])
+                tickets.append((float(tols[i]), srv.submit(ops[j], pools[j][i % args.serve_pool], tol=float(tols[i]))))
+            lat, ok = [], True
+            for tol, t in tickets:
+                x, st = srv.wait(t, timeout=3600)
+                lat.append(st["latency_ms"])
+                ok &= st["status"] == 0 and st["true_rel_res"] <= tol
+            wall = time.perf_counter() - t0
+            return {"solves_s": nreq / wall, "requests": nreq, "wall_s": wall,
+                    "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+                    "verified": bool(ok)}
+
+        burst = run_requests(args.serve_burst, None)
+        rate = args.load * burst["solves_s"]
+        nreq = max(1, int(rate * args.duration))
+        poisson = run_requests(nreq, rng.exponential(1.0 / rate, nreq))
+        poisson.update({"rate_req_s": rate, "load": args.load, "arrival_window_s": args.duration})
+        out[form] = {"capacity": burst, "poisson": poisson, "slots": [srv.capacity(o) for o in ops],
+                     "device_bytes": srv.device_bytes}
+        srv.close()
+    head = out[forms[0]]["poisson"]
+    line = {"mode": "serve", "metric": METRIC, "value": head["solves_s"], "unit": "solves/s",
+            "latency_ms": head["latency_ms"], "forms": out,
+            "config": {"workload": "serve6_helmholtz", "budget_gb": args.budget_gb, "m": M, "k": K,
+                       "operators": "64^3/96^3/128^3 x damping 0.05/0.2", "tolerances": [1e-6, 1e-8, 1e-10]}}
+    if len(forms) == 2:
+        line["mixed_over_plain"] = out["mixed"]["capacity"]["solves_s"] / out["fp64"]["capacity"]["solves_s"]
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_sequence(args, rank):
+    """Drifting-sequence workload: 3D 7-point Helmholtz 128^3 (kappa 30, damping 0.1,
+    n = 2,097,152), right-hand sides b_1 a unit complex Gaussian and b_(j+1) = b_j + 0.05 ||b_j||
+    g_j / ||g_j||, solved one after another with the recycled deflation space (m = 60, k = 20,
+    tol 1e-10): plain complex128 (the drop-in, gdmr_solve mode 0 then 1), fp64e, and the
+    complex64-inner / FP64-refined form (gdmr_solve_batch one right-hand side at a time, the
+    system's deflation space carried from call to call), on the first --seq-count of the 32.
+    Each form first solves b_1 once untimed (kernel tuning), then drops its deflation space."""
+    import gdmr
+    gdmr.load()
+    A, seq, cfg = problems.config_3d128()
+    B = seq(args.seq_count)
+    tol = cfg["tol"]
+    S = A.to_scipy()
+    out = {}
+    for form in ("mixed", "fp64e", "fp64"):
+        s = gdmr.System(A, cfg["m"], cfg["k"], capacity=1, precision=form)
+        if form == "mixed":
+            s.solve_batch(B[:1], tol=tol, max_cycles=args.max_cycles)
+        else:
+            s.solve(B[0], mode=0, tol=tol, mat_rank=args.max_cycles)
+        s.drop_deflation()
+        cyc, lat, worst, ok = [], [], 0.0, True
+        t0 = time.perf_counter()
+        for i, b in enumerate(B):
+            t = time.perf_counter()
+            if form == "mixed":
+                X, st = s.solve_batch(b[None], tol=tol, max_cycles=args.max_cycles)
+                x, st = X[0], st[0]
+            else:
+                x, st = s.solve(b, mode=0 if i == 0 else 1, tol=tol, mat_rank=args.max_cycles)
+            lat.append(time.perf_counter() - t)
+            cyc.append(int(st["cycles"]))
+            ok &= st["status"] == 0
+            worst = max(worst, float(np.linalg.norm(b - S @ x) / np.linalg.norm(b)))
+        el = time.perf_counter() - t0
+        out[form] = {"solves_s": len(B) / el, "cycles": cyc, "latency_s_each": lat, "verified": bool(ok),
+                     "host_worst_true_rel_res": worst}
+        s.close()
+    line = {"mode": "sequence", "metric": METRIC, "value": out["mixed"]["solves_s"], "unit": "solves/s",
+            "forms": out, "mixed_over_plain": out["mixed"]["solves_s"] / out["fp64"]["solves_s"],
+            "mixed_over_fp64e": out["mixed"]["solves_s"] / out["fp64e"]["solves_s"],
+            "config": {"workload": "helmholtz128_drifting_sequence", "n": int(A.n), "nnz": int(A.nnz),
+                       "kappa": 30.0, "damping": 0.1, "m": cfg["m"], "k": cfg["k"], "tol": tol,
+                       "rhs": len(B), "of": 32}}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -405,11 +473,16 @@ def main():
     ap.add_argument("--serve", action="store_true", help="serving workload instead of the batched bench")
     ap.add_argument("--multi-operator", action="store_true", help="48-operator workload instead of the batched bench")
     ap.add_argument("--small", action="store_true", help="64x64 reference-parity case (plain FP64 drop-in)")
+    ap.add_argument("--sequence", action="store_true",
+                    help="128^3 drifting sequence of right-hand sides: plain complex128, fp64e and mixed")
+    ap.add_argument("--seq-count", type=int, default=4, help="right-hand sides of the sequence timed (of 32)")
     ap.add_argument("--operators", type=int, default=48)
     ap.add_argument("--rhs-per-operator", type=int, default=4)
-    ap.add_argument("--serve-precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--rate", type=float, default=200.0)
-    ap.add_argument("--duration", type=float, default=2.0, help="arrival window in seconds")
+    ap.add_argument("--serve-precision", default="both", choices=["mixed", "fp64", "both"])
+    ap.add_argument("--load", type=float, default=0.7,
+                    help="serving: Poisson arrival rate as a fraction of the measured capacity")
+    ap.add_argument("--serve-burst", type=int, default=48, help="serving: requests of the capacity phase")
+    ap.add_argument("--duration", type=float, default=60.0, help="serving: Poisson arrival window in seconds")
     ap.add_argument("--budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-slots", type=int, default=64)
     ap.add_argument("--serve-pool", type=int, default=4)
@@ -446,6 +519,9 @@ def main():
         return
     if args.small:
         run_small(args, rank)
+        return
+    if args.sequence:
+        run_sequence(args, rank)
         return
 
     import torch

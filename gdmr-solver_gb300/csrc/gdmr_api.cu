@@ -841,6 +841,16 @@ extern "C" int gdmr_system_set_fused(gdmr_system *S, int on) {
     return GDMR_OK;
 }
 
+extern "C" int gdmr_system_set_compat_eye(gdmr_system *S, int on) {
+    if (!S) return fail(GDMR_EINVAL, "gdmr_system_set_compat_eye", "null system");
+    std::lock_guard<std::mutex> lk(S->mu);
+    cudaSetDevice(S->device);
+    S->e32.set_compat_eye(on != 0);
+    S->e64.set_compat_eye(on != 0);
+    S->edf.set_compat_eye(on != 0);
+    return GDMR_OK;
+}
+
 extern "C" int gdmr_system_grid(const gdmr_system *S, int *dims) {
     if (!S || !dims) return fail(GDMR_EINVAL, "gdmr_system_grid", "null system or dims");
     dims[0] = S->A.gx;

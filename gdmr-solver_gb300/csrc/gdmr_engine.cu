@@ -313,6 +313,13 @@ int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, 
         d.gx = gx;
         d.gy = gy;
         d.gz = gz;
+        // real planes (the off-diagonals of a Helmholtz operator): the kernels skip the products
+        // with their zero imaginary parts, which add nothing
+        for (int e = 0; e < np; ++e) {
+            bool real = true;
+            for (int r = 0; real && r < n; ++r) real = gim[(size_t)e * n + r] == 0.0;
+            if (real) d.greal |= 1u << e;
+        }
         // one precision at a time, each host copy released after its upload
         if (want32) {
             std::vector<float2> g(gsz);

@@ -49,6 +49,7 @@ struct DeviceSell {
     double2 *grid64 = nullptr;
     dfc *griddf = nullptr;
     int gx = 0, gy = 0, gz = 0;
+    unsigned greal = 0;                // bit p: plane p is real (imaginary parts all zero)
     SellMatrix view(const void *v, const void *g) const {
         SellMatrix m{n, nslices, slice_ptr, cols, v, nnz};
         m.uniform = uniform;
@@ -58,6 +59,7 @@ struct DeviceSell {
         m.gx = gx;
         m.gy = gy;
         m.gz = gz;
+        m.greal = greal;
         return m;
     }
     SellMatrix view32() const { return view(vals32, grid32); }
@@ -124,6 +126,13 @@ template <class R> class Engine {
     bool use_graphs = true;     // capture restart cycles of small systems as CUDA graphs
     bool fused_small = true;    // one small system: the Krylov loop as one cooperative kernel
     bool compat_eye = true;     // reproduce the reference's breakdown identity tail (gDMR.cu:2275)
+    // Changes compat_eye; restart-cycle graphs captured with the other setting are dropped.
+    void set_compat_eye(bool on) {
+        if (on == compat_eye) return;
+        compat_eye = on;
+        for (auto &g : graphs_) cudaGraphExecDestroy(g.exec);
+        graphs_.clear();
+    }
 
     // Reference semantics on system 0 (solverDMR): b, x are device vectors of precision R;
     // x holds x0 on entry and the solution on exit.  With a hook operator x must be the hook's

@@ -70,12 +70,31 @@ template <class C> __device__ __forceinline__ void cfma(C &acc, C a, C b) {
     acc.y = rfma(a.x, b.y, acc.y);
     acc.y = rfma(a.y, b.x, acc.y);
 }
+// acc += a * b where a is known to be real when `real` (its zero imaginary part would add
+// zeros: the same value either way, with half the multiplies)
+template <class C> __device__ __forceinline__ void cfma_r(C &acc, C a, C b, bool real) {
+    if (real) {
+        acc.x = rfma(a.x, b.x, acc.x);
+        acc.y = rfma(a.x, b.y, acc.y);
+    } else {
+        cfma(acc, a, b);
+    }
+}
 // acc -= a * b
 template <class C> __device__ __forceinline__ void cfms(C &acc, C a, C b) {
     acc.x = rfma(-a.x, b.x, acc.x);
     acc.x = rfma(a.y, b.y, acc.x);
     acc.y = rfma(-a.x, b.y, acc.y);
     acc.y = rfma(-a.y, b.x, acc.y);
+}
+// acc -= a * b, a real when `real` (as cfma_r)
+template <class C> __device__ __forceinline__ void cfms_r(C &acc, C a, C b, bool real) {
+    if (real) {
+        acc.x = rfma(-a.x, b.x, acc.x);
+        acc.y = rfma(-a.x, b.y, acc.y);
+    } else {
+        cfms(acc, a, b);
+    }
 }
 // acc += conj(a) * b
 template <class C> __device__ __forceinline__ void cdotacc(C &acc, C a, C b) {
@@ -3010,7 +3029,7 @@ __global__ void __launch_bounds__(NT) k_stencil(int nx, int ny, int nz, double2 
 constexpr int GR_ZC = 8;
 template <class R, int SG>
 __global__ void __launch_bounds__(NT) k_grid_spmm(int nx, int ny, int nz, int ngroups, int ntiles,
-                                                  const typename CT<R>::t *__restrict__ coef,
+                                                  unsigned greal, const typename CT<R>::t *__restrict__ coef,
                                                   const typename CT<R>::t *__restrict__ x0, size_t strideX,
                                                   typename CT<R>::t *__restrict__ y0, size_t strideY,
                                                   const int *__restrict__ act, int nsys,
@@ -3041,6 +3060,11 @@ __global__ void __launch_bounds__(NT) k_grid_spmm(int nx, int ny, int nz, int ng
         }
     }
     const bool xl = ix > 0, xh = ix + 1 < nx, yl = iy > 0, yh = iy + 1 < ny;
+    // real planes, in the planes' order (-P first in 3D)
+    const int pb = d3 ? 1 : 0;
+    const bool rmP = d3 && (greal & 1u), rmQ = (greal >> pb) & 1u, rm1 = (greal >> (pb + 1)) & 1u,
+               r00 = (greal >> (pb + 2)) & 1u, rp1 = (greal >> (pb + 3)) & 1u, rpQ = (greal >> (pb + 4)) & 1u,
+               rpP = d3 && ((greal >> 6) & 1u);
     for (int z = z0; z < z1; ++z, idx += plane) {
         const bool zl = z > 0, zh = z + 1 < nz;
         const C amP = zl ? coef[idx] : czero<C>();
@@ -3052,13 +3076,13 @@ __global__ void __launch_bounds__(NT) k_grid_spmm(int nx, int ny, int nz, int ng
                 const C *x = xs[g];
                 const C above = zh ? x[idx + plane] : czero<C>();
                 C acc = czero<C>();
-                if (zl) cfma(acc, amP, below[g]);
-                if (yl) cfma(acc, amQ, x[idx - nx]);
-                if (xl) cfma(acc, am1, x[idx - 1]);
-                cfma(acc, a00, cur[g]);
-                if (xh) cfma(acc, ap1, x[idx + 1]);
-                if (yh) cfma(acc, apQ, x[idx + nx]);
-                if (zh) cfma(acc, apP, above);
+                if (zl) cfma_r(acc, amP, below[g], rmP);
+                if (yl) cfma_r(acc, amQ, x[idx - nx], rmQ);
+                if (xl) cfma_r(acc, am1, x[idx - 1], rm1);
+                cfma_r(acc, a00, cur[g], r00);
+                if (xh) cfma_r(acc, ap1, x[idx + 1], rp1);
+                if (yh) cfma_r(acc, apQ, x[idx + nx], rpQ);
+                if (zh) cfma_r(acc, apP, above, rpP);
                 const int sys = act[g0 + g];
                 if (scale) {   // pending normalisation, as in k_spmm
                     const SysState &stt = scale[sys];
@@ -3241,8 +3265,17 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
 }
 
 // r = b - A x in FP64 with ||r||^2 reduced; last CTA sets true_res and alpha.
+// GRID: the matrix's structured-grid form (coefficient planes, real planes skipping their zero
+// imaginary parts), terms in the order the SELL loop takes them, so the same values.
+struct GridForm {
+    const double2 *coef;
+    int nx, ny, nz;
+    unsigned greal;
+};
+template <bool GRID>
 __global__ void __launch_bounds__(NT) k_residual64(int n, const int *__restrict__ slice_ptr, const int *__restrict__ cols,
-                                                   const double2 *__restrict__ vals, const double2 *__restrict__ b0,
+                                                   const double2 *__restrict__ vals, GridForm gf,
+                                                   const double2 *__restrict__ b0,
                                                    size_t strideB, const double2 *__restrict__ x0, size_t strideX,
                                                    double2 *__restrict__ r0, size_t strideR, const int *__restrict__ act,
                                                    double2 *__restrict__ partials, unsigned *tickets, SysState *state) {
@@ -3253,12 +3286,29 @@ __global__ void __launch_bounds__(NT) k_residual64(int n, const int *__restrict_
     __shared__ double red[1][NW];
     double n2 = 0;
     for (int row = blockIdx.y * NT + tid; row < n; row += G * NT) {
-        const int slice = row >> 5, lane = row & 31;
-        const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
         double2 acc = b[row];
-        for (int c = 0; c < width; ++c) {
-            const int e = beg + c * 32 + lane;
-            cfms(acc, vals[e], x[cols[e]]);
+        if constexpr (GRID) {
+            const int nx = gf.nx, ny = gf.ny, nz = gf.nz;
+            const long plane = (long)nx * ny;
+            const int ix = row % nx, iy = (row / nx) % ny, iz = (int)(row / plane);
+            const bool d3 = nz > 1;
+            const int pb = d3 ? 1 : 0;
+            const unsigned gr = gf.greal;
+            const double2 *cf = gf.coef + (d3 ? n : 0);
+            if (d3 && iz > 0) cfms_r(acc, gf.coef[row], x[row - plane], gr & 1u);
+            if (iy > 0) cfms_r(acc, cf[row], x[row - nx], (gr >> pb) & 1u);
+            if (ix > 0) cfms_r(acc, cf[(long)n + row], x[row - 1], (gr >> (pb + 1)) & 1u);
+            cfms_r(acc, cf[2L * n + row], x[row], (gr >> (pb + 2)) & 1u);
+            if (ix + 1 < nx) cfms_r(acc, cf[3L * n + row], x[row + 1], (gr >> (pb + 3)) & 1u);
+            if (iy + 1 < ny) cfms_r(acc, cf[4L * n + row], x[row + nx], (gr >> (pb + 4)) & 1u);
+            if (d3 && iz + 1 < nz) cfms_r(acc, cf[5L * n + row], x[row + plane], (gr >> 6) & 1u);
+        } else {
+            const int slice = row >> 5, lane = row & 31;
+            const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
+            for (int c = 0; c < width; ++c) {
+                const int e = beg + c * 32 + lane;
+                cfms(acc, vals[e], x[cols[e]]);
+            }
         }
         r[row] = acc;
         n2 += acc.x * acc.x + acc.y * acc.y;
@@ -4275,8 +4325,8 @@ void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX
         if (blocks <= 0x7fffffffL) {
             const auto *cf = (const typename CT<R>::t *)A.grid;
 #define GRID_LAUNCH_(SGV)                                                                                              \
-    k_grid_spmm<R, SGV><<<(unsigned)blocks, NT, 0, st>>>(A.gx, A.gy, A.gz, ngroups, ntiles, cf, x, strideX, y, strideY, \
-                                                         act, nsys, scale, vout, strideVO)
+    k_grid_spmm<R, SGV><<<(unsigned)blocks, NT, 0, st>>>(A.gx, A.gy, A.gz, ngroups, ntiles, A.greal, cf, x, strideX, y, \
+                                                         strideY, act, nsys, scale, vout, strideVO)
             if (sg == 1)
                 GRID_LAUNCH_(1);
             else if (sg == 2)
@@ -4320,8 +4370,14 @@ void launch_residual64(const SellMatrix &A, const double2 *b, size_t strideB, co
                        SysState *state, cudaStream_t st) {
     if (nsys <= 0) return;
     Launch L_(KC_RESID64, spmm_bytes(A, sizeof(double2), nsys) + (double)sizeof(double2) * A.n * nsys, st, 1);
-    k_residual64<<<grid2(nsys, capped_grid(A.n, nsys, 8)), NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const double2 *)A.vals, b, strideB, x,
+    const dim3 grid = grid2(nsys, capped_grid(A.n, nsys, 8));
+    const GridForm gf{(const double2 *)A.grid, A.gx, A.gy, A.gz, A.greal};
+    if (A.grid && grid_operator())
+        k_residual64<true><<<grid, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const double2 *)A.vals, gf, b, strideB, x,
                                                 strideX, r, strideR, act, partials, tickets, state);
+    else
+        k_residual64<false><<<grid, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const double2 *)A.vals, gf, b, strideB, x,
+                                                 strideX, r, strideR, act, partials, tickets, state);
 }
 
 template <class R>

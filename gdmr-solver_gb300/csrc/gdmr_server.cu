@@ -9,6 +9,14 @@
 // finished solutions back; requests of different operators run on different streams and
 // overlap on the device.  The device memory of all engines is fixed at registration and
 // bounded by the server's budget, which is what admission by HBM budget means here.
+//
+// A server may span several devices (independent operators shard across GPUs with no
+// collective: §8(e) of the design; the reference instead splits one basis across devices with
+// peer copies, gDMR.cu:1478-1520).  Each device of the server's list has its own budget, and
+// gdmr_server_add_operator places an operator, with its matrix, its deflation space, its
+// engine and its queue, on the device that keeps the most budget free after taking it
+// (worst fit, which balances memory and so the work across devices).  A device may appear
+// twice in the list (two budgets on one GPU), as the reference's device lists allow.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -50,6 +58,7 @@ struct Done {
 
 struct ServedOperator {
     int id = 0, n = 0, m = 0, k = 0, capacity = 0, precision = 1, device = 0;
+    int slot_dev = 0;              // index of the server's device (budget) list it was placed on
     DeviceSell A;
     Engine<float> e32;
     Engine<double> e64;
@@ -62,13 +71,28 @@ struct ServedOperator {
     std::vector<bool> slot_busy;
     std::thread worker;
     long long bytes = 0;
+    // frees everything it holds, also after a registration that failed part of the way (the
+    // worker thread, if any, has been joined)
+    ~ServedOperator() {
+        cudaSetDevice(device);
+        if (st) cudaStreamSynchronize(st);
+        e32.release();
+        e64.release();
+        sell_free(A);
+        if (stage) cudaFree(stage);
+        if (pinned_b) cudaFreeHost(pinned_b);
+        if (pinned_x) cudaFreeHost(pinned_x);
+        if (st) cudaStreamDestroy(st);
+    }
 };
 
 }  // namespace
 
 struct gdmr_server {
-    long long budget = 0, used = 0;
-    int device = 0;
+    long long budget = 0, used = 0;            // totals over the devices
+    int device = 0;                           // the first device of the list
+    std::vector<int> devices;                 // CUDA ordinals, one per budget
+    std::vector<long long> dev_budget, dev_used;
     std::vector<std::unique_ptr<ServedOperator>> ops;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -185,15 +209,60 @@ extern "C" long long gdmr_server_slot_bytes(int n, int basisDim, int precision) 
     return (long long)slot_bytes(n, basisDim, precision);
 }
 
-extern "C" int gdmr_server_create(gdmr_server **out, long long budget_bytes, int device) {
-    if (!out || budget_bytes <= 0) return srv_fail(nullptr, GDMR_EINVAL, "null output or non-positive budget");
-    if (cudaSetDevice(device) != cudaSuccess) return srv_fail(nullptr, GDMR_ECUDA, "cudaSetDevice");
+// Placement of one operator: the device (index into the budget lists) that keeps the most
+// budget free after taking the operator's fixed bytes plus `capacity` slots; capacity <= 0
+// asks for as many slots as fit (at most 256) on the device with the most budget free.
+// Returns the index, -1 if no device can take the operator with at least one slot.
+extern "C" int gdmr_place_operator(int ndev, const long long *budget, const long long *used, long long fixed,
+                                   long long per_slot, int capacity, int *capacity_out) {
+    int best = -1;
+    long long best_left = -1;
+    int best_cap = 0;
+    for (int d = 0; d < ndev; ++d) {
+        const long long room = budget[d] - used[d] - fixed;
+        if (room < per_slot) continue;
+        const int cap = capacity > 0 ? capacity : (int)std::min(room / per_slot, 256LL);
+        const long long left = room - per_slot * cap;
+        if (left < 0) continue;
+        // with capacity 0 the device with the most room wins (it gets the most slots)
+        const long long key = capacity > 0 ? left : room;
+        if (key > best_left) {
+            best_left = key;
+            best = d;
+            best_cap = cap;
+        }
+    }
+    if (capacity_out) *capacity_out = best >= 0 ? best_cap : 0;
+    return best;
+}
+
+extern "C" int gdmr_server_create_multi(gdmr_server **out, long long budget_per_device, const int *devices,
+                                        int ndevices) {
+    if (!out || budget_per_device <= 0 || !devices || ndevices < 1)
+        return srv_fail(nullptr, GDMR_EINVAL, "null output, non-positive budget or empty device list");
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess) return srv_fail(nullptr, GDMR_ECUDA, "cudaGetDeviceCount");
+    for (int i = 0; i < ndevices; ++i)
+        if (devices[i] < 0 || devices[i] >= count) return srv_fail(nullptr, GDMR_EINVAL, "device ordinal out of range");
+    if (cudaSetDevice(devices[0]) != cudaSuccess) return srv_fail(nullptr, GDMR_ECUDA, "cudaSetDevice");
     auto *s = new gdmr_server();
-    s->budget = budget_bytes;
-    s->device = device;
+    s->device = devices[0];
+    s->devices.assign(devices, devices + ndevices);
+    s->dev_budget.assign(ndevices, budget_per_device);
+    s->dev_used.assign(ndevices, 0);
+    s->budget = budget_per_device * ndevices;
     *out = s;
     set_last_error(GDMR_OK, "ok");
     return GDMR_OK;
+}
+
+extern "C" int gdmr_server_create(gdmr_server **out, long long budget_bytes, int device) {
+    return gdmr_server_create_multi(out, budget_bytes, &device, 1);
+}
+
+extern "C" int gdmr_server_operator_device(gdmr_server *srv, int op_id) {
+    if (!srv || op_id < 0 || op_id >= (int)srv->ops.size()) return -1;
+    return srv->ops[op_id]->slot_dev;
 }
 
 extern "C" int gdmr_server_add_operator(gdmr_server *srv, int n, const int *rowPtr, const int *colIdx,
@@ -202,36 +271,43 @@ extern "C" int gdmr_server_add_operator(gdmr_server *srv, int n, const int *rowP
     if (!srv || !op_id) return srv_fail(srv, GDMR_EINVAL, "null argument");
     if (srv->running) return srv_fail(srv, GDMR_EINVAL, "operators are registered before gdmr_server_start");
     if (precision != 0 && precision != 1) return srv_fail(srv, GDMR_EINVAL, "precision must be 0 or 1");
-    cudaSetDevice(srv->device);
+    // the matrix's padded size decides its fixed bytes: count it on the host before placing it
+    long padded = 0;
+    for (int s0 = 0; s0 < (n + 31) / 32; ++s0) {
+        int w = 0;
+        for (int r = s0 * 32; r < std::min(n, s0 * 32 + 32); ++r) w = std::max(w, rowPtr[r + 1] - rowPtr[r]);
+        padded += 32L * w;
+    }
+    const long long fixed = (long long)fixed_bytes(n, basisDim, deflatDim, precision, padded);
+    const long long per = (long long)slot_bytes(n, basisDim, precision);
+    int cap = 0;
+    const int slot = gdmr_place_operator((int)srv->devices.size(), srv->dev_budget.data(), srv->dev_used.data(), fixed,
+                                         per, capacity, &cap);
+    if (slot < 0) return srv_fail(srv, GDMR_ENOMEM, "operator does not fit in the remaining memory budget");
+    capacity = cap;
+    const int device = srv->devices[slot];
+    cudaSetDevice(device);
     std::unique_ptr<ServedOperator> op(new ServedOperator());
     op->id = (int)srv->ops.size();
-    op->n = n; op->m = basisDim; op->k = deflatDim; op->precision = precision; op->device = srv->device;
+    op->n = n; op->m = basisDim; op->k = deflatDim; op->precision = precision; op->device = device;
+    op->slot_dev = slot;
     if (cudaStreamCreateWithFlags(&op->st, cudaStreamNonBlocking) != cudaSuccess)
         return srv_fail(srv, GDMR_ECUDA, "stream");
     int rc = sell_from_csr(op->A, n, rowPtr, colIdx, vals_ri, precision == 1, true, op->st);
     if (rc != GDMR_OK) return rc;
-    const long long fixed = (long long)fixed_bytes(n, basisDim, deflatDim, precision, op->A.padded);
-    const long long per = (long long)slot_bytes(n, basisDim, precision);
-    const long long left = srv->budget - srv->used - fixed;
-    if (capacity <= 0) capacity = (int)std::max(0LL, std::min(left / per, 256LL));
-    if (capacity < 1 || fixed + per * capacity > srv->budget - srv->used) {
-        sell_free(op->A);
-        cudaStreamDestroy(op->st);
-        return srv_fail(srv, GDMR_ENOMEM, "operator does not fit in the remaining memory budget");
-    }
     op->capacity = capacity;
     if (precision == 1) {
-        rc = op->e32.init(n, basisDim, deflatDim, capacity, srv->device);
+        rc = op->e32.init(n, basisDim, deflatDim, capacity, device);
         op->e32.op.kind = Operator<float>::SELL;
         op->e32.op.sell = op->A.view32();
         op->e32.stream = op->st;
     } else {
-        rc = op->e64.init(n, basisDim, deflatDim, capacity, srv->device);
+        rc = op->e64.init(n, basisDim, deflatDim, capacity, device);
         op->e64.op.kind = Operator<double>::SELL;
         op->e64.op.sell = op->A.view64();
         op->e64.stream = op->st;
     }
-    if (rc != GDMR_OK) { sell_free(op->A); cudaStreamDestroy(op->st); return rc; }
+    if (rc != GDMR_OK) return rc;
     const size_t vb = sizeof(double2) * (size_t)n * capacity;
     if (cudaMalloc(&op->stage, vb) != cudaSuccess || cudaMallocHost(&op->pinned_b, vb) != cudaSuccess ||
         cudaMallocHost(&op->pinned_x, vb) != cudaSuccess)
@@ -240,6 +316,7 @@ extern "C" int gdmr_server_add_operator(gdmr_server *srv, int n, const int *rowP
     op->slot_busy.assign(capacity, false);
     op->bytes = fixed + per * capacity;
     srv->used += op->bytes;
+    srv->dev_used[slot] += op->bytes;
     *op_id = op->id;
     srv->ops.push_back(std::move(op));
     set_last_error(GDMR_OK, "ok");
@@ -323,17 +400,7 @@ extern "C" int gdmr_server_destroy(gdmr_server *srv) {
     srv->cv_work.notify_all();
     for (auto &op : srv->ops)
         if (op->worker.joinable()) op->worker.join();
-    cudaSetDevice(srv->device);
-    for (auto &op : srv->ops) {
-        if (op->st) cudaStreamSynchronize(op->st);
-        op->e32.release();
-        op->e64.release();
-        sell_free(op->A);
-        if (op->stage) cudaFree(op->stage);
-        if (op->pinned_b) cudaFreeHost(op->pinned_b);
-        if (op->pinned_x) cudaFreeHost(op->pinned_x);
-        if (op->st) cudaStreamDestroy(op->st);
-    }
+    srv->ops.clear();   // each operator's destructor frees it on its own device
     delete srv;
     return GDMR_OK;
 }

@@ -76,6 +76,7 @@ SIGNATURES = {
     "gdmr_system_set_graphs": (I, [P, I]),
     "gdmr_system_set_fused": (I, [P, I]),
     "gdmr_system_grid": (I, [P, P]),
+    "gdmr_system_set_compat_eye": (I, [P, I]),
     "gdmr_solve": (I, [P, I, P, P, D, I, I, P]),
     "gdmr_solve_batch": (I, [P, I, P, P, P, I, I, P]),
     "gdmr_true_residual": (I, [P, I, P, P, I, P]),
@@ -88,6 +89,9 @@ SIGNATURES = {
     "gdmr_save_deflation": (I, [P, ctypes.c_char_p]),
     "gdmr_load_deflation": (I, [P, ctypes.c_char_p]),
     "gdmr_server_create": (I, [P, LL, I]),
+    "gdmr_server_create_multi": (I, [P, LL, P, I]),
+    "gdmr_server_operator_device": (I, [P, I]),
+    "gdmr_place_operator": (I, [I, P, P, LL, LL, I, P]),
     "gdmr_server_add_operator": (I, [P, I, P, P, P, I, I, I, I, P]),
     "gdmr_server_slot_bytes": (LL, [I, I, I]),
     "gdmr_server_operator_capacity": (I, [P, I]),
@@ -272,6 +276,17 @@ def load(path: str = LIB_PATH):
     return L
 
 
+def place_operator(budget, used, fixed_bytes: int, per_slot_bytes: int, capacity: int = 0):
+    """Host-only placement rule of the server (gdmr_place_operator): (device index or -1,
+    capacity granted) for an operator on devices with the given budgets and used bytes."""
+    b = np.ascontiguousarray(budget, dtype=np.int64)
+    u = np.ascontiguousarray(used, dtype=np.int64)
+    cap = ctypes.c_int(0)
+    d = load().gdmr_place_operator(len(b), _ptr(b), _ptr(u), int(fixed_bytes), int(per_slot_bytes), int(capacity),
+                                   ctypes.byref(cap))
+    return int(d), int(cap.value)
+
+
 def write_deflation(path: str, Z) -> None:
     """Host-only: write a k x n complex128 deflation space in the versioned on-disk format."""
     Z = np.ascontiguousarray(Z, dtype=np.complex128)
@@ -424,6 +439,10 @@ class System:
         """One small system: run the Krylov loop as one cooperative kernel (default) or step by step."""
         _check(self.L.gdmr_system_set_fused(self._h, 1 if on else 0), "gdmr_system_set_fused")
 
+    def set_compat_eye(self, on: bool) -> None:
+        """The reference's breakdown identity tail (default) or the standard one (see gdmr_ext.h)."""
+        _check(self.L.gdmr_system_set_compat_eye(self._h, 1 if on else 0), "gdmr_system_set_compat_eye")
+
     def grid_shape(self):
         """(nx, ny, nz) if the CSR operator has the structured-grid form, else None."""
         dims = np.zeros(3, dtype=np.int32)
@@ -519,11 +538,17 @@ class Server:
     """Serving layer (gdmr_server_*): resident operators with their deflation spaces,
     continuous batching of requests, admission bounded by a device-memory budget."""
 
-    def __init__(self, budget_bytes: int, device: int = 0):
+    def __init__(self, budget_bytes: int, device: int = 0, devices=None):
+        """budget_bytes per device; devices: a list of CUDA ordinals (operators are placed across
+        them by budget; an ordinal may repeat), default [device]."""
         self.L = load()
         h = ctypes.c_void_p()
-        _check(self.L.gdmr_server_create(ctypes.byref(h), int(budget_bytes), device), "gdmr_server_create")
+        devs = list(devices) if devices is not None else [int(device)]
+        arr = (ctypes.c_int * len(devs))(*devs)
+        _check(self.L.gdmr_server_create_multi(ctypes.byref(h), int(budget_bytes), arr, len(devs)),
+               "gdmr_server_create_multi")
         self._h = h
+        self.devices = devs
         self._keep = {}          # ticket -> (b, x) buffers that must outlive the request
         self.n = {}
 
@@ -539,6 +564,10 @@ class Server:
 
     def capacity(self, op: int) -> int:
         return int(self.L.gdmr_server_operator_capacity(self._h, op))
+
+    def device_of(self, op: int) -> int:
+        """Index into `devices` of the device the operator was placed on."""
+        return int(self.L.gdmr_server_operator_device(self._h, op))
 
     @property
     def device_bytes(self) -> int:

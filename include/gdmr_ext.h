@@ -207,6 +207,12 @@ int gdmr_system_set_graphs(gdmr_system *sys, int on);
  * 0 launches its operator, projection, update and scaling kernels step by step). */
 int gdmr_system_set_fused(gdmr_system *sys, int on);
 
+/* The Hessenberg's identity tail after a Krylov breakdown.  1 (default): the reference's, from
+ * column j of a breakdown at step j (eyeArrayDMR, gDMR.cu:2256-2289), which in a deflated cycle
+ * overwrites the diagonal of valid columns, so the least squares and with it the recursive
+ * residual go wrong while the solve reports convergence (the true FP64 residual in the stats
+ * shows it).  0: the tail starts after the last valid column, kk + j. */
+int gdmr_system_set_compat_eye(gdmr_system *sys, int on);
 /* dims[0..2] <- the grid's edge lengths (nx, ny, nz) if the system's CSR operator has the
  * structured-grid form (gdmrGridOperator), zeros if not. */
 int gdmr_system_grid(const gdmr_system *sys, int *dims);
@@ -269,6 +275,21 @@ int gdmr_load_deflation(gdmr_system *sys, const char *path);
  * must stay valid until the request completes. */
 typedef struct gdmr_server gdmr_server;
 int gdmr_server_create(gdmr_server **out, long long budgetBytes, int device);
+/* A server over several devices, each with its own budget of budgetBytesPerDevice (a device
+ * listed twice gets two budgets on one GPU).  Independent operators shard across them with no
+ * collective, replacing the reference's split of one basis across devices with peer copies
+ * (gDMR.cu:1478-1520, 871-872): gdmr_server_add_operator places each operator, with its
+ * matrix, deflation space, engine, stream and queue, on the device that keeps the most budget
+ * free after taking it (gdmr_place_operator). */
+int gdmr_server_create_multi(gdmr_server **out, long long budgetBytesPerDevice, const int *devices, int ndevices);
+/* Index into the server's device list of the device an operator was placed on (-1: none). */
+int gdmr_server_operator_device(gdmr_server *srv, int opId);
+/* Host-only placement rule of gdmr_server_add_operator: for devices with budget[d] and used[d]
+ * bytes, the device that keeps the most budget free after taking fixedBytes plus capacity
+ * slots of perSlotBytes (capacity <= 0: as many slots as fit, at most 256, on the device with
+ * the most room).  Returns the device index and the capacity granted, or -1 if none fits. */
+int gdmr_place_operator(int ndev, const long long *budget, const long long *used, long long fixedBytes,
+                        long long perSlotBytes, int capacity, int *capacityOut);
 int gdmr_server_add_operator(gdmr_server *srv, int n, const int *rowPtr, const int *colIdx, const double *vals_ri,
                              int basisDim, int deflatDim, int capacity, int precision, int *opId);
 /* Device bytes one slot costs (basis, work vectors, FP64 slot vectors). */

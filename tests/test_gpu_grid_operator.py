@@ -84,3 +84,27 @@ def test_plain_solve_is_identical_on_both_kernels(precision):
     assert sg["status"] == 0 and sg["true_rel_res"] <= 2e-10, sg
     assert sg["cycles"] == ss["cycles"]
     assert np.array_equal(xg, xs)
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_fp64_true_residual_is_identical_on_both_kernels(case):
+    """The FP64 true residual b - A x on the coefficient planes (real planes skip their zero
+    imaginary products) against the SELL form: the same values, bit for bit."""
+    make, shape, nrhs = CASES[case]
+    A = make()
+    rng = np.random.default_rng(11)
+    B = np.array([problems.unit_gaussian_rhs(A.n, 70 + i) for i in range(nrhs)])
+    X = rng.standard_normal(B.shape) + 1j * rng.standard_normal(B.shape)
+    out = {}
+    for grid in (True, False):
+        gdmr.grid_operator(grid)
+        try:
+            s = gdmr.System(A, 30, 10, capacity=nrhs, precision="mixed")
+            out[grid] = s.true_residual(B, X)
+            s.close()
+        finally:
+            gdmr.grid_operator(True)
+    assert np.array_equal(out[True], out[False])
+    S = A.to_scipy()
+    ref = np.linalg.norm(B - (S @ X.T).T, axis=1) / np.linalg.norm(B, axis=1)
+    assert np.allclose(out[True], ref, rtol=1e-12)

@@ -84,3 +84,25 @@ def test_result_same_alone_and_in_the_mix(ops):
     assert np.linalg.norm(xa - xd) / np.linalg.norm(xd) < 1e-8
     assert np.linalg.norm(xm - xd) / np.linalg.norm(xd) < 1e-8
     assert np.linalg.norm(xa - xm) / np.linalg.norm(xd) < 2e-8
+
+
+def test_operators_spread_over_a_device_list_and_solve_correctly(ops):
+    """A server over two budgets (the device list names device 0 twice, as the reference's
+    device lists may): operators go to the budget with the most room left, requests of both
+    run and meet their tolerance, and no budget is exceeded."""
+    A1, A2 = ops
+    per_dev = 3 << 30
+    srv = gdmr.Server(budget_bytes=per_dev, devices=[0, 0])
+    ids = [srv.add_operator(A, 30, 8, capacity=4, precision="mixed") for A in (A1, A2, A1, A2)]
+    placed = [srv.device_of(i) for i in ids]
+    assert sorted(placed) == [0, 0, 1, 1] and placed[0] != placed[1]
+    assert srv.device_bytes <= 2 * per_dev
+    srv.start()
+    reqs = [(j, problems.unit_gaussian_rhs((A1 if j % 2 == 0 else A2).n, 1300 + j)) for j in range(4)]
+    tickets = [srv.submit(ids[j], b, tol=1e-10) for j, b in reqs]
+    for (j, b), t in zip(reqs, tickets):
+        x, st = srv.wait(t, timeout=120)
+        A = A1 if j % 2 == 0 else A2
+        assert st["status"] == 0 and st["true_rel_res"] <= 1e-10
+        assert np.linalg.norm(b - A.to_scipy() @ x) / np.linalg.norm(b) <= 1.5e-10
+    srv.close()
