@@ -892,6 +892,211 @@ extern "C" int gdmr_solve_batch(gdmr_system *S, int nrhs, const double *b, doubl
     return batch_impl<double>(S, nrhs, b, x, tol, maxCycles, on_device, stats);
 }
 
+// ================================================================ many operators in lockstep
+// gdmr_multi_solve: the refined batched solve of several systems (operators) at once, their
+// restart cycles in lockstep and the Krylov loops of every right-hand side in flight, across all
+// operators, in one cooperative launch a cycle (k_krylov_multi), instead of one engine and stream
+// per operator each launching its own kernels.  The rest of a cycle (true residual, deflation
+// loop, least squares, combinations, deflation update) stays on each operator's own stream.
+namespace {
+template <class R>
+int multi_impl(int nops, gdmr_system *const *sys, const int *nrhs, const double *const *b, double *const *x,
+               const double *tol, int maxCycles, gdmr_stats *const *stats) {
+    const char *F = "gdmr_multi_solve";
+    const int dev = sys[0]->device;
+    std::vector<Engine<R> *> E(nops);
+    int total = 0, max_jobs = 0, qmax = 0;
+    for (int o = 0; o < nops; ++o) {
+        E[o] = &eng_of<R>(sys[o]);
+        int rc = E[o]->refine_setup(sys[o]->A.view64());
+        if (rc != GDMR_OK) return rc;
+        total += nrhs[o];
+        max_jobs += E[o]->capacity();
+        qmax = std::max(qmax, sys[o]->m + 1);
+    }
+    const int resident = krylov_multi_resident();
+    if (resident < 1) return fail(GDMR_ECUDA, F, "the many-system kernel cannot be resident");
+    // driver-owned device buffers: jobs, the job of each CTA, partial sums, barrier counters
+    KrylovJob<R> *djobs = nullptr, *hjobs = nullptr;
+    int *dcta = nullptr, *hcta = nullptr, *dabort = nullptr;
+    double *dpart = nullptr;
+    unsigned *dbar = nullptr;
+    cudaStream_t ms = nullptr;
+    cudaEvent_t ev_kernel = nullptr;
+    std::vector<cudaEvent_t> ev_front(nops, nullptr);
+    auto release = [&]() {
+        cudaFree(djobs);
+        cudaFreeHost(hjobs);
+        cudaFree(dcta);
+        cudaFreeHost(hcta);
+        cudaFree(dabort);
+        cudaFree(dpart);
+        cudaFree(dbar);
+        if (ev_kernel) cudaEventDestroy(ev_kernel);
+        for (auto &e : ev_front)
+            if (e) cudaEventDestroy(e);
+        if (ms) cudaStreamDestroy(ms);
+    };
+    const size_t part_doubles = (size_t)resident * (2 * (size_t)qmax + 3);
+    if (cudaMalloc(&djobs, sizeof(KrylovJob<R>) * max_jobs) != cudaSuccess ||
+        cudaMallocHost(&hjobs, sizeof(KrylovJob<R>) * max_jobs) != cudaSuccess ||
+        cudaMalloc(&dcta, sizeof(int) * resident) != cudaSuccess ||
+        cudaMallocHost(&hcta, sizeof(int) * resident) != cudaSuccess || cudaMalloc(&dabort, sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&dpart, sizeof(double) * part_doubles) != cudaSuccess ||
+        cudaMalloc(&dbar, sizeof(unsigned) * max_jobs) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ms, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev_kernel, cudaEventDisableTiming) != cudaSuccess) {
+        release();
+        return fail(GDMR_ENOMEM, F, "driver buffers");
+    }
+    for (auto &e : ev_front)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            release();
+            return fail(GDMR_ECUDA, F, "events");
+        }
+    std::vector<std::vector<int>> slot_of(nops);
+    std::vector<int> next(nops, 0);
+    for (int o = 0; o < nops; ++o) slot_of[o].assign(E[o]->capacity(), -1);
+    int finished = 0, worst = GDMR_OK;
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<KrylovJob<R>> jobs;
+    std::vector<long> job_nnz;   // non-zeros of each job's operator (algorithmic bytes)
+    while (finished < total) {
+        // admission into free slots, then the true residuals of every operator (enqueued)
+        for (int o = 0; o < nops; ++o) {
+            gdmr_system *S = sys[o];
+            const size_t vb = sizeof(double2) * (size_t)S->n;
+            for (int sl = 0; sl < E[o]->capacity() && next[o] < nrhs[o]; ++sl) {
+                if (slot_of[o][sl] >= 0) continue;
+                const int r = next[o]++;
+                if (cudaMemcpyAsync(S->db + (size_t)sl * S->n, b[o] + (size_t)2 * r * S->n, vb, cudaMemcpyHostToDevice,
+                                    S->st) != cudaSuccess ||
+                    cudaMemcpyAsync(S->dx + (size_t)sl * S->n, x[o] + (size_t)2 * r * S->n, vb, cudaMemcpyHostToDevice,
+                                    S->st) != cudaSuccess) {
+                    release();
+                    return fail(GDMR_ECUDA, F, "host to device copy failed");
+                }
+                int rc = E[o]->refine_admit(sl, S->db + (size_t)sl * S->n, S->dx + (size_t)sl * S->n,
+                                            tol ? tol[o] : 1e-10, maxCycles);
+                if (rc != GDMR_OK) { release(); return rc; }
+                slot_of[o][sl] = r;
+            }
+            int rc = E[o]->multi_residual();
+            if (rc != GDMR_OK) { release(); return rc; }
+        }
+        // convergence, retirement, and the front of the cycle of each operator
+        jobs.clear();
+        job_nnz.clear();
+        for (int o = 0; o < nops; ++o) {
+            gdmr_system *S = sys[o];
+            std::vector<int> done;
+            const int nrun = E[o]->multi_select(&done);
+            if (nrun < 0) { release(); return GDMR_ECUDA; }
+            for (int sl : done) {
+                const int r = slot_of[o][sl];
+                cudaMemcpyAsync(x[o] + (size_t)2 * r * S->n, E[o]->slot_x(sl), sizeof(double2) * (size_t)S->n,
+                                cudaMemcpyDeviceToHost, S->st);
+                if (stats && stats[o]) {
+                    to_stats(E[o]->slot_stats(sl), &stats[o][r]);
+                    stats[o][r].latency_ms =
+                        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+                }
+                worst = std::max(worst, E[o]->slot_stats(sl).status);
+                slot_of[o][sl] = -1;
+                ++finished;
+            }
+            if (nrun > 0) {
+                int rc = E[o]->multi_front();
+                if (rc != GDMR_OK) { release(); return rc; }
+                if (cudaEventRecord(ev_front[o], E[o]->main_stream()) != cudaSuccess ||
+                    cudaStreamWaitEvent(ms, ev_front[o], 0) != cudaSuccess) {
+                    release();
+                    return fail(GDMR_ECUDA, F, "events");
+                }
+                E[o]->multi_jobs(jobs);
+                job_nnz.resize(jobs.size(), S->A.nnz);
+            }
+        }
+        if (jobs.empty()) continue;
+        const int njobs = (int)jobs.size();
+        if (njobs > resident || njobs > max_jobs) {
+            release();
+            return fail(GDMR_EINVAL, F, "more right-hand sides in flight than the persistent launch holds");
+        }
+        // CTAs to jobs in proportion to n (at least one, at most one per slice); partials and
+        // barrier counters per job
+        double sum_n = 0;
+        for (auto &j : jobs) sum_n += j.n;
+        int ctas = 0;
+        size_t poff = 0;
+        double bytes = 0;
+        for (int i = 0; i < njobs; ++i) {
+            KrylovJob<R> &j = jobs[i];
+            const int left = resident - ctas - (njobs - 1 - i);   // keep one for each job after this
+            int c = (int)((double)resident * j.n / sum_n);
+            c = std::max(1, std::min(c, std::min(j.nslices, left)));
+            j.cta0 = ctas;
+            j.ncta = c;
+            j.part = dpart + poff;
+            j.bar = dbar + i;
+            poff += (size_t)c * (2 * (size_t)j.qmax + 3);
+            for (int q = 0; q < c; ++q) hcta[ctas + q] = i;
+            ctas += c;
+            const SellMatrix A{j.n, j.nslices, j.slice_ptr, j.cols, j.vals, job_nnz[i]};
+            bytes += krylov_loop_bytes(A, sizeof(typename CT<R>::t), j.kk, j.m);
+            hjobs[i] = j;
+        }
+        if (cudaMemcpyAsync(djobs, hjobs, sizeof(KrylovJob<R>) * njobs, cudaMemcpyHostToDevice, ms) != cudaSuccess ||
+            cudaMemcpyAsync(dcta, hcta, sizeof(int) * ctas, cudaMemcpyHostToDevice, ms) != cudaSuccess ||
+            cudaMemsetAsync(dbar, 0, sizeof(unsigned) * njobs, ms) != cudaSuccess ||
+            cudaMemsetAsync(dabort, 0, sizeof(int), ms) != cudaSuccess ||
+            launch_krylov_multi<R>(djobs, dcta, ctas, dabort, bytes, ms) != 1 ||
+            cudaEventRecord(ev_kernel, ms) != cudaSuccess) {
+            release();
+            return fail(GDMR_ECUDA, F, "the many-system launch failed");
+        }
+        for (int o = 0; o < nops; ++o) {
+            int rc = E[o]->multi_back(ev_kernel);
+            if (rc != GDMR_OK) { release(); return rc; }
+        }
+        // the host buffers of this launch are reused only after every operator's stream, which
+        // waits for it, has been synchronised by the next round's multi_select
+    }
+    for (int o = 0; o < nops; ++o) cudaStreamSynchronize(sys[o]->st);
+    cudaStreamSynchronize(ms);
+    release();
+    (void)dev;
+    if (worst != GDMR_OK)
+        set_last_error(worst, "gdmr_multi_solve: some right-hand sides did not converge; see the stats");
+    else
+        set_last_error(GDMR_OK, "ok");
+    return worst;
+}
+}  // namespace
+
+extern "C" int gdmr_multi_solve(int nops, gdmr_system *const *systems, const int *nrhs, const double *const *b,
+                                double *const *x, const double *tol, int maxCycles, gdmr_stats *const *stats) {
+    if (nops < 1 || !systems || !nrhs || !b || !x) return fail(GDMR_EINVAL, "gdmr_multi_solve", "null argument");
+    const int prec = systems[0] ? systems[0]->precision : -1, dev = systems[0] ? systems[0]->device : -1;
+    for (int o = 0; o < nops; ++o) {
+        if (!systems[o] || !b[o] || !x[o] || nrhs[o] < 0)
+            return fail(GDMR_EINVAL, "gdmr_multi_solve", "null system or buffer, or a negative count");
+        if (systems[o]->precision != prec || systems[o]->device != dev)
+            return fail(GDMR_EINVAL, "gdmr_multi_solve", "all systems need the same precision and device");
+    }
+    std::vector<std::unique_lock<std::mutex>> locks;
+    for (int o = 0; o < nops; ++o) {
+        bool seen = false;   // the same system twice: lock it once
+        for (int p = 0; p < o; ++p) seen |= systems[p] == systems[o];
+        if (seen) return fail(GDMR_EINVAL, "gdmr_multi_solve", "a system is listed twice");
+        locks.emplace_back(systems[o]->mu);
+    }
+    cudaSetDevice(dev);
+    if (prec == 1) return multi_impl<float>(nops, systems, nrhs, b, x, tol, maxCycles, stats);
+    if (prec == 2) return multi_impl<dfr>(nops, systems, nrhs, b, x, tol, maxCycles, stats);
+    return multi_impl<double>(nops, systems, nrhs, b, x, tol, maxCycles, stats);
+}
+
 extern "C" int gdmr_true_residual(gdmr_system *S, int nrhs, const double *b, const double *x, int on_device,
                                   double *relres) {
     if (!S || !b || !x || !relres || nrhs < 1) return fail(GDMR_EINVAL, "gdmr_true_residual", "bad argument");

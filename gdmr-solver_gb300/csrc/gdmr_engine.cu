@@ -632,6 +632,15 @@ template <class R> int Engine<R>::run_cycle(int kk, int nsys, int lead, double t
 }
 
 template <class R> int Engine<R>::enqueue_cycle(int kk, int nsys, double tol, long *matvecs, bool join) {
+    int rc = enqueue_front(kk, nsys, matvecs);
+    if (rc != GDMR_OK) return rc;
+    if ((rc = enqueue_krylov(kk, nsys, tol, matvecs)) != GDMR_OK) return rc;
+    return enqueue_back(kk, nsys, join);
+}
+
+// The cycle up to its Krylov loop: H cleared, the deflation loop (W = orth(A Z), the shared
+// block of H) and v_0 <- (I - W W^H) v_0 / ||.||.
+template <class R> int Engine<R>::enqueue_front(int kk, int nsys, long *matvecs) {
     const int n = n_, m = m_;
     const size_t sV = strideV(), sC = strideC();
     const bool hook = op.kind == Operator<R>::HOOK;
@@ -679,8 +688,16 @@ template <class R> int Engine<R>::enqueue_cycle(int kk, int nsys, double tol, lo
     } else if (hook) {
         cudaMemcpyAsync(op.ext, V_, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
     }
-    // Krylov loop (gDMR.cu:2069-2328): classical Gram-Schmidt against [W V] in one pass.  One
-    // small system with a SELL operator runs the whole loop as one cooperative kernel.
+    GDMR_CK(cudaGetLastError());
+    return GDMR_OK;
+}
+
+// The Krylov loop (gDMR.cu:2069-2328): classical Gram-Schmidt against [W V] in one pass.
+template <class R> int Engine<R>::enqueue_krylov(int kk, int nsys, double tol, long *matvecs) {
+    const int n = n_, m = m_;
+    const size_t sV = strideV(), sC = strideC();
+    const bool hook = op.kind == Operator<R>::HOOK;
+    // One small system with a SELL operator runs the whole loop as one cooperative kernel.
     const bool fused = nsys == 1 && op.kind == Operator<R>::SELL && fused_small &&
                        launch_krylov_small<R>(n, kk, m, op.sell, W_, V_, sV, act_, state_, H_, strideH(), coef_, sC,
                                               (double *)partials_, qmax(), ks_bar_, tol, compat_eye, stream);
@@ -716,6 +733,15 @@ template <class R> int Engine<R>::enqueue_cycle(int kk, int nsys, double tol, lo
             launch_scale<R>(n, T_, n, V_ + (size_t)j * n, sV, hook ? op.ext : nullptr, 0, act_, nsys, state_, true,
                             stream);
     }
+    GDMR_CK(cudaGetLastError());
+    return GDMR_OK;
+}
+
+// The cycle after its Krylov loop: the deflation-space update on the side stream, g, the
+// least squares, the residual and solution combinations.
+template <class R> int Engine<R>::enqueue_back(int kk, int nsys, bool join) {
+    const int n = n_, m = m_;
+    const size_t sV = strideV(), sC = strideC();
     // deflation-space update from the lead system (genDeflatDMR, gDMR.cu:1583-1704), on the
     // side stream: it needs only H_lead and the basis, which nothing below modifies
     if (k_ > 0) {
@@ -1003,6 +1029,154 @@ template <class R> int Engine<R>::refine_cycle(std::vector<int> *done) {
         if (st.broken) S.stats.breakdowns++;
     }
     kk_prev_ = kk;
+    return GDMR_OK;
+}
+
+// ----------------------------------------------------------------- lockstep (many-operator) form
+template <class R> int Engine<R>::multi_residual() {
+    if (act_h_.empty()) return GDMR_OK;
+    const int n = n_;
+    std::vector<int> act = act_h_;
+    if (set_active(act) != GDMR_OK) return GDMR_ECUDA;
+    std::vector<int> fresh;
+    for (int s : act)
+        if (slot_[s].bnorm < 0) fresh.push_back(s);
+    if (!fresh.empty()) {
+        if (set_active(fresh) != GDMR_OK) return GDMR_ECUDA;
+        launch_norm<double>(n, b64_, n, act_, (int)fresh.size(), partials_, tickets_, state_, 1, stream);
+        if (set_active(act) != GDMR_OK) return GDMR_ECUDA;
+    }
+    launch_residual64(A64_, b64_, n, x64_, n, r64_, n, act_, (int)act.size(), partials_, tickets_, state_, stream);
+    GDMR_CK(cudaGetLastError());
+    return GDMR_OK;
+}
+
+template <class R> int Engine<R>::multi_select(std::vector<int> *done) {
+    mf_nsys_ = 0;
+    if (act_h_.empty()) return 0;
+    if (read_state(cap_) != GDMR_OK) return -1;
+    // the last cycle's bookkeeping (refine_cycle does it right after its cycle)
+    if (mf_ran_) {
+        for (int s : mf_act_) {
+            Slot &S = slot_[s];
+            const SysState &st = hstate_[s];
+            if (st.rho > 0.995) { S.loop_flag = 1; ++S.flag_count; } else S.loop_flag = 0;
+            S.stats.cycles += 1;
+            S.stats.matvecs += m_;
+            if (st.broken) S.stats.breakdowns++;
+        }
+        kk_prev_ = mf_kk_;
+        mf_ran_ = false;
+    }
+    const bool lost = timed_out();
+    if (lost) {
+        to_base_ = timeouts_now();
+        drop_deflation();
+        set_last_error(GDMR_ETIMEOUT, "a bounded device wait ran out during the solve (gdmrWaitLimit)");
+    }
+    std::vector<int> next;
+    int lead = -1;
+    double worst = -1;
+    for (int s : act_h_) {
+        Slot &S = slot_[s];
+        const SysState &st = hstate_[s];
+        if (S.bnorm < 0) S.bnorm = st.bnorm;
+        const double rel = S.bnorm > 0 ? st.true_res / S.bnorm : 0.0;
+        S.stats.true_rel_res = rel;
+        S.stats.rel_res = rel;
+        S.stats.matvecs += 1;
+        int fin = -1;
+        if (lost && S.stats.cycles > 0) fin = GDMR_ETIMEOUT;
+        else if (st.bad || !std::isfinite(rel)) fin = GDMR_ENONFINITE;
+        else if (rel <= S.tol) fin = GDMR_OK;
+        else if (S.stats.cycles >= S.max_cycles) fin = GDMR_ENOCONV;
+        if (fin >= 0) {
+            S.stats.status = fin;
+            S.stats.its = S.stats.cycles > 0 ? S.stats.cycles - 1 : 0;
+            S.active = false;
+            if (done) done->push_back(s);
+            continue;
+        }
+        next.push_back(s);
+        if (rel > worst) { worst = rel; lead = s; }
+    }
+    act_h_ = next;
+    if (next.empty()) {
+        if (sync_deflation() != GDMR_OK) return -1;
+        return 0;
+    }
+    lead_host_ = lead;
+    mf_nsys_ = (int)next.size();
+    return mf_nsys_;
+}
+
+template <class R> int Engine<R>::multi_front() {
+    if (mf_nsys_ == 0) return GDMR_OK;
+    if (op.kind != Operator<R>::SELL) {
+        set_last_error(GDMR_EINVAL, "many-operator solve: needs a SELL operator");
+        return GDMR_EINVAL;
+    }
+    const int n = n_, m = m_, k = k_;
+    const std::vector<int> next = act_h_;
+    const int na = (int)next.size();
+    if (set_active(next) != GDMR_OK) return GDMR_ECUDA;
+    launch_demote_unit<R>(n, r64_, n, R_, n, act_, na, state_, stream);
+    k_cycle_reset<<<1, 256, 0, stream>>>(act_, na, state_, 1);
+    if (sync_deflation() != GDMR_OK) return GDMR_ECUDA;
+    const int kk = (k > 0 && have_z_) ? k : 0;
+    for (int s : next) {
+        Slot &S = slot_[s];
+        const int period = (2 * S.max_cycles) / (m - k);
+        if (S.loop_flag == 0 || (period != 0 && S.flag_count % period == 0)) {
+            cudaMemcpyAsync(Vs(s), R_ + (size_t)s * n, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
+        } else {
+            const int idx = kk + (m - k) / 2 - kk_prev_;
+            if (idx > 0 && idx <= m)
+                cudaMemcpyAsync(Vs(s), Vs(s) + (size_t)idx * n, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
+        }
+    }
+    GDMR_CK(cudaMemcpyAsync(lead_dev_, &lead_host_, sizeof(int), cudaMemcpyHostToDevice, stream));
+    long mv = 0;
+    int rc = enqueue_front(kk, na, &mv);
+    if (rc != GDMR_OK) return rc;
+    ++cycles_run_;
+    mf_kk_ = kk;
+    mf_tol_ = sizeof(R) == 4 ? 1e-6 : 1e-14;   // breakdown of unit vectors, as refine_cycle
+    mf_act_ = next;
+    return GDMR_OK;
+}
+
+template <class R> void Engine<R>::multi_jobs(std::vector<KrylovJob<R>> &jobs) const {
+    for (int s : mf_act_) {
+        KrylovJob<R> j{};
+        j.n = n_;
+        j.nslices = op.sell.nslices;
+        j.kk = mf_kk_;
+        j.m = m_;
+        j.compat_eye = compat_eye ? 1 : 0;
+        j.qmax = qmax();
+        j.tol = mf_tol_;
+        j.slice_ptr = op.sell.slice_ptr;
+        j.cols = op.sell.cols;
+        j.vals = (const C *)op.sell.vals;
+        j.W = W_;
+        j.V = Vs(s);
+        j.y = Y_ + (size_t)s * n_;
+        j.state = state_ + s;
+        j.H = H_ + (size_t)s * strideH();
+        j.coef = coef_ + (size_t)s * strideC();
+        jobs.push_back(j);
+    }
+}
+
+template <class R> int Engine<R>::multi_back(cudaEvent_t after) {
+    if (mf_nsys_ == 0) return GDMR_OK;
+    GDMR_CK(cudaStreamWaitEvent(stream, after, 0));
+    int rc = enqueue_back(mf_kk_, mf_nsys_, false);
+    if (rc != GDMR_OK) return rc;
+    launch_refine_update<R>(n_, x64_, n_, X_, n_, act_, mf_nsys_, state_, stream);
+    GDMR_CK(cudaGetLastError());
+    mf_ran_ = true;
     return GDMR_OK;
 }
 

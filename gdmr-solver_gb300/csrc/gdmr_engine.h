@@ -159,6 +159,20 @@ template <class R> class Engine {
     // FP64 relative residual ||b_s - A64 x_s|| / ||b_s|| of arbitrary device pairs (s < capacity slots used as scratch).
     int true_residual(int count, const double2 *b, const double2 *x, double *relres);
 
+    // Lockstep driving of several engines, the Krylov loops of all their systems in one launch
+    // (the many-operator form, gdmr_multi_solve).  A refined cycle in five parts:
+    // multi_residual enqueues the true FP64 residual of the active slots; multi_select
+    // synchronises, books the previous cycle, retires finished slots into `done` and returns how
+    // many systems run a cycle now; multi_front enqueues the cycle up to its Krylov loop;
+    // multi_jobs appends one Krylov job per such system; multi_back waits for the event `after`
+    // (the launch) and enqueues the rest of the cycle and the FP64 correction.  SELL operators.
+    int multi_residual();
+    int multi_select(std::vector<int> *done);
+    int multi_front();
+    void multi_jobs(std::vector<KrylovJob<R>> &jobs) const;
+    int multi_back(cudaEvent_t after);
+    cudaStream_t main_stream() const { return stream; }
+
     // Deflation basis (k x n, vector-contiguous) between host and device, precision R.
     int import_deflation(const C *host);
     int export_deflation(C *host);
@@ -239,6 +253,14 @@ template <class R> class Engine {
     int cycles_run_ = 0, zpar_ = 0, lead_host_ = 0;
     int *lead_dev_ = nullptr;
     int enqueue_cycle(int kk, int nsys, double tol, long *matvecs, bool join);
+    int enqueue_front(int kk, int nsys, long *matvecs);
+    int enqueue_krylov(int kk, int nsys, double tol, long *matvecs);
+    int enqueue_back(int kk, int nsys, bool join);
+    // lockstep (many-operator) form: the cycle the last multi_front set up
+    int mf_kk_ = 0, mf_nsys_ = 0;
+    bool mf_ran_ = false;       // a cycle ran since the last multi_select
+    double mf_tol_ = 0;
+    std::vector<int> mf_act_;   // the slots of that cycle
 
     size_t strideV() const { return (size_t)(m_ + 1) * n_; }
     size_t strideH() const { return (size_t)(m_ + 1) * m_; }

@@ -195,48 +195,7 @@ int capped_grid(int n, int nsys, int per_sm) {
 }
 
 // ----------------------------------------------------------------- finishing
-__device__ void run_finish(const FinishArgs &f, int s, SysState &st, double n2, double cre, double cim) {
-    st.nrm2 = n2;
-    st.cross_re = cre;
-    st.cross_im = cim;
-    const double nrm = sqrt(n2);
-    if (!isfinite(nrm)) st.bad = 1;
-    switch (f.mode) {
-    case FIN_KRYLOV: {
-        double2 *H = f.H + (size_t)s * f.strideH;
-        const double2 *c = f.coef + (size_t)s * f.strideC;
-        for (int p = 0; p < f.nco; ++p) H[(size_t)f.col * f.ldH + p] = c[p];
-        const int j = f.col - f.kk + 1;
-        if (nrm < f.tol) {   // absolute breakdown threshold, gDMR.cu:2256
-            st.broken = j;
-            st.alpha = 0.0;
-            for (int cc = f.compat_eye ? j : f.kk + j; cc < f.m; ++cc) H[(size_t)cc * f.ldH + cc] = make_double2(1.0, 0.0);
-        } else {
-            st.alpha = 1.0 / nrm;
-            H[(size_t)f.col * f.ldH + f.col + 1] = make_double2(cre / nrm, cim / nrm);
-        }
-        break;
-    }
-    case FIN_DEFLATION: {
-        double2 *H = f.H;
-        const double2 *c = f.coef;
-        for (int p = 0; p < f.nco; ++p) H[(size_t)f.col * f.ldH + p] = c[p];
-        st.alpha = 1.0 / nrm;
-        H[(size_t)f.col * f.ldH + f.col] = make_double2(cre / nrm, cim / nrm);
-        break;
-    }
-    case FIN_UNIT:
-        st.alpha = 1.0 / nrm;
-        break;
-    case FIN_RESIDUAL:
-        st.rho = nrm;
-        st.alpha = 1.0 / nrm;
-        st.rho_abs = st.rho_abs * nrm;
-        break;
-    default:
-        break;
-    }
-}
+// run_finish: gdmr_kernels.cuh
 
 // ----------------------------------------------------------------- multi-dot
 // A CTA owns one chunk of NT*EPT elements of one system.  Thread tid holds EPT/VEC
@@ -1100,6 +1059,7 @@ __device__ bool ks_grid_sync(unsigned *bar, unsigned target, int *abort) {
 }
 template <class C> __device__ __forceinline__ C ldcg_c(const C *p);
 template <> __device__ __forceinline__ double2 ldcg_c<double2>(const double2 *p) { return __ldcg(p); }
+template <> __device__ __forceinline__ float2 ldcg_c<float2>(const float2 *p) { return __ldcg(p); }
 template <> __device__ __forceinline__ dfc ldcg_c<dfc>(const dfc *p) {
     const float4 f = __ldcg(reinterpret_cast<const float4 *>(p));
     dfc c;
@@ -1264,7 +1224,9 @@ __global__ void __launch_bounds__(KS_THREADS) k_krylov_small(KrylovSmallArgs<R> 
                 run_finish(f, s, *st, n2, red[1], red[2]);
             }
         }
-        // (6) v_j = w / ||w|| (zero after a breakdown, which ends the cycle's Krylov loop)
+        // (6) v_j = w / ||w||; a breakdown ends the cycle's Krylov loop with v_j and the rest of
+        // the basis zero, as the reference clears it (gDMR.cu:2256-2289): the cycle-end
+        // projection reads all of it
         if (warp == 0 && row < n) {
             C v = ws[lane];
             const R al = broken ? R(0.f) : R(1.0 / nrm);
@@ -1272,9 +1234,182 @@ __global__ void __launch_bounds__(KS_THREADS) k_krylov_small(KrylovSmallArgs<R> 
             v.y = v.y * al;
             if (broken) v = czero<C>();
             V[(size_t)j * n + row] = v;
+            if (broken)
+                for (int jj = j + 1; jj <= a.m - kk; ++jj) V[(size_t)jj * n + row] = czero<C>();
         }
         if (broken) return;
         if (!ks_grid_sync(a.bar, (++k) * G, abort)) return;
+    }
+}
+
+// ----------------------------------------------------------------- many systems, one launch
+// The Krylov loops of one restart cycle of many systems, of operators of different sizes, in one
+// cooperative launch: the restart cycles of the 48-operator workload run in lockstep, and the
+// Krylov loop of every system still in flight (the per-system convergence mask is the job list)
+// is one kernel instead of four launches a step on each operator's stream.  Each job (one
+// system) owns a contiguous range of CTAs sized to its n; its warps own SELL slices
+// g, g + W, ... (g the warp's index in the job, W the job's warps), the same slices in every
+// phase, so a warp only reads other warps' rows where the operator gathers v_{j-1}.  A step
+// (arnoldiDMR's Krylov loop with the deflator, gDMR.cu:2069-2328):
+//   SpMV of v_{j-1} into the job's scratch y, projection partials of [W V] against y (eight
+//   coefficients a pass, warp sums, CTA sums in warp order) -> | CTA c sums coefficients
+//   c, c + ncta, ... over the CTAs in order -> | update out = y - sum c_p B_p in place of y,
+//   norm and cross-term partials -> | every CTA sums those in the same order, CTA 0 of the job
+//   runs the step's finish (H column, breakdown test and identity tail), all scale their rows
+//   into V_j -> | next step.
+// The barriers are per job (the job's counter, target = passes x ncta); values other CTAs wrote
+// are read through L2 (ld.global.cg).  Every wait is bounded by the process's wait limit and a
+// timeout raises a flag that ends every job's loop.
+// KrylovJob<R>: gdmr_kernels.cuh
+
+constexpr int KM_THREADS = 256, KM_WARPS = KM_THREADS / 32, KM_PB = 8;   // coefficients a pass
+
+
+template <class R>
+__global__ void __launch_bounds__(KM_THREADS) k_krylov_multi(const KrylovJob<R> *__restrict__ jobs,
+                                                              const int *__restrict__ cta_job, int *abort) {
+    using C = typename CT<R>::t;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const KrylovJob<R> a = jobs[cta_job[blockIdx.x]];
+    const int c = blockIdx.x - a.cta0, ncta = a.ncta, n = a.n, kk = a.kk;
+    const int gw = c * KM_WARPS + warp, nw = ncta * KM_WARPS;   // the warp's index in the job
+    double *npart = a.part + (size_t)ncta * a.qmax * 2;
+    __shared__ double wsum[KM_WARPS][KM_PB][2];
+    __shared__ double red[KM_WARPS][3];
+    __shared__ C cs[QMAX];
+    __shared__ double s_norm[3];
+    unsigned k = 0;   // barrier passes
+    for (int j = 1; j <= a.m - kk; ++j) {
+        const int q = kk + j;
+        const C *x = a.V + (size_t)(j - 1) * n;
+        // (1) y = A v_{j-1} on the warp's slices (v_{j-1} rows of other warps through L2)
+        for (int sl = gw; sl < a.nslices; sl += nw) {
+            const int row = sl * 32 + lane;
+            const int beg = a.slice_ptr[sl], width = (a.slice_ptr[sl + 1] - beg) >> 5;
+            C acc = czero<C>();
+            for (int e = 0; e < width; ++e) {
+                const int idx = beg + e * 32 + lane;
+                cfma(acc, a.vals[idx], ldcg_c(x + a.cols[idx]));
+            }
+            if (row < n) a.y[row] = canon(acc);
+        }
+        __syncwarp();
+        // (2) projection partials <B_p, y>, KM_PB coefficients a pass over the warp's rows
+        for (int p0 = 0; p0 < q; p0 += KM_PB) {
+            C acc[KM_PB];
+#pragma unroll
+            for (int u = 0; u < KM_PB; ++u) acc[u] = czero<C>();
+            for (int sl = gw; sl < a.nslices; sl += nw) {
+                const int row = sl * 32 + lane;
+                if (row >= n) continue;
+                const C yv = a.y[row];
+#pragma unroll
+                for (int u = 0; u < KM_PB; ++u) {
+                    const int p = p0 + u;
+                    if (p < q) {
+                        const C *B = p < kk ? a.W + (size_t)p * n : a.V + (size_t)(p - kk) * n;
+                        cdotacc(acc[u], B[row], yv);
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < KM_PB; ++u) {
+                const double re = warp_sum((double)acc[u].x), im = warp_sum((double)acc[u].y);
+                if (lane == 0) {
+                    wsum[warp][u][0] = re;
+                    wsum[warp][u][1] = im;
+                }
+            }
+            __syncthreads();
+            if (tid < 2 * KM_PB && p0 + tid / 2 < q) {
+                double t = 0;
+                for (int w = 0; w < KM_WARPS; ++w) t += wsum[w][tid / 2][tid & 1];
+                a.part[((size_t)c * a.qmax + p0 + tid / 2) * 2 + (tid & 1)] = t;
+            }
+            __syncthreads();
+        }
+        if (!ks_grid_sync(a.bar, (++k) * ncta, abort)) return;
+        // (3) coefficient p summed over the job's CTAs by CTA p mod ncta, in order
+        if (warp == 0)
+            for (int p = c; p < q; p += ncta) {
+                double re = 0, im = 0;
+                for (int g = lane; g < ncta; g += 32) {
+                    re += __ldcg(a.part + ((size_t)g * a.qmax + p) * 2);
+                    im += __ldcg(a.part + ((size_t)g * a.qmax + p) * 2 + 1);
+                }
+                re = warp_sum(re);
+                im = warp_sum(im);
+                if (lane == 0) a.coef[p] = make_double2(re, im);
+            }
+        if (!ks_grid_sync(a.bar, (++k) * ncta, abort)) return;
+        // (4) out = y - sum_p c_p B_p in place of y; ||out||^2 and <out, y> partials
+        for (int p = tid; p < q; p += KM_THREADS) cs[p] = from_d<C>(__ldcg(a.coef + p));
+        __syncthreads();
+        double v0 = 0, v1 = 0, v2 = 0;
+        for (int sl = gw; sl < a.nslices; sl += nw) {
+            const int row = sl * 32 + lane;
+            if (row >= n) continue;
+            const C yv = a.y[row];
+            C w = yv;
+            for (int p = 0; p < q; ++p) {
+                const C *B = p < kk ? a.W + (size_t)p * n : a.V + (size_t)(p - kk) * n;
+                cfms(w, cs[p], B[row]);
+            }
+            w = canon(w);
+            a.y[row] = w;
+            C ln = czero<C>(), lc = czero<C>();
+            cdotacc(ln, w, w);
+            cdotacc(lc, w, yv);
+            v0 += (double)canon(ln).x;
+            v1 += (double)canon(lc).x;
+            v2 += (double)canon(lc).y;
+        }
+        v0 = warp_sum(v0);
+        v1 = warp_sum(v1);
+        v2 = warp_sum(v2);
+        if (lane == 0) { red[warp][0] = v0; red[warp][1] = v1; red[warp][2] = v2; }
+        __syncthreads();
+        if (tid < 3) {
+            double t = 0;
+            for (int w = 0; w < KM_WARPS; ++w) t += red[w][tid];
+            npart[(size_t)c * 3 + tid] = t;
+        }
+        if (!ks_grid_sync(a.bar, (++k) * ncta, abort)) return;
+        // (5) the norms summed by every CTA in the same order; CTA 0 of the job runs the finish
+        if (tid < 3) {
+            double t = 0;
+            for (int g = 0; g < ncta; ++g) t += __ldcg(npart + (size_t)g * 3 + tid);
+            s_norm[tid] = t;
+        }
+        __syncthreads();
+        const double n2 = s_norm[0], nrm = sqrt(n2);
+        const bool broken = nrm < a.tol;
+        if (c == 0) {
+            for (int p = tid; p < q; p += KM_THREADS) a.H[(size_t)(kk + j - 1) * (a.m + 1) + p] = __ldcg(a.coef + p);
+            if (tid == 0) {
+                FinishArgs f{};
+                f.mode = FIN_KRYLOV; f.col = kk + j - 1; f.nco = 0; f.ldH = a.m + 1; f.m = a.m; f.kk = kk;
+                f.compat_eye = a.compat_eye; f.tol = a.tol; f.H = a.H; f.strideH = 0;
+                f.coef = a.coef; f.strideC = 0;
+                run_finish(f, 0, *a.state, n2, s_norm[1], s_norm[2]);
+            }
+        }
+        // (6) v_j = out / ||out|| on the warp's rows; a breakdown ends the loop with v_j and the
+        // rest of the basis zero (gDMR.cu:2256-2289), which the cycle-end projection reads
+        const R al = broken ? R(0.f) : R(1.0 / nrm);
+        for (int sl = gw; sl < a.nslices; sl += nw) {
+            const int row = sl * 32 + lane;
+            if (row >= n) continue;
+            C v = a.y[row];
+            v.x = v.x * al;
+            v.y = v.y * al;
+            if (broken) v = czero<C>();
+            a.V[(size_t)j * n + row] = v;
+            if (broken)
+                for (int jj = j + 1; jj <= a.m - kk; ++jj) a.V[(size_t)jj * n + row] = czero<C>();
+        }
+        if (broken) return;
+        if (!ks_grid_sync(a.bar, (++k) * ncta, abort)) return;
     }
 }
 
@@ -3265,17 +3400,8 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
 }
 
 // r = b - A x in FP64 with ||r||^2 reduced; last CTA sets true_res and alpha.
-// GRID: the matrix's structured-grid form (coefficient planes, real planes skipping their zero
-// imaginary parts), terms in the order the SELL loop takes them, so the same values.
-struct GridForm {
-    const double2 *coef;
-    int nx, ny, nz;
-    unsigned greal;
-};
-template <bool GRID>
 __global__ void __launch_bounds__(NT) k_residual64(int n, const int *__restrict__ slice_ptr, const int *__restrict__ cols,
-                                                   const double2 *__restrict__ vals, GridForm gf,
-                                                   const double2 *__restrict__ b0,
+                                                   const double2 *__restrict__ vals, const double2 *__restrict__ b0,
                                                    size_t strideB, const double2 *__restrict__ x0, size_t strideX,
                                                    double2 *__restrict__ r0, size_t strideR, const int *__restrict__ act,
                                                    double2 *__restrict__ partials, unsigned *tickets, SysState *state) {
@@ -3287,28 +3413,11 @@ __global__ void __launch_bounds__(NT) k_residual64(int n, const int *__restrict_
     double n2 = 0;
     for (int row = blockIdx.y * NT + tid; row < n; row += G * NT) {
         double2 acc = b[row];
-        if constexpr (GRID) {
-            const int nx = gf.nx, ny = gf.ny, nz = gf.nz;
-            const long plane = (long)nx * ny;
-            const int ix = row % nx, iy = (row / nx) % ny, iz = (int)(row / plane);
-            const bool d3 = nz > 1;
-            const int pb = d3 ? 1 : 0;
-            const unsigned gr = gf.greal;
-            const double2 *cf = gf.coef + (d3 ? n : 0);
-            if (d3 && iz > 0) cfms_r(acc, gf.coef[row], x[row - plane], gr & 1u);
-            if (iy > 0) cfms_r(acc, cf[row], x[row - nx], (gr >> pb) & 1u);
-            if (ix > 0) cfms_r(acc, cf[(long)n + row], x[row - 1], (gr >> (pb + 1)) & 1u);
-            cfms_r(acc, cf[2L * n + row], x[row], (gr >> (pb + 2)) & 1u);
-            if (ix + 1 < nx) cfms_r(acc, cf[3L * n + row], x[row + 1], (gr >> (pb + 3)) & 1u);
-            if (iy + 1 < ny) cfms_r(acc, cf[4L * n + row], x[row + nx], (gr >> (pb + 4)) & 1u);
-            if (d3 && iz + 1 < nz) cfms_r(acc, cf[5L * n + row], x[row + plane], (gr >> 6) & 1u);
-        } else {
-            const int slice = row >> 5, lane = row & 31;
-            const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
-            for (int c = 0; c < width; ++c) {
-                const int e = beg + c * 32 + lane;
-                cfms(acc, vals[e], x[cols[e]]);
-            }
+        const int slice = row >> 5, lane = row & 31;
+        const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
+        for (int c = 0; c < width; ++c) {
+            const int e = beg + c * 32 + lane;
+            cfms(acc, vals[e], x[cols[e]]);
         }
         r[row] = acc;
         n2 += acc.x * acc.x + acc.y * acc.y;
@@ -3757,7 +3866,8 @@ std::string tune_report() {
 //   complex64:  0 (8,2,1)  1 (8,2,2)  2 (16,2,2)  3 (8,4,2)  4 (2,2,1)  5 (1,4,1)  6 grp(4,4)  7 grp(4,2)
 //               projection only: 8 split-vector(4); 9 batched shared-W (CUDA cores);
 //               10 batched shared-W on the tensor cores (tcgen05, 3xTF32);
-//               update only: 8 batched shared-W (CUDA cores), 9 shared part on the tensor cores
+//               update only: 8 batched shared-W (CUDA cores), 9 shared part on the tensor cores,
+//               10 the whole update in one kernel with the shared part on the tensor cores
 //   complex128 and double-float: 0 (4,2,1)  1 (8,2,1)  2 (4,4,1)  3 (1,4,1)  4 (2,2,1)  5 grp(4,2)
 //               projection: 6 split-vector(4), 7 batched shared-W (complex128), 8 (4,2,1) prefetching
 //               update: 6 batched shared-W (complex128), 7 (4,2,1) prefetching
@@ -4031,6 +4141,17 @@ int update_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const t
     auto fits = [&](int ept) { return (size_t)nsys * 3 * (((size_t)n + NT * ept - 1) / (NT * ept)) <= cap; };
     constexpr int VW = sizeof(R) == 4 ? 8 : 6;   // batched shared-W variant
     if constexpr (sizeof(R) == 4) {
+        // 10: the whole update in one kernel, the shared part W c on the tensor cores and
+        // subtracted from TMEM by the epilogue that streams w_s and V_s
+        if (v == 10) {
+            if (qa > 0 && wupdate_tc_ok(n, qa, qb, nsys) && (qb == 0 || segB) &&
+                (size_t)nsys * 3 * wupdate_tc_grid(n) <= cap) {
+                launch_wupdate_tc(n, qa, segA, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef, strideC,
+                                  (double *)partials, tickets, state, fin, skip_broken, st);
+                return 1;
+            }
+            v = 0;
+        }
         // 9: the shared part W c on the tensor cores into the free slot segB_s[qb] (the next
         // Krylov vector's), then the per-system update with that slot as one more basis vector
         // of coefficient 1 (written by the apply kernel at coef_s[qa + qb])
@@ -4163,7 +4284,7 @@ void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename 
     int v = 0;
     if (forced_variant(1) >= 0) v = forced_variant(1);
     else if (representative(nsys, qa, qb) && !profile_enabled())
-        v = tuned_variant(prec_key<R>(), 1, n, nsys, qa, sizeof(R) == 4 ? 10 : 13, st, run);
+        v = tuned_variant(prec_key<R>(), 1, n, nsys, qa, sizeof(R) == 4 ? 11 : 13, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)
@@ -4198,12 +4319,29 @@ template <class R>
 void launch_zupdate(int n, int kk, int m, int k, const typename CT<R>::t *Z, const typename CT<R>::t *V,
                     size_t strideV, const int *lead, const double2 *vs, typename CT<R>::t *Znew, double2 *partials,
                     unsigned *ticket, double *znorm2, cudaStream_t st) {
-    Launch L_(KC_ZUPDATE, (double)sizeof(typename CT<R>::t) * n * ((double)m + k), st, (k + (sizeof(R) == 4 ? 16 : 8) - 1) / (sizeof(R) == 4 ? 16 : 8));
     using C = typename CT<R>::t;
-    constexpr int KB = sizeof(R) == 4 ? 16 : 8;
     int chunks = (n + NT - 1) / NT;
     int G = num_sms() * 4;
     if (G > chunks) G = chunks;
+    // complex64: every output in one pass over [Z V] (blocks of 24 or 32 outputs in registers),
+    // so the basis is read once; the double-float forms keep 8 outputs a pass (registers)
+    if constexpr (sizeof(R) == 4) {
+        if (k <= 32) {
+            Launch L_(KC_ZUPDATE, (double)sizeof(C) * n * ((double)m + k), st, 1);
+            auto run = [&](auto kb) {
+                constexpr int KB = decltype(kb)::value;
+                const size_t smem = (size_t)m * KB * sizeof(typename ZW<C>::t);
+                k_zupdate<R, KB><<<G, NT, smem, st>>>(n, kk, m, k, 0, Z, V, strideV, lead, vs, Znew, partials, ticket,
+                                                      znorm2);
+            };
+            if (k <= 16) run(std::integral_constant<int, 16>{});
+            else if (k <= 24) run(std::integral_constant<int, 24>{});
+            else run(std::integral_constant<int, 32>{});
+            return;
+        }
+    }
+    constexpr int KB = sizeof(R) == 4 ? 16 : 8;
+    Launch L_(KC_ZUPDATE, (double)sizeof(C) * n * ((double)m + k), st, (k + KB - 1) / KB);
     for (int t0 = 0; t0 < k; t0 += KB) {
         size_t smem = (size_t)m * KB * sizeof(typename ZW<C>::t);
         k_zupdate<R, KB><<<G, NT, smem, st>>>(n, kk, m, k, t0, Z, V, strideV, lead, vs, Znew, partials, ticket,
@@ -4244,6 +4382,51 @@ void launch_svd_smallest(int m, int k, const double2 *H, size_t strideH, const i
 
 // Algorithmic bytes of the fused Krylov loop: per step the operator product, the projection
 // against kk + j vectors (and y), the update (the same vectors, y, w) and the scaling.
+double krylov_small_bytes(const SellMatrix &A, size_t vs, int kk, int m);
+
+int krylov_multi_resident() {
+    static std::mutex mu;
+    static std::vector<int> per_dev;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    if ((int)per_dev.size() <= dev) per_dev.resize(dev + 1, -1);
+    if (per_dev[dev] < 0) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_krylov_multi<float>, KM_THREADS, 0) != cudaSuccess)
+            per_sm = 0;
+        int per_sm2 = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_krylov_multi<double>, KM_THREADS, 0) !=
+            cudaSuccess)
+            per_sm2 = 0;
+        int per_sm3 = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm3, k_krylov_multi<dfr>, KM_THREADS, 0) != cudaSuccess)
+            per_sm3 = 0;
+        per_dev[dev] = std::min(per_sm, std::min(per_sm2, per_sm3)) * num_sms();
+    }
+    return per_dev[dev];
+}
+
+template <class R>
+int launch_krylov_multi(const KrylovJob<R> *jobs, const int *cta_job, int ctas, int *abort, double algorithmic_bytes,
+                        cudaStream_t st) {
+    if (ctas < 1) return 0;
+    Launch L_(KC_UPDATE, algorithmic_bytes, st, 1);
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)ctas);
+    cfg.blockDim = dim3(KM_THREADS);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_krylov_multi<R>, jobs, cta_job, abort) == cudaSuccess ? 1 : -1;
+}
+
+double krylov_loop_bytes(const SellMatrix &A, size_t vs, int kk, int m) { return krylov_small_bytes(A, vs, kk, m); }
+
 double krylov_small_bytes(const SellMatrix &A, size_t vs, int kk, int m) {
     double b = 0;
     for (int j = 1; j <= m - kk; ++j)
@@ -4370,14 +4553,10 @@ void launch_residual64(const SellMatrix &A, const double2 *b, size_t strideB, co
                        SysState *state, cudaStream_t st) {
     if (nsys <= 0) return;
     Launch L_(KC_RESID64, spmm_bytes(A, sizeof(double2), nsys) + (double)sizeof(double2) * A.n * nsys, st, 1);
-    const dim3 grid = grid2(nsys, capped_grid(A.n, nsys, 8));
-    const GridForm gf{(const double2 *)A.grid, A.gx, A.gy, A.gz, A.greal};
-    if (A.grid && grid_operator())
-        k_residual64<true><<<grid, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const double2 *)A.vals, gf, b, strideB, x,
-                                                strideX, r, strideR, act, partials, tickets, state);
-    else
-        k_residual64<false><<<grid, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const double2 *)A.vals, gf, b, strideB, x,
-                                                 strideX, r, strideR, act, partials, tickets, state);
+    k_residual64<<<grid2(nsys, capped_grid(A.n, nsys, 8)), NT, 0, st>>>(A.n, A.slice_ptr, A.cols,
+                                                                        (const double2 *)A.vals, b, strideB, x,
+                                                                        strideX, r, strideR, act, partials, tickets,
+                                                                        state);
 }
 
 template <class R>
@@ -4454,6 +4633,7 @@ void launch_broadcast_hdef(int m, int kk, const double2 *Hd, double2 *H, size_t 
                                         const SysState *, cudaStream_t);                                               \
     template void launch_norm<R>(int, const CT<R>::t *, size_t, const int *, int, double2 *, unsigned *, SysState *,   \
                                  int, cudaStream_t);                                                                   \
+    template int launch_krylov_multi<R>(const KrylovJob<R> *, const int *, int, int *, double, cudaStream_t);         \
     template bool launch_krylov_small<R>(int, int, int, const SellMatrix &, const CT<R>::t *, CT<R>::t *, size_t,      \
                                          const int *, SysState *, double2 *, size_t, double2 *, size_t, double *, int, \
                                          unsigned *, double, bool, cudaStream_t);

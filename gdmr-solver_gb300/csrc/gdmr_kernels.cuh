@@ -118,6 +118,54 @@ struct FinishArgs {
     size_t strideC;
 };
 
+#ifdef __CUDACC__
+// The finishing step of a reduction kernel's last CTA: stores the reduced norm and cross term,
+// then, per mode, the Hessenberg column with the breakdown test and the reference's identity
+// tail (gDMR.cu:2256-2289), the deflation loop's diagonal, or the cycle-end residual factor.
+__device__ inline void run_finish(const FinishArgs &f, int s, SysState &st, double n2, double cre, double cim) {
+    st.nrm2 = n2;
+    st.cross_re = cre;
+    st.cross_im = cim;
+    const double nrm = sqrt(n2);
+    if (!isfinite(nrm)) st.bad = 1;
+    switch (f.mode) {
+    case FIN_KRYLOV: {
+        double2 *H = f.H + (size_t)s * f.strideH;
+        const double2 *c = f.coef + (size_t)s * f.strideC;
+        for (int p = 0; p < f.nco; ++p) H[(size_t)f.col * f.ldH + p] = c[p];
+        const int j = f.col - f.kk + 1;
+        if (nrm < f.tol) {   // absolute breakdown threshold, gDMR.cu:2256
+            st.broken = j;
+            st.alpha = 0.0;
+            for (int cc = f.compat_eye ? j : f.kk + j; cc < f.m; ++cc) H[(size_t)cc * f.ldH + cc] = make_double2(1.0, 0.0);
+        } else {
+            st.alpha = 1.0 / nrm;
+            H[(size_t)f.col * f.ldH + f.col + 1] = make_double2(cre / nrm, cim / nrm);
+        }
+        break;
+    }
+    case FIN_DEFLATION: {
+        double2 *H = f.H;
+        const double2 *c = f.coef;
+        for (int p = 0; p < f.nco; ++p) H[(size_t)f.col * f.ldH + p] = c[p];
+        st.alpha = 1.0 / nrm;
+        H[(size_t)f.col * f.ldH + f.col] = make_double2(cre / nrm, cim / nrm);
+        break;
+    }
+    case FIN_UNIT:
+        st.alpha = 1.0 / nrm;
+        break;
+    case FIN_RESIDUAL:
+        st.rho = nrm;
+        st.alpha = 1.0 / nrm;
+        st.rho_abs = st.rho_abs * nrm;
+        break;
+    default:
+        break;
+    }
+}
+#endif
+
 // ----------------------------------------------------------------- instrumentation
 // Every launcher counts its kernel launches.  With profiling on, it also brackets
 // each launch with CUDA events on its stream and books the launch's algorithmic
@@ -189,6 +237,17 @@ int launch_wproj_tc(int n, int kk, const float2 *W, const float2 *Y, size_t stri
 bool wapply_tc_ok(int n, int kk, int nsys);
 int launch_wapply_tc(int n, int kk, const float2 *W, double2 *coef, size_t strideC, const int *act, int nsys,
                      float2 *P, size_t strideP, int unit_idx, cudaStream_t st);
+// The batched update with its shared part on the tensor cores in one kernel (complex64;
+// gdmr_tc.cu): out_s = w_s - V_s c_s[kk..kk+qb) - W c_s[0..kk) for the active systems, with
+// ||out_s||^2 and <out_s, w_s> reduced through partials (wupdate_tc_grid(n) x 3 x nsys doubles)
+// and tickets (nsys counters) and `fin` run per system, as launch_update does.  wupdate_tc_ok:
+// kk <= 32, qb <= 32, 8 <= nsys <= 64.
+bool wupdate_tc_ok(int n, int kk, int qb, int nsys);
+int wupdate_tc_grid(int n);
+int launch_wupdate_tc(int n, int kk, const float2 *W, const float2 *V, size_t strideV, int qb, const float2 *w,
+                      size_t strideW, float2 *out, size_t strideO, const int *act, int nsys, const double2 *coef,
+                      size_t strideC, double *partials, unsigned *tickets, SysState *state, FinishArgs fin,
+                      bool skip_broken, cudaStream_t st);
 // mbarrier waits of the tensor-core kernels that ran out of time (0 in a healthy process).
 unsigned wproj_tc_timeouts();
 // Bounded mbarrier waits of the bulk-copy Gram-Schmidt pipelines and grid barriers of the fused
@@ -310,6 +369,37 @@ bool launch_krylov_small(int n, int kk, int m, const SellMatrix &A, const typena
                          typename CT<R>::t *V, size_t strideV, const int *act, SysState *state, double2 *H,
                          size_t strideH, double2 *coef, size_t strideC, double *partials, int qmax, unsigned *bar,
                          double tol, bool compat_eye, cudaStream_t st);
+
+// One system's Krylov loop in the many-system persistent launch (launch_krylov_multi): its
+// operator (SELL-32), its operator's shared deflation vectors, its basis with v_0 normalised,
+// a scratch vector, its state, Hessenberg and coefficients, and its share of the launch's CTAs
+// (cta0 .. cta0 + ncta - 1) with partial sums and a barrier counter of its own.
+template <class R> struct KrylovJob {
+    using C = typename CT<R>::t;
+    int n, nslices, kk, m, compat_eye, qmax, cta0, ncta;
+    double tol;
+    const int *slice_ptr, *cols;
+    const C *vals;          // the job's operator
+    const C *W;             // its operator's shared deflation vectors (kk x n)
+    C *V;                   // the system's basis ((m + 1) x n, v_0 normalised)
+    C *y;                   // the system's scratch vector (n)
+    SysState *state;
+    double2 *H;             // the system's Hessenberg (ld m + 1)
+    double2 *coef;          // the system's projection coefficients
+    double *part;           // ncta x qmax x 2 projection partials, then ncta x 3 norm partials
+    unsigned *bar;          // the job's barrier counter (zeroed before the launch)
+};
+// CTAs of the many-system launch that fit on the current device at once (the launch is
+// cooperative: every CTA resident).
+int krylov_multi_resident();
+// The Krylov loops of njobs systems (jobs and cta_job, the job of each CTA, in device memory;
+// every job's barrier counter and *abort zeroed before it on `st`) as one cooperative launch of
+// ctas CTAs.  algorithmic_bytes: booked to the update class when profiling.
+template <class R>
+int launch_krylov_multi(const KrylovJob<R> *jobs, const int *cta_job, int ctas, int *abort, double algorithmic_bytes,
+                        cudaStream_t st);
+// Algorithmic bytes of one system's Krylov loop (operator products, projections, updates).
+double krylov_loop_bytes(const SellMatrix &A, size_t vs, int kk, int m);
 
 // y_s = b_s - A x_s in FP64 with ||y_s||^2 reduced into state[s].nrm2 (refined form).
 void launch_residual64(const SellMatrix &A, const double2 *b, size_t strideB, const double2 *x, size_t strideX,

@@ -118,6 +118,12 @@ __device__ __forceinline__ void st4(float *p, float a, float b, float c, float d
     *reinterpret_cast<float4 *>(p) = make_float4(a, b, c, d);
 }
 
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 // Double-float accumulate: (hi, lo) += v with the rounding error of the add kept in lo.
 __device__ __forceinline__ void df_add(float &hi, float &lo, float v) {
     const float s = hi + v;
@@ -430,10 +436,11 @@ __global__ void __launch_bounds__(256) k_wproj_tc_reduce(int kk, int nsys, int G
 //     re row: (cr_p, -ci_p), im row: (ci_p, cr_p), so D[i][(s,re)] = Re(w_i c_s), D[i][(s,im)] = Im;
 //   per K step: A_big x B (N = 4 NSp) and A_small x B_big (N = 2 NSp) into one TMEM tile, and
 //   P = D[:, big block] + D[:, small block].
-// Warp roles: warps 0-3 epilogue (TMEM lanes 0-127 -> P stores), warps 4-11 producers (W tile
-// -> split, swizzled A operands), warp 12 issues the MMAs.  A and the TMEM tile are
-// double-buffered; mbarriers only.
-constexpr int WA_EPI = 4, WA_PROD = 8;
+// Warp roles: warps 0-7 epilogue (warp w reads TMEM lane quarter w % 4, the tile's elements
+// 32 (w % 4) .. + 31, and stores P for half w / 4 of the systems; four warps of stores ran the
+// kernel at about half the HBM rate), warps 8-15 producers (W tile -> split, swizzled A
+// operands), warp 16 issues the MMAs.  A and the TMEM tile are double-buffered; mbarriers only.
+constexpr int WA_EPI = 8, WA_PROD = 8;
 constexpr int WA_MMA_WARP = WA_EPI + WA_PROD;
 constexpr int WA_THREADS = (WA_MMA_WARP + 1) * 32;
 constexpr int WA_TILE = 128;                      // elements per tile (MMA M)
@@ -579,8 +586,10 @@ __global__ void __launch_bounds__(WA_THREADS, 1)
                          : "memory");
         }
     } else {
-        // ---- epilogue: warp w reads TMEM lanes 32w..32w+31 = elements of the tile, sums the big
-        // and small blocks and stores P_s for every system (lanes = consecutive elements)
+        // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 = elements of the tile, sums
+        // the big and small blocks and stores P_s (lanes = consecutive elements) for the systems
+        // of every other group of 16 columns (8 systems), starting at group w / 4
+        const int quarter = warp & 3, half = warp >> 2;
         for (int i = 0; i < my_tiles; ++i) {
             const int buf = i & 1;
             int ok = 1;
@@ -590,9 +599,9 @@ __global__ void __launch_bounds__(WA_THREADS, 1)
             }
             if (!__shfl_sync(0xffffffffu, ok, 0)) break;
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const long g = ((long)blockIdx.x + (long)i * G) * WA_TILE + warp * 32 + lane;
-            const uint32_t row = taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)(buf * 256);
-            for (int c0 = 0; c0 < 2 * nsp; c0 += 16) {
+            const long g = ((long)blockIdx.x + (long)i * G) * WA_TILE + quarter * 32 + lane;
+            const uint32_t row = taddr + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * 256);
+            for (int c0 = 16 * half; c0 < 2 * nsp; c0 += 32) {
                 uint32_t vb[16], vs[16];
                 tmem_ld16(row + (uint32_t)c0, vb);
                 tmem_ld16(row + (uint32_t)(2 * nsp + c0), vs);
@@ -617,6 +626,285 @@ __global__ void __launch_bounds__(WA_THREADS, 1)
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "n"(TC_TMEM_COLS));
+}
+
+// ================================================================ fused shared-basis update
+// The whole batched Gram-Schmidt update of a Krylov step in one kernel:
+//   out_s = w_s - V_s c_s^V - W c_s^W,   ||out_s||^2 and <out_s, w_s> reduced, then the update's
+//   finish (Hessenberg column, breakdown test and identity tail, normalisation factor) per system,
+// the classical Gram-Schmidt step of arnoldiDMR against [W V] with the deflator (gDMR.cu:1710-1787,
+// 2115-2310) for a batch of systems that share W.  The shared part W c_s^W of every system comes
+// from the tensor cores with the operands and MMAs of k_wapply_tc, and the epilogue warps take it
+// straight from TMEM while they stream w_s and V_s, so it never goes through memory (the split
+// form writes P_s = W c_s^W and the per-system update reads it back: two extra vectors a system).
+//   * warps 0-15 epilogue: warp w reads TMEM lane quarter w % 4 (the tile's elements 32 (w % 4) ..
+//     + 31, one a lane) and handles the systems 16 (w / 4) .. + 15; per element and system it
+//     subtracts the own basis in the order of the per-system update kernel, then P, stores out and
+//     accumulates the two reductions (warp sums per tile, FP64 slots per lane quarter and system);
+//   * warps 16-23 produce the big/small TF32 A operands of each 128-element W tile;
+//   * warp 24 issues the MMAs into one of two TMEM tiles (256 columns each).
+// After the last tile every CTA writes its partial sums per system and arrives on the system's
+// ticket; the last CTA of a system sums the partials over the CTAs in order (deterministic) and
+// runs the finish.  Systems flagged broken are skipped when skip_broken is set, as in k_update.
+constexpr int WU_EPI = 16, WU_PROD = 8;
+constexpr int WU_MMA_WARP = WU_EPI + WU_PROD;
+constexpr int WU_THREADS = (WU_MMA_WARP + 1) * 32;
+constexpr int WU_QB = 32;                                      // own basis vectors at most
+constexpr int WU_ITEMS = TC_KMAX * WA_TILE / (WU_PROD * 32);   // W values per producer per tile
+
+__device__ __forceinline__ void tmem_ld8(uint32_t addr, uint32_t (&v)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+                 : "r"(addr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void cfms2(float2 &acc, float2 c, float2 v) {   // acc -= c * v (k_update's order)
+    acc.x = fmaf(-c.x, v.x, acc.x);
+    acc.x = fmaf(c.y, v.y, acc.x);
+    acc.y = fmaf(-c.x, v.y, acc.y);
+    acc.y = fmaf(-c.y, v.x, acc.y);
+}
+
+__global__ void __launch_bounds__(WU_THREADS, 1)
+    k_wupdate_tc(int n, int kk, const float2 *__restrict__ W, const float2 *__restrict__ V0, size_t strideV, int qb,
+                 const float2 *__restrict__ w0, size_t strideW, float2 *__restrict__ out0, size_t strideO,
+                 const int *__restrict__ act, int nsys, int nsp, const double2 *__restrict__ coef0, size_t strideC,
+                 double *__restrict__ partials, unsigned *tickets, SysState *state, FinishArgs fin, int skip_broken) {
+    extern __shared__ __align__(1024) unsigned char wu_sm[];
+    unsigned char *base = wu_sm + ((1024u - (smem_u32(wu_sm) & 1023u)) & 1023u);
+    const int brows = 4 * nsp;
+    float *A = reinterpret_cast<float *>(base);                        // [buf][big|small]
+    float *B = reinterpret_cast<float *>(base + 4 * WA_AOP);           // 4 nsp rows x 2 atom columns
+    float2 *cv = reinterpret_cast<float2 *>(base + 4 * WA_AOP + (size_t)brows * 2 * TC_ROW);   // [sys][WU_QB]
+    double *sacc = reinterpret_cast<double *>(cv + (size_t)TC_NMAX * WU_QB);                   // [quarter][sys][3]
+    __shared__ __align__(8) uint64_t full[2], mdone[2], tempty[2], done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_act[TC_NMAX], s_skip[TC_NMAX];
+    __shared__ volatile int s_abort;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, G = gridDim.x;
+    const long ntiles = ((long)n + WA_TILE - 1) / WA_TILE;
+    const int my_tiles = (int)((ntiles - blockIdx.x + G - 1) / G);
+
+    for (int e = tid; e < (4 * WA_AOP + brows * 2 * TC_ROW) / 16; e += WU_THREADS)
+        reinterpret_cast<float4 *>(base)[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int e = tid; e < 4 * TC_NMAX * 3; e += WU_THREADS) sacc[e] = 0.0;
+    if (tid < nsys) {
+        const int sy = act[tid];
+        s_act[tid] = sy;
+        s_skip[tid] = skip_broken && state[sy].broken;
+    }
+    if (tid == 0) {
+        s_abort = 0;
+        for (int b = 0; b < 2; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&full[b])), "r"(WU_PROD));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mdone[b])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&tempty[b])), "r"(WU_EPI));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&done)));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
+                     "n"(TC_TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    __syncthreads();
+    // B from the shared coefficients (as k_wapply_tc), cv from the own coefficients
+    for (int e = tid; e < nsys * kk; e += WU_THREADS) {
+        const int sl = e / kk, p = e % kk;
+        const double2 c = coef0[(size_t)s_act[sl] * strideC + p];
+        const float cr = (float)c.x, ci = (float)c.y;
+        const float vals[2][2] = {{cr, -ci}, {ci, cr}};
+#pragma unroll
+        for (int o = 0; o < 2; ++o)
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const float v = vals[o][q], big = tf32_big(v);
+                B[swz(2 * sl + o, 2 * p + q, brows)] = big;
+                B[swz(2 * nsp + 2 * sl + o, 2 * p + q, brows)] = v - big;
+            }
+    }
+    for (int e = tid; e < nsys * qb; e += WU_THREADS) {
+        const int sl = e / qb, p = e % qb;
+        const double2 c = coef0[(size_t)s_act[sl] * strideC + kk + p];
+        cv[sl * WU_QB + p] = make_float2((float)c.x, (float)c.y);
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t taddr = tmem_base;
+
+    if (warp >= WU_EPI && warp < WU_MMA_WARP) {
+        // ---- producers (as k_wapply_tc, without its register prefetch of the next tile: 800
+        // threads leave 80 registers a thread, and a tile's W loads take a small part of the
+        // epilogue's time for the same tile)
+        const int ptid = tid - WU_EPI * 32;
+        float2 cur[WU_ITEMS];
+        const long t0 = blockIdx.x;
+        for (int i = 0; i < my_tiles; ++i) {
+            const int buf = i & 1;
+#pragma unroll
+            for (int u = 0; u < WU_ITEMS; ++u) {
+                const int e = ptid + u * WU_PROD * 32, p = e / WA_TILE, r = e % WA_TILE;
+                const long g = (t0 + (long)i * G) * WA_TILE + r;
+                cur[u] = (p < kk && g < n) ? W[(size_t)p * n + g] : make_float2(0.f, 0.f);
+            }
+            if (i >= 2) {   // the MMAs of tile i - 2 read this A buffer
+                int ok = 1;
+                if (lane == 0) {
+                    ok = mbar_wait(smem_u32(&mdone[buf]), ((i >> 1) - 1) & 1, &s_abort);
+                    if (!ok && !s_abort) { atomicAdd(&g_tc_timeouts, 1u); s_abort = 1; }
+                }
+                if (!__shfl_sync(0xffffffffu, ok, 0)) break;
+            }
+            float *Ab = A + (size_t)buf * 2 * (WA_AOP / 4), *As = Ab + WA_AOP / 4;
+#pragma unroll
+            for (int u = 0; u < WU_ITEMS; ++u) {
+                const int e = ptid + u * WU_PROD * 32, p = e / WA_TILE, r = e % WA_TILE;
+                if (p >= kk) continue;
+                const float br = tf32_big(cur[u].x), bi = tf32_big(cur[u].y);
+                const int o = swz(r, 2 * p, WA_TILE);
+                *reinterpret_cast<float2 *>(Ab + o) = make_float2(br, bi);
+                *reinterpret_cast<float2 *>(As + o) = make_float2(cur[u].x - br, cur[u].y - bi);
+            }
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&full[buf]));
+        }
+    } else if (warp == WU_MMA_WARP) {
+        if (lane == 0) {
+            // ---- MMA issuer (as k_wapply_tc)
+            const int ksteps = (2 * kk + 7) / 8;
+            const uint32_t id_all = idesc_tf32(TC_M, 4 * nsp), id_big = idesc_tf32(TC_M, 2 * nsp);
+            const uint64_t a0 = sdesc(smem_u32(A)), b0 = sdesc(smem_u32(B));
+            const uint64_t abuf = (uint64_t)(2 * WA_AOP) >> 4, asmall = (uint64_t)WA_AOP >> 4;
+            const uint64_t acol = (uint64_t)(WA_TILE * TC_ROW) >> 4, bcol = (uint64_t)(brows * TC_ROW) >> 4;
+            for (int i = 0; i < my_tiles; ++i) {
+                const int buf = i & 1;
+                if (!mbar_wait(smem_u32(&full[buf]), (i >> 1) & 1, &s_abort) ||
+                    (i >= 2 && !mbar_wait(smem_u32(&tempty[buf]), ((i >> 1) - 1) & 1, &s_abort))) {
+                    if (!s_abort) { atomicAdd(&g_tc_timeouts, 1u); s_abort = 1; }
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t d = taddr + (uint32_t)(buf * 256);
+                for (int ks = 0; ks < ksteps; ++ks) {
+                    const uint64_t koff = (uint64_t)((ks & 3) * 32) >> 4;
+                    const uint64_t ab = a0 + buf * abuf + (ks >> 2) * acol + koff;
+                    const uint64_t bd = b0 + (ks >> 2) * bcol + koff;
+                    asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+                                 "l"(ab), "l"(bd), "r"(id_all), "r"(ks > 0 ? 1u : 0u));
+                    asm volatile("tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, 1;\n" ::"r"(d),
+                                 "l"(ab + asmall), "l"(bd), "r"(id_big));
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                                 smem_u32(&mdone[buf]))
+                             : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             smem_u32(&done))
+                         : "memory");
+        }
+    } else {
+        // ---- epilogue: the update proper
+        const int quarter = warp & 3, group = warp >> 2;
+        const int s_lo = group * 16, s_hi = min(nsys, s_lo + 16);
+        double *myacc = sacc + (size_t)quarter * TC_NMAX * 3;
+        for (int i = 0; i < my_tiles; ++i) {
+            const int buf = i & 1;
+            int ok = 1;
+            if (lane == 0) {
+                ok = mbar_wait(smem_u32(&mdone[buf]), (i >> 1) & 1, &s_abort);
+                if (!ok && !s_abort) { atomicAdd(&g_tc_timeouts, 1u); s_abort = 1; }
+            }
+            if (!__shfl_sync(0xffffffffu, ok, 0)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const long e = ((long)blockIdx.x + (long)i * G) * WA_TILE + quarter * 32 + lane;
+            const bool in = e < n;
+            const uint32_t row = taddr + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * 256);
+            for (int s0 = s_lo; s0 < s_hi; s0 += 4) {
+                uint32_t vb[8], vs[8];
+                tmem_ld8(row + (uint32_t)(2 * s0), vb);
+                tmem_ld8(row + (uint32_t)(2 * nsp + 2 * s0), vs);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int sl = s0 + u;
+                    if (sl >= s_hi || s_skip[sl]) continue;   // warp-uniform
+                    const int sy = s_act[sl];
+                    const float2 P = make_float2(__uint_as_float(vb[2 * u]) + __uint_as_float(vs[2 * u]),
+                                                 __uint_as_float(vb[2 * u + 1]) + __uint_as_float(vs[2 * u + 1]));
+                    float2 org = make_float2(0.f, 0.f), acc = org;
+                    if (in) {
+                        org = w0[(size_t)sy * strideW + e];
+                        acc = org;
+                        const float2 *vp = V0 + (size_t)sy * strideV + e;
+                        const float2 *cs = cv + sl * WU_QB;
+                        int p = 0;
+                        for (; p + 8 <= qb; p += 8) {   // eight loads in flight before their use
+                            float2 v[8];
+#pragma unroll
+                            for (int q = 0; q < 8; ++q) v[q] = vp[(size_t)(p + q) * n];
+#pragma unroll
+                            for (int q = 0; q < 8; ++q) cfms2(acc, cs[p + q], v[q]);
+                        }
+                        for (; p < qb; ++p) cfms2(acc, cs[p], vp[(size_t)p * n]);
+                        cfms2(acc, make_float2(1.f, 0.f), P);
+                        out0[(size_t)sy * strideO + e] = acc;
+                    }
+                    // ||out||^2 and <out, w> = sum conj(out) w, summed over the warp, into the
+                    // lane quarter's FP64 slot of the system
+                    float ln = acc.x * acc.x + acc.y * acc.y;
+                    float cr = acc.x * org.x + acc.y * org.y, ci = acc.x * org.y - acc.y * org.x;
+                    ln = warp_sum_f(ln);
+                    cr = warp_sum_f(cr);
+                    ci = warp_sum_f(ci);
+                    if (lane == 0) {
+                        myacc[sl * 3] += (double)ln;
+                        myacc[sl * 3 + 1] += (double)cr;
+                        myacc[sl * 3 + 2] += (double)ci;
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&tempty[buf]));
+        }
+    }
+    __syncthreads();
+    if (!mbar_wait(smem_u32(&done), 0, nullptr, TC_WAIT_CYCLES) && tid == 0) {
+        atomicAdd(&g_tc_timeouts, 1u);
+        s_abort = 1;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(taddr), "n"(TC_TMEM_COLS));
+    // per system: this CTA's partials, then the ticket; the last CTA sums over the CTAs in order and
+    // runs the finish.  Every CTA arrives (with zeros after an abort) so the tickets stay balanced.
+    if (tid < nsys && !s_skip[tid]) {
+        const int sl = tid;
+        double *part = partials + (size_t)sl * 3 * G;
+        for (int v = 0; v < 3; ++v) {
+            double t = 0;
+            for (int q = 0; q < 4; ++q) t += sacc[(size_t)q * TC_NMAX * 3 + sl * 3 + v];
+            part[(size_t)v * G + blockIdx.x] = s_abort ? 0.0 : t;
+        }
+        __threadfence();
+        if (atomicAdd(&tickets[sl], 1u) == (unsigned)G - 1) {
+            __threadfence();
+            double tot[3];
+            for (int v = 0; v < 3; ++v) {
+                double t = 0;
+                for (int g = 0; g < G; ++g) t += __ldcg(part + (size_t)v * G + g);
+                tot[v] = t;
+            }
+            const int sy = s_act[sl];
+            run_finish(fin, sy, state[sy], tot[0], tot[1], tot[2]);
+            tickets[sl] = 0;
+        }
+    }
 }
 
 std::mutex g_tc_mu;
@@ -692,6 +980,47 @@ int launch_wapply_tc(int n, int kk, const float2 *W, double2 *coef, size_t strid
     }
     k_wapply_tc<<<G, WA_THREADS, wapply_smem_bytes(nsp), st>>>(n, kk, W, coef, strideC, act, nsys, nsp, P, strideP,
                                                                unit_idx);
+    return 1;
+}
+
+size_t wupdate_smem_bytes(int nsp) {
+    return (size_t)4 * WA_AOP + (size_t)4 * nsp * 2 * TC_ROW + sizeof(float2) * TC_NMAX * WU_QB +
+           sizeof(double) * 4 * TC_NMAX * 3 + 1024;
+}
+
+bool wupdate_tc_ok(int n, int kk, int qb, int nsys) {
+    return n > 0 && kk > 0 && kk <= TC_KMAX && qb >= 0 && qb <= WU_QB && nsys >= 8 && nsys <= TC_NMAX;
+}
+
+int wupdate_tc_grid(int n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const long ntiles = ((long)n + WA_TILE - 1) / WA_TILE;
+    const int sms = device_sms(dev);
+    return (int)(ntiles < sms ? ntiles : sms);
+}
+
+int launch_wupdate_tc(int n, int kk, const float2 *W, const float2 *V, size_t strideV, int qb, const float2 *w,
+                      size_t strideW, float2 *out, size_t strideO, const int *act, int nsys, const double2 *coef,
+                      size_t strideC, double *partials, unsigned *tickets, SysState *state, FinishArgs fin,
+                      bool skip_broken, cudaStream_t st) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int G = wupdate_tc_grid(n);
+    const int nsp = ((nsys + 7) / 8) * 8;
+    static std::vector<char> set;
+    {
+        std::lock_guard<std::mutex> lk(g_tc_mu);
+        if ((int)set.size() <= dev) set.resize(dev + 1, 0);
+        if (!set[dev]) {
+            cudaFuncSetAttribute(k_wupdate_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)wupdate_smem_bytes(TC_NMAX));
+            set[dev] = 1;
+        }
+    }
+    k_wupdate_tc<<<G, WU_THREADS, wupdate_smem_bytes(nsp), st>>>(n, kk, W, V, strideV, qb, w, strideW, out, strideO,
+                                                                  act, nsys, nsp, coef, strideC, partials, tickets,
+                                                                  state, fin, skip_broken ? 1 : 0);
     return 1;
 }
 

