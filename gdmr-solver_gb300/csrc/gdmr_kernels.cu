@@ -1266,32 +1266,50 @@ constexpr int KM_THREADS = 256, KM_WARPS = KM_THREADS / 32, KM_PB = 8;   // coef
 
 
 template <class R>
-__global__ void __launch_bounds__(KM_THREADS) k_krylov_multi(const KrylovJob<R> *__restrict__ jobs,
-                                                              const int *__restrict__ cta_job, int *abort) {
+__global__ void __launch_bounds__(KM_THREADS, 3) k_krylov_multi(const KrylovJob<R> *__restrict__ jobs,
+                                                                 const int *__restrict__ cta_job, int *abort) {
     using C = typename CT<R>::t;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const KrylovJob<R> a = jobs[cta_job[blockIdx.x]];
-    const int c = blockIdx.x - a.cta0, ncta = a.ncta, n = a.n, kk = a.kk;
+    const KrylovJob<R> &a = jobs[cta_job[blockIdx.x]];
+    const int c = blockIdx.x - a.cta0, ncta = a.ncta, n = a.n, kk = a.kk, nsl = a.nslices;
     const int gw = c * KM_WARPS + warp, nw = ncta * KM_WARPS;   // the warp's index in the job
-    double *npart = a.part + (size_t)ncta * a.qmax * 2;
+    const C *__restrict__ W = a.W;
+    C *__restrict__ V = a.V;
+    C *__restrict__ y = a.y;
+    double *part = a.part;
+    double *npart = part + (size_t)ncta * a.qmax * 2;
     __shared__ double wsum[KM_WARPS][KM_PB][2];
     __shared__ double red[KM_WARPS][3];
     __shared__ C cs[QMAX];
     __shared__ double s_norm[3];
     unsigned k = 0;   // barrier passes
+    auto basis = [&](int p) -> const C * { return p < kk ? W + (size_t)p * n : V + (size_t)(p - kk) * n; };
     for (int j = 1; j <= a.m - kk; ++j) {
         const int q = kk + j;
-        const C *x = a.V + (size_t)(j - 1) * n;
-        // (1) y = A v_{j-1} on the warp's slices (v_{j-1} rows of other warps through L2)
-        for (int sl = gw; sl < a.nslices; sl += nw) {
+        const C *x = V + (size_t)(j - 1) * n;
+        // (1) y = A v_{j-1} on the warp's slices (v_{j-1} rows of other warps through L2); the
+        // entries of a slice four at a time, their loads issued before their products
+        for (int sl = gw; sl < nsl; sl += nw) {
             const int row = sl * 32 + lane;
             const int beg = a.slice_ptr[sl], width = (a.slice_ptr[sl + 1] - beg) >> 5;
             C acc = czero<C>();
-            for (int e = 0; e < width; ++e) {
+            int e = 0;
+            for (; e + 4 <= width; e += 4) {
+                C av[4], xv[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int idx = beg + (e + u) * 32 + lane;
+                    av[u] = a.vals[idx];
+                    xv[u] = ldcg_c(x + a.cols[idx]);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) cfma(acc, av[u], xv[u]);
+            }
+            for (; e < width; ++e) {
                 const int idx = beg + e * 32 + lane;
                 cfma(acc, a.vals[idx], ldcg_c(x + a.cols[idx]));
             }
-            if (row < n) a.y[row] = canon(acc);
+            if (row < n) y[row] = canon(acc);
         }
         __syncwarp();
         // (2) projection partials <B_p, y>, KM_PB coefficients a pass over the warp's rows
@@ -1299,18 +1317,19 @@ __global__ void __launch_bounds__(KM_THREADS) k_krylov_multi(const KrylovJob<R> 
             C acc[KM_PB];
 #pragma unroll
             for (int u = 0; u < KM_PB; ++u) acc[u] = czero<C>();
-            for (int sl = gw; sl < a.nslices; sl += nw) {
+            const C *bp[KM_PB];
+#pragma unroll
+            for (int u = 0; u < KM_PB; ++u) bp[u] = basis(p0 + u < q ? p0 + u : q - 1);
+#pragma unroll 2
+            for (int sl = gw; sl < nsl; sl += nw) {
                 const int row = sl * 32 + lane;
                 if (row >= n) continue;
-                const C yv = a.y[row];
+                const C yv = y[row];
+                C bv[KM_PB];
 #pragma unroll
-                for (int u = 0; u < KM_PB; ++u) {
-                    const int p = p0 + u;
-                    if (p < q) {
-                        const C *B = p < kk ? a.W + (size_t)p * n : a.V + (size_t)(p - kk) * n;
-                        cdotacc(acc[u], B[row], yv);
-                    }
-                }
+                for (int u = 0; u < KM_PB; ++u) bv[u] = bp[u][row];
+#pragma unroll
+                for (int u = 0; u < KM_PB; ++u) cdotacc(acc[u], bv[u], yv);
             }
 #pragma unroll
             for (int u = 0; u < KM_PB; ++u) {
@@ -1324,7 +1343,7 @@ __global__ void __launch_bounds__(KM_THREADS) k_krylov_multi(const KrylovJob<R> 
             if (tid < 2 * KM_PB && p0 + tid / 2 < q) {
                 double t = 0;
                 for (int w = 0; w < KM_WARPS; ++w) t += wsum[w][tid / 2][tid & 1];
-                a.part[((size_t)c * a.qmax + p0 + tid / 2) * 2 + (tid & 1)] = t;
+                part[((size_t)c * a.qmax + p0 + tid / 2) * 2 + (tid & 1)] = t;
             }
             __syncthreads();
         }
@@ -1334,29 +1353,35 @@ __global__ void __launch_bounds__(KM_THREADS) k_krylov_multi(const KrylovJob<R> 
             for (int p = c; p < q; p += ncta) {
                 double re = 0, im = 0;
                 for (int g = lane; g < ncta; g += 32) {
-                    re += __ldcg(a.part + ((size_t)g * a.qmax + p) * 2);
-                    im += __ldcg(a.part + ((size_t)g * a.qmax + p) * 2 + 1);
+                    re += __ldcg(part + ((size_t)g * a.qmax + p) * 2);
+                    im += __ldcg(part + ((size_t)g * a.qmax + p) * 2 + 1);
                 }
                 re = warp_sum(re);
                 im = warp_sum(im);
                 if (lane == 0) a.coef[p] = make_double2(re, im);
             }
         if (!ks_grid_sync(a.bar, (++k) * ncta, abort)) return;
-        // (4) out = y - sum_p c_p B_p in place of y; ||out||^2 and <out, y> partials
+        // (4) out = y - sum_p c_p B_p in place of y (eight basis vectors' loads in flight before
+        // their products); ||out||^2 and <out, y> partials
         for (int p = tid; p < q; p += KM_THREADS) cs[p] = from_d<C>(__ldcg(a.coef + p));
         __syncthreads();
         double v0 = 0, v1 = 0, v2 = 0;
-        for (int sl = gw; sl < a.nslices; sl += nw) {
+        for (int sl = gw; sl < nsl; sl += nw) {
             const int row = sl * 32 + lane;
             if (row >= n) continue;
-            const C yv = a.y[row];
+            const C yv = y[row];
             C w = yv;
-            for (int p = 0; p < q; ++p) {
-                const C *B = p < kk ? a.W + (size_t)p * n : a.V + (size_t)(p - kk) * n;
-                cfms(w, cs[p], B[row]);
+            int p = 0;
+            for (; p + 8 <= q; p += 8) {
+                C bv[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) bv[u] = basis(p + u)[row];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) cfms(w, cs[p + u], bv[u]);
             }
+            for (; p < q; ++p) cfms(w, cs[p], basis(p)[row]);
             w = canon(w);
-            a.y[row] = w;
+            y[row] = w;
             C ln = czero<C>(), lc = czero<C>();
             cdotacc(ln, w, w);
             cdotacc(lc, w, yv);
@@ -1397,16 +1422,16 @@ __global__ void __launch_bounds__(KM_THREADS) k_krylov_multi(const KrylovJob<R> 
         // (6) v_j = out / ||out|| on the warp's rows; a breakdown ends the loop with v_j and the
         // rest of the basis zero (gDMR.cu:2256-2289), which the cycle-end projection reads
         const R al = broken ? R(0.f) : R(1.0 / nrm);
-        for (int sl = gw; sl < a.nslices; sl += nw) {
+        for (int sl = gw; sl < nsl; sl += nw) {
             const int row = sl * 32 + lane;
             if (row >= n) continue;
-            C v = a.y[row];
+            C v = y[row];
             v.x = v.x * al;
             v.y = v.y * al;
             if (broken) v = czero<C>();
-            a.V[(size_t)j * n + row] = v;
+            V[(size_t)j * n + row] = v;
             if (broken)
-                for (int jj = j + 1; jj <= a.m - kk; ++jj) a.V[(size_t)jj * n + row] = czero<C>();
+                for (int jj = j + 1; jj <= a.m - kk; ++jj) V[(size_t)jj * n + row] = czero<C>();
         }
         if (broken) return;
         if (!ks_grid_sync(a.bar, (++k) * ncta, abort)) return;
@@ -2124,6 +2149,125 @@ __global__ void __launch_bounds__(NT) k_combine(int n, int kk, int m, const type
         f.mode = FIN_RESIDUAL;
         run_finish(f, s, state[s], tot[0], 0, 0);
         tickets[slot] = 0;
+    }
+}
+
+// The cycle-end combinations for a batch, SB systems a CTA: each element of the shared W and Z
+// is loaded once for the SB systems of the group (k_combine has every system re-read them from
+// L2), then each system's own basis.  Per element the operations and their order are
+// k_combine's; the norm partials are summed per system as there (last CTA of each system).
+template <class R, int SB, int EPT>
+__global__ void __launch_bounds__(NT) k_combine_grp(int n, int kk, int m, const typename CT<R>::t *__restrict__ W,
+                                                    const typename CT<R>::t *__restrict__ Z,
+                                                    const typename CT<R>::t *__restrict__ V0, size_t strideV,
+                                                    typename CT<R>::t *__restrict__ r0, size_t strideR,
+                                                    typename CT<R>::t *__restrict__ x0, size_t strideX,
+                                                    const double2 *__restrict__ t0, const double2 *__restrict__ y0,
+                                                    size_t strideC, const int *__restrict__ act, int nsys,
+                                                    double2 *__restrict__ partials, unsigned *tickets, SysState *state) {
+    using C = typename CT<R>::t;
+    const int g0 = blockIdx.x * SB, chunk = blockIdx.y, G = gridDim.y, tid = threadIdx.x;
+    const int ns = min(SB, nsys - g0);
+    __shared__ C ts[SB][QMAX], ys[SB][QMAX];
+    __shared__ double red[SB][NW];
+    __shared__ int sys[SB];
+    if (tid < SB) sys[tid] = tid < ns ? act[g0 + tid] : act[g0];
+    __syncthreads();
+    for (int e = tid; e < SB * (m + 1); e += NT) {
+        const int g = e / (m + 1), p = e % (m + 1), s = sys[g];
+        const R ra = (R)state[s].rho_abs;
+        ts[g][p] = from_d<C>(t0[(size_t)s * strideC + p]);
+        C yy = p < m ? from_d<C>(y0[(size_t)s * strideC + p]) : czero<C>();
+        yy.x *= ra;
+        yy.y *= ra;
+        ys[g][p] = yy;
+    }
+    __syncthreads();
+    const long c0 = (long)chunk * NT * EPT;
+    C ra_[SB][EPT], xa[SB][EPT];
+#pragma unroll
+    for (int g = 0; g < SB; ++g)
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            const long i = c0 + tid + (long)e * NT;
+            const bool in = g < ns && i < n;
+            ra_[g][e] = in ? r0[(size_t)sys[g] * strideR + i] : czero<C>();
+            xa[g][e] = in ? x0[(size_t)sys[g] * strideX + i] : czero<C>();
+        }
+    for (int p = 0; p < kk; ++p) {
+        C wv[EPT], zv[EPT];
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            const long i = c0 + tid + (long)e * NT;
+            wv[e] = i < n ? W[(size_t)p * n + i] : czero<C>();
+            zv[e] = i < n ? Z[(size_t)p * n + i] : czero<C>();
+        }
+#pragma unroll
+        for (int g = 0; g < SB; ++g) {
+            const C tc = ts[g][p], yc = ys[g][p];
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) {
+                cfms(ra_[g][e], tc, wv[e]);
+                cfma(xa[g][e], yc, zv[e]);
+                ra_[g][e] = canon(ra_[g][e]);
+                xa[g][e] = canon(xa[g][e]);
+            }
+        }
+    }
+#pragma unroll
+    for (int g = 0; g < SB; ++g) {
+        if (g >= ns) break;
+        const C *V = V0 + (size_t)sys[g] * strideV;
+#pragma unroll 4
+        for (int p = 0; p <= m - kk; ++p) {
+            const C tc = ts[g][kk + p], yc = ys[g][kk + p];   // ys[m] = 0: target side only
+            const C *vp = V + (size_t)p * n;
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) {
+                const long i = c0 + tid + (long)e * NT;
+                if (i < n) {
+                    const C vv = vp[i];
+                    cfms(ra_[g][e], tc, vv);
+                    cfma(xa[g][e], yc, vv);
+                }
+                ra_[g][e] = canon(ra_[g][e]);
+                xa[g][e] = canon(xa[g][e]);
+            }
+        }
+    }
+    double v[SB];
+#pragma unroll
+    for (int g = 0; g < SB; ++g) {
+        C ln = czero<C>();
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            const long i = c0 + tid + (long)e * NT;
+            ra_[g][e] = canon(ra_[g][e]);
+            xa[g][e] = canon(xa[g][e]);
+            if (g < ns && i < n) {
+                r0[(size_t)sys[g] * strideR + i] = ra_[g][e];
+                x0[(size_t)sys[g] * strideX + i] = xa[g][e];
+            }
+            cdotacc(ln, ra_[g][e], ra_[g][e]);
+        }
+        v[g] = (double)ln.x;
+    }
+    block_sum<SB>(v, red);
+    if (tid == 0)
+        for (int g = 0; g < ns; ++g) ((double *)partials)[(size_t)(g0 + g) * G + chunk] = v[g];
+    for (int g = 0; g < ns; ++g) {
+        const int slot = g0 + g;
+        if (!arrive_last(&tickets[slot], G)) continue;
+        double tot[1];
+        __syncthreads();
+        sum_partials<1>((double *)partials + (size_t)slot * G, G, tot, red);
+        if (tid == 0) {
+            FinishArgs f{};
+            f.mode = FIN_RESIDUAL;
+            run_finish(f, sys[g], state[sys[g]], tot[0], 0, 0);
+            tickets[slot] = 0;
+        }
+        __syncthreads();
     }
 }
 
@@ -4311,6 +4455,14 @@ void launch_combine(int n, int kk, int m, const typename CT<R>::t *W, const type
                     const int *act, int nsys, double2 *partials, unsigned *tickets, SysState *state, cudaStream_t st) {
     if (nsys <= 0) return;
     Launch L_(KC_COMBINE, (double)sizeof(typename CT<R>::t) * n * (2.0 * kk + (double)nsys * (m + 1 - kk + 4)), st, 1);
+    if (kk > 0 && nsys >= 4 && combine_group() > 0) {
+        // the grouped form: the shared W and Z loaded once for four systems
+        constexpr int EPT = sizeof(R) == 4 ? 2 : 1;
+        const int G = (n + NT * EPT - 1) / (NT * EPT);
+        k_combine_grp<R, 4, EPT><<<dim3((unsigned)((nsys + 3) / 4), (unsigned)G), NT, 0, st>>>(
+            n, kk, m, W, Z, V, strideV, r, strideR, x, strideX, t, y, strideC, act, nsys, partials, tickets, state);
+        return;
+    }
     k_combine<R><<<grid2(nsys, nchunks<R>(n)), NT, 0, st>>>(n, kk, m, W, Z, V, strideV, r, strideR, x, strideX, t, y, strideC, act,
                                                  partials, tickets, state);
 }
@@ -4478,6 +4630,9 @@ bool launch_krylov_small(int n, int kk, int m, const SellMatrix &A, const typena
     }
 }
 
+static std::atomic<int> g_combine_group{1};
+void set_combine_group(int on) { g_combine_group.store(on ? 1 : 0); }
+int combine_group() { return g_combine_group.load(); }
 static std::atomic<int> g_grid_operator{1};
 static std::atomic<int> g_grid_batch{0};
 void set_grid_operator(int enable) { g_grid_operator.store(enable ? 1 : 0); }

@@ -284,6 +284,10 @@ void launch_combine(int n, int kk, int m, const typename CT<R>::t *W, const type
                     typename CT<R>::t *x, size_t strideX, const double2 *t, const double2 *y, size_t strideC,
                     const int *act, int nsys, double2 *partials, unsigned *tickets, SysState *state, cudaStream_t st);
 
+// Batches of four or more systems with a deflation segment take a grouped form of the cycle-end
+// combination (W and Z loaded once for four systems); 0 returns them to one system a CTA.
+void set_combine_group(int on);
+int combine_group();
 // Z_new[t] = [Z V] vs[:, t] for t < k, plus squared norms into znorm2 (k doubles).
 // V: basis of system 0 (system s at V + s*strideV); the lead system is read from device memory.
 template <class R>

@@ -63,6 +63,7 @@ SIGNATURES = {
     "gdmrTuneForce": (None, [I, I]),
     "gdmrGridOperator": (None, [I]),
     "gdmrGridBatch": (None, [I]),
+    "gdmrCombineGroup": (None, [I]),
     "gdmr_csr_grid_form": (I, [I, P, P, P, P]),
     "gdmrAsyncTimeouts": (ctypes.c_uint, []),
     "gdmr_hessenberg_svd": (I, [I, I, P, P, P, P]),
@@ -188,6 +189,11 @@ def grid_batch(systems_per_thread: int) -> None:
     """Batched operator products on the grid kernel with 1, 2 or 4 systems a thread; 0 (the
     default) keeps them on the SELL-32 kernel."""
     load().gdmrGridBatch(int(systems_per_thread))
+
+
+def combine_group(enable: bool) -> None:
+    """Cycle-end combinations of batches four systems a CTA (on by default) or one."""
+    load().gdmrCombineGroup(1 if enable else 0)
 
 
 def csr_grid_form(A):

@@ -170,6 +170,11 @@ void gdmrGridOperator(int enable);
  * default, keeps them on the SELL-32 kernel, which measured faster for the 64-system batch. */
 void gdmrGridBatch(int systemsPerThread);
 
+/* The cycle-end combinations (r -= [W V] t, x += rho [Z V] y) of batches of four or more
+ * systems with a deflation segment run four systems a CTA, each element of the shared W and Z
+ * loaded once for the four (on by default); 0 returns them to one system a CTA. */
+void gdmrCombineGroup(int enable);
+
 /* Host-only check of a CSR matrix (complex values interleaved re, im) for the structured-grid
  * form: dims[0..2] <- (nx, ny, nz), zeros if it has none.  GDMR_EINVAL for malformed arrays. */
 int gdmr_csr_grid_form(int n, const int *rowPtr, const int *colIdx, const double *vals_ri, int *dims);

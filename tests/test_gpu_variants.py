@@ -62,3 +62,26 @@ def test_pinned_variant_solves_the_batch(batch20, precision, pair):
     rel = s.true_residual(rhs, X)
     assert np.all(rel <= 1.5e-10)
     assert gdmr.async_timeouts() == timeouts0
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_grouped_combination_matches_one_system_a_cta(batch20, precision):
+    """The cycle-end combination four systems a CTA (W and Z loaded once for the four) against
+    one system a CTA: the same per-element operations, so both batches converge alike and to
+    the direct solution."""
+    A, rhs, cfg, direct = batch20
+    out = {}
+    for grouped in (True, False):
+        gdmr.combine_group(grouped)
+        try:
+            s = gdmr.System(A, cfg["m"], cfg["k"], capacity=NRHS, precision=precision)
+            out[grouped] = s.solve_batch(rhs, tol=1e-10, max_cycles=2000)
+        finally:
+            gdmr.combine_group(True)
+    for grouped, (X, stats) in out.items():
+        assert all(st["status"] == 0 and st["true_rel_res"] <= 1.5e-10 for st in stats), grouped
+        err = np.linalg.norm(X - direct, axis=1) / np.linalg.norm(direct, axis=1)
+        assert err.max() < 1e-8, (grouped, err.max())
+    cg = [st["cycles"] for st in out[True][1]]
+    cs = [st["cycles"] for st in out[False][1]]
+    assert max(abs(a - b) for a, b in zip(cg, cs)) <= 2, (cg, cs)
