@@ -1273,25 +1273,33 @@ __global__ void __launch_bounds__(KM_THREADS, 3) k_krylov_multi(const KrylovJob<
     const KrylovJob<R> &a = jobs[cta_job[blockIdx.x]];
     const int c = blockIdx.x - a.cta0, ncta = a.ncta, n = a.n, kk = a.kk, nsl = a.nslices;
     const int gw = c * KM_WARPS + warp, nw = ncta * KM_WARPS;   // the warp's index in the job
+    // the job's fields in registers: the loops store through other pointers, so fields read
+    // through the reference would be loaded again before every use
     const C *__restrict__ W = a.W;
     C *__restrict__ V = a.V;
     C *__restrict__ y = a.y;
+    const int *__restrict__ slice_ptr = a.slice_ptr;
+    const int *__restrict__ cols = a.cols;
+    const C *__restrict__ vals = a.vals;
+    double2 *coef = a.coef;
+    unsigned *bar = a.bar;
+    const int m = a.m, qmax = qmax;
     double *part = a.part;
-    double *npart = part + (size_t)ncta * a.qmax * 2;
+    double *npart = part + (size_t)ncta * qmax * 2;
     __shared__ double wsum[KM_WARPS][KM_PB][2];
     __shared__ double red[KM_WARPS][3];
     __shared__ C cs[QMAX];
     __shared__ double s_norm[3];
     unsigned k = 0;   // barrier passes
     auto basis = [&](int p) -> const C * { return p < kk ? W + (size_t)p * n : V + (size_t)(p - kk) * n; };
-    for (int j = 1; j <= a.m - kk; ++j) {
+    for (int j = 1; j <= m - kk; ++j) {
         const int q = kk + j;
         const C *x = V + (size_t)(j - 1) * n;
         // (1) y = A v_{j-1} on the warp's slices (v_{j-1} rows of other warps through L2); the
         // entries of a slice four at a time, their loads issued before their products
         for (int sl = gw; sl < nsl; sl += nw) {
             const int row = sl * 32 + lane;
-            const int beg = a.slice_ptr[sl], width = (a.slice_ptr[sl + 1] - beg) >> 5;
+            const int beg = slice_ptr[sl], width = (slice_ptr[sl + 1] - beg) >> 5;
             C acc = czero<C>();
             int e = 0;
             for (; e + 4 <= width; e += 4) {
@@ -1299,15 +1307,15 @@ __global__ void __launch_bounds__(KM_THREADS, 3) k_krylov_multi(const KrylovJob<
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     const int idx = beg + (e + u) * 32 + lane;
-                    av[u] = a.vals[idx];
-                    xv[u] = ldcg_c(x + a.cols[idx]);
+                    av[u] = vals[idx];
+                    xv[u] = ldcg_c(x + cols[idx]);
                 }
 #pragma unroll
                 for (int u = 0; u < 4; ++u) cfma(acc, av[u], xv[u]);
             }
             for (; e < width; ++e) {
                 const int idx = beg + e * 32 + lane;
-                cfma(acc, a.vals[idx], ldcg_c(x + a.cols[idx]));
+                cfma(acc, vals[idx], ldcg_c(x + cols[idx]));
             }
             if (row < n) y[row] = canon(acc);
         }
@@ -1343,27 +1351,27 @@ __global__ void __launch_bounds__(KM_THREADS, 3) k_krylov_multi(const KrylovJob<
             if (tid < 2 * KM_PB && p0 + tid / 2 < q) {
                 double t = 0;
                 for (int w = 0; w < KM_WARPS; ++w) t += wsum[w][tid / 2][tid & 1];
-                part[((size_t)c * a.qmax + p0 + tid / 2) * 2 + (tid & 1)] = t;
+                part[((size_t)c * qmax + p0 + tid / 2) * 2 + (tid & 1)] = t;
             }
             __syncthreads();
         }
-        if (!ks_grid_sync(a.bar, (++k) * ncta, abort)) return;
+        if (!ks_grid_sync(bar, (++k) * ncta, abort)) return;
         // (3) coefficient p summed over the job's CTAs by CTA p mod ncta, in order
         if (warp == 0)
             for (int p = c; p < q; p += ncta) {
                 double re = 0, im = 0;
                 for (int g = lane; g < ncta; g += 32) {
-                    re += __ldcg(part + ((size_t)g * a.qmax + p) * 2);
-                    im += __ldcg(part + ((size_t)g * a.qmax + p) * 2 + 1);
+                    re += __ldcg(part + ((size_t)g * qmax + p) * 2);
+                    im += __ldcg(part + ((size_t)g * qmax + p) * 2 + 1);
                 }
                 re = warp_sum(re);
                 im = warp_sum(im);
-                if (lane == 0) a.coef[p] = make_double2(re, im);
+                if (lane == 0) coef[p] = make_double2(re, im);
             }
-        if (!ks_grid_sync(a.bar, (++k) * ncta, abort)) return;
+        if (!ks_grid_sync(bar, (++k) * ncta, abort)) return;
         // (4) out = y - sum_p c_p B_p in place of y (eight basis vectors' loads in flight before
         // their products); ||out||^2 and <out, y> partials
-        for (int p = tid; p < q; p += KM_THREADS) cs[p] = from_d<C>(__ldcg(a.coef + p));
+        for (int p = tid; p < q; p += KM_THREADS) cs[p] = from_d<C>(__ldcg(coef + p));
         __syncthreads();
         double v0 = 0, v1 = 0, v2 = 0;
         for (int sl = gw; sl < nsl; sl += nw) {
@@ -1399,7 +1407,7 @@ __global__ void __launch_bounds__(KM_THREADS, 3) k_krylov_multi(const KrylovJob<
             for (int w = 0; w < KM_WARPS; ++w) t += red[w][tid];
             npart[(size_t)c * 3 + tid] = t;
         }
-        if (!ks_grid_sync(a.bar, (++k) * ncta, abort)) return;
+        if (!ks_grid_sync(bar, (++k) * ncta, abort)) return;
         // (5) the norms summed by every CTA in the same order; CTA 0 of the job runs the finish
         if (tid < 3) {
             double t = 0;
@@ -1410,12 +1418,12 @@ __global__ void __launch_bounds__(KM_THREADS, 3) k_krylov_multi(const KrylovJob<
         const double n2 = s_norm[0], nrm = sqrt(n2);
         const bool broken = nrm < a.tol;
         if (c == 0) {
-            for (int p = tid; p < q; p += KM_THREADS) a.H[(size_t)(kk + j - 1) * (a.m + 1) + p] = __ldcg(a.coef + p);
+            for (int p = tid; p < q; p += KM_THREADS) a.H[(size_t)(kk + j - 1) * (m + 1) + p] = __ldcg(coef + p);
             if (tid == 0) {
                 FinishArgs f{};
-                f.mode = FIN_KRYLOV; f.col = kk + j - 1; f.nco = 0; f.ldH = a.m + 1; f.m = a.m; f.kk = kk;
+                f.mode = FIN_KRYLOV; f.col = kk + j - 1; f.nco = 0; f.ldH = a.m + 1; f.m = m; f.kk = kk;
                 f.compat_eye = a.compat_eye; f.tol = a.tol; f.H = a.H; f.strideH = 0;
-                f.coef = a.coef; f.strideC = 0;
+                f.coef = coef; f.strideC = 0;
                 run_finish(f, 0, *a.state, n2, s_norm[1], s_norm[2]);
             }
         }
@@ -1431,10 +1439,10 @@ __global__ void __launch_bounds__(KM_THREADS, 3) k_krylov_multi(const KrylovJob<
             if (broken) v = czero<C>();
             V[(size_t)j * n + row] = v;
             if (broken)
-                for (int jj = j + 1; jj <= a.m - kk; ++jj) V[(size_t)jj * n + row] = czero<C>();
+                for (int jj = j + 1; jj <= m - kk; ++jj) V[(size_t)jj * n + row] = czero<C>();
         }
         if (broken) return;
-        if (!ks_grid_sync(a.bar, (++k) * ncta, abort)) return;
+        if (!ks_grid_sync(bar, (++k) * ncta, abort)) return;
     }
 }
 
@@ -4489,6 +4497,20 @@ void launch_zupdate(int n, int kk, int m, int k, const typename CT<R>::t *Z, con
             if (k <= 16) run(std::integral_constant<int, 16>{});
             else if (k <= 24) run(std::integral_constant<int, 24>{});
             else run(std::integral_constant<int, 32>{});
+            return;
+        }
+    }
+    if constexpr (sizeof(R) != 4) {
+        // double-float accumulators (four FP32 words an output): 12 outputs a pass, so k = 24
+        // reads [Z V] twice instead of three times
+        if (k <= 24) {
+            constexpr int KB = 12;
+            Launch L_(KC_ZUPDATE, (double)sizeof(C) * n * ((double)m + k), st, (k + KB - 1) / KB);
+            for (int t0 = 0; t0 < k; t0 += KB) {
+                const size_t smem = (size_t)m * KB * sizeof(typename ZW<C>::t);
+                k_zupdate<R, KB><<<G, NT, smem, st>>>(n, kk, m, k, t0, Z, V, strideV, lead, vs, Znew, partials,
+                                                      ticket, znorm2);
+            }
             return;
         }
     }
