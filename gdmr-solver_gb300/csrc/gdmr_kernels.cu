@@ -1283,7 +1283,7 @@ __global__ void __launch_bounds__(KM_THREADS, 3) k_krylov_multi(const KrylovJob<
     const C *__restrict__ vals = a.vals;
     double2 *coef = a.coef;
     unsigned *bar = a.bar;
-    const int m = a.m, qmax = qmax;
+    const int m = a.m, qmax = a.qmax;
     double *part = a.part;
     double *npart = part + (size_t)ncta * qmax * 2;
     __shared__ double wsum[KM_WARPS][KM_PB][2];
@@ -1732,6 +1732,120 @@ __global__ void __launch_bounds__(NT, 2) k_update_wreg(int n, int kk, const type
         }
         __syncthreads();
     }
+}
+
+// ----------------------------------------------------------------- row-stationary batched update
+// The complex64 batched update with a shared deflation segment, every system of the batch in
+// one CTA.  Each thread keeps its row of W (the kk shared vectors) in registers and walks the
+// systems, so W is read from memory once per launch and the shared part W c_s never goes
+// through memory (the tensor-core apply writes it and the per-system update reads it back,
+// 16 bytes a row a system on top of the algorithmic bytes).  CTAs own contiguous ranges of
+// 256-row chunks, about two a SM.  A system's V_s loads go out in batches of VB ahead of the
+// arithmetic, the shared part is computed while they are in flight.  Norm and cross term are
+// summed per warp in FP32 butterflies (one FP64 warp instruction is ~64 scheduler clocks on
+// GB300, three FP64 butterflies per system per chunk would bound the kernel), accumulated per
+// warp in shared memory over the CTA's chunks and summed in FP64 once per CTA; the last CTA
+// sums the CTAs' partials, one warp a system, in a fixed order.
+inline size_t update_rows_smem(int nsys, int q) {
+    return sizeof(float2) * (size_t)nsys * q + sizeof(float) * (size_t)nsys * 3 * NW + 2 * sizeof(int) * (size_t)nsys;
+}
+
+template <int KW, int VB>
+__global__ void __launch_bounds__(NT, 2) k_update_rows(int n, int kk, const float2 *__restrict__ W,
+                                                       const float2 *__restrict__ V0, size_t strideV, int qb,
+                                                       const float2 *__restrict__ w0, size_t strideW,
+                                                       float2 *__restrict__ out0, size_t strideO,
+                                                       const int *__restrict__ act, int nsys,
+                                                       const double2 *__restrict__ coef0, size_t strideC, int cpb,
+                                                       double *__restrict__ partials, unsigned *tickets,
+                                                       SysState *state, FinishArgs fin, int skip_broken) {
+    extern __shared__ __align__(16) unsigned char ur_sm[];
+    const int q = kk + qb;
+    float2 *cs = reinterpret_cast<float2 *>(ur_sm);                       // [nsys][q]
+    float *red = reinterpret_cast<float *>(cs + (size_t)nsys * q);         // [nsys * 3][NW]
+    int *s_act = reinterpret_cast<int *>(red + (size_t)nsys * 3 * NW);    // [nsys]
+    int *s_live = s_act + nsys;                                           // [nsys]
+    __shared__ unsigned s_last;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, G = gridDim.x;
+    for (int e = tid; e < nsys * q; e += NT) {
+        const int g = e / q, p = e - g * q;
+        cs[e] = from_d<float2>(coef0[(size_t)act[g] * strideC + p]);
+    }
+    for (int e = tid; e < nsys * 3 * NW; e += NT) red[e] = 0.f;
+    for (int g = tid; g < nsys; g += NT) {
+        const int s = act[g];
+        s_act[g] = s;
+        s_live[g] = !(skip_broken && state[s].broken);
+    }
+    __syncthreads();
+    const long nch = ((long)n + NT - 1) / NT, c0 = (long)blockIdx.x * cpb;
+    const long c1 = c0 + cpb < nch ? c0 + cpb : nch;
+    for (long c = c0; c < c1; ++c) {
+        const long i = c * NT + tid;
+        const bool in = i < n;
+        float2 wr[KW];
+#pragma unroll
+        for (int p = 0; p < KW; ++p) wr[p] = (p < kk && in) ? W[(size_t)p * n + i] : czero<float2>();
+        for (int g = 0; g < nsys; ++g) {
+            const int s = s_act[g];
+            const bool live = in && s_live[g];
+            const float2 *cg = cs + (size_t)g * q;
+            const float2 *V = V0 + (size_t)s * strideV + i;
+            float2 vb[VB];
+#pragma unroll
+            for (int u = 0; u < VB; ++u) vb[u] = (live && u < qb) ? V[(size_t)u * n] : czero<float2>();
+            const float2 org = live ? w0[(size_t)s * strideW + i] : czero<float2>();
+            float2 acc = org;
+#pragma unroll
+            for (int p = 0; p < KW; ++p)
+                if (p < kk) cfms(acc, cg[p], wr[p]);
+#pragma unroll
+            for (int u = 0; u < VB; ++u)
+                if (u < qb) cfms(acc, cg[kk + u], vb[u]);
+            for (int p0 = VB; p0 < qb; p0 += VB) {
+#pragma unroll
+                for (int u = 0; u < VB; ++u) vb[u] = (live && p0 + u < qb) ? V[(size_t)(p0 + u) * n] : czero<float2>();
+#pragma unroll
+                for (int u = 0; u < VB; ++u)
+                    if (p0 + u < qb) cfms(acc, cg[kk + p0 + u], vb[u]);
+            }
+            if (live) out0[(size_t)s * strideO + i] = acc;
+            float2 ln = czero<float2>(), lc = czero<float2>();
+            cdotacc(ln, acc, acc);
+            cdotacc(lc, acc, org);
+            const float v0 = warp_sum(ln.x), v1 = warp_sum(lc.x), v2 = warp_sum(lc.y);
+            if (lane == 0) {
+                red[((size_t)g * 3 + 0) * NW + warp] += v0;
+                red[((size_t)g * 3 + 1) * NW + warp] += v1;
+                red[((size_t)g * 3 + 2) * NW + warp] += v2;
+            }
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < nsys * 3; e += NT) {
+        double t = 0;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) t += (double)red[(size_t)e * NW + w];
+        partials[(size_t)e * G + blockIdx.x] = t;
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(&tickets[0], 1u) == (unsigned)G - 1 ? 1u : 0u;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (int g = warp; g < nsys; g += NW) {
+        double t[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            double a = 0;
+            for (int b = lane; b < G; b += 32) a += __ldcg(partials + ((size_t)g * 3 + j) * G + b);
+            t[j] = warp_sum(a);
+        }
+        if (lane == 0 && s_live[g]) run_finish(fin, s_act[g], state[s_act[g]], t[0], t[1], t[2]);
+    }
+    __syncthreads();
+    if (tid == 0) tickets[0] = 0;
 }
 
 // ----------------------------------------------------------------- split-vector projection
@@ -2202,44 +2316,65 @@ __global__ void __launch_bounds__(NT) k_combine_grp(int n, int kk, int m, const 
             ra_[g][e] = in ? r0[(size_t)sys[g] * strideR + i] : czero<C>();
             xa[g][e] = in ? x0[(size_t)sys[g] * strideX + i] : czero<C>();
         }
-    for (int p = 0; p < kk; ++p) {
-        C wv[EPT], zv[EPT];
+    // Loads go out in batches ahead of their products (WB shared vectors of W and of Z, VB
+    // vectors of V_s), so that a thread has 2 WB EPT or VB EPT loads in flight; the products
+    // run in the order of the one-vector loop.
+    constexpr int WB = 4, VB = 8;
+    for (int p0 = 0; p0 < kk; p0 += WB) {
+        C wv[WB][EPT], zv[WB][EPT];
 #pragma unroll
-        for (int e = 0; e < EPT; ++e) {
-            const long i = c0 + tid + (long)e * NT;
-            wv[e] = i < n ? W[(size_t)p * n + i] : czero<C>();
-            zv[e] = i < n ? Z[(size_t)p * n + i] : czero<C>();
-        }
-#pragma unroll
-        for (int g = 0; g < SB; ++g) {
-            const C tc = ts[g][p], yc = ys[g][p];
+        for (int u = 0; u < WB; ++u)
 #pragma unroll
             for (int e = 0; e < EPT; ++e) {
-                cfms(ra_[g][e], tc, wv[e]);
-                cfma(xa[g][e], yc, zv[e]);
-                ra_[g][e] = canon(ra_[g][e]);
-                xa[g][e] = canon(xa[g][e]);
+                const long i = c0 + tid + (long)e * NT;
+                const bool ok = p0 + u < kk && i < n;
+                wv[u][e] = ok ? W[(size_t)(p0 + u) * n + i] : czero<C>();
+                zv[u][e] = ok ? Z[(size_t)(p0 + u) * n + i] : czero<C>();
+            }
+#pragma unroll
+        for (int u = 0; u < WB; ++u) {
+            if (p0 + u >= kk) break;
+#pragma unroll
+            for (int g = 0; g < SB; ++g) {
+                const C tc = ts[g][p0 + u], yc = ys[g][p0 + u];
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) {
+                    cfms(ra_[g][e], tc, wv[u][e]);
+                    cfma(xa[g][e], yc, zv[u][e]);
+                    ra_[g][e] = canon(ra_[g][e]);
+                    xa[g][e] = canon(xa[g][e]);
+                }
             }
         }
     }
+    const int nv = m - kk + 1;
 #pragma unroll
     for (int g = 0; g < SB; ++g) {
         if (g >= ns) break;
         const C *V = V0 + (size_t)sys[g] * strideV;
-#pragma unroll 4
-        for (int p = 0; p <= m - kk; ++p) {
-            const C tc = ts[g][kk + p], yc = ys[g][kk + p];   // ys[m] = 0: target side only
-            const C *vp = V + (size_t)p * n;
+        for (int p0 = 0; p0 < nv; p0 += VB) {
+            C vb[VB][EPT];
 #pragma unroll
-            for (int e = 0; e < EPT; ++e) {
-                const long i = c0 + tid + (long)e * NT;
-                if (i < n) {
-                    const C vv = vp[i];
-                    cfms(ra_[g][e], tc, vv);
-                    cfma(xa[g][e], yc, vv);
+            for (int u = 0; u < VB; ++u)
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) {
+                    const long i = c0 + tid + (long)e * NT;
+                    vb[u][e] = (p0 + u < nv && i < n) ? V[(size_t)(p0 + u) * n + i] : czero<C>();
                 }
-                ra_[g][e] = canon(ra_[g][e]);
-                xa[g][e] = canon(xa[g][e]);
+#pragma unroll
+            for (int u = 0; u < VB; ++u) {
+                if (p0 + u >= nv) break;
+                const C tc = ts[g][kk + p0 + u], yc = ys[g][kk + p0 + u];   // ys[m] = 0: target side only
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) {
+                    const long i = c0 + tid + (long)e * NT;
+                    if (i < n) {
+                        cfms(ra_[g][e], tc, vb[u][e]);
+                        cfma(xa[g][e], yc, vb[u][e]);
+                    }
+                    ra_[g][e] = canon(ra_[g][e]);
+                    xa[g][e] = canon(xa[g][e]);
+                }
             }
         }
     }
@@ -3563,16 +3698,33 @@ __global__ void __launch_bounds__(NT) k_residual64(int n, const int *__restrict_
     double2 *r = r0 + (size_t)s * strideR;
     __shared__ double red[1][NW];
     double n2 = 0;
-    for (int row = blockIdx.y * NT + tid; row < n; row += G * NT) {
-        double2 acc = b[row];
-        const int slice = row >> 5, lane = row & 31;
+    // A warp is one SELL slice and walks it whole (padding lanes past n included, their
+    // results dropped), so the test for a column of real values is warp-uniform: a real value
+    // takes two FP64 FMAs instead of four (the skipped products are zeros; the sums are the same
+    // but for the sign of a zero) and the FP64 pipe, which bounds this kernel, does 28 -> 16 a
+    // row on a 7-point operator with real off-diagonals.  The test reads the value's bits on
+    // the integer pipe.
+    for (int base = blockIdx.y * NT + (tid & ~31); base < n; base += G * NT) {
+        const int lane = tid & 31, row = base + lane, slice = base >> 5;
+        const bool ok = row < n;
+        double2 acc = ok ? b[row] : make_double2(0.0, 0.0);
         const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
         for (int c = 0; c < width; ++c) {
             const int e = beg + c * 32 + lane;
-            cfms(acc, vals[e], x[cols[e]]);
+            const double2 a = vals[e];
+            const double2 xv = x[cols[e]];
+            const bool real = (__double_as_longlong(a.y) << 1) == 0;
+            if (__all_sync(0xffffffffu, real)) {
+                acc.x = rfma(-a.x, xv.x, acc.x);
+                acc.y = rfma(-a.x, xv.y, acc.y);
+            } else {
+                cfms(acc, a, xv);
+            }
         }
-        r[row] = acc;
-        n2 += acc.x * acc.x + acc.y * acc.y;
+        if (ok) {
+            r[row] = acc;
+            n2 += acc.x * acc.x + acc.y * acc.y;
+        }
     }
     double v[1] = {n2};
     block_sum<1>(v, red);
@@ -4128,6 +4280,33 @@ void update_wreg_run(int n, int kk, const typename CT<R>::t *W, const typename C
     }
 }
 
+// k_update_rows over about two CTAs a SM, each on a contiguous range of chunks; false (nothing
+// launched) when the batch or the partials do not fit.
+inline bool update_rows_run(int n, int kk, const float2 *W, const float2 *V, size_t strideV, int qb,
+                            const float2 *w, size_t strideW, float2 *out, size_t strideO, const int *act, int nsys,
+                            const double2 *coef, size_t strideC, double2 *partials, unsigned *tickets,
+                            SysState *state, FinishArgs fin, bool skip_broken, cudaStream_t st) {
+    if (kk <= 0 || kk > 32 || nsys <= 0 || nsys > 128 || (qb > 0 && !V)) return false;
+    const long nch = ((long)n + NT - 1) / NT;
+    long target = 2L * num_sms();
+    if (target > nch) target = nch;
+    const int cpb = (int)((nch + target - 1) / target);
+    const int G = (int)((nch + cpb - 1) / cpb);
+    if ((size_t)nsys * 3 * G > scratch_capacity(partials)) return false;
+    const size_t smem = update_rows_smem(nsys, kk + qb);
+    if (smem > 200 * 1024) return false;
+    auto go = [&](auto kernel) {
+        allow_smem(kernel, smem);
+        kernel<<<G, NT, smem, st>>>(n, kk, W, V, strideV, qb, w, strideW, out, strideO, act, nsys, coef, strideC, cpb,
+                                    (double *)partials, tickets, state, fin, skip_broken ? 1 : 0);
+    };
+    if (kk <= 8) go(k_update_rows<8, 16>);
+    else if (kk <= 16) go(k_update_rows<16, 16>);
+    else if (kk <= 24) go(k_update_rows<24, 16>);
+    else go(k_update_rows<32, 8>);
+    return true;
+}
+
 // The projection variants; returns the number of kernels launched.
 template <class R>
 int mdot_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const typename CT<R>::t *segB, size_t strideB,
@@ -4293,6 +4472,13 @@ int update_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const t
     auto fits = [&](int ept) { return (size_t)nsys * 3 * (((size_t)n + NT * ept - 1) / (NT * ept)) <= cap; };
     constexpr int VW = sizeof(R) == 4 ? 8 : 6;   // batched shared-W variant
     if constexpr (sizeof(R) == 4) {
+        // 11: every system of the batch per CTA, W rows in registers (k_update_rows)
+        if (v == 11) {
+            if (qa > 0 && update_rows_run(n, qa, segA, segB, strideB, qb, w, strideW, out, strideO, act, nsys, coef,
+                                          strideC, partials, tickets, state, fin, skip_broken, st))
+                return 1;
+            v = 0;
+        }
         // 10: the whole update in one kernel, the shared part W c on the tensor cores and
         // subtracted from TMEM by the epilogue that streams w_s and V_s
         if (v == 10) {
@@ -4436,7 +4622,7 @@ void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename 
     int v = 0;
     if (forced_variant(1) >= 0) v = forced_variant(1);
     else if (representative(nsys, qa, qb) && !profile_enabled())
-        v = tuned_variant(prec_key<R>(), 1, n, nsys, qa, sizeof(R) == 4 ? 11 : 13, st, run);
+        v = tuned_variant(prec_key<R>(), 1, n, nsys, qa, sizeof(R) == 4 ? 12 : 13, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)
