@@ -1740,8 +1740,8 @@ __global__ void __launch_bounds__(NT, 2) k_update_wreg(int n, int kk, const type
 // systems, so W is read from memory once per launch and the shared part W c_s never goes
 // through memory (the tensor-core apply writes it and the per-system update reads it back,
 // 16 bytes a row a system on top of the algorithmic bytes).  CTAs own contiguous ranges of
-// 256-row chunks, about two a SM.  A system's V_s loads go out in batches of VB ahead of the
-// arithmetic, the shared part is computed while they are in flight.  Norm and cross term are
+// 256-row chunks, about two a SM.  Two systems' V loads go out together, VB vectors of each
+// ahead of the arithmetic, and the shared part is computed while they are in flight.  Norm and cross term are
 // summed per warp in FP32 butterflies (one FP64 warp instruction is ~64 scheduler clocks on
 // GB300, three FP64 butterflies per system per chunk would bound the kernel), accumulated per
 // warp in shared memory over the CTA's chunks and summed in FP64 once per CTA; the last CTA
@@ -1786,38 +1786,66 @@ __global__ void __launch_bounds__(NT, 2) k_update_rows(int n, int kk, const floa
         float2 wr[KW];
 #pragma unroll
         for (int p = 0; p < KW; ++p) wr[p] = (p < kk && in) ? W[(size_t)p * n + i] : czero<float2>();
-        for (int g = 0; g < nsys; ++g) {
-            const int s = s_act[g];
-            const bool live = in && s_live[g];
-            const float2 *cg = cs + (size_t)g * q;
-            const float2 *V = V0 + (size_t)s * strideV + i;
-            float2 vb[VB];
+        // two systems at a time: 2 (VB + 1) loads in flight before their products
+        for (int g = 0; g < nsys; g += 2) {
+            const bool two = g + 1 < nsys;
+            const int gb = two ? g + 1 : g;
+            const int sa = s_act[g], sb = s_act[gb];
+            const bool la = in && s_live[g], lb = in && two && s_live[gb];
+            const float2 *ca = cs + (size_t)g * q, *cb = cs + (size_t)gb * q;
+            const float2 *Va = V0 + (size_t)sa * strideV + i, *Vb = V0 + (size_t)sb * strideV + i;
+            float2 va[VB], vb[VB];
 #pragma unroll
-            for (int u = 0; u < VB; ++u) vb[u] = (live && u < qb) ? V[(size_t)u * n] : czero<float2>();
-            const float2 org = live ? w0[(size_t)s * strideW + i] : czero<float2>();
-            float2 acc = org;
+            for (int u = 0; u < VB; ++u) {
+                va[u] = (la && u < qb) ? Va[(size_t)u * n] : czero<float2>();
+                vb[u] = (lb && u < qb) ? Vb[(size_t)u * n] : czero<float2>();
+            }
+            const float2 oa = la ? w0[(size_t)sa * strideW + i] : czero<float2>();
+            const float2 ob = lb ? w0[(size_t)sb * strideW + i] : czero<float2>();
+            float2 aa = oa, ab = ob;
 #pragma unroll
             for (int p = 0; p < KW; ++p)
-                if (p < kk) cfms(acc, cg[p], wr[p]);
+                if (p < kk) {
+                    cfms(aa, ca[p], wr[p]);
+                    cfms(ab, cb[p], wr[p]);
+                }
 #pragma unroll
             for (int u = 0; u < VB; ++u)
-                if (u < qb) cfms(acc, cg[kk + u], vb[u]);
+                if (u < qb) {
+                    cfms(aa, ca[kk + u], va[u]);
+                    cfms(ab, cb[kk + u], vb[u]);
+                }
             for (int p0 = VB; p0 < qb; p0 += VB) {
 #pragma unroll
-                for (int u = 0; u < VB; ++u) vb[u] = (live && p0 + u < qb) ? V[(size_t)(p0 + u) * n] : czero<float2>();
+                for (int u = 0; u < VB; ++u) {
+                    va[u] = (la && p0 + u < qb) ? Va[(size_t)(p0 + u) * n] : czero<float2>();
+                    vb[u] = (lb && p0 + u < qb) ? Vb[(size_t)(p0 + u) * n] : czero<float2>();
+                }
 #pragma unroll
                 for (int u = 0; u < VB; ++u)
-                    if (p0 + u < qb) cfms(acc, cg[kk + p0 + u], vb[u]);
+                    if (p0 + u < qb) {
+                        cfms(aa, ca[kk + p0 + u], va[u]);
+                        cfms(ab, cb[kk + p0 + u], vb[u]);
+                    }
             }
-            if (live) out0[(size_t)s * strideO + i] = acc;
-            float2 ln = czero<float2>(), lc = czero<float2>();
-            cdotacc(ln, acc, acc);
-            cdotacc(lc, acc, org);
-            const float v0 = warp_sum(ln.x), v1 = warp_sum(lc.x), v2 = warp_sum(lc.y);
+            if (la) out0[(size_t)sa * strideO + i] = aa;
+            if (lb) out0[(size_t)sb * strideO + i] = ab;
+            float2 na = czero<float2>(), xa = czero<float2>(), nb = czero<float2>(), xb = czero<float2>();
+            cdotacc(na, aa, aa);
+            cdotacc(xa, aa, oa);
+            cdotacc(nb, ab, ab);
+            cdotacc(xb, ab, ob);
+            const float v0 = warp_sum(na.x), v1 = warp_sum(xa.x), v2 = warp_sum(xa.y);
+            const float v3 = warp_sum(nb.x), v4 = warp_sum(xb.x), v5 = warp_sum(xb.y);
             if (lane == 0) {
                 red[((size_t)g * 3 + 0) * NW + warp] += v0;
                 red[((size_t)g * 3 + 1) * NW + warp] += v1;
                 red[((size_t)g * 3 + 2) * NW + warp] += v2;
+                if (two) {
+                    red[((size_t)gb * 3 + 0) * NW + warp] += v3;
+                    red[((size_t)gb * 3 + 1) * NW + warp] += v4;
+                    red[((size_t)gb * 3 + 2) * NW + warp] += v5;
+                }
             }
         }
     }
@@ -3698,33 +3726,16 @@ __global__ void __launch_bounds__(NT) k_residual64(int n, const int *__restrict_
     double2 *r = r0 + (size_t)s * strideR;
     __shared__ double red[1][NW];
     double n2 = 0;
-    // A warp is one SELL slice and walks it whole (padding lanes past n included, their
-    // results dropped), so the test for a column of real values is warp-uniform: a real value
-    // takes two FP64 FMAs instead of four (the skipped products are zeros; the sums are the same
-    // but for the sign of a zero) and the FP64 pipe, which bounds this kernel, does 28 -> 16 a
-    // row on a 7-point operator with real off-diagonals.  The test reads the value's bits on
-    // the integer pipe.
-    for (int base = blockIdx.y * NT + (tid & ~31); base < n; base += G * NT) {
-        const int lane = tid & 31, row = base + lane, slice = base >> 5;
-        const bool ok = row < n;
-        double2 acc = ok ? b[row] : make_double2(0.0, 0.0);
+    for (int row = blockIdx.y * NT + tid; row < n; row += G * NT) {
+        double2 acc = b[row];
+        const int slice = row >> 5, lane = row & 31;
         const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
         for (int c = 0; c < width; ++c) {
             const int e = beg + c * 32 + lane;
-            const double2 a = vals[e];
-            const double2 xv = x[cols[e]];
-            const bool real = (__double_as_longlong(a.y) << 1) == 0;
-            if (__all_sync(0xffffffffu, real)) {
-                acc.x = rfma(-a.x, xv.x, acc.x);
-                acc.y = rfma(-a.x, xv.y, acc.y);
-            } else {
-                cfms(acc, a, xv);
-            }
+            cfms(acc, vals[e], x[cols[e]]);
         }
-        if (ok) {
-            r[row] = acc;
-            n2 += acc.x * acc.x + acc.y * acc.y;
-        }
+        r[row] = acc;
+        n2 += acc.x * acc.x + acc.y * acc.y;
     }
     double v[1] = {n2};
     block_sum<1>(v, red);
@@ -4300,10 +4311,10 @@ inline bool update_rows_run(int n, int kk, const float2 *W, const float2 *V, siz
         kernel<<<G, NT, smem, st>>>(n, kk, W, V, strideV, qb, w, strideW, out, strideO, act, nsys, coef, strideC, cpb,
                                     (double *)partials, tickets, state, fin, skip_broken ? 1 : 0);
     };
-    if (kk <= 8) go(k_update_rows<8, 16>);
-    else if (kk <= 16) go(k_update_rows<16, 16>);
-    else if (kk <= 24) go(k_update_rows<24, 16>);
-    else go(k_update_rows<32, 8>);
+    if (kk <= 8) go(k_update_rows<8, 8>);
+    else if (kk <= 16) go(k_update_rows<16, 8>);
+    else if (kk <= 24) go(k_update_rows<24, 8>);
+    else go(k_update_rows<32, 4>);
     return true;
 }
 

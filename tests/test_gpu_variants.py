@@ -70,16 +70,20 @@ def test_pinned_variant_solves_the_batch(batch20, precision, pair):
 def test_grouped_combination_matches_one_system_a_cta(batch20, precision):
     """The cycle-end combination four systems a CTA (W and Z loaded once for the four) against
     one system a CTA: the same per-element operations, so both batches converge alike and to
-    the direct solution."""
+    the direct solution.  The Gram-Schmidt variants are pinned for both runs: with the tuner,
+    the first run's launches before its tuning take variant 0 and the second run's the tuned
+    one, and complex64 cycle counts follow such rounding differences by several cycles."""
     A, rhs, cfg, direct = batch20
     out = {}
     for grouped in (True, False):
         gdmr.combine_group(grouped)
+        gdmr.tune_force(0, 0)
         try:
             s = gdmr.System(A, cfg["m"], cfg["k"], capacity=NRHS, precision=precision)
             out[grouped] = s.solve_batch(rhs, tol=1e-10, max_cycles=2000)
         finally:
             gdmr.combine_group(True)
+            gdmr.tune_force(-1, -1)
     for grouped, (X, stats) in out.items():
         assert all(st["status"] == 0 and st["true_rel_res"] <= 1.5e-10 for st in stats), grouped
         err = np.linalg.norm(X - direct, axis=1) / np.linalg.norm(direct, axis=1)
