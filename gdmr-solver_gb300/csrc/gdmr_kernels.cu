@@ -2519,17 +2519,31 @@ __global__ void __launch_bounds__(NT) k_zupdate(int n, int kk, int m, int k, int
     WR nrm_w[KB];
 #pragma unroll
     for (int t = 0; t < KB; ++t) nrm_w[t] = WR(0.f);
+    // basis values are loaded PA steps ahead of their products (a ring of raw values), so a
+    // thread has PA loads in flight instead of waiting on each one
+    constexpr int PA = sizeof(C) == 8 ? 4 : 2;
+    auto ld = [&](int p, long i) -> C { return p < kk ? Z[(size_t)p * n + i] : V[(size_t)(p - kk) * n + i]; };
     for (long i = (long)blockIdx.x * NT + tid; i < n; i += (long)G * NT) {
         W acc[KB];
 #pragma unroll
         for (int t = 0; t < KB; ++t) acc[t] = czero<W>();
-        for (int p = 0; p < m; ++p) {
-            const W b = zin(p < kk ? Z[(size_t)p * n + i] : V[(size_t)(p - kk) * n + i]);
+        C pf[PA];
 #pragma unroll
-            for (int t = 0; t < KB; ++t) {
-                cfma(acc[t], cs[p * KB + t], b);
-                if constexpr (DF)
-                    if ((p & 3) == 3) acc[t] = canon(acc[t]);
+        for (int u = 0; u < PA; ++u) pf[u] = u < m ? ld(u, i) : czero<C>();
+        for (int p0 = 0; p0 < m; p0 += PA) {
+#pragma unroll
+            for (int u = 0; u < PA; ++u) {
+                const int p = p0 + u;
+                if (p < m) {
+                    const W b = zin(pf[u]);
+                    if (p + PA < m) pf[u] = ld(p + PA, i);
+#pragma unroll
+                    for (int t = 0; t < KB; ++t) {
+                        cfma(acc[t], cs[p * KB + t], b);
+                        if constexpr (DF)
+                            if ((p & 3) == 3) acc[t] = canon(acc[t]);
+                    }
+                }
             }
         }
 #pragma unroll
@@ -2546,7 +2560,9 @@ __global__ void __launch_bounds__(NT) k_zupdate(int n, int kk, int m, int k, int
     block_sum<KB>(nrm, red);
     double *part = (double *)partials;
     if (tid == 0)
-        for (int t = 0; t < nt; ++t) part[(size_t)t * G + blockIdx.x] = nrm[t];
+#pragma unroll
+        for (int t = 0; t < KB; ++t)
+            if (t < nt) part[(size_t)t * G + blockIdx.x] = nrm[t];
     if (!arrive_last(ticket, gridDim.x)) return;
     __syncthreads();
     double tot[KB];
@@ -2559,7 +2575,9 @@ __global__ void __launch_bounds__(NT) k_zupdate(int n, int kk, int m, int k, int
     }
     block_sum<KB>(tot, red);
     if (tid == 0) {
-        for (int t = 0; t < nt; ++t) znorm2[t0 + t] = tot[t];
+#pragma unroll
+        for (int t = 0; t < KB; ++t)
+            if (t < nt) znorm2[t0 + t] = tot[t];
         *ticket = 0;
     }
 }
@@ -3726,16 +3744,48 @@ __global__ void __launch_bounds__(NT) k_residual64(int n, const int *__restrict_
     double2 *r = r0 + (size_t)s * strideR;
     __shared__ double red[1][NW];
     double n2 = 0;
-    for (int row = blockIdx.y * NT + tid; row < n; row += G * NT) {
-        double2 acc = b[row];
-        const int slice = row >> 5, lane = row & 31;
+    // This kernel is FP64-rate bound (28 FP64 FMAs a 7-point row against 48 bytes of HBM).  A
+    // warp is one SELL slice and walks it whole (padding lanes past n included, their results
+    // dropped); it loads every entry of its rows and their x values first, then, per column slot,
+    // a warp vote on the values' bits (integer pipe) sends a slot whose values are all real
+    // through two FMAs instead of four: the skipped products are zeros, so the sums are the same
+    // but for the sign of a zero.  A 7-point Helmholtz row (real off-diagonals) takes 16.
+    constexpr int WMAX = SELL_PATTERN;
+    const int lane = tid & 31;
+    for (int base = blockIdx.y * NT + (tid & ~31); base < n; base += G * NT) {
+        const int row = base + lane, slice = base >> 5;
+        const bool ok = row < n;
+        double2 acc = ok ? b[row] : make_double2(0.0, 0.0);
         const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
-        for (int c = 0; c < width; ++c) {
-            const int e = beg + c * 32 + lane;
-            cfms(acc, vals[e], x[cols[e]]);
+        if (width <= WMAX) {
+            double2 av[WMAX], xv[WMAX];
+#pragma unroll
+            for (int c = 0; c < WMAX; ++c)
+                if (c < width) av[c] = vals[beg + c * 32 + lane];
+#pragma unroll
+            for (int c = 0; c < WMAX; ++c)
+                if (c < width) xv[c] = x[cols[beg + c * 32 + lane]];
+#pragma unroll
+            for (int c = 0; c < WMAX; ++c) {
+                if (c >= width) break;
+                const bool real = (__double_as_longlong(av[c].y) << 1) == 0;
+                if (__all_sync(0xffffffffu, real)) {
+                    acc.x = rfma(-av[c].x, xv[c].x, acc.x);
+                    acc.y = rfma(-av[c].x, xv[c].y, acc.y);
+                } else {
+                    cfms(acc, av[c], xv[c]);
+                }
+            }
+        } else {
+            for (int c = 0; c < width; ++c) {
+                const int e = beg + c * 32 + lane;
+                cfms(acc, vals[e], x[cols[e]]);
+            }
         }
-        r[row] = acc;
-        n2 += acc.x * acc.x + acc.y * acc.y;
+        if (ok) {
+            r[row] = acc;
+            n2 += acc.x * acc.x + acc.y * acc.y;
+        }
     }
     double v[1] = {n2};
     block_sum<1>(v, red);
