@@ -140,6 +140,27 @@ template <int NV> __device__ __forceinline__ void block_sum(double (&v)[NV], dou
         }
 }
 
+// Block-wide sum of NV floats per thread, warp sums in FP32 (an FP64 warp butterfly is five FP64
+// warp instructions, ~20 SM clocks each on GB300, per value and CTA) and the warps' sums added in
+// FP64 in warp order; result valid in thread 0.
+template <int NV> __device__ __forceinline__ void block_sum_f(const float (&f)[NV], double (&v)[NV], double (*red)[NW]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+        const float s = warp_sum(f[j]);
+        if (lane == 0) red[j][warp] = (double)s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+            double s = 0;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) s += red[j][w];
+            v[j] = s;
+        }
+}
+
 // Last-CTA-done protocol: returns true in every thread of the CTA that arrived last.
 __device__ __forceinline__ bool arrive_last(unsigned *ticket, unsigned count) {
     __shared__ unsigned s_last;
@@ -454,8 +475,16 @@ __global__ void __launch_bounds__(NT, PF ? 2 : min_blocks<typename CT<R>::t>(EPT
             cdotacc(lc, acc[e].v[j], org[e].v[j]);
         }
     }
-    double v[3] = {(double)ln.x, (double)lc.x, (double)lc.y};
-    block_sum<3>(v, red);
+    double v[3];
+    if constexpr (std::is_same<C, float2>::value) {
+        const float f[3] = {ln.x, lc.x, lc.y};
+        block_sum_f<3>(f, v, red);
+    } else {
+        v[0] = (double)ln.x;
+        v[1] = (double)lc.x;
+        v[2] = (double)lc.y;
+        block_sum<3>(v, red);
+    }
     double *part = (double *)partials + (size_t)slot * 3 * G;
     if (tid == 0) {
         part[chunk] = v[0];
@@ -2407,6 +2436,7 @@ __global__ void __launch_bounds__(NT) k_combine_grp(int n, int kk, int m, const 
         }
     }
     double v[SB];
+    float fv[SB];
 #pragma unroll
     for (int g = 0; g < SB; ++g) {
         C ln = czero<C>();
@@ -2422,8 +2452,10 @@ __global__ void __launch_bounds__(NT) k_combine_grp(int n, int kk, int m, const 
             cdotacc(ln, ra_[g][e], ra_[g][e]);
         }
         v[g] = (double)ln.x;
+        if constexpr (std::is_same<C, float2>::value) fv[g] = ln.x;
     }
-    block_sum<SB>(v, red);
+    if constexpr (std::is_same<C, float2>::value) block_sum_f<SB>(fv, v, red);
+    else block_sum<SB>(v, red);
     if (tid == 0)
         for (int g = 0; g < ns; ++g) ((double *)partials)[(size_t)(g0 + g) * G + chunk] = v[g];
     for (int g = 0; g < ns; ++g) {
@@ -2554,32 +2586,31 @@ __global__ void __launch_bounds__(NT) k_zupdate(int n, int kk, int m, int k, int
             if constexpr (DF) nrm_w[t] = canon(dfc{nrm_w[t], dfr(0.f, 0.f)}).x;
         }
     }
-    double nrm[KB];
-#pragma unroll
-    for (int t = 0; t < KB; ++t) nrm[t] = (double)nrm_w[t];
-    block_sum<KB>(nrm, red);
-    double *part = (double *)partials;
-    if (tid == 0)
-#pragma unroll
-        for (int t = 0; t < KB; ++t)
-            if (t < nt) part[(size_t)t * G + blockIdx.x] = nrm[t];
-    if (!arrive_last(ticket, gridDim.x)) return;
-    __syncthreads();
-    double tot[KB];
+    // column norms: warp sums in the working type (FP32 or double-float butterflies; FP64 warp
+    // arithmetic is slow on GB300), the CTA's warps summed in FP64 by one thread per column, and
+    // the last CTA sums the CTAs' partials, one warp per column, in a fixed order
+    const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
     for (int t = 0; t < KB; ++t) {
+        const WR v = warp_sum(nrm_w[t]);
+        if (lane == 0) red[t][warp] = (double)v;
+    }
+    __syncthreads();
+    double *part = (double *)partials;
+    if (tid < nt) {
         double sacc = 0;
-        if (t < nt)
-            for (int g = tid; g < G; g += NT) sacc += __ldcg(part + (size_t)t * G + g);
-        tot[t] = sacc;
-    }
-    block_sum<KB>(tot, red);
-    if (tid == 0) {
 #pragma unroll
-        for (int t = 0; t < KB; ++t)
-            if (t < nt) znorm2[t0 + t] = tot[t];
-        *ticket = 0;
+        for (int w = 0; w < NW; ++w) sacc += red[tid][w];
+        part[(size_t)tid * G + blockIdx.x] = sacc;
     }
+    if (!arrive_last(ticket, gridDim.x)) return;
+    for (int t = warp; t < nt; t += NW) {
+        double sacc = 0;
+        for (int g = lane; g < G; g += 32) sacc += __ldcg(part + (size_t)t * G + g);
+        sacc = warp_sum(sacc);
+        if (lane == 0) znorm2[t0 + t] = sacc;
+    }
+    if (tid == 0) *ticket = 0;
 }
 
 template <class R>
@@ -3744,48 +3775,16 @@ __global__ void __launch_bounds__(NT) k_residual64(int n, const int *__restrict_
     double2 *r = r0 + (size_t)s * strideR;
     __shared__ double red[1][NW];
     double n2 = 0;
-    // This kernel is FP64-rate bound (28 FP64 FMAs a 7-point row against 48 bytes of HBM).  A
-    // warp is one SELL slice and walks it whole (padding lanes past n included, their results
-    // dropped); it loads every entry of its rows and their x values first, then, per column slot,
-    // a warp vote on the values' bits (integer pipe) sends a slot whose values are all real
-    // through two FMAs instead of four: the skipped products are zeros, so the sums are the same
-    // but for the sign of a zero.  A 7-point Helmholtz row (real off-diagonals) takes 16.
-    constexpr int WMAX = SELL_PATTERN;
-    const int lane = tid & 31;
-    for (int base = blockIdx.y * NT + (tid & ~31); base < n; base += G * NT) {
-        const int row = base + lane, slice = base >> 5;
-        const bool ok = row < n;
-        double2 acc = ok ? b[row] : make_double2(0.0, 0.0);
+    for (int row = blockIdx.y * NT + tid; row < n; row += G * NT) {
+        double2 acc = b[row];
+        const int slice = row >> 5, lane = row & 31;
         const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
-        if (width <= WMAX) {
-            double2 av[WMAX], xv[WMAX];
-#pragma unroll
-            for (int c = 0; c < WMAX; ++c)
-                if (c < width) av[c] = vals[beg + c * 32 + lane];
-#pragma unroll
-            for (int c = 0; c < WMAX; ++c)
-                if (c < width) xv[c] = x[cols[beg + c * 32 + lane]];
-#pragma unroll
-            for (int c = 0; c < WMAX; ++c) {
-                if (c >= width) break;
-                const bool real = (__double_as_longlong(av[c].y) << 1) == 0;
-                if (__all_sync(0xffffffffu, real)) {
-                    acc.x = rfma(-av[c].x, xv[c].x, acc.x);
-                    acc.y = rfma(-av[c].x, xv[c].y, acc.y);
-                } else {
-                    cfms(acc, av[c], xv[c]);
-                }
-            }
-        } else {
-            for (int c = 0; c < width; ++c) {
-                const int e = beg + c * 32 + lane;
-                cfms(acc, vals[e], x[cols[e]]);
-            }
+        for (int c = 0; c < width; ++c) {
+            const int e = beg + c * 32 + lane;
+            cfms(acc, vals[e], x[cols[e]]);
         }
-        if (ok) {
-            r[row] = acc;
-            n2 += acc.x * acc.x + acc.y * acc.y;
-        }
+        r[row] = acc;
+        n2 += acc.x * acc.x + acc.y * acc.y;
     }
     double v[1] = {n2};
     block_sum<1>(v, red);
