@@ -290,6 +290,21 @@ int sell_from_csr(DeviceSell &out, int n, const int *rowptr, const int *colidx, 
     d.band = band;
     d.npat = np;
     for (int e = 0; e < np; ++e) d.pat[e] = pat[e];
+    // pattern entries that are real in every pattern-stored slice (conservatively: no CSR value
+    // stored there has a non-zero imaginary part; padding zeros are real)
+    if (np > 0) {
+        unsigned real = (1u << np) - 1u;
+        for (int s = 0; s < ns && real; ++s) {
+            if (!uni[s]) continue;
+            for (int r = s * 32; r < std::min(n, s * 32 + 32); ++r)
+                for (int q = rowptr[r]; q < rowptr[r + 1]; ++q)
+                    if (vals_ri[2 * (size_t)q + 1] != 0.0) {
+                        const int e = (int)(std::find(pat.begin(), pat.end(), colidx[q] - r) - pat.begin());
+                        real &= ~(1u << e);
+                    }
+        }
+        d.preal = real;
+    }
     SELL_CK_(cudaGetDevice(&d.device));
     SELL_CK_(cudaMalloc(&d.slice_ptr, sizeof(int) * (ns + 1)));
     SELL_CK_(cudaMalloc(&d.cols, sizeof(int) * std::max<long>(padded, 1)));

@@ -50,6 +50,7 @@ struct DeviceSell {
     dfc *griddf = nullptr;
     int gx = 0, gy = 0, gz = 0;
     unsigned greal = 0;                // bit p: plane p is real (imaginary parts all zero)
+    unsigned preal = 0;                // bit e: entry e of every pattern-stored slice is real
     SellMatrix view(const void *v, const void *g) const {
         SellMatrix m{n, nslices, slice_ptr, cols, v, nnz};
         m.uniform = uniform;
@@ -60,6 +61,7 @@ struct DeviceSell {
         m.gy = gy;
         m.gz = gz;
         m.greal = greal;
+        m.preal = preal;
         return m;
     }
     SellMatrix view32() const { return view(vals32, grid32); }

@@ -1370,7 +1370,9 @@ __global__ void __launch_bounds__(KM_THREADS, 3) k_krylov_multi(const KrylovJob<
             }
 #pragma unroll
             for (int u = 0; u < KM_PB; ++u) {
-                const double re = warp_sum((double)acc[u].x), im = warp_sum((double)acc[u].y);
+                // warp sums in the working precision: FP32 butterflies for complex64 (an FP64 warp
+                // instruction is ~20 SM clocks on GB300)
+                const double re = (double)warp_sum(acc[u].x), im = (double)warp_sum(acc[u].y);
                 if (lane == 0) {
                     wsum[warp][u][0] = re;
                     wsum[warp][u][1] = im;
@@ -1402,7 +1404,9 @@ __global__ void __launch_bounds__(KM_THREADS, 3) k_krylov_multi(const KrylovJob<
         // their products); ||out||^2 and <out, y> partials
         for (int p = tid; p < q; p += KM_THREADS) cs[p] = from_d<C>(__ldcg(coef + p));
         __syncthreads();
-        double v0 = 0, v1 = 0, v2 = 0;
+        // per-thread norm accumulators in FP32 for complex64 (no FP64 operation per element)
+        using NA = typename std::conditional<std::is_same<C, float2>::value, float, double>::type;
+        NA v0 = 0, v1 = 0, v2 = 0;
         for (int sl = gw; sl < nsl; sl += nw) {
             const int row = sl * 32 + lane;
             if (row >= n) continue;
@@ -1422,14 +1426,14 @@ __global__ void __launch_bounds__(KM_THREADS, 3) k_krylov_multi(const KrylovJob<
             C ln = czero<C>(), lc = czero<C>();
             cdotacc(ln, w, w);
             cdotacc(lc, w, yv);
-            v0 += (double)canon(ln).x;
-            v1 += (double)canon(lc).x;
-            v2 += (double)canon(lc).y;
+            v0 += (NA)canon(ln).x;
+            v1 += (NA)canon(lc).x;
+            v2 += (NA)canon(lc).y;
         }
         v0 = warp_sum(v0);
         v1 = warp_sum(v1);
         v2 = warp_sum(v2);
-        if (lane == 0) { red[warp][0] = v0; red[warp][1] = v1; red[warp][2] = v2; }
+        if (lane == 0) { red[warp][0] = (double)v0; red[warp][1] = (double)v1; red[warp][2] = (double)v2; }
         __syncthreads();
         if (tid < 3) {
             double t = 0;
@@ -2177,8 +2181,16 @@ __global__ void __launch_bounds__(NT, 2)
                 cdotacc(lc, acc[g][e], org[g][e]);
             }
         }
-        double v[3] = {(double)ln.x, (double)lc.x, (double)lc.y};
-        block_sum<3>(v, red);
+        double v[3];
+        if constexpr (std::is_same<C, float2>::value) {
+            const float f[3] = {ln.x, lc.x, lc.y};
+            block_sum_f<3>(f, v, red);
+        } else {
+            v[0] = (double)ln.x;
+            v[1] = (double)lc.x;
+            v[2] = (double)lc.y;
+            block_sum<3>(v, red);
+        }
         if (tid == 0 && g < ns) {
             double *part = (double *)partials + (size_t)(slot0 + g) * 3 * G;
             part[chunk] = v[0];
@@ -2316,7 +2328,12 @@ __global__ void __launch_bounds__(NT) k_combine(int n, int kk, int m, const type
         cdotacc(ln, ra_[e], ra_[e]);
     }
     double v[1] = {(double)ln.x};
-    block_sum<1>(v, red);
+    if constexpr (std::is_same<C, float2>::value) {
+        const float f[1] = {ln.x};
+        block_sum_f<1>(f, v, red);
+    } else {
+        block_sum<1>(v, red);
+    }
     double *part = (double *)partials + (size_t)slot * G;
     if (tid == 0) part[chunk] = v[0];
     if (!arrive_last(&tickets[slot], G)) return;
@@ -3550,12 +3567,20 @@ __global__ void __launch_bounds__(NT) k_grid_spmm(int nx, int ny, int nz, int ng
     long idx = (long)iy * nx + ix + (long)z0 * plane;
     const C *xs[SG];
     C below[SG], cur[SG];
+    R al[SG];      // pending normalisation factors, converted once (a double -> float conversion
+    bool bk[SG];   // is an FP64-pipe instruction on GB300)
 #pragma unroll
     for (int g = 0; g < SG; ++g) {
+        al[g] = R(1.0);
+        bk[g] = false;
         if (g < ng) {
             xs[g] = x0 + (size_t)act[g0 + g] * strideX;
             below[g] = z0 > 0 ? xs[g][idx - plane] : czero<C>();
             cur[g] = xs[g][idx];
+            if (scale) {
+                al[g] = (R)scale[act[g0 + g]].alpha;
+                bk[g] = scale[act[g0 + g]].broken != 0;
+            }
         }
     }
     const bool xl = ix > 0, xh = ix + 1 < nx, yl = iy > 0, yh = iy + 1 < ny;
@@ -3584,14 +3609,12 @@ __global__ void __launch_bounds__(NT) k_grid_spmm(int nx, int ny, int nz, int ng
                 if (zh) cfma_r(acc, apP, above, rpP);
                 const int sys = act[g0 + g];
                 if (scale) {   // pending normalisation, as in k_spmm
-                    const SysState &stt = scale[sys];
-                    const R al = (R)stt.alpha;
                     C v = cur[g];
-                    v.x = v.x * al;
-                    v.y = v.y * al;
-                    acc.x = acc.x * al;
-                    acc.y = acc.y * al;
-                    if (stt.broken) v = czero<C>();
+                    v.x = v.x * al[g];
+                    v.y = v.y * al[g];
+                    acc.x = acc.x * al[g];
+                    acc.y = acc.y * al[g];
+                    if (bk[g]) v = czero<C>();
                     vout0[(size_t)sys * strideVO + idx] = canon(v);
                 }
                 y0[(size_t)sys * strideY + idx] = canon(acc);
@@ -3692,17 +3715,26 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
     const int ng = min(SG, nsys - g0);
     // With `scale`, x_s is the unnormalised Krylov vector w_s: y_s = a_s (A w_s) and the row's
     // basis entry v_s = a_s w_s goes to vout_s (a_s = state[s].alpha; zeros after a breakdown),
-    // which spares the normalisation kernel its pass over w.
-    auto fin = [&](int sys, long row, C acc, const C *x) {
+    // which spares the normalisation kernel its pass over w.  The factors are converted once per
+    // CTA: a double -> float conversion per row and system would be an FP64-pipe instruction
+    // per element on GB300.
+    __shared__ R s_al[SG];
+    __shared__ int s_bk[SG];
+    if (scale && (int)threadIdx.x < ng) {
+        const SysState &stt = scale[act[g0 + threadIdx.x]];
+        s_al[threadIdx.x] = (R)stt.alpha;
+        s_bk[threadIdx.x] = stt.broken;
+    }
+    __syncthreads();
+    auto fin = [&](int g, int sys, long row, C acc, const C *x) {
         if (scale) {
-            const SysState &stt = scale[sys];
-            const R al = (R)stt.alpha;
+            const R al = s_al[g];
             C v = x[row];
             v.x = v.x * al;
             v.y = v.y * al;
             acc.x = acc.x * al;
             acc.y = acc.y * al;
-            if (stt.broken) v = czero<C>();
+            if (s_bk[g]) v = czero<C>();
             vout0[(size_t)sys * strideVO + row] = canon(v);
         }
         y0[(size_t)sys * strideY + row] = canon(acc);
@@ -3736,8 +3768,8 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
                         cfma(a1, v[e], xb[c[e]]);
                     }
                 }
-                fin(s0, row, a0, xa);
-                fin(s1, row, a1, xb);
+                fin(g, s0, row, a0, xa);
+                fin(g + 1, s1, row, a1, xb);
             }
             if (g < ng) {
                 const int s0 = act[g0 + g];
@@ -3746,7 +3778,7 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
 #pragma unroll
                 for (int e = 0; e < WMAX; ++e)
                     if (e < width) cfma(a0, v[e], xa[c[e]]);
-                fin(s0, row, a0, xa);
+                fin(g, s0, row, a0, xa);
             }
         } else {
             for (int g = 0; g < ng; ++g) {
@@ -3757,18 +3789,28 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
                     const int idx = beg + e * 32 + lane;
                     cfma(acc, vals[idx], x[cols[idx]]);
                 }
-                fin(s, row, acc, x);
+                fin(g, s, row, acc, x);
             }
         }
     }
 }
 
+// Pattern entries of the FP64 residual: idx lists the entries with complex values before the
+// real ones, off[j] the column offset of entry idx[j].
+struct ResidPattern {
+    const unsigned char *uniform;
+    int idx[SELL_PATTERN];
+    int off[SELL_PATTERN];
+};
+
 // r = b - A x in FP64 with ||r||^2 reduced; last CTA sets true_res and alpha.
+template <int NCX, int WID>
 __global__ void __launch_bounds__(NT) k_residual64(int n, const int *__restrict__ slice_ptr, const int *__restrict__ cols,
                                                    const double2 *__restrict__ vals, const double2 *__restrict__ b0,
                                                    size_t strideB, const double2 *__restrict__ x0, size_t strideX,
                                                    double2 *__restrict__ r0, size_t strideR, const int *__restrict__ act,
-                                                   double2 *__restrict__ partials, unsigned *tickets, SysState *state) {
+                                                   double2 *__restrict__ partials, unsigned *tickets, SysState *state,
+                                                   ResidPattern rp) {
     const int slot = blockIdx.x, s = act[slot], G = gridDim.y, tid = threadIdx.x;
     const double2 *b = b0 + (size_t)s * strideB;
     const double2 *x = x0 + (size_t)s * strideX;
@@ -3779,9 +3821,30 @@ __global__ void __launch_bounds__(NT) k_residual64(int n, const int *__restrict_
         double2 acc = b[row];
         const int slice = row >> 5, lane = row & 31;
         const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
-        for (int c = 0; c < width; ++c) {
-            const int e = beg + c * 32 + lane;
-            cfms(acc, vals[e], x[cols[e]]);
+        if (WID > 0 && rp.uniform[slice]) {
+            // pattern-stored slice (WID entries): its NCX complex entries with four FP64 FMAs,
+            // then its real ones (zero imaginary parts, host-checked) with two.  The kernel is
+            // FP64-rate bound; a 7-point Helmholtz row goes from 28 FMAs to 16.  Both loops have
+            // compile-time trip counts: nothing is predicated, and the entry list stays in the
+            // parameter space.
+#pragma unroll
+            for (int j = 0; j < NCX; ++j) {
+                const int c = rp.idx[j];
+                cfms(acc, vals[beg + c * 32 + lane], x[row + rp.off[j]]);
+            }
+#pragma unroll
+            for (int j = NCX; j < WID; ++j) {
+                const int c = rp.idx[j];
+                const double a = vals[beg + c * 32 + lane].x;
+                const double2 xv = x[row + rp.off[j]];
+                acc.x = rfma(-a, xv.x, acc.x);
+                acc.y = rfma(-a, xv.y, acc.y);
+            }
+        } else {
+            for (int c = 0; c < width; ++c) {
+                const int e = beg + c * 32 + lane;
+                cfms(acc, vals[e], x[cols[e]]);
+            }
         }
         r[row] = acc;
         n2 += acc.x * acc.x + acc.y * acc.y;
@@ -4976,10 +5039,33 @@ void launch_residual64(const SellMatrix &A, const double2 *b, size_t strideB, co
                        SysState *state, cudaStream_t st) {
     if (nsys <= 0) return;
     Launch L_(KC_RESID64, spmm_bytes(A, sizeof(double2), nsys) + (double)sizeof(double2) * A.n * nsys, st, 1);
-    k_residual64<<<grid2(nsys, capped_grid(A.n, nsys, 8)), NT, 0, st>>>(A.n, A.slice_ptr, A.cols,
-                                                                        (const double2 *)A.vals, b, strideB, x,
-                                                                        strideX, r, strideR, act, partials, tickets,
-                                                                        state);
+    // pattern entries in the order complex first, real after (an entry is real when it is real
+    // in every pattern-stored slice); instances for 5- and 7-entry patterns with up to two
+    // complex entries, the plain loop otherwise
+    ResidPattern rp{};
+    int ncx = -1;
+    if (A.npat > 0 && A.uniform && A.preal) {
+        rp.uniform = A.uniform;
+        int j = 0;
+        for (int e = 0; e < A.npat; ++e)
+            if (!(A.preal >> e & 1u)) rp.idx[j++] = e;
+        ncx = j;
+        for (int e = 0; e < A.npat; ++e)
+            if (A.preal >> e & 1u) rp.idx[j++] = e;
+        for (int q = 0; q < A.npat; ++q) rp.off[q] = A.pat[rp.idx[q]];
+    }
+    const dim3 grid = grid2(nsys, capped_grid(A.n, nsys, 8));
+    auto go = [&](auto kernel) {
+        kernel<<<grid, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const double2 *)A.vals, b, strideB, x, strideX, r,
+                                    strideR, act, partials, tickets, state, rp);
+    };
+    if (A.npat == 7 && ncx == 1) go(k_residual64<1, 7>);
+    else if (A.npat == 7 && ncx == 0) go(k_residual64<0, 7>);
+    else if (A.npat == 7 && ncx == 2) go(k_residual64<2, 7>);
+    else if (A.npat == 5 && ncx == 1) go(k_residual64<1, 5>);
+    else if (A.npat == 5 && ncx == 0) go(k_residual64<0, 5>);
+    else if (A.npat == 5 && ncx == 2) go(k_residual64<2, 5>);
+    else go(k_residual64<0, 0>);
 }
 
 template <class R>

@@ -335,6 +335,7 @@ struct SellMatrix {
     const void *grid = nullptr;
     int gx = 0, gy = 0, gz = 0;
     unsigned greal = 0;   // bit p: every value of plane p has a zero imaginary part
+    unsigned preal = 0;   // bit e: entry e of every pattern-stored slice has a zero imaginary part
 };
 // Process-wide switch for the structured-grid operator kernel (on by default); launch_spmm
 // takes the SELL kernels when it is off or the matrix has no grid form.  grid_batch: systems a

@@ -42,8 +42,8 @@
 namespace gdmr {
 namespace {
 
-constexpr int TC_PRODUCERS = 768;              // warps 0-23 load, split and store operand tiles
-constexpr int TC_MMA_WARP = TC_PRODUCERS / 32; // warp 24 issues the MMAs
+constexpr int TC_PRODUCERS = 512;              // warps 0-15 load, split and store operand tiles
+constexpr int TC_MMA_WARP = TC_PRODUCERS / 32; // warp 16 issues the MMAs
 constexpr int TC_THREADS = TC_PRODUCERS + 32;
 constexpr int TC_KT = 32;                      // complex elements per K tile
 constexpr int TC_KCH = 2 * TC_KT / 4;          // 16-byte chunks per operand row per tile (2 swizzle atoms)

@@ -83,3 +83,43 @@ def test_unstructured_matrix_has_no_pattern():
     indices = np.concatenate([np.sort(rng.choice(n, per_row, replace=False)) for _ in range(n)])
     data = rng.standard_normal(n * per_row) + 1j * rng.standard_normal(n * per_row)
     _check(CSR(n, indptr, indices, data), 7)
+
+
+def _with_complex_entry(A, row, col, value):
+    S = A.to_scipy().tolil()
+    S[row, col] = value
+    S = S.tocsr()
+    S.sort_indices()
+    return CSR(A.n, S.indptr.astype(np.int32), S.indices.astype(np.int32), S.data.astype(np.complex128))
+
+
+@pytest.mark.parametrize("case", ["helmholtz3d", "one_complex_offdiag", "all_complex", "helmholtz2d"])
+def test_fp64_residual_real_pattern_entries(case):
+    """The FP64 true residual takes two FMAs instead of four for pattern entries that are real in
+    every pattern-stored slice (the Helmholtz off-diagonals), decided on the host.  Against numpy
+    ||b - A x|| / ||b|| to 1e-13: a 3D 7-point operator (one complex entry, the diagonal), the same
+    with one complex off-diagonal value in one interior row (that entry is then complex in every
+    slice), a 7-point operator with complex values everywhere (the plain loop), and a 2D 5-point
+    operator."""
+    rng = np.random.default_rng(11)
+    if case == "helmholtz2d":
+        A = problems.helmholtz((40, 33), 9.0, 0.1)
+    else:
+        A = problems.helmholtz((14, 12, 11), 6.0, 0.1)
+    if case == "one_complex_offdiag":
+        r = A.n // 2
+        A = _with_complex_entry(A, r, r + 1, -1.0 + 0.25j)
+    if case == "all_complex":
+        S = A.to_scipy().tocsr()
+        S.data = S.data + 1j * rng.uniform(0.1, 0.5, S.nnz)
+        A = CSR(A.n, S.indptr.astype(np.int32), S.indices.astype(np.int32), S.data.astype(np.complex128))
+    s = gdmr.System(A, 10, 2, capacity=3, precision="mixed")
+    try:
+        B = rng.standard_normal((3, A.n)) + 1j * rng.standard_normal((3, A.n))
+        X = rng.standard_normal((3, A.n)) + 1j * rng.standard_normal((3, A.n))
+        rel = s.true_residual(B, X)
+    finally:
+        s.close()
+    S = A.to_scipy()
+    ref = np.array([np.linalg.norm(b - S @ x) / np.linalg.norm(b) for b, x in zip(B, X)])
+    assert np.max(np.abs(rel - ref) / ref) < 1e-13, (rel, ref)
