@@ -409,6 +409,7 @@ extern "C" double gdmrWaitLimit(double ms) {
 }
 extern "C" void gdmrInjectAllocFailure(int nth) { inject_alloc_failure(nth); }
 extern "C" void gdmrCombineGroup(int enable) { set_combine_group(enable); }
+extern "C" void gdmrSpmmPair(int enable) { set_spmm_pair(enable); }
 extern "C" void gdmrProfile(int on) { profile_enable(on != 0); }
 extern "C" void gdmrProfileReset(void) { profile_reset(); }
 extern "C" void gdmrTune(int on) { tune_enable(on != 0); }
@@ -1232,31 +1233,22 @@ int noalloc_scratch(int device, NoallocScratch *out) {
 
 // One kernel: ||b - A x||^2 and ||b||^2 per right-hand side over a grid-stride row loop, CTA
 // partials into the static scratch, the last CTA of each right-hand side sums them in order.
+template <int NCX, int WID>
 __global__ void __launch_bounds__(256) k_relres_noalloc(int n, const int *__restrict__ slice_ptr,
                                                         const int *__restrict__ cols,
                                                         const double2 *__restrict__ vals,
                                                         const double2 *__restrict__ b0,
                                                         const double2 *__restrict__ x0, double *partials,
-                                                        unsigned *tickets, double *relres) {
+                                                        unsigned *tickets, double *relres, ResidPattern rp) {
     const int s = blockIdx.x, G = gridDim.y, tid = threadIdx.x;
     const double2 *b = b0 + (size_t)s * n;
     const double2 *x = x0 + (size_t)s * n;
     double r2 = 0, b2 = 0;
     for (long row = (long)blockIdx.y * 256 + tid; row < n; row += (long)G * 256) {
-        const int slice = (int)(row >> 5), lane = (int)(row & 31);
-        const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
         const double2 bv = b[row];
-        double2 acc = bv;
-        for (int c = 0; c < width; ++c) {
-            const int e = beg + c * 32 + lane;
-            const double2 a = vals[e], xv = x[cols[e]];
-            // the same fused sequence as the allocating residual kernel: near convergence the
-            // residual cancels ~10 digits, so the per-entry rounding must match exactly
-            acc.x = fma(-a.x, xv.x, acc.x);
-            acc.x = fma(a.y, xv.y, acc.x);
-            acc.y = fma(-a.x, xv.y, acc.y);
-            acc.y = fma(-a.y, xv.x, acc.y);
-        }
+        // the row code of the allocating residual kernel: near convergence the residual cancels
+        // ~10 digits, so the per-entry operations and their order must match exactly
+        const double2 acc = resid_row<NCX, WID>(bv, row, slice_ptr, cols, vals, x, rp);
         r2 += acc.x * acc.x + acc.y * acc.y;
         b2 += bv.x * bv.x + bv.y * bv.y;
     }
@@ -1305,9 +1297,15 @@ extern "C" int gdmr_true_residual_noalloc(gdmr_system *S, int nrhs, const double
     int G = (S->n + 255) / 256;
     if (G > NOALLOC_CTAS) G = NOALLOC_CTAS;
     if (G < 1) G = 1;
-    k_relres_noalloc<<<dim3((unsigned)nrhs, (unsigned)G), 256, 0, (cudaStream_t)stream>>>(
-        S->n, S->A.slice_ptr, S->A.cols, S->A.vals64, (const double2 *)b, (const double2 *)x, sc.partials,
-        sc.tickets, relres);
+    const SellMatrix A = S->A.view64();
+    ResidPattern rp{};
+    const int ncx = resid_pattern(A, rp);
+    resid_dispatch(A.npat, ncx, [&](auto ncx_c, auto wid_c) {
+        k_relres_noalloc<decltype(ncx_c)::value, decltype(wid_c)::value>
+            <<<dim3((unsigned)nrhs, (unsigned)G), 256, 0, (cudaStream_t)stream>>>(
+                S->n, S->A.slice_ptr, S->A.cols, S->A.vals64, (const double2 *)b, (const double2 *)x, sc.partials,
+                sc.tickets, relres, rp);
+    });
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(GDMR_ECUDA, "gdmr_true_residual_noalloc", cudaGetErrorString(e));
     return GDMR_OK;

@@ -3699,6 +3699,106 @@ __global__ void __launch_bounds__(NT, 2) k_spmv2(int n, const int *__restrict__ 
     }
 }
 
+// Complex64 SELL-32 product of a batch, two consecutive rows a thread.  In a pattern-stored
+// slice the two rows' values of entry e are one 16-byte load (lanes r and r + 1 of the slice),
+// and x[r + off] and x[r + 1 + off] are one 16-byte load when off is even (the 7-point offsets
+// -P, -Q, 0, +Q, +P on a grid of even width), two 8-byte loads when it is odd; y and v are
+// written 16 bytes at a time.  Per row the terms are added in the same order as k_spmm (entry
+// order), so both kernels give the same values.  Other slices, and a last odd row, take
+// k_spmm's per-row code.  Needs x, y and v 16-byte aligned with even strides (host-checked).
+template <int SG>
+__global__ void __launch_bounds__(NT) k_spmm_pair(int n, const int *__restrict__ slice_ptr, const int *__restrict__ cols,
+                                                  const float2 *__restrict__ vals, const float2 *__restrict__ x0,
+                                                  size_t strideX, float2 *__restrict__ y0, size_t strideY,
+                                                  const int *__restrict__ act, int nsys, SellPattern pat,
+                                                  const SysState *__restrict__ scale, float2 *__restrict__ vout0,
+                                                  size_t strideVO) {
+    constexpr int WMAX = SELL_PATTERN;
+    const int g0 = blockIdx.x * SG;
+    const int ng = min(SG, nsys - g0);
+    __shared__ float s_al[SG];
+    __shared__ int s_bk[SG];
+    if (scale && (int)threadIdx.x < ng) {
+        const SysState &stt = scale[act[g0 + threadIdx.x]];
+        s_al[threadIdx.x] = (float)stt.alpha;
+        s_bk[threadIdx.x] = stt.broken;
+    }
+    __syncthreads();
+    auto fin1 = [&](int g, int sys, long row, float2 acc, const float2 *x) {
+        if (scale) {
+            const float al = s_al[g];
+            float2 v = x[row];
+            v.x *= al;
+            v.y *= al;
+            acc.x *= al;
+            acc.y *= al;
+            if (s_bk[g]) v = czero<float2>();
+            vout0[(size_t)sys * strideVO + row] = v;
+        }
+        y0[(size_t)sys * strideY + row] = acc;
+    };
+    for (long r = ((long)blockIdx.y * NT + threadIdx.x) * 2; r < n; r += (long)gridDim.y * NT * 2) {
+        const int slice = (int)(r >> 5), lane = (int)(r & 31);
+        const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
+        if (r + 1 < n && pat.uniform && pat.uniform[slice] && width <= WMAX) {
+            float4 v[WMAX];
+#pragma unroll
+            for (int e = 0; e < WMAX; ++e)
+                v[e] = e < width ? *reinterpret_cast<const float4 *>(vals + beg + e * 32 + lane)
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int g = 0; g < ng; ++g) {
+                const int sys = act[g0 + g];
+                const float2 *x = x0 + (size_t)sys * strideX;
+                float2 a0 = czero<float2>(), a1 = czero<float2>();
+#pragma unroll
+                for (int e = 0; e < WMAX; ++e) {
+                    if (e < width) {
+                        const long c = r + pat.off[e];
+                        float2 xa, xb;
+                        if ((pat.off[e] & 1) == 0) {
+                            const float4 t = *reinterpret_cast<const float4 *>(x + c);
+                            xa = make_float2(t.x, t.y);
+                            xb = make_float2(t.z, t.w);
+                        } else {
+                            xa = x[c];
+                            xb = x[c + 1];
+                        }
+                        cfma(a0, make_float2(v[e].x, v[e].y), xa);
+                        cfma(a1, make_float2(v[e].z, v[e].w), xb);
+                    }
+                }
+                if (scale) {
+                    const float al = s_al[g];
+                    const float4 xr = *reinterpret_cast<const float4 *>(x + r);
+                    float4 vv = make_float4(xr.x * al, xr.y * al, xr.z * al, xr.w * al);
+                    if (s_bk[g]) vv = make_float4(0.f, 0.f, 0.f, 0.f);
+                    *reinterpret_cast<float4 *>(vout0 + (size_t)sys * strideVO + r) = vv;
+                    a0.x *= al;
+                    a0.y *= al;
+                    a1.x *= al;
+                    a1.y *= al;
+                }
+                *reinterpret_cast<float4 *>(y0 + (size_t)sys * strideY + r) = make_float4(a0.x, a0.y, a1.x, a1.y);
+            }
+        } else {
+            // (the stored column indices, which pattern-stored slices also keep)
+            for (long row = r; row < r + 2 && row < n; ++row) {
+                const int ln = (int)(row & 31);
+                for (int g = 0; g < ng; ++g) {
+                    const int sys = act[g0 + g];
+                    const float2 *x = x0 + (size_t)sys * strideX;
+                    float2 acc = czero<float2>();
+                    for (int e = 0; e < width; ++e) {
+                        const int idx = beg + e * 32 + ln;
+                        cfma(acc, vals[idx], x[cols[idx]]);
+                    }
+                    fin1(g, sys, row, acc, x);
+                }
+            }
+        }
+    }
+}
+
 // Grid (system groups, row chunks): the groups of one row chunk run together, so the
 // matrix slice is read from HBM once and from L2 for the other groups.
 template <class R, int SG>
@@ -3795,14 +3895,6 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
     }
 }
 
-// Pattern entries of the FP64 residual: idx lists the entries with complex values before the
-// real ones, off[j] the column offset of entry idx[j].
-struct ResidPattern {
-    const unsigned char *uniform;
-    int idx[SELL_PATTERN];
-    int off[SELL_PATTERN];
-};
-
 // r = b - A x in FP64 with ||r||^2 reduced; last CTA sets true_res and alpha.
 template <int NCX, int WID>
 __global__ void __launch_bounds__(NT) k_residual64(int n, const int *__restrict__ slice_ptr, const int *__restrict__ cols,
@@ -3818,34 +3910,7 @@ __global__ void __launch_bounds__(NT) k_residual64(int n, const int *__restrict_
     __shared__ double red[1][NW];
     double n2 = 0;
     for (int row = blockIdx.y * NT + tid; row < n; row += G * NT) {
-        double2 acc = b[row];
-        const int slice = row >> 5, lane = row & 31;
-        const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
-        if (WID > 0 && rp.uniform[slice]) {
-            // pattern-stored slice (WID entries): its NCX complex entries with four FP64 FMAs,
-            // then its real ones (zero imaginary parts, host-checked) with two.  The kernel is
-            // FP64-rate bound; a 7-point Helmholtz row goes from 28 FMAs to 16.  Both loops have
-            // compile-time trip counts: nothing is predicated, and the entry list stays in the
-            // parameter space.
-#pragma unroll
-            for (int j = 0; j < NCX; ++j) {
-                const int c = rp.idx[j];
-                cfms(acc, vals[beg + c * 32 + lane], x[row + rp.off[j]]);
-            }
-#pragma unroll
-            for (int j = NCX; j < WID; ++j) {
-                const int c = rp.idx[j];
-                const double a = vals[beg + c * 32 + lane].x;
-                const double2 xv = x[row + rp.off[j]];
-                acc.x = rfma(-a, xv.x, acc.x);
-                acc.y = rfma(-a, xv.y, acc.y);
-            }
-        } else {
-            for (int c = 0; c < width; ++c) {
-                const int e = beg + c * 32 + lane;
-                cfms(acc, vals[e], x[cols[e]]);
-            }
-        }
+        const double2 acc = resid_row<NCX, WID>(b[row], row, slice_ptr, cols, vals, x, rp);
         r[row] = acc;
         n2 += acc.x * acc.x + acc.y * acc.y;
     }
@@ -4966,6 +5031,9 @@ void set_combine_group(int on) { g_combine_group.store(on ? 1 : 0); }
 int combine_group() { return g_combine_group.load(); }
 static std::atomic<int> g_grid_operator{1};
 static std::atomic<int> g_grid_batch{0};
+static std::atomic<int> g_spmm_pair{1};
+void set_spmm_pair(int on) { g_spmm_pair.store(on ? 1 : 0); }
+int spmm_pair() { return g_spmm_pair.load(); }
 void set_grid_operator(int enable) { g_grid_operator.store(enable ? 1 : 0); }
 int grid_operator() { return g_grid_operator.load(); }
 void set_grid_batch(int sg) { g_grid_batch.store(sg == 1 || sg == 2 || sg == 4 ? sg : 0); }
@@ -5014,6 +5082,18 @@ void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX
         return;
     }
     constexpr int SG = 8;
+    if constexpr (sizeof(R) == 4) {
+        // two rows a thread with 16-byte loads and stores: x, y, v 16-byte aligned, even strides
+        auto al16 = [](const void *p) { return ((uintptr_t)p & 15u) == 0; };
+        if (spmm_pair() && A.npat > 0 && al16(x) && al16(y) && strideX % 2 == 0 && strideY % 2 == 0 &&
+            (!scale || (al16(vout) && strideVO % 2 == 0)) && al16(A.vals)) {
+            const int rows = (A.n + 2 * NT - 1) / (2 * NT);
+            const dim3 grid((nsys + SG - 1) / SG, rows < 65535 ? rows : 65535);
+            k_spmm_pair<SG><<<grid, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const float2 *)A.vals, x, strideX, y,
+                                                 strideY, act, nsys, sell_pattern(A), scale, vout, strideVO);
+            return;
+        }
+    }
     int rows = (A.n + NT - 1) / NT;
     dim3 grid((nsys + SG - 1) / SG, rows < 65535 ? rows : 65535);
     k_spmm<R, SG><<<grid, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const typename CT<R>::t *)A.vals, x, strideX, y,
@@ -5034,38 +5114,33 @@ void launch_stencil(const Stencil7 &S, const typename CT<R>::t *x, size_t stride
                                       vout, strideVO);
 }
 
+int resid_pattern(const SellMatrix &A, ResidPattern &rp) {
+    rp = ResidPattern{};
+    if (A.npat <= 0 || !A.uniform || !A.preal) return -1;
+    rp.uniform = A.uniform;
+    int j = 0;
+    for (int e = 0; e < A.npat; ++e)
+        if (!(A.preal >> e & 1u)) rp.idx[j++] = e;
+    const int ncx = j;
+    for (int e = 0; e < A.npat; ++e)
+        if (A.preal >> e & 1u) rp.idx[j++] = e;
+    for (int q = 0; q < A.npat; ++q) rp.off[q] = A.pat[rp.idx[q]];
+    return ncx;
+}
+
 void launch_residual64(const SellMatrix &A, const double2 *b, size_t strideB, const double2 *x, size_t strideX,
                        double2 *r, size_t strideR, const int *act, int nsys, double2 *partials, unsigned *tickets,
                        SysState *state, cudaStream_t st) {
     if (nsys <= 0) return;
     Launch L_(KC_RESID64, spmm_bytes(A, sizeof(double2), nsys) + (double)sizeof(double2) * A.n * nsys, st, 1);
-    // pattern entries in the order complex first, real after (an entry is real when it is real
-    // in every pattern-stored slice); instances for 5- and 7-entry patterns with up to two
-    // complex entries, the plain loop otherwise
     ResidPattern rp{};
-    int ncx = -1;
-    if (A.npat > 0 && A.uniform && A.preal) {
-        rp.uniform = A.uniform;
-        int j = 0;
-        for (int e = 0; e < A.npat; ++e)
-            if (!(A.preal >> e & 1u)) rp.idx[j++] = e;
-        ncx = j;
-        for (int e = 0; e < A.npat; ++e)
-            if (A.preal >> e & 1u) rp.idx[j++] = e;
-        for (int q = 0; q < A.npat; ++q) rp.off[q] = A.pat[rp.idx[q]];
-    }
+    const int ncx = resid_pattern(A, rp);
     const dim3 grid = grid2(nsys, capped_grid(A.n, nsys, 8));
-    auto go = [&](auto kernel) {
-        kernel<<<grid, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const double2 *)A.vals, b, strideB, x, strideX, r,
-                                    strideR, act, partials, tickets, state, rp);
-    };
-    if (A.npat == 7 && ncx == 1) go(k_residual64<1, 7>);
-    else if (A.npat == 7 && ncx == 0) go(k_residual64<0, 7>);
-    else if (A.npat == 7 && ncx == 2) go(k_residual64<2, 7>);
-    else if (A.npat == 5 && ncx == 1) go(k_residual64<1, 5>);
-    else if (A.npat == 5 && ncx == 0) go(k_residual64<0, 5>);
-    else if (A.npat == 5 && ncx == 2) go(k_residual64<2, 5>);
-    else go(k_residual64<0, 0>);
+    resid_dispatch(A.npat, ncx, [&](auto ncx_c, auto wid_c) {
+        k_residual64<decltype(ncx_c)::value, decltype(wid_c)::value><<<grid, NT, 0, st>>>(
+            A.n, A.slice_ptr, A.cols, (const double2 *)A.vals, b, strideB, x, strideX, r, strideR, act, partials,
+            tickets, state, rp);
+    });
 }
 
 template <class R>

@@ -17,6 +17,8 @@
 
 #include <string>
 
+#include <type_traits>
+
 namespace gdmr {
 
 // Double-float real: value = hi + lo with |lo| <= ulp(hi)/2, about 48 significant bits.  It
@@ -345,6 +347,10 @@ void set_grid_operator(int enable);
 int grid_operator();
 void set_grid_batch(int sg);
 int grid_batch();
+// Complex64 batched SELL products two rows a thread with 16-byte loads and stores (on by
+// default; k_spmm_pair), else one row a thread (k_spmm).  Both give the same values.
+void set_spmm_pair(int on);
+int spmm_pair();
 // Matrix-free constant-coefficient stencil on an nx x ny x nz grid (nz = 1: 5-point 2D),
 // unknowns numbered i + nx (j + ny l), Dirichlet boundary (neighbours outside are dropped):
 //   y = d x + wx (x[i-1] + x[i+1]) + wy (x[j-1] + x[j+1]) + wz (x[l-1] + x[l+1]).
@@ -405,6 +411,69 @@ int launch_krylov_multi(const KrylovJob<R> *jobs, const int *cta_job, int ctas, 
                         cudaStream_t st);
 // Algorithmic bytes of one system's Krylov loop (operator products, projections, updates).
 double krylov_loop_bytes(const SellMatrix &A, size_t vs, int kk, int m);
+
+// The FP64 residual's row: acc - sum_e A[row][e] x[col_e].  A pattern-stored slice adds its
+// complex pattern entries (idx[0..NCX-1]) with four FP64 FMAs each, then its real ones (zero
+// imaginary part in every pattern-stored slice, decided on the host) with two; the FP64 pipe
+// bounds this product on GB300 and a 7-point Helmholtz row goes from 28 FMAs to 16.  Both loops
+// have compile-time trip counts (nothing predicated; the entry list stays in parameter space).
+// Other slices take the SELL loop.  Every residual kernel uses it, so they agree bit for bit.
+struct ResidPattern {
+    const unsigned char *uniform;   // per slice: pattern-stored (null: none)
+    int idx[SELL_PATTERN];          // pattern entries, complex ones first
+    int off[SELL_PATTERN];          // column offset of entry idx[j]
+};
+// Fills rp for A and returns the number of complex entries, or -1 when every slice takes the
+// SELL loop (no pattern, or no real entry).
+int resid_pattern(const SellMatrix &A, ResidPattern &rp);
+// Calls f(NCX, WID) with compile-time constants for the instantiated shapes (5- and 7-entry
+// patterns with up to two complex entries), or f(0, 0) (the SELL loop).
+template <class F> void resid_dispatch(int npat, int ncx, F &&f) {
+    using std::integral_constant;
+    if (npat == 7 && ncx == 1) f(integral_constant<int, 1>{}, integral_constant<int, 7>{});
+    else if (npat == 7 && ncx == 0) f(integral_constant<int, 0>{}, integral_constant<int, 7>{});
+    else if (npat == 7 && ncx == 2) f(integral_constant<int, 2>{}, integral_constant<int, 7>{});
+    else if (npat == 5 && ncx == 1) f(integral_constant<int, 1>{}, integral_constant<int, 5>{});
+    else if (npat == 5 && ncx == 0) f(integral_constant<int, 0>{}, integral_constant<int, 5>{});
+    else if (npat == 5 && ncx == 2) f(integral_constant<int, 2>{}, integral_constant<int, 5>{});
+    else f(integral_constant<int, 0>{}, integral_constant<int, 0>{});
+}
+#ifdef __CUDACC__
+template <int NCX, int WID>
+__device__ __forceinline__ double2 resid_row(double2 acc, long row, const int *__restrict__ slice_ptr,
+                                             const int *__restrict__ cols, const double2 *__restrict__ vals,
+                                             const double2 *__restrict__ x, const ResidPattern &rp) {
+    const int slice = (int)(row >> 5), lane = (int)(row & 31);
+    const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
+    if (WID > 0 && rp.uniform[slice]) {
+#pragma unroll
+        for (int j = 0; j < NCX; ++j) {
+            const double2 a = vals[beg + rp.idx[j] * 32 + lane], xv = x[row + rp.off[j]];
+            acc.x = ::fma(-a.x, xv.x, acc.x);
+            acc.x = ::fma(a.y, xv.y, acc.x);
+            acc.y = ::fma(-a.x, xv.y, acc.y);
+            acc.y = ::fma(-a.y, xv.x, acc.y);
+        }
+#pragma unroll
+        for (int j = NCX; j < WID; ++j) {
+            const double a = vals[beg + rp.idx[j] * 32 + lane].x;
+            const double2 xv = x[row + rp.off[j]];
+            acc.x = ::fma(-a, xv.x, acc.x);
+            acc.y = ::fma(-a, xv.y, acc.y);
+        }
+    } else {
+        for (int c = 0; c < width; ++c) {
+            const int e = beg + c * 32 + lane;
+            const double2 a = vals[e], xv = x[cols[e]];
+            acc.x = ::fma(-a.x, xv.x, acc.x);
+            acc.x = ::fma(a.y, xv.y, acc.x);
+            acc.y = ::fma(-a.x, xv.y, acc.y);
+            acc.y = ::fma(-a.y, xv.x, acc.y);
+        }
+    }
+    return acc;
+}
+#endif
 
 // y_s = b_s - A x_s in FP64 with ||y_s||^2 reduced into state[s].nrm2 (refined form).
 void launch_residual64(const SellMatrix &A, const double2 *b, size_t strideB, const double2 *x, size_t strideX,
