@@ -409,7 +409,6 @@ extern "C" double gdmrWaitLimit(double ms) {
 }
 extern "C" void gdmrInjectAllocFailure(int nth) { inject_alloc_failure(nth); }
 extern "C" void gdmrCombineGroup(int enable) { set_combine_group(enable); }
-extern "C" void gdmrSpmmPair(int enable) { set_spmm_pair(enable); }
 extern "C" void gdmrProfile(int on) { profile_enable(on != 0); }
 extern "C" void gdmrProfileReset(void) { profile_reset(); }
 extern "C" void gdmrTune(int on) { tune_enable(on != 0); }

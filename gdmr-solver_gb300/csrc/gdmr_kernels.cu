@@ -3699,106 +3699,6 @@ __global__ void __launch_bounds__(NT, 2) k_spmv2(int n, const int *__restrict__ 
     }
 }
 
-// Complex64 SELL-32 product of a batch, two consecutive rows a thread.  In a pattern-stored
-// slice the two rows' values of entry e are one 16-byte load (lanes r and r + 1 of the slice),
-// and x[r + off] and x[r + 1 + off] are one 16-byte load when off is even (the 7-point offsets
-// -P, -Q, 0, +Q, +P on a grid of even width), two 8-byte loads when it is odd; y and v are
-// written 16 bytes at a time.  Per row the terms are added in the same order as k_spmm (entry
-// order), so both kernels give the same values.  Other slices, and a last odd row, take
-// k_spmm's per-row code.  Needs x, y and v 16-byte aligned with even strides (host-checked).
-template <int SG>
-__global__ void __launch_bounds__(NT) k_spmm_pair(int n, const int *__restrict__ slice_ptr, const int *__restrict__ cols,
-                                                  const float2 *__restrict__ vals, const float2 *__restrict__ x0,
-                                                  size_t strideX, float2 *__restrict__ y0, size_t strideY,
-                                                  const int *__restrict__ act, int nsys, SellPattern pat,
-                                                  const SysState *__restrict__ scale, float2 *__restrict__ vout0,
-                                                  size_t strideVO) {
-    constexpr int WMAX = SELL_PATTERN;
-    const int g0 = blockIdx.x * SG;
-    const int ng = min(SG, nsys - g0);
-    __shared__ float s_al[SG];
-    __shared__ int s_bk[SG];
-    if (scale && (int)threadIdx.x < ng) {
-        const SysState &stt = scale[act[g0 + threadIdx.x]];
-        s_al[threadIdx.x] = (float)stt.alpha;
-        s_bk[threadIdx.x] = stt.broken;
-    }
-    __syncthreads();
-    auto fin1 = [&](int g, int sys, long row, float2 acc, const float2 *x) {
-        if (scale) {
-            const float al = s_al[g];
-            float2 v = x[row];
-            v.x *= al;
-            v.y *= al;
-            acc.x *= al;
-            acc.y *= al;
-            if (s_bk[g]) v = czero<float2>();
-            vout0[(size_t)sys * strideVO + row] = v;
-        }
-        y0[(size_t)sys * strideY + row] = acc;
-    };
-    for (long r = ((long)blockIdx.y * NT + threadIdx.x) * 2; r < n; r += (long)gridDim.y * NT * 2) {
-        const int slice = (int)(r >> 5), lane = (int)(r & 31);
-        const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
-        if (r + 1 < n && pat.uniform && pat.uniform[slice] && width <= WMAX) {
-            float4 v[WMAX];
-#pragma unroll
-            for (int e = 0; e < WMAX; ++e)
-                v[e] = e < width ? *reinterpret_cast<const float4 *>(vals + beg + e * 32 + lane)
-                                 : make_float4(0.f, 0.f, 0.f, 0.f);
-            for (int g = 0; g < ng; ++g) {
-                const int sys = act[g0 + g];
-                const float2 *x = x0 + (size_t)sys * strideX;
-                float2 a0 = czero<float2>(), a1 = czero<float2>();
-#pragma unroll
-                for (int e = 0; e < WMAX; ++e) {
-                    if (e < width) {
-                        const long c = r + pat.off[e];
-                        float2 xa, xb;
-                        if ((pat.off[e] & 1) == 0) {
-                            const float4 t = *reinterpret_cast<const float4 *>(x + c);
-                            xa = make_float2(t.x, t.y);
-                            xb = make_float2(t.z, t.w);
-                        } else {
-                            xa = x[c];
-                            xb = x[c + 1];
-                        }
-                        cfma(a0, make_float2(v[e].x, v[e].y), xa);
-                        cfma(a1, make_float2(v[e].z, v[e].w), xb);
-                    }
-                }
-                if (scale) {
-                    const float al = s_al[g];
-                    const float4 xr = *reinterpret_cast<const float4 *>(x + r);
-                    float4 vv = make_float4(xr.x * al, xr.y * al, xr.z * al, xr.w * al);
-                    if (s_bk[g]) vv = make_float4(0.f, 0.f, 0.f, 0.f);
-                    *reinterpret_cast<float4 *>(vout0 + (size_t)sys * strideVO + r) = vv;
-                    a0.x *= al;
-                    a0.y *= al;
-                    a1.x *= al;
-                    a1.y *= al;
-                }
-                *reinterpret_cast<float4 *>(y0 + (size_t)sys * strideY + r) = make_float4(a0.x, a0.y, a1.x, a1.y);
-            }
-        } else {
-            // (the stored column indices, which pattern-stored slices also keep)
-            for (long row = r; row < r + 2 && row < n; ++row) {
-                const int ln = (int)(row & 31);
-                for (int g = 0; g < ng; ++g) {
-                    const int sys = act[g0 + g];
-                    const float2 *x = x0 + (size_t)sys * strideX;
-                    float2 acc = czero<float2>();
-                    for (int e = 0; e < width; ++e) {
-                        const int idx = beg + e * 32 + ln;
-                        cfma(acc, vals[idx], x[cols[idx]]);
-                    }
-                    fin1(g, sys, row, acc, x);
-                }
-            }
-        }
-    }
-}
-
 // Grid (system groups, row chunks): the groups of one row chunk run together, so the
 // matrix slice is read from HBM once and from L2 for the other groups.
 template <class R, int SG>
@@ -5031,9 +4931,6 @@ void set_combine_group(int on) { g_combine_group.store(on ? 1 : 0); }
 int combine_group() { return g_combine_group.load(); }
 static std::atomic<int> g_grid_operator{1};
 static std::atomic<int> g_grid_batch{0};
-static std::atomic<int> g_spmm_pair{1};
-void set_spmm_pair(int on) { g_spmm_pair.store(on ? 1 : 0); }
-int spmm_pair() { return g_spmm_pair.load(); }
 void set_grid_operator(int enable) { g_grid_operator.store(enable ? 1 : 0); }
 int grid_operator() { return g_grid_operator.load(); }
 void set_grid_batch(int sg) { g_grid_batch.store(sg == 1 || sg == 2 || sg == 4 ? sg : 0); }
@@ -5082,18 +4979,6 @@ void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX
         return;
     }
     constexpr int SG = 8;
-    if constexpr (sizeof(R) == 4) {
-        // two rows a thread with 16-byte loads and stores: x, y, v 16-byte aligned, even strides
-        auto al16 = [](const void *p) { return ((uintptr_t)p & 15u) == 0; };
-        if (spmm_pair() && A.npat > 0 && al16(x) && al16(y) && strideX % 2 == 0 && strideY % 2 == 0 &&
-            (!scale || (al16(vout) && strideVO % 2 == 0)) && al16(A.vals)) {
-            const int rows = (A.n + 2 * NT - 1) / (2 * NT);
-            const dim3 grid((nsys + SG - 1) / SG, rows < 65535 ? rows : 65535);
-            k_spmm_pair<SG><<<grid, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const float2 *)A.vals, x, strideX, y,
-                                                 strideY, act, nsys, sell_pattern(A), scale, vout, strideVO);
-            return;
-        }
-    }
     int rows = (A.n + NT - 1) / NT;
     dim3 grid((nsys + SG - 1) / SG, rows < 65535 ? rows : 65535);
     k_spmm<R, SG><<<grid, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const typename CT<R>::t *)A.vals, x, strideX, y,

@@ -677,7 +677,9 @@ __global__ void __launch_bounds__(WU_THREADS, 1)
     float *A = reinterpret_cast<float *>(base);                        // [buf][big|small]
     float *B = reinterpret_cast<float *>(base + 4 * WA_AOP);           // 4 nsp rows x 2 atom columns
     float2 *cv = reinterpret_cast<float2 *>(base + 4 * WA_AOP + (size_t)brows * 2 * TC_ROW);   // [sys][WU_QB]
-    double *sacc = reinterpret_cast<double *>(cv + (size_t)TC_NMAX * WU_QB);                   // [quarter][sys][3]
+    // per lane quarter and system: the tiles' warp sums in FP32 (an FP64 add per system, tile and
+    // warp was about the epilogue's memory time on GB300's FP64 pipe); FP64 once per CTA
+    float *sacc = reinterpret_cast<float *>(cv + (size_t)TC_NMAX * WU_QB);                     // [quarter][sys][3]
     __shared__ __align__(8) uint64_t full[2], mdone[2], tempty[2], done;
     __shared__ uint32_t tmem_base;
     __shared__ int s_act[TC_NMAX], s_skip[TC_NMAX];
@@ -688,7 +690,7 @@ __global__ void __launch_bounds__(WU_THREADS, 1)
 
     for (int e = tid; e < (4 * WA_AOP + brows * 2 * TC_ROW) / 16; e += WU_THREADS)
         reinterpret_cast<float4 *>(base)[e] = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int e = tid; e < 4 * TC_NMAX * 3; e += WU_THREADS) sacc[e] = 0.0;
+    for (int e = tid; e < 4 * TC_NMAX * 3; e += WU_THREADS) sacc[e] = 0.f;
     if (tid < nsys) {
         const int sy = act[tid];
         s_act[tid] = sy;
@@ -812,7 +814,7 @@ __global__ void __launch_bounds__(WU_THREADS, 1)
         // ---- epilogue: the update proper
         const int quarter = warp & 3, group = warp >> 2;
         const int s_lo = group * 16, s_hi = min(nsys, s_lo + 16);
-        double *myacc = sacc + (size_t)quarter * TC_NMAX * 3;
+        float *myacc = sacc + (size_t)quarter * TC_NMAX * 3;
         for (int i = 0; i < my_tiles; ++i) {
             const int buf = i & 1;
             int ok = 1;
@@ -862,9 +864,9 @@ __global__ void __launch_bounds__(WU_THREADS, 1)
                     cr = warp_sum_f(cr);
                     ci = warp_sum_f(ci);
                     if (lane == 0) {
-                        myacc[sl * 3] += (double)ln;
-                        myacc[sl * 3 + 1] += (double)cr;
-                        myacc[sl * 3 + 2] += (double)ci;
+                        myacc[sl * 3] += ln;
+                        myacc[sl * 3 + 1] += cr;
+                        myacc[sl * 3 + 2] += ci;
                     }
                 }
             }
@@ -888,7 +890,7 @@ __global__ void __launch_bounds__(WU_THREADS, 1)
         double *part = partials + (size_t)sl * 3 * G;
         for (int v = 0; v < 3; ++v) {
             double t = 0;
-            for (int q = 0; q < 4; ++q) t += sacc[(size_t)q * TC_NMAX * 3 + sl * 3 + v];
+            for (int q = 0; q < 4; ++q) t += (double)sacc[(size_t)q * TC_NMAX * 3 + sl * 3 + v];
             part[(size_t)v * G + blockIdx.x] = s_abort ? 0.0 : t;
         }
         __threadfence();
@@ -985,7 +987,7 @@ int launch_wapply_tc(int n, int kk, const float2 *W, double2 *coef, size_t strid
 
 size_t wupdate_smem_bytes(int nsp) {
     return (size_t)4 * WA_AOP + (size_t)4 * nsp * 2 * TC_ROW + sizeof(float2) * TC_NMAX * WU_QB +
-           sizeof(double) * 4 * TC_NMAX * 3 + 1024;
+           sizeof(float) * 4 * TC_NMAX * 3 + 1024;
 }
 
 bool wupdate_tc_ok(int n, int kk, int qb, int nsys) {

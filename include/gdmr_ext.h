@@ -176,11 +176,6 @@ void gdmrGridBatch(int systemsPerThread);
  * loaded once for the four (on by default); 0 returns them to one system a CTA. */
 void gdmrCombineGroup(int enable);
 
-/* Complex64 batched SELL-32 products two rows a thread, with 16-byte loads of the two rows'
- * values and of x where the column offset is even and 16-byte stores (on by default); 0 returns
- * them to one row a thread.  Both add a row's terms in the same order (the same values). */
-void gdmrSpmmPair(int enable);
-
 /* Host-only check of a CSR matrix (complex values interleaved re, im) for the structured-grid
  * form: dims[0..2] <- (nx, ny, nz), zeros if it has none.  GDMR_EINVAL for malformed arrays. */
 int gdmr_csr_grid_form(int n, const int *rowPtr, const int *colIdx, const double *vals_ri, int *dims);

@@ -92,25 +92,3 @@ def test_grouped_combination_matches_one_system_a_cta(batch20, precision):
     cs = [st["cycles"] for st in out[False][1]]
     assert max(abs(a - b) for a, b in zip(cg, cs)) <= 2, (cg, cs)
 
-
-def test_pair_spmm_matches_one_row_a_thread(batch20):
-    """The complex64 batched operator product two rows a thread (16-byte loads and stores)
-    against one row a thread: the same terms in the same order, so with the Gram-Schmidt
-    variants pinned the two batches are bit for bit the same."""
-    A, rhs, cfg, direct = batch20
-    out = {}
-    for pair in (True, False):
-        gdmr.spmm_pair(pair)
-        gdmr.tune_force(0, 0)
-        try:
-            s = gdmr.System(A, cfg["m"], cfg["k"], capacity=NRHS, precision="mixed")
-            out[pair] = s.solve_batch(rhs, tol=1e-10, max_cycles=2000)
-        finally:
-            gdmr.spmm_pair(True)
-            gdmr.tune_force(-1, -1)
-    (Xp, sp_), (Xr, sr) = out[True], out[False]
-    assert [t["cycles"] for t in sp_] == [t["cycles"] for t in sr]
-    assert np.array_equal(Xp, Xr)
-    assert all(t["status"] == 0 and t["true_rel_res"] <= 1.5e-10 for t in sp_)
-    err = np.linalg.norm(Xp - direct, axis=1) / np.linalg.norm(direct, axis=1)
-    assert err.max() < 1e-8
