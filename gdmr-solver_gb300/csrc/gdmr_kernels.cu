@@ -161,6 +161,34 @@ template <int NV> __device__ __forceinline__ void block_sum_f(const float (&f)[N
         }
 }
 
+// Complex64 kernels keep their cross-CTA partial sums as double-float (two floats in the slot
+// of a double): the per-CTA and last-CTA sums then run on the FP32 pipes, and a result is
+// converted to double once.  A last CTA summing a few hundred FP64 partials per coefficient in
+// FP64 spent ~20 SM clocks per FP64 warp instruction, about 2% of a projection launch.
+__device__ __forceinline__ void store_df(double *slot, dfr v) { *reinterpret_cast<dfr *>(slot) = v; }
+__device__ __forceinline__ dfr load_df(const double *slot) {
+    const float2 t = __ldcg(reinterpret_cast<const float2 *>(slot));
+    return dfr(t.x, t.y);
+}
+// As block_sum_f, with the warps' sums added in double-float and returned as such (thread 0).
+template <int NV> __device__ __forceinline__ void block_sum_df(const float (&f)[NV], dfr (&v)[NV], float (*red)[NW]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+        const float s = warp_sum(f[j]);
+        if (lane == 0) red[j][warp] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+            dfr s(0.f, 0.f);
+#pragma unroll
+            for (int w = 0; w < NW; ++w) s = s + dfr(red[j][w], 0.f);
+            v[j] = s;
+        }
+}
+
 // Last-CTA-done protocol: returns true in every thread of the CTA that arrived last.
 __device__ __forceinline__ bool arrive_last(unsigned *ticket, unsigned count) {
     __shared__ unsigned s_last;
@@ -371,24 +399,47 @@ __global__ void __launch_bounds__(NT, PF ? 2 : min_blocks<typename CT<R>::t>(EPT
     }
     __syncthreads();
     double *part = (double *)partials + (size_t)slot * qmax * 2 * G;   // [p][re|im][G]
+    constexpr bool DFP = std::is_same<C, float2>::value;   // double-float partials (complex64)
     for (int p = tid; p < q; p += NT) {
-        double re = 0, im = 0;
-#pragma unroll
-        for (int ww = 0; ww < NW; ++ww) { re += (double)wsum[ww][p].x; im += (double)wsum[ww][p].y; }
         double *pp = part + (size_t)p * 2 * G;
-        pp[chunk] = re;
-        pp[G + chunk] = im;
+        if constexpr (DFP) {
+            dfr re(0.f, 0.f), im(0.f, 0.f);
+#pragma unroll
+            for (int ww = 0; ww < NW; ++ww) {
+                re = re + dfr((float)wsum[ww][p].x, 0.f);
+                im = im + dfr((float)wsum[ww][p].y, 0.f);
+            }
+            store_df(pp + chunk, re);
+            store_df(pp + G + chunk, im);
+        } else {
+            double re = 0, im = 0;
+#pragma unroll
+            for (int ww = 0; ww < NW; ++ww) { re += (double)wsum[ww][p].x; im += (double)wsum[ww][p].y; }
+            pp[chunk] = re;
+            pp[G + chunk] = im;
+        }
     }
     if (!arrive_last(&tickets[slot], G)) return;
     // one warp per coefficient, lanes stride over the G partials (fixed order)
     double2 *coef = coef0 + (size_t)s * strideC;
     for (int p = warp; p < q; p += NW) {
         const double *pp = part + (size_t)p * 2 * G;
-        double re = 0, im = 0;
-        for (int g = lane; g < G; g += 32) { re += __ldcg(pp + g); im += __ldcg(pp + G + g); }
-        re = warp_sum(re);
-        im = warp_sum(im);
-        if (lane == 0) coef[p] = make_double2(re, im);
+        if constexpr (DFP) {
+            dfr re(0.f, 0.f), im(0.f, 0.f);
+            for (int g = lane; g < G; g += 32) {
+                re = re + load_df(pp + g);
+                im = im + load_df(pp + G + g);
+            }
+            re = warp_sum(re);
+            im = warp_sum(im);
+            if (lane == 0) coef[p] = make_double2((double)re, (double)im);
+        } else {
+            double re = 0, im = 0;
+            for (int g = lane; g < G; g += 32) { re += __ldcg(pp + g); im += __ldcg(pp + G + g); }
+            re = warp_sum(re);
+            im = warp_sum(im);
+            if (lane == 0) coef[p] = make_double2(re, im);
+        }
     }
     if (tid == 0) tickets[slot] = 0;
 }
@@ -475,29 +526,59 @@ __global__ void __launch_bounds__(NT, PF ? 2 : min_blocks<typename CT<R>::t>(EPT
             cdotacc(lc, acc[e].v[j], org[e].v[j]);
         }
     }
-    double v[3];
-    if constexpr (std::is_same<C, float2>::value) {
-        const float f[3] = {ln.x, lc.x, lc.y};
-        block_sum_f<3>(f, v, red);
-    } else {
-        v[0] = (double)ln.x;
-        v[1] = (double)lc.x;
-        v[2] = (double)lc.y;
-        block_sum<3>(v, red);
-    }
     double *part = (double *)partials + (size_t)slot * 3 * G;
-    if (tid == 0) {
-        part[chunk] = v[0];
-        part[G + chunk] = v[1];
-        part[2 * G + chunk] = v[2];
-    }
-    if (!arrive_last(&tickets[slot], G)) return;
-    double tot[3];
-    __syncthreads();
-    sum_partials<3>(part, G, tot, red);
-    if (tid == 0) {
-        run_finish(fin, s, state[s], tot[0], tot[1], tot[2]);
-        tickets[slot] = 0;
+    if constexpr (std::is_same<C, float2>::value) {
+        // double-float partials, summed on the FP32 pipes
+        __shared__ float redf[3][NW];
+        const float f[3] = {ln.x, lc.x, lc.y};
+        dfr v[3];
+        block_sum_df<3>(f, v, redf);
+        if (tid == 0) {
+            store_df(part + chunk, v[0]);
+            store_df(part + G + chunk, v[1]);
+            store_df(part + 2 * G + chunk, v[2]);
+        }
+        if (!arrive_last(&tickets[slot], G)) return;
+        const int lane = tid & 31, warp = tid >> 5;
+        __shared__ dfr tw[3][NW];
+        dfr a[3] = {dfr(0.f, 0.f), dfr(0.f, 0.f), dfr(0.f, 0.f)};
+        for (int g = tid; g < G; g += NT)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) a[j] = a[j] + load_df(part + (size_t)j * G + g);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            a[j] = warp_sum(a[j]);
+            if (lane == 0) tw[j][warp] = a[j];
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double tot[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                dfr t(0.f, 0.f);
+#pragma unroll
+                for (int w = 0; w < NW; ++w) t = t + tw[j][w];
+                tot[j] = (double)t;
+            }
+            run_finish(fin, s, state[s], tot[0], tot[1], tot[2]);
+            tickets[slot] = 0;
+        }
+    } else {
+        double v[3] = {(double)ln.x, (double)lc.x, (double)lc.y};
+        block_sum<3>(v, red);
+        if (tid == 0) {
+            part[chunk] = v[0];
+            part[G + chunk] = v[1];
+            part[2 * G + chunk] = v[2];
+        }
+        if (!arrive_last(&tickets[slot], G)) return;
+        double tot[3];
+        __syncthreads();
+        sum_partials<3>(part, G, tot, red);
+        if (tid == 0) {
+            run_finish(fin, s, state[s], tot[0], tot[1], tot[2]);
+            tickets[slot] = 0;
+        }
     }
 }
 
