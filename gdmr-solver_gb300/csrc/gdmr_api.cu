@@ -3,6 +3,7 @@
 #include <cuComplex.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -409,6 +410,13 @@ extern "C" double gdmrWaitLimit(double ms) {
 }
 extern "C" void gdmrInjectAllocFailure(int nth) { inject_alloc_failure(nth); }
 extern "C" void gdmrCombineGroup(int enable) { set_combine_group(enable); }
+// Systems in flight at or below which gdmr_multi_solve finishes on the engines' own cycles.
+static std::atomic<int> g_multi_tail{8};
+extern "C" int gdmrMultiTail(int systems) {
+    const int prev = g_multi_tail.load();
+    if (systems >= 0) g_multi_tail.store(systems);
+    return prev;
+}
 extern "C" void gdmrProfile(int on) { profile_enable(on != 0); }
 extern "C" void gdmrProfileReset(void) { profile_reset(); }
 extern "C" void gdmrTune(int on) { tune_enable(on != 0); }
@@ -985,14 +993,9 @@ int multi_impl(int nops, gdmr_system *const *sys, const int *nrhs, const double 
             int rc = E[o]->multi_residual();
             if (rc != GDMR_OK) { release(); return rc; }
         }
-        // convergence, retirement, and the front of the cycle of each operator
-        jobs.clear();
-        job_nnz.clear();
-        for (int o = 0; o < nops; ++o) {
+        // convergence and retirement of every operator
+        auto retire = [&](int o, const std::vector<int> &done) {
             gdmr_system *S = sys[o];
-            std::vector<int> done;
-            const int nrun = E[o]->multi_select(&done);
-            if (nrun < 0) { release(); return GDMR_ECUDA; }
             for (int sl : done) {
                 const int r = slot_of[o][sl];
                 cudaMemcpyAsync(x[o] + (size_t)2 * r * S->n, E[o]->slot_x(sl), sizeof(double2) * (size_t)S->n,
@@ -1006,7 +1009,42 @@ int multi_impl(int nops, gdmr_system *const *sys, const int *nrhs, const double 
                 slot_of[o][sl] = -1;
                 ++finished;
             }
-            if (nrun > 0) {
+        };
+        std::vector<int> nrun(nops, 0);
+        int in_flight = 0;
+        bool all_admitted = true;
+        for (int o = 0; o < nops; ++o) {
+            std::vector<int> done;
+            nrun[o] = E[o]->multi_select(&done);
+            if (nrun[o] < 0) { release(); return GDMR_ECUDA; }
+            retire(o, done);
+            in_flight += nrun[o];
+            all_admitted &= next[o] >= nrhs[o];
+        }
+        // the tail: with every right-hand side admitted and few systems left, a lockstep cycle is
+        // as long as its largest system's Krylov loop run by a fraction of the CTAs; the engines'
+        // own batched cycles finish the remaining systems, operator by operator
+        const int tail = g_multi_tail.load();
+        if (all_admitted && in_flight > 0 && in_flight <= tail) {
+            for (bool any = true; any;) {
+                any = false;
+                for (int o = 0; o < nops; ++o) {
+                    if (E[o]->active_count() == 0) continue;
+                    std::vector<int> done;
+                    int rc = E[o]->refine_cycle(&done);
+                    if (rc != GDMR_OK) { release(); return rc; }
+                    retire(o, done);
+                    any |= E[o]->active_count() > 0;
+                }
+            }
+            break;
+        }
+        // the front of the cycle of each operator
+        jobs.clear();
+        job_nnz.clear();
+        for (int o = 0; o < nops; ++o) {
+            gdmr_system *S = sys[o];
+            if (nrun[o] > 0) {
                 int rc = E[o]->multi_front();
                 if (rc != GDMR_OK) { release(); return rc; }
                 if (cudaEventRecord(ev_front[o], E[o]->main_stream()) != cudaSuccess ||

@@ -436,11 +436,12 @@ __global__ void __launch_bounds__(256) k_wproj_tc_reduce(int kk, int nsys, int G
 //     re row: (cr_p, -ci_p), im row: (ci_p, cr_p), so D[i][(s,re)] = Re(w_i c_s), D[i][(s,im)] = Im;
 //   per K step: A_big x B (N = 4 NSp) and A_small x B_big (N = 2 NSp) into one TMEM tile, and
 //   P = D[:, big block] + D[:, small block].
-// Warp roles: warps 0-7 epilogue (warp w reads TMEM lane quarter w % 4, the tile's elements
-// 32 (w % 4) .. + 31, and stores P for half w / 4 of the systems; four warps of stores ran the
-// kernel at about half the HBM rate), warps 8-15 producers (W tile -> split, swizzled A
-// operands), warp 16 issues the MMAs.  A and the TMEM tile are double-buffered; mbarriers only.
-constexpr int WA_EPI = 8, WA_PROD = 8;
+// Warp roles: warps 0 .. WA_EPI-1 epilogue (warp w reads TMEM lane quarter w % 4, the tile's
+// elements 32 (w % 4) .. + 31, and stores P for every (WA_EPI / 4)-th group of 8 systems from
+// group w / 4; four warps of stores ran the kernel at about half the HBM rate), the next WA_PROD
+// warps producers (W tile -> split, swizzled A operands), the last warp issues the MMAs.  A and
+// the TMEM tile are double-buffered; mbarriers only.
+constexpr int WA_EPI = 16, WA_PROD = 8;
 constexpr int WA_MMA_WARP = WA_EPI + WA_PROD;
 constexpr int WA_THREADS = (WA_MMA_WARP + 1) * 32;
 constexpr int WA_TILE = 128;                      // elements per tile (MMA M)
@@ -451,7 +452,7 @@ __device__ __forceinline__ int swz(int r, int kf, int rows) {   // float offset 
     return ((kf >> 5) * rows * TC_ROW + r * TC_ROW + ((((kf >> 2) & 7) ^ (r & 7)) << 4) + ((kf & 3) << 2)) >> 2;
 }
 
-__global__ void __launch_bounds__(WA_THREADS, 1)
+__global__ void __maxnreg__(80)
     k_wapply_tc(int n, int kk, const float2 *__restrict__ W, double2 *__restrict__ coef0, size_t strideC,
                 const int *__restrict__ act, int nsys, int nsp, float2 *__restrict__ P0, size_t strideP,
                 int unit_idx) {
@@ -589,7 +590,7 @@ __global__ void __launch_bounds__(WA_THREADS, 1)
         // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 = elements of the tile, sums
         // the big and small blocks and stores P_s (lanes = consecutive elements) for the systems
         // of every other group of 16 columns (8 systems), starting at group w / 4
-        const int quarter = warp & 3, half = warp >> 2;
+        const int quarter = warp & 3, part = warp >> 2;
         for (int i = 0; i < my_tiles; ++i) {
             const int buf = i & 1;
             int ok = 1;
@@ -601,7 +602,7 @@ __global__ void __launch_bounds__(WA_THREADS, 1)
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
             const long g = ((long)blockIdx.x + (long)i * G) * WA_TILE + quarter * 32 + lane;
             const uint32_t row = taddr + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(buf * 256);
-            for (int c0 = 16 * half; c0 < 2 * nsp; c0 += 32) {
+            for (int c0 = 16 * part; c0 < 2 * nsp; c0 += 16 * (WA_EPI / 4)) {
                 uint32_t vb[16], vs[16];
                 tmem_ld16(row + (uint32_t)c0, vb);
                 tmem_ld16(row + (uint32_t)(2 * nsp + c0), vs);

@@ -82,6 +82,7 @@ SIGNATURES = {
     "gdmr_solve_batch": (I, [P, I, P, P, P, I, I, P]),
     "gdmr_true_residual": (I, [P, I, P, P, I, P]),
     "gdmr_multi_solve": (I, [I, P, P, P, P, P, I, P]),
+    "gdmrMultiTail": (I, [I]),
     "gdmr_true_residual_noalloc": (I, [P, I, P, P, P, P]),
     "gdmr_export_deflation": (I, [P, P]),
     "gdmr_import_deflation": (I, [P, P]),
@@ -539,6 +540,12 @@ class System:
 
     def drop_deflation(self):
         _check(self.L.gdmr_drop_deflation(self._h), "gdmr_drop_deflation")
+
+
+def multi_tail(systems: int = -1) -> int:
+    """gdmrMultiTail: systems in flight at or below which multi_solve finishes on the systems'
+    own batched cycles (default 8; 0: lockstep to the end); returns the previous value."""
+    return int(load().gdmrMultiTail(int(systems)))
 
 
 def multi_solve(systems, Bs, tol=1e-10, max_cycles: int = 5000):

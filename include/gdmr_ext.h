@@ -253,6 +253,11 @@ int gdmr_solve_batch(gdmr_system *sys, int nrhs, const double *b, double *x, con
  * capacities must stay within the CTAs resident at once, a few hundred on a GB300). */
 int gdmr_multi_solve(int nops, gdmr_system *const *systems, const int *nrhs, const double *const *b, double *const *x,
                      const double *tol, int maxCycles, gdmr_stats *const *stats);
+/* gdmr_multi_solve's tail: once every right-hand side has been admitted and at most this many
+ * systems remain in flight (default 8), the remaining ones finish on each system's own batched
+ * cycles (as gdmr_solve_batch), operator by operator, instead of in the lockstep launch; 0 keeps
+ * the lockstep to the end.  systems < 0 only reads.  Returns the previous value. */
+int gdmrMultiTail(int systems);
 
 /* FP64 ||b_s - A x_s|| / ||b_s|| for nrhs pairs. */
 int gdmr_true_residual(gdmr_system *sys, int nrhs, const double *b, const double *x, int on_device, double *relres);
