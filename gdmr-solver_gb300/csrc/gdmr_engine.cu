@@ -956,6 +956,21 @@ int Engine<R>::refine_admit(int slot, const double2 *b, const double2 *x0, doubl
     return GDMR_OK;
 }
 
+// The stagnation rule of the restart (arnoldiSetupDMR, gDMR.cu:2600-2621): a system whose last
+// cycle stagnated starts from the Krylov vector at storage index kk + (m - k)/2 of that cycle
+// instead of from the unit residual, which k_demote_unit has already written as basis vector 0.
+template <class R> void Engine<R>::restart_vectors(const std::vector<int> &next, int kk) {
+    const int n = n_, m = m_, k = k_;
+    for (int s : next) {
+        Slot &S = slot_[s];
+        const int period = (2 * S.max_cycles) / (m - k);
+        if (S.loop_flag == 0 || (period != 0 && S.flag_count % period == 0)) continue;
+        const int idx = kk + (m - k) / 2 - kk_prev_;
+        if (idx > 0 && idx <= m)
+            cudaMemcpyAsync(Vs(s), Vs(s) + (size_t)idx * n, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
+    }
+}
+
 template <class R> int Engine<R>::refine_cycle(std::vector<int> *done) {
     const int n = n_, m = m_, k = k_;
     if (act_h_.empty()) return GDMR_OK;
@@ -1013,22 +1028,14 @@ template <class R> int Engine<R>::refine_cycle(std::vector<int> *done) {
     if (next.empty()) return sync_deflation();
     if (set_active(next) != GDMR_OK) return GDMR_ECUDA;
     na = (int)next.size();
-    // unit residual direction in precision R; the inner recursion starts at rho_abs = 1
-    launch_demote_unit<R>(n, r64_, n, R_, n, act_, na, state_, stream);
-    k_cycle_reset<<<1, 256, 0, stream>>>(act_, na, state_, 1);
+    // unit residual direction in precision R, also the first basis vector of every system (the
+    // side stream's deflation update reads the previous cycle's basis: join it first); the
+    // inner recursion starts at rho_abs = 1
     if (sync_deflation() != GDMR_OK) return GDMR_ECUDA;
+    launch_demote_unit<R>(n, r64_, n, R_, n, V_, strideV(), act_, na, state_, stream);
+    k_cycle_reset<<<1, 256, 0, stream>>>(act_, na, state_, 1);
     const int kk = (k > 0 && have_z_) ? k : 0;
-    for (int s : next) {
-        Slot &S = slot_[s];
-        const int period = (2 * S.max_cycles) / (m - k);
-        if (S.loop_flag == 0 || (period != 0 && S.flag_count % period == 0)) {
-            cudaMemcpyAsync(Vs(s), R_ + (size_t)s * n, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
-        } else {
-            const int idx = kk + (m - k) / 2 - kk_prev_;
-            if (idx > 0 && idx <= m)
-                cudaMemcpyAsync(Vs(s), Vs(s) + (size_t)idx * n, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
-        }
-    }
+    restart_vectors(next, kk);
     long mv = 0;
     // breakdown of unit vectors: an invariant subspace at working precision
     const double inner_tol = sizeof(R) == 4 ? 1e-6 : 1e-14;
@@ -1135,21 +1142,11 @@ template <class R> int Engine<R>::multi_front() {
     const std::vector<int> next = act_h_;
     const int na = (int)next.size();
     if (set_active(next) != GDMR_OK) return GDMR_ECUDA;
-    launch_demote_unit<R>(n, r64_, n, R_, n, act_, na, state_, stream);
-    k_cycle_reset<<<1, 256, 0, stream>>>(act_, na, state_, 1);
     if (sync_deflation() != GDMR_OK) return GDMR_ECUDA;
+    launch_demote_unit<R>(n, r64_, n, R_, n, V_, strideV(), act_, na, state_, stream);
+    k_cycle_reset<<<1, 256, 0, stream>>>(act_, na, state_, 1);
     const int kk = (k > 0 && have_z_) ? k : 0;
-    for (int s : next) {
-        Slot &S = slot_[s];
-        const int period = (2 * S.max_cycles) / (m - k);
-        if (S.loop_flag == 0 || (period != 0 && S.flag_count % period == 0)) {
-            cudaMemcpyAsync(Vs(s), R_ + (size_t)s * n, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
-        } else {
-            const int idx = kk + (m - k) / 2 - kk_prev_;
-            if (idx > 0 && idx <= m)
-                cudaMemcpyAsync(Vs(s), Vs(s) + (size_t)idx * n, sizeof(C) * n, cudaMemcpyDeviceToDevice, stream);
-        }
-    }
+    restart_vectors(next, kk);
     GDMR_CK(cudaMemcpyAsync(lead_dev_, &lead_host_, sizeof(int), cudaMemcpyHostToDevice, stream));
     long mv = 0;
     int rc = enqueue_front(kk, na, &mv);

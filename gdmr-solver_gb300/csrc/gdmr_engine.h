@@ -169,6 +169,7 @@ template <class R> class Engine {
     // multi_jobs appends one Krylov job per such system; multi_back waits for the event `after`
     // (the launch) and enqueues the rest of the cycle and the FP64 correction.  SELL operators.
     int multi_residual();
+    void restart_vectors(const std::vector<int> &next, int kk);
     int multi_select(std::vector<int> *done);
     int multi_front();
     void multi_jobs(std::vector<KrylovJob<R>> &jobs) const;

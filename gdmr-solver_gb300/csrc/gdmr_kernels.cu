@@ -4158,8 +4158,15 @@ __global__ void __launch_bounds__(NT) k_refine_update(int n, double2 *__restrict
     for (long i = (long)blockIdx.x * NT + threadIdx.x; i < n; i += (long)gridDim.x * NT) {
         C dv = d[i];
         double2 xv = x[i];
-        xv.x += sc * (double)dv.x;
-        xv.y += sc * (double)dv.y;
+        if constexpr (std::is_same<C, float2>::value) {
+            // the exact float -> double conversion by integer operations: two FP64 FMAs an
+            // element instead of four FP64-pipe instructions
+            xv.x = ::fma(sc, f2d_bits(dv.x), xv.x);
+            xv.y = ::fma(sc, f2d_bits(dv.y), xv.y);
+        } else {
+            xv.x += sc * (double)dv.x;
+            xv.y += sc * (double)dv.y;
+        }
         x[i] = xv;
         d[i] = czero<C>();
     }
@@ -4168,13 +4175,26 @@ __global__ void __launch_bounds__(NT) k_refine_update(int n, double2 *__restrict
 template <class R>
 __global__ void __launch_bounds__(NT) k_demote_unit(int n, const double2 *__restrict__ r0, size_t strideR,
                                                     typename CT<R>::t *__restrict__ h0, size_t strideH,
+                                                    typename CT<R>::t *__restrict__ v0, size_t strideV,
                                                     const int *__restrict__ act, const SysState *__restrict__ state) {
     using C = typename CT<R>::t;
     const int s = act[blockIdx.y];
     const double a = state[s].alpha;
+    const float af = (float)a;
     for (long i = (long)blockIdx.x * NT + threadIdx.x; i < n; i += (long)gridDim.x * NT) {
         double2 v = r0[(size_t)s * strideR + i];
-        h0[(size_t)s * strideH + i] = from_d<C>(make_double2(v.x * a, v.y * a));
+        C h;
+        if constexpr (std::is_same<C, float2>::value) {
+            // complex64: the double -> float conversion by integer operations (hi + lo rounds to
+            // nearest) and the scaling in FP32; two FP64 multiplies and two conversions per
+            // element, all on GB300's FP64 pipe, bounded this kernel
+            const dfr xr = d2df_bits(v.x), xi = d2df_bits(v.y);
+            h = make_float2((xr.hi + xr.lo) * af, (xi.hi + xi.lo) * af);
+        } else {
+            h = from_d<C>(make_double2(v.x * a, v.y * a));
+        }
+        h0[(size_t)s * strideH + i] = h;
+        if (v0) v0[(size_t)s * strideV + i] = h;
     }
 }
 
@@ -5351,10 +5371,12 @@ void launch_refine_update(int n, double2 *x, size_t strideX, typename CT<R>::t *
 
 template <class R>
 void launch_demote_unit(int n, const double2 *r64, size_t strideR, typename CT<R>::t *rhat, size_t strideH,
-                        const int *act, int nsys, const SysState *state, cudaStream_t st) {
+                        typename CT<R>::t *v0, size_t strideV, const int *act, int nsys, const SysState *state,
+                        cudaStream_t st) {
     if (nsys <= 0) return;
-    Launch L_(KC_OTHER, (double)(sizeof(typename CT<R>::t) + sizeof(double2)) * n * nsys, st, 1);
-    k_demote_unit<R><<<grid2(stream_grid<R>(n, nsys), nsys), NT, 0, st>>>(n, r64, strideR, rhat, strideH, act, state);
+    Launch L_(KC_OTHER, (double)((v0 ? 2 : 1) * sizeof(typename CT<R>::t) + sizeof(double2)) * n * nsys, st, 1);
+    k_demote_unit<R><<<grid2(stream_grid<R>(n, nsys), nsys), NT, 0, st>>>(n, r64, strideR, rhat, strideH, v0, strideV,
+                                                                          act, state);
 }
 
 template <class R>
@@ -5396,8 +5418,8 @@ void launch_broadcast_hdef(int m, int kk, const double2 *Hd, double2 *H, size_t 
                                      cudaStream_t);                                                                    \
     template void launch_refine_update<R>(int, double2 *, size_t, CT<R>::t *, size_t, const int *, int,                \
                                           const SysState *, cudaStream_t);                                             \
-    template void launch_demote_unit<R>(int, const double2 *, size_t, CT<R>::t *, size_t, const int *, int,            \
-                                        const SysState *, cudaStream_t);                                               \
+    template void launch_demote_unit<R>(int, const double2 *, size_t, CT<R>::t *, size_t, CT<R>::t *, size_t,         \
+                                        const int *, int, const SysState *, cudaStream_t);                             \
     template void launch_norm<R>(int, const CT<R>::t *, size_t, const int *, int, double2 *, unsigned *, SysState *,   \
                                  int, cudaStream_t);                                                                   \
     template int launch_krylov_multi<R>(const KrylovJob<R> *, const int *, int, int *, double, cudaStream_t);         \

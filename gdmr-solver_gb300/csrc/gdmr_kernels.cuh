@@ -492,10 +492,12 @@ void launch_copy_vec(int n, const typename CT<R>::t *src, size_t strideS, typena
 template <class R>
 void launch_refine_update(int n, double2 *x, size_t strideX, typename CT<R>::t *d, size_t strideD,
                           const int *act, int nsys, const SysState *state, cudaStream_t st);
-// rhat_s = (R) (r64_s / sqrt(nrm2_s)).
+// rhat_s = (R) (r64_s / sqrt(nrm2_s)); also into v0_s (the cycle's first basis vector) unless
+// v0 is null.
 template <class R>
 void launch_demote_unit(int n, const double2 *r64, size_t strideR, typename CT<R>::t *rhat, size_t strideH,
-                        const int *act, int nsys, const SysState *state, cudaStream_t st);
+                        typename CT<R>::t *v0, size_t strideV, const int *act, int nsys, const SysState *state,
+                        cudaStream_t st);
 // Squared norm of each active vector into state[s].nrm2 (and bnorm if set_bnorm).
 // mode 0: nrm2 only; 1: also bnorm = ||v||; 2: also rho_abs = ||v|| and alpha = 1/||v||.
 template <class R>
