@@ -10,6 +10,7 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -1027,15 +1028,35 @@ int multi_impl(int nops, gdmr_system *const *sys, const int *nrhs, const double 
         // own batched cycles finish the remaining systems, operator by operator
         const int tail = g_multi_tail.load();
         if (all_admitted && in_flight > 0 && in_flight <= tail) {
-            for (bool any = true; any;) {
-                any = false;
-                for (int o = 0; o < nops; ++o) {
-                    if (E[o]->active_count() == 0) continue;
-                    std::vector<int> done;
-                    int rc = E[o]->refine_cycle(&done);
-                    if (rc != GDMR_OK) { release(); return rc; }
-                    retire(o, done);
-                    any |= E[o]->active_count() > 0;
+            // one host thread per remaining operator drives its engine (each engine has its own
+            // stream and buffers, as the server's workers do), so their cycles overlap on the GPU
+            std::vector<std::thread> th;
+            std::vector<int> trc(nops, GDMR_OK);
+            std::vector<std::vector<std::pair<int, double>>> tdone(nops);
+            for (int o = 0; o < nops; ++o) {
+                if (E[o]->active_count() == 0) continue;
+                th.emplace_back([&, o] {
+                    if (cudaSetDevice(dev) != cudaSuccess) { trc[o] = GDMR_ECUDA; return; }
+                    while (E[o]->active_count() > 0) {
+                        std::vector<int> done;
+                        const int rc = E[o]->refine_cycle(&done);
+                        if (rc != GDMR_OK) { trc[o] = rc; return; }
+                        const double ms =
+                            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+                        for (int sl : done) tdone[o].emplace_back(sl, ms);
+                    }
+                });
+            }
+            for (auto &t : th) t.join();
+            for (int o = 0; o < nops; ++o) {
+                if (trc[o] != GDMR_OK) {
+                    release();
+                    return fail(trc[o], F, "a system's own cycles failed in the tail");
+                }
+                for (auto &d : tdone[o]) {
+                    const int r = slot_of[o][d.first];
+                    retire(o, std::vector<int>{d.first});
+                    if (stats && stats[o]) stats[o][r].latency_ms = d.second;   // when its thread saw it finish
                 }
             }
             break;

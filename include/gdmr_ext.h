@@ -262,8 +262,9 @@ int gdmr_multi_solve(int nops, gdmr_system *const *systems, const int *nrhs, con
                      const double *tol, int maxCycles, gdmr_stats *const *stats);
 /* gdmr_multi_solve's tail: once every right-hand side has been admitted and at most this many
  * systems remain in flight (default 8), the remaining ones finish on each system's own batched
- * cycles (as gdmr_solve_batch), operator by operator, instead of in the lockstep launch; 0 keeps
- * the lockstep to the end.  systems < 0 only reads.  Returns the previous value. */
+ * cycles (as gdmr_solve_batch), one host thread per system driving its own stream, instead of in
+ * the lockstep launch; 0 keeps the lockstep to the end.  systems < 0 only reads.  Returns the
+ * previous value. */
 int gdmrMultiTail(int systems);
 
 /* FP64 ||b_s - A x_s|| / ||b_s|| for nrhs pairs. */
