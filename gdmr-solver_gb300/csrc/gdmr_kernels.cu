@@ -3808,6 +3808,8 @@ struct SpmmStagePlan {
     int win;                     // staged index of x[r0]
 };
 
+constexpr int SS_MAXSYS = 512;   // systems a launch whose factors and slots are kept in shared memory
+
 __global__ void __launch_bounds__(SS_THREADS, 1)
     k_spmm_staged(int n, const int *__restrict__ slice_ptr, const int *__restrict__ cols,
                   const float2 *__restrict__ vals, const float2 *__restrict__ x0, size_t strideX,
@@ -3816,8 +3818,9 @@ __global__ void __launch_bounds__(SS_THREADS, 1)
                   size_t strideVO) {
     extern __shared__ __align__(128) unsigned char ss_sm[];
     __shared__ __align__(8) unsigned long long full[SS_NS], empty[SS_NS];
-    __shared__ int s_staged[SS_NS], s_bk[SS_NS][SS_SG];
-    __shared__ float s_al[SS_NS][SS_SG];
+    __shared__ int s_staged[SS_NS];
+    __shared__ int s_act[SS_MAXSYS], s_bk[SS_MAXSYS];
+    __shared__ float s_al[SS_MAXSYS];
     __shared__ volatile int s_abort;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ngroups = (nsys + SS_SG - 1) / SS_SG;
@@ -3825,6 +3828,13 @@ __global__ void __launch_bounds__(SS_THREADS, 1)
     const long my = items > (long)blockIdx.x ? (items - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
     const size_t vbytes = (size_t)plan.npat * SS_ROWS * sizeof(float2);
     const size_t stage_bytes = vbytes + (size_t)SS_SG * plan.xlen * sizeof(float2);
+    // the launch's systems, their normalisation factors (converted once) and broken flags
+    for (int g = tid; g < nsys; g += SS_THREADS) {
+        const int sy = act[g];
+        s_act[g] = sy;
+        s_al[g] = scale ? (float)scale[sy].alpha : 1.f;
+        s_bk[g] = scale ? scale[sy].broken : 0;
+    }
     if (tid == 0) {
         s_abort = 0;
         for (int b = 0; b < SS_NS; ++b) {
@@ -3835,54 +3845,74 @@ __global__ void __launch_bounds__(SS_THREADS, 1)
     }
     __syncthreads();
     if (warp == SS_CW) {
-        // ---- producer (one thread)
-        if (lane != 0) return;
+        // ---- producer warp.  An item's chunk metadata is loaded one item ahead by ten lanes
+        // (lanes 0-7 a slice's pattern flag each, lanes 8-9 the chunk's first and last slice
+        // offsets), so its latency overlaps the previous item; the copies are issued by all lanes.
         long last[SS_NS];
         for (int b = 0; b < SS_NS; ++b) last[b] = -1;
-        for (long k = 0; k < my && !s_abort; ++k) {
+        // per lane: the raw metadata of item k (a load whose value is used an item later)
+        auto meta_load = [&](long k) -> int {
+            const long it = blockIdx.x + k * (long)gridDim.x, c = it / ngroups, r0 = c * SS_ROWS;
+            if (!(r0 - SS_WIN >= 0 && r0 + SS_ROWS + SS_WIN <= n)) return 0;   // not a full chunk
+            if (lane < 8) return pat.uniform[c * 8 + lane] != 0;
+            if (lane == 8) return slice_ptr[c * 8];
+            if (lane == 9) return slice_ptr[c * 8 + 8];
+            return 1;
+        };
+        // warp-uniform: the chunk's first value offset and whether it is staged
+        auto meta_use = [&](long k, int v, int &beg, int &ok) {
+            const long it = blockIdx.x + k * (long)gridDim.x, c = it / ngroups, r0 = c * SS_ROWS;
+            const bool full_chunk = r0 - SS_WIN >= 0 && r0 + SS_ROWS + SS_WIN <= n;
+            const unsigned flags = __ballot_sync(0xffffffffu, lane >= 8 || v != 0);
+            const int b0 = __shfl_sync(0xffffffffu, v, 8), b1 = __shfl_sync(0xffffffffu, v, 9);
+            beg = b0;
+            ok = full_chunk && flags == 0xffffffffu && b1 - b0 == 8 * 32 * plan.npat;
+        };
+        int pending = my > 0 ? meta_load(0) : 0;
+        for (long k = 0; k < my; ++k) {
+            if (__shfl_sync(0xffffffffu, (int)s_abort, 0)) break;
             const int b = (int)(k % SS_NS);
             const long use = k / SS_NS;
-            if (use > 0 && !bk_wait(bk_u32(&empty[b]), (uint32_t)((use - 1) & 1), &s_abort, c_wait_cycles)) {
+            int beg, st;
+            meta_use(k, pending, beg, st);
+            if (k + 1 < my) pending = meta_load(k + 1);
+            int ok = 1;
+            if (lane == 0 && use > 0 && !bk_wait(bk_u32(&empty[b]), (uint32_t)((use - 1) & 1), &s_abort, c_wait_cycles)) {
                 if (!s_abort) { atomicAdd(&g_bulk_timeouts, 1u); s_abort = 1; }
-                break;
+                ok = 0;
             }
+            if (!__shfl_sync(0xffffffffu, ok, 0)) break;
             const long it = blockIdx.x + k * (long)gridDim.x, c = it / ngroups;
             const int g0 = (int)(it % ngroups) * SS_SG, ng = min(SS_SG, nsys - g0);
             const long r0 = c * SS_ROWS;
-            // staged only for a full chunk of 8 pattern-stored slices of the pattern's width
-            // whose window stays inside 0..n-1
-            bool st = r0 - SS_WIN >= 0 && r0 + SS_ROWS + SS_WIN <= n &&
-                      slice_ptr[c * 8 + 8] - slice_ptr[c * 8] == 8 * 32 * plan.npat;
-            for (int j = 0; st && j < 8; ++j) st = pat.uniform[c * 8 + j] != 0;
-            s_staged[b] = st ? 1 : 0;
-            for (int gg = 0; gg < SS_SG; ++gg) {
-                float al = 1.f;
-                int bk = 0;
-                if (scale && gg < ng) {
-                    al = (float)scale[act[g0 + gg]].alpha;
-                    bk = scale[act[g0 + gg]].broken;
-                }
-                s_al[b][gg] = al;
-                s_bk[b][gg] = bk;
-            }
             unsigned char *base = ss_sm + (size_t)b * stage_bytes;
+            if (lane == 0) {
+                s_staged[b] = st;
+                if (st) bk_arrive_tx(bk_u32(&full[b]), (uint32_t)(vbytes + (size_t)ng * plan.xlen * sizeof(float2)));
+            }
+            __syncwarp();
             if (st) {
-                bk_arrive_tx(bk_u32(&full[b]), (uint32_t)(vbytes + (size_t)ng * plan.xlen * sizeof(float2)));
-                bk_copy(bk_u32(base), vals + slice_ptr[c * 8], (uint32_t)vbytes, bk_u32(&full[b]));
-                for (int gg = 0; gg < ng; ++gg) {
-                    const float2 *x = x0 + (size_t)act[g0 + gg] * strideX + r0;
-                    for (int r = 0; r < plan.nr; ++r)
+                // copy 0: the slices' values; copy 1 + gg * nr + r: range r of system gg
+                const int ncopy = 1 + ng * plan.nr;
+                for (int q = lane; q < ncopy; q += 32) {
+                    if (q == 0) {
+                        bk_copy(bk_u32(base), vals + beg, (uint32_t)vbytes, bk_u32(&full[b]));
+                    } else {
+                        const int gg = (q - 1) / plan.nr, r = (q - 1) - gg * plan.nr;
+                        const float2 *x = x0 + (size_t)s_act[g0 + gg] * strideX + r0;
                         bk_copy(bk_u32(base + vbytes + ((size_t)gg * plan.xlen + plan.rbase[r]) * sizeof(float2)),
                                 x + plan.rstart[r], (uint32_t)(plan.rlen[r] * sizeof(float2)), bk_u32(&full[b]));
+                    }
                 }
-            } else {
+            } else if (lane == 0) {
                 bk_arrive(bk_u32(&full[b]));   // nothing staged: the consumers read global memory
             }
             last[b] = use;
         }
-        for (int b = 0; b < SS_NS; ++b)   // no copy in flight when the CTA exits (fixed bound)
-            if (last[b] >= 0 && !bk_wait(bk_u32(&full[b]), (uint32_t)(last[b] & 1), nullptr, BK_WAIT_CYCLES))
-                atomicAdd(&g_bulk_timeouts, 1u);
+        if (lane == 0)
+            for (int b = 0; b < SS_NS; ++b)   // no copy in flight when the CTA exits (fixed bound)
+                if (last[b] >= 0 && !bk_wait(bk_u32(&full[b]), (uint32_t)(last[b] & 1), nullptr, BK_WAIT_CYCLES))
+                    atomicAdd(&g_bulk_timeouts, 1u);
         return;
     }
     // ---- consumers: thread t is row r0 + t of the item
@@ -3906,13 +3936,13 @@ __global__ void __launch_bounds__(SS_THREADS, 1)
 #pragma unroll
                 for (int e = 0; e < SELL_PATTERN; ++e)
                     if (e < plan.npat) cfma(acc, v[e], xs[plan.eidx[e] + t]);
-                const int sys = act[g0 + gg];
+                const int sys = s_act[g0 + gg];
                 if (scale) {
-                    const float al = s_al[b][gg];
+                    const float al = s_al[g0 + gg];
                     float2 vv = xs[plan.win + t];
                     vv.x *= al;
                     vv.y *= al;
-                    if (s_bk[b][gg]) vv = czero<float2>();
+                    if (s_bk[g0 + gg]) vv = czero<float2>();
                     vout0[(size_t)sys * strideVO + row] = vv;
                     acc.x *= al;
                     acc.y *= al;
@@ -3923,7 +3953,7 @@ __global__ void __launch_bounds__(SS_THREADS, 1)
             const int slice = (int)(row >> 5);
             const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
             for (int gg = 0; gg < ng; ++gg) {
-                const int sys = act[g0 + gg];
+                const int sys = s_act[g0 + gg];
                 const float2 *x = x0 + (size_t)sys * strideX;
                 float2 acc = czero<float2>();
                 for (int e = 0; e < width; ++e) {
@@ -3931,11 +3961,11 @@ __global__ void __launch_bounds__(SS_THREADS, 1)
                     cfma(acc, vals[idx], x[cols[idx]]);
                 }
                 if (scale) {
-                    const float al = s_al[b][gg];
+                    const float al = s_al[g0 + gg];
                     float2 vv = x[row];
                     vv.x *= al;
                     vv.y *= al;
-                    if (s_bk[b][gg]) vv = czero<float2>();
+                    if (s_bk[g0 + gg]) vv = czero<float2>();
                     vout0[(size_t)sys * strideVO + row] = vv;
                     acc.x *= al;
                     acc.y *= al;
@@ -5289,7 +5319,8 @@ void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX
         SpmmStagePlan pl;
         size_t smem = 0;
         auto al16 = [](const void *p) { return ((uintptr_t)p & 15u) == 0; };
-        if (spmm_staged() && spmm_stage_plan(A, pl, &smem) && al16(x) && al16(A.vals) && strideX % 2 == 0) {
+        if (spmm_staged() && nsys <= SS_MAXSYS && spmm_stage_plan(A, pl, &smem) && al16(x) && al16(A.vals) &&
+            strideX % 2 == 0) {
             allow_smem(k_spmm_staged, smem);
             k_spmm_staged<<<num_sms(), SS_THREADS, smem, st>>>(A.n, A.slice_ptr, A.cols, (const float2 *)A.vals, x,
                                                               strideX, y, strideY, act, nsys, sell_pattern(A), pl,
