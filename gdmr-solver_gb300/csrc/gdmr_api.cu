@@ -411,7 +411,6 @@ extern "C" double gdmrWaitLimit(double ms) {
 }
 extern "C" void gdmrInjectAllocFailure(int nth) { inject_alloc_failure(nth); }
 extern "C" void gdmrCombineGroup(int enable) { set_combine_group(enable); }
-extern "C" void gdmrSpmmStaged(int enable) { set_spmm_staged(enable); }
 // Systems in flight at or below which gdmr_multi_solve finishes on the engines' own cycles.
 static std::atomic<int> g_multi_tail{8};
 extern "C" int gdmrMultiTail(int systems) {

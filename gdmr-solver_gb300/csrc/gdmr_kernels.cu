@@ -3780,238 +3780,6 @@ __global__ void __launch_bounds__(NT, 2) k_spmv2(int n, const int *__restrict__ 
     }
 }
 
-// ----------------------------------------------------------------- staged batched SpMM
-// The complex64 batched SELL-32 product with its gathers staged in shared memory.  A work item
-// is 256 rows (8 SELL slices) for 8 systems.  When the 8 slices are pattern-stored, the rows'
-// x values lie in a few contiguous ranges per system: one range of 256 per large column offset
-// (+-Q, +-P of a grid stencil) and one window x[r0 - 2 .. r0 + 258) for the offsets -2..+2.  A
-// producer warp copies the slices' values and those ranges into shared memory with
-// cp.async.bulk (the TMA engine) two items ahead, behind "full"/"empty" mbarriers, and eight
-// consumer warps (one row a thread) compute from shared memory: no gather waits on HBM or L2.
-// Terms are added in entry order, as k_spmm does (the same values).  Other chunks (boundary
-// planes, the partial last chunk) are computed from global memory as k_spmm computes them.
-// Persistent CTAs, one a SM (two stages of ~97 KB for a 7-point pattern); items are strided
-// over the CTAs with the system group fastest, so a chunk's values and halo ranges are read from
-// HBM once and from L2 by the other groups.  Every wait is bounded (the process's wait limit; a
-// timeout is counted in g_bulk_timeouts and the kernel stops), and the producer waits for its
-// last copies before the CTA exits.
-constexpr int SS_ROWS = 256, SS_SG = 8, SS_CONS = 256, SS_CW = SS_CONS / 32, SS_THREADS = SS_CONS + 32;
-constexpr int SS_WIN = 2, SS_NS = 2;
-struct SpmmStagePlan {
-    int npat;                    // entries a row (the pattern width)
-    int nr;                      // staged ranges a system
-    int rstart[SELL_PATTERN];    // range r covers x[r0 + rstart[r] .. + rlen[r])
-    int rlen[SELL_PATTERN];      // elements (even: 16-byte copies)
-    int rbase[SELL_PATTERN];     // element offset of range r in a system's staged x
-    int eidx[SELL_PATTERN];      // entry e of row r0 + t reads staged x[eidx[e] + t]
-    int xlen;                    // staged elements a system
-    int win;                     // staged index of x[r0]
-};
-
-constexpr int SS_MAXSYS = 512;   // systems a launch whose factors and slots are kept in shared memory
-
-__global__ void __launch_bounds__(SS_THREADS, 1)
-    k_spmm_staged(int n, const int *__restrict__ slice_ptr, const int *__restrict__ cols,
-                  const float2 *__restrict__ vals, const float2 *__restrict__ x0, size_t strideX,
-                  float2 *__restrict__ y0, size_t strideY, const int *__restrict__ act, int nsys, SellPattern pat,
-                  SpmmStagePlan plan, const SysState *__restrict__ scale, float2 *__restrict__ vout0,
-                  size_t strideVO) {
-    extern __shared__ __align__(128) unsigned char ss_sm[];
-    __shared__ __align__(8) unsigned long long full[SS_NS], empty[SS_NS];
-    __shared__ int s_staged[SS_NS];
-    __shared__ int s_act[SS_MAXSYS], s_bk[SS_MAXSYS];
-    __shared__ float s_al[SS_MAXSYS];
-    __shared__ volatile int s_abort;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int ngroups = (nsys + SS_SG - 1) / SS_SG;
-    const long nch = ((long)n + SS_ROWS - 1) / SS_ROWS, items = nch * ngroups;
-    const long my = items > (long)blockIdx.x ? (items - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
-    const size_t vbytes = (size_t)plan.npat * SS_ROWS * sizeof(float2);
-    const size_t stage_bytes = vbytes + (size_t)SS_SG * plan.xlen * sizeof(float2);
-    // the launch's systems, their normalisation factors (converted once) and broken flags
-    for (int g = tid; g < nsys; g += SS_THREADS) {
-        const int sy = act[g];
-        s_act[g] = sy;
-        s_al[g] = scale ? (float)scale[sy].alpha : 1.f;
-        s_bk[g] = scale ? scale[sy].broken : 0;
-    }
-    if (tid == 0) {
-        s_abort = 0;
-        for (int b = 0; b < SS_NS; ++b) {
-            bk_init(bk_u32(&full[b]), 1);
-            bk_init(bk_u32(&empty[b]), SS_CW);
-        }
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    }
-    __syncthreads();
-    if (warp == SS_CW) {
-        // ---- producer warp.  An item's chunk metadata is loaded one item ahead by ten lanes
-        // (lanes 0-7 a slice's pattern flag each, lanes 8-9 the chunk's first and last slice
-        // offsets), so its latency overlaps the previous item; the copies are issued by all lanes.
-        long last[SS_NS];
-        for (int b = 0; b < SS_NS; ++b) last[b] = -1;
-        // per lane: the raw metadata of item k (a load whose value is used an item later)
-        auto meta_load = [&](long k) -> int {
-            const long it = blockIdx.x + k * (long)gridDim.x, c = it / ngroups, r0 = c * SS_ROWS;
-            if (!(r0 - SS_WIN >= 0 && r0 + SS_ROWS + SS_WIN <= n)) return 0;   // not a full chunk
-            if (lane < 8) return pat.uniform[c * 8 + lane] != 0;
-            if (lane == 8) return slice_ptr[c * 8];
-            if (lane == 9) return slice_ptr[c * 8 + 8];
-            return 1;
-        };
-        // warp-uniform: the chunk's first value offset and whether it is staged
-        auto meta_use = [&](long k, int v, int &beg, int &ok) {
-            const long it = blockIdx.x + k * (long)gridDim.x, c = it / ngroups, r0 = c * SS_ROWS;
-            const bool full_chunk = r0 - SS_WIN >= 0 && r0 + SS_ROWS + SS_WIN <= n;
-            const unsigned flags = __ballot_sync(0xffffffffu, lane >= 8 || v != 0);
-            const int b0 = __shfl_sync(0xffffffffu, v, 8), b1 = __shfl_sync(0xffffffffu, v, 9);
-            beg = b0;
-            ok = full_chunk && flags == 0xffffffffu && b1 - b0 == 8 * 32 * plan.npat;
-        };
-        int pending = my > 0 ? meta_load(0) : 0;
-        for (long k = 0; k < my; ++k) {
-            if (__shfl_sync(0xffffffffu, (int)s_abort, 0)) break;
-            const int b = (int)(k % SS_NS);
-            const long use = k / SS_NS;
-            int beg, st;
-            meta_use(k, pending, beg, st);
-            if (k + 1 < my) pending = meta_load(k + 1);
-            int ok = 1;
-            if (lane == 0 && use > 0 && !bk_wait(bk_u32(&empty[b]), (uint32_t)((use - 1) & 1), &s_abort, c_wait_cycles)) {
-                if (!s_abort) { atomicAdd(&g_bulk_timeouts, 1u); s_abort = 1; }
-                ok = 0;
-            }
-            if (!__shfl_sync(0xffffffffu, ok, 0)) break;
-            const long it = blockIdx.x + k * (long)gridDim.x, c = it / ngroups;
-            const int g0 = (int)(it % ngroups) * SS_SG, ng = min(SS_SG, nsys - g0);
-            const long r0 = c * SS_ROWS;
-            unsigned char *base = ss_sm + (size_t)b * stage_bytes;
-            if (lane == 0) {
-                s_staged[b] = st;
-                if (st) bk_arrive_tx(bk_u32(&full[b]), (uint32_t)(vbytes + (size_t)ng * plan.xlen * sizeof(float2)));
-            }
-            __syncwarp();
-            if (st) {
-                // copy 0: the slices' values; copy 1 + gg * nr + r: range r of system gg
-                const int ncopy = 1 + ng * plan.nr;
-                for (int q = lane; q < ncopy; q += 32) {
-                    if (q == 0) {
-                        bk_copy(bk_u32(base), vals + beg, (uint32_t)vbytes, bk_u32(&full[b]));
-                    } else {
-                        const int gg = (q - 1) / plan.nr, r = (q - 1) - gg * plan.nr;
-                        const float2 *x = x0 + (size_t)s_act[g0 + gg] * strideX + r0;
-                        bk_copy(bk_u32(base + vbytes + ((size_t)gg * plan.xlen + plan.rbase[r]) * sizeof(float2)),
-                                x + plan.rstart[r], (uint32_t)(plan.rlen[r] * sizeof(float2)), bk_u32(&full[b]));
-                    }
-                }
-            } else if (lane == 0) {
-                bk_arrive(bk_u32(&full[b]));   // nothing staged: the consumers read global memory
-            }
-            last[b] = use;
-        }
-        if (lane == 0)
-            for (int b = 0; b < SS_NS; ++b)   // no copy in flight when the CTA exits (fixed bound)
-                if (last[b] >= 0 && !bk_wait(bk_u32(&full[b]), (uint32_t)(last[b] & 1), nullptr, BK_WAIT_CYCLES))
-                    atomicAdd(&g_bulk_timeouts, 1u);
-        return;
-    }
-    // ---- consumers: thread t is row r0 + t of the item
-    const int t = tid, j = t >> 5;
-    for (long k = 0; k < my; ++k) {
-        const int b = (int)(k % SS_NS);
-        if (!bk_warp_wait(bk_u32(&full[b]), (uint32_t)((k / SS_NS) & 1), &s_abort, lane)) break;
-        const long it = blockIdx.x + k * (long)gridDim.x, c = it / ngroups;
-        const int g0 = (int)(it % ngroups) * SS_SG, ng = min(SS_SG, nsys - g0);
-        const long row = c * SS_ROWS + t;
-        if (s_staged[b]) {
-            const float2 *sv = reinterpret_cast<const float2 *>(ss_sm + (size_t)b * stage_bytes);
-            const float2 *sx = sv + (size_t)plan.npat * SS_ROWS;
-            float2 v[SELL_PATTERN];
-#pragma unroll
-            for (int e = 0; e < SELL_PATTERN; ++e)
-                v[e] = e < plan.npat ? sv[(j * plan.npat + e) * 32 + lane] : czero<float2>();
-            for (int gg = 0; gg < ng; ++gg) {
-                const float2 *xs = sx + (size_t)gg * plan.xlen;
-                float2 acc = czero<float2>();
-#pragma unroll
-                for (int e = 0; e < SELL_PATTERN; ++e)
-                    if (e < plan.npat) cfma(acc, v[e], xs[plan.eidx[e] + t]);
-                const int sys = s_act[g0 + gg];
-                if (scale) {
-                    const float al = s_al[g0 + gg];
-                    float2 vv = xs[plan.win + t];
-                    vv.x *= al;
-                    vv.y *= al;
-                    if (s_bk[g0 + gg]) vv = czero<float2>();
-                    vout0[(size_t)sys * strideVO + row] = vv;
-                    acc.x *= al;
-                    acc.y *= al;
-                }
-                y0[(size_t)sys * strideY + row] = acc;
-            }
-        } else if (row < n) {
-            const int slice = (int)(row >> 5);
-            const int beg = slice_ptr[slice], width = (slice_ptr[slice + 1] - beg) >> 5;
-            for (int gg = 0; gg < ng; ++gg) {
-                const int sys = s_act[g0 + gg];
-                const float2 *x = x0 + (size_t)sys * strideX;
-                float2 acc = czero<float2>();
-                for (int e = 0; e < width; ++e) {
-                    const int idx = beg + e * 32 + lane;
-                    cfma(acc, vals[idx], x[cols[idx]]);
-                }
-                if (scale) {
-                    const float al = s_al[g0 + gg];
-                    float2 vv = x[row];
-                    vv.x *= al;
-                    vv.y *= al;
-                    if (s_bk[g0 + gg]) vv = czero<float2>();
-                    vout0[(size_t)sys * strideVO + row] = vv;
-                    acc.x *= al;
-                    acc.y *= al;
-                }
-                y0[(size_t)sys * strideY + row] = acc;
-            }
-        }
-        __syncwarp();
-        if (lane == 0) bk_arrive(bk_u32(&empty[b]));
-    }
-}
-
-// The staged product's plan for A (false: not applicable).
-inline bool spmm_stage_plan(const SellMatrix &A, SpmmStagePlan &pl, size_t *smem) {
-    if (A.npat <= 0 || !A.uniform) return false;
-    pl = SpmmStagePlan{};
-    pl.npat = A.npat;
-    int r = 0;
-    for (int e = 0; e < A.npat; ++e) {   // large offsets: a range each (offsets ascend)
-        const int off = A.pat[e];
-        if (off >= -SS_WIN && off <= SS_WIN) continue;
-        if (off % 2 != 0) return false;  // a range must start 16-byte aligned
-        pl.rstart[r] = off;
-        pl.rlen[r] = SS_ROWS;
-        ++r;
-    }
-    pl.rstart[r] = -SS_WIN;              // the window: offsets -2..+2 and x[r0..] for v
-    pl.rlen[r] = SS_ROWS + 2 * SS_WIN;
-    const int wr = r++;
-    pl.nr = r;
-    int base = 0;
-    for (int q = 0; q < r; ++q) {
-        pl.rbase[q] = base;
-        base += pl.rlen[q];
-    }
-    pl.xlen = base;
-    pl.win = pl.rbase[wr] + SS_WIN;
-    for (int e = 0, q = 0; e < A.npat; ++e) {
-        const int off = A.pat[e];
-        if (off >= -SS_WIN && off <= SS_WIN) pl.eidx[e] = pl.rbase[wr] + SS_WIN + off;
-        else pl.eidx[e] = pl.rbase[q++];
-    }
-    *smem = (size_t)SS_NS * ((size_t)pl.npat * SS_ROWS + (size_t)SS_SG * pl.xlen) * sizeof(float2);
-    return *smem <= 220 * 1024;
-}
-
 // Grid (system groups, row chunks): the groups of one row chunk run together, so the
 // matrix slice is read from HBM once and from L2 for the other groups.
 template <class R, int SG>
@@ -5264,9 +5032,6 @@ void set_combine_group(int on) { g_combine_group.store(on ? 1 : 0); }
 int combine_group() { return g_combine_group.load(); }
 static std::atomic<int> g_grid_operator{1};
 static std::atomic<int> g_grid_batch{0};
-static std::atomic<int> g_spmm_staged{1};
-void set_spmm_staged(int on) { g_spmm_staged.store(on ? 1 : 0); }
-int spmm_staged() { return g_spmm_staged.load(); }
 void set_grid_operator(int enable) { g_grid_operator.store(enable ? 1 : 0); }
 int grid_operator() { return g_grid_operator.load(); }
 void set_grid_batch(int sg) { g_grid_batch.store(sg == 1 || sg == 2 || sg == 4 ? sg : 0); }
@@ -5315,19 +5080,6 @@ void launch_spmm(const SellMatrix &A, const typename CT<R>::t *x, size_t strideX
         return;
     }
     constexpr int SG = 8;
-    if constexpr (sizeof(R) == 4) {
-        SpmmStagePlan pl;
-        size_t smem = 0;
-        auto al16 = [](const void *p) { return ((uintptr_t)p & 15u) == 0; };
-        if (spmm_staged() && nsys <= SS_MAXSYS && spmm_stage_plan(A, pl, &smem) && al16(x) && al16(A.vals) &&
-            strideX % 2 == 0) {
-            allow_smem(k_spmm_staged, smem);
-            k_spmm_staged<<<num_sms(), SS_THREADS, smem, st>>>(A.n, A.slice_ptr, A.cols, (const float2 *)A.vals, x,
-                                                              strideX, y, strideY, act, nsys, sell_pattern(A), pl,
-                                                              scale, vout, strideVO);
-            return;
-        }
-    }
     int rows = (A.n + NT - 1) / NT;
     dim3 grid((nsys + SG - 1) / SG, rows < 65535 ? rows : 65535);
     k_spmm<R, SG><<<grid, NT, 0, st>>>(A.n, A.slice_ptr, A.cols, (const typename CT<R>::t *)A.vals, x, strideX, y,

@@ -347,10 +347,6 @@ void set_grid_operator(int enable);
 int grid_operator();
 void set_grid_batch(int sg);
 int grid_batch();
-// Complex64 batched SELL products with their gathers staged in shared memory by bulk copies
-// (on by default; k_spmm_staged), else k_spmm.  Both give the same values.
-void set_spmm_staged(int on);
-int spmm_staged();
 // Matrix-free constant-coefficient stencil on an nx x ny x nz grid (nz = 1: 5-point 2D),
 // unknowns numbered i + nx (j + ny l), Dirichlet boundary (neighbours outside are dropped):
 //   y = d x + wx (x[i-1] + x[i+1]) + wy (x[j-1] + x[j+1]) + wz (x[l-1] + x[l+1]).

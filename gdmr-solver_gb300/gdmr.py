@@ -64,7 +64,6 @@ SIGNATURES = {
     "gdmrGridOperator": (None, [I]),
     "gdmrGridBatch": (None, [I]),
     "gdmrCombineGroup": (None, [I]),
-    "gdmrSpmmStaged": (None, [I]),
     "gdmr_csr_grid_form": (I, [I, P, P, P, P]),
     "gdmrAsyncTimeouts": (ctypes.c_uint, []),
     "gdmr_hessenberg_svd": (I, [I, I, P, P, P, P]),
@@ -196,11 +195,6 @@ def grid_batch(systems_per_thread: int) -> None:
 def combine_group(enable: bool) -> None:
     """Cycle-end combinations of batches four systems a CTA (on by default) or one."""
     load().gdmrCombineGroup(1 if enable else 0)
-
-
-def spmm_staged(enable: bool) -> None:
-    """Complex64 batched operator products with gathers staged by bulk copies (on by default)."""
-    load().gdmrSpmmStaged(1 if enable else 0)
 
 
 def csr_grid_form(A):

@@ -176,13 +176,6 @@ void gdmrGridBatch(int systemsPerThread);
  * loaded once for the four (on by default); 0 returns them to one system a CTA. */
 void gdmrCombineGroup(int enable);
 
-/* Complex64 batched SELL-32 products with their gathers staged in shared memory (on by default):
- * for 256 rows of pattern-stored slices, a producer warp bulk-copies (cp.async.bulk) the rows'
- * values and the contiguous ranges of x their column offsets span, and the other warps compute
- * from shared memory.  0 returns them to the register kernel.  Both add a row's terms in the
- * same order (the same values). */
-void gdmrSpmmStaged(int enable);
-
 /* Host-only check of a CSR matrix (complex values interleaved re, im) for the structured-grid
  * form: dims[0..2] <- (nx, ny, nz), zeros if it has none.  GDMR_EINVAL for malformed arrays. */
 int gdmr_csr_grid_form(int n, const int *rowPtr, const int *colIdx, const double *vals_ri, int *dims);

@@ -93,31 +93,3 @@ def test_grouped_combination_matches_one_system_a_cta(batch20, precision):
     assert max(abs(a - b) for a, b in zip(cg, cs)) <= 2, (cg, cs)
 
 
-
-@pytest.mark.parametrize("shape", [(64, 64), (20, 18, 16)], ids=["2d", "3d"])
-def test_staged_spmm_matches_the_register_kernel(shape):
-    """The complex64 batched product with its gathers staged in shared memory by bulk copies
-    (pattern-stored 256-row chunks; boundary chunks from global memory) against the register
-    kernel: the same terms in the same order, so with the Gram-Schmidt variants pinned a batch
-    of 12 systems (more than one group of 8) is bit for bit the same, and solves."""
-    import scipy.sparse.linalg as spl
-    A = problems.helmholtz(shape, 6.0, 0.1)
-    rhs = np.array([problems.unit_gaussian_rhs(A.n, 70 + s) for s in range(12)])
-    out = {}
-    for staged in (True, False):
-        gdmr.spmm_staged(staged)
-        gdmr.tune_force(0, 0)
-        try:
-            s = gdmr.System(A, 30, 8, capacity=12, precision="mixed")
-            out[staged] = s.solve_batch(rhs, tol=1e-10, max_cycles=2000)
-        finally:
-            gdmr.spmm_staged(True)
-            gdmr.tune_force(-1, -1)
-    (Xs, ss), (Xr, sr) = out[True], out[False]
-    assert [t["cycles"] for t in ss] == [t["cycles"] for t in sr]
-    assert np.array_equal(Xs, Xr)
-    lu = spl.splu(A.to_scipy().tocsc())
-    for b, x, t in zip(rhs, Xs, ss):
-        assert t["status"] == 0 and t["true_rel_res"] <= 1.5e-10
-        d = lu.solve(b)
-        assert np.linalg.norm(x - d) / np.linalg.norm(d) < 1e-8
