@@ -939,10 +939,11 @@ int wproj_tc_grid(int n) {
 }
 
 int launch_wproj_tc(int n, int kk, const float2 *W, const float2 *Y, size_t strideY, const int *act, int nsys,
-                    double *part, double2 *coef, size_t strideC, cudaStream_t st) {
+                    double *part, double2 *coef, size_t strideC, cudaStream_t st, int ctas) {
     int dev = 0;
     cudaGetDevice(&dev);
-    const int G = wproj_tc_grid(n);
+    int G = wproj_tc_grid(n);
+    if (ctas > 0 && ctas < G) G = ctas;
     const int np = ((nsys + 15) / 16) * 16;
     const size_t smem = tc_smem_bytes(np);
     {
