@@ -4469,38 +4469,6 @@ void update_wreg_run(int n, int kk, const typename CT<R>::t *W, const typename C
     }
 }
 
-// A side stream and fork/join events per device and host thread (each host thread driving an
-// engine gets its own, so concurrent engines never share an event), created on first use.
-struct TcSide {
-    cudaStream_t side = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
-    bool ok() const { return side && fork && join; }
-};
-struct TcSides {
-    std::vector<TcSide> dev;
-    ~TcSides() {
-        for (auto &d : dev) {
-            if (d.fork) cudaEventDestroy(d.fork);
-            if (d.join) cudaEventDestroy(d.join);
-            if (d.side) cudaStreamDestroy(d.side);
-        }
-    }
-};
-inline TcSide &tc_side() {
-    static thread_local TcSides sides;
-    int d = 0;
-    cudaGetDevice(&d);
-    if ((int)sides.dev.size() <= d) sides.dev.resize(d + 1);
-    TcSide &s = sides.dev[d];
-    if (!s.side) {
-        if (cudaStreamCreateWithFlags(&s.side, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming) != cudaSuccess)
-            cudaGetLastError();
-    }
-    return s;
-}
-
 // k_update_rows over about two CTAs a SM, each on a contiguous range of chunks; false (nothing
 // launched) when the batch or the partials do not fit.
 inline bool update_rows_run(int n, int kk, const float2 *W, const float2 *V, size_t strideV, int qb,
@@ -4538,38 +4506,6 @@ int mdot_dispatch(int v, int n, const typename CT<R>::t *segA, int qa, const typ
     auto fits = [&](int ept) { return (size_t)nsys * qmax * 2 * (((size_t)n + NT * ept - 1) / (NT * ept)) <= cap; };
     constexpr int VW = sizeof(R) == 4 ? 9 : 7;   // batched shared-W variant
     if constexpr (sizeof(R) == 4) {
-        // 11: the tensor-core shared part on a side stream with a third of the SMs, beside the
-        // own-basis part on the others.  The tensor-core kernel is bound by its producer warps'
-        // issue, not by HBM, so the own part's streaming fills the bandwidth it leaves; its
-        // partials sit at the top of the scratch, clear of the own part's.
-        if (v == 11) {
-            const int tc_ctas = num_sms() / 3;
-            const size_t tc_need = (size_t)tc_ctas * qa * nsys * 2;
-            const size_t own_worst = (size_t)nsys * qmax * 2 * (((size_t)n + NT - 1) / NT);
-            if (qa > 0 && qb > 0 && tc_ctas > 0 && wproj_tc_ok(n, qa, nsys, segA, w, strideW) &&
-                own_worst + tc_need <= cap) {
-                TcSide &sd = tc_side();
-                if (sd.ok()) {
-                    int vown = 0;
-                    {
-                        std::lock_guard<std::mutex> lk(g_tune_mu);
-                        for (auto &e : g_tuned)
-                            if (e.key == TuneKey{prec_key<R>(), 0, n, bucket_of(nsys, 0)}) vown = e.variant;
-                    }
-                    if (vown >= VW) vown = 0;
-                    cudaEventRecord(sd.fork, st);
-                    cudaStreamWaitEvent(sd.side, sd.fork, 0);
-                    const int k1 = launch_wproj_tc(n, qa, segA, w, strideW, act, nsys, (double *)partials + cap - tc_need,
-                                                   coef, strideC, sd.side, tc_ctas);
-                    const int k2 = mdot_dispatch<R>(vown, n, nullptr, 0, segB, strideB, qb, w, strideW, act, nsys,
-                                                    partials, qmax, tickets, coef + qa, strideC, state, skip_broken, st);
-                    cudaEventRecord(sd.join, sd.side);
-                    cudaStreamWaitEvent(st, sd.join, 0);
-                    return k1 + k2;
-                }
-            }
-            v = 10;
-        }
         if (v == 10) {   // batched shared-W projection on the tensor cores
             if (qa > 0 && wproj_tc_ok(n, qa, nsys, segA, w, strideW) &&
                 (size_t)qa * nsys * 2 * wproj_tc_grid(n) <= cap) {
@@ -4705,7 +4641,7 @@ void launch_mdot(int n, const typename CT<R>::t *segA, int qa, const typename CT
     };
     int v = 0;
     if (forced_variant(0) >= 0) v = forced_variant(0);
-    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(prec_key<R>(), 0, n, nsys, qa, sizeof(R) == 4 ? 12 : 14, st, run);
+    else if (representative(nsys, qa, qb) && !profile_enabled()) v = tuned_variant(prec_key<R>(), 0, n, nsys, qa, sizeof(R) == 4 ? 11 : 14, st, run);
     else {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (auto &e : g_tuned)

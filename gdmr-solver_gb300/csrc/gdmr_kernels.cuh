@@ -225,14 +225,13 @@ void launch_update(int n, const typename CT<R>::t *segA, int qa, const typename 
 
 // Tensor-core split-K projection of a batch onto the shared deflation vectors (complex64;
 // gdmr_tc.cu): coef[act[s]*strideC + p] = <W_p, y_s> for p < kk, s < nsys, through per-CTA
-// partials in `part` (G x kk x nsys x 2 doubles, G = wproj_tc_grid(n) or ctas when positive and
-// smaller: the persistent CTAs, one a SM); returns the number of kernels launched.
-// wproj_tc_ok says when it applies (kk <= 32, 8 <= nsys <= 64, even n and stride, 16-byte
-// aligned vectors).
+// partials in `part` (wproj_tc_grid(n) x kk x nsys x 2 doubles); returns the number of
+// kernels launched.  wproj_tc_ok says when it applies (kk <= 32, 8 <= nsys <= 64, even n and
+// stride, 16-byte aligned vectors).
 bool wproj_tc_ok(int n, int kk, int nsys, const void *W, const void *Y, size_t strideY);
 int wproj_tc_grid(int n);
 int launch_wproj_tc(int n, int kk, const float2 *W, const float2 *Y, size_t strideY, const int *act, int nsys,
-                    double *part, double2 *coef, size_t strideC, cudaStream_t st, int ctas = 0);
+                    double *part, double2 *coef, size_t strideC, cudaStream_t st);
 // Tensor-core apply of the shared deflation vectors for a batch (complex64; gdmr_tc.cu):
 // P[act[s]*strideP + i] = sum_p coef[act[s]*strideC + p] W_p[i] for p < kk, and
 // coef[act[s]*strideC + unit_idx] = 1, so that a per-system update with P as one more basis

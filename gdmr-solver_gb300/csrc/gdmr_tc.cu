@@ -939,11 +939,10 @@ int wproj_tc_grid(int n) {
 }
 
 int launch_wproj_tc(int n, int kk, const float2 *W, const float2 *Y, size_t strideY, const int *act, int nsys,
-                    double *part, double2 *coef, size_t strideC, cudaStream_t st, int ctas) {
+                    double *part, double2 *coef, size_t strideC, cudaStream_t st) {
     int dev = 0;
     cudaGetDevice(&dev);
-    int G = wproj_tc_grid(n);
-    if (ctas > 0 && ctas < G) G = ctas;
+    const int G = wproj_tc_grid(n);
     const int np = ((nsys + 15) / 16) * 16;
     const size_t smem = tc_smem_bytes(np);
     {

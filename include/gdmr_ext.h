@@ -147,11 +147,10 @@ void gdmrTune(int on);
 const char *gdmrTuneReport(void);
 /* Pins the Gram-Schmidt variants by their index in the tuner report (-1: tuner).  Used to
  * check every variant against the others; an index a launch cannot use falls back to 0.
- * complex64 projection 0-11, update 0-11; complex128 and fp64e projection 0-8, update 0-7
+ * complex64 projection 0-10, update 0-11; complex128 and fp64e projection 0-8, update 0-7
  * (projection 8 and update 7 prefetch the next group of basis vectors).
  * Batched shared-deflation-basis variants (8 to 64 systems, k <= 32): complex64 projection 9
- * (CUDA cores), 10 (tensor cores) and 11 (10 with the tensor-core part on a side stream over a
- * third of the SMs, beside the own-basis part on the others), update 8 (CUDA cores), 9 (shared part on the tensor cores
+ * (CUDA cores) and 10 (tensor cores), update 8 (CUDA cores), 9 (shared part on the tensor cores
  * into the next basis slot, then the per-system update), 10 (one kernel: the shared part on
  * the tensor cores, subtracted from TMEM while the own basis streams; at most 32 own vectors)
  * and 11 (one kernel, every system of the batch per CTA with the rows of the shared part in
