@@ -487,7 +487,10 @@ template <class R> int Engine<R>::init(int n, int m, int k, int capacity, int de
     A_(tickets_, sizeof(unsigned) * (capacity + 1));
     A_(state_, sizeof(SysState) * (capacity + 1));
     A_(act_, sizeof(int) * (capacity + 1));
-    A_(ident_, sizeof(int) * (capacity + 1));
+    // 0..max(cap, k - 1): the batch's identity list (entry cap is the deflation pseudo-system)
+    // and the deflation loop's batched operator product over the k vectors of Z
+    const int nident = std::max(capacity + 1, k);
+    A_(ident_, sizeof(int) * nident);
     A_(partials_side_, sizeof(double) * scratch_doubles(16, 1, 1));
     A_(lead_dev_, sizeof(int));
     A_(ticket_side_, sizeof(unsigned));
@@ -507,9 +510,9 @@ template <class R> int Engine<R>::init(int n, int m, int k, int capacity, int de
         return GDMR_ENOMEM;
     }
     hto_[0] = hto_[1] = 0;
-    std::vector<int> id(capacity + 1);
-    for (int i = 0; i <= capacity; ++i) id[i] = i;
-    GDMR_CK(cudaMemcpy(ident_, id.data(), sizeof(int) * (capacity + 1), cudaMemcpyHostToDevice));
+    std::vector<int> id(nident);
+    for (int i = 0; i < nident; ++i) id[i] = i;
+    GDMR_CK(cudaMemcpy(ident_, id.data(), sizeof(int) * nident, cudaMemcpyHostToDevice));
     GDMR_CK(cudaMemset(tickets_, 0, sizeof(unsigned) * (capacity + 1)));
     GDMR_CK(cudaMemset(ticket_side_, 0, sizeof(unsigned)));
     GDMR_CK(cudaMemset(V_, 0, vn * (m + 1) * capacity));
@@ -666,16 +669,18 @@ template <class R> int Engine<R>::enqueue_front(int kk, int nsys, long *matvecs)
         // The shared pseudo-system has state index cap_ and active list ident_+cap_.
         GDMR_CK(cudaMemsetAsync(Hd_, 0, sizeof(double2) * strideH(), stream));
         int *pact = ident_ + cap_;
+        // SELL and stencil operators: the kk products A z_i are independent, so they run as one
+        // batched product straight into W's slots (the matrix read once, not kk times); step i
+        // then orthogonalises slot i against the finished slots 0..i-1 and normalises it in place
+        const bool batched = op.kind == Operator<R>::SELL || op.kind == Operator<R>::STENCIL;
+        if (batched) {
+            *matvecs += kk;
+            if (op.kind == Operator<R>::SELL) launch_spmm<R>(op.sell, Z_, n, W_, n, ident_, kk, stream);
+            else launch_stencil<R>(op.stencil, Z_, n, W_, n, ident_, kk, stream);
+        }
         for (int i = 0; i < kk; ++i) {
-            C *az = hook ? op.ext : AZ_;
-            // the SELL path uses the pseudo-system slot so the batch list is not disturbed
-            if (op.kind == Operator<R>::SELL) {
-                *matvecs += 1;
-                launch_spmm<R>(op.sell, Z_ + (size_t)i * n, 0, az, 0, ident_, 1, stream);
-            } else if (op.kind == Operator<R>::STENCIL) {
-                *matvecs += 1;
-                launch_stencil<R>(op.stencil, Z_ + (size_t)i * n, 0, az, 0, ident_, 1, stream);
-            } else {
+            C *az = batched ? W_ + (size_t)i * n : (hook ? op.ext : AZ_);
+            if (!batched) {
                 std::vector<int> keep = act_h_;
                 act_h_ = {0};
                 apply(Z_ + (size_t)i * n, 0, az, 0, 1, matvecs);
