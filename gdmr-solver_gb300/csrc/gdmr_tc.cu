@@ -441,7 +441,7 @@ __global__ void __launch_bounds__(256) k_wproj_tc_reduce(int kk, int nsys, int G
 // group w / 4; four warps of stores ran the kernel at about half the HBM rate), the next WA_PROD
 // warps producers (W tile -> split, swizzled A operands), the last warp issues the MMAs.  A and
 // the TMEM tile are double-buffered; mbarriers only.
-constexpr int WA_EPI = 12, WA_PROD = 8;
+constexpr int WA_EPI = 8, WA_PROD = 8;
 constexpr int WA_MMA_WARP = WA_EPI + WA_PROD;
 constexpr int WA_THREADS = (WA_MMA_WARP + 1) * 32;
 constexpr int WA_TILE = 128;                      // elements per tile (MMA M)
@@ -452,7 +452,7 @@ __device__ __forceinline__ int swz(int r, int kf, int rows) {   // float offset 
     return ((kf >> 5) * rows * TC_ROW + r * TC_ROW + ((((kf >> 2) & 7) ^ (r & 7)) << 4) + ((kf & 3) << 2)) >> 2;
 }
 
-__global__ void __maxnreg__(80)   // 672 threads x 80 registers: a sixth of the file left free
+__global__ void __launch_bounds__(WA_THREADS, 1)
     k_wapply_tc(int n, int kk, const float2 *__restrict__ W, double2 *__restrict__ coef0, size_t strideC,
                 const int *__restrict__ act, int nsys, int nsp, float2 *__restrict__ P0, size_t strideP,
                 int unit_idx) {
