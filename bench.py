@@ -391,6 +391,9 @@ def run_multi_operator(args, rank):
     rhs = [np.array([problems.unit_gaussian_rhs(A.n, 9000 + 10 * i + j) for j in range(per_op)])
            for i, A in enumerate(mats)]
     forms = {}
+    if args.multi_tail >= 0:
+        gdmr.multi_tail(args.multi_tail)
+    tail = gdmr.multi_tail()
     # lockstep: warm-up of the per-operator kernels' tuning on a first solve, then the timed one
     systems = [gdmr.System(A, 40, 16, capacity=per_op, precision=args.serve_precision if
                            args.serve_precision != "both" else "mixed") for A in mats]
@@ -408,7 +411,7 @@ def run_multi_operator(args, rank):
     forms["lockstep"] = {"solves_s": len(lat) / wall, "wall_s": wall,
                          "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
                          "cycles": {"mean": float(np.mean(cyc)), "max": int(np.max(cyc))}, "verified": bool(ok),
-                         "host_worst_true_rel_res": host}
+                         "host_worst_true_rel_res": host, "tail": tail}
     for s in systems:
         s.close()
     # streams: the serving layer
@@ -505,6 +508,8 @@ def main():
                     help="128^3 drifting sequence of right-hand sides: plain complex128, fp64e and mixed")
     ap.add_argument("--seq-count", type=int, default=4, help="right-hand sides of the sequence timed (of 32)")
     ap.add_argument("--operators", type=int, default=48)
+    ap.add_argument("--multi-tail", type=int, default=-1,
+                    help="multi-operator: systems in flight at which the lockstep hands over (-1: library default)")
     ap.add_argument("--rhs-per-operator", type=int, default=4)
     ap.add_argument("--serve-precision", default="both", choices=["mixed", "fp64", "both"])
     ap.add_argument("--load", type=float, default=0.7,

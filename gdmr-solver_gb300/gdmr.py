@@ -544,7 +544,7 @@ class System:
 
 def multi_tail(systems: int = -1) -> int:
     """gdmrMultiTail: systems in flight at or below which multi_solve finishes on the systems'
-    own batched cycles (default 8; 0: lockstep to the end); returns the previous value."""
+    own batched cycles (default 48; 0: lockstep to the end); returns the previous value."""
     return int(load().gdmrMultiTail(int(systems)))
 
 

@@ -254,7 +254,7 @@ int gdmr_solve_batch(gdmr_system *sys, int nrhs, const double *b, double *x, con
 int gdmr_multi_solve(int nops, gdmr_system *const *systems, const int *nrhs, const double *const *b, double *const *x,
                      const double *tol, int maxCycles, gdmr_stats *const *stats);
 /* gdmr_multi_solve's tail: once every right-hand side has been admitted and at most this many
- * systems remain in flight (default 8), the remaining ones finish on each system's own batched
+ * systems remain in flight (default 48), the remaining ones finish on each system's own batched
  * cycles (as gdmr_solve_batch), one host thread per system driving its own stream, instead of in
  * the lockstep launch; 0 keeps the lockstep to the end.  systems < 0 only reads.  Returns the
  * previous value. */
