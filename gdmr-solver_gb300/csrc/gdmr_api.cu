@@ -411,6 +411,7 @@ extern "C" double gdmrWaitLimit(double ms) {
 }
 extern "C" void gdmrInjectAllocFailure(int nth) { inject_alloc_failure(nth); }
 extern "C" void gdmrCombineGroup(int enable) { set_combine_group(enable); }
+extern "C" int gdmrOverlapResidual(int ctasPerSm) { return set_overlap_residual(ctasPerSm); }
 // Systems in flight at or below which gdmr_multi_solve finishes on the engines' own cycles.
 static std::atomic<int> g_multi_tail{48};
 extern "C" int gdmrMultiTail(int systems) {

@@ -416,10 +416,19 @@ template <class R> void Engine<R>::release() {
         cudaStreamDestroy(side_);
         side_ = nullptr;
     }
+    if (res_) {
+        cudaStreamSynchronize(res_);
+        cudaStreamDestroy(res_);
+        res_ = nullptr;
+    }
     if (ev_krylov_) cudaEventDestroy(ev_krylov_);
     if (ev_zdone_) cudaEventDestroy(ev_zdone_);
-    ev_krylov_ = ev_zdone_ = nullptr;
+    if (ev_x_) cudaEventDestroy(ev_x_);
+    if (ev_res_) cudaEventDestroy(ev_res_);
+    ev_krylov_ = ev_zdone_ = ev_x_ = ev_res_ = nullptr;
     z_pending_ = false;
+    front_done_ = false;
+    partials_res_ = nullptr;
     if (partials_) unregister_scratch(partials_);
     partials_side_ = nullptr;
     ticket_side_ = nullptr;
@@ -492,13 +501,17 @@ template <class R> int Engine<R>::init(int n, int m, int k, int capacity, int de
     const int nident = std::max(capacity + 1, k);
     A_(ident_, sizeof(int) * nident);
     A_(partials_side_, sizeof(double) * scratch_doubles(16, 1, 1));
+    A_(partials_res_, sizeof(double) * scratch_doubles(0, capacity + 1, 1));
     A_(lead_dev_, sizeof(int));
     A_(ticket_side_, sizeof(unsigned));
     A_(ks_bar_, 2 * sizeof(unsigned));
 #undef A_
     if (cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&res_, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ev_krylov_, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ev_zdone_, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&ev_zdone_, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev_x_, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev_res_, cudaEventDisableTiming) != cudaSuccess) {
         release();
         set_last_error(GDMR_ECUDA, "engine: side stream or events");
         return GDMR_ECUDA;
@@ -598,11 +611,8 @@ template <class R> int Engine<R>::run_cycle(int kk, int nsys, int lead, double t
     if (sync_deflation() != GDMR_OK) return GDMR_ECUDA;
     lead_host_ = lead;
     GDMR_CK(cudaMemcpyAsync(lead_dev_, &lead_host_, sizeof(int), cudaMemcpyHostToDevice, stream));
-    // CUDA graphs pay off where launch overhead is comparable to the work: small n x batch.
-    // The first two cycles of an engine run eagerly: they tune the kernels of both cycle
-    // shapes (without and with the deflation space) before anything is captured.
-    const bool graphable = use_graphs && op.kind != Operator<R>::HOOK && !profile_enabled() && cycles_run_ > 1 &&
-                           (long)n_ * nsys <= (1L << 20);
+    // a cycle whose deflation loop is already enqueued runs eagerly (a graph holds whole cycles)
+    const bool graphable = !front_done_ && graph_ok(nsys);
     ++cycles_run_;
     if (!graphable) return enqueue_cycle(kk, nsys, tol, matvecs, false);
     const int zpar = zpar_;
@@ -649,6 +659,14 @@ template <class R> int Engine<R>::run_cycle(int kk, int nsys, int lead, double t
     return GDMR_OK;
 }
 
+// CUDA graphs pay off where launch overhead is comparable to the work: small n x batch.  The
+// first two cycles of an engine run eagerly: they tune the kernels of both cycle shapes
+// (without and with the deflation space) before anything is captured.
+template <class R> bool Engine<R>::graph_ok(int nsys) const {
+    return use_graphs && op.kind != Operator<R>::HOOK && !profile_enabled() && cycles_run_ > 1 &&
+           (long)n_ * nsys <= (1L << 20);
+}
+
 template <class R> int Engine<R>::enqueue_cycle(int kk, int nsys, double tol, long *matvecs, bool join) {
     int rc = enqueue_front(kk, nsys, matvecs);
     if (rc != GDMR_OK) return rc;
@@ -665,37 +683,8 @@ template <class R> int Engine<R>::enqueue_front(int kk, int nsys, long *matvecs)
     GDMR_CK(cudaMemsetAsync(H_, 0, sizeof(double2) * strideH() * cap_, stream));
     k_cycle_reset<<<1, 256, 0, stream>>>(act_, nsys, state_, 0);
     if (kk > 0) {
-        // Deflation loop (arnoldiDMR, gDMR.cu:1823-2030): W_i = orth(A z_i), H[:i+1, i].
-        // The shared pseudo-system has state index cap_ and active list ident_+cap_.
-        GDMR_CK(cudaMemsetAsync(Hd_, 0, sizeof(double2) * strideH(), stream));
-        int *pact = ident_ + cap_;
-        // SELL and stencil operators: the kk products A z_i are independent, so they run as one
-        // batched product straight into W's slots (the matrix read once, not kk times); step i
-        // then orthogonalises slot i against the finished slots 0..i-1 and normalises it in place
-        const bool batched = op.kind == Operator<R>::SELL || op.kind == Operator<R>::STENCIL;
-        if (batched) {
-            *matvecs += kk;
-            if (op.kind == Operator<R>::SELL) launch_spmm<R>(op.sell, Z_, n, W_, n, ident_, kk, stream);
-            else launch_stencil<R>(op.stencil, Z_, n, W_, n, ident_, kk, stream);
-        }
-        for (int i = 0; i < kk; ++i) {
-            C *az = batched ? W_ + (size_t)i * n : (hook ? op.ext : AZ_);
-            if (!batched) {
-                std::vector<int> keep = act_h_;
-                act_h_ = {0};
-                apply(Z_ + (size_t)i * n, 0, az, 0, 1, matvecs);
-                act_h_ = keep;
-            }
-            if (i > 0)
-                launch_mdot<R>(n, W_, i, nullptr, 0, 0, az, 0, pact, 1, partials_, qmax(), tickets_ + cap_, coefD_, 0,
-                               state_, false, stream);
-            FinishArgs f{};
-            f.mode = FIN_DEFLATION; f.col = i; f.nco = i; f.ldH = m + 1; f.m = m; f.kk = kk;
-            f.H = Hd_; f.strideH = 0; f.coef = coefD_; f.strideC = 0;
-            launch_update<R>(n, W_, i, nullptr, 0, 0, az, 0, T_, 0, pact, 1, coefD_, 0, partials_, tickets_ + cap_,
-                             state_, f, false, stream);
-            launch_scale<R>(n, T_, 0, W_ + (size_t)i * n, 0, nullptr, 0, pact, 1, state_, false, stream);
-        }
+        if (!front_done_) enqueue_deflation_loop(kk, matvecs);
+        front_done_ = false;
         launch_broadcast_hdef(m, kk, Hd_, H_, strideH(), act_, nsys, stream);
         // v0 <- (I - W W^H) v0 / ||.||  (deflatorDMR(0,0), gDMR.cu:2033-2059)
         launch_mdot<R>(n, W_, kk, nullptr, 0, 0, V_, sV, act_, nsys, partials_, qmax(), tickets_, coef_, sC, state_,
@@ -710,6 +699,43 @@ template <class R> int Engine<R>::enqueue_front(int kk, int nsys, long *matvecs)
     }
     GDMR_CK(cudaGetLastError());
     return GDMR_OK;
+}
+
+// Deflation loop (arnoldiDMR, gDMR.cu:1823-2030): W_i = orth(A z_i), H[:i+1, i] into Hd_.  It
+// reads only Z and writes only W, Hd, T's slot 0 and the shared pseudo-system (state index cap_,
+// active list ident_+cap_, tickets_[cap_]); no system's own data.
+template <class R> void Engine<R>::enqueue_deflation_loop(int kk, long *matvecs) {
+    const int n = n_, m = m_;
+    const bool hook = op.kind == Operator<R>::HOOK;
+    cudaMemsetAsync(Hd_, 0, sizeof(double2) * strideH(), stream);
+    int *pact = ident_ + cap_;
+    // SELL and stencil operators: the kk products A z_i are independent, so they run as one
+    // batched product straight into W's slots (the matrix read once, not kk times); step i
+    // then orthogonalises slot i against the finished slots 0..i-1 and normalises it in place
+    const bool batched = op.kind == Operator<R>::SELL || op.kind == Operator<R>::STENCIL;
+    if (batched) {
+        *matvecs += kk;
+        if (op.kind == Operator<R>::SELL) launch_spmm<R>(op.sell, Z_, n, W_, n, ident_, kk, stream);
+        else launch_stencil<R>(op.stencil, Z_, n, W_, n, ident_, kk, stream);
+    }
+    for (int i = 0; i < kk; ++i) {
+        C *az = batched ? W_ + (size_t)i * n : (hook ? op.ext : AZ_);
+        if (!batched) {
+            std::vector<int> keep = act_h_;
+            act_h_ = {0};
+            apply(Z_ + (size_t)i * n, 0, az, 0, 1, matvecs);
+            act_h_ = keep;
+        }
+        if (i > 0)
+            launch_mdot<R>(n, W_, i, nullptr, 0, 0, az, 0, pact, 1, partials_, qmax(), tickets_ + cap_, coefD_, 0,
+                           state_, false, stream);
+        FinishArgs f{};
+        f.mode = FIN_DEFLATION; f.col = i; f.nco = i; f.ldH = m + 1; f.m = m; f.kk = kk;
+        f.H = Hd_; f.strideH = 0; f.coef = coefD_; f.strideC = 0;
+        launch_update<R>(n, W_, i, nullptr, 0, 0, az, 0, T_, 0, pact, 1, coefD_, 0, partials_, tickets_ + cap_,
+                         state_, f, false, stream);
+        launch_scale<R>(n, T_, 0, W_ + (size_t)i * n, 0, nullptr, 0, pact, 1, state_, false, stream);
+    }
 }
 
 // The Krylov loop (gDMR.cu:2069-2328): classical Gram-Schmidt against [W V] in one pass.
@@ -927,6 +953,7 @@ template <class R> int Engine<R>::refine_setup(const SellMatrix &A64) {
         return GDMR_EINVAL;
     }
     A64_ = A64;
+    front_done_ = false;
     if (!r64_) {
         int rc;
         if ((rc = alloc((void **)&r64_, sizeof(double2) * (size_t)n_ * cap_)) != GDMR_OK) return rc;
@@ -991,9 +1018,28 @@ template <class R> int Engine<R>::refine_cycle(std::vector<int> *done) {
         launch_norm<double>(n, b64_, n, act_, (int)fresh.size(), partials_, tickets_, state_, 1, stream);
         if (set_active(act) != GDMR_OK) return GDMR_ECUDA;
     }
-    // true FP64 residual of every active system
+    // true FP64 residual of every active system.  From the engine's third cycle on, with a
+    // deflation space and no cycle graph, it runs on its own stream on a few CTAs an SM, beside
+    // the next cycle's deflation loop on the main stream (W = orth(A Z) needs only Z): the
+    // residual is bound by the FP64 pipe, the loop's single-system kernels by memory and
+    // latency, so they share the SMs.  The host reads the states once both are done.
     Range range("gdmr refined cycle");
-    launch_residual64(A64_, b64_, n, x64_, n, r64_, n, act_, na, partials_, tickets_, state_, stream);
+    const int res_per_sm = overlap_residual();
+    const bool early = k > 0 && res_per_sm > 0 && cycles_run_ > 1 && !graph_ok(na) && (have_z_ || z_pending_);
+    if (early) {
+        GDMR_CK(cudaEventRecord(ev_x_, stream));
+        GDMR_CK(cudaStreamWaitEvent(res_, ev_x_, 0));
+        launch_residual64(A64_, b64_, n, x64_, n, r64_, n, act_, na, partials_res_, tickets_, state_, res_,
+                          res_per_sm);
+        GDMR_CK(cudaEventRecord(ev_res_, res_));
+        if (sync_deflation() != GDMR_OK) return GDMR_ECUDA;
+        long dmv = 0;
+        enqueue_deflation_loop(k, &dmv);
+        front_done_ = true;
+        GDMR_CK(cudaStreamWaitEvent(stream, ev_res_, 0));
+    } else {
+        launch_residual64(A64_, b64_, n, x64_, n, r64_, n, act_, na, partials_, tickets_, state_, stream);
+    }
     if (read_state(cap_) != GDMR_OK) return GDMR_ECUDA;
     // a bounded wait that ran out since the last look (the previous cycle's kernels) leaves
     // every system in flight, and the shared deflation space, untrustworthy
@@ -1030,7 +1076,10 @@ template <class R> int Engine<R>::refine_cycle(std::vector<int> *done) {
         if (rel > worst) { worst = rel; lead = s; }
     }
     act_h_ = next;
-    if (next.empty()) return sync_deflation();
+    if (next.empty()) {
+        front_done_ = false;
+        return sync_deflation();
+    }
     if (set_active(next) != GDMR_OK) return GDMR_ECUDA;
     na = (int)next.size();
     // unit residual direction in precision R, also the first basis vector of every system (the
@@ -1040,6 +1089,7 @@ template <class R> int Engine<R>::refine_cycle(std::vector<int> *done) {
     launch_demote_unit<R>(n, r64_, n, R_, n, V_, strideV(), act_, na, state_, stream);
     k_cycle_reset<<<1, 256, 0, stream>>>(act_, na, state_, 1);
     const int kk = (k > 0 && have_z_) ? k : 0;
+    if (kk == 0) front_done_ = false;   // the deflation space was dropped after a timeout
     restart_vectors(next, kk);
     long mv = 0;
     // breakdown of unit vectors: an invariant subspace at working precision

@@ -246,6 +246,14 @@ template <class R> class Engine {
     double2 *partials_side_ = nullptr;
     unsigned *ticket_side_ = nullptr;
     int sync_deflation();
+    // The refined form's FP64 residual can run on its own stream beside the next cycle's
+    // deflation loop, which needs only Z (front_done_: the loop is already enqueued).
+    cudaStream_t res_ = nullptr;
+    cudaEvent_t ev_x_ = nullptr, ev_res_ = nullptr;
+    double2 *partials_res_ = nullptr;
+    bool front_done_ = false;
+    void enqueue_deflation_loop(int kk, long *matvecs);
+    bool graph_ok(int nsys) const;
     // restart-cycle graphs (key: deflation dimension, batch size, Z buffer parity, tolerance)
     struct GraphEntry {
         int kk, nsys, zpar;

@@ -3876,33 +3876,39 @@ __global__ void __launch_bounds__(NT) k_spmm(int n, const int *__restrict__ slic
     }
 }
 
-// r = b - A x in FP64 with ||r||^2 reduced; last CTA sets true_res and alpha.
+// r = b - A x in FP64 with ||r||^2 reduced; last CTA sets true_res and alpha.  The rows of a
+// system are split into Gv virtual blocks (row = vb * NT + tid + i * Gv * NT), each with its own
+// partial sum; a CTA takes virtual blocks blockIdx.y, blockIdx.y + gridDim.y, ...  So a grid of
+// fewer CTAs (to leave room on the SMs for a concurrent stream) adds the same numbers in the
+// same order as one CTA per virtual block.
 template <int NCX, int WID>
 __global__ void __launch_bounds__(NT) k_residual64(int n, const int *__restrict__ slice_ptr, const int *__restrict__ cols,
                                                    const double2 *__restrict__ vals, const double2 *__restrict__ b0,
                                                    size_t strideB, const double2 *__restrict__ x0, size_t strideX,
                                                    double2 *__restrict__ r0, size_t strideR, const int *__restrict__ act,
                                                    double2 *__restrict__ partials, unsigned *tickets, SysState *state,
-                                                   ResidPattern rp) {
+                                                   ResidPattern rp, int Gv) {
     const int slot = blockIdx.x, s = act[slot], G = gridDim.y, tid = threadIdx.x;
     const double2 *b = b0 + (size_t)s * strideB;
     const double2 *x = x0 + (size_t)s * strideX;
     double2 *r = r0 + (size_t)s * strideR;
     __shared__ double red[1][NW];
-    double n2 = 0;
-    for (int row = blockIdx.y * NT + tid; row < n; row += G * NT) {
-        const double2 acc = resid_row<NCX, WID>(b[row], row, slice_ptr, cols, vals, x, rp);
-        r[row] = acc;
-        n2 += acc.x * acc.x + acc.y * acc.y;
+    double *part = (double *)partials + (size_t)slot * Gv;
+    for (int vb = blockIdx.y; vb < Gv; vb += G) {
+        double n2 = 0;
+        for (int row = vb * NT + tid; row < n; row += Gv * NT) {
+            const double2 acc = resid_row<NCX, WID>(b[row], row, slice_ptr, cols, vals, x, rp);
+            r[row] = acc;
+            n2 += acc.x * acc.x + acc.y * acc.y;
+        }
+        double v[1] = {n2};
+        block_sum<1>(v, red);
+        if (tid == 0) part[vb] = v[0];
+        __syncthreads();   // red is reused by the next virtual block
     }
-    double v[1] = {n2};
-    block_sum<1>(v, red);
-    double *part = (double *)partials + (size_t)slot * G;
-    if (tid == 0) part[blockIdx.y] = v[0];
     if (!arrive_last(&tickets[slot], G)) return;
     double tot[1];
-    __syncthreads();
-    sum_partials<1>(part, G, tot, red);
+    sum_partials<1>(part, Gv, tot, red);
     if (tid == 0) {
         SysState &st = state[s];
         st.nrm2 = tot[0];
@@ -5030,6 +5036,13 @@ bool launch_krylov_small(int n, int kk, int m, const SellMatrix &A, const typena
 static std::atomic<int> g_combine_group{1};
 void set_combine_group(int on) { g_combine_group.store(on ? 1 : 0); }
 int combine_group() { return g_combine_group.load(); }
+static std::atomic<int> g_overlap_residual{2};
+int set_overlap_residual(int ctas_per_sm) {
+    const int prev = g_overlap_residual.load();
+    if (ctas_per_sm >= 0) g_overlap_residual.store(std::min(ctas_per_sm, 8));
+    return prev;
+}
+int overlap_residual() { return g_overlap_residual.load(); }
 static std::atomic<int> g_grid_operator{1};
 static std::atomic<int> g_grid_batch{0};
 void set_grid_operator(int enable) { g_grid_operator.store(enable ? 1 : 0); }
@@ -5116,16 +5129,18 @@ int resid_pattern(const SellMatrix &A, ResidPattern &rp) {
 
 void launch_residual64(const SellMatrix &A, const double2 *b, size_t strideB, const double2 *x, size_t strideX,
                        double2 *r, size_t strideR, const int *act, int nsys, double2 *partials, unsigned *tickets,
-                       SysState *state, cudaStream_t st) {
+                       SysState *state, cudaStream_t st, int per_sm) {
     if (nsys <= 0) return;
     Launch L_(KC_RESID64, spmm_bytes(A, sizeof(double2), nsys) + (double)sizeof(double2) * A.n * nsys, st, 1);
     ResidPattern rp{};
     const int ncx = resid_pattern(A, rp);
-    const dim3 grid = grid2(nsys, capped_grid(A.n, nsys, 8));
+    const int Gv = capped_grid(A.n, nsys, 8);
+    const int G = per_sm > 0 ? std::min(Gv, capped_grid(A.n, nsys, per_sm)) : Gv;
+    const dim3 grid = grid2(nsys, G);
     resid_dispatch(A.npat, ncx, [&](auto ncx_c, auto wid_c) {
         k_residual64<decltype(ncx_c)::value, decltype(wid_c)::value><<<grid, NT, 0, st>>>(
             A.n, A.slice_ptr, A.cols, (const double2 *)A.vals, b, strideB, x, strideX, r, strideR, act, partials,
-            tickets, state, rp);
+            tickets, state, rp, Gv);
     });
 }
 

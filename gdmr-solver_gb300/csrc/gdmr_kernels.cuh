@@ -290,6 +290,11 @@ void launch_combine(int n, int kk, int m, const typename CT<R>::t *W, const type
 // combination (W and Z loaded once for four systems); 0 returns them to one system a CTA.
 void set_combine_group(int on);
 int combine_group();
+// The refined form's FP64 residual beside the next cycle's deflation loop, on its own stream,
+// on about ctas_per_sm CTAs an SM (0: off, the residual before the loop).  ctas_per_sm < 0 only
+// reads; returns the previous setting.
+int set_overlap_residual(int ctas_per_sm);
+int overlap_residual();
 // Z_new[t] = [Z V] vs[:, t] for t < k, plus squared norms into znorm2 (k doubles).
 // V: basis of system 0 (system s at V + s*strideV); the lead system is read from device memory.
 template <class R>
@@ -472,9 +477,11 @@ __device__ __forceinline__ double2 resid_row(double2 acc, long row, const int *_
 #endif
 
 // y_s = b_s - A x_s in FP64 with ||y_s||^2 reduced into state[s].nrm2 (refined form).
+// per_sm > 0 caps the grid near per_sm CTAs an SM (to share the SMs with another stream); the
+// result is the same bit for bit whatever the cap.
 void launch_residual64(const SellMatrix &A, const double2 *b, size_t strideB, const double2 *x, size_t strideX,
                        double2 *r, size_t strideR, const int *act, int nsys, double2 *partials, unsigned *tickets,
-                       SysState *state, cudaStream_t st);
+                       SysState *state, cudaStream_t st, int per_sm = 0);
 // Dense column-major n x n operator (the reference's impOptLS form): y = A x.
 template <class R>
 void launch_dense_gemv(int n, const typename CT<R>::t *A, const typename CT<R>::t *x, typename CT<R>::t *y,

@@ -64,6 +64,7 @@ SIGNATURES = {
     "gdmrGridOperator": (None, [I]),
     "gdmrGridBatch": (None, [I]),
     "gdmrCombineGroup": (None, [I]),
+    "gdmrOverlapResidual": (I, [I]),
     "gdmr_csr_grid_form": (I, [I, P, P, P, P]),
     "gdmrAsyncTimeouts": (ctypes.c_uint, []),
     "gdmr_hessenberg_svd": (I, [I, I, P, P, P, P]),
@@ -195,6 +196,13 @@ def grid_batch(systems_per_thread: int) -> None:
 def combine_group(enable: bool) -> None:
     """Cycle-end combinations of batches four systems a CTA (on by default) or one."""
     load().gdmrCombineGroup(1 if enable else 0)
+
+
+def overlap_residual(ctas_per_sm: int = -1) -> int:
+    """gdmrOverlapResidual: the refined solves' FP64 residual beside the next cycle's deflation
+    loop, on its own stream with its grid capped at about ctas_per_sm CTAs an SM (default 2), or
+    before the loop (0); -1 only reads.  Returns the previous setting."""
+    return int(load().gdmrOverlapResidual(int(ctas_per_sm)))
 
 
 def csr_grid_form(A):

@@ -176,6 +176,13 @@ void gdmrGridBatch(int systemsPerThread);
  * loaded once for the four (on by default); 0 returns them to one system a CTA. */
 void gdmrCombineGroup(int enable);
 
+/* The refined solves' FP64 residual b - A x on its own stream, beside the next restart cycle's
+ * deflation loop (which needs only the deflation space), from a system's third cycle on when the
+ * cycle is not a CUDA graph: ctasPerSm (1-8, default 2) caps its grid so that the loop's kernels
+ * keep room on the SMs; 0 runs it before the loop.  The results are the same bit for bit either
+ * way.  ctasPerSm < 0 only reads; returns the previous setting. */
+int gdmrOverlapResidual(int ctasPerSm);
+
 /* Host-only check of a CSR matrix (complex values interleaved re, im) for the structured-grid
  * form: dims[0..2] <- (nx, ny, nz), zeros if it has none.  GDMR_EINVAL for malformed arrays. */
 int gdmr_csr_grid_form(int n, const int *rowPtr, const int *colIdx, const double *vals_ri, int *dims);

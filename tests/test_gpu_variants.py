@@ -93,3 +93,31 @@ def test_grouped_combination_matches_one_system_a_cta(batch20, precision):
     assert max(abs(a - b) for a, b in zip(cg, cs)) <= 2, (cg, cs)
 
 
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64", "fp64e"])
+def test_residual_beside_the_deflation_loop_changes_nothing(batch20, precision):
+    """The FP64 residual on its own stream beside the next cycle's deflation loop against the
+    residual before the loop (eager cycles: graphs off, so the overlap runs from the third
+    cycle on).  The same kernels read the same data, and the residual's smaller grid sums the
+    same virtual blocks in the same order, so answers and cycle counts agree bit for bit."""
+    A, rhs, cfg, direct = batch20
+    out = {}
+    for on in (2, 0):
+        prev = gdmr.overlap_residual(on)
+        gdmr.tune_force(0, 0)
+        try:
+            s = gdmr.System(A, cfg["m"], cfg["k"], capacity=NRHS, precision=precision)
+            s.set_graphs(False)
+            out[on] = s.solve_batch(rhs, tol=1e-10, max_cycles=2000)
+            s.close()
+        finally:
+            gdmr.overlap_residual(prev)
+            gdmr.tune_force(-1, -1)
+    (X1, st1), (X0, st0) = out[2], out[0]
+    assert [st["cycles"] for st in st1] == [st["cycles"] for st in st0]
+    assert max(st["cycles"] for st in st1) >= 3
+    assert np.array_equal(X1, X0)
+    assert all(st["status"] == 0 and st["true_rel_res"] <= 1.5e-10 for st in st1)
+    err = np.linalg.norm(X1 - direct, axis=1) / np.linalg.norm(direct, axis=1)
+    assert err.max() < 1e-8
