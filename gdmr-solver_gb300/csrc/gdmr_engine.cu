@@ -1018,11 +1018,11 @@ template <class R> int Engine<R>::refine_cycle(std::vector<int> *done) {
         launch_norm<double>(n, b64_, n, act_, (int)fresh.size(), partials_, tickets_, state_, 1, stream);
         if (set_active(act) != GDMR_OK) return GDMR_ECUDA;
     }
-    // true FP64 residual of every active system.  From the engine's third cycle on, with a
-    // deflation space and no cycle graph, it runs on its own stream on a few CTAs an SM, beside
-    // the next cycle's deflation loop on the main stream (W = orth(A Z) needs only Z): the
-    // residual is bound by the FP64 pipe, the loop's single-system kernels by memory and
-    // latency, so they share the SMs.  The host reads the states once both are done.
+    // true FP64 residual of every active system.  With gdmrOverlapResidual(n > 0), from the
+    // engine's third cycle on, with a deflation space and no cycle graph, it runs on its own
+    // stream on about n CTAs an SM, beside the next cycle's deflation loop on the main stream
+    // (W = orth(A Z) needs only Z); the host reads the states once both are done.  The 96^3
+    // batch measured the same cycle time either way, so it is off by default.
     Range range("gdmr refined cycle");
     const int res_per_sm = overlap_residual();
     const bool early = k > 0 && res_per_sm > 0 && cycles_run_ > 1 && !graph_ok(na) && (have_z_ || z_pending_);

@@ -5036,7 +5036,7 @@ bool launch_krylov_small(int n, int kk, int m, const SellMatrix &A, const typena
 static std::atomic<int> g_combine_group{1};
 void set_combine_group(int on) { g_combine_group.store(on ? 1 : 0); }
 int combine_group() { return g_combine_group.load(); }
-static std::atomic<int> g_overlap_residual{2};
+static std::atomic<int> g_overlap_residual{0};
 int set_overlap_residual(int ctas_per_sm) {
     const int prev = g_overlap_residual.load();
     if (ctas_per_sm >= 0) g_overlap_residual.store(std::min(ctas_per_sm, 8));

@@ -291,7 +291,7 @@ void launch_combine(int n, int kk, int m, const typename CT<R>::t *W, const type
 void set_combine_group(int on);
 int combine_group();
 // The refined form's FP64 residual beside the next cycle's deflation loop, on its own stream,
-// on about ctas_per_sm CTAs an SM (0: off, the residual before the loop).  ctas_per_sm < 0 only
+// on about ctas_per_sm CTAs an SM (0, the default: the residual before the loop).  ctas_per_sm < 0 only
 // reads; returns the previous setting.
 int set_overlap_residual(int ctas_per_sm);
 int overlap_residual();

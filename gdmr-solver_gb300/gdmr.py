@@ -200,8 +200,8 @@ def combine_group(enable: bool) -> None:
 
 def overlap_residual(ctas_per_sm: int = -1) -> int:
     """gdmrOverlapResidual: the refined solves' FP64 residual beside the next cycle's deflation
-    loop, on its own stream with its grid capped at about ctas_per_sm CTAs an SM (default 2), or
-    before the loop (0); -1 only reads.  Returns the previous setting."""
+    loop, on its own stream with its grid capped at about ctas_per_sm CTAs an SM, or before the
+    loop (0, the default); -1 only reads.  Returns the previous setting."""
     return int(load().gdmrOverlapResidual(int(ctas_per_sm)))
 
 

@@ -178,9 +178,9 @@ void gdmrCombineGroup(int enable);
 
 /* The refined solves' FP64 residual b - A x on its own stream, beside the next restart cycle's
  * deflation loop (which needs only the deflation space), from a system's third cycle on when the
- * cycle is not a CUDA graph: ctasPerSm (1-8, default 2) caps its grid so that the loop's kernels
- * keep room on the SMs; 0 runs it before the loop.  The results are the same bit for bit either
- * way.  ctasPerSm < 0 only reads; returns the previous setting. */
+ * cycle is not a CUDA graph: ctasPerSm (1-8) caps its grid so that the loop's kernels keep room
+ * on the SMs; 0, the default, runs it before the loop.  The results are the same bit for bit
+ * either way.  ctasPerSm < 0 only reads; returns the previous setting. */
 int gdmrOverlapResidual(int ctasPerSm);
 
 /* Host-only check of a CSR matrix (complex values interleaved re, im) for the structured-grid
