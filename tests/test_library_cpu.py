@@ -75,6 +75,19 @@ def test_solver_before_init_reports_not_initialised(lib):
     assert lib.gdmrLastStatus() == 6
 
 
+def test_process_settings_read_set_and_restore(lib):
+    """The process-wide settings that take a count (multi-solve hand-over point, residual grid
+    cap) read with -1, return the previous value when set, and clamp the cap."""
+    tail = gdmr.multi_tail()
+    assert tail == 48
+    assert gdmr.multi_tail(3) == 48 and gdmr.multi_tail() == 3
+    assert gdmr.multi_tail(tail) == 3 and gdmr.multi_tail() == tail
+    cap = gdmr.overlap_residual()
+    assert cap == 0
+    assert gdmr.overlap_residual(20) == 0 and gdmr.overlap_residual() == 8
+    assert gdmr.overlap_residual(cap) == 8 and gdmr.overlap_residual() == cap
+
+
 @pytest.mark.skipif(not REFERENCE_PROG or not os.path.exists(REFERENCE_PROG) or shutil.which("gcc") is None,
                     reason="GDMR_REFERENCE_DIR unset or without progDMR.c, or no gcc")
 def test_reference_control_program_links_unchanged(tmp_path):
